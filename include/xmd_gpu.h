@@ -1,0 +1,191 @@
+/*
+ * xmd_gpu.h - C ABI of the GB300 engine for XMD's per-step hot path.
+ *
+ * The reference (vitreusx/xmd) exposes its hot path as C++ "term objects"
+ * (public parameter fields, raw array views, operator()() / omp_async())
+ * wired together by the driver in src/freeform/main.cpp:208-1077 and
+ * configured by the YAML keys of src/freeform/defaults.yml.  This header is
+ * the flat, FFI-friendly replacement for that wiring: one context owns the
+ * device state of one or more systems ("replicas"), is configured by the same
+ * YAML keys and units, and runs the same force terms and integrator.
+ *
+ * Conventions
+ *  - Every function returns XMD_OK (0) or a negative XMD_ERR_* code; the
+ *    message of the last failure on the calling thread is returned by
+ *    xmd_gpu_last_error().  No C++ exception crosses this boundary (the
+ *    reference reports errors only through C++ exceptions, e.g.
+ *    include/xmd/store/store.h:152).
+ *  - Lengths, energies and times are in the reference's internal units
+ *    (include/xmd/utils/units.h:11-62: length 1 = 5 A, energy eps, time tau,
+ *    kB = 1).  YAML values carry units and are converted on parsing.
+ *  - Arrays of vectors are flat double[3*n] (x0,y0,z0,x1,...).  Caller
+ *    arrays are copied; the context owns all device memory.
+ *  - Bead indices in topology arrays are 0-based and local to the replica.
+ *  - One host thread drives a context at a time (the reference's master
+ *    thread, src/freeform/main.cpp:1007-1075); contexts are independent.
+ */
+#ifndef XMD_GPU_H
+#define XMD_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define XMD_GPU_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+    XMD_OK = 0,
+    XMD_ERR_ARG = -1,       /* invalid argument (null pointer, bad index, ...) */
+    XMD_ERR_CONFIG = -2,    /* YAML / unit parse error or unknown key value    */
+    XMD_ERR_STATE = -3,     /* call out of order (e.g. step before topology)   */
+    XMD_ERR_CUDA = -4,      /* CUDA runtime error or no usable GPU             */
+    XMD_ERR_CAPACITY = -5,  /* a fixed-capacity device list overflowed         */
+    XMD_ERR_NUMERIC = -6,   /* non-finite force/energy detected on the device  */
+    XMD_ERR_BUDGET = -7     /* request does not fit the serving memory budget  */
+};
+
+/* ---- force terms (mirrors the kernel<T> opt-in of main.cpp:29-75) ------ */
+enum {
+    XMD_TERM_TETHER = 0,    /* eval_tether_forces      src/forces/tether.cpp:21-36            */
+    XMD_TERM_NAT_ANG = 1,   /* eval_native_angle_forces src/forces/angle/native.cpp:13-39     */
+    XMD_TERM_CND = 2,       /* eval_cnd_forces  src/forces/dihedral/complex_native.cpp:13-49  */
+    XMD_TERM_SND = 3,       /* eval_snd_forces  src/forces/dihedral/simple_native.cpp:13-45   */
+    XMD_TERM_GO = 4,        /* eval_go_forces   src/forces/go.cpp:31-46                        */
+    XMD_TERM_PAULI = 5,     /* eval_pauli_exclusion_forces src/forces/pauli.cpp:32-48         */
+    XMD_TERM_CONST_ES = 6,  /* eval_const_es_forces src/forces/es/const.cpp:13-32             */
+    XMD_TERM_REL_ES = 7,    /* eval_relative_es_forces src/forces/es/relative.cpp:13-32       */
+    XMD_TERM_QA = 8,        /* qa::process_contacts src/forces/qa/process_contacts.cpp:13-57  */
+    XMD_NUM_TERMS = 9
+};
+
+enum { XMD_PREC_FP64 = 0, XMD_PREC_MIXED = 1 };
+
+#define XMD_NUM_AA 20
+#define XMD_NUM_SS (XMD_NUM_AA * XMD_NUM_AA)
+
+/* Resolved numeric parameters, internal units.  Filled from YAML by
+ * xmd_gpu_create(); field names follow the reference's params structs
+ * (include/xmd/freeform/params.h) and term fields. */
+typedef struct xmd_params {
+    int32_t on[XMD_NUM_TERMS];          /* `enabled:` of each term section          */
+    int32_t langevin_on;                /* langevin: enabled                        */
+    int32_t precision;                  /* XMD_PREC_*  (engine key `precision`)     */
+
+    /* general */
+    double total_time;                  /* general: total time                      */
+    uint64_t seed;                      /* general: seed                            */
+
+    /* langevin / integrator (lang_pc.h:9-10) */
+    double gamma_factor, temperature, dt;
+
+    /* neighbor list (legacy_update.h:11); cutoff/skin are additive engine keys:
+       <= 0 means "derive as the reference does" */
+    double pad_factor, nl_cutoff, nl_skin;
+
+    /* tether forces (tether.h:21-22) */
+    double tether_H1, tether_H2, tether_def_length;
+    /* native angles / dihedrals */
+    double nat_ang_k, cnd_CDA, cnd_CDB, snd_CDH;
+    /* native contacts (go.h:13; report_structure.cpp:85) */
+    double go_depth, go_active_threshold;
+    /* Pauli exclusion (pauli.h:24) */
+    double pauli_r_excl, pauli_depth;
+    /* const ES / relative ES (es/const.h:10-11, es/relative.h:10-11) */
+    double const_es_screen_dist, const_es_permittivity;
+    double rel_es_screen_dist, rel_es_factor;
+    /* amino acid data: charge, polarization (NONE=0, POLAR=1, HYDROPHOBIC=2),
+       contact limits {back, side_all, side_polar, side_hydrophobic} */
+    double charge[XMD_NUM_AA];
+    int32_t polarization[XMD_NUM_AA];
+    int32_t limits[XMD_NUM_AA][4];
+    /* quasi-adiabatic potential (process_contacts.h:15-16, sift_candidates.h:14) */
+    double qa_phase_duration, qa_breaking_factor;
+    double qa_min_cos_hr, qa_min_cos_hh, qa_max_cos_nr;
+    /* lj force variants (lj_variants.h:13-14); ss tables indexed 20*aa1+aa2 */
+    double lj_bb_r_min, lj_bb_depth, lj_bs_r_min, lj_bs_depth;
+    int32_t ss_sinking;
+    double ss_depth[XMD_NUM_SS], ss_r_max[XMD_NUM_SS];
+} xmd_params;
+
+typedef struct xmd_gpu_ctx xmd_gpu_ctx;
+
+/* ---- library ----------------------------------------------------------- */
+int xmd_gpu_abi_version(void);
+/* sizeof(xmd_params) as compiled into the library (layout check for FFI). */
+int xmd_gpu_params_size(void);
+const char *xmd_gpu_last_error(void);
+/* Advance a reference generator state (rand_gen.h:22-28) by n draws with the
+ * GF(2) jump-ahead the engine uses to give every bead its own stream slice. */
+uint64_t xmd_gpu_rng_jump(uint64_t state, uint64_t n_draws);
+/* Parse YAML text (merged over the built-in defaults, as main.cpp:97-106 does)
+ * into resolved parameters without creating a context or touching the GPU. */
+int xmd_gpu_parse_params(const char *yaml_text, xmd_params *out);
+
+/* ---- context lifecycle -------------------------------------------------- */
+/* yaml_text: YAML overrides (may be NULL or "" for pure defaults). */
+int xmd_gpu_create(const char *yaml_text, xmd_gpu_ctx **out);
+int xmd_gpu_create_from_file(const char *yaml_path, xmd_gpu_ctx **out);
+int xmd_gpu_destroy(xmd_gpu_ctx *ctx);
+int xmd_gpu_get_params(const xmd_gpu_ctx *ctx, xmd_params *out);
+/* Replace all parameters (before the first add_replica). */
+int xmd_gpu_set_params(xmd_gpu_ctx *ctx, const xmd_params *p);
+/* Opt a term in or out (kernel<T> semantics, main.cpp:29-75). */
+int xmd_gpu_enable_term(xmd_gpu_ctx *ctx, int term, int on);
+int xmd_gpu_set_precision(xmd_gpu_ctx *ctx, int precision);
+
+/* ---- topology and state (per replica) ----------------------------------- */
+/* Add one system of n beads.  Beads of a chain must be contiguous and in
+ * sequence order (seq_idx = 0,1,2,... within each chain), as the driver lays
+ * them out (main.cpp:134-206).  cell = box edge lengths, 0 = open boundary
+ * along that axis (box.h:12-22).  temperature <= 0 uses the YAML value.
+ * Returns the replica id (>= 0) through *replica_id. */
+int xmd_gpu_add_replica(xmd_gpu_ctx *ctx, int32_t n, const int32_t *chain_idx,
+                        const int32_t *seq_idx, const uint8_t *atype,
+                        const double cell[3], double temperature, uint64_t seed,
+                        int32_t *replica_id);
+/* Bonded lists; entries must be consecutive beads of one chain
+ * (i2 = i1+1, ...), which is how main.cpp:400-479 builds them. */
+int xmd_gpu_set_tethers(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1,
+                        const int32_t *i2, const double *nat_dist);
+int xmd_gpu_set_angles(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1,
+                       const int32_t *i2, const int32_t *i3, const double *nat_theta);
+int xmd_gpu_set_dihedrals(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1,
+                          const int32_t *i2, const int32_t *i3, const int32_t *i4,
+                          const double *nat_phi);
+/* All native contacts (nat_cont{i1,i2,nat_dist}, main.cpp:505-552). */
+int xmd_gpu_set_native_contacts(xmd_gpu_ctx *ctx, int32_t rep, int32_t n,
+                                const int32_t *i1, const int32_t *i2,
+                                const double *nat_dist);
+/* Positions r[3n] (and optional velocities v[3n], NULL = 0): y0 = r,
+ * y1 = v*dt, y2..y5 = 0, t = 0, as main.cpp:208-253 initialises them. */
+int xmd_gpu_set_state(xmd_gpu_ctx *ctx, int32_t rep, const double *r, const double *v);
+/* Full predictor-corrector history y[6][3n], time and generator state. */
+int xmd_gpu_set_history(xmd_gpu_ctx *ctx, int32_t rep, const double *y, double t,
+                        uint64_t rng_state);
+int xmd_gpu_get_state(xmd_gpu_ctx *ctx, int32_t rep, double *r, double *v, double *t);
+int xmd_gpu_get_history(xmd_gpu_ctx *ctx, int32_t rep, double *y, double *t,
+                        uint64_t *rng_state);
+
+/* ---- hot path ------------------------------------------------------------ */
+/* Forces and per-term energies at the current state of one replica (the
+ * force phase of one step, without integration).  The neighbour list is
+ * verified and rebuilt first if needed (verify.cpp:4-23).  F[3n], V[XMD_NUM_TERMS]. */
+int xmd_gpu_eval_forces(xmd_gpu_ctx *ctx, int32_t rep, double *F, double *V);
+/* Advance every replica by nsteps Langevin predictor-corrector steps. */
+int xmd_gpu_step(xmd_gpu_ctx *ctx, int32_t nsteps);
+/* Observables of one replica (total_energy.cpp:4-11, gyration.cpp:4-19,
+ * report_structure.cpp:85): E = V + K, K, Rg, Q (active native fraction). */
+int xmd_gpu_observables(xmd_gpu_ctx *ctx, int32_t rep, double *E, double *K,
+                        double *Rg, double *Q);
+/* Device-side error word of the last step/eval (0 = none). */
+int xmd_gpu_device_status(xmd_gpu_ctx *ctx, int32_t *status);
+int xmd_gpu_synchronize(xmd_gpu_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* XMD_GPU_H */

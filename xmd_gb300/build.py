@@ -1,0 +1,117 @@
+"""In-tree build of the engine (libxmdgpu.so) and of the CPU oracle.
+
+The engine is compiled for sm_103a only, with nvcc directly (no CMake, no
+torch extension machinery): CUDA sources and host C++ become one shared
+library exporting the C ABI of include/xmd_gpu.h.  Translation units are
+compiled in parallel into _build/ and linked in place.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent.parent
+PKG = ROOT / "xmd_gb300"
+CSRC = PKG / "csrc"
+BUILD = ROOT / "_build"
+LIB = PKG / "libxmdgpu.so"
+ORACLE_SRC = ROOT / "oracle" / "xmd_oracle.c"
+ORACLE_LIB = ROOT / "oracle" / "liboracle.so"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC"]
+
+CUDA_SOURCES = ["engine.cu"]
+CXX_SOURCES = ["capi.cpp", "config.cpp", "defaults_yml.cpp"]
+
+
+def _nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", shutil.which("nvcc")):
+        if cand and Path(cand).exists():
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _cuda_home() -> Path:
+    return Path(_nvcc()).resolve().parent.parent
+
+
+def _run(cmd: list[str], verbose: bool) -> None:
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"command failed ({res.returncode}): {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
+    if verbose and res.stderr.strip():
+        print(res.stderr, file=sys.stderr)
+
+
+def _stale(target: Path, deps: list[Path]) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    return any(d.stat().st_mtime > t for d in deps)
+
+
+def build_engine(verbose: bool = False, force: bool = False) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    nvcc = _nvcc()
+    headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "xmd_gpu.h"]
+    jobs = []
+    objs = []
+    for src in CUDA_SOURCES:
+        obj = BUILD / (src + ".o")
+        objs.append(obj)
+        if force or _stale(obj, [CSRC / src] + headers):
+            jobs.append([nvcc, *ARCH, *NVCC_FLAGS, "-c", str(CSRC / src), "-o", str(obj)])
+    for src in CXX_SOURCES:
+        obj = BUILD / (src + ".o")
+        objs.append(obj)
+        if force or _stale(obj, [CSRC / src] + headers):
+            jobs.append(["g++", *CXX_FLAGS, f"-I{_cuda_home() / 'include'}", "-c", str(CSRC / src), "-o", str(obj)])
+    with ThreadPoolExecutor(max_workers=max(1, min(8, os.cpu_count() or 1))) as ex:
+        list(ex.map(lambda c: _run(c, verbose), jobs))
+    if force or _stale(LIB, objs):
+        _run([nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart"], verbose)
+    return LIB
+
+
+def build_oracle(verbose: bool = False, force: bool = False) -> Path:
+    """The CPU restatement (test oracle and timed CPU baseline)."""
+    deps = [ORACLE_SRC, ORACLE_SRC.with_suffix(".h"), ROOT / "include" / "xmd_gpu.h"]
+    if force or _stale(ORACLE_LIB, deps):
+        # -ffp-contract=off: the same uncontracted arithmetic on every host, so
+        # list-membership decisions are reproducible across x86 and Arm.
+        _run(["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-std=c11",
+              "-D_GNU_SOURCE", str(ORACLE_SRC), "-o", str(ORACLE_LIB), "-lm"], verbose)
+    return ORACLE_LIB
+
+
+def build_reference_oracle(verbose: bool = False) -> Path | None:
+    """Compile the reference's own kernels when its source tree is present."""
+    ref_root = Path(os.environ.get("XMD_REF_ROOT", "/root/reference"))
+    if not (ref_root / "xmd" / "src").is_dir():
+        return None
+    script = ROOT / "oracle" / "ref" / "build_ref.sh"
+    out = ROOT / "oracle" / "_ref" / "libxmdref64.so"
+    deps = [script, ROOT / "oracle" / "ref" / "ref_driver.cpp", ROOT / "include" / "xmd_gpu.h"]
+    if _stale(out, deps):
+        _run(["bash", str(script)], verbose)
+    return out
+
+
+def build_all(verbose: bool = False, force: bool = False) -> None:
+    with ThreadPoolExecutor(max_workers=3) as ex:
+        futs = [ex.submit(build_engine, verbose, force), ex.submit(build_oracle, verbose, force),
+                ex.submit(build_reference_oracle, verbose)]
+        for f in futs:
+            f.result()
+
+
+if __name__ == "__main__":
+    build_all(verbose=True, force="--force" in sys.argv)

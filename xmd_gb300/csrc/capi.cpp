@@ -1,0 +1,220 @@
+// capi.cpp - the extern "C" boundary (include/xmd_gpu.h).  No exception
+// crosses it: every failure becomes a status code plus a thread-local message.
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+
+#include "../../include/xmd_gpu.h"
+#include "config.h"
+#include "engine.h"
+
+struct xmd_gpu_ctx {
+    xmdg::Engine *eng = nullptr;
+};
+
+namespace {
+int fail(int code, const std::string &msg) {
+    xmdg::last_error() = msg;
+    return code;
+}
+template <class F>
+int guard(F &&f) {
+    try {
+        f();
+        xmdg::last_error().clear();
+        return XMD_OK;
+    } catch (std::length_error &e) {
+        return fail(XMD_ERR_CAPACITY, e.what());
+    } catch (std::domain_error &e) {
+        return fail(XMD_ERR_NUMERIC, e.what());
+    } catch (std::invalid_argument &e) {
+        return fail(XMD_ERR_ARG, e.what());
+    } catch (std::logic_error &e) {
+        return fail(XMD_ERR_STATE, e.what());
+    } catch (std::runtime_error &e) {
+        std::string m = e.what();
+        if (m.rfind("CUDA", 0) == 0 || m.find("CUDA device") != std::string::npos)
+            return fail(XMD_ERR_CUDA, m);
+        return fail(XMD_ERR_CONFIG, m);
+    } catch (std::exception &e) {
+        return fail(XMD_ERR_STATE, e.what());
+    } catch (...) {
+        return fail(XMD_ERR_STATE, "unknown error");
+    }
+}
+#define NEED_CTX                                                          \
+    if (!ctx || !ctx->eng) return fail(XMD_ERR_ARG, "null context");
+}  // namespace
+
+extern "C" {
+
+int xmd_gpu_abi_version(void) { return XMD_GPU_ABI_VERSION; }
+
+int xmd_gpu_params_size(void) { return (int)sizeof(xmd_params); }
+
+uint64_t xmd_gpu_rng_jump(uint64_t state, uint64_t n_draws) { return xmdg::rng_jump(state, n_draws); }
+
+const char *xmd_gpu_last_error(void) { return xmdg::last_error().c_str(); }
+
+int xmd_gpu_parse_params(const char *yaml_text, xmd_params *out) {
+    if (!out) return fail(XMD_ERR_ARG, "null output");
+    return guard([&] { xmdg::params_from_yaml(yaml_text ? yaml_text : "", out); });
+}
+
+int xmd_gpu_create(const char *yaml_text, xmd_gpu_ctx **out) {
+    if (!out) return fail(XMD_ERR_ARG, "null output");
+    *out = nullptr;
+    xmd_params p;
+    int rc = guard([&] { xmdg::params_from_yaml(yaml_text ? yaml_text : "", &p); });
+    if (rc) return rc;
+    return guard([&] {
+        auto *c = new xmd_gpu_ctx;
+        try {
+            c->eng = new xmdg::Engine(p);
+        } catch (...) {
+            delete c;
+            throw;
+        }
+        *out = c;
+    });
+}
+
+int xmd_gpu_create_from_file(const char *yaml_path, xmd_gpu_ctx **out) {
+    if (!yaml_path) return fail(XMD_ERR_ARG, "null path");
+    std::ifstream in(yaml_path);
+    if (!in) return fail(XMD_ERR_CONFIG, std::string("cannot open ") + yaml_path);
+    std::stringstream ss;
+    ss << in.rdbuf();
+    return xmd_gpu_create(ss.str().c_str(), out);
+}
+
+int xmd_gpu_destroy(xmd_gpu_ctx *ctx) {
+    if (!ctx) return XMD_OK;
+    int rc = guard([&] { delete ctx->eng; });
+    delete ctx;
+    return rc;
+}
+
+int xmd_gpu_get_params(const xmd_gpu_ctx *ctx, xmd_params *out) {
+    NEED_CTX;
+    if (!out) return fail(XMD_ERR_ARG, "null output");
+    *out = ctx->eng->params;
+    return XMD_OK;
+}
+
+int xmd_gpu_set_params(xmd_gpu_ctx *ctx, const xmd_params *p) {
+    NEED_CTX;
+    if (!p) return fail(XMD_ERR_ARG, "null params");
+    if (ctx->eng->finalized || !ctx->eng->reps.empty())
+        return fail(XMD_ERR_STATE, "parameters are fixed once replicas exist");
+    ctx->eng->params = *p;
+    return XMD_OK;
+}
+
+int xmd_gpu_enable_term(xmd_gpu_ctx *ctx, int term, int on) {
+    NEED_CTX;
+    if (term < 0 || term >= XMD_NUM_TERMS) return fail(XMD_ERR_ARG, "term out of range");
+    if (ctx->eng->finalized) return fail(XMD_ERR_STATE, "terms are fixed after the first eval/step");
+    ctx->eng->params.on[term] = on ? 1 : 0;
+    return XMD_OK;
+}
+
+int xmd_gpu_set_precision(xmd_gpu_ctx *ctx, int precision) {
+    NEED_CTX;
+    if (precision != XMD_PREC_FP64 && precision != XMD_PREC_MIXED) return fail(XMD_ERR_ARG, "bad precision");
+    ctx->eng->params.precision = precision;
+    return XMD_OK;
+}
+
+int xmd_gpu_add_replica(xmd_gpu_ctx *ctx, int32_t n, const int32_t *chain_idx, const int32_t *seq_idx,
+                        const uint8_t *atype, const double cell[3], double temperature, uint64_t seed,
+                        int32_t *replica_id) {
+    NEED_CTX;
+    return guard([&] {
+        int id = ctx->eng->add_replica(n, chain_idx, seq_idx, atype, cell, temperature, seed);
+        if (replica_id) *replica_id = id;
+    });
+}
+
+int xmd_gpu_set_tethers(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1, const int32_t *i2,
+                        const double *nat_dist) {
+    NEED_CTX;
+    if (n < 0 || (n > 0 && (!i1 || !i2))) return fail(XMD_ERR_ARG, "bad tether arrays");
+    return guard([&] { ctx->eng->set_tethers(rep, n, i1, i2, nat_dist); });
+}
+
+int xmd_gpu_set_angles(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1, const int32_t *i2,
+                       const int32_t *i3, const double *nat_theta) {
+    NEED_CTX;
+    if (n < 0 || (n > 0 && (!i1 || !i2 || !i3 || !nat_theta))) return fail(XMD_ERR_ARG, "bad angle arrays");
+    return guard([&] { ctx->eng->set_angles(rep, n, i1, i2, i3, nat_theta); });
+}
+
+int xmd_gpu_set_dihedrals(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1, const int32_t *i2,
+                          const int32_t *i3, const int32_t *i4, const double *nat_phi) {
+    NEED_CTX;
+    if (n < 0 || (n > 0 && (!i1 || !i2 || !i3 || !i4 || !nat_phi)))
+        return fail(XMD_ERR_ARG, "bad dihedral arrays");
+    return guard([&] { ctx->eng->set_dihedrals(rep, n, i1, i2, i3, i4, nat_phi); });
+}
+
+int xmd_gpu_set_native_contacts(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1,
+                                const int32_t *i2, const double *nat_dist) {
+    NEED_CTX;
+    if (n < 0 || (n > 0 && (!i1 || !i2 || !nat_dist))) return fail(XMD_ERR_ARG, "bad native arrays");
+    return guard([&] { ctx->eng->set_native(rep, n, i1, i2, nat_dist); });
+}
+
+int xmd_gpu_set_state(xmd_gpu_ctx *ctx, int32_t rep, const double *r, const double *v) {
+    NEED_CTX;
+    return guard([&] { ctx->eng->set_state(rep, r, v); });
+}
+
+int xmd_gpu_set_history(xmd_gpu_ctx *ctx, int32_t rep, const double *y, double t, uint64_t rng_state) {
+    NEED_CTX;
+    if (!y) return fail(XMD_ERR_ARG, "null history");
+    return guard([&] { ctx->eng->set_history(rep, y, t, rng_state); });
+}
+
+int xmd_gpu_get_state(xmd_gpu_ctx *ctx, int32_t rep, double *r, double *v, double *t) {
+    NEED_CTX;
+    return guard([&] { ctx->eng->get_state(rep, r, v, t); });
+}
+
+int xmd_gpu_get_history(xmd_gpu_ctx *ctx, int32_t rep, double *y, double *t, uint64_t *rng_state) {
+    NEED_CTX;
+    return guard([&] { ctx->eng->get_history(rep, y, t, rng_state); });
+}
+
+int xmd_gpu_eval_forces(xmd_gpu_ctx *ctx, int32_t rep, double *F, double *V) {
+    NEED_CTX;
+    return guard([&] { ctx->eng->eval_forces(rep, F, V); });
+}
+
+int xmd_gpu_step(xmd_gpu_ctx *ctx, int32_t nsteps) {
+    NEED_CTX;
+    if (nsteps < 0) return fail(XMD_ERR_ARG, "negative step count");
+    return guard([&] { ctx->eng->step(nsteps); });
+}
+
+int xmd_gpu_observables(xmd_gpu_ctx *ctx, int32_t rep, double *E, double *K, double *Rg, double *Q) {
+    NEED_CTX;
+    return guard([&] { ctx->eng->observables(rep, E, K, Rg, Q); });
+}
+
+int xmd_gpu_device_status(xmd_gpu_ctx *ctx, int32_t *status) {
+    NEED_CTX;
+    return guard([&] {
+        int s = ctx->eng->device_status();
+        if (status) *status = s;
+    });
+}
+
+int xmd_gpu_synchronize(xmd_gpu_ctx *ctx) {
+    NEED_CTX;
+    return guard([&] { ctx->eng->sync(); });
+}
+
+}  // extern "C"

@@ -1,0 +1,288 @@
+// device.cuh - per-interaction physics of the hot path, precision-templated.
+//
+// FT is the type the interaction arithmetic runs in: double for the plain
+// FP64 path, float for the mixed path (pair and bonded forces in FP32,
+// accumulated per bead in FP64 by the caller).  Coordinate differences are
+// always taken in FP64 and then narrowed, so FP32 never sees absolute
+// coordinates.  Operation order follows the cited reference functions.
+#pragma once
+#include <cstdint>
+
+#include "../../include/xmd_gpu.h"
+#include "types.h"
+
+namespace xmdg {
+
+template <class T> struct V3 { T x, y, z; };
+
+template <class T> __device__ __forceinline__ V3<T> v3(T x, T y, T z) { return V3<T>{x, y, z}; }
+template <class T> __device__ __forceinline__ V3<T> operator+(V3<T> a, V3<T> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <class T> __device__ __forceinline__ V3<T> operator-(V3<T> a, V3<T> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <class T> __device__ __forceinline__ V3<T> operator-(V3<T> a) { return {-a.x, -a.y, -a.z}; }
+template <class T> __device__ __forceinline__ V3<T> operator*(T s, V3<T> a) { return {s * a.x, s * a.y, s * a.z}; }
+// vec3.h:133-158, 349-360
+template <class T> __device__ __forceinline__ T nsq(V3<T> a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
+template <class T> __device__ __forceinline__ T dot(V3<T> a, V3<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <class T> __device__ __forceinline__ V3<T> cross(V3<T> a, V3<T> b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+
+__device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
+__device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
+__device__ __forceinline__ double acos_(double x) { return acos(x); }
+__device__ __forceinline__ float acos_(float x) { return acosf(x); }
+__device__ __forceinline__ double exp_(double x) { return exp(x); }
+__device__ __forceinline__ float exp_(float x) { return expf(x); }
+__device__ __forceinline__ void sincos_(double x, double *s, double *c) { sincos(x, s, c); }
+__device__ __forceinline__ void sincos_(float x, float *s, float *c) { sincosf(x, s, c); }
+
+template <class T> __device__ __forceinline__ T norm(V3<T> a) { return sqrt_(nsq(a)); }
+template <class T> __device__ __forceinline__ T ninv(V3<T> a) { return T(1) / norm(a); }
+template <class T> __device__ __forceinline__ V3<T> unit(V3<T> a) { return ninv(a) * a; }
+
+// clamp: math.h:77-80 (a NaN maps to the upper bound)
+template <class T> __device__ __forceinline__ T clampv(T v, T lo, T hi) {
+    return v < lo ? lo : (v < hi ? v : hi);
+}
+// clamped acos: math.h:41-45
+template <class T> __device__ __forceinline__ T acos_c(T x) {
+    T x_ = x < T(-1) ? T(-1) : (x > T(1) ? T(1) : x);
+    return acos_(x_);
+}
+template <class T> __device__ __forceinline__ T ipow6(T s) { return s * (s * (s * (s * (s * s)))); }
+
+// FP64 difference, narrowed to FT
+template <class T>
+__device__ __forceinline__ V3<T> diff(double4_32a u, double4_32a w) {
+    return V3<T>{T(w.x - u.x), T(w.y - u.y), T(w.z - u.z)};
+}
+
+
+
+// box::r_uv: box.h:36-49.  The wrap is done in FP64 before narrowing.
+template <class T>
+__device__ __forceinline__ V3<T> r_uv(const BoxD &b, double4_32a u, double4_32a w) {
+    double dx = w.x - u.x, dy = w.y - u.y, dz = w.z - u.z;
+    dx -= b.cell[0] * rint(dx * b.cell_inv[0]);
+    dy -= b.cell[1] * rint(dy * b.cell_inv[1]);
+    dz -= b.cell[2] * rint(dz * b.cell_inv[2]);
+    return V3<T>{T(dx), T(dy), T(dz)};
+}
+
+// Same minimum image with every product and sum rounded separately, so the
+// neighbour-list membership decisions reproduce an uncontracted CPU build
+// bit for bit.
+__device__ __forceinline__ double dist_exact(const BoxD &b, double4_32a u, double4_32a w) {
+    double d[3] = {__dsub_rn(w.x, u.x), __dsub_rn(w.y, u.y), __dsub_rn(w.z, u.z)};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) d[a] = __dsub_rn(d[a], __dmul_rn(b.cell[a], rint(__dmul_rn(d[a], b.cell_inv[a]))));
+    double s = __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
+    return __dsqrt_rn(s);
+}
+
+
+
+// ---- bonded terms: contributions per centre bead ----------------------------
+
+// harmonic bond (c, c+1): eval_tether_forces::iter tether.cpp:21-36,
+// harmonic::operator() harmonic.h:18-25.  Returns the force on c (the force on
+// c+1 is its negative).
+template <class T>
+__device__ __forceinline__ V3<T> tether_term(const TermP &p, double4_32a r1, double4_32a r2, T nat_dist, T *V) {
+    V3<T> r12 = diff<T>(r1, r2);
+    T r12_n = norm(r12);
+    T dr = r12_n - nat_dist, dr2 = dr * dr;
+    T H1 = T(p.tether_H1), H2 = T(p.tether_H2);
+    T V_ = T(0.5) * dr2 * (H1 + H2 * dr2);
+    T dV_dr = dr * (H1 + T(2) * H2 * dr2);
+    V_ = clampv<T>(V_, T(-1.0e3), T(1.0e3));
+    dV_dr = clampv<T>(dV_dr, T(-1.0e3), T(1.0e3));
+    *V = V_;
+    V3<T> u{r12.x / r12_n, r12.y / r12_n, r12.z / r12_n};
+    return dV_dr * u;
+}
+
+// native angle (c-1, c, c+1): eval_native_angle_forces::iter
+// angle/native.cpp:13-39.  Writes the forces on the three beads.
+template <class T>
+__device__ __forceinline__ void angle_term(const TermP &p, double4_32a q1, double4_32a q2, double4_32a q3, T nat_theta,
+                                           V3<T> *f1, V3<T> *f2, V3<T> *f3, T *V) {
+    V3<T> r12 = diff<T>(q1, q2), r23 = diff<T>(q2, q3);
+    V3<T> x12_23 = cross(r12, r23);
+    T r12_rn = ninv(r12), r23_rn = ninv(r23);
+    V3<T> d1 = r12_rn * unit(cross(r12, x12_23));
+    V3<T> d3 = r23_rn * unit(cross(r23, x12_23));
+    V3<T> d2 = (-d1) - d3;
+    T cos_theta = -dot(r12, r23) * r12_rn * r23_rn;
+    T theta = acos_c(cos_theta);
+    T dtheta = theta - nat_theta;
+    T k = T(p.nat_ang_k);
+    *V = T(0.5) * k * dtheta * dtheta;
+    T dV = k * dtheta;
+    *f1 = -(dV * d1);
+    *f2 = -(dV * d2);
+    *f3 = -(dV * d3);
+}
+
+// native dihedral (c-1, c, c+1, c+2): eval_cnd_forces::iter
+// dihedral/complex_native.cpp:13-49 and eval_snd_forces::iter
+// dihedral/simple_native.cpp:13-45
+template <class T>
+__device__ __forceinline__ void dihedral_term(const TermP &p, double4_32a q1, double4_32a q2, double4_32a q3, double4_32a q4,
+                                              T nat_phi, bool cnd, bool snd, V3<T> *f, T *Vc, T *Vs) {
+    V3<T> r12 = diff<T>(q1, q2), r23 = diff<T>(q2, q3), r34 = diff<T>(q3, q4);
+    V3<T> x12_23 = cross(r12, r23), x23_34 = cross(r23, r34);
+    T x12_23_rn = ninv(x12_23), x23_34_rn = ninv(x23_34);
+    V3<T> x12_23_u = x12_23_rn * x12_23, x23_34_u = x23_34_rn * x23_34;
+    T cos_phi = dot(x12_23_u, x23_34_u);
+    T phi = acos_c(cos_phi);
+    if (dot(x12_23, r34) < T(0)) phi = -phi;
+    T diff_ = phi - nat_phi;
+    T dV = T(0);
+    *Vc = T(0);
+    *Vs = T(0);
+    if (cnd) {
+        T sin_diff, cos_diff, sin_3diff, cos_3diff;
+        sincos_(diff_, &sin_diff, &cos_diff);
+        sincos_(T(3) * diff_, &sin_3diff, &cos_3diff);
+        T CDA = T(p.cnd_CDA), CDB = T(p.cnd_CDB);
+        *Vc = CDA * (T(1) - cos_diff) + CDB * (T(1) - cos_3diff);
+        dV += CDA * sin_diff + CDB * T(3) * sin_3diff;
+    }
+    if (snd) {
+        T CDH = T(p.snd_CDH);
+        *Vs = T(0.5) * CDH * diff_ * diff_;
+        dV += CDH * diff_;
+    }
+    T r23_n = norm(r23);
+    V3<T> d1 = x12_23_rn * (r23_n * (-x12_23_u));
+    V3<T> d4 = x23_34_rn * (r23_n * x23_34_u);
+    T k1 = dot(r12, r23), k4 = dot(r23, r34), den = r23_n * r23_n;
+    V3<T> df{(-d1.x * k1 + d4.x * k4) / den, (-d1.y * k1 + d4.y * k4) / den, (-d1.z * k1 + d4.z * k4) / den};
+    V3<T> d2 = (-d1) + df;
+    V3<T> d3 = (-d4) - df;
+    f[0] = -(dV * d1);
+    f[1] = -(dV * d2);
+    f[2] = -(dV * d3);
+    f[3] = -(dV * d4);
+}
+
+// ---- pair terms: force on the first bead of r12 = r_uv(r_i, r_j) ------------
+
+// lj::operator(): primitives/lj.h:22-30
+template <class T>
+__device__ __forceinline__ void lj_eval(T depth, T r_min, T r_inv, T *V, T *dV) {
+    T s = r_inv * r_min, s6 = ipow6(s), s12 = s6 * s6;
+    T V_ = depth * (s12 - T(2) * s6);
+    T dV_dr = T(12) * depth * r_inv * (s6 - s12);
+    *V = clampv<T>(V_, T(-1.0e3), T(1.0e3));
+    *dV = clampv<T>(dV_dr, T(-1.0e3), T(1.0e3));
+}
+
+// Go contact: eval_go_forces::iter go.cpp:31-46
+template <class T>
+__device__ __forceinline__ V3<T> go_pair(const TermP &p, V3<T> r12, T nat_dist, T *V) {
+    T r12_rn = ninv(r12);
+    V3<T> u = r12_rn * r12;
+    T dV;
+    lj_eval<T>(T(p.go_depth), nat_dist, r12_rn, V, &dV);
+    return dV * u;
+}
+
+// Pauli exclusion: eval_pauli_exclusion_forces::iter pauli.cpp:32-48,
+// shifted_lj::operator() shifted_lj.h:14-21
+template <class T>
+__device__ __forceinline__ V3<T> pauli_pair(const TermP &p, V3<T> r12, T *V) {
+    T r12_rn = ninv(r12);
+    T r_excl = T(p.pauli_r_excl);
+    if (T(1) < r12_rn * r_excl) {
+        V3<T> u = r12_rn * r12;
+        T depth = T(p.pauli_depth);
+        T s = r12_rn * r_excl, s6 = ipow6(s), s12 = s6 * s6;
+        T V_ = depth * (s12 - T(2) * s6 + T(1));
+        T dV_dr = T(12) * depth * r12_rn * (s6 - s12);
+        *V = clampv<T>(V_, T(-1.0e3), T(1.0e3));
+        dV_dr = clampv<T>(dV_dr, T(-1.0e3), T(1.0e3));
+        return dV_dr * u;
+    }
+    *V = T(0);
+    return V3<T>{T(0), T(0), T(0)};
+}
+
+// Debye-Hueckel: eval_const_es_forces::iter es/const.cpp:13-32 and
+// eval_relative_es_forces::iter es/relative.cpp:13-32
+template <class T>
+__device__ __forceinline__ V3<T> es_pair(const TermP &p, V3<T> r12, T q1_x_q2, T *V) {
+    T r12_n = norm(r12), r12_rn = T(1) / r12_n;
+    V3<T> u = r12_rn * r12;
+    T sdi = T(p.es_sdi);
+    T Vij = T(p.es_Vf) * q1_x_q2 * exp_(-r12_n * sdi) * r12_rn * r12_rn;
+    T dVij_dr = p.es_rel ? -Vij * (sdi + T(2) * r12_rn) : -Vij * (sdi + r12_rn);
+    *V = Vij;
+    return dVij_dr * u;
+}
+
+// sink_lj::operator(): primitives/sink_lj.h:24-33
+template <class T>
+__device__ __forceinline__ void sink_lj_eval(T depth, T r_min, T r_max, T r, T r_inv, T *V, T *dV) {
+    T r_eff = (r < r_min ? r_min : (r < r_max ? r : r_max));
+    T s = r_inv * r_eff, s6 = ipow6(s), s12 = s6 * s6;
+    T V_ = depth * (s12 - T(2) * s6);
+    T dV_dr = T(12) * depth * r_inv * (s6 - s12);
+    dV_dr = (r_min < r && r < r_max) ? T(0) : dV_dr;
+    *V = clampv<T>(V_, T(-1.0e3), T(1.0e3));
+    *dV = clampv<T>(dV_dr, T(-1.0e3), T(1.0e3));
+}
+
+// ---- generator: rand_gen.h:22-58 ----------------------------------------------
+__device__ __forceinline__ uint64_t rng_next(uint64_t &st) {
+    uint64_t res = st * 0xd989bcacc137dcd5ull;
+    st ^= st >> 11;
+    st ^= st << 31;
+    st ^= st >> 18;
+    return res;
+}
+// Four draws of one bead (normal_x2 then normal, lang_pc.cpp:15-16)
+__device__ __forceinline__ void noise3(uint64_t st, double *nx, double *ny, double *nz) {
+    const double inv = 1.0 / 4294967296.0;
+    double u1 = (double)(rng_next(st) >> 32) * inv;
+    double u2 = (double)(rng_next(st) >> 32) * inv;
+    double u3 = (double)(rng_next(st) >> 32) * inv;
+    double u4 = (double)(rng_next(st) >> 32) * inv;
+    double r = sqrt(-2.0 * log(u1));
+    if (isnan(r)) r = 0.0;
+    double t = (2.0 * 3.141592653589793) * u2;
+    double s, c;
+    sincos(t, &s, &c);
+    *nx = r * c;
+    *ny = r * s;
+    double r2 = sqrt(-2.0 * log(u3));
+    if (isnan(r2)) r2 = 0.0;
+    *nz = r2 * cos((2.0 * 3.141592653589793) * u4);
+}
+// The same draws in FP32, as the reference's float build takes them
+__device__ __forceinline__ void noise3f(uint64_t st, double *nx, double *ny, double *nz) {
+    const float inv = 1.0f / 4294967296.0f;
+    float u1 = (float)(rng_next(st) >> 32) * inv;
+    float u2 = (float)(rng_next(st) >> 32) * inv;
+    float u3 = (float)(rng_next(st) >> 32) * inv;
+    float u4 = (float)(rng_next(st) >> 32) * inv;
+    float r = sqrtf(-2.0f * logf(u1));
+    if (isnan(r)) r = 0.0f;
+    float s, c;
+    sincosf((float)(2.0 * 3.141592653589793) * u2, &s, &c);
+    *nx = r * c;
+    *ny = r * s;
+    float r2 = sqrtf(-2.0f * logf(u3));
+    if (isnan(r2)) r2 = 0.0f;
+    *nz = r2 * cosf((float)(2.0 * 3.141592653589793) * u4);
+}
+// 64x64 GF(2) matrix (columns) times state: the xorshift jump-ahead
+__device__ __forceinline__ uint64_t gf2_apply(const uint64_t *__restrict__ col, uint64_t x) {
+    uint64_t y = 0;
+#pragma unroll 16
+    for (int k = 0; k < 64; ++k) y ^= col[k] & (0ull - ((x >> k) & 1ull));
+    return y;
+}
+
+}  // namespace xmdg

@@ -1,0 +1,1020 @@
+// engine.cu - sm_103a kernels of the hot path and the context that runs them.
+//
+// Data layout in HBM (N beads of all replicas packed, replica r owning the
+// contiguous range [begin_r, begin_r + n_r)):
+//   pos[2]   double4_32a (x, y, z, charge), double-buffered: one step reads
+//            pos[cur] and writes pos[cur^1]; y0 of the predictor-corrector IS
+//            the position.
+//   yh       y1..y5 as 15 SoA double arrays (coalesced per component).
+//   orig     double4_32a positions of the last Verlet rebuild (skin test).
+//   bonded   per-centre parameters (bond i->i+1, angle at i, dihedral with
+//            second bead i) and a flag word per bead; chains are contiguous,
+//            so bonded partners are i-3..i+3 and come from a shared-memory
+//            tile of the block.
+//   natives  CSR per bead (both directions) with an "in Go list" byte.
+//   Verlet   ELL rows nl_row[k*N + i] = j | flags<<30 holding only pairs that
+//            some enabled pair term keeps (Pauli r < r_excl+pad, ES r < 2D+pad
+//            with q_i q_j != 0); pairs no term keeps are dropped at build time.
+//   cells    per-replica grids (cell budget fixed per replica), counting sort
+//            with a deterministic in-cell order.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstring>
+#include <stdexcept>
+
+#include "device.cuh"
+#include "engine.h"
+
+namespace xmdg {
+
+std::string &last_error() {
+    static thread_local std::string e;
+    return e;
+}
+
+#define CK(call)                                                                     \
+    do {                                                                             \
+        cudaError_t e_ = (call);                                                     \
+        if (e_ != cudaSuccess)                                                       \
+            throw std::runtime_error(std::string("CUDA error ") + cudaGetErrorString(e_) + \
+                                     " at " #call);                                  \
+    } while (0)
+
+constexpr int FB = 128;              // beads per force block
+constexpr int NL_MASK = 0x3FFFFFFF;
+constexpr int NL_PAULI = 1 << 30;
+constexpr int NL_ES = (int)(1u << 31);
+
+enum : int { ST_CAPACITY = 1, ST_NONFINITE = 2 };
+
+// ---- generator jump-ahead (host) ---------------------------------------------
+using GF2 = std::array<uint64_t, 64>;
+static uint64_t xs_step(uint64_t s) {
+    s ^= s >> 11;
+    s ^= s << 31;
+    s ^= s >> 18;
+    return s;
+}
+static uint64_t gf2_apply_h(const GF2 &m, uint64_t x) {
+    uint64_t y = 0;
+    for (int k = 0; k < 64; ++k)
+        if ((x >> k) & 1) y ^= m[k];
+    return y;
+}
+static GF2 gf2_mul(const GF2 &a, const GF2 &b) {
+    GF2 c;
+    for (int k = 0; k < 64; ++k) c[k] = gf2_apply_h(a, b[k]);
+    return c;
+}
+// matrix of `draws` generator steps
+static GF2 gf2_jump(uint64_t draws) {
+    GF2 m, r;
+    for (int k = 0; k < 64; ++k) {
+        m[k] = xs_step(1ull << k);
+        r[k] = 1ull << k;
+    }
+    while (draws) {
+        if (draws & 1) r = gf2_mul(m, r);
+        m = gf2_mul(m, m);
+        draws >>= 1;
+    }
+    return r;
+}
+
+uint64_t rng_jump(uint64_t state, uint64_t n_draws) { return gf2_apply_h(gf2_jump(n_draws), state); }
+
+// ---- device helpers -----------------------------------------------------------
+__device__ __forceinline__ double warp_max(double v) {
+    for (int o = 16; o; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+template <class FT>
+__device__ __forceinline__ void add3(double &fx, double &fy, double &fz, V3<FT> f) {
+    fx += (double)f.x;
+    fy += (double)f.y;
+    fz += (double)f.z;
+}
+
+// ---- force (+ integrate) kernel --------------------------------------------------
+// MODE 0: forces and per-term energies at pos[cur] (eval).
+// MODE 1: forces, then one Langevin predictor-corrector step (lang_pc.cpp:5-41)
+//         writing pos[cur^1], y1..y5, the generator state and the skin-test
+//         displacement (verify.cpp:10-15).
+template <class FT, int MODE>
+__global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
+    const double4_32a *__restrict__ pin = d.pos[cur];
+    const int N = d.N, t = threadIdx.x, i0 = blockIdx.x * FB;
+    __shared__ double4_32a P[FB + 6];
+    __shared__ V3<FT> Ct[FB + 3], Ca[3][FB + 3], Cd[4][FB + 3];
+
+    for (int k = t; k < FB + 6; k += FB) {
+        int idx = i0 - 3 + k;
+        P[k] = (idx >= 0 && idx < N) ? pin[idx] : make_double4_32a(0, 0, 0, 0);
+    }
+    __syncthreads();
+
+    // bonded contributions of centres c in [i0-2, i0+FB]
+    for (int sc = t; sc < FB + 3; sc += FB) {
+        int c = i0 - 2 + sc;
+        uint32_t fl = (c >= 0 && c < N) ? d.bflags[c] : 0u;
+        V3<FT> z{FT(0), FT(0), FT(0)};
+        V3<FT> ft = z, a1 = z, a2 = z, a3 = z, q[4] = {z, z, z, z};
+        int sp = c - (i0 - 3);
+        bool own = (c >= i0 && c < i0 + FB);
+        int rc = own ? d.rep_of[c] : 0;
+        if ((fl & BF_TETH) && p.on[XMD_TERM_TETHER]) {
+            FT V_;
+            ft = tether_term<FT>(p, P[sp], P[sp + 1], (FT)d.teth_r0[c], &V_);
+            if (MODE == 0 && own) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_TETHER], (double)V_);
+        }
+        if ((fl & BF_ANG) && p.on[XMD_TERM_NAT_ANG]) {
+            FT V_;
+            angle_term<FT>(p, P[sp - 1], P[sp], P[sp + 1], (FT)d.ang_t0[c], &a1, &a2, &a3, &V_);
+            if (MODE == 0 && own) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_NAT_ANG], (double)V_);
+        }
+        if ((fl & BF_DIH) && (p.on[XMD_TERM_CND] || p.on[XMD_TERM_SND])) {
+            FT Vc, Vs;
+            dihedral_term<FT>(p, P[sp - 1], P[sp], P[sp + 1], P[sp + 2], (FT)d.dih_p0[c],
+                              p.on[XMD_TERM_CND] != 0, p.on[XMD_TERM_SND] != 0, q, &Vc, &Vs);
+            if (MODE == 0 && own) {
+                if (p.on[XMD_TERM_CND]) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_CND], (double)Vc);
+                if (p.on[XMD_TERM_SND]) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_SND], (double)Vs);
+            }
+        }
+        Ct[sc] = ft;
+        Ca[0][sc] = a1; Ca[1][sc] = a2; Ca[2][sc] = a3;
+        Cd[0][sc] = q[0]; Cd[1][sc] = q[1]; Cd[2][sc] = q[2]; Cd[3][sc] = q[3];
+    }
+    __syncthreads();
+
+    const int i = i0 + t;
+    if (i >= N) return;
+    const int s = t + 2;   // centre slot of bead i
+    double fx = 0, fy = 0, fz = 0;
+    add3(fx, fy, fz, Ct[s]);
+    add3(fx, fy, fz, -Ct[s - 1]);
+    add3(fx, fy, fz, Ca[2][s - 1]);
+    add3(fx, fy, fz, Ca[1][s]);
+    add3(fx, fy, fz, Ca[0][s + 1]);
+    add3(fx, fy, fz, Cd[0][s + 1]);
+    add3(fx, fy, fz, Cd[1][s]);
+    add3(fx, fy, fz, Cd[2][s - 1]);
+    add3(fx, fy, fz, Cd[3][s - 2]);
+
+    const double4_32a pi = P[t + 3];
+    const int r = d.rep_of[i];
+    const BoxD bx = d.rep[r].box;
+    double vgo = 0, vpa = 0, ves = 0;
+
+    if (p.on[XMD_TERM_GO]) {
+        const int k1 = d.nat_start[i + 1];
+        for (int k = d.nat_start[i]; k < k1; ++k) {
+            if (!d.nat_on[k]) continue;
+            int j = d.nat_j[k];
+            FT V_;
+            V3<FT> f = go_pair<FT>(p, r_uv<FT>(bx, pi, pin[j]), (FT)d.nat_d[k], &V_);
+            add3(fx, fy, fz, f);
+            if (MODE == 0 && i < j) vgo += (double)V_;
+        }
+    }
+    const int cnt = d.nl_cnt[i];
+    for (int k = 0; k < cnt; ++k) {
+        int e = d.nl_row[(size_t)k * N + i];
+        int j = e & NL_MASK;
+        double4_32a pj = pin[j];
+        V3<FT> r12 = r_uv<FT>(bx, pi, pj);
+        if (e & NL_PAULI) {
+            FT V_;
+            V3<FT> f = pauli_pair<FT>(p, r12, &V_);
+            add3(fx, fy, fz, f);
+            if (MODE == 0 && i < j) vpa += (double)V_;
+        }
+        if (e & NL_ES) {
+            FT V_;
+            V3<FT> f = es_pair<FT>(p, r12, (FT)(pi.w * pj.w), &V_);
+            add3(fx, fy, fz, f);
+            if (MODE == 0 && i < j) ves += (double)V_;
+        }
+    }
+
+    if (!(isfinite(fx) && isfinite(fy) && isfinite(fz))) atomicOr(d.status, ST_NONFINITE);
+
+    if (MODE == 0) {
+        d.F[3 * i] = fx;
+        d.F[3 * i + 1] = fy;
+        d.F[3 * i + 2] = fz;
+        double *Vr = d.Vrep + r * XMD_NUM_TERMS;
+        if (vgo != 0.0) atomicAdd(&Vr[XMD_TERM_GO], vgo);
+        if (vpa != 0.0) atomicAdd(&Vr[XMD_TERM_PAULI], vpa);
+        if (ves != 0.0) atomicAdd(&Vr[p.es_rel ? XMD_TERM_REL_ES : XMD_TERM_CONST_ES], ves);
+        return;
+    }
+
+    // ---- lang_pc_step::operator(), lang_pc.cpp:11-37, mass = 1 (main.cpp:156) ----
+    uint64_t st = d.rng[i];
+    double nz[3];
+    if (sizeof(FT) == 8) noise3(st, &nz[0], &nz[1], &nz[2]);
+    else noise3f(st, &nz[0], &nz[1], &nz[2]);
+    d.rng[i] = gf2_apply(d.jump + 64 * r, st);
+    const double dt = p.dt, dt_inv = 1.0 / dt, h = dt * dt / 2.0;
+    const double gamma = p.gamma_factor * 1.0;
+    const double nsd = d.rep[r].noise_sd;
+    const double F3[3] = {fx, fy, fz};
+    double y0[3] = {pi.x, pi.y, pi.z};
+    double *yh = d.yh;
+    const size_t Ns = (size_t)N;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        double y1 = yh[(0 * 3 + a) * Ns + i], y2 = yh[(1 * 3 + a) * Ns + i];
+        double y3 = yh[(2 * 3 + a) * Ns + i], y4 = yh[(3 * 3 + a) * Ns + i];
+        double y5 = yh[(4 * 3 + a) * Ns + i];
+        double v = y1 * dt_inv;
+        double a_ = F3[a] * 1.0 - gamma * v + nsd * nz[a];
+        double error = y2 - a_ * h;
+        y0[a] -= 3.0 / 16.0 * error;
+        y1 -= 251.0 / 360.0 * error;
+        y2 -= 1.0 * error;
+        y3 -= 11.0 / 18.0 * error;
+        y4 -= 1.0 / 6.0 * error;
+        y5 -= 1.0 / 60.0 * error;
+        y0[a] += y1 + y2 + y3 + y4 + y5;
+        y1 += 2.0 * y2 + 3.0 * y3 + 4.0 * y4 + 5.0 * y5;
+        y2 += 3.0 * y3 + 6.0 * y4 + 10.0 * y5;
+        y3 += 4.0 * y4 + 10.0 * y5;
+        y4 += 5.0 * y5;
+        yh[(0 * 3 + a) * Ns + i] = y1;
+        yh[(1 * 3 + a) * Ns + i] = y2;
+        yh[(2 * 3 + a) * Ns + i] = y3;
+        yh[(3 * 3 + a) * Ns + i] = y4;
+        yh[(4 * 3 + a) * Ns + i] = y5;
+    }
+    double4_32a pn = make_double4_32a(y0[0], y0[1], y0[2], pi.w);
+    d.pos[cur ^ 1][i] = pn;
+    // skin test displacement: norm(box->r_uv(r_, orig_r_)), verify.cpp:12-14
+    double disp = dist_exact(bx, pn, d.orig[i]);
+    const unsigned lane = t & 31;
+    int r0 = __shfl_sync(0xffffffffu & __activemask(), r, 0);
+    unsigned mask = __activemask();
+    if (__all_sync(mask, r == r0) && mask == 0xffffffffu) {
+        double m = warp_max(disp);
+        if (lane == 0) atomicMax(&d.rep[r].maxdisp, (unsigned long long)__double_as_longlong(m));
+    } else {
+        atomicMax(&d.rep[r].maxdisp, (unsigned long long)__double_as_longlong(disp));
+    }
+}
+
+// ---- skin decision (nl::verify, verify.cpp:4-23) --------------------------------
+__global__ void k_nl_check(Dev d, int advance, double dt) {
+    __shared__ int any_s;
+    if (threadIdx.x == 0) any_s = 0;
+    __syncthreads();
+    int any = 0;
+    for (int r = threadIdx.x; r < d.R; r += blockDim.x) {
+        RepDev &rp = d.rep[r];
+        if (advance) rp.t += dt;                       // *t = (*true_t += dt)
+        double md = __longlong_as_double((long long)rp.maxdisp);
+        rp.maxdisp = 0ull;
+        int rb = rp.first || (2.0 * md + 0.0 > rp.pad);
+        rp.rebuild = rb;
+        any |= rb;
+    }
+    if (any) atomicOr(&any_s, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) *d.any_rebuild = any_s;
+}
+
+// ---- cell lists: one block per flagged replica -----------------------------------
+__device__ __forceinline__ int cell_coord(const RepDev &rp, int a, double x) {
+    int k;
+    if (rp.per[a]) {
+        double f = x * rp.box.cell_inv[a];
+        f -= floor(f);
+        k = (int)(f * rp.dims[a]);
+    } else {
+        k = (int)floor((x - rp.lo[a]) / rp.cs[a]);
+    }
+    return k < 0 ? 0 : (k >= rp.dims[a] ? rp.dims[a] - 1 : k);
+}
+__device__ __forceinline__ double comp(double4_32a v, int a) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); }
+
+constexpr int CB = 1024;
+__global__ void __launch_bounds__(CB) k_cells(Dev d, int cur) {
+    const int r = blockIdx.x;
+    RepDev &rp = d.rep[r];
+    if (!rp.rebuild) return;
+    const double4_32a *pos = d.pos[cur];
+    const int b = rp.begin, n = rp.n, off = rp.cell_off, bud = rp.cell_budget;
+    __shared__ double red_lo[3][32], red_hi[3][32];
+    __shared__ int scan_s[CB];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+
+    // bounding box along open axes
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int i = b + t; i < b + n; i += CB) {
+        double4_32a q = pos[i];
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = fmin(lo[a], comp(q, a));
+            hi[a] = fmax(hi[a], comp(q, a));
+        }
+    }
+    for (int a = 0; a < 3; ++a) {
+        for (int o = 16; o; o >>= 1) {
+            lo[a] = fmin(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+            hi[a] = fmax(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+        }
+        if (lane == 0) { red_lo[a][w] = lo[a]; red_hi[a][w] = hi[a]; }
+    }
+    __syncthreads();
+    if (t == 0) {
+        const double rr = rp.req_r * (1.0 + 1e-9);
+        long total = 1;
+        for (int a = 0; a < 3; ++a) {
+            double l = 1e300, hh = -1e300;
+            for (int q = 0; q < CB / 32; ++q) { l = fmin(l, red_lo[a][q]); hh = fmax(hh, red_hi[a][q]); }
+            int dm;
+            if (rp.per[a]) {
+                dm = (int)floor(rp.box.cell[a] / rr);
+                rp.lo[a] = 0.0;
+            } else {
+                double ext = hh - l;
+                dm = (int)floor(ext / rr);
+                rp.lo[a] = l;
+            }
+            dm = dm < 1 ? 1 : (dm > 1024 ? 1024 : dm);
+            rp.dims[a] = dm;
+            total *= dm;
+        }
+        while (total > bud) {   // keep within the replica's fixed cell budget
+            int am = 0;
+            for (int a = 1; a < 3; ++a) if (rp.dims[a] > rp.dims[am]) am = a;
+            rp.dims[am] = rp.dims[am] > 1 ? rp.dims[am] - 1 : 1;
+            total = (long)rp.dims[0] * rp.dims[1] * rp.dims[2];
+        }
+        for (int a = 0; a < 3; ++a) {
+            if (rp.per[a]) {
+                rp.cs[a] = rp.box.cell[a] / rp.dims[a];
+            } else {
+                double l = 1e300, hh = -1e300;
+                for (int q = 0; q < CB / 32; ++q) { l = fmin(l, red_lo[a][q]); hh = fmax(hh, red_hi[a][q]); }
+                rp.cs[a] = fmax((hh - l) / rp.dims[a], rr);
+            }
+        }
+        rp.first = 0;
+        rp.rebuilds += 1;
+    }
+    __syncthreads();
+    const int ncell = rp.dims[0] * rp.dims[1] * rp.dims[2];
+    for (int c = t; c < ncell; c += CB) {
+        d.cell_cnt[off + c] = 0;
+        d.cell_fill[off + c] = 0;
+    }
+    __syncthreads();
+    for (int i = b + t; i < b + n; i += CB) {
+        double4_32a q = pos[i];
+        int c = (cell_coord(rp, 2, q.z) * rp.dims[1] + cell_coord(rp, 1, q.y)) * rp.dims[0] +
+                cell_coord(rp, 0, q.x);
+        d.bead_cell[i] = off + c;
+        atomicAdd(&d.cell_cnt[off + c], 1);
+    }
+    __syncthreads();
+    // exclusive scan of the counts, contiguous chunk per thread
+    const int chunk = (ncell + CB - 1) / CB;
+    const int c0 = t * chunk, c1 = min(ncell, c0 + chunk);
+    int sum = 0;
+    for (int c = c0; c < c1; ++c) sum += d.cell_cnt[off + c];
+    scan_s[t] = sum;
+    __syncthreads();
+    for (int o = 1; o < CB; o <<= 1) {
+        int v = t >= o ? scan_s[t - o] : 0;
+        __syncthreads();
+        scan_s[t] += v;
+        __syncthreads();
+    }
+    int run = b + scan_s[t] - sum;
+    for (int c = c0; c < c1; ++c) {
+        d.cell_start[off + c] = run;
+        run += d.cell_cnt[off + c];
+    }
+    __syncthreads();
+    for (int i = b + t; i < b + n; i += CB) {
+        int c = d.bead_cell[i];
+        int slot = atomicAdd(&d.cell_fill[c], 1);
+        d.cell_items[d.cell_start[c] + slot] = i;
+    }
+    __syncthreads();
+    // deterministic order inside each cell
+    for (int c = t; c < ncell; c += CB) {
+        int s0 = d.cell_start[off + c], m = d.cell_cnt[off + c];
+        int *it = d.cell_items + s0;
+        for (int x = 1; x < m; ++x) {
+            int v = it[x], y = x - 1;
+            while (y >= 0 && it[y] > v) { it[y + 1] = it[y]; --y; }
+            it[y + 1] = v;
+        }
+    }
+}
+
+// ---- Verlet rows (legacy_update.cpp:16-62 + the update_* filters) ---------------
+__global__ void __launch_bounds__(128) k_nl_build(Dev d, TermP p, int cur) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.N) return;
+    const int r = d.rep_of[i];
+    const RepDev &rp = d.rep[r];
+    if (!rp.rebuild) return;
+    const double4_32a *pos = d.pos[cur];
+    const double4_32a pi = pos[i];
+    const BoxD bx = rp.box;
+    const int ci = d.chain[i], si = d.seq[i];
+    const int n0 = d.nat_start[i], n1 = d.nat_start[i + 1];
+    const double pad = rp.pad;
+
+    // Go list: update_go_contacts, go.cpp:11-22
+    for (int k = n0; k < n1; ++k) {
+        double dd = dist_exact(bx, pi, pos[d.nat_j[k]]);
+        d.nat_on[k] = dd < __dadd_rn(2.0 * d.nat_d[k], pad);
+    }
+
+    int cc[3];
+    cc[0] = cell_coord(rp, 0, pi.x);
+    cc[1] = cell_coord(rp, 1, pi.y);
+    cc[2] = cell_coord(rp, 2, pi.z);
+    int offs[3][3], noff[3];
+    for (int a = 0; a < 3; ++a) {
+        noff[a] = 0;
+        for (int dlt = -1; dlt <= 1; ++dlt) {
+            int k = cc[a] + dlt;
+            if (rp.per[a]) k = ((k % rp.dims[a]) + rp.dims[a]) % rp.dims[a];
+            else if (k < 0 || k >= rp.dims[a]) continue;
+            bool dup = false;
+            for (int q = 0; q < noff[a]; ++q) dup |= offs[a][q] == k;
+            if (!dup) offs[a][noff[a]++] = k;
+        }
+    }
+    const bool pauli_on = p.on[XMD_TERM_PAULI] != 0;
+    const bool es_on = (p.on[XMD_TERM_CONST_ES] || p.on[XMD_TERM_REL_ES]);
+    int cnt = 0;
+    const int cap = d.nl_cap;
+    for (int az = 0; az < noff[2]; ++az)
+        for (int ay = 0; ay < noff[1]; ++ay)
+            for (int ax = 0; ax < noff[0]; ++ax) {
+                int c = rp.cell_off + (offs[2][az] * rp.dims[1] + offs[1][ay]) * rp.dims[0] + offs[0][ax];
+                int q0 = d.cell_start[c], q1 = q0 + d.cell_cnt[c];
+                for (int q = q0; q < q1; ++q) {
+                    int j = d.cell_items[q];
+                    if (j == i) continue;
+                    int cj = d.chain[j], sj = d.seq[j];
+                    int df = si > sj ? si - sj : sj - si;
+                    if (ci == cj && df < 3) continue;
+                    double4_32a pj = pos[j];
+                    double dd = dist_exact(bx, pi, pj);
+                    if (!(dd < rp.req_r)) continue;
+                    bool native = false;
+                    for (int k = n0; k < n1; ++k) native |= d.nat_j[k] == j;
+                    if (native) continue;
+                    double inv = __ddiv_rn(1.0, dd);
+                    int flags = 0;
+                    if (pauli_on && inv > rp.pauli_min_inv) flags |= NL_PAULI;
+                    if (es_on && inv > rp.es_min_inv && pi.w * pj.w != 0.0) flags |= NL_ES;
+                    if (!flags) continue;
+                    if (cnt < cap) d.nl_row[(size_t)cnt * d.N + i] = j | flags;
+                    ++cnt;
+                }
+            }
+    if (cnt > cap) {
+        atomicOr(d.status, ST_CAPACITY);
+        cnt = cap;
+    }
+    d.nl_cnt[i] = cnt;
+    d.orig[i] = pi;
+}
+
+// =================================================================== host ==
+
+Engine::Engine(const xmd_params &p) : params(p) {
+    int ndev = 0;
+    CK(cudaGetDeviceCount(&ndev));
+    if (ndev < 1) throw std::runtime_error("no CUDA device");
+    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    CK(cudaMallocHost(&h_any, sizeof(int) * 4));
+}
+
+Engine::~Engine() {
+    release();
+    if (h_any) cudaFreeHost(h_any);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+void *Engine::dalloc(size_t bytes) {
+    void *p = nullptr;
+    CK(cudaMalloc(&p, bytes < 16 ? 16 : bytes));
+    CK(cudaMemsetAsync(p, 0, bytes < 16 ? 16 : bytes, stream));
+    allocs.push_back(p);
+    return p;
+}
+
+void Engine::release() {
+    for (void *p : allocs) cudaFree(p);
+    allocs.clear();
+    d = Dev{};
+    finalized = false;
+}
+
+int Engine::add_replica(int n, const int32_t *chain, const int32_t *seq, const uint8_t *atype,
+                        const double cell[3], double temperature, uint64_t seed) {
+    if (finalized) throw std::invalid_argument("replicas must be added before the first eval/step");
+    if (n <= 0 || n > NL_MASK) throw std::invalid_argument("bead count out of range");
+    if (!chain || !seq || !atype) throw std::invalid_argument("null topology array");
+    RepHost r;
+    r.n = n;
+    r.chain.assign(chain, chain + n);
+    r.seq.assign(seq, seq + n);
+    r.atype.assign(atype, atype + n);
+    for (int i = 0; i < n; ++i)
+        if (atype[i] >= XMD_NUM_AA) throw std::invalid_argument("atype out of range (0..19)");
+    for (int a = 0; a < 3; ++a) {
+        r.cell[a] = cell ? cell[a] : 0.0;
+        if (r.cell[a] < 0 || !std::isfinite(r.cell[a])) throw std::invalid_argument("bad cell");
+    }
+    r.temperature = temperature > 0 ? temperature : params.temperature;
+    r.seed = seed;
+    const double nan = std::nan("");
+    r.teth_r0.assign(n, nan);
+    r.ang_t0.assign(n, nan);
+    r.dih_p0.assign(n, nan);
+    reps.push_back(std::move(r));
+    return (int)reps.size() - 1;
+}
+
+static void check_rep(const std::vector<RepHost> &reps, int rep) {
+    if (rep < 0 || rep >= (int)reps.size()) throw std::invalid_argument("replica id out of range");
+}
+static bool consecutive(const RepHost &r, int a, int b) {
+    return a >= 0 && b < r.n && b == a + 1 && r.chain[a] == r.chain[b] && r.seq[b] == r.seq[a] + 1;
+}
+
+void Engine::set_tethers(int rep, int n, const int32_t *i1, const int32_t *i2, const double *dd) {
+    check_rep(reps, rep);
+    if (finalized) throw std::invalid_argument("topology is fixed after the first eval/step");
+    RepHost &r = reps[rep];
+    std::fill(r.teth_r0.begin(), r.teth_r0.end(), std::nan(""));
+    for (int k = 0; k < n; ++k) {
+        int a = std::min(i1[k], i2[k]), b = std::max(i1[k], i2[k]);
+        if (!consecutive(r, a, b)) throw std::invalid_argument("tether is not a bond between consecutive beads of a chain");
+        if (!std::isnan(r.teth_r0[a])) throw std::invalid_argument("duplicate tether");
+        // tether.length.value_or(def_length), main.cpp:409-413
+        r.teth_r0[a] = (dd && dd[k] > 0) ? dd[k] : params.tether_def_length;
+    }
+}
+void Engine::set_angles(int rep, int n, const int32_t *i1, const int32_t *i2, const int32_t *i3,
+                        const double *th) {
+    check_rep(reps, rep);
+    if (finalized) throw std::invalid_argument("topology is fixed after the first eval/step");
+    RepHost &r = reps[rep];
+    std::fill(r.ang_t0.begin(), r.ang_t0.end(), std::nan(""));
+    for (int k = 0; k < n; ++k) {
+        if (!consecutive(r, i1[k], i2[k]) || !consecutive(r, i2[k], i3[k]))
+            throw std::invalid_argument("angle must be (i-1, i, i+1) of one chain");
+        if (!std::isnan(r.ang_t0[i2[k]])) throw std::invalid_argument("duplicate angle");
+        if (!std::isfinite(th[k])) throw std::invalid_argument("non-finite native angle");
+        r.ang_t0[i2[k]] = th[k];
+    }
+}
+void Engine::set_dihedrals(int rep, int n, const int32_t *i1, const int32_t *i2, const int32_t *i3,
+                           const int32_t *i4, const double *ph) {
+    check_rep(reps, rep);
+    if (finalized) throw std::invalid_argument("topology is fixed after the first eval/step");
+    RepHost &r = reps[rep];
+    std::fill(r.dih_p0.begin(), r.dih_p0.end(), std::nan(""));
+    for (int k = 0; k < n; ++k) {
+        if (!consecutive(r, i1[k], i2[k]) || !consecutive(r, i2[k], i3[k]) || !consecutive(r, i3[k], i4[k]))
+            throw std::invalid_argument("dihedral must be (i-1, i, i+1, i+2) of one chain");
+        if (!std::isnan(r.dih_p0[i2[k]])) throw std::invalid_argument("duplicate dihedral");
+        if (!std::isfinite(ph[k])) throw std::invalid_argument("non-finite native dihedral");
+        r.dih_p0[i2[k]] = ph[k];
+    }
+}
+void Engine::set_native(int rep, int n, const int32_t *i1, const int32_t *i2, const double *dd) {
+    check_rep(reps, rep);
+    if (finalized) throw std::invalid_argument("topology is fixed after the first eval/step");
+    RepHost &r = reps[rep];
+    std::vector<std::tuple<int, int, double>> v;
+    for (int k = 0; k < n; ++k) {
+        int a = std::min(i1[k], i2[k]), b = std::max(i1[k], i2[k]);
+        if (a < 0 || b >= r.n || a == b) throw std::invalid_argument("native contact index out of range");
+        if (!(dd[k] > 0)) throw std::invalid_argument("native distance must be positive");
+        v.emplace_back(a, b, dd[k]);
+    }
+    std::sort(v.begin(), v.end());
+    for (size_t k = 1; k < v.size(); ++k)
+        if (std::get<0>(v[k]) == std::get<0>(v[k - 1]) && std::get<1>(v[k]) == std::get<1>(v[k - 1]))
+            throw std::invalid_argument("duplicate native contact");
+    r.nat_i1.clear(); r.nat_i2.clear(); r.nat_d.clear();
+    for (auto &[a, b, x] : v) { r.nat_i1.push_back(a); r.nat_i2.push_back(b); r.nat_d.push_back(x); }
+}
+
+void Engine::derive_rep(int ri, RepDev &rd) {
+    const RepHost &r = reps[ri];
+    const xmd_params &p = params;
+    std::memset(&rd, 0, sizeof rd);
+    for (int a = 0; a < 3; ++a) {
+        rd.box.cell[a] = r.cell[a];
+        rd.box.cell_inv[a] = r.cell[a] != 0.0 ? 1.0 / r.cell[a] : 0.0;   // box.h:12-22
+        rd.per[a] = r.cell[a] != 0.0;
+    }
+    // max_cutoff: main.cpp:500, 545-551, 628-630, 642-644, 742-746
+    double mc = 0.0;
+    if (p.on[XMD_TERM_PAULI]) mc = std::max(mc, p.pauli_r_excl);
+    if (p.on[XMD_TERM_GO]) for (double x : r.nat_d) mc = std::max(mc, 2.0 * x);
+    if (p.on[XMD_TERM_CONST_ES]) mc = std::max(mc, 2.0 * p.const_es_screen_dist);
+    if (p.on[XMD_TERM_REL_ES]) mc = std::max(mc, 2.0 * p.rel_es_screen_dist);
+    if (p.nl_cutoff > 0.0) mc = p.nl_cutoff;
+    rd.pad = p.nl_skin > 0.0 ? p.nl_skin : p.pad_factor * mc;   // legacy_update.cpp:7-8
+    rd.req_r = mc + rd.pad;
+    double es_cut = p.on[XMD_TERM_CONST_ES] ? 2.0 * p.const_es_screen_dist : 2.0 * p.rel_es_screen_dist;
+    rd.es_min_inv = 1.0 / (es_cut + rd.pad);                      // es_pair.cpp:9
+    rd.pauli_min_inv = 1.0 / (p.pauli_r_excl + rd.pad);           // pauli.cpp:12-13
+    rd.noise_sd = std::sqrt(2.0 * 1.0 * r.temperature) * std::sqrt(p.gamma_factor) * 1.0;
+    rd.begin = r.begin;
+    rd.n = r.n;
+    rd.first = 1;
+}
+
+void Engine::finalize() {
+    if (finalized) return;
+    if (reps.empty()) throw std::logic_error("no replica added");
+    for (auto &r : reps)
+        if (!r.have_state) throw std::logic_error("set_state must be called for every replica");
+    const xmd_params &p = params;
+    int N = 0;
+    int R = (int)reps.size();
+    long cells = 0;
+    std::vector<int> cell_off(R), cell_bud(R);
+    for (int k = 0; k < R; ++k) {
+        reps[k].begin = N;
+        N += reps[k].n;
+        cell_off[k] = (int)cells;
+        cell_bud[k] = std::max(64, 2 * reps[k].n);
+        cells += cell_bud[k];
+    }
+    d.N = N;
+    d.R = R;
+    d.nl_cap = nl_cap;
+    d.pos[0] = (double4_32a *)dalloc(sizeof(double4_32a) * N);
+    d.pos[1] = (double4_32a *)dalloc(sizeof(double4_32a) * N);
+    d.yh = (double *)dalloc(sizeof(double) * 15 * (size_t)N);
+    d.orig = (double4_32a *)dalloc(sizeof(double4_32a) * N);
+    d.F = (double *)dalloc(sizeof(double) * 3 * (size_t)N);
+    d.Vrep = (double *)dalloc(sizeof(double) * XMD_NUM_TERMS * R);
+    d.rep_of = (int32_t *)dalloc(sizeof(int32_t) * N);
+    d.bflags = (uint32_t *)dalloc(sizeof(uint32_t) * N);
+    d.chain = (int32_t *)dalloc(sizeof(int32_t) * N);
+    d.seq = (int32_t *)dalloc(sizeof(int32_t) * N);
+    d.atype = (uint8_t *)dalloc(N);
+    d.teth_r0 = (double *)dalloc(sizeof(double) * N);
+    d.ang_t0 = (double *)dalloc(sizeof(double) * N);
+    d.dih_p0 = (double *)dalloc(sizeof(double) * N);
+    d.nat_start = (int32_t *)dalloc(sizeof(int32_t) * (N + 1));
+    d.nl_row = (int32_t *)dalloc(sizeof(int32_t) * (size_t)nl_cap * N);
+    d.nl_cnt = (int32_t *)dalloc(sizeof(int32_t) * N);
+    d.cell_cnt = (int32_t *)dalloc(sizeof(int32_t) * cells);
+    d.cell_start = (int32_t *)dalloc(sizeof(int32_t) * cells);
+    d.cell_fill = (int32_t *)dalloc(sizeof(int32_t) * cells);
+    d.cell_items = (int32_t *)dalloc(sizeof(int32_t) * N);
+    d.bead_cell = (int32_t *)dalloc(sizeof(int32_t) * N);
+    d.rng = (uint64_t *)dalloc(sizeof(uint64_t) * N);
+    d.jump = (uint64_t *)dalloc(sizeof(uint64_t) * 64 * R);
+    d.rep = (RepDev *)dalloc(sizeof(RepDev) * R);
+    d.any_rebuild = (int *)dalloc(sizeof(int) * 4);
+    d.status = (int *)dalloc(sizeof(int) * 4);
+
+    // host staging of the static per-bead data
+    std::vector<int32_t> rep_of(N), chain(N), seq(N), nat_start(N + 1, 0);
+    std::vector<uint32_t> bfl(N, 0);
+    std::vector<uint8_t> at(N);
+    std::vector<double> tr(N, 0.0), ar(N, 0.0), dr(N, 0.0);
+    std::vector<std::vector<std::pair<int, double>>> nat(N);
+    std::vector<RepDev> rd(R);
+    std::vector<uint64_t> jumps(64 * (size_t)R);
+    int chain_base = 0;
+    for (int k = 0; k < R; ++k) {
+        RepHost &r = reps[k];
+        int maxc = 0;
+        for (int i = 0; i < r.n; ++i) {
+            int g = r.begin + i;
+            rep_of[g] = k;
+            chain[g] = chain_base + r.chain[i];
+            maxc = std::max(maxc, r.chain[i] + 1);
+            seq[g] = r.seq[i];
+            at[g] = r.atype[i];
+            uint32_t f = 0;
+            if (!std::isnan(r.teth_r0[i])) { f |= BF_TETH; tr[g] = r.teth_r0[i]; }
+            if (!std::isnan(r.ang_t0[i])) { f |= BF_ANG; ar[g] = r.ang_t0[i]; }
+            if (!std::isnan(r.dih_p0[i])) { f |= BF_DIH; dr[g] = r.dih_p0[i]; }
+            if (i > 0 && consecutive(r, i - 1, i)) f |= BF_PREV;
+            if (i + 1 < r.n && consecutive(r, i, i + 1)) f |= BF_NEXT;
+            bfl[g] = f;
+        }
+        chain_base += maxc;
+        for (size_t q = 0; q < r.nat_i1.size(); ++q) {
+            int a = r.begin + r.nat_i1[q], b = r.begin + r.nat_i2[q];
+            nat[a].push_back({b, r.nat_d[q]});
+            nat[b].push_back({a, r.nat_d[q]});
+        }
+        derive_rep(k, rd[k]);
+        rd[k].cell_off = cell_off[k];
+        rd[k].cell_budget = cell_bud[k];
+        GF2 j = gf2_jump(4ull * (uint64_t)r.n);
+        std::copy(j.begin(), j.end(), jumps.begin() + 64 * (size_t)k);
+    }
+    std::vector<int32_t> nat_j;
+    std::vector<double> nat_d;
+    for (int i = 0; i < N; ++i) {
+        std::sort(nat[i].begin(), nat[i].end());
+        nat_start[i] = (int)nat_j.size();
+        for (auto &e : nat[i]) { nat_j.push_back(e.first); nat_d.push_back(e.second); }
+    }
+    nat_start[N] = (int)nat_j.size();
+    size_t NN = nat_j.size();
+    d.nat_j = (int32_t *)dalloc(sizeof(int32_t) * (NN ? NN : 1));
+    d.nat_d = (double *)dalloc(sizeof(double) * (NN ? NN : 1));
+    d.nat_on = (uint8_t *)dalloc(NN ? NN : 1);
+
+    CK(cudaMemcpyAsync(d.rep_of, rep_of.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d.chain, chain.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d.seq, seq.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d.atype, at.data(), N, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d.bflags, bfl.data(), sizeof(uint32_t) * N, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d.teth_r0, tr.data(), sizeof(double) * N, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d.ang_t0, ar.data(), sizeof(double) * N, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d.dih_p0, dr.data(), sizeof(double) * N, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d.nat_start, nat_start.data(), sizeof(int32_t) * (N + 1), cudaMemcpyHostToDevice, stream));
+    if (NN) {
+        CK(cudaMemcpyAsync(d.nat_j, nat_j.data(), sizeof(int32_t) * NN, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(d.nat_d, nat_d.data(), sizeof(double) * NN, cudaMemcpyHostToDevice, stream));
+    }
+    CK(cudaMemcpyAsync(d.rep, rd.data(), sizeof(RepDev) * R, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d.jump, jumps.data(), sizeof(uint64_t) * 64 * R, cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+
+    // term parameters
+    std::memset(&tp, 0, sizeof tp);
+    for (int k = 0; k < XMD_NUM_TERMS; ++k) tp.on[k] = p.on[k];
+    tp.dt = p.dt;
+    tp.gamma_factor = p.gamma_factor;
+    tp.tether_H1 = p.tether_H1; tp.tether_H2 = p.tether_H2;
+    tp.nat_ang_k = p.nat_ang_k; tp.cnd_CDA = p.cnd_CDA; tp.cnd_CDB = p.cnd_CDB; tp.snd_CDH = p.snd_CDH;
+    tp.go_depth = p.go_depth;
+    tp.pauli_r_excl = p.pauli_r_excl; tp.pauli_depth = p.pauli_depth;
+    if (p.on[XMD_TERM_CONST_ES]) {      // main.cpp:619-631
+        tp.es_Vf = 1.0 / (4.0 * M_PI * p.const_es_permittivity);
+        tp.es_sdi = 1.0 / p.const_es_screen_dist;
+        tp.es_rel = 0;
+    } else {                            // main.cpp:633-645
+        tp.es_Vf = 1.0 / (4.0 * M_PI * p.rel_es_factor);
+        tp.es_sdi = 1.0 / p.rel_es_screen_dist;
+        tp.es_rel = 1;
+    }
+    if (p.on[XMD_TERM_CONST_ES] && p.on[XMD_TERM_REL_ES])
+        throw std::invalid_argument("const ES and relative ES cannot both be enabled in this engine");
+    tp.qa_cycle = p.qa_phase_duration;
+    tp.qa_cycle_inv = 1.0 / p.qa_phase_duration;
+    tp.qa_factor = p.qa_breaking_factor * (double)powf(2.0f, -1.0f / 6.0f);   // main.cpp:719-723
+    tp.lj_bb_r_min = p.lj_bb_r_min; tp.lj_bb_depth = p.lj_bb_depth;
+    tp.lj_bs_r_min = p.lj_bs_r_min; tp.lj_bs_depth = p.lj_bs_depth;
+    tp.ss_sinking = p.ss_sinking;
+    if (p.on[XMD_TERM_QA]) throw std::invalid_argument("quasi-adiabatic contacts are not enabled in this build of the engine");
+
+    finalized = true;
+    for (int k = 0; k < R; ++k) upload_state(k);
+}
+
+void Engine::upload_state(int k) {
+    RepHost &r = reps[k];
+    int n = r.n, b = r.begin;
+    std::vector<double4_32a> pos(n);
+    for (int i = 0; i < n; ++i) {
+        double q = params.charge[r.atype[i]];
+        pos[i] = make_double4_32a(r.r[3 * i], r.r[3 * i + 1], r.r[3 * i + 2], q);
+    }
+    CK(cudaMemcpyAsync(d.pos[cur] + b, pos.data(), sizeof(double4_32a) * n, cudaMemcpyHostToDevice, stream));
+    // y1 = v*dt, y2..y5 = 0
+    std::vector<double> col(n);
+    for (int k2 = 0; k2 < 15; ++k2) {
+        for (int i = 0; i < n; ++i) col[i] = k2 < 3 ? r.v[3 * i + k2] * params.dt : 0.0;
+        CK(cudaMemcpyAsync(d.yh + (size_t)k2 * d.N + b, col.data(), sizeof(double) * n,
+                           cudaMemcpyHostToDevice, stream));
+    }
+    std::vector<uint64_t> st(n);
+    uint64_t s = r.seed;
+    for (int i = 0; i < n; ++i) {
+        st[i] = s;
+        for (int q = 0; q < 4; ++q) s = xs_step(s);
+    }
+    CK(cudaMemcpyAsync(d.rng + b, st.data(), sizeof(uint64_t) * n, cudaMemcpyHostToDevice, stream));
+    RepDev rd;
+    CK(cudaMemcpyAsync(&rd, d.rep + k, sizeof(RepDev), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    rd.t = 0.0;
+    rd.first = 1;
+    rd.maxdisp = 0;
+    CK(cudaMemcpyAsync(d.rep + k, &rd, sizeof(RepDev), cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+}
+
+void Engine::set_state(int rep, const double *r, const double *v) {
+    check_rep(reps, rep);
+    if (!r) throw std::invalid_argument("null positions");
+    RepHost &h = reps[rep];
+    h.r.assign(r, r + 3 * (size_t)h.n);
+    if (v) h.v.assign(v, v + 3 * (size_t)h.n);
+    else h.v.assign(3 * (size_t)h.n, 0.0);
+    for (double x : h.r) if (!std::isfinite(x)) throw std::invalid_argument("non-finite position");
+    h.have_state = true;
+    if (finalized) upload_state(rep);
+}
+
+void Engine::set_history(int rep, const double *y, double t, uint64_t rngs) {
+    check_rep(reps, rep);
+    if (!finalized) finalize();
+    RepHost &h = reps[rep];
+    int n = h.n, b = h.begin;
+    size_t n3 = 3 * (size_t)n;
+    std::vector<double4_32a> pos(n);
+    for (int i = 0; i < n; ++i)
+        pos[i] = make_double4_32a(y[3 * i], y[3 * i + 1], y[3 * i + 2], params.charge[h.atype[i]]);
+    CK(cudaMemcpyAsync(d.pos[cur] + b, pos.data(), sizeof(double4_32a) * n, cudaMemcpyHostToDevice, stream));
+    std::vector<double> col(n);
+    for (int ord = 1; ord < 6; ++ord)
+        for (int a = 0; a < 3; ++a) {
+            for (int i = 0; i < n; ++i) col[i] = y[ord * n3 + 3 * i + a];
+            CK(cudaMemcpyAsync(d.yh + (size_t)((ord - 1) * 3 + a) * d.N + b, col.data(), sizeof(double) * n,
+                               cudaMemcpyHostToDevice, stream));
+        }
+    std::vector<uint64_t> st(n);
+    uint64_t s = rngs;
+    for (int i = 0; i < n; ++i) {
+        st[i] = s;
+        for (int q = 0; q < 4; ++q) s = xs_step(s);
+    }
+    CK(cudaMemcpyAsync(d.rng + b, st.data(), sizeof(uint64_t) * n, cudaMemcpyHostToDevice, stream));
+    RepDev rd;
+    CK(cudaMemcpyAsync(&rd, d.rep + rep, sizeof(RepDev), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    rd.t = t;
+    rd.first = 1;
+    rd.maxdisp = 0;
+    CK(cudaMemcpyAsync(d.rep + rep, &rd, sizeof(RepDev), cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+}
+
+void Engine::get_state(int rep, double *r, double *v, double *t) {
+    check_rep(reps, rep);
+    if (!finalized) finalize();
+    const RepHost &h = reps[rep];
+    int n = h.n, b = h.begin;
+    std::vector<double4_32a> pos(n);
+    CK(cudaMemcpyAsync(pos.data(), d.pos[cur] + b, sizeof(double4_32a) * n, cudaMemcpyDeviceToHost, stream));
+    std::vector<double> y1(3 * (size_t)n);
+    for (int a = 0; a < 3; ++a)
+        CK(cudaMemcpyAsync(y1.data() + (size_t)a * n, d.yh + (size_t)a * d.N + b, sizeof(double) * n,
+                           cudaMemcpyDeviceToHost, stream));
+    RepDev rd;
+    CK(cudaMemcpyAsync(&rd, d.rep + rep, sizeof(RepDev), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    const double dt_inv = 1.0 / params.dt;
+    for (int i = 0; i < n; ++i) {
+        if (r) { r[3 * i] = pos[i].x; r[3 * i + 1] = pos[i].y; r[3 * i + 2] = pos[i].z; }
+        if (v) for (int a = 0; a < 3; ++a) v[3 * i + a] = y1[(size_t)a * n + i] * dt_inv;
+    }
+    if (t) *t = rd.t;
+}
+
+void Engine::get_history(int rep, double *y, double *t, uint64_t *rngs) {
+    check_rep(reps, rep);
+    if (!finalized) finalize();
+    const RepHost &h = reps[rep];
+    int n = h.n, b = h.begin;
+    size_t n3 = 3 * (size_t)n;
+    std::vector<double4_32a> pos(n);
+    CK(cudaMemcpyAsync(pos.data(), d.pos[cur] + b, sizeof(double4_32a) * n, cudaMemcpyDeviceToHost, stream));
+    std::vector<double> col(15 * (size_t)n);
+    for (int k = 0; k < 15; ++k)
+        CK(cudaMemcpyAsync(col.data() + (size_t)k * n, d.yh + (size_t)k * d.N + b, sizeof(double) * n,
+                           cudaMemcpyDeviceToHost, stream));
+    uint64_t s0 = 0;
+    CK(cudaMemcpyAsync(&s0, d.rng + b, sizeof(uint64_t), cudaMemcpyDeviceToHost, stream));
+    RepDev rd;
+    CK(cudaMemcpyAsync(&rd, d.rep + rep, sizeof(RepDev), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    if (y) {
+        for (int i = 0; i < n; ++i) { y[3 * i] = pos[i].x; y[3 * i + 1] = pos[i].y; y[3 * i + 2] = pos[i].z; }
+        for (int ord = 1; ord < 6; ++ord)
+            for (int a = 0; a < 3; ++a)
+                for (int i = 0; i < n; ++i)
+                    y[ord * n3 + 3 * i + a] = col[(size_t)((ord - 1) * 3 + a) * n + i];
+    }
+    if (t) *t = rd.t;
+    if (rngs) *rngs = s0;
+}
+
+void Engine::launch_rebuild() {
+    k_cells<<<d.R, CB, 0, stream>>>(d, cur);
+    k_nl_build<<<(d.N + 127) / 128, 128, 0, stream>>>(d, tp, cur);
+}
+
+void Engine::ensure_nl() {
+    k_nl_check<<<1, 1024, 0, stream>>>(d, 0, 0.0);
+    CK(cudaMemcpyAsync(h_any, d.any_rebuild, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    if (*h_any) launch_rebuild();
+}
+
+void Engine::check_status(const char *where) {
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, d.status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    CK(cudaGetLastError());
+    if (st & ST_CAPACITY)
+        throw std::length_error(std::string(where) + ": Verlet row capacity exceeded (raise `engine: nl capacity`)");
+    if (st & ST_NONFINITE) throw std::domain_error(std::string(where) + ": non-finite force");
+}
+
+void Engine::eval_forces(int rep, double *F, double *V) {
+    check_rep(reps, rep);
+    finalize();
+    ensure_nl();
+    CK(cudaMemsetAsync(d.Vrep, 0, sizeof(double) * XMD_NUM_TERMS * d.R, stream));
+    int nb = (d.N + FB - 1) / FB;
+    if (params.precision == XMD_PREC_MIXED) k_force<float, 0><<<nb, FB, 0, stream>>>(d, tp, cur);
+    else k_force<double, 0><<<nb, FB, 0, stream>>>(d, tp, cur);
+    const RepHost &h = reps[rep];
+    if (F) CK(cudaMemcpyAsync(F, d.F + 3 * (size_t)h.begin, sizeof(double) * 3 * h.n, cudaMemcpyDeviceToHost, stream));
+    if (V) CK(cudaMemcpyAsync(V, d.Vrep + (size_t)rep * XMD_NUM_TERMS, sizeof(double) * XMD_NUM_TERMS,
+                              cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    check_status("eval_forces");
+}
+
+void Engine::step(int nsteps) {
+    finalize();
+    if (!params.langevin_on) throw std::invalid_argument("langevin: enabled is false; nothing integrates");
+    ensure_nl();
+    int nb = (d.N + FB - 1) / FB;
+    for (int s = 0; s < nsteps; ++s) {
+        if (params.precision == XMD_PREC_MIXED) k_force<float, 1><<<nb, FB, 0, stream>>>(d, tp, cur);
+        else k_force<double, 1><<<nb, FB, 0, stream>>>(d, tp, cur);
+        cur ^= 1;
+        k_nl_check<<<1, 1024, 0, stream>>>(d, 1, params.dt);
+        CK(cudaMemcpyAsync(h_any, d.any_rebuild, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        if (*h_any) launch_rebuild();
+    }
+    check_status("step");
+}
+
+void Engine::observables(int rep, double *E, double *K, double *Rg, double *Q) {
+    check_rep(reps, rep);
+    double V[XMD_NUM_TERMS];
+    eval_forces(rep, nullptr, V);
+    const RepHost &h = reps[rep];
+    std::vector<double> r(3 * (size_t)h.n), v(3 * (size_t)h.n);
+    get_state(rep, r.data(), v.data(), nullptr);
+    double Vt = 0;
+    for (double x : V) Vt += x;
+    double K_ = 0;   // total_energy.cpp:4-11
+    for (int i = 0; i < h.n; ++i)
+        K_ += 0.5 * 1.0 * (v[3 * i] * v[3 * i] + v[3 * i + 1] * v[3 * i + 1] + v[3 * i + 2] * v[3 * i + 2]);
+    double cm[3] = {0, 0, 0};   // gyration.cpp:4-19
+    for (int i = 0; i < h.n; ++i) for (int a = 0; a < 3; ++a) cm[a] += r[3 * i + a];
+    for (int a = 0; a < 3; ++a) cm[a] /= h.n;
+    double g = 0;
+    for (int i = 0; i < h.n; ++i)
+        for (int a = 0; a < 3; ++a) g += (r[3 * i + a] - cm[a]) * (r[3 * i + a] - cm[a]);
+    double act = 0;   // report_structure.cpp:85
+    double thr = params.go_active_threshold * std::pow(2.0, -1.0 / 6.0);
+    for (size_t k = 0; k < h.nat_i1.size(); ++k) {
+        int a = h.nat_i1[k], b = h.nat_i2[k];
+        double dx = r[3 * a] - r[3 * b], dy = r[3 * a + 1] - r[3 * b + 1], dz = r[3 * a + 2] - r[3 * b + 2];
+        if (std::sqrt(dx * dx + dy * dy + dz * dz) < thr * h.nat_d[k]) act += 1;
+    }
+    if (E) *E = Vt + K_;
+    if (K) *K = K_;
+    if (Rg) *Rg = std::sqrt(g / h.n);
+    if (Q) *Q = h.nat_i1.empty() ? 0.0 : act / h.nat_i1.size();
+}
+
+int Engine::device_status() {
+    if (!finalized) return 0;
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, d.status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    return st;
+}
+
+void Engine::sync() { CK(cudaStreamSynchronize(stream)); }
+
+}  // namespace xmdg

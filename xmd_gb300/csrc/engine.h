@@ -1,0 +1,129 @@
+// engine.h - host-side state of one engine context.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/xmd_gpu.h"
+#include "types.h"
+
+namespace xmdg {
+
+// bead flags (bflags)
+enum : uint32_t {
+    BF_TETH = 1u,  // bond (i, i+1)
+    BF_ANG = 2u,   // angle (i-1, i, i+1)
+    BF_DIH = 4u,   // dihedral (i-1, i, i+1, i+2)
+    BF_PREV = 8u,  // i-1 is the previous bead of the same chain
+    BF_NEXT = 16u  // i+1 is the next bead of the same chain
+};
+
+// per-replica device record
+struct RepDev {
+    BoxD box;
+    double pad, req_r, noise_sd;
+    double es_min_inv, pauli_min_inv, qa_min_inv;
+    double t;
+    int begin, n;
+    int cell_off, cell_budget;
+    int per[3];
+    int dims[3];
+    double lo[3], cs[3];
+    int first, rebuild;
+    unsigned long long maxdisp;
+    unsigned long long rebuilds;
+};
+
+// everything a kernel needs, passed by value
+struct Dev {
+    int N, R, nl_cap;
+    double4_32a *pos[2];        // x, y, z, charge; double-buffered
+    double *yh;             // [15][N]: y1x y1y y1z y2x ... y5z
+    double4_32a *orig;          // positions at the last list rebuild
+    double *F;              // [3N] force output of eval
+    double *Vrep;           // [R][XMD_NUM_TERMS] energies of eval
+    int32_t *rep_of;        // bead -> replica
+    uint32_t *bflags;
+    int32_t *chain, *seq;
+    uint8_t *atype;
+    double *teth_r0, *ang_t0, *dih_p0;
+    int32_t *nat_start, *nat_j;
+    double *nat_d;
+    uint8_t *nat_on;
+    int32_t *nl_row, *nl_cnt;
+    int32_t *cell_cnt, *cell_start, *cell_fill, *cell_items, *bead_cell;
+    uint64_t *rng;          // per-bead generator state
+    uint64_t *jump;         // [R][64] GF(2) jump matrices (4 N_r draws)
+    RepDev *rep;
+    int *any_rebuild;
+    int *status;            // device error word
+};
+
+struct RepHost {
+    int n = 0;
+    std::vector<int32_t> chain, seq;
+    std::vector<uint8_t> atype;
+    double cell[3] = {0, 0, 0};
+    double temperature = 0;
+    uint64_t seed = 0;
+    std::vector<double> teth_r0, ang_t0, dih_p0;   // per centre, NaN = absent
+    std::vector<int32_t> nat_i1, nat_i2;
+    std::vector<double> nat_d;
+    std::vector<double> r, v;                      // initial state
+    bool have_state = false;
+    int begin = 0;
+};
+
+class Engine {
+public:
+    explicit Engine(const xmd_params &p);
+    ~Engine();
+
+    xmd_params params;
+    std::vector<RepHost> reps;
+    bool finalized = false;
+    int nl_cap = 64;
+
+    int add_replica(int n, const int32_t *chain, const int32_t *seq, const uint8_t *atype,
+                    const double cell[3], double temperature, uint64_t seed);
+    void set_tethers(int rep, int n, const int32_t *i1, const int32_t *i2, const double *d);
+    void set_angles(int rep, int n, const int32_t *i1, const int32_t *i2, const int32_t *i3,
+                    const double *th);
+    void set_dihedrals(int rep, int n, const int32_t *i1, const int32_t *i2, const int32_t *i3,
+                       const int32_t *i4, const double *ph);
+    void set_native(int rep, int n, const int32_t *i1, const int32_t *i2, const double *d);
+    void set_state(int rep, const double *r, const double *v);
+    void set_history(int rep, const double *y, double t, uint64_t rng);
+    void get_state(int rep, double *r, double *v, double *t);
+    void get_history(int rep, double *y, double *t, uint64_t *rng);
+    void eval_forces(int rep, double *F, double *V);
+    void step(int nsteps);
+    void observables(int rep, double *E, double *K, double *Rg, double *Q);
+    int device_status();
+    void sync();
+
+private:
+    Dev d{};
+    int cur = 0;                 // which pos buffer is current
+    cudaStream_t stream = nullptr;
+    std::vector<void *> allocs;
+    int *h_any = nullptr;        // pinned
+    TermP tp{};
+    std::vector<double> max_cutoff_r;
+
+    void *dalloc(size_t bytes);
+    void finalize();
+    void release();
+    void derive_rep(int r, RepDev &rd);
+    void ensure_nl();
+    void launch_rebuild();
+    void check_status(const char *where);
+    void upload_state(int rep);
+};
+
+std::string &last_error();
+uint64_t rng_jump(uint64_t state, uint64_t n_draws);
+
+}  // namespace xmdg

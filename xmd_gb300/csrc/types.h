@@ -1,0 +1,29 @@
+// types.h - plain records shared by host code and kernels.
+#pragma once
+#include <cstdint>
+
+#include "../../include/xmd_gpu.h"
+
+namespace xmdg {
+
+// orthorhombic box (box.h:6-59); cell 0 = open along that axis
+struct BoxD {
+    double cell[3], cell_inv[3];
+};
+
+// ---- parameters shared by all terms (kernel argument, by value) --------------
+struct TermP {
+    int on[XMD_NUM_TERMS];
+    double dt, gamma_factor;
+    double tether_H1, tether_H2;
+    double nat_ang_k, cnd_CDA, cnd_CDB, snd_CDH;
+    double go_depth;
+    double pauli_r_excl, pauli_depth;
+    double es_Vf, es_sdi;        // const ES (or relative ES) V_factor, 1/screening distance
+    int es_rel;                  // 1: relative ES force law
+    double qa_cycle, qa_cycle_inv, qa_factor;
+    double lj_bb_r_min, lj_bb_depth, lj_bs_r_min, lj_bs_depth;
+    int ss_sinking;
+};
+
+}  // namespace xmdg

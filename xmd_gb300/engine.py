@@ -1,0 +1,114 @@
+"""Host-side handle on an engine context (thin wrapper over the C ABI).
+
+Mirrors the way the reference drives its hot path (src/freeform/main.cpp):
+parameters come from YAML, each system's topology and native structure are
+handed over once, and the step loop runs on the device.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .abi import check, dptr, iptr, u8ptr
+
+
+class Engine:
+    def __init__(self, yaml_text: str = ""):
+        self.lib = abi.load()
+        h = C.c_void_p()
+        check(self.lib.xmd_gpu_create(yaml_text.encode(), C.byref(h)))
+        self.h = h
+        self.sizes: list[int] = []
+
+    def close(self):
+        if self.h:
+            self.lib.xmd_gpu_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def params(self) -> abi.Params:
+        p = abi.Params()
+        check(self.lib.xmd_gpu_get_params(self.h, C.byref(p)))
+        return p
+
+    def enable_term(self, term: int, on: bool = True):
+        check(self.lib.xmd_gpu_enable_term(self.h, term, int(on)))
+
+    def add_system(self, s, temperature: float | None = None, seed: int | None = None) -> int:
+        """Add a synth.System (or anything with the same fields) as a replica."""
+        chain = np.ascontiguousarray(s.chain, dtype=np.int32)
+        seq = np.ascontiguousarray(s.seq, dtype=np.int32)
+        at = np.ascontiguousarray(s.atype, dtype=np.uint8)
+        cell = np.ascontiguousarray(s.cell, dtype=np.float64)
+        rid = C.c_int32()
+        T = s.temperature if temperature is None else temperature
+        sd = s.seed if seed is None else seed
+        check(self.lib.xmd_gpu_add_replica(self.h, s.n, iptr(chain), iptr(seq), u8ptr(at), dptr(cell),
+                                           float(T), int(sd) & (2**64 - 1), C.byref(rid)))
+        r = rid.value
+        t1, t2, td = (np.ascontiguousarray(x) for x in s.tethers)
+        check(self.lib.xmd_gpu_set_tethers(self.h, r, len(t1), iptr(t1), iptr(t2), dptr(td)))
+        a1, a2, a3, at0 = (np.ascontiguousarray(x) for x in s.angles)
+        check(self.lib.xmd_gpu_set_angles(self.h, r, len(a1), iptr(a1), iptr(a2), iptr(a3), dptr(at0)))
+        d1, d2, d3, d4, dp = (np.ascontiguousarray(x) for x in s.dihedrals)
+        check(self.lib.xmd_gpu_set_dihedrals(self.h, r, len(d1), iptr(d1), iptr(d2), iptr(d3), iptr(d4),
+                                             dptr(dp)))
+        n1, n2, nd = (np.ascontiguousarray(x) for x in s.natives)
+        check(self.lib.xmd_gpu_set_native_contacts(self.h, r, len(n1), iptr(n1), iptr(n2), dptr(nd)))
+        rr = np.ascontiguousarray(s.r, dtype=np.float64).reshape(-1)
+        check(self.lib.xmd_gpu_set_state(self.h, r, dptr(rr), None))
+        self.sizes.append(s.n)
+        return r
+
+    def eval_forces(self, rep: int = 0):
+        n = self.sizes[rep]
+        F = np.zeros(3 * n)
+        V = np.zeros(abi.NUM_TERMS)
+        check(self.lib.xmd_gpu_eval_forces(self.h, rep, dptr(F), dptr(V)))
+        return F.reshape(n, 3), V
+
+    def step(self, nsteps: int):
+        check(self.lib.xmd_gpu_step(self.h, int(nsteps)))
+
+    def get_state(self, rep: int = 0):
+        n = self.sizes[rep]
+        r, v, t = np.zeros(3 * n), np.zeros(3 * n), C.c_double()
+        check(self.lib.xmd_gpu_get_state(self.h, rep, dptr(r), dptr(v), C.byref(t)))
+        return r.reshape(n, 3), v.reshape(n, 3), t.value
+
+    def get_history(self, rep: int = 0):
+        n = self.sizes[rep]
+        y, t, st = np.zeros(18 * n), C.c_double(), C.c_uint64()
+        check(self.lib.xmd_gpu_get_history(self.h, rep, dptr(y), C.byref(t), C.byref(st)))
+        return y.reshape(6, n, 3), t.value, st.value
+
+    def set_history(self, rep: int, y: np.ndarray, t: float, rng_state: int):
+        y = np.ascontiguousarray(y, dtype=np.float64).reshape(-1)
+        check(self.lib.xmd_gpu_set_history(self.h, rep, dptr(y), float(t), int(rng_state)))
+
+    def observables(self, rep: int = 0):
+        E, K, Rg, Q = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+        check(self.lib.xmd_gpu_observables(self.h, rep, C.byref(E), C.byref(K), C.byref(Rg), C.byref(Q)))
+        return {"E": E.value, "K": K.value, "Rg": Rg.value, "Q": Q.value}
+
+    def device_status(self) -> int:
+        s = C.c_int32()
+        check(self.lib.xmd_gpu_device_status(self.h, C.byref(s)))
+        return s.value
+
+    def synchronize(self):
+        check(self.lib.xmd_gpu_synchronize(self.h))

@@ -1,0 +1,301 @@
+"""Seeded synthetic systems with the shapes of the benchmark configurations.
+
+There is no dataset behind these configurations: chains are generated here.
+Initial conformations restate the reference's chain generator
+(model::morph_into_saw, src/model/model.cpp:101-147: random start in a cube of
+side cbrt(n / density), direction on the sphere, each step turned by a
+spread angle in [-pi/12, pi/12] about an axis perpendicular to the direction
+and by an angle in [-pi, pi] about the direction), with a light overlap
+rejection so that starting structures are self-avoiding.  Native structures
+(contact maps with r < 7.5 A and |i-j| >= 3, native angles and dihedrals) come
+from a second, compact random walk confined to a sphere.  numpy's PCG64 seeds
+every draw, so a (config, seed) pair always yields the same system.
+
+All lengths returned are in the engine's internal unit (1 = 5 A).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .abi import AA
+
+ANGSTROM = 0.2  # include/xmd/utils/units.h:15
+CHARGED_POS = [AA.index("ARG"), AA.index("LYS")]
+CHARGED_NEG = [AA.index("ASP"), AA.index("GLU")]
+NEUTRAL = [k for k in range(20) if k not in CHARGED_POS + CHARGED_NEG]
+
+
+@dataclass
+class System:
+    """One replica: topology, native structure and initial state."""
+    n: int
+    chain: np.ndarray            # int32[n]
+    seq: np.ndarray              # int32[n]
+    atype: np.ndarray            # uint8[n]
+    cell: np.ndarray             # float64[3], 0 = open
+    r: np.ndarray                # float64[n, 3] initial positions
+    tethers: tuple               # (i1, i2, nat_dist)
+    angles: tuple                # (i1, i2, i3, theta0)
+    dihedrals: tuple             # (i1, i2, i3, i4, phi0)
+    natives: tuple               # (i1, i2, nat_dist)
+    temperature: float = 0.0
+    seed: int = 0
+    meta: dict = field(default_factory=dict)
+
+
+def _unit(v):
+    return v / np.linalg.norm(v)
+
+
+def _perp(v):
+    # perp_v: model.cpp:93-99
+    p1 = np.cross(v, [1.0, 0.0, 0.0])
+    p2 = np.cross(v, [0.0, 1.0, 0.0])
+    p = p1 if np.linalg.norm(p1) > np.linalg.norm(p2) else p2
+    return _unit(p)
+
+
+def _rot(v, axis, ang):
+    # Rodrigues rotation of v about the unit axis
+    c, s = math.cos(ang), math.sin(ang)
+    return v * c + np.cross(axis, v) * s + axis * np.dot(axis, v) * (1.0 - c)
+
+
+def _sphere(rng):
+    v = rng.normal(size=3)
+    return _unit(v)
+
+
+def saw_chain(rng, n, bond, start, min_sep=4.0 * ANGSTROM, tries=20, others=None):
+    """A persistent random walk as in morph_into_saw with overlap rejection."""
+    max_spread, max_around = math.pi / 12.0, math.pi
+    pos = np.empty((n, 3))
+    pos[0] = start
+    d = _sphere(rng)
+    for k in range(1, n):
+        best, best_d = None, -1.0
+        for _ in range(tries):
+            sp = rng.uniform(-max_spread, max_spread)
+            ar = rng.uniform(-max_around, max_around)
+            nd = _unit(_rot(_rot(d, _perp(d), sp), d, ar))
+            cand = pos[k - 1] + bond * nd
+            if k >= 3:
+                dmin = np.min(np.linalg.norm(pos[:k - 2] - cand, axis=1))
+            else:
+                dmin = np.inf
+            if others is not None and len(others):
+                dmin = min(dmin, np.min(np.linalg.norm(others - cand, axis=1)))
+            if dmin >= min_sep:
+                best = (cand, nd)
+                break
+            if dmin > best_d:
+                best_d, best = dmin, (cand, nd)
+        pos[k], d = best
+    return pos
+
+
+def compact_walk(rng, n, bond, density=1.0 / 120.0, min_sep=4.2 * ANGSTROM, tries=60):
+    """A random walk confined to a sphere holding n beads at `density` (per A^3),
+    with overlap rejection: the native conformation of one chain."""
+    radius = (3.0 * n / (4.0 * math.pi * density)) ** (1.0 / 3.0) * ANGSTROM
+    radius = max(radius, 2.0 * bond)
+    pos = np.zeros((n, 3))
+    for k in range(1, n):
+        best, best_score = None, -np.inf
+        for _ in range(tries):
+            cand = pos[k - 1] + bond * _sphere(rng)
+            dmin = np.min(np.linalg.norm(pos[:k - 1] - cand, axis=1)) if k >= 2 else np.inf
+            out = max(0.0, np.linalg.norm(cand) - radius)
+            score = min(dmin - min_sep, 0.0) - out
+            if score >= 0.0:
+                best = cand
+                break
+            if score > best_score:
+                best_score, best = score, cand
+        pos[k] = best
+    return pos
+
+
+def bonded_natives(pos):
+    """Native angles and dihedrals of one chain, with the force terms'
+    conventions (angle/native.cpp:20-30, dihedral/complex_native.cpp:20-28)."""
+    n = len(pos)
+    th = []
+    for c in range(1, n - 1):
+        r12, r23 = pos[c] - pos[c - 1], pos[c + 1] - pos[c]
+        ct = -np.dot(r12, r23) / (np.linalg.norm(r12) * np.linalg.norm(r23))
+        th.append(math.acos(max(-1.0, min(1.0, ct))))
+    ph = []
+    for c in range(1, n - 2):
+        r12, r23, r34 = pos[c] - pos[c - 1], pos[c + 1] - pos[c], pos[c + 2] - pos[c + 1]
+        x1, x2 = np.cross(r12, r23), np.cross(r23, r34)
+        cp = np.dot(x1, x2) / (np.linalg.norm(x1) * np.linalg.norm(x2))
+        p = math.acos(max(-1.0, min(1.0, cp)))
+        if np.dot(x1, r34) < 0:
+            p = -p
+        ph.append(p)
+    return np.array(th), np.array(ph)
+
+
+def native_map(pos, cutoff=7.5 * ANGSTROM, min_sep=3):
+    n = len(pos)
+    d = np.linalg.norm(pos[:, None, :] - pos[None, :, :], axis=2)
+    i1, i2 = np.nonzero(np.triu(d < cutoff, k=min_sep))
+    return i1.astype(np.int32), i2.astype(np.int32), d[i1, i2].astype(np.float64)
+
+
+def _types(rng, n, mode):
+    if mode == "uniform20":
+        return rng.integers(0, 20, size=n).astype(np.uint8)
+    # +-1 charge with probability 0.1 each, realised through residue types
+    u = rng.random(n)
+    t = np.empty(n, dtype=np.uint8)
+    pos_m, neg_m = u < 0.1, (u >= 0.1) & (u < 0.2)
+    t[pos_m] = rng.choice(CHARGED_POS, size=pos_m.sum())
+    t[neg_m] = rng.choice(CHARGED_NEG, size=neg_m.sum())
+    rest = ~(pos_m | neg_m)
+    t[rest] = rng.choice(NEUTRAL, size=rest.sum())
+    return t
+
+
+def make_system(chain_lengths, seed, box=None, density=1e-3, types="charged10",
+                bond=3.8 * ANGSTROM, native=True, temperature=0.0, rng_seed=None):
+    """Build one replica.  box: edge in internal units (periodic cube) or None
+    for open boundaries; density (per A^3) sizes the starting cube."""
+    rng = np.random.default_rng(seed)
+    lens = [int(x) for x in chain_lengths]
+    n = sum(lens)
+    chain = np.concatenate([np.full(L, c, dtype=np.int32) for c, L in enumerate(lens)])
+    seq = np.concatenate([np.arange(L, dtype=np.int32) for L in lens])
+    atype = _types(rng, n, types)
+    if box is not None:
+        a = box
+    else:
+        a = (n / density) ** (1.0 / 3.0) * ANGSTROM   # morph_into_saw cell_a
+    r = np.empty((n, 3))
+    tet_i1, tet_i2, tet_d = [], [], []
+    ang = ([], [], [], [])
+    dih = ([], [], [], [], [])
+    nat = ([], [], [])
+    off = 0
+    for c, L in enumerate(lens):
+        start = rng.uniform(-a / 2.0, a / 2.0, size=3)
+        others = r[max(0, off - 2000):off] if off else None
+        r[off:off + L] = saw_chain(rng, L, bond, start, others=others)
+        if L >= 2:
+            tet_i1 += list(range(off, off + L - 1))
+            tet_i2 += list(range(off + 1, off + L))
+            tet_d += [bond] * (L - 1)
+        if native and L >= 3:
+            npos = compact_walk(rng, L, bond)
+            th, ph = bonded_natives(npos)
+            for k, t in enumerate(th):
+                ang[0].append(off + k); ang[1].append(off + k + 1); ang[2].append(off + k + 2); ang[3].append(t)
+            for k, p in enumerate(ph):
+                dih[0].append(off + k); dih[1].append(off + k + 1); dih[2].append(off + k + 2)
+                dih[3].append(off + k + 3); dih[4].append(p)
+            i1, i2, dd = native_map(npos)
+            nat[0].extend((i1 + off).tolist()); nat[1].extend((i2 + off).tolist()); nat[2].extend(dd.tolist())
+        off += L
+    cell = np.array([box, box, box], dtype=np.float64) if box is not None else np.zeros(3)
+    as32 = lambda x: np.asarray(x, dtype=np.int32)
+    asf = lambda x: np.asarray(x, dtype=np.float64)
+    return System(
+        n=n, chain=chain, seq=seq, atype=atype, cell=cell, r=r,
+        tethers=(as32(tet_i1), as32(tet_i2), asf(tet_d)),
+        angles=(as32(ang[0]), as32(ang[1]), as32(ang[2]), asf(ang[3])),
+        dihedrals=(as32(dih[0]), as32(dih[1]), as32(dih[2]), as32(dih[3]), asf(dih[4])),
+        natives=(as32(nat[0]), as32(nat[1]), asf(nat[2])),
+        temperature=temperature, seed=int(rng_seed if rng_seed is not None else seed * 7919 + 17),
+        meta={"chains": lens},
+    )
+
+
+# ---- the benchmark configurations ------------------------------------------------
+
+YAML_COMMON = """
+langevin:
+  enabled: true
+  gamma factor: 2.0 1/tau
+  temperature: 0.35 eps/kB
+integrator:
+  dt: 5e-3 tau
+tether forces:
+  enabled: true
+native angles:
+  enabled: true
+complex native dihedrals:
+  enabled: true
+native contacts:
+  enabled: true
+  lj depth: 1 eps
+Pauli exclusion:
+  enabled: true
+  r_excl: 4.0 A
+"""
+
+
+def yaml_for(config: str, precision: str = "fp64") -> str:
+    """YAML overrides of a benchmark configuration (keys of defaults.yml)."""
+    if config == "c1":   # 100 beads, no box, Go + Pauli + bonded, NL 18 A + 2 A skin
+        extra = """
+const ES:
+  enabled: false
+quasi-adiabatic potential:
+  enabled: false
+neighbor list:
+  cutoff: 18 A
+  skin: 2 A
+"""
+    elif config in ("c2", "c4", "c5"):   # + Debye-Hueckel, kappa^-1 = 10 A, eps_r = 80
+        extra = """
+const ES:
+  enabled: true
+  screening distance: 10.0 A
+  permittivity: 80.0 eps_0
+quasi-adiabatic potential:
+  enabled: false
+"""
+    elif config == "c3":   # Go + DH + quasi-adiabatic
+        extra = """
+const ES:
+  enabled: true
+  screening distance: 10.0 A
+  permittivity: 80.0 eps_0
+quasi-adiabatic potential:
+  enabled: true
+"""
+    else:
+        raise ValueError(config)
+    return YAML_COMMON + extra + f"engine:\n  precision: {precision}\n"
+
+
+def config_c1(seed=1):
+    return make_system([100], seed, box=None, types="charged10", temperature=0.35)
+
+
+def config_c2(seed=2, chains=16, length=500):
+    return make_system([length] * chains, seed, box=300.0 * ANGSTROM, types="charged10", temperature=0.35)
+
+
+def config_c3(seed=3, chains=512, length=60):
+    n = chains * length
+    box = (n / 1e-3) ** (1.0 / 3.0) * ANGSTROM
+    return make_system([length] * chains, seed, box=box, types="uniform20", temperature=0.35)
+
+
+def c4_lengths(seed=4, count=256, lo=50, hi=800):
+    rng = np.random.default_rng(seed)
+    return np.floor(np.exp(rng.uniform(math.log(lo), math.log(hi), size=count))).astype(int)
+
+
+def config_c4(seed=4, count=256):
+    lens = c4_lengths(seed, count)
+    rng = np.random.default_rng(seed + 1000)
+    temps = rng.uniform(0.3, 0.6, size=count)
+    return [make_system([int(L)], seed * 100003 + k, box=None, types="charged10",
+                        temperature=float(temps[k]), rng_seed=seed * 7 + k * 131)
+            for k, L in enumerate(lens)]
