@@ -1,0 +1,431 @@
+#!/usr/bin/env python3
+"""Headline benchmark: batched mixed-precision MD steps on one GB300.
+
+Workload (config 4 of the benchmark set): 256 independent single-chain
+systems, lengths log-uniform in [50, 800] beads, Go native contacts +
+Debye-Hueckel + Pauli + tether/angle/dihedral terms, per-replica temperature
+uniform in [0.3, 0.6], all packed into one engine context.  A bench "step" is
+--md-steps Langevin predictor-corrector steps over every replica (one chunk
+of graph-captured device work); L2 is flushed (256 MiB device write) before
+each timed step and is excluded from the timing.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
+
+One JSON line on rank 0.  --impl reference times the CPU implementation of
+the same path (the C restatement of the reference's kernels, all host
+threads, one thread per replica group) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "bead-steps/s mixed+batched vs plain FP64 at ≤1e-5 force err; p99 req latency"
+L2_FLUSH_BYTES = 256 << 20
+
+
+# ---------------------------------------------------------------- helpers --
+def cudart():
+    """libcudart as already mapped into this process by the engine library."""
+    from xmd_gb300 import abi
+    abi.load()
+    path = None
+    with open("/proc/self/maps") as f:
+        for line in f:
+            if "libcudart.so" in line:
+                path = line.split()[-1]
+                break
+    lib = C.CDLL(path or "libcudart.so")
+    return lib
+
+
+class Events:
+    def __init__(self, rt, stream):
+        self.rt, self.stream = rt, stream
+
+    def new(self):
+        e = C.c_void_p()
+        assert self.rt.cudaEventCreate(C.byref(e)) == 0
+        return e
+
+    def record(self, e):
+        assert self.rt.cudaEventRecord(e, self.stream) == 0
+
+    def ms(self, a, b):
+        self.rt.cudaEventSynchronize(b)
+        v = C.c_float()
+        assert self.rt.cudaEventElapsedTime(C.byref(v), a, b) == 0
+        return v.value
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """Per-launch DRAM traffic of the dominant kernel from the committed ncu
+    summary (line `traffic_bytes_per_launch: <int>`), or None."""
+    p = ROOT / "profiles" / "k_force_mixed_c4.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)),
+            int(os.environ.get("WORLD_SIZE", 1)))
+
+
+def make_workload(rank: int, workers: int):
+    from xmd_gb300 import synth
+    return synth.config_c4(seed=4 + 1000 * rank, workers=workers)
+
+
+def pack_history(eng, nrep):
+    hs = [eng.get_history(r)[0] for r in range(nrep)]     # each [6, n, 3]
+    return np.ascontiguousarray(np.concatenate(hs, axis=1).reshape(6, -1))
+
+
+# ------------------------------------------------------------ engine arm --
+def run_engine(args, rank, local, world):
+    from xmd_gb300 import Engine, abi, synth
+    dev = local
+    systems = make_workload(rank, workers=min(16, os.cpu_count() or 1))
+    nbeads = sum(s.n for s in systems)
+    y_mixed = synth.yaml_for("c4", "mixed") + f"  device: {dev}\n"
+    y_fp64 = synth.yaml_for("c4", "fp64") + f"  device: {dev}\n"
+    eng = Engine(y_mixed)
+    for s in systems:
+        eng.add_system(s)
+    rt = cudart()
+    rt.cudaSetDevice(dev)
+    stream = C.c_void_p()
+    abi.check(eng.lib.xmd_gpu_get_stream(eng.h, C.byref(stream)))
+    ev = Events(rt, stream)
+    flush = C.c_void_p()
+    assert rt.cudaMalloc(C.byref(flush), C.c_size_t(L2_FLUSH_BYTES)) == 0
+
+    def flush_l2():
+        rt.cudaMemsetAsync(flush, 1, C.c_size_t(L2_FLUSH_BYTES), stream)
+
+    def stats():
+        out = np.zeros(abi_n_stats(), dtype=np.int64)
+        abi.check(eng.lib.xmd_gpu_stats(eng.h, out.ctypes.data_as(C.POINTER(C.c_int64))))
+        return out
+
+    def abi_n_stats():
+        return 8
+
+    def barrier():
+        eng.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    md = args.md_steps
+    # warm-up (also builds the graphs and the first lists)
+    for _ in range(args.warmup):
+        eng.step(md)
+    barrier()
+    s0 = stats()
+    clocks = Clocks(dev)
+    clocks.start()
+    e0, e1 = ev.new(), ev.new()
+    t_ms = 0.0
+    for _ in range(args.steps):
+        flush_l2()
+        ev.record(e0)
+        eng.step(md)
+        ev.record(e1)
+        t_ms += ev.ms(e0, e1)
+    barrier()
+    clk = clocks.stop()
+    s1 = stats()
+    launches = int(s1[5] - s0[5])
+    t_max = t_ms
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        tt = torch.tensor([t_ms], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    value = world * nbeads * md * args.steps / (t_max / 1e3)
+
+    # dominant kernel: force+integrate, timed with events around each launch
+    abi.check(eng.lib.xmd_gpu_set_kernel_timing(eng.h, 1))
+    eng.step(md)
+    fms, nf, rms, nr = C.c_double(), C.c_int64(), C.c_double(), C.c_int64()
+    abi.check(eng.lib.xmd_gpu_kernel_times(eng.h, C.byref(fms), C.byref(nf), C.byref(rms), C.byref(nr)))
+    abi.check(eng.lib.xmd_gpu_set_kernel_timing(eng.h, 0))
+    force_ms = fms.value / max(1, nf.value)
+    st = stats()
+    P = st[2] / 2.0          # unique pairs kept by the pair terms
+    Cg = st[3] / 2.0         # active Go contacts
+    alg_bytes = 325.0 * nbeads + 4.0 * P + 12.0 * Cg     # mixed, per MD step (Q = 0)
+    peak, peak_kind = peaks()
+    achieved = alg_bytes / (force_ms / 1e3) / 1e9
+    traffic = profile_traffic()
+
+    # end-to-end through the C ABI with pinned host buffers: every bench step
+    # uploads the packed history of all replicas, runs md steps, reads back
+    # all positions
+    nrep = len(systems)
+    yh = pack_history(eng, nrep)
+    hbuf = C.c_void_p()
+    assert rt.cudaHostAlloc(C.byref(hbuf), C.c_size_t(yh.nbytes + 24 * nbeads), 0) == 0
+    hy = np.ctypeslib.as_array((C.c_double * yh.size).from_address(hbuf.value))
+    hy[:] = yh.reshape(-1)
+    hr = np.ctypeslib.as_array((C.c_double * (3 * nbeads)).from_address(hbuf.value + yh.nbytes))
+    e2e_steps = max(2, args.steps // 2)
+    pd = C.POINTER(C.c_double)
+    for _ in range(1):
+        abi.check(eng.lib.xmd_gpu_upload_history_all(eng.h, hy.ctypes.data_as(pd)))
+        eng.step(md)
+        abi.check(eng.lib.xmd_gpu_download_positions_all(eng.h, hr.ctypes.data_as(pd)))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        abi.check(eng.lib.xmd_gpu_upload_history_all(eng.h, hy.ctypes.data_as(pd)))
+        eng.step(md)
+        abi.check(eng.lib.xmd_gpu_download_positions_all(eng.h, hr.ctypes.data_as(pd)))
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = world * nbeads * md * e2e_steps / e2e_s
+
+    # plain FP64 on the same replicas (same protocol), and the mixed force error
+    eng64 = Engine(y_fp64)
+    for s in systems:
+        eng64.add_system(s)
+    for _ in range(args.warmup):
+        eng64.step(md)
+    eng64.synchronize()
+    abi.check(eng64.lib.xmd_gpu_get_stream(eng64.h, C.byref(stream)))
+    ev64 = Events(rt, stream)
+    t64 = 0.0
+    k64 = max(2, args.steps // 2)
+    for _ in range(k64):
+        rt.cudaMemsetAsync(flush, 1, C.c_size_t(L2_FLUSH_BYTES), stream)
+        ev64.record(e0)
+        eng64.step(md)
+        ev64.record(e1)
+        t64 += ev64.ms(e0, e1)
+    value64 = nbeads * md * k64 / (t64 / 1e3)
+    # force error of the mixed path on identical states (fresh engines at t=0)
+    errs = []
+    with Engine(y_mixed) as em, Engine(y_fp64) as ed:
+        for s in systems[:16]:
+            em.add_system(s)
+            ed.add_system(s)
+        for r in range(16):
+            Fm, _ = em.eval_forces(r)
+            Fd, _ = ed.eval_forces(r)
+            errs.append(float(np.abs(Fm - Fd).max() / max(np.abs(Fd).max(), 1e-300)))
+    eng64.close()
+
+    cpu = cpu_baseline(systems, sample_steps=args.cpu_sample_steps) if rank == 0 else None
+    rt.cudaFree(flush)
+    rt.cudaFreeHost(hbuf)
+    eng.close()
+    if rank != 0:
+        return
+    out = {
+        "metric": METRIC, "value": value, "unit": "bead-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {
+            "workload": f"256 uneven single-chain replicas (log-uniform 50-800 beads, {nbeads} beads), "
+                        "Go+Debye-Hueckel+Pauli+tether/angle/dihedral, per-replica T in [0.3,0.6], "
+                        "mixed precision (FP32 forces, FP64 accumulate/integrate), one context",
+            "md_steps_per_step": md, "beads_per_gpu": nbeads, "replicas_per_gpu": nrep,
+            "l2": "256 MiB device write before each timed step (not timed)",
+            "plain_fp64_value": value64, "mixed_over_fp64": value / world / value64,
+            "mixed_force_rel_err_max": max(errs), "graph_steps_per_launch": 16,
+            "p99_req_latency_ms": None,
+        },
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "k_force<float,1> (force+integrate)", "kernel_ms": force_ms,
+                     "alg_bytes_per_launch": alg_bytes, "peak_source": peak_kind},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "bead-steps/s", "h2d_bytes_per_step": int(yh.nbytes),
+                "d2h_bytes_per_step": int(24 * nbeads)},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    print(json.dumps(out), flush=True)
+
+
+# ------------------------------------------------------------- CPU arms --
+def _cpu_run(systems, steps, threads, warm=0):
+    """All replicas on the CPU restatement, replicas spread over `threads`
+    host threads (ctypes releases the GIL during each call)."""
+    from oracle.pyoracle import Oracle
+    from xmd_gb300 import abi, synth
+    p = abi.parse_params(synth.yaml_for("c4", "fp64"))
+    orcs = [Oracle(p, s, "port") for s in systems]
+    order = sorted(range(len(orcs)), key=lambda k: -systems[k].n)
+    groups = [[] for _ in range(threads)]
+    load = [0] * threads
+    for k in order:   # longest-first greedy balance
+        g = int(np.argmin(load))
+        groups[g].append(k)
+        load[g] += systems[k].n
+
+    def work(g, n):
+        for k in groups[g]:
+            orcs[k].step(n)
+
+    def run(n):
+        ts = [threading.Thread(target=work, args=(g, n)) for g in range(threads)]
+        t0 = time.perf_counter()
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+        return time.perf_counter() - t0
+
+    if warm:
+        run(warm)
+    return orcs, run
+
+
+def cpu_baseline(systems, sample_steps=200):
+    threads = os.cpu_count() or 1
+    nb = sum(s.n for s in systems)
+    _, run = _cpu_run(systems, sample_steps, threads, warm=1)
+    dt = run(sample_steps)
+    return {"value": nb * sample_steps / dt, "unit": "bead-steps/s", "cores": threads, "kind": "port",
+            "sample": f"all {len(systems)} replicas x {sample_steps} steps ({nb} beads), "
+                      f"{dt:.1f} s wall on {threads} host threads"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    systems = make_workload(0, workers=min(16, os.cpu_count() or 1))
+    nb = sum(s.n for s in systems)
+    threads = os.cpu_count() or 1
+    md = args.md_steps_ref
+    _, run = _cpu_run(systems, md, threads)
+    for _ in range(args.warmup):
+        run(md)
+    t = 0.0
+    for _ in range(args.steps):
+        t += run(md)
+    value = nb * md * args.steps / t
+    out = {
+        "metric": METRIC, "value": value, "unit": "bead-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": {"workload": f"256 uneven single-chain replicas (log-uniform 50-800 beads, {nb} beads), "
+                               "Go+Debye-Hueckel+Pauli+tether/angle/dihedral, per-replica T in [0.3,0.6]",
+                   "md_steps_per_step": md,
+                   "implementation": "C restatement of the reference's FP64 kernels (bit-exact to them), "
+                                     "one host thread per replica group"},
+        "cpu_baseline": {"value": value, "unit": "bead-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"all {len(systems)} replicas x {md} steps per bench step"},
+        "e2e": {"value": value, "unit": "bead-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--md-steps", type=int, default=96)
+    ap.add_argument("--md-steps-ref", type=int, default=5)
+    ap.add_argument("--cpu-sample-steps", type=int, default=100)
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    rank, local, world = dist_env()
+    if args.impl == "reference":
+        # rank 0 alone times the CPU implementation; other ranks have no work
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    if True:
+        from xmd_gb300 import build
+        build.build_engine()
+        build.build_oracle()
+        run_engine(args, rank, local, world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

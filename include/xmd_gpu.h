@@ -108,7 +108,27 @@ typedef struct xmd_params {
     double lj_bb_r_min, lj_bb_depth, lj_bs_r_min, lj_bs_depth;
     int32_t ss_sinking;
     double ss_depth[XMD_NUM_SS], ss_r_max[XMD_NUM_SS];
+    /* engine: initial Verlet row capacity per bead (entries kept by pair
+       terms) and whether rows grow when a rebuild needs more (else the
+       overflow is reported as XMD_ERR_CAPACITY) */
+    int32_t nl_capacity;
+    int32_t nl_grow;
+    /* engine: CUDA device ordinal the context runs on */
+    int32_t device;
 } xmd_params;
+
+/* xmd_gpu_stats() slots */
+enum {
+    XMD_STAT_BEADS = 0,          /* beads of all replicas                         */
+    XMD_STAT_REPLICAS = 1,
+    XMD_STAT_NL_ENTRIES = 2,     /* Verlet entries kept (directed, both beads)     */
+    XMD_STAT_GO_ACTIVE = 3,      /* native contacts in the Go list (directed)      */
+    XMD_STAT_REBUILDS = 4,       /* list rebuilds summed over replicas             */
+    XMD_STAT_LAUNCHES = 5,       /* kernels launched by this context so far        */
+    XMD_STAT_QA_CONTACTS = 6,    /* live quasi-adiabatic contacts                  */
+    XMD_STAT_MD_STEPS = 7,       /* steps taken                                    */
+    XMD_NUM_STATS = 8
+};
 
 typedef struct xmd_gpu_ctx xmd_gpu_ctx;
 
@@ -180,9 +200,37 @@ int xmd_gpu_step(xmd_gpu_ctx *ctx, int32_t nsteps);
  * report_structure.cpp:85): E = V + K, K, Rg, Q (active native fraction). */
 int xmd_gpu_observables(xmd_gpu_ctx *ctx, int32_t rep, double *E, double *K,
                         double *Rg, double *Q);
+/* Live quasi-adiabatic contacts of one replica in slot order, as
+ * report_structure lists them (src/io/report_structure.cpp): out4[4*k] =
+ * (i1, i2, contact type, status 0 = forming/formed, 1 = breaking), ref_time[k]
+ * (may be NULL).  Returns the number of live contacts through *count (entries
+ * beyond cap are not written). */
+int xmd_gpu_qa_contacts(xmd_gpu_ctx *ctx, int32_t rep, int32_t cap, int32_t *out4,
+                        double *ref_time, int32_t *count);
+/* Valence counters sync[n][4] = back, side_all, side_polar, side_hydrophobic
+ * (include/xmd/forces/qa/sync_data.h). */
+int xmd_gpu_qa_sync(xmd_gpu_ctx *ctx, int32_t rep, int8_t *out);
+
 /* Device-side error word of the last step/eval (0 = none). */
 int xmd_gpu_device_status(xmd_gpu_ctx *ctx, int32_t *status);
 int xmd_gpu_synchronize(xmd_gpu_ctx *ctx);
+
+/* ---- packed host-buffer path and instrumentation --------------------------- */
+/* All replicas at once, beads in replica order (replica r starts after the
+ * beads of replicas 0..r-1).  y: [6][3*N] history with y0 = positions (pinned
+ * host memory makes the copy asynchronous).  Uploading restarts the skin test
+ * from the new positions (the next step verifies and rebuilds as needed). */
+int xmd_gpu_upload_history_all(xmd_gpu_ctx *ctx, const double *y);
+int xmd_gpu_download_positions_all(xmd_gpu_ctx *ctx, double *r);
+/* The CUDA stream (cudaStream_t) all work of the context is ordered on. */
+int xmd_gpu_get_stream(xmd_gpu_ctx *ctx, void **stream);
+/* Counters, see XMD_STAT_*; out[XMD_NUM_STATS]. */
+int xmd_gpu_stats(xmd_gpu_ctx *ctx, int64_t *out);
+/* When on, CUDA events bracket every force and list-rebuild launch; the sums
+ * are returned (ms, launches) by xmd_gpu_kernel_times and reset on enabling. */
+int xmd_gpu_set_kernel_timing(xmd_gpu_ctx *ctx, int on);
+int xmd_gpu_kernel_times(xmd_gpu_ctx *ctx, double *force_ms, int64_t *force_launches,
+                         double *rebuild_ms, int64_t *rebuild_launches);
 
 #ifdef __cplusplus
 }

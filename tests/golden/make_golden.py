@@ -1,0 +1,122 @@
+"""Generate the golden fixtures of tests/golden/ from the reference's OWN kernels.
+
+The reference ships no tests and no expected outputs, so the known answers
+are produced by its compiled hot-path translation units (FP64 build,
+oracle/_ref/libxmdref64.so, built by oracle/ref/build_ref.sh from the
+reference tree).  Each fixture stores the full input (topology, native
+structure, positions, YAML) and the reference's outputs, so the tests need
+neither the reference tree nor the synthetic generator to replay it.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from oracle.pyoracle import Oracle, rng_stream  # noqa: E402
+from xmd_gb300 import abi, synth  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+QA_SHORT = "quasi-adiabatic potential:\n  phase duration: 0.25 tau\n"
+
+CASES = {
+    # 100-bead chain from the extended start, open boundary, Go + Pauli +
+    # tether + angle + CND, 18 A + 2 A list
+    "c1_chain100": dict(sys=lambda: synth.config_c1(seed=1), yaml=synth.yaml_for("c1"), steps=1000),
+    # the same chain started in its native conformation at T = 0.1 (a start
+    # near equilibrium: the 1000-step trajectory case)
+    "c1_native100": dict(sys=lambda: synth.make_system([100], 1, box=None, temperature=0.1, start="native"),
+                         yaml=synth.yaml_for("c1"), steps=1000),
+    # 8 x 60 beads from extended starts, 80 A periodic box, + Debye-Hueckel
+    "c2_periodic480": dict(sys=lambda: synth.make_system([60] * 8, 5, box=80 * 0.2, temperature=0.35),
+                           yaml=synth.yaml_for("c2"), steps=1000),
+    # 4 x 60 native chains in a 200 A periodic box, + Debye-Hueckel
+    "c2_sparse240": dict(sys=lambda: synth.make_system([60] * 4, 5, box=200 * 0.2, temperature=0.35,
+                                                       start="native"),
+                         yaml=synth.yaml_for("c2"), steps=1000),
+    # 20 x 30 beads, uniform 20-letter types, + quasi-adiabatic with a short phase
+    "c3_qa600": dict(sys=lambda: synth.make_system([30] * 20, 11, box=(600 / 1e-3) ** (1 / 3) * 0.2 * 0.5,
+                                                   types="uniform20", temperature=0.35),
+                     yaml=synth.yaml_for("c3") + QA_SHORT, steps=500),
+}
+
+
+def pack_system(s):
+    return dict(n=np.int64(s.n), chain=s.chain, seq=s.seq, atype=s.atype, cell=s.cell, r0=s.r,
+                temperature=np.float64(s.temperature), seed=np.uint64(s.seed),
+                teth_i1=s.tethers[0], teth_i2=s.tethers[1], teth_d=s.tethers[2],
+                ang_i1=s.angles[0], ang_i2=s.angles[1], ang_i3=s.angles[2], ang_t=s.angles[3],
+                dih_i1=s.dihedrals[0], dih_i2=s.dihedrals[1], dih_i3=s.dihedrals[2], dih_i4=s.dihedrals[3],
+                dih_p=s.dihedrals[4], nat_i1=s.natives[0], nat_i2=s.natives[1], nat_d=s.natives[2])
+
+
+SNAPSHOTS = (100, 200)
+
+
+def parity_horizon(s, p, total):
+    """Largest snapshot step count at which the oracle agrees with itself under
+    a reordered force summation (its OpenMP driver, 4 threads) to <= 1e-9 A,
+    a tenth of the trajectory bar.  Beyond it the dynamics amplifies rounding
+    (and then flips Verlet-list decisions), so trajectory parity between any
+    two correct FP64 implementations is only defined up to there."""
+    a, b = Oracle(p, s, "port"), Oracle(p, s, "port")
+    done, best = 0, 0
+    for n in list(SNAPSHOTS) + [total]:
+        a.step(n - done)
+        b.step_omp(n - done, 4)
+        done = n
+        ra, _, _ = a.get_state()
+        rb, _, _ = b.get_state()
+        if np.abs(ra - rb).max() / 0.2 <= 1e-9:
+            best = n
+        else:
+            break
+    return best
+
+
+def main():
+    for name, c in CASES.items():
+        s = c["sys"]()
+        p = abi.parse_params(c["yaml"])
+        ref = Oracle(p, s, "ref")
+        F0, V0 = ref.eval_forces()
+        counts0 = ref.counts()
+        snaps = {}
+        done = 0
+        for k in SNAPSHOTS:
+            ref.step(k - done)
+            done = k
+            snaps[f"y_{k}"] = ref.get_history()[0]
+            snaps[f"rng_{k}"] = np.uint64(ref.get_history()[2])
+            qk, _ = ref.qa_contacts()
+            if qk.size:
+                snaps[f"qa_{k}"] = qk
+        ref.step(c["steps"] - done)
+        y, t, rng = ref.get_history()
+        snaps["parity_steps"] = np.int64(parity_horizon(s, p, c["steps"]))
+        F1, V1 = ref.eval_forces()
+        qa, qa_t = ref.qa_contacts()
+        extra = {}
+        if qa.size:
+            extra = dict(qa_contacts=qa, qa_ref_time=qa_t, sync=ref.sync())
+        np.savez_compressed(OUT / f"{name}.npz", yaml=np.array(c["yaml"]), steps=np.int64(c["steps"]),
+                            F0=F0, V0=V0, n_go0=np.int64(counts0["go"]), n_pauli0=np.int64(counts0["pauli"]),
+                            n_es0=np.int64(counts0["es"]), y=y, t=np.float64(t), rng=np.uint64(rng),
+                            F1=F1, V1=V1, rebuilds=np.int64(ref.counts()["rebuilds"]),
+                            **pack_system(s), **extra, **snaps)
+        print(name, s.n, "atoms,", c["steps"], "steps, V0 =", V0.sum(), "rebuilds", ref.counts()["rebuilds"],
+              "parity horizon", int(snaps["parity_steps"]))
+    raw, st = rng_stream("ref", 42, 64)
+    np.savez_compressed(OUT / "rng_seed42.npz", raw=raw, state_after=np.uint64(st))
+    print("rng", raw[:3])
+
+
+if __name__ == "__main__":
+    main()

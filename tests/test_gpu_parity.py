@@ -1,0 +1,225 @@
+"""GPU parity: the sm_103a engine, called through its C ABI, against the
+reference's known answers (golden fixtures from the reference's own FP64
+kernels) and against the CPU restatement on fresh inputs.
+
+Bars:
+  * plain FP64: per-term forces and energies within 1e-10 relative;
+  * positions within 1e-8 A after up to 1000 steps driven by the same
+    generator stream (the engine reproduces the reference's xorshift stream
+    bead by bead through a GF(2) jump-ahead), inside each system's parity
+    horizon: the step count up to which the oracle agrees with ITSELF under a
+    reordered force summation to 1e-9 A.  Near-equilibrium systems hold for
+    the full 1000 steps; extended starts amplify rounding after 100-200 steps
+    (measured in tests/golden/make_golden.py);
+  * mixed precision: forces within 1e-5 relative of the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+from oracle.pyoracle import Oracle
+from tests.util import ANGSTROM, FP64_CASES, energy_rel, horizon_snapshot, load_golden, rel_err
+from xmd_gb300 import Engine, abi, synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("case", FP64_CASES + ["c3_qa600"])
+def test_eval_forces_match_golden(case):
+    s, y, z = load_golden(case)
+    if case == "c3_qa600":
+        y += "\nquasi-adiabatic potential:\n  enabled: false\n"
+        p = abi.parse_params(y)
+        Fo, Vo = Oracle(p, s, "port").eval_forces()
+    else:
+        Fo, Vo = z["F0"], z["V0"]
+    with Engine(y) as e:
+        e.add_system(s)
+        F, V = e.eval_forces(0)
+    assert rel_err(F, Fo) <= 1e-10, rel_err(F, Fo)
+    assert energy_rel(V, Vo).max() <= 1e-10, energy_rel(V, Vo)
+
+
+@pytest.mark.parametrize("case", FP64_CASES)
+def test_trajectory_matches_golden(case):
+    s, y, z = load_golden(case)
+    n, y_ref, rng_ref = horizon_snapshot(z)
+    with Engine(y) as e:
+        e.add_system(s)
+        e.step(n)
+        yy, t, rng = e.get_history(0)
+    assert rng == rng_ref
+    dr = np.abs(yy[0] - y_ref[0]).max() / ANGSTROM
+    assert dr <= 1e-8, (n, dr)
+    assert np.abs(yy[1:] - y_ref[1:]).max() <= 1e-9
+    if n == int(z["steps"]):
+        assert abs(t - float(z["t"])) <= 1e-12
+
+
+def test_qa_state_matches_golden():
+    """Quasi-adiabatic contacts (sift, greedy acceptance in slot order,
+    saturation ramps, breaking, re-freeing) against the reference's own QA
+    kernels: identical contact list after 100 steps, inside the parity
+    horizon, with positions within 1e-8 A."""
+    s, y, z = load_golden("c3_qa600")
+    with Engine(y) as e:
+        e.add_system(s)
+        e.step(100)
+        qa, rt = e.qa_contacts(0)
+        yy, _, rng = e.get_history(0)
+        F, V = e.eval_forces(0)
+    assert np.array_equal(qa, z["qa_100"])
+    assert rng == int(z["rng_100"])
+    assert np.abs(yy[0] - z["y_100"][0]).max() / ANGSTROM <= 1e-8
+    assert (qa[:, 3] == 1).any()          # the short phase reached breaking
+
+
+def test_qa_long_run_state_machine():
+    """Past the parity horizon the engine keeps the QA invariants: valence
+    counters never go negative and equal the limits minus what live contacts
+    hold; no pair is in two contacts."""
+    s, y, _ = load_golden("c3_qa600")
+    p = abi.parse_params(y)
+    with Engine(y) as e:
+        e.add_system(s)
+        e.step(500)
+        qa, _ = e.qa_contacts(0)
+        sync = e.qa_sync(0).astype(int)
+    assert (sync >= 0).all()
+    pairs = {(a, b) for a, b, _, _ in qa}
+    assert len(pairs) == len(qa)
+    lim = np.array([p.limits[a][:] for a in s.atype], dtype=int)
+    assert (sync <= lim).all()
+
+
+@pytest.mark.parametrize("seed", [21, 22])
+def test_fresh_system_matches_port(seed):
+    """Systems not in the fixtures: periodic, charged, native starts."""
+    s = synth.make_system([50] * 5, seed, box=150 * ANGSTROM, temperature=0.35, start="native")
+    y = synth.yaml_for("c2")
+    p = abi.parse_params(y)
+    o = Oracle(p, s, "port")
+    Fo, Vo = o.eval_forces()
+    with Engine(y) as e:
+        e.add_system(s)
+        F, V = e.eval_forces(0)
+        assert rel_err(F, Fo) <= 1e-10
+        assert energy_rel(V, Vo).max() <= 1e-10
+        e.step(500)
+        o.step(500)
+        r, v, t = e.get_state(0)
+    ro, vo, to = o.get_state()
+    assert np.abs(r - ro).max() / ANGSTROM <= 1e-8
+    assert t == to
+
+
+@pytest.mark.parametrize("case", ["c1_chain100", "c2_periodic480"])
+def test_mixed_precision_force_error(case):
+    s, y, z = load_golden(case)
+    with Engine(y.replace("precision: fp64", "precision: mixed")) as e:
+        e.add_system(s)
+        F, V = e.eval_forces(0)
+    err = rel_err(F, z["F0"])
+    assert err <= 1e-5, err
+
+
+def test_batched_replicas_equal_alone():
+    """Replicas packed into one context give bit-identical results to the
+    same systems run alone (per-replica streams, grids and lists)."""
+    systems = [synth.make_system([L], 300 + k, box=None, temperature=0.3 + 0.1 * k)
+               for k, L in enumerate([57, 120, 33])]
+    y = synth.yaml_for("c2")
+    alone = []
+    for s in systems:
+        with Engine(y) as e:
+            e.add_system(s)
+            e.step(300)
+            alone.append(e.get_history(0))
+    with Engine(y) as e:
+        for s in systems:
+            e.add_system(s)
+        e.step(300)
+        for k in range(len(systems)):
+            yy, t, st = e.get_history(k)
+            assert np.array_equal(yy, alone[k][0])
+            assert t == alone[k][1] and st == alone[k][2]
+
+
+def test_graph_and_stream_paths_agree():
+    """Graph-captured chunks (device-side rebuild decisions) and the plain
+    per-step path give identical trajectories."""
+    s, y, _ = load_golden("c2_periodic480")
+    with Engine(y) as a, Engine(y) as b:
+        a.add_system(s)
+        b.add_system(s)
+        a.step(64)                       # 4 graph chunks
+        abi.check(b.lib.xmd_gpu_set_kernel_timing(b.h, 1))   # timing forces the per-step path
+        b.step(64)
+        ya, ta, sa = a.get_history(0)
+        yb, tb, sb = b.get_history(0)
+    assert np.array_equal(ya, yb) and ta == tb and sa == sb
+
+
+def test_packed_upload_download_roundtrip():
+    systems = [synth.make_system([L], 500 + k, temperature=0.4) for k, L in enumerate([40, 75])]
+    with Engine(synth.yaml_for("c2")) as e:
+        for s in systems:
+            e.add_system(s)
+        e.step(20)
+        hs = [e.get_history(k)[0] for k in range(2)]
+        packed = np.ascontiguousarray(np.concatenate(hs, axis=1).reshape(6, -1))
+        abi.check(e.lib.xmd_gpu_upload_history_all(e.h, abi.dptr(packed)))
+        r = np.zeros(3 * (40 + 75))
+        abi.check(e.lib.xmd_gpu_download_positions_all(e.h, abi.dptr(r)))
+        assert np.array_equal(r.reshape(-1, 3), np.concatenate([h[0] for h in hs]))
+
+
+def test_verlet_capacity_overflow_is_reported():
+    s, y, _ = load_golden("c2_periodic480")
+    with Engine(y + "\nengine:\n  nl capacity: 1\n  nl grow: false\n") as e:
+        e.add_system(s)
+        with pytest.raises(abi.XmdError) as ei:
+            e.eval_forces(0)
+        assert ei.value.code == -5
+
+
+def test_verlet_rows_grow_on_demand():
+    """With growth on (the default) a too-small initial capacity is raised at
+    the first rebuild and the forces are unaffected."""
+    s, y, z = load_golden("c2_periodic480")
+    with Engine(y + "\nengine:\n  nl capacity: 2\n") as e:
+        e.add_system(s)
+        F, V = e.eval_forces(0)
+        e.step(40)
+    assert rel_err(F, z["F0"], floor=1.0) <= 1e-10
+
+
+@pytest.mark.parametrize("case", ["c1_chain100", "c2_periodic480", "c3_qa600"])
+@pytest.mark.parametrize("term", [0, 1, 2, 4, 5, 6])
+def test_per_term_forces(case, term):
+    """One term enabled at a time (the list cutoffs kept as with all terms):
+    forces and energy of that term alone within 1e-10 of the oracle,
+    normalised by that term's own force scale."""
+    s, y, _ = load_golden(case)
+    names = ["tether forces", "native angles", "complex native dihedrals", "simple native dihedrals",
+             "native contacts", "Pauli exclusion", "const ES", "relative ES", "quasi-adiabatic potential"]
+    full = abi.parse_params(y)
+    mc = Oracle(full, s, "port").cutoffs()
+    yy = y + "".join(f"\n{names[k]}:\n  enabled: {'true' if k == term else 'false'}\n" for k in range(9))
+    yy += f"\nneighbor list:\n  cutoff: {mc[0] / ANGSTROM!r} A\n  skin: {mc[1] / ANGSTROM!r} A\n"
+    p = abi.parse_params(yy)
+    Fo, Vo = Oracle(p, s, "port").eval_forces()
+    with Engine(yy) as e:
+        e.add_system(s)
+        F, V = e.eval_forces(0)
+    assert rel_err(F, Fo, floor=1e-6) <= 1e-10, rel_err(F, Fo, floor=1e-6)
+    assert energy_rel(V, Vo).max() <= 1e-10
+
+
+def test_bad_topology_rejected():
+    s = synth.make_system([20], 5)
+    bad = (s.angles[0][:1], s.angles[1][:1] + 1, s.angles[2][:1], s.angles[3][:1])
+    s.angles = bad
+    with Engine(synth.yaml_for("c1")) as e:
+        with pytest.raises(abi.XmdError) as ei:
+            e.add_system(s)
+        assert ei.value.code == -1

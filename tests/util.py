@@ -1,0 +1,60 @@
+"""Shared helpers of the test suite."""
+from __future__ import annotations
+
+from pathlib import Path
+
+import numpy as np
+
+from xmd_gb300.synth import System
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+GOLDEN_CASES = ["c1_chain100", "c1_native100", "c2_periodic480", "c2_sparse240", "c3_qa600"]
+FP64_CASES = ["c1_chain100", "c1_native100", "c2_periodic480", "c2_sparse240"]
+ANGSTROM = 0.2
+
+
+def horizon_snapshot(z):
+    """(steps, y[6,n,3], rng_state) of the fixture's last snapshot inside its
+    parity horizon: the step count up to which the oracle agrees with itself
+    under a reordered force summation to 1e-9 A (beyond it the dynamics
+    amplifies rounding, so no two FP64 implementations stay within 1e-8 A)."""
+    h = int(z["parity_steps"])
+    if h >= int(z["steps"]):
+        return int(z["steps"]), z["y"], int(z["rng"])
+    best = max(k for k in (100, 200) if k <= max(h, 100))
+    return best, z[f"y_{best}"], int(z[f"rng_{best}"])
+
+
+def load_golden(name: str):
+    z = np.load(GOLDEN / f"{name}.npz")
+    s = System(
+        n=int(z["n"]), chain=z["chain"], seq=z["seq"], atype=z["atype"], cell=z["cell"], r=z["r0"],
+        tethers=(z["teth_i1"], z["teth_i2"], z["teth_d"]),
+        angles=(z["ang_i1"], z["ang_i2"], z["ang_i3"], z["ang_t"]),
+        dihedrals=(z["dih_i1"], z["dih_i2"], z["dih_i3"], z["dih_i4"], z["dih_p"]),
+        natives=(z["nat_i1"], z["nat_i2"], z["nat_d"]),
+        temperature=float(z["temperature"]), seed=int(z["seed"]),
+    )
+    return s, str(z["yaml"]), z
+
+
+def rel_err(a, b, floor=1.0):
+    """max |a - b| over max |b| (norm-wise relative error).  The denominator is
+    floored (default 1 eps per internal length unit): at an energy minimum the
+    net forces cancel to ~1e-13 while each contribution is O(1), so rounding
+    would otherwise read as a large relative error.  Per-term comparisons use
+    a tiny floor."""
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    den = max(np.abs(b).max(), floor)
+    return float(np.abs(a - b).max() / den)
+
+
+def energy_rel(Va, Vb, floor=1e-6):
+    """Per-term relative energy errors.  The denominator is floored at 1e-6 eps:
+    a term whose exact value is ~0 (e.g. bonds exactly at their rest length,
+    V ~ 1e-25) carries only rounding noise, which a relative test would
+    amplify without meaning."""
+    out = []
+    for x, y in zip(Va, Vb):
+        out.append(abs(x - y) / max(abs(y), floor))
+    return np.array(out)

@@ -47,6 +47,7 @@ class Params(C.Structure):
         ("qa_min_cos_hr", _d), ("qa_min_cos_hh", _d), ("qa_max_cos_nr", _d),
         ("lj_bb_r_min", _d), ("lj_bb_depth", _d), ("lj_bs_r_min", _d), ("lj_bs_depth", _d),
         ("ss_sinking", _i), ("ss_depth", _d * NUM_SS), ("ss_r_max", _d * NUM_SS),
+        ("nl_capacity", _i), ("nl_grow", _i), ("device", _i),
     ]
 
     def copy(self) -> "Params":
@@ -89,6 +90,14 @@ SIGNATURES = [
     ("xmd_gpu_step", C.c_int, [C.c_void_p, C.c_int32]),
     ("xmd_gpu_observables", C.c_int, [C.c_void_p, C.c_int32, _pd, _pd, _pd, _pd]),
     ("xmd_gpu_device_status", C.c_int, [C.c_void_p, _pi32]),
+    ("xmd_gpu_qa_contacts", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _pi32, _pd, _pi32]),
+    ("xmd_gpu_qa_sync", C.c_int, [C.c_void_p, C.c_int32, P(C.c_int8)]),
+    ("xmd_gpu_upload_history_all", C.c_int, [C.c_void_p, _pd]),
+    ("xmd_gpu_download_positions_all", C.c_int, [C.c_void_p, _pd]),
+    ("xmd_gpu_get_stream", C.c_int, [C.c_void_p, P(C.c_void_p)]),
+    ("xmd_gpu_stats", C.c_int, [C.c_void_p, P(C.c_int64)]),
+    ("xmd_gpu_set_kernel_timing", C.c_int, [C.c_void_p, C.c_int]),
+    ("xmd_gpu_kernel_times", C.c_int, [C.c_void_p, _pd, P(C.c_int64), _pd, P(C.c_int64)]),
     ("xmd_gpu_synchronize", C.c_int, [C.c_void_p]),
 ]
 

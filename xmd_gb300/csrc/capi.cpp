@@ -142,14 +142,14 @@ int xmd_gpu_set_tethers(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t 
                         const double *nat_dist) {
     NEED_CTX;
     if (n < 0 || (n > 0 && (!i1 || !i2))) return fail(XMD_ERR_ARG, "bad tether arrays");
-    return guard([&] { ctx->eng->set_tethers(rep, n, i1, i2, nat_dist); });
+    return guard([&] { ctx->eng->use_device(); ctx->eng->set_tethers(rep, n, i1, i2, nat_dist); });
 }
 
 int xmd_gpu_set_angles(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1, const int32_t *i2,
                        const int32_t *i3, const double *nat_theta) {
     NEED_CTX;
     if (n < 0 || (n > 0 && (!i1 || !i2 || !i3 || !nat_theta))) return fail(XMD_ERR_ARG, "bad angle arrays");
-    return guard([&] { ctx->eng->set_angles(rep, n, i1, i2, i3, nat_theta); });
+    return guard([&] { ctx->eng->use_device(); ctx->eng->set_angles(rep, n, i1, i2, i3, nat_theta); });
 }
 
 int xmd_gpu_set_dihedrals(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1, const int32_t *i2,
@@ -157,51 +157,51 @@ int xmd_gpu_set_dihedrals(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_
     NEED_CTX;
     if (n < 0 || (n > 0 && (!i1 || !i2 || !i3 || !i4 || !nat_phi)))
         return fail(XMD_ERR_ARG, "bad dihedral arrays");
-    return guard([&] { ctx->eng->set_dihedrals(rep, n, i1, i2, i3, i4, nat_phi); });
+    return guard([&] { ctx->eng->use_device(); ctx->eng->set_dihedrals(rep, n, i1, i2, i3, i4, nat_phi); });
 }
 
 int xmd_gpu_set_native_contacts(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1,
                                 const int32_t *i2, const double *nat_dist) {
     NEED_CTX;
     if (n < 0 || (n > 0 && (!i1 || !i2 || !nat_dist))) return fail(XMD_ERR_ARG, "bad native arrays");
-    return guard([&] { ctx->eng->set_native(rep, n, i1, i2, nat_dist); });
+    return guard([&] { ctx->eng->use_device(); ctx->eng->set_native(rep, n, i1, i2, nat_dist); });
 }
 
 int xmd_gpu_set_state(xmd_gpu_ctx *ctx, int32_t rep, const double *r, const double *v) {
     NEED_CTX;
-    return guard([&] { ctx->eng->set_state(rep, r, v); });
+    return guard([&] { ctx->eng->use_device(); ctx->eng->set_state(rep, r, v); });
 }
 
 int xmd_gpu_set_history(xmd_gpu_ctx *ctx, int32_t rep, const double *y, double t, uint64_t rng_state) {
     NEED_CTX;
     if (!y) return fail(XMD_ERR_ARG, "null history");
-    return guard([&] { ctx->eng->set_history(rep, y, t, rng_state); });
+    return guard([&] { ctx->eng->use_device(); ctx->eng->set_history(rep, y, t, rng_state); });
 }
 
 int xmd_gpu_get_state(xmd_gpu_ctx *ctx, int32_t rep, double *r, double *v, double *t) {
     NEED_CTX;
-    return guard([&] { ctx->eng->get_state(rep, r, v, t); });
+    return guard([&] { ctx->eng->use_device(); ctx->eng->get_state(rep, r, v, t); });
 }
 
 int xmd_gpu_get_history(xmd_gpu_ctx *ctx, int32_t rep, double *y, double *t, uint64_t *rng_state) {
     NEED_CTX;
-    return guard([&] { ctx->eng->get_history(rep, y, t, rng_state); });
+    return guard([&] { ctx->eng->use_device(); ctx->eng->get_history(rep, y, t, rng_state); });
 }
 
 int xmd_gpu_eval_forces(xmd_gpu_ctx *ctx, int32_t rep, double *F, double *V) {
     NEED_CTX;
-    return guard([&] { ctx->eng->eval_forces(rep, F, V); });
+    return guard([&] { ctx->eng->use_device(); ctx->eng->eval_forces(rep, F, V); });
 }
 
 int xmd_gpu_step(xmd_gpu_ctx *ctx, int32_t nsteps) {
     NEED_CTX;
     if (nsteps < 0) return fail(XMD_ERR_ARG, "negative step count");
-    return guard([&] { ctx->eng->step(nsteps); });
+    return guard([&] { ctx->eng->use_device(); ctx->eng->step(nsteps); });
 }
 
 int xmd_gpu_observables(xmd_gpu_ctx *ctx, int32_t rep, double *E, double *K, double *Rg, double *Q) {
     NEED_CTX;
-    return guard([&] { ctx->eng->observables(rep, E, K, Rg, Q); });
+    return guard([&] { ctx->eng->use_device(); ctx->eng->observables(rep, E, K, Rg, Q); });
 }
 
 int xmd_gpu_device_status(xmd_gpu_ctx *ctx, int32_t *status) {
@@ -212,9 +212,65 @@ int xmd_gpu_device_status(xmd_gpu_ctx *ctx, int32_t *status) {
     });
 }
 
+int xmd_gpu_upload_history_all(xmd_gpu_ctx *ctx, const double *y) {
+    NEED_CTX;
+    if (!y) return fail(XMD_ERR_ARG, "null history");
+    return guard([&] { ctx->eng->use_device(); ctx->eng->upload_history_all(y); });
+}
+
+int xmd_gpu_download_positions_all(xmd_gpu_ctx *ctx, double *r) {
+    NEED_CTX;
+    if (!r) return fail(XMD_ERR_ARG, "null output");
+    return guard([&] { ctx->eng->use_device(); ctx->eng->download_positions_all(r); });
+}
+
+int xmd_gpu_get_stream(xmd_gpu_ctx *ctx, void **stream) {
+    NEED_CTX;
+    if (!stream) return fail(XMD_ERR_ARG, "null output");
+    *stream = (void *)ctx->eng->get_stream();
+    return XMD_OK;
+}
+
+int xmd_gpu_stats(xmd_gpu_ctx *ctx, int64_t *out) {
+    NEED_CTX;
+    if (!out) return fail(XMD_ERR_ARG, "null output");
+    return guard([&] { ctx->eng->use_device(); ctx->eng->stats(out); });
+}
+
+int xmd_gpu_set_kernel_timing(xmd_gpu_ctx *ctx, int on) {
+    NEED_CTX;
+    return guard([&] { ctx->eng->use_device(); ctx->eng->set_kernel_timing(on != 0); });
+}
+
+int xmd_gpu_kernel_times(xmd_gpu_ctx *ctx, double *force_ms, int64_t *force_launches, double *rebuild_ms,
+                         int64_t *rebuild_launches) {
+    NEED_CTX;
+    return guard([&] {
+        ctx->eng->use_device();
+        ctx->eng->kernel_times(force_ms, force_launches, rebuild_ms, rebuild_launches);
+    });
+}
+
+int xmd_gpu_qa_contacts(xmd_gpu_ctx *ctx, int32_t rep, int32_t cap, int32_t *out4, double *ref_time,
+                        int32_t *count) {
+    NEED_CTX;
+    if (cap < 0 || (cap > 0 && !out4)) return fail(XMD_ERR_ARG, "bad output buffer");
+    return guard([&] {
+        ctx->eng->use_device();
+        int m = ctx->eng->qa_contacts(rep, cap, out4, ref_time);
+        if (count) *count = m;
+    });
+}
+
+int xmd_gpu_qa_sync(xmd_gpu_ctx *ctx, int32_t rep, int8_t *out) {
+    NEED_CTX;
+    if (!out) return fail(XMD_ERR_ARG, "null output");
+    return guard([&] { ctx->eng->use_device(); ctx->eng->qa_sync(rep, out); });
+}
+
 int xmd_gpu_synchronize(xmd_gpu_ctx *ctx) {
     NEED_CTX;
-    return guard([&] { ctx->eng->sync(); });
+    return guard([&] { ctx->eng->use_device(); ctx->eng->sync(); });
 }
 
 }  // extern "C"

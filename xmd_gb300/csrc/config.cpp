@@ -595,7 +595,19 @@ void resolve_params(const YNode &root, xmd_params *o) {
     }
     // engine-only section
     o->precision = XMD_PREC_FP64;
+    o->nl_capacity = 64;
+    o->nl_grow = 1;
+    o->device = 0;
     if (const YNode *en = root.get("engine")) {
+        if (en->get("nl grow")) o->nl_grow = bval(*en, "nl grow", "engine: ");
+        if (const YNode *dv = en->get("device"); dv && dv->kind == YNode::Scalar) {
+            o->device = std::atoi(dv->scalar.c_str());
+            if (o->device < 0) throw std::runtime_error("engine: device must be >= 0");
+        }
+        if (const YNode *nc = en->get("nl capacity"); nc && nc->kind == YNode::Scalar) {
+            o->nl_capacity = std::atoi(nc->scalar.c_str());
+            if (o->nl_capacity < 1) throw std::runtime_error("engine: nl capacity must be >= 1");
+        }
         if (const YNode *pr = en->get("precision"); pr && pr->kind == YNode::Scalar) {
             if (pr->scalar == "fp64") o->precision = XMD_PREC_FP64;
             else if (pr->scalar == "mixed") o->precision = XMD_PREC_MIXED;

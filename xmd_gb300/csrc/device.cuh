@@ -167,6 +167,80 @@ __device__ __forceinline__ void dihedral_term(const TermP &p, double4_32a q1, do
     f[3] = -(dV * d4);
 }
 
+// ---- bonded terms of the mixed path -------------------------------------------
+// The reference formulation (acos of a clamped cosine; cross products of bond
+// vectors) loses all accuracy in FP32 near straight triples, where the stiff
+// starting chains live: the reference's own FP32 build misses by ~1e-3.  Here
+// the bond vectors, their cross products and the dihedral's triple product are
+// formed in FP64 and the angles are taken with atan2 in FP32:
+//   theta = atan2(|r12 x r23|, -r12.r23)                    (= acos of the cosine)
+//   phi   = atan2(|r23| (x12_23 . r34), x12_23 . x23_34)    (= +-acos, sign of
+//            x12_23 . r34 as in complex_native.cpp:27-28)
+// after which every FP32 operation is well conditioned.  Force expressions are
+// those of angle/native.cpp:25-38 and dihedral/complex_native.cpp:37-48.
+__device__ __forceinline__ V3<double> dsub(double4_32a u, double4_32a w) {
+    return V3<double>{w.x - u.x, w.y - u.y, w.z - u.z};
+}
+__device__ __forceinline__ V3<float> f3(V3<double> a) { return V3<float>{(float)a.x, (float)a.y, (float)a.z}; }
+
+__device__ __forceinline__ void angle_mixed(const TermP &p, V3<double> r12d, V3<double> r23d, V3<double> xd,
+                                            float nat_theta, V3<float> *f1, V3<float> *f2, V3<float> *f3o,
+                                            float *V) {
+    V3<float> r12 = f3(r12d), r23 = f3(r23d), x12_23 = f3(xd);
+    float r12_rn = 1.0f / norm(r12), r23_rn = 1.0f / norm(r23);
+    V3<float> d1 = r12_rn * unit(cross(r12, x12_23));
+    V3<float> d3 = r23_rn * unit(cross(r23, x12_23));
+    V3<float> d2 = (-d1) - d3;
+    float theta = atan2f(norm(x12_23), -dot(r12, r23));
+    float dtheta = theta - nat_theta;
+    float k = (float)p.nat_ang_k;
+    *V = 0.5f * k * dtheta * dtheta;
+    float dV = k * dtheta;
+    *f1 = -(dV * d1);
+    *f2 = -(dV * d2);
+    *f3o = -(dV * d3);
+}
+
+__device__ __forceinline__ void dihedral_mixed(const TermP &p, V3<double> r12d, V3<double> r23d, V3<double> r34d,
+                                               V3<double> x1d, float nat_phi, bool cnd, bool snd, V3<float> *f,
+                                               float *Vc, float *Vs) {
+    V3<double> x2d = cross(r23d, r34d);
+    double X = dot(x1d, x2d);
+    double T = dot(x1d, r34d);
+    V3<float> r12 = f3(r12d), r23 = f3(r23d), r34 = f3(r34d), x12_23 = f3(x1d), x23_34 = f3(x2d);
+    float r23_n = norm(r23);
+    float phi = atan2f(r23_n * (float)T, (float)X);
+    float diff_ = phi - nat_phi;
+    float dV = 0.0f;
+    *Vc = 0.0f;
+    *Vs = 0.0f;
+    if (cnd) {
+        float s1, c1, s3, c3;
+        sincosf(diff_, &s1, &c1);
+        sincosf(3.0f * diff_, &s3, &c3);
+        float CDA = (float)p.cnd_CDA, CDB = (float)p.cnd_CDB;
+        *Vc = CDA * (1.0f - c1) + CDB * (1.0f - c3);
+        dV += CDA * s1 + CDB * 3.0f * s3;
+    }
+    if (snd) {
+        float CDH = (float)p.snd_CDH;
+        *Vs = 0.5f * CDH * diff_ * diff_;
+        dV += CDH * diff_;
+    }
+    float x12_23_rn = 1.0f / norm(x12_23), x23_34_rn = 1.0f / norm(x23_34);
+    V3<float> x12_23_u = x12_23_rn * x12_23, x23_34_u = x23_34_rn * x23_34;
+    V3<float> d1 = x12_23_rn * (r23_n * (-x12_23_u));
+    V3<float> d4 = x23_34_rn * (r23_n * x23_34_u);
+    float k1 = dot(r12, r23), k4 = dot(r23, r34), den = r23_n * r23_n;
+    V3<float> df{(-d1.x * k1 + d4.x * k4) / den, (-d1.y * k1 + d4.y * k4) / den, (-d1.z * k1 + d4.z * k4) / den};
+    V3<float> d2 = (-d1) + df;
+    V3<float> d3 = (-d4) - df;
+    f[0] = -(dV * d1);
+    f[1] = -(dV * d2);
+    f[2] = -(dV * d3);
+    f[3] = -(dV * d4);
+}
+
 // ---- pair terms: force on the first bead of r12 = r_uv(r_i, r_j) ------------
 
 // lj::operator(): primitives/lj.h:22-30

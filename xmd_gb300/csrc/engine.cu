@@ -27,6 +27,7 @@
 
 #include "device.cuh"
 #include "engine.h"
+#include "qa.cuh"
 
 namespace xmdg {
 
@@ -124,25 +125,47 @@ __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
         V3<FT> z{FT(0), FT(0), FT(0)};
         V3<FT> ft = z, a1 = z, a2 = z, a3 = z, q[4] = {z, z, z, z};
         int sp = c - (i0 - 3);
-        bool own = (c >= i0 && c < i0 + FB);
+        bool own = (c >= i0 && c < i0 + FB && c < N);
         int rc = own ? d.rep_of[c] : 0;
         if ((fl & BF_TETH) && p.on[XMD_TERM_TETHER]) {
             FT V_;
             ft = tether_term<FT>(p, P[sp], P[sp + 1], (FT)d.teth_r0[c], &V_);
             if (MODE == 0 && own) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_TETHER], (double)V_);
         }
-        if ((fl & BF_ANG) && p.on[XMD_TERM_NAT_ANG]) {
-            FT V_;
-            angle_term<FT>(p, P[sp - 1], P[sp], P[sp + 1], (FT)d.ang_t0[c], &a1, &a2, &a3, &V_);
-            if (MODE == 0 && own) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_NAT_ANG], (double)V_);
-        }
-        if ((fl & BF_DIH) && (p.on[XMD_TERM_CND] || p.on[XMD_TERM_SND])) {
-            FT Vc, Vs;
-            dihedral_term<FT>(p, P[sp - 1], P[sp], P[sp + 1], P[sp + 2], (FT)d.dih_p0[c],
-                              p.on[XMD_TERM_CND] != 0, p.on[XMD_TERM_SND] != 0, q, &Vc, &Vs);
-            if (MODE == 0 && own) {
-                if (p.on[XMD_TERM_CND]) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_CND], (double)Vc);
-                if (p.on[XMD_TERM_SND]) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_SND], (double)Vs);
+        const bool do_ang = (fl & BF_ANG) && p.on[XMD_TERM_NAT_ANG];
+        const bool do_dih = (fl & BF_DIH) && (p.on[XMD_TERM_CND] || p.on[XMD_TERM_SND]);
+        if constexpr (sizeof(FT) == 8) {
+            if (do_ang) {
+                FT V_;
+                angle_term<FT>(p, P[sp - 1], P[sp], P[sp + 1], (FT)d.ang_t0[c], &a1, &a2, &a3, &V_);
+                if (MODE == 0 && own) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_NAT_ANG], (double)V_);
+            }
+            if (do_dih) {
+                FT Vc, Vs;
+                dihedral_term<FT>(p, P[sp - 1], P[sp], P[sp + 1], P[sp + 2], (FT)d.dih_p0[c],
+                                  p.on[XMD_TERM_CND] != 0, p.on[XMD_TERM_SND] != 0, q, &Vc, &Vs);
+                if (MODE == 0 && own) {
+                    if (p.on[XMD_TERM_CND]) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_CND], (double)Vc);
+                    if (p.on[XMD_TERM_SND]) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_SND], (double)Vs);
+                }
+            }
+        } else if (do_ang || do_dih) {
+            // mixed path: FP64 bond vectors and cross products, FP32 forces
+            V3<double> r12 = dsub(P[sp - 1], P[sp]), r23 = dsub(P[sp], P[sp + 1]);
+            V3<double> x12_23 = cross(r12, r23);
+            if (do_ang) {
+                float V_;
+                angle_mixed(p, r12, r23, x12_23, (float)d.ang_t0[c], &a1, &a2, &a3, &V_);
+                if (MODE == 0 && own) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_NAT_ANG], (double)V_);
+            }
+            if (do_dih) {
+                float Vc, Vs;
+                dihedral_mixed(p, r12, r23, dsub(P[sp + 1], P[sp + 2]), x12_23, (float)d.dih_p0[c],
+                               p.on[XMD_TERM_CND] != 0, p.on[XMD_TERM_SND] != 0, q, &Vc, &Vs);
+                if (MODE == 0 && own) {
+                    if (p.on[XMD_TERM_CND]) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_CND], (double)Vc);
+                    if (p.on[XMD_TERM_SND]) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_SND], (double)Vs);
+                }
             }
         }
         Ct[sc] = ft;
@@ -201,6 +224,48 @@ __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
         }
     }
 
+    // quasi-adiabatic contacts: the force part of process_contacts::iter
+    // (process_contacts.cpp:25-40), summed in contact-slot order
+    double vqa = 0;
+    if (d.qa_on && p.on[XMD_TERM_QA]) {
+        const QaDev &q = d.qa;
+        int nref = min(q.ref_cnt[i], QA_REF_CAP);
+        int sl[QA_REF_CAP];
+        for (int k = 0; k < nref; ++k) sl[k] = q.ref[(size_t)k * N + i];
+        for (int x = 1; x < nref; ++x) {
+            int v = sl[x], y = x - 1;
+            while (y >= 0 && sl[y] > v) { sl[y + 1] = sl[y]; --y; }
+            sl[y + 1] = v;
+        }
+        const double tnow = d.rep[r].t;
+        for (int k = 0; k < nref; ++k) {
+            int slot = sl[k];
+            int i1 = q.ct_i1[slot], i2 = q.ct_i2[slot];
+            V3<FT> r12 = r_uv<FT>(bx, pin[i1], pin[i2]);
+            FT r12_rn = ninv(r12);
+            V3<FT> u = r12_rn * r12;
+            double sat = fmin(tnow - q.ct_ref[slot], p.qa_cycle) * p.qa_cycle_inv;
+            if (q.ct_status[slot] == QA_BREAKING) sat = 1.0 - sat;
+            double depth, rmin, rmax;
+            qa_lj(p, q, q.ct_type[slot], &depth, &rmin, &rmax);
+            FT V_, dV_;
+            sink_lj_eval<FT>((FT)depth, (FT)rmin, (FT)rmax, r12_rn * nsq(r12), r12_rn, &V_, &dV_);
+            V3<FT> f = ((FT)sat * dV_) * u;
+            if (i == i1) add3(fx, fy, fz, f);
+            else add3(fx, fy, fz, -f);
+            if (MODE == 0 && i == i1) vqa += sat * (double)V_;
+        }
+        if (MODE == 1) {
+            // n and h at this step's positions (precompute_nh.cpp:12-20)
+            D3 n{0, 0, 0}, h{0, 0, 0};
+            const uint32_t fl = d.bflags[i];
+            if ((fl & BF_PREV) && (fl & BF_NEXT)) qa_nh(P[t + 2], P[t + 3], P[t + 4], &n, &h);
+            const size_t Ns = (size_t)N;
+            q.nh[i] = n.x; q.nh[Ns + i] = n.y; q.nh[2 * Ns + i] = n.z;
+            q.nh[3 * Ns + i] = h.x; q.nh[4 * Ns + i] = h.y; q.nh[5 * Ns + i] = h.z;
+        }
+    }
+
     if (!(isfinite(fx) && isfinite(fy) && isfinite(fz))) atomicOr(d.status, ST_NONFINITE);
 
     if (MODE == 0) {
@@ -211,6 +276,7 @@ __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
         if (vgo != 0.0) atomicAdd(&Vr[XMD_TERM_GO], vgo);
         if (vpa != 0.0) atomicAdd(&Vr[XMD_TERM_PAULI], vpa);
         if (ves != 0.0) atomicAdd(&Vr[p.es_rel ? XMD_TERM_REL_ES : XMD_TERM_CONST_ES], ves);
+        if (vqa != 0.0) atomicAdd(&Vr[XMD_TERM_QA], vqa);
         return;
     }
 
@@ -268,7 +334,8 @@ __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
 }
 
 // ---- skin decision (nl::verify, verify.cpp:4-23) --------------------------------
-__global__ void k_nl_check(Dev d, int advance, double dt) {
+// setc: also set the conditional handle of the graph's rebuild IF node
+__global__ void k_nl_check(Dev d, int advance, double dt, cudaGraphConditionalHandle h, int setc) {
     __shared__ int any_s;
     if (threadIdx.x == 0) any_s = 0;
     __syncthreads();
@@ -284,7 +351,16 @@ __global__ void k_nl_check(Dev d, int advance, double dt) {
     }
     if (any) atomicOr(&any_s, 1);
     __syncthreads();
-    if (threadIdx.x == 0) *d.any_rebuild = any_s;
+    if (threadIdx.x == 0) {
+        *d.any_rebuild = any_s;
+        if (setc) cudaGraphSetConditional(h, any_s ? 1u : 0u);
+    }
+}
+
+// every replica rebuilds at the next check (after the rows were reallocated)
+__global__ void k_mark_all(Dev d) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < d.R) d.rep[r].first = 1;
 }
 
 // ---- cell lists: one block per flagged replica -----------------------------------
@@ -304,6 +380,7 @@ __device__ __forceinline__ double comp(double4_32a v, int a) { return a == 0 ? v
 constexpr int CB = 1024;
 __global__ void __launch_bounds__(CB) k_cells(Dev d, int cur) {
     const int r = blockIdx.x;
+    if (r == 0 && threadIdx.x == 0) atomicAdd(d.ctr, 1ull);
     RepDev &rp = d.rep[r];
     if (!rp.rebuild) return;
     const double4_32a *pos = d.pos[cur];
@@ -456,7 +533,9 @@ __global__ void __launch_bounds__(128) k_nl_build(Dev d, TermP p, int cur) {
     }
     const bool pauli_on = p.on[XMD_TERM_PAULI] != 0;
     const bool es_on = (p.on[XMD_TERM_CONST_ES] || p.on[XMD_TERM_REL_ES]);
-    int cnt = 0;
+    const bool qa_on = d.qa_on && p.on[XMD_TERM_QA];
+    const int nref = qa_on ? min(d.qa.ref_cnt[i], QA_REF_CAP) : 0;
+    int cnt = 0, tcnt = 0;
     const int cap = d.nl_cap;
     for (int az = 0; az < noff[2]; ++az)
         for (int ay = 0; ay < noff[1]; ++ay)
@@ -476,6 +555,20 @@ __global__ void __launch_bounds__(128) k_nl_build(Dev d, TermP p, int cur) {
                     for (int k = n0; k < n1; ++k) native |= d.nat_j[k] == j;
                     if (native) continue;
                     double inv = __ddiv_rn(1.0, dd);
+                    // quasi-adiabatic free pairs (update_free_pairs, free_pair.cpp:9-19),
+                    // j > i, minus pairs already in contact
+                    if (qa_on && j > i && inv > rp.qa_min_inv) {
+                        bool in_contact = false;
+                        for (int k = 0; k < nref; ++k) {
+                            int s = d.qa.ref[(size_t)k * d.N + i];
+                            int other = d.qa.ct_i1[s] == i ? d.qa.ct_i2[s] : d.qa.ct_i1[s];
+                            in_contact |= other == j;
+                        }
+                        if (!in_contact) {
+                            if (tcnt < QA_TMP_CAP) d.qa.tmp[(size_t)tcnt * d.N + i] = j;
+                            ++tcnt;
+                        }
+                    }
                     int flags = 0;
                     if (pauli_on && inv > rp.pauli_min_inv) flags |= NL_PAULI;
                     if (es_on && inv > rp.es_min_inv && pi.w * pj.w != 0.0) flags |= NL_ES;
@@ -484,12 +577,17 @@ __global__ void __launch_bounds__(128) k_nl_build(Dev d, TermP p, int cur) {
                     ++cnt;
                 }
             }
+    atomicMax(&d.ctr[1], (unsigned long long)cnt);   // longest row needed
     if (cnt > cap) {
         atomicOr(d.status, ST_CAPACITY);
         cnt = cap;
     }
     d.nl_cnt[i] = cnt;
     d.orig[i] = pi;
+    if (qa_on) {
+        if (tcnt > QA_TMP_CAP) atomicOr(d.status, ST_CAPACITY);
+        d.qa.tmp_cnt[i] = min(tcnt, QA_TMP_CAP);
+    }
 }
 
 // =================================================================== host ==
@@ -498,11 +596,22 @@ Engine::Engine(const xmd_params &p) : params(p) {
     int ndev = 0;
     CK(cudaGetDeviceCount(&ndev));
     if (ndev < 1) throw std::runtime_error("no CUDA device");
+    device = p.device;
+    if (device < 0 || device >= ndev) throw std::invalid_argument("engine: device out of range");
+    use_device();
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     CK(cudaMallocHost(&h_any, sizeof(int) * 4));
 }
 
 Engine::~Engine() {
+    cudaSetDevice(device);
+    for (auto &row : graphs)
+        for (auto &g : row) {
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+            if (g.graph) cudaGraphDestroy(g.graph);
+        }
+    for (auto e : ev_force) cudaEventDestroy(e);
+    for (auto e : ev_rebuild) cudaEventDestroy(e);
     release();
     if (h_any) cudaFreeHost(h_any);
     if (stream) cudaStreamDestroy(stream);
@@ -631,12 +740,18 @@ void Engine::derive_rep(int ri, RepDev &rd) {
     if (p.on[XMD_TERM_GO]) for (double x : r.nat_d) mc = std::max(mc, 2.0 * x);
     if (p.on[XMD_TERM_CONST_ES]) mc = std::max(mc, 2.0 * p.const_es_screen_dist);
     if (p.on[XMD_TERM_REL_ES]) mc = std::max(mc, 2.0 * p.rel_es_screen_dist);
+    // max req_min_dist over contact types (main.cpp:742-746), also the
+    // intended max_formation_min_dist of update_free_pairs
+    double max_form = std::max(p.lj_bb_r_min, p.lj_bs_r_min);
+    for (int k = 0; k < XMD_NUM_SS; ++k) max_form = std::max(max_form, p.ss_r_max[k]);
+    if (p.on[XMD_TERM_QA]) mc = std::max(mc, max_form);
     if (p.nl_cutoff > 0.0) mc = p.nl_cutoff;
     rd.pad = p.nl_skin > 0.0 ? p.nl_skin : p.pad_factor * mc;   // legacy_update.cpp:7-8
     rd.req_r = mc + rd.pad;
     double es_cut = p.on[XMD_TERM_CONST_ES] ? 2.0 * p.const_es_screen_dist : 2.0 * p.rel_es_screen_dist;
     rd.es_min_inv = 1.0 / (es_cut + rd.pad);                      // es_pair.cpp:9
     rd.pauli_min_inv = 1.0 / (p.pauli_r_excl + rd.pad);           // pauli.cpp:12-13
+    rd.qa_min_inv = 1.0 / (max_form + rd.pad);                     // free_pair.cpp:9-10
     rd.noise_sd = std::sqrt(2.0 * 1.0 * r.temperature) * std::sqrt(p.gamma_factor) * 1.0;
     rd.begin = r.begin;
     rd.n = r.n;
@@ -660,6 +775,8 @@ void Engine::finalize() {
         cell_bud[k] = std::max(64, 2 * reps[k].n);
         cells += cell_bud[k];
     }
+    nl_cap = p.nl_capacity > 0 ? p.nl_capacity : 64;
+    auto_grow = p.nl_grow != 0;
     d.N = N;
     d.R = R;
     d.nl_cap = nl_cap;
@@ -690,6 +807,7 @@ void Engine::finalize() {
     d.rep = (RepDev *)dalloc(sizeof(RepDev) * R);
     d.any_rebuild = (int *)dalloc(sizeof(int) * 4);
     d.status = (int *)dalloc(sizeof(int) * 4);
+    d.ctr = (unsigned long long *)dalloc(sizeof(unsigned long long) * 4);
 
     // host staging of the static per-bead data
     std::vector<int32_t> rep_of(N), chain(N), seq(N), nat_start(N + 1, 0);
@@ -698,6 +816,7 @@ void Engine::finalize() {
     std::vector<double> tr(N, 0.0), ar(N, 0.0), dr(N, 0.0);
     std::vector<std::vector<std::pair<int, double>>> nat(N);
     std::vector<RepDev> rd(R);
+    int fp_total = 0, ct_total = 0;
     std::vector<uint64_t> jumps(64 * (size_t)R);
     int chain_base = 0;
     for (int k = 0; k < R; ++k) {
@@ -727,6 +846,14 @@ void Engine::finalize() {
         derive_rep(k, rd[k]);
         rd[k].cell_off = cell_off[k];
         rd[k].cell_budget = cell_bud[k];
+        if (p.on[XMD_TERM_QA]) {
+            rd[k].fp_off = fp_total;
+            rd[k].fp_cap = r.n * QA_FP_PER_BEAD + 256;
+            fp_total += rd[k].fp_cap;
+            rd[k].ct_off = ct_total;
+            rd[k].ct_cap = r.n * QA_CT_PER_BEAD + 256;
+            ct_total += rd[k].ct_cap;
+        }
         GF2 j = gf2_jump(4ull * (uint64_t)r.n);
         std::copy(j.begin(), j.end(), jumps.begin() + 64 * (size_t)k);
     }
@@ -786,7 +913,76 @@ void Engine::finalize() {
     tp.lj_bb_r_min = p.lj_bb_r_min; tp.lj_bb_depth = p.lj_bb_depth;
     tp.lj_bs_r_min = p.lj_bs_r_min; tp.lj_bs_depth = p.lj_bs_depth;
     tp.ss_sinking = p.ss_sinking;
-    if (p.on[XMD_TERM_QA]) throw std::invalid_argument("quasi-adiabatic contacts are not enabled in this build of the engine");
+    if (p.on[XMD_TERM_QA]) {
+        // quasi-adiabatic state: valences start at the residue limits
+        // (intended main.cpp:662-672), tables of main.cpp:681-700 and
+        // lj_variants.cpp:59-62
+        d.qa_on = 1;
+        QaDev &q = d.qa;
+        q.nh = (double *)dalloc(sizeof(double) * 6 * (size_t)N);
+        q.sync = (int32_t *)dalloc(sizeof(int32_t) * N);
+        q.ref_cnt = (int32_t *)dalloc(sizeof(int32_t) * N);
+        q.ref = (int32_t *)dalloc(sizeof(int32_t) * QA_REF_CAP * (size_t)N);
+        q.tmp_cnt = (int32_t *)dalloc(sizeof(int32_t) * N);
+        q.tmp = (int32_t *)dalloc(sizeof(int32_t) * QA_TMP_CAP * (size_t)N);
+        q.fp_total = fp_total;
+        q.ct_total = ct_total;
+        q.fp_i1 = (int32_t *)dalloc(sizeof(int32_t) * fp_total);
+        q.fp_i2 = (int32_t *)dalloc(sizeof(int32_t) * fp_total);
+        q.fp_rep = (int32_t *)dalloc(sizeof(int32_t) * fp_total);
+        q.fp_vac = (uint8_t *)dalloc(fp_total);
+        q.cand_type = (int32_t *)dalloc(sizeof(int32_t) * fp_total);
+        q.cand_d1 = (int32_t *)dalloc(sizeof(int32_t) * fp_total);
+        q.cand_d2 = (int32_t *)dalloc(sizeof(int32_t) * fp_total);
+        q.ct_i1 = (int32_t *)dalloc(sizeof(int32_t) * ct_total);
+        q.ct_i2 = (int32_t *)dalloc(sizeof(int32_t) * ct_total);
+        q.ct_type = (int32_t *)dalloc(sizeof(int32_t) * ct_total);
+        q.ct_d1 = (int32_t *)dalloc(sizeof(int32_t) * ct_total);
+        q.ct_d2 = (int32_t *)dalloc(sizeof(int32_t) * ct_total);
+        q.ct_status = (uint8_t *)dalloc(ct_total);
+        q.ct_vac = (uint8_t *)dalloc(ct_total);
+        q.ct_ref = (double *)dalloc(sizeof(double) * ct_total);
+        std::vector<double> req(4 + XMD_NUM_SS, 0.0), sd(XMD_NUM_SS), smin(XMD_NUM_SS), smax(XMD_NUM_SS);
+        req[1] = p.lj_bb_r_min;
+        req[2] = req[3] = p.lj_bs_r_min;
+        for (int a1 = 0; a1 < XMD_NUM_AA; ++a1)
+            for (int a2 = 0; a2 < XMD_NUM_AA; ++a2)
+                req[4 + a1 + XMD_NUM_AA * a2] = p.ss_r_max[a1 * XMD_NUM_AA + a2];
+        for (int k = 0; k < XMD_NUM_SS; ++k) {
+            sd[k] = p.ss_depth[k];
+            smax[k] = p.ss_r_max[k];
+            smin[k] = p.ss_sinking ? p.lj_bb_r_min : p.ss_r_max[k];
+        }
+        double *t_req = (double *)dalloc(sizeof(double) * req.size());
+        double *t_sd = (double *)dalloc(sizeof(double) * XMD_NUM_SS);
+        double *t_smin = (double *)dalloc(sizeof(double) * XMD_NUM_SS);
+        double *t_smax = (double *)dalloc(sizeof(double) * XMD_NUM_SS);
+        int32_t *t_pt = (int32_t *)dalloc(sizeof(int32_t) * XMD_NUM_AA);
+        CK(cudaMemcpyAsync(t_req, req.data(), sizeof(double) * req.size(), cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(t_sd, sd.data(), sizeof(double) * XMD_NUM_SS, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(t_smin, smin.data(), sizeof(double) * XMD_NUM_SS, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(t_smax, smax.data(), sizeof(double) * XMD_NUM_SS, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(t_pt, p.polarization, sizeof(int32_t) * XMD_NUM_AA, cudaMemcpyHostToDevice, stream));
+        q.req_min_dist = t_req;
+        q.ss_depth = t_sd;
+        q.ss_rmin = t_smin;
+        q.ss_rmax = t_smax;
+        q.ptype = t_pt;
+        q.min_cos_hr = p.qa_min_cos_hr;
+        q.min_cos_hh = p.qa_min_cos_hh;
+        q.max_cos_nr = p.qa_max_cos_nr;
+        std::vector<int32_t> fprep(fp_total);
+        for (int k = 0; k < R; ++k)
+            for (int s = 0; s < rd[k].fp_cap; ++s) fprep[rd[k].fp_off + s] = k;
+        CK(cudaMemcpyAsync(q.fp_rep, fprep.data(), sizeof(int32_t) * fp_total, cudaMemcpyHostToDevice, stream));
+        std::vector<int32_t> sy(N);
+        for (int i = 0; i < N; ++i) {
+            const int32_t *lim = p.limits[at[i]];
+            sy[i] = (lim[0] & 0xff) | ((lim[1] & 0xff) << 8) | ((lim[2] & 0xff) << 16) | ((lim[3] & 0xff) << 24);
+        }
+        CK(cudaMemcpyAsync(q.sync, sy.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, stream));
+        CK(cudaStreamSynchronize(stream));
+    }
 
     finalized = true;
     for (int k = 0; k < R; ++k) upload_state(k);
@@ -921,16 +1117,178 @@ void Engine::get_history(int rep, double *y, double *t, uint64_t *rngs) {
     if (rngs) *rngs = s0;
 }
 
+void Engine::use_device() const { CK(cudaSetDevice(device)); }
+
+void Engine::record(std::vector<cudaEvent_t> &pool, size_t &n) {
+    if (n >= pool.size()) {
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        pool.push_back(e);
+    }
+    CK(cudaEventRecord(pool[n++], stream));
+}
+
 void Engine::launch_rebuild() {
+    if (timing) record(ev_rebuild, n_ev_rebuild);
     k_cells<<<d.R, CB, 0, stream>>>(d, cur);
     k_nl_build<<<(d.N + 127) / 128, 128, 0, stream>>>(d, tp, cur);
+    if (d.qa_on) k_qa_rebuild<<<d.R, 1024, 0, stream>>>(d);
+    if (timing) record(ev_rebuild, n_ev_rebuild);
+}
+
+// Grow the Verlet rows when the longest row needed (recorded by k_nl_build)
+// reaches `frac` of the capacity.  Returns true when the rows were
+// reallocated (lists must then be rebuilt; captured graphs are dropped).
+bool Engine::grow_rows(double frac) {
+    unsigned long long need = 0;
+    CK(cudaMemcpyAsync(&need, d.ctr + 1, sizeof(need), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    if ((double)need < frac * nl_cap) return false;
+    int ncap = (int)(need + need / 2 + 8);
+    int32_t *rows = nullptr;
+    CK(cudaMalloc(&rows, sizeof(int32_t) * (size_t)ncap * d.N));
+    for (auto &a : allocs)
+        if (a == (void *)d.nl_row) {
+            CK(cudaFree(a));
+            a = rows;
+        }
+    d.nl_row = rows;
+    d.nl_cap = nl_cap = ncap;
+    drop_graphs();
+    return true;
+}
+
+void Engine::drop_graphs() {
+    for (auto &row : graphs)
+        for (auto &g : row) {
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+            if (g.graph) cudaGraphDestroy(g.graph);
+            g.exec = nullptr;
+            g.graph = nullptr;
+        }
 }
 
 void Engine::ensure_nl() {
-    k_nl_check<<<1, 1024, 0, stream>>>(d, 0, 0.0);
-    CK(cudaMemcpyAsync(h_any, d.any_rebuild, sizeof(int), cudaMemcpyDeviceToHost, stream));
-    CK(cudaStreamSynchronize(stream));
-    if (*h_any) launch_rebuild();
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        k_nl_check<<<1, 1024, 0, stream>>>(d, 0, 0.0, (cudaGraphConditionalHandle)0, 0);
+        ++launches;
+        CK(cudaMemcpyAsync(h_any, d.any_rebuild, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        if (*h_any) launch_rebuild();
+        int st = 0;
+        CK(cudaMemcpyAsync(&st, d.status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        if (!(st & ST_CAPACITY) || !auto_grow) {
+            if (auto_grow) grow_rows(0.75);   // keep headroom for the run ahead
+            return;
+        }
+        // rows overflowed at this rebuild: grow, clear the flag, rebuild all
+        if (!grow_rows(0.0)) return;
+        CK(cudaMemsetAsync(d.status, 0, sizeof(int), stream));
+        k_mark_all<<<(d.R + 255) / 256, 256, 0, stream>>>(d);
+    }
+}
+
+void Engine::launch_force_step() {
+    int nb = (d.N + FB - 1) / FB;
+    if (timing) record(ev_force, n_ev_force);
+    if (params.precision == XMD_PREC_MIXED) k_force<float, 1><<<nb, FB, 0, stream>>>(d, tp, cur);
+    else k_force<double, 1><<<nb, FB, 0, stream>>>(d, tp, cur);
+    if (timing) record(ev_force, n_ev_force);
+    ++launches;
+    if (d.qa_on) {
+        // sift + acceptance + transitions at this step's positions (qa.cpp:20-31)
+        k_qa_sift<<<(d.qa.fp_total + 255) / 256, 256, 0, stream>>>(d, tp, cur);
+        k_qa_step<<<d.R, 1024, 0, stream>>>(d, tp, cur);
+        launches += 2;
+    }
+}
+
+// One graph runs GRAPH_STEPS steps: per step a force+integrate node, a skin
+// check that sets a conditional handle on the device, and an IF node whose
+// body rebuilds the lists of the flagged replicas (cells, then rows).  An
+// even step count leaves the position double buffer where it started.
+cudaGraphExec_t Engine::graph_for(int start_cur) {
+    GraphSet &gs = graphs[params.precision == XMD_PREC_MIXED][start_cur];
+    if (gs.exec) return gs.exec;
+    cudaGraph_t g;
+    CK(cudaGraphCreate(&g, 0));
+    cudaGraphNode_t prev = nullptr;
+    const int nb = (d.N + FB - 1) / FB;
+    void *fk = params.precision == XMD_PREC_MIXED ? (void *)k_force<float, 1> : (void *)k_force<double, 1>;
+    double dt = params.dt;
+    for (int s = 0; s < GRAPH_STEPS; ++s) {
+        int c = start_cur ^ (s & 1), cn = c ^ 1;
+        int adv = 1, setc = 1;
+        cudaKernelNodeParams kf{};
+        void *fargs[] = {&d, &tp, &c};
+        kf.func = fk;
+        kf.gridDim = dim3(nb);
+        kf.blockDim = dim3(FB);
+        kf.kernelParams = fargs;
+        cudaGraphNode_t nf, nc, ncond;
+        CK(cudaGraphAddKernelNode(&nf, g, prev ? &prev : nullptr, prev ? 1 : 0, &kf));
+        if (d.qa_on) {
+            cudaKernelNodeParams ks{}, kq{};
+            void *sargs[] = {&d, &tp, &c};
+            ks.func = (void *)k_qa_sift;
+            ks.gridDim = dim3((d.qa.fp_total + 255) / 256);
+            ks.blockDim = dim3(256);
+            ks.kernelParams = sargs;
+            kq.func = (void *)k_qa_step;
+            kq.gridDim = dim3(d.R);
+            kq.blockDim = dim3(1024);
+            kq.kernelParams = sargs;
+            cudaGraphNode_t n1, n2;
+            CK(cudaGraphAddKernelNode(&n1, g, &nf, 1, &ks));
+            CK(cudaGraphAddKernelNode(&n2, g, &n1, 1, &kq));
+            nf = n2;
+        }
+        cudaGraphConditionalHandle h;
+        CK(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
+        cudaKernelNodeParams kc{};
+        void *cargs[] = {&d, &adv, &dt, &h, &setc};
+        kc.func = (void *)k_nl_check;
+        kc.gridDim = dim3(1);
+        kc.blockDim = dim3(1024);
+        kc.kernelParams = cargs;
+        CK(cudaGraphAddKernelNode(&nc, g, &nf, 1, &kc));
+        cudaGraphNodeParams cp{};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeIf;
+        cp.conditional.size = 1;
+        CK(cudaGraphAddNode(&ncond, g, &nc, nullptr, 1, &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        cudaKernelNodeParams k1{}, k2{};
+        void *a1[] = {&d, &cn};
+        k1.func = (void *)k_cells;
+        k1.gridDim = dim3(d.R);
+        k1.blockDim = dim3(CB);
+        k1.kernelParams = a1;
+        void *a2[] = {&d, &tp, &cn};
+        k2.func = (void *)k_nl_build;
+        k2.gridDim = dim3((d.N + 127) / 128);
+        k2.blockDim = dim3(128);
+        k2.kernelParams = a2;
+        cudaGraphNode_t b1, b2;
+        CK(cudaGraphAddKernelNode(&b1, body, nullptr, 0, &k1));
+        CK(cudaGraphAddKernelNode(&b2, body, &b1, 1, &k2));
+        if (d.qa_on) {
+            cudaKernelNodeParams k3{};
+            void *a3[] = {&d};
+            k3.func = (void *)k_qa_rebuild;
+            k3.gridDim = dim3(d.R);
+            k3.blockDim = dim3(1024);
+            k3.kernelParams = a3;
+            cudaGraphNode_t b3;
+            CK(cudaGraphAddKernelNode(&b3, body, &b2, 1, &k3));
+        }
+        prev = ncond;
+    }
+    CK(cudaGraphInstantiate(&gs.exec, g, 0));
+    gs.graph = g;
+    return gs.exec;
 }
 
 void Engine::check_status(const char *where) {
@@ -960,20 +1318,183 @@ void Engine::eval_forces(int rep, double *F, double *V) {
 }
 
 void Engine::step(int nsteps) {
+    use_device();
     finalize();
     if (!params.langevin_on) throw std::invalid_argument("langevin: enabled is false; nothing integrates");
     ensure_nl();
-    int nb = (d.N + FB - 1) / FB;
-    for (int s = 0; s < nsteps; ++s) {
-        if (params.precision == XMD_PREC_MIXED) k_force<float, 1><<<nb, FB, 0, stream>>>(d, tp, cur);
-        else k_force<double, 1><<<nb, FB, 0, stream>>>(d, tp, cur);
+    int s = 0;
+    if (!timing && use_graphs) {
+        for (; s + GRAPH_STEPS <= nsteps; s += GRAPH_STEPS) {
+            CK(cudaGraphLaunch(graph_for(cur), stream));
+            // per step: force, check, and (when taken) two rebuild kernels
+            launches += 2 * GRAPH_STEPS;
+            md_steps += GRAPH_STEPS;
+        }
+    }
+    for (; s < nsteps; ++s) {
+        launch_force_step();
         cur ^= 1;
-        k_nl_check<<<1, 1024, 0, stream>>>(d, 1, params.dt);
+        k_nl_check<<<1, 1024, 0, stream>>>(d, 1, params.dt, (cudaGraphConditionalHandle)0, 0);
+        ++launches;
+        ++md_steps;
         CK(cudaMemcpyAsync(h_any, d.any_rebuild, sizeof(int), cudaMemcpyDeviceToHost, stream));
         CK(cudaStreamSynchronize(stream));
         if (*h_any) launch_rebuild();
     }
     check_status("step");
+    if (auto_grow && grow_rows(0.75)) k_mark_all<<<(d.R + 255) / 256, 256, 0, stream>>>(d);
+}
+
+// ---- packed host-buffer path ----------------------------------------------------
+__global__ void k_unpack_history(Dev d, const double *__restrict__ y, int cur) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.N) return;
+    const size_t n3 = 3 * (size_t)d.N;
+    double4_32a p = d.pos[cur][i];
+    p.x = y[3 * (size_t)i];
+    p.y = y[3 * (size_t)i + 1];
+    p.z = y[3 * (size_t)i + 2];
+    d.pos[cur][i] = p;
+    for (int ord = 1; ord < 6; ++ord)
+        for (int a = 0; a < 3; ++a)
+            d.yh[(size_t)((ord - 1) * 3 + a) * d.N + i] = y[ord * n3 + 3 * (size_t)i + a];
+    // the skin test sees the new positions like any other displacement
+    int r = d.rep_of[i];
+    double disp = dist_exact(d.rep[r].box, p, d.orig[i]);
+    atomicMax(&d.rep[r].maxdisp, (unsigned long long)__double_as_longlong(disp));
+}
+__global__ void k_pack_positions(Dev d, double *__restrict__ r, int cur) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.N) return;
+    double4_32a p = d.pos[cur][i];
+    r[3 * (size_t)i] = p.x;
+    r[3 * (size_t)i + 1] = p.y;
+    r[3 * (size_t)i + 2] = p.z;
+}
+
+void Engine::upload_history_all(const double *y) {
+    use_device();
+    finalize();
+    if (!staging) staging = (double *)dalloc(sizeof(double) * 18 * (size_t)d.N);
+    CK(cudaMemcpyAsync(staging, y, sizeof(double) * 18 * (size_t)d.N, cudaMemcpyHostToDevice, stream));
+    k_unpack_history<<<(d.N + 255) / 256, 256, 0, stream>>>(d, staging, cur);
+    ++launches;
+}
+
+void Engine::download_positions_all(double *r) {
+    use_device();
+    finalize();
+    if (!staging) staging = (double *)dalloc(sizeof(double) * 18 * (size_t)d.N);
+    k_pack_positions<<<(d.N + 255) / 256, 256, 0, stream>>>(d, staging, cur);
+    ++launches;
+    CK(cudaMemcpyAsync(r, staging, sizeof(double) * 3 * (size_t)d.N, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+}
+
+void Engine::stats(int64_t *out) {
+    use_device();
+    for (int k = 0; k < XMD_NUM_STATS; ++k) out[k] = 0;
+    int64_t nb = 0;
+    for (auto &r : reps) nb += r.n;
+    out[XMD_STAT_BEADS] = nb;
+    out[XMD_STAT_REPLICAS] = (int64_t)reps.size();
+    out[XMD_STAT_LAUNCHES] = launches;
+    out[XMD_STAT_MD_STEPS] = md_steps;
+    if (!finalized) return;
+    std::vector<int32_t> cnt(d.N);
+    CK(cudaMemcpyAsync(cnt.data(), d.nl_cnt, sizeof(int32_t) * d.N, cudaMemcpyDeviceToHost, stream));
+    int32_t nn = 0;
+    CK(cudaMemcpyAsync(&nn, d.nat_start + d.N, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    std::vector<uint8_t> on(nn > 0 ? nn : 1);
+    if (nn) CK(cudaMemcpyAsync(on.data(), d.nat_on, nn, cudaMemcpyDeviceToHost, stream));
+    std::vector<RepDev> rd(d.R);
+    CK(cudaMemcpyAsync(rd.data(), d.rep, sizeof(RepDev) * d.R, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    unsigned long long passes = 0;
+    CK(cudaMemcpyAsync(&passes, d.ctr, sizeof(passes), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    out[XMD_STAT_LAUNCHES] = launches + 2 * (int64_t)passes;   // k_cells + k_nl_build per pass
+    for (int32_t c : cnt) out[XMD_STAT_NL_ENTRIES] += c;
+    for (int k = 0; k < nn; ++k) out[XMD_STAT_GO_ACTIVE] += on[k];
+    for (auto &r : rd) out[XMD_STAT_REBUILDS] += (int64_t)r.rebuilds;
+}
+
+int Engine::qa_contacts(int rep, int cap, int32_t *out4, double *ref_time) {
+    check_rep(reps, rep);
+    finalize();
+    if (!d.qa_on) return 0;
+    RepDev rd;
+    CK(cudaMemcpyAsync(&rd, d.rep + rep, sizeof(RepDev), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    int n = rd.ct_n, o = rd.ct_off;
+    std::vector<int32_t> i1(n), i2(n), ty(n);
+    std::vector<uint8_t> st(n), vac(n);
+    std::vector<double> rf(n);
+    if (n) {
+        CK(cudaMemcpyAsync(i1.data(), d.qa.ct_i1 + o, 4 * n, cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(i2.data(), d.qa.ct_i2 + o, 4 * n, cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(ty.data(), d.qa.ct_type + o, 4 * n, cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(st.data(), d.qa.ct_status + o, n, cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(vac.data(), d.qa.ct_vac + o, n, cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(rf.data(), d.qa.ct_ref + o, 8 * n, cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+    }
+    int m = 0;
+    const int b = reps[rep].begin;
+    for (int k = 0; k < n; ++k) {
+        if (vac[k]) continue;
+        if (m < cap) {
+            if (out4) {
+                out4[4 * m] = i1[k] - b; out4[4 * m + 1] = i2[k] - b;
+                out4[4 * m + 2] = ty[k]; out4[4 * m + 3] = st[k];
+            }
+            if (ref_time) ref_time[m] = rf[k];
+        }
+        ++m;
+    }
+    return m;
+}
+
+void Engine::qa_sync(int rep, int8_t *out) {
+    check_rep(reps, rep);
+    finalize();
+    const RepHost &h = reps[rep];
+    if (!d.qa_on) {
+        for (int i = 0; i < h.n; ++i)
+            for (int k = 0; k < 4; ++k) out[4 * i + k] = (int8_t)params.limits[h.atype[i]][k];
+        return;
+    }
+    std::vector<int32_t> s(h.n);
+    CK(cudaMemcpyAsync(s.data(), d.qa.sync + h.begin, 4 * (size_t)h.n, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    for (int i = 0; i < h.n; ++i)
+        for (int k = 0; k < 4; ++k) out[4 * i + k] = (int8_t)((s[i] >> (8 * k)) & 0xff);
+}
+
+void Engine::set_kernel_timing(bool on) {
+    timing = on;
+    n_ev_force = n_ev_rebuild = 0;
+}
+
+void Engine::kernel_times(double *force_ms, int64_t *nf, double *rebuild_ms, int64_t *nr) {
+    use_device();
+    CK(cudaStreamSynchronize(stream));
+    double f = 0, r = 0;
+    for (size_t k = 0; k + 1 < n_ev_force; k += 2) {
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, ev_force[k], ev_force[k + 1]));
+        f += ms;
+    }
+    for (size_t k = 0; k + 1 < n_ev_rebuild; k += 2) {
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, ev_rebuild[k], ev_rebuild[k + 1]));
+        r += ms;
+    }
+    if (force_ms) *force_ms = f;
+    if (nf) *nf = (int64_t)(n_ev_force / 2);
+    if (rebuild_ms) *rebuild_ms = r;
+    if (nr) *nr = (int64_t)(n_ev_rebuild / 2);
 }
 
 void Engine::observables(int rep, double *E, double *K, double *Rg, double *Q) {

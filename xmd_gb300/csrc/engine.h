@@ -34,6 +34,34 @@ struct RepDev {
     int first, rebuild;
     unsigned long long maxdisp;
     unsigned long long rebuilds;
+    // quasi-adiabatic lists: free pairs [fp_off, fp_off + fp_n) of capacity
+    // fp_cap, contacts [ct_off, ct_off + ct_n) of capacity ct_cap
+    int fp_off, fp_cap, fp_n;
+    int ct_off, ct_cap, ct_n;
+};
+
+constexpr int QA_REF_CAP = 16;   // contacts per bead (valence bounds it by 10)
+constexpr int QA_TMP_CAP = 128;  // free-pair partners j > i per bead at a rebuild
+constexpr int QA_FP_PER_BEAD = 96;   // free-pair slots per bead of a replica (+256)
+constexpr int QA_CT_PER_BEAD = 8;    // contact slots per bead of a replica (+256)
+
+// device record of the quasi-adiabatic state
+struct QaDev {
+    double *nh;                  // [6][N]: n then h (precompute_nh.cpp:12-20)
+    int32_t *sync;               // [N] packed int8 x4: back | side_all | side_polar | side_hydrophobic
+    int32_t *ref_cnt, *ref;      // [N], [QA_REF_CAP][N] contact slots per bead
+    int32_t *tmp_cnt, *tmp;      // [N], [QA_TMP_CAP][N] partners collected at a rebuild
+    int32_t *fp_i1, *fp_i2, *fp_rep;   // free-pair slots
+    uint8_t *fp_vac;
+    int32_t *cand_type, *cand_d1, *cand_d2;   // per free-pair slot, 0 = not a candidate
+    int32_t *ct_i1, *ct_i2, *ct_type, *ct_d1, *ct_d2;
+    uint8_t *ct_status, *ct_vac;
+    double *ct_ref;
+    const double *req_min_dist;  // [404] by contact type (main.cpp:681-697)
+    const double *ss_depth, *ss_rmin, *ss_rmax;   // [400] ss potentials (lj_variants.cpp)
+    const int32_t *ptype;        // [20] polarization
+    int fp_total, ct_total;
+    double min_cos_hr, min_cos_hh, max_cos_nr;
 };
 
 // everything a kernel needs, passed by value
@@ -59,6 +87,9 @@ struct Dev {
     RepDev *rep;
     int *any_rebuild;
     int *status;            // device error word
+    unsigned long long *ctr;  // [0]: list-rebuild passes launched
+    int qa_on;
+    QaDev qa;
 };
 
 struct RepHost {
@@ -103,15 +134,45 @@ public:
     void observables(int rep, double *E, double *K, double *Rg, double *Q);
     int device_status();
     void sync();
+    void upload_history_all(const double *y);
+    void download_positions_all(double *r);
+    cudaStream_t get_stream() const { return stream; }
+    void stats(int64_t *out);
+    void set_kernel_timing(bool on);
+    int qa_contacts(int rep, int cap, int32_t *out4, double *ref_time);
+    void qa_sync(int rep, int8_t *out);
+    void kernel_times(double *force_ms, int64_t *nf, double *rebuild_ms, int64_t *nr);
+    void use_device() const;
 
 private:
     Dev d{};
     int cur = 0;                 // which pos buffer is current
+    int device = 0;
     cudaStream_t stream = nullptr;
     std::vector<void *> allocs;
     int *h_any = nullptr;        // pinned
     TermP tp{};
-    std::vector<double> max_cutoff_r;
+    int64_t launches = 0, md_steps = 0;
+    double *staging = nullptr;   // packed host-layout buffer [18 N]
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_force, ev_rebuild;   // start/stop pairs
+    size_t n_ev_force = 0, n_ev_rebuild = 0;
+
+    void record(std::vector<cudaEvent_t> &pool, size_t &n);
+    void launch_force_step();
+
+    // graph-captured step chunks, per precision and starting buffer
+    static constexpr int GRAPH_STEPS = 16;
+    struct GraphSet {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+    };
+    GraphSet graphs[2][2];
+    bool use_graphs = true;
+    bool auto_grow = true;       // grow Verlet rows instead of failing
+    cudaGraphExec_t graph_for(int start_cur);
+    bool grow_rows(double frac);
+    void drop_graphs();
 
     void *dalloc(size_t bytes);
     void finalize();

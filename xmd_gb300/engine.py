@@ -105,6 +105,25 @@ class Engine:
         check(self.lib.xmd_gpu_observables(self.h, rep, C.byref(E), C.byref(K), C.byref(Rg), C.byref(Q)))
         return {"E": E.value, "K": K.value, "Rg": Rg.value, "Q": Q.value}
 
+    def qa_contacts(self, rep: int = 0, cap: int = 1 << 20):
+        out = np.zeros(4 * cap, dtype=np.int32)
+        rt = np.zeros(cap)
+        m = C.c_int32()
+        check(self.lib.xmd_gpu_qa_contacts(self.h, rep, cap, iptr(out), dptr(rt), C.byref(m)))
+        k = min(m.value, cap)
+        return out[:4 * k].reshape(k, 4), rt[:k]
+
+    def qa_sync(self, rep: int = 0):
+        out = np.zeros(4 * self.sizes[rep], dtype=np.int8)
+        check(self.lib.xmd_gpu_qa_sync(self.h, rep, out.ctypes.data_as(C.POINTER(C.c_int8))))
+        return out.reshape(-1, 4)
+
+    def stats(self) -> dict:
+        out = np.zeros(8, dtype=np.int64)
+        check(self.lib.xmd_gpu_stats(self.h, out.ctypes.data_as(C.POINTER(C.c_int64))))
+        keys = ["beads", "replicas", "nl_entries", "go_active", "rebuilds", "launches", "qa_contacts", "md_steps"]
+        return dict(zip(keys, out.tolist()))
+
     def device_status(self) -> int:
         s = C.c_int32()
         check(self.lib.xmd_gpu_device_status(self.h, C.byref(s)))

@@ -69,52 +69,66 @@ def _sphere(rng):
     return _unit(v)
 
 
-def saw_chain(rng, n, bond, start, min_sep=4.0 * ANGSTROM, tries=20, others=None):
-    """A persistent random walk as in morph_into_saw with overlap rejection."""
+def saw_chain(rng, n, bond, start, min_sep=4.0 * ANGSTROM, tries=16, others=None):
+    """A persistent random walk as in morph_into_saw with overlap rejection:
+    each step turns the direction by a spread angle about perp_v(dir) and an
+    around angle about dir; `tries` turns are drawn at once and the first
+    whose bead keeps min_sep from earlier beads is taken (else the best)."""
     max_spread, max_around = math.pi / 12.0, math.pi
     pos = np.empty((n, 3))
     pos[0] = start
     d = _sphere(rng)
     for k in range(1, n):
-        best, best_d = None, -1.0
-        for _ in range(tries):
-            sp = rng.uniform(-max_spread, max_spread)
-            ar = rng.uniform(-max_around, max_around)
-            nd = _unit(_rot(_rot(d, _perp(d), sp), d, ar))
-            cand = pos[k - 1] + bond * nd
-            if k >= 3:
-                dmin = np.min(np.linalg.norm(pos[:k - 2] - cand, axis=1))
-            else:
-                dmin = np.inf
-            if others is not None and len(others):
-                dmin = min(dmin, np.min(np.linalg.norm(others - cand, axis=1)))
-            if dmin >= min_sep:
-                best = (cand, nd)
-                break
-            if dmin > best_d:
-                best_d, best = dmin, (cand, nd)
-        pos[k], d = best
+        sp = rng.uniform(-max_spread, max_spread, size=tries)[:, None]
+        ar = rng.uniform(-max_around, max_around, size=tries)[:, None]
+        p = _perp(d)
+        # Rodrigues rotations (p is perpendicular to d)
+        v1 = d * np.cos(sp) + np.cross(p, d) * np.sin(sp)
+        dv = (v1 * d).sum(axis=1, keepdims=True)
+        v2 = v1 * np.cos(ar) + np.cross(d, v1) * np.sin(ar) + d * dv * (1.0 - np.cos(ar))
+        v2 /= np.linalg.norm(v2, axis=1, keepdims=True)
+        cand = pos[k - 1] + bond * v2
+        dmin = np.full(tries, np.inf)
+        if k >= 3:
+            dmin = np.sqrt(((cand[:, None, :] - pos[None, :k - 2, :]) ** 2).sum(axis=2).min(axis=1))
+        if others is not None and len(others):
+            do = np.sqrt(((cand[:, None, :] - others[None, :, :]) ** 2).sum(axis=2).min(axis=1))
+            dmin = np.minimum(dmin, do)
+        ok = np.nonzero(dmin >= min_sep)[0]
+        pick = ok[0] if len(ok) else int(np.argmax(dmin))
+        pos[k], d = cand[pick], v2[pick]
     return pos
 
 
-def compact_walk(rng, n, bond, density=1.0 / 120.0, min_sep=4.2 * ANGSTROM, tries=60):
+def compact_walk(rng, n, bond, density=1.0 / 120.0, min_sep=4.2 * ANGSTROM, tries=48):
     """A random walk confined to a sphere holding n beads at `density` (per A^3),
-    with overlap rejection: the native conformation of one chain."""
+    with overlap rejection: the native conformation of one chain.  Each step
+    draws `tries` candidate directions at once and keeps the first admissible
+    one (else the least bad)."""
     radius = (3.0 * n / (4.0 * math.pi * density)) ** (1.0 / 3.0) * ANGSTROM
     radius = max(radius, 2.0 * bond)
     pos = np.zeros((n, 3))
+    batch = 8
     for k in range(1, n):
         best, best_score = None, -np.inf
-        for _ in range(tries):
-            cand = pos[k - 1] + bond * _sphere(rng)
-            dmin = np.min(np.linalg.norm(pos[:k - 1] - cand, axis=1)) if k >= 2 else np.inf
-            out = max(0.0, np.linalg.norm(cand) - radius)
-            score = min(dmin - min_sep, 0.0) - out
-            if score >= 0.0:
-                best = cand
+        for _ in range(0, tries, batch):
+            dirs = rng.normal(size=(batch, 3))
+            dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+            cand = pos[k - 1] + bond * dirs
+            if k >= 2:
+                d2 = ((cand[:, None, :] - pos[None, :k - 1, :]) ** 2).sum(axis=2)
+                dmin = np.sqrt(d2.min(axis=1))
+            else:
+                dmin = np.full(batch, np.inf)
+            out = np.maximum(0.0, np.linalg.norm(cand, axis=1) - radius)
+            score = np.minimum(dmin - min_sep, 0.0) - out
+            ok = np.nonzero(score >= 0.0)[0]
+            if len(ok):
+                best = cand[ok[0]]
                 break
-            if score > best_score:
-                best_score, best = score, cand
+            j = int(np.argmax(score))
+            if score[j] > best_score:
+                best_score, best = score[j], cand[j]
         pos[k] = best
     return pos
 
@@ -122,22 +136,16 @@ def compact_walk(rng, n, bond, density=1.0 / 120.0, min_sep=4.2 * ANGSTROM, trie
 def bonded_natives(pos):
     """Native angles and dihedrals of one chain, with the force terms'
     conventions (angle/native.cpp:20-30, dihedral/complex_native.cpp:20-28)."""
-    n = len(pos)
-    th = []
-    for c in range(1, n - 1):
-        r12, r23 = pos[c] - pos[c - 1], pos[c + 1] - pos[c]
-        ct = -np.dot(r12, r23) / (np.linalg.norm(r12) * np.linalg.norm(r23))
-        th.append(math.acos(max(-1.0, min(1.0, ct))))
-    ph = []
-    for c in range(1, n - 2):
-        r12, r23, r34 = pos[c] - pos[c - 1], pos[c + 1] - pos[c], pos[c + 2] - pos[c + 1]
-        x1, x2 = np.cross(r12, r23), np.cross(r23, r34)
-        cp = np.dot(x1, x2) / (np.linalg.norm(x1) * np.linalg.norm(x2))
-        p = math.acos(max(-1.0, min(1.0, cp)))
-        if np.dot(x1, r34) < 0:
-            p = -p
-        ph.append(p)
-    return np.array(th), np.array(ph)
+    b = pos[1:] - pos[:-1]                      # bond vectors
+    r12, r23 = b[:-1], b[1:]
+    ct = -(r12 * r23).sum(axis=1) / (np.linalg.norm(r12, axis=1) * np.linalg.norm(r23, axis=1))
+    th = np.arccos(np.clip(ct, -1.0, 1.0))
+    r12, r23, r34 = b[:-2], b[1:-1], b[2:]
+    x1, x2 = np.cross(r12, r23), np.cross(r23, r34)
+    cp = (x1 * x2).sum(axis=1) / (np.linalg.norm(x1, axis=1) * np.linalg.norm(x2, axis=1))
+    ph = np.arccos(np.clip(cp, -1.0, 1.0))
+    ph = np.where((x1 * r34).sum(axis=1) < 0, -ph, ph)
+    return th, ph
 
 
 def native_map(pos, cutoff=7.5 * ANGSTROM, min_sep=3):
@@ -162,9 +170,13 @@ def _types(rng, n, mode):
 
 
 def make_system(chain_lengths, seed, box=None, density=1e-3, types="charged10",
-                bond=3.8 * ANGSTROM, native=True, temperature=0.0, rng_seed=None):
+                bond=3.8 * ANGSTROM, native=True, temperature=0.0, rng_seed=None, start="saw"):
     """Build one replica.  box: edge in internal units (periodic cube) or None
-    for open boundaries; density (per A^3) sizes the starting cube."""
+    for open boundaries; density (per A^3) sizes the starting cube.
+    start="saw" begins from the extended walk (far from the native structure,
+    as the benchmark configurations specify); start="native" places each chain
+    in its native conformation, translated to its random start point (a start
+    near equilibrium, where the dynamics does not amplify rounding)."""
     rng = np.random.default_rng(seed)
     lens = [int(x) for x in chain_lengths]
     n = sum(lens)
@@ -182,15 +194,17 @@ def make_system(chain_lengths, seed, box=None, density=1e-3, types="charged10",
     nat = ([], [], [])
     off = 0
     for c, L in enumerate(lens):
-        start = rng.uniform(-a / 2.0, a / 2.0, size=3)
+        start_pt = rng.uniform(-a / 2.0, a / 2.0, size=3)
         others = r[max(0, off - 2000):off] if off else None
-        r[off:off + L] = saw_chain(rng, L, bond, start, others=others)
+        r[off:off + L] = saw_chain(rng, L, bond, start_pt, others=others)
         if L >= 2:
             tet_i1 += list(range(off, off + L - 1))
             tet_i2 += list(range(off + 1, off + L))
             tet_d += [bond] * (L - 1)
         if native and L >= 3:
             npos = compact_walk(rng, L, bond)
+            if start == "native":
+                r[off:off + L] = npos - npos.mean(axis=0) + start_pt
             th, ph = bonded_natives(npos)
             for k, t in enumerate(th):
                 ang[0].append(off + k); ang[1].append(off + k + 1); ang[2].append(off + k + 2); ang[3].append(t)
@@ -292,10 +306,23 @@ def c4_lengths(seed=4, count=256, lo=50, hi=800):
     return np.floor(np.exp(rng.uniform(math.log(lo), math.log(hi), size=count))).astype(int)
 
 
-def config_c4(seed=4, count=256):
+def _c4_one(args):
+    seed, k, L, T = args
+    return make_system([int(L)], seed * 100003 + k, box=None, types="charged10",
+                       temperature=float(T), rng_seed=seed * 7 + k * 131)
+
+
+def config_c4(seed=4, count=256, workers=0):
+    """256 single-chain replicas, lengths log-uniform in [50, 800], per-replica
+    temperature uniform in [0.3, 0.6].  workers > 1 generates them in a spawned
+    process pool (same systems, same order)."""
     lens = c4_lengths(seed, count)
     rng = np.random.default_rng(seed + 1000)
     temps = rng.uniform(0.3, 0.6, size=count)
-    return [make_system([int(L)], seed * 100003 + k, box=None, types="charged10",
-                        temperature=float(temps[k]), rng_seed=seed * 7 + k * 131)
-            for k, L in enumerate(lens)]
+    jobs = [(seed, k, int(L), float(temps[k])) for k, L in enumerate(lens)]
+    if workers and workers > 1:
+        import multiprocessing as mp
+        from concurrent.futures import ProcessPoolExecutor
+        with ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+            return list(ex.map(_c4_one, jobs, chunksize=4))
+    return [_c4_one(j) for j in jobs]
