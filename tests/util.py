@@ -16,13 +16,28 @@ ANGSTROM = 0.2
 def horizon_snapshot(z):
     """(steps, y[6,n,3], rng_state) of the fixture's last snapshot inside its
     parity horizon: the step count up to which the oracle agrees with itself
-    under a reordered force summation to 1e-9 A (beyond it the dynamics
+    under a reordered force summation to 1e-11 A (beyond it the dynamics
     amplifies rounding, so no two FP64 implementations stay within 1e-8 A)."""
     h = int(z["parity_steps"])
     if h >= int(z["steps"]):
         return int(z["steps"]), z["y"], int(z["rng"])
-    best = max(k for k in (100, 200) if k <= max(h, 100))
+    best = max(k for k in (50, 100, 200) if k <= max(h, 50))
     return best, z[f"y_{best}"], int(z[f"rng_{best}"])
+
+
+def cudart():
+    """ctypes handle on the CUDA runtime the engine library already mapped."""
+    import ctypes
+
+    from xmd_gb300 import abi
+    abi.load()
+    path = None
+    with open("/proc/self/maps") as f:
+        for line in f:
+            if "libcudart.so" in line:
+                path = line.split()[-1]
+                break
+    return ctypes.CDLL(path or "libcudart.so")
 
 
 def load_golden(name: str):

@@ -92,6 +92,7 @@ SIGNATURES = [
     ("xmd_gpu_device_status", C.c_int, [C.c_void_p, _pi32]),
     ("xmd_gpu_qa_contacts", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _pi32, _pd, _pi32]),
     ("xmd_gpu_qa_sync", C.c_int, [C.c_void_p, C.c_int32, P(C.c_int8)]),
+    ("xmd_gpu_verlet_pairs", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _pi32, _pu8, _pi32]),
     ("xmd_gpu_upload_history_all", C.c_int, [C.c_void_p, _pd]),
     ("xmd_gpu_download_positions_all", C.c_int, [C.c_void_p, _pd]),
     ("xmd_gpu_get_stream", C.c_int, [C.c_void_p, P(C.c_void_p)]),

@@ -262,6 +262,17 @@ int xmd_gpu_qa_contacts(xmd_gpu_ctx *ctx, int32_t rep, int32_t cap, int32_t *out
     });
 }
 
+int xmd_gpu_verlet_pairs(xmd_gpu_ctx *ctx, int32_t rep, int32_t cap, int32_t *out2, uint8_t *flags,
+                         int32_t *count) {
+    NEED_CTX;
+    if (cap < 0 || (cap > 0 && !out2)) return fail(XMD_ERR_ARG, "bad output buffer");
+    return guard([&] {
+        ctx->eng->use_device();
+        int m = ctx->eng->verlet_pairs(rep, cap, out2, flags);
+        if (count) *count = m;
+    });
+}
+
 int xmd_gpu_qa_sync(xmd_gpu_ctx *ctx, int32_t rep, int8_t *out) {
     NEED_CTX;
     if (!out) return fail(XMD_ERR_ARG, "null output");

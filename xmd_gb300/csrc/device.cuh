@@ -69,15 +69,25 @@ __device__ __forceinline__ V3<T> r_uv(const BoxD &b, double4_32a u, double4_32a 
     return V3<T>{T(dx), T(dy), T(dz)};
 }
 
+// box::r_uv for a replica that may be open on every axis: there the wrap
+// subtracts exactly 0 * rint(0), so skipping it changes no bit.
+template <class T>
+__device__ __forceinline__ V3<T> r_uv_p(const BoxD &b, bool periodic, double4_32a u, double4_32a w) {
+    if (periodic) return r_uv<T>(b, u, w);
+    return V3<T>{T(w.x - u.x), T(w.y - u.y), T(w.z - u.z)};
+}
+
 // Same minimum image with every product and sum rounded separately, so the
 // neighbour-list membership decisions reproduce an uncontracted CPU build
-// bit for bit.
-__device__ __forceinline__ double dist_exact(const BoxD &b, double4_32a u, double4_32a w) {
+// bit for bit.  dist2_exact is the squared distance (no square root).
+__device__ __forceinline__ double dist2_exact(const BoxD &b, double4_32a u, double4_32a w) {
     double d[3] = {__dsub_rn(w.x, u.x), __dsub_rn(w.y, u.y), __dsub_rn(w.z, u.z)};
 #pragma unroll
     for (int a = 0; a < 3; ++a) d[a] = __dsub_rn(d[a], __dmul_rn(b.cell[a], rint(__dmul_rn(d[a], b.cell_inv[a]))));
-    double s = __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
-    return __dsqrt_rn(s);
+    return __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
+}
+__device__ __forceinline__ double dist_exact(const BoxD &b, double4_32a u, double4_32a w) {
+    return __dsqrt_rn(dist2_exact(b, u, w));
 }
 
 

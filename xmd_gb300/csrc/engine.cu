@@ -191,6 +191,7 @@ __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
     const double4_32a pi = P[t + 3];
     const int r = d.rep_of[i];
     const BoxD bx = d.rep[r].box;
+    const bool per = bx.cell_inv[0] != 0.0 || bx.cell_inv[1] != 0.0 || bx.cell_inv[2] != 0.0;
     double vgo = 0, vpa = 0, ves = 0;
 
     if (p.on[XMD_TERM_GO]) {
@@ -199,7 +200,7 @@ __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
             if (!d.nat_on[k]) continue;
             int j = d.nat_j[k];
             FT V_;
-            V3<FT> f = go_pair<FT>(p, r_uv<FT>(bx, pi, pin[j]), (FT)d.nat_d[k], &V_);
+            V3<FT> f = go_pair<FT>(p, r_uv_p<FT>(bx, per, pi, pin[j]), (FT)d.nat_d[k], &V_);
             add3(fx, fy, fz, f);
             if (MODE == 0 && i < j) vgo += (double)V_;
         }
@@ -209,7 +210,7 @@ __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
         int e = d.nl_row[(size_t)k * N + i];
         int j = e & NL_MASK;
         double4_32a pj = pin[j];
-        V3<FT> r12 = r_uv<FT>(bx, pi, pj);
+        V3<FT> r12 = r_uv_p<FT>(bx, per, pi, pj);
         if (e & NL_PAULI) {
             FT V_;
             V3<FT> f = pauli_pair<FT>(p, r12, &V_);
@@ -241,7 +242,7 @@ __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
         for (int k = 0; k < nref; ++k) {
             int slot = sl[k];
             int i1 = q.ct_i1[slot], i2 = q.ct_i2[slot];
-            V3<FT> r12 = r_uv<FT>(bx, pin[i1], pin[i2]);
+            V3<FT> r12 = r_uv_p<FT>(bx, per, pin[i1], pin[i2]);
             FT r12_rn = ninv(r12);
             V3<FT> u = r12_rn * r12;
             double sat = fmin(tnow - q.ct_ref[slot], p.qa_cycle) * p.qa_cycle_inv;
@@ -321,7 +322,9 @@ __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
     double4_32a pn = make_double4_32a(y0[0], y0[1], y0[2], pi.w);
     d.pos[cur ^ 1][i] = pn;
     // skin test displacement: norm(box->r_uv(r_, orig_r_)), verify.cpp:12-14
-    double disp = dist_exact(bx, pn, d.orig[i]);
+    // squared; the check takes one square root of the maximum (sqrt is
+    // monotone and correctly rounded, so that equals the max of the norms)
+    double disp = dist2_exact(bx, pn, d.orig[i]);
     const unsigned lane = t & 31;
     int r0 = __shfl_sync(0xffffffffu & __activemask(), r, 0);
     unsigned mask = __activemask();
@@ -343,7 +346,7 @@ __global__ void k_nl_check(Dev d, int advance, double dt, cudaGraphConditionalHa
     for (int r = threadIdx.x; r < d.R; r += blockDim.x) {
         RepDev &rp = d.rep[r];
         if (advance) rp.t += dt;                       // *t = (*true_t += dt)
-        double md = __longlong_as_double((long long)rp.maxdisp);
+        double md = __dsqrt_rn(__longlong_as_double((long long)rp.maxdisp));
         rp.maxdisp = 0ull;
         int rb = rp.first || (2.0 * md + 0.0 > rp.pad);
         rp.rebuild = rb;
@@ -364,16 +367,33 @@ __global__ void k_mark_all(Dev d) {
 }
 
 // ---- cell lists: one block per flagged replica -----------------------------------
+// Cells have an edge of at least the Verlet radius.  Periodic axes are cut
+// into dims = floor(L / r) cells (wrapped); open axes count cells from the
+// bounding-box minimum without bound.  When every axis is periodic and the
+// grid fits the replica's bucket budget, a cell IS a bucket; otherwise cells
+// are hashed into the budget (chains in open space occupy few of their
+// bounding box's cells).  Buckets are visited once each, so collisions only
+// add candidates; the exact distance test decides.
 __device__ __forceinline__ int cell_coord(const RepDev &rp, int a, double x) {
-    int k;
     if (rp.per[a]) {
         double f = x * rp.box.cell_inv[a];
         f -= floor(f);
-        k = (int)(f * rp.dims[a]);
-    } else {
-        k = (int)floor((x - rp.lo[a]) / rp.cs[a]);
+        int k = (int)(f * rp.dims[a]);
+        return k < 0 ? 0 : (k >= rp.dims[a] ? rp.dims[a] - 1 : k);
     }
-    return k < 0 ? 0 : (k >= rp.dims[a] ? rp.dims[a] - 1 : k);
+    int k = (int)floor((x - rp.lo[a]) * rp.cs[a]);   // cs holds 1 / cell edge on open axes
+    return k < 0 ? 0 : k;
+}
+__device__ __forceinline__ int cell_key(const RepDev &rp, int cx, int cy, int cz) {
+    if (!rp.hashed) return (cz * rp.dims[1] + cy) * rp.dims[0] + cx;
+    uint32_t h = (uint32_t)cx * 73856093u ^ (uint32_t)cy * 19349663u ^ (uint32_t)cz * 83492791u;
+    return (int)(h % (uint32_t)rp.cell_budget);
+}
+// FP32 coordinate for the pre-filter: wrapped into [0, L) or taken from the
+// bounding-box minimum
+__device__ __forceinline__ float rel_coord(const RepDev &rp, int a, double x) {
+    if (rp.per[a]) return (float)(x - rp.box.cell[a] * floor(x * rp.box.cell_inv[a]));
+    return (float)(x - rp.lo[a]);
 }
 __device__ __forceinline__ double comp(double4_32a v, int a) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); }
 
@@ -409,42 +429,37 @@ __global__ void __launch_bounds__(CB) k_cells(Dev d, int cur) {
     if (t == 0) {
         const double rr = rp.req_r * (1.0 + 1e-9);
         long total = 1;
+        bool all_per = true;
+        double ext = 0.0;
         for (int a = 0; a < 3; ++a) {
             double l = 1e300, hh = -1e300;
             for (int q = 0; q < CB / 32; ++q) { l = fmin(l, red_lo[a][q]); hh = fmax(hh, red_hi[a][q]); }
-            int dm;
             if (rp.per[a]) {
-                dm = (int)floor(rp.box.cell[a] / rr);
+                int dm = (int)floor(rp.box.cell[a] / rr);
+                dm = dm < 1 ? 1 : (dm > 4096 ? 4096 : dm);
+                rp.dims[a] = dm;
                 rp.lo[a] = 0.0;
+                rp.cs[a] = 0.0;
+                total *= dm;
+                ext = fmax(ext, rp.box.cell[a]);
             } else {
-                double ext = hh - l;
-                dm = (int)floor(ext / rr);
+                all_per = false;
+                rp.dims[a] = 0;
                 rp.lo[a] = l;
-            }
-            dm = dm < 1 ? 1 : (dm > 1024 ? 1024 : dm);
-            rp.dims[a] = dm;
-            total *= dm;
-        }
-        while (total > bud) {   // keep within the replica's fixed cell budget
-            int am = 0;
-            for (int a = 1; a < 3; ++a) if (rp.dims[a] > rp.dims[am]) am = a;
-            rp.dims[am] = rp.dims[am] > 1 ? rp.dims[am] - 1 : 1;
-            total = (long)rp.dims[0] * rp.dims[1] * rp.dims[2];
-        }
-        for (int a = 0; a < 3; ++a) {
-            if (rp.per[a]) {
-                rp.cs[a] = rp.box.cell[a] / rp.dims[a];
-            } else {
-                double l = 1e300, hh = -1e300;
-                for (int q = 0; q < CB / 32; ++q) { l = fmin(l, red_lo[a][q]); hh = fmax(hh, red_hi[a][q]); }
-                rp.cs[a] = fmax((hh - l) / rp.dims[a], rr);
+                rp.cs[a] = 1.0 / rr;
+                ext = fmax(ext, hh - l);
             }
         }
+        rp.hashed = !(all_per && total <= bud);
+        // FP32 pre-filter radius: relative coordinates carry <= ext * 2^-24
+        // rounding each, so this margin never rejects a pair inside req_r
+        double m = rp.req_r + 1e-3 + 4e-7 * ext;
+        rp.pre2 = (float)(m * m);
         rp.first = 0;
         rp.rebuilds += 1;
     }
     __syncthreads();
-    const int ncell = rp.dims[0] * rp.dims[1] * rp.dims[2];
+    const int ncell = rp.hashed ? bud : rp.dims[0] * rp.dims[1] * rp.dims[2];
     for (int c = t; c < ncell; c += CB) {
         d.cell_cnt[off + c] = 0;
         d.cell_fill[off + c] = 0;
@@ -452,8 +467,7 @@ __global__ void __launch_bounds__(CB) k_cells(Dev d, int cur) {
     __syncthreads();
     for (int i = b + t; i < b + n; i += CB) {
         double4_32a q = pos[i];
-        int c = (cell_coord(rp, 2, q.z) * rp.dims[1] + cell_coord(rp, 1, q.y)) * rp.dims[0] +
-                cell_coord(rp, 0, q.x);
+        int c = cell_key(rp, cell_coord(rp, 0, q.x), cell_coord(rp, 1, q.y), cell_coord(rp, 2, q.z));
         d.bead_cell[i] = off + c;
         atomicAdd(&d.cell_cnt[off + c], 1);
     }
@@ -483,7 +497,7 @@ __global__ void __launch_bounds__(CB) k_cells(Dev d, int cur) {
         d.cell_items[d.cell_start[c] + slot] = i;
     }
     __syncthreads();
-    // deterministic order inside each cell
+    // deterministic order inside each bucket, then the FP32 coordinates
     for (int c = t; c < ncell; c += CB) {
         int s0 = d.cell_start[off + c], m = d.cell_cnt[off + c];
         int *it = d.cell_items + s0;
@@ -492,6 +506,13 @@ __global__ void __launch_bounds__(CB) k_cells(Dev d, int cur) {
             while (y >= 0 && it[y] > v) { it[y + 1] = it[y]; --y; }
             it[y + 1] = v;
         }
+    }
+    __syncthreads();
+    for (int k = b + t; k < b + n; k += CB) {
+        int i = d.cell_items[k];
+        double4_32a q = pos[i];
+        d.cell_pos[k] = make_float4(rel_coord(rp, 0, q.x), rel_coord(rp, 1, q.y), rel_coord(rp, 2, q.z),
+                                    __int_as_float(i));
     }
 }
 
@@ -525,26 +546,45 @@ __global__ void __launch_bounds__(128) k_nl_build(Dev d, TermP p, int cur) {
         for (int dlt = -1; dlt <= 1; ++dlt) {
             int k = cc[a] + dlt;
             if (rp.per[a]) k = ((k % rp.dims[a]) + rp.dims[a]) % rp.dims[a];
-            else if (k < 0 || k >= rp.dims[a]) continue;
+            else if (k < 0) continue;
             bool dup = false;
             for (int q = 0; q < noff[a]; ++q) dup |= offs[a][q] == k;
             if (!dup) offs[a][noff[a]++] = k;
         }
     }
+    // distinct buckets of the neighbouring cells
+    int keys[27], nk = 0;
+    for (int az = 0; az < noff[2]; ++az)
+        for (int ay = 0; ay < noff[1]; ++ay)
+            for (int ax = 0; ax < noff[0]; ++ax) {
+                int key = cell_key(rp, offs[0][ax], offs[1][ay], offs[2][az]);
+                bool dup = false;
+                for (int q = 0; q < nk; ++q) dup |= keys[q] == key;
+                if (!dup) keys[nk++] = key;
+            }
+    const float mx = rel_coord(rp, 0, pi.x), my = rel_coord(rp, 1, pi.y), mz = rel_coord(rp, 2, pi.z);
+    const float Lx = (float)bx.cell[0], Ly = (float)bx.cell[1], Lz = (float)bx.cell[2];
+    const float Lix = (float)bx.cell_inv[0], Liy = (float)bx.cell_inv[1], Liz = (float)bx.cell_inv[2];
+    const float pre2 = rp.pre2;
     const bool pauli_on = p.on[XMD_TERM_PAULI] != 0;
     const bool es_on = (p.on[XMD_TERM_CONST_ES] || p.on[XMD_TERM_REL_ES]);
     const bool qa_on = d.qa_on && p.on[XMD_TERM_QA];
     const int nref = qa_on ? min(d.qa.ref_cnt[i], QA_REF_CAP) : 0;
     int cnt = 0, tcnt = 0;
     const int cap = d.nl_cap;
-    for (int az = 0; az < noff[2]; ++az)
-        for (int ay = 0; ay < noff[1]; ++ay)
-            for (int ax = 0; ax < noff[0]; ++ax) {
-                int c = rp.cell_off + (offs[2][az] * rp.dims[1] + offs[1][ay]) * rp.dims[0] + offs[0][ax];
+    for (int kk = 0; kk < nk; ++kk) {
+                int c = rp.cell_off + keys[kk];
                 int q0 = d.cell_start[c], q1 = q0 + d.cell_cnt[c];
                 for (int q = q0; q < q1; ++q) {
-                    int j = d.cell_items[q];
+                    const float4 f = d.cell_pos[q];
+                    int j = __float_as_int(f.w);
                     if (j == i) continue;
+                    // FP32 pre-filter (min image on periodic axes)
+                    float ddx = f.x - mx, ddy = f.y - my, ddz = f.z - mz;
+                    ddx -= Lx * rintf(ddx * Lix);
+                    ddy -= Ly * rintf(ddy * Liy);
+                    ddz -= Lz * rintf(ddz * Liz);
+                    if (ddx * ddx + ddy * ddy + ddz * ddz > pre2) continue;
                     int cj = d.chain[j], sj = d.seq[j];
                     int df = si > sj ? si - sj : sj - si;
                     if (ci == cj && df < 3) continue;
@@ -802,6 +842,7 @@ void Engine::finalize() {
     d.cell_fill = (int32_t *)dalloc(sizeof(int32_t) * cells);
     d.cell_items = (int32_t *)dalloc(sizeof(int32_t) * N);
     d.bead_cell = (int32_t *)dalloc(sizeof(int32_t) * N);
+    d.cell_pos = (float4 *)dalloc(sizeof(float4) * N);
     d.rng = (uint64_t *)dalloc(sizeof(uint64_t) * N);
     d.jump = (uint64_t *)dalloc(sizeof(uint64_t) * 64 * R);
     d.rep = (RepDev *)dalloc(sizeof(RepDev) * R);
@@ -1144,7 +1185,7 @@ bool Engine::grow_rows(double frac) {
     CK(cudaMemcpyAsync(&need, d.ctr + 1, sizeof(need), cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
     if ((double)need < frac * nl_cap) return false;
-    int ncap = (int)(need + need / 2 + 8);
+    int ncap = (int)(2 * need + 16);
     int32_t *rows = nullptr;
     CK(cudaMalloc(&rows, sizeof(int32_t) * (size_t)ncap * d.N));
     for (auto &a : allocs)
@@ -1179,7 +1220,7 @@ void Engine::ensure_nl() {
         CK(cudaMemcpyAsync(&st, d.status, sizeof(int), cudaMemcpyDeviceToHost, stream));
         CK(cudaStreamSynchronize(stream));
         if (!(st & ST_CAPACITY) || !auto_grow) {
-            if (auto_grow) grow_rows(0.75);   // keep headroom for the run ahead
+            if (auto_grow) grow_rows(0.6);   // keep headroom for the run ahead
             return;
         }
         // rows overflowed at this rebuild: grow, clear the flag, rebuild all
@@ -1342,7 +1383,7 @@ void Engine::step(int nsteps) {
         if (*h_any) launch_rebuild();
     }
     check_status("step");
-    if (auto_grow && grow_rows(0.75)) k_mark_all<<<(d.R + 255) / 256, 256, 0, stream>>>(d);
+    if (auto_grow && grow_rows(0.6)) k_mark_all<<<(d.R + 255) / 256, 256, 0, stream>>>(d);
 }
 
 // ---- packed host-buffer path ----------------------------------------------------
@@ -1360,7 +1401,7 @@ __global__ void k_unpack_history(Dev d, const double *__restrict__ y, int cur) {
             d.yh[(size_t)((ord - 1) * 3 + a) * d.N + i] = y[ord * n3 + 3 * (size_t)i + a];
     // the skin test sees the new positions like any other displacement
     int r = d.rep_of[i];
-    double disp = dist_exact(d.rep[r].box, p, d.orig[i]);
+    double disp = dist2_exact(d.rep[r].box, p, d.orig[i]);   // squared, as k_force records it
     atomicMax(&d.rep[r].maxdisp, (unsigned long long)__double_as_longlong(disp));
 }
 __global__ void k_pack_positions(Dev d, double *__restrict__ r, int cur) {
@@ -1454,6 +1495,33 @@ int Engine::qa_contacts(int rep, int cap, int32_t *out4, double *ref_time) {
         ++m;
     }
     return m;
+}
+
+int Engine::verlet_pairs(int rep, int cap, int32_t *out2, uint8_t *flags) {
+    check_rep(reps, rep);
+    finalize();
+    ensure_nl();
+    const RepHost &h = reps[rep];
+    std::vector<int32_t> cnt(h.n), rows((size_t)nl_cap * h.n);
+    CK(cudaMemcpyAsync(cnt.data(), d.nl_cnt + h.begin, sizeof(int32_t) * h.n, cudaMemcpyDeviceToHost, stream));
+    for (int k = 0; k < nl_cap; ++k)
+        CK(cudaMemcpyAsync(rows.data() + (size_t)k * h.n, d.nl_row + (size_t)k * d.N + h.begin,
+                           sizeof(int32_t) * h.n, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    std::vector<std::tuple<int, int, int>> v;
+    for (int i = 0; i < h.n; ++i)
+        for (int k = 0; k < cnt[i]; ++k) {
+            int e = rows[(size_t)k * h.n + i];
+            int j = (e & NL_MASK) - h.begin;
+            if (j > i) v.emplace_back(i, j, ((e & NL_PAULI) ? 1 : 0) | ((e & NL_ES) ? 2 : 0));
+        }
+    std::sort(v.begin(), v.end());
+    for (size_t k = 0; k < v.size() && (int)k < cap; ++k) {
+        out2[2 * k] = std::get<0>(v[k]);
+        out2[2 * k + 1] = std::get<1>(v[k]);
+        if (flags) flags[k] = (uint8_t)std::get<2>(v[k]);
+    }
+    return (int)v.size();
 }
 
 void Engine::qa_sync(int rep, int8_t *out) {

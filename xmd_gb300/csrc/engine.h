@@ -29,8 +29,10 @@ struct RepDev {
     int begin, n;
     int cell_off, cell_budget;
     int per[3];
-    int dims[3];
-    double lo[3], cs[3];
+    int dims[3];             // cells along periodic axes
+    double lo[3], cs[3];     // bounding-box minimum and 1/cell edge along open axes
+    int hashed;              // cells hashed into the bucket budget
+    float pre2;              // squared FP32 pre-filter radius of the Verlet build
     int first, rebuild;
     unsigned long long maxdisp;
     unsigned long long rebuilds;
@@ -41,7 +43,7 @@ struct RepDev {
 };
 
 constexpr int QA_REF_CAP = 16;   // contacts per bead (valence bounds it by 10)
-constexpr int QA_TMP_CAP = 128;  // free-pair partners j > i per bead at a rebuild
+constexpr int QA_TMP_CAP = 256;  // free-pair partners j > i per bead at a rebuild
 constexpr int QA_FP_PER_BEAD = 96;   // free-pair slots per bead of a replica (+256)
 constexpr int QA_CT_PER_BEAD = 8;    // contact slots per bead of a replica (+256)
 
@@ -82,6 +84,7 @@ struct Dev {
     uint8_t *nat_on;
     int32_t *nl_row, *nl_cnt;
     int32_t *cell_cnt, *cell_start, *cell_fill, *cell_items, *bead_cell;
+    float4 *cell_pos;       // bucket-sorted FP32 coordinates (+ bead index bits)
     uint64_t *rng;          // per-bead generator state
     uint64_t *jump;         // [R][64] GF(2) jump matrices (4 N_r draws)
     RepDev *rep;
@@ -140,6 +143,7 @@ public:
     void stats(int64_t *out);
     void set_kernel_timing(bool on);
     int qa_contacts(int rep, int cap, int32_t *out4, double *ref_time);
+    int verlet_pairs(int rep, int cap, int32_t *out2, uint8_t *flags);
     void qa_sync(int rep, int8_t *out);
     void kernel_times(double *force_ms, int64_t *nf, double *rebuild_ms, int64_t *nr);
     void use_device() const;
