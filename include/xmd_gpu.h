@@ -239,6 +239,36 @@ int xmd_gpu_set_kernel_timing(xmd_gpu_ctx *ctx, int on);
 int xmd_gpu_kernel_times(xmd_gpu_ctx *ctx, double *force_ms, int64_t *force_launches,
                          double *rebuild_ms, int64_t *rebuild_launches);
 
+/* ---- allocation-free pair search --------------------------------------------- */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory where they need a pair list: code running while a CUDA graph is
+ * captured on its stream, hosts whose device memory belongs to a fixed pool
+ * or a framework allocator, loops that cannot take cudaMalloc's implicit
+ * device synchronisation.  Every input and output is a device pointer the
+ * caller owns; the function calls no cudaMalloc, cudaFree or allocating
+ * library routine.  Its scratch is a file-scope __device__ array of about
+ * 1.75 MiB that every GPU which loads the library holds until exit, sized for
+ * XMD_NOALLOC_MAX_BEADS beads; larger n is rejected with XMD_ERR_CAPACITY.
+ *
+ * Computes, on `stream` (a cudaStream_t; NULL = legacy default stream), the
+ * pairs i < j of the engine's Verlet search: not in the same chain with
+ * |seq_i - seq_j| < 3, minimum-image distance below `cutoff`
+ * (legacy_update.cpp:24-29 semantics), written as (i, j) into d_pairs[2*k] in
+ * (i, j) order, at most `cap` pairs; *d_count receives the number found
+ * (which may exceed cap).  d_r = positions [3n], d_chain / d_seq = [n];
+ * cell = host array, 0 = open along that axis.
+ *
+ * The first call on a device looks up the scratch's device address (once per
+ * device, with that device current); make that first call before any stream
+ * capture.  All calls share the scratch and leave their contents in it; each
+ * call clears what must start at zero.  Calls that overlap on the GPU (on
+ * different streams, or from different threads without ordering) race on the
+ * scratch and must be serialised by the caller. */
+#define XMD_NOALLOC_MAX_BEADS 65536
+int xmd_gpu_verlet_pairs_noalloc(const double *d_r, const int32_t *d_chain, const int32_t *d_seq,
+                                 int32_t n, const double cell[3], double cutoff, int32_t *d_pairs,
+                                 int32_t cap, int32_t *d_count, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -17,6 +17,7 @@ TERM_NAMES = ["tether", "nat_ang", "cnd", "snd", "go", "pauli", "const_es", "rel
 (TERM_TETHER, TERM_NAT_ANG, TERM_CND, TERM_SND, TERM_GO, TERM_PAULI, TERM_CONST_ES,
  TERM_REL_ES, TERM_QA) = range(NUM_TERMS)
 PREC_FP64, PREC_MIXED = 0, 1
+NOALLOC_MAX_BEADS = 65536   # XMD_NOALLOC_MAX_BEADS
 
 ERRORS = {-1: "XMD_ERR_ARG", -2: "XMD_ERR_CONFIG", -3: "XMD_ERR_STATE", -4: "XMD_ERR_CUDA",
           -5: "XMD_ERR_CAPACITY", -6: "XMD_ERR_NUMERIC", -7: "XMD_ERR_BUDGET"}
@@ -93,6 +94,8 @@ SIGNATURES = [
     ("xmd_gpu_qa_contacts", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _pi32, _pd, _pi32]),
     ("xmd_gpu_qa_sync", C.c_int, [C.c_void_p, C.c_int32, P(C.c_int8)]),
     ("xmd_gpu_verlet_pairs", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _pi32, _pu8, _pi32]),
+    ("xmd_gpu_verlet_pairs_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, _pd, C.c_double,
+                                               C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     ("xmd_gpu_upload_history_all", C.c_int, [C.c_void_p, _pd]),
     ("xmd_gpu_download_positions_all", C.c_int, [C.c_void_p, _pd]),
     ("xmd_gpu_get_stream", C.c_int, [C.c_void_p, P(C.c_void_p)]),

@@ -279,6 +279,22 @@ int xmd_gpu_qa_sync(xmd_gpu_ctx *ctx, int32_t rep, int8_t *out) {
     return guard([&] { ctx->eng->use_device(); ctx->eng->qa_sync(rep, out); });
 }
 
+int xmd_gpu_verlet_pairs_noalloc(const double *d_r, const int32_t *d_chain, const int32_t *d_seq, int32_t n,
+                                 const double cell[3], double cutoff, int32_t *d_pairs, int32_t cap,
+                                 int32_t *d_count, void *stream) {
+    if (n < 0) return fail(XMD_ERR_ARG, "negative bead count");
+    if (n > XMD_NOALLOC_MAX_BEADS)
+        return fail(XMD_ERR_CAPACITY, "xmd_gpu_verlet_pairs_noalloc: " + std::to_string(n) +
+                                          " beads exceed the allocation-free scratch (XMD_NOALLOC_MAX_BEADS = " +
+                                          std::to_string(XMD_NOALLOC_MAX_BEADS) + ")");
+    if (!cell || !d_count || (n > 0 && (!d_r || !d_chain || !d_seq)) || cap < 0 || (cap > 0 && !d_pairs))
+        return fail(XMD_ERR_ARG, "null or invalid buffer");
+    if (!(cutoff > 0.0)) return fail(XMD_ERR_ARG, "cutoff must be positive");
+    for (int a = 0; a < 3; ++a)
+        if (!(cell[a] >= 0.0)) return fail(XMD_ERR_ARG, "bad cell");
+    return guard([&] { xmdg::verlet_pairs_noalloc(d_r, d_chain, d_seq, n, cell, cutoff, d_pairs, cap, d_count, stream); });
+}
+
 int xmd_gpu_synchronize(xmd_gpu_ctx *ctx) {
     NEED_CTX;
     return guard([&] { ctx->eng->use_device(); ctx->eng->sync(); });

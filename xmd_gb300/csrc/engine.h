@@ -190,5 +190,8 @@ private:
 
 std::string &last_error();
 uint64_t rng_jump(uint64_t state, uint64_t n_draws);
+int verlet_pairs_noalloc(const double *d_r, const int32_t *d_chain, const int32_t *d_seq, int32_t n,
+                         const double cell[3], double cutoff, int32_t *d_pairs, int32_t cap, int32_t *d_count,
+                         void *stream);
 
 }  // namespace xmdg
