@@ -278,6 +278,8 @@ def run_engine(args, rank, local, world):
         ev64.record(e1)
         t64 += ev64.ms(e0, e1)
     value64 = nbeads * md * k64 / (t64 / 1e3)
+    eng64.close()
+    plain64 = plain_fp64(systems, y_fp64, md, args.warmup, rt, flush)
     # force error of the mixed path on identical states (fresh engines at t=0)
     errs = []
     with Engine(y_mixed) as em, Engine(y_fp64) as ed:
@@ -288,7 +290,6 @@ def run_engine(args, rank, local, world):
             Fm, _ = em.eval_forces(r)
             Fd, _ = ed.eval_forces(r)
             errs.append(float(np.abs(Fm - Fd).max() / max(np.abs(Fd).max(), 1e-300)))
-    eng64.close()
 
     cpu = cpu_baseline(systems, sample_steps=args.cpu_sample_steps) if rank == 0 else None
     rt.cudaFree(flush)
@@ -306,7 +307,9 @@ def run_engine(args, rank, local, world):
                         "mixed precision (FP32 forces, FP64 accumulate/integrate), one context",
             "md_steps_per_step": md, "beads_per_gpu": nbeads, "replicas_per_gpu": nrep,
             "l2": "256 MiB device write before each timed step (not timed)",
-            "plain_fp64_value": value64, "mixed_over_fp64": value / world / value64,
+            "plain_fp64_value": plain64["value"], "plain_fp64_sample": plain64["sample"],
+            "mixed_over_plain_fp64": value / world / plain64["value"],
+            "batched_fp64_value": value64, "mixed_over_batched_fp64": value / world / value64,
             "mixed_force_rel_err_max": max(errs), "graph_steps_per_launch": 16,
             "p99_req_latency_ms": None,
         },
@@ -321,6 +324,36 @@ def run_engine(args, rank, local, world):
         "clocks": clk,
     }
     print(json.dumps(out), flush=True)
+
+
+def plain_fp64(systems, yaml_fp64, md, warmup, rt, flush, sample=16):
+    """The plain FP64 path: each system alone in its own context (no packing,
+    FP64 forces), over a size-stratified sample of the replicas.  Returns
+    summed bead-steps over summed device time."""
+    from xmd_gb300 import Engine, abi
+    order = sorted(range(len(systems)), key=lambda k: systems[k].n)
+    pick = [order[int(q)] for q in np.linspace(0, len(order) - 1, min(sample, len(order)))]
+    work, t_ms = 0, 0.0
+    stream = C.c_void_p()
+    for k in pick:
+        with Engine(yaml_fp64) as e:
+            e.add_system(systems[k])
+            for _ in range(max(1, warmup)):
+                e.step(md)
+            e.synchronize()
+            abi.check(e.lib.xmd_gpu_get_stream(e.h, C.byref(stream)))
+            ev = Events(rt, stream)
+            a, b = ev.new(), ev.new()
+            rt.cudaMemsetAsync(flush, 1, C.c_size_t(L2_FLUSH_BYTES), stream)
+            ev.record(a)
+            e.step(md)
+            ev.record(b)
+            t_ms += ev.ms(a, b)
+            work += systems[k].n * md
+    nb = sum(systems[k].n for k in pick)
+    return {"value": work / (t_ms / 1e3),
+            "sample": f"{len(pick)} size-stratified replicas ({nb} beads), each alone in an FP64 context, "
+                      f"{md} steps each"}
 
 
 # ------------------------------------------------------------- CPU arms --

@@ -115,7 +115,12 @@ typedef struct xmd_params {
     int32_t nl_grow;
     /* engine: CUDA device ordinal the context runs on */
     int32_t device;
+    /* engine: Verlet build, XMD_NL_BUILD_* ("nl build: auto | cell | tile");
+       both builds keep exactly the same pairs */
+    int32_t nl_build;
 } xmd_params;
+
+enum { XMD_NL_BUILD_AUTO = 0, XMD_NL_BUILD_CELL = 1, XMD_NL_BUILD_TILE = 2 };
 
 /* xmd_gpu_stats() slots */
 enum {
@@ -238,6 +243,12 @@ int xmd_gpu_stats(xmd_gpu_ctx *ctx, int64_t *out);
 int xmd_gpu_set_kernel_timing(xmd_gpu_ctx *ctx, int on);
 int xmd_gpu_kernel_times(xmd_gpu_ctx *ctx, double *force_ms, int64_t *force_launches,
                          double *rebuild_ms, int64_t *rebuild_launches);
+
+/* No counterpart in the reference.  Measures the FP64 fused multiply-add
+ * rate of CUDA device `device` (TFLOP/s, 2 flops per FMA, best of four timed
+ * launches of a kernel that fills every SM); the FP64 roof against which the
+ * step kernels are reported.  Takes about 0.1 s. */
+int xmd_gpu_fp64_peak(int32_t device, double *tflops);
 
 /* ---- allocation-free pair search --------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device

@@ -143,8 +143,10 @@ void legacy_update_restated(xr_sys *s) {
             if (orig_dist < s->req_r) {
                 bool non_native = true;
                 auto key = std::make_pair(i1, i2);
-                while (nat_idx < s->nat_sorted.size() && s->nat_sorted[nat_idx] < key) ++nat_idx;
-                if (nat_idx < s->nat_sorted.size() && s->nat_sorted[nat_idx] == key) {
+                // all_nat_cont is wired only when native contacts are enabled
+                // (main.cpp:504-530); otherwise natives are ordinary pairs
+                while (s->p.on[XMD_TERM_GO] && nat_idx < s->nat_sorted.size() && s->nat_sorted[nat_idx] < key) ++nat_idx;
+                if (s->p.on[XMD_TERM_GO] && nat_idx < s->nat_sorted.size() && s->nat_sorted[nat_idx] == key) {
                     s->nl.native_contacts.emplace_back(i1, i2, orig_dist);
                     non_native = false;
                 }

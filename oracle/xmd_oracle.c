@@ -541,10 +541,12 @@ static void nl_rebuild(xo_sys *s) {
             if (orig_dist < req_r) {
                 int non_native = 1;
                 /* sorted merge against the native list [D2] */
-                while (nat_idx < s->n_nat &&
+                /* the native list takes part only with native contacts
+                   enabled (main.cpp:504-530 wires all_nat_cont there) */
+                while (p->on[XMD_TERM_GO] && nat_idx < s->n_nat &&
                        (s->nat[nat_idx].i1 < i1 || (s->nat[nat_idx].i1 == i1 && s->nat[nat_idx].i2 < i2)))
                     ++nat_idx;
-                if (nat_idx < s->n_nat && s->nat[nat_idx].i1 == i1 && s->nat[nat_idx].i2 == i2)
+                if (p->on[XMD_TERM_GO] && nat_idx < s->n_nat && s->nat[nat_idx].i1 == i1 && s->nat[nat_idx].i2 == i2)
                     non_native = 0;
                 if (non_native) {                                       /* [D3] */
                     GROW(s->nl, s->n_nl, s->cap_nl, pair_i);

@@ -173,14 +173,37 @@ def test_packed_upload_download_roundtrip():
         assert np.array_equal(r.reshape(-1, 3), np.concatenate([h[0] for h in hs]))
 
 
+def with_engine_key(y: str, line: str) -> str:
+    """YAML with `line` added to its engine section (one section per key)."""
+    if "\nengine:\n" in "\n" + y:
+        return ("\n" + y).replace("\nengine:\n", "\nengine:\n  " + line + "\n", 1)[1:]
+    return y + "\nengine:\n  " + line + "\n"
+
+
+def verlet_pairs(e, rep, cap):
+    import ctypes
+    out = np.zeros(2 * cap, dtype=np.int32)
+    flags = np.zeros(cap, dtype=np.uint8)
+    cnt = ctypes.c_int32()
+    abi.check(e.lib.xmd_gpu_verlet_pairs(e.h, rep, cap, abi.iptr(out),
+                                          flags.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
+                                          ctypes.byref(cnt)))
+    assert cnt.value <= cap
+    return {(int(out[2 * k]), int(out[2 * k + 1])): int(flags[k]) for k in range(cnt.value)}
+
+
+@pytest.mark.parametrize("build", ["cell", "tile"])
 @pytest.mark.parametrize("case", ["c2_periodic480", "c1_chain100", "c3_qa600"])
-def test_verlet_pairs_match_oracle(case):
-    """The cell-list build keeps exactly the pairs of the reference's list
-    filters: non-native pairs within the Verlet radius (legacy_update.cpp),
-    Pauli within r_excl + pad (pauli.cpp:9-24), ES within 2D + pad with
-    q1 q2 != 0 (es_pair.cpp:6-23); as sets, with identical membership."""
+def test_verlet_pairs_match_oracle(case, build):
+    """Both Verlet builds (cell grid, whole-replica tiles) keep exactly the
+    pairs of the reference's list filters: non-native pairs within the Verlet
+    radius (legacy_update.cpp), Pauli within r_excl + pad (pauli.cpp:9-24), ES
+    within 2D + pad with q1 q2 != 0 (es_pair.cpp:6-23); as sets, with
+    identical membership."""
     s, y, _ = load_golden(case)
+    y = with_engine_key(y, f"nl build: {build}")
     p = abi.parse_params(y)
+    assert p.nl_build == {"cell": 1, "tile": 2}[build]
     o = Oracle(p, s, "port")
     o.eval_forces()
     nl = o.nl_pairs()
@@ -202,16 +225,33 @@ def test_verlet_pairs_match_oracle(case):
     want = {(int(a), int(b)): int(f) for (a, b), f in zip(nl, fl) if f}
     with Engine(y) as e:
         e.add_system(s)
-        cap = 4 * len(nl) + 16
-        out = np.zeros(2 * cap, dtype=np.int32)
-        flags = np.zeros(cap, dtype=np.uint8)
-        import ctypes
-        cnt = ctypes.c_int32()
-        abi.check(e.lib.xmd_gpu_verlet_pairs(e.h, 0, cap, abi.iptr(out),
-                                              flags.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
-                                              ctypes.byref(cnt)))
-    got = {(int(out[2 * k]), int(out[2 * k + 1])): int(flags[k]) for k in range(cnt.value)}
+        e.eval_forces(0)
+        got = verlet_pairs(e, 0, 4 * len(nl) + 16)
     assert got == want
+
+
+@pytest.mark.parametrize("case", ["c2_periodic480", "c2_sparse240", "c3_qa600", "c1_native100"])
+def test_cell_and_tile_builds_agree(case):
+    """Along a trajectory (lists rebuilt many times), the cell-grid and the
+    tile build keep the same pairs, the same Go list and the same QA state;
+    forces differ only by the summation order of each bead's pair row."""
+    s, y, _ = load_golden(case)
+    res = {}
+    for build in ("cell", "tile"):
+        with Engine(with_engine_key(y, f"nl build: {build}")) as e:
+            e.add_system(s)
+            e.step(40)
+            pairs = verlet_pairs(e, 0, 1 << 20)
+            F, V = e.eval_forces(0)
+            st = e.stats()
+            res[build] = (pairs, F, V, st, e.qa_contacts(0) if "qa" in case else None, e.get_state(0)[0])
+    a, b = res["cell"], res["tile"]
+    assert a[0] == b[0]
+    assert rel_err(b[1], a[1]) <= 1e-12
+    assert a[3]["go_active"] == b[3]["go_active"] and a[3]["rebuilds"] == b[3]["rebuilds"]
+    assert np.abs(a[5] - b[5]).max() <= 1e-9
+    if a[4] is not None:
+        assert np.array_equal(a[4][0], b[4][0])
 
 
 def test_verlet_capacity_overflow_is_reported():

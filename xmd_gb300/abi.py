@@ -48,7 +48,7 @@ class Params(C.Structure):
         ("qa_min_cos_hr", _d), ("qa_min_cos_hh", _d), ("qa_max_cos_nr", _d),
         ("lj_bb_r_min", _d), ("lj_bb_depth", _d), ("lj_bs_r_min", _d), ("lj_bs_depth", _d),
         ("ss_sinking", _i), ("ss_depth", _d * NUM_SS), ("ss_r_max", _d * NUM_SS),
-        ("nl_capacity", _i), ("nl_grow", _i), ("device", _i),
+        ("nl_capacity", _i), ("nl_grow", _i), ("device", _i), ("nl_build", _i),
     ]
 
     def copy(self) -> "Params":
@@ -103,6 +103,7 @@ SIGNATURES = [
     ("xmd_gpu_set_kernel_timing", C.c_int, [C.c_void_p, C.c_int]),
     ("xmd_gpu_kernel_times", C.c_int, [C.c_void_p, _pd, P(C.c_int64), _pd, P(C.c_int64)]),
     ("xmd_gpu_synchronize", C.c_int, [C.c_void_p]),
+    ("xmd_gpu_fp64_peak", C.c_int, [C.c_int32, _pd]),
 ]
 
 _lib = None

@@ -26,7 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC"]
 
-CUDA_SOURCES = ["engine.cu", "noalloc.cu"]
+CUDA_SOURCES = ["engine.cu", "noalloc.cu", "probe.cu"]
 CXX_SOURCES = ["capi.cpp", "config.cpp", "defaults_yml.cpp"]
 
 

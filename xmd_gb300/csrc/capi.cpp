@@ -242,6 +242,11 @@ int xmd_gpu_set_kernel_timing(xmd_gpu_ctx *ctx, int on) {
     return guard([&] { ctx->eng->use_device(); ctx->eng->set_kernel_timing(on != 0); });
 }
 
+int xmd_gpu_fp64_peak(int32_t device, double *tflops) {
+    if (!tflops || device < 0) return fail(XMD_ERR_ARG, "bad argument");
+    return guard([&] { *tflops = xmdg::fp64_peak(device); });
+}
+
 int xmd_gpu_kernel_times(xmd_gpu_ctx *ctx, double *force_ms, int64_t *force_launches, double *rebuild_ms,
                          int64_t *rebuild_launches) {
     NEED_CTX;

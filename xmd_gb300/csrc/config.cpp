@@ -598,7 +598,14 @@ void resolve_params(const YNode &root, xmd_params *o) {
     o->nl_capacity = 64;
     o->nl_grow = 1;
     o->device = 0;
+    o->nl_build = XMD_NL_BUILD_AUTO;
     if (const YNode *en = root.get("engine")) {
+        if (const YNode *nb = en->get("nl build"); nb && nb->kind == YNode::Scalar) {
+            if (nb->scalar == "auto") o->nl_build = XMD_NL_BUILD_AUTO;
+            else if (nb->scalar == "cell") o->nl_build = XMD_NL_BUILD_CELL;
+            else if (nb->scalar == "tile") o->nl_build = XMD_NL_BUILD_TILE;
+            else throw std::runtime_error("engine: nl build must be 'auto', 'cell' or 'tile'");
+        }
         if (en->get("nl grow")) o->nl_grow = bval(*en, "nl grow", "engine: ");
         if (const YNode *dv = en->get("device"); dv && dv->kind == YNode::Scalar) {
             o->device = std::atoi(dv->scalar.c_str());

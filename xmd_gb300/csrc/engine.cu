@@ -402,7 +402,7 @@ __global__ void __launch_bounds__(CB) k_cells(Dev d, int cur) {
     const int r = blockIdx.x;
     if (r == 0 && threadIdx.x == 0) atomicAdd(d.ctr, 1ull);
     RepDev &rp = d.rep[r];
-    if (!rp.rebuild) return;
+    if (!rp.rebuild || rp.tile) return;
     const double4_32a *pos = d.pos[cur];
     const int b = rp.begin, n = rp.n, off = rp.cell_off, bud = rp.cell_budget;
     __shared__ double red_lo[3][32], red_hi[3][32];
@@ -522,7 +522,7 @@ __global__ void __launch_bounds__(128) k_nl_build(Dev d, TermP p, int cur) {
     if (i >= d.N) return;
     const int r = d.rep_of[i];
     const RepDev &rp = d.rep[r];
-    if (!rp.rebuild) return;
+    if (!rp.rebuild || rp.tile) return;
     const double4_32a *pos = d.pos[cur];
     const double4_32a pi = pos[i];
     const BoxD bx = rp.box;
@@ -567,6 +567,7 @@ __global__ void __launch_bounds__(128) k_nl_build(Dev d, TermP p, int cur) {
     const float Lix = (float)bx.cell_inv[0], Liy = (float)bx.cell_inv[1], Liz = (float)bx.cell_inv[2];
     const float pre2 = rp.pre2;
     const bool pauli_on = p.on[XMD_TERM_PAULI] != 0;
+    const bool go_on = p.on[XMD_TERM_GO] != 0;
     const bool es_on = (p.on[XMD_TERM_CONST_ES] || p.on[XMD_TERM_REL_ES]);
     const bool qa_on = d.qa_on && p.on[XMD_TERM_QA];
     const int nref = qa_on ? min(d.qa.ref_cnt[i], QA_REF_CAP) : 0;
@@ -591,8 +592,11 @@ __global__ void __launch_bounds__(128) k_nl_build(Dev d, TermP p, int cur) {
                     double4_32a pj = pos[j];
                     double dd = dist_exact(bx, pi, pj);
                     if (!(dd < rp.req_r)) continue;
+                    // natives leave the list only when native contacts are
+                    // enabled (main.cpp:504-530 wires all_nat_cont there)
                     bool native = false;
-                    for (int k = n0; k < n1; ++k) native |= d.nat_j[k] == j;
+                    if (go_on)
+                        for (int k = n0; k < n1; ++k) native |= d.nat_j[k] == j;
                     if (native) continue;
                     double inv = __ddiv_rn(1.0, dd);
                     // quasi-adiabatic free pairs (update_free_pairs, free_pair.cpp:9-19),
@@ -627,6 +631,196 @@ __global__ void __launch_bounds__(128) k_nl_build(Dev d, TermP p, int cur) {
     if (qa_on) {
         if (tcnt > QA_TMP_CAP) atomicOr(d.status, ST_CAPACITY);
         d.qa.tmp_cnt[i] = min(tcnt, QA_TMP_CAP);
+    }
+}
+
+// ---- Verlet build for replicas of at most TILE_MAX beads ---------------------------
+// One block per chunk of TL_CH beads i; the block holds the whole replica in
+// shared memory (FP32 coordinates relative to the replica, chain and sequence
+// index) and each warp scans every bead j of the replica for one bead i at a
+// time, lane k taking j = j0 + k.  A pair is decided in FP32 when its FP32
+// distance is farther than the error margin m from every threshold (the list
+// radius, r_excl + pad, 2D + pad, the QA formation radius + pad); otherwise the
+// exact FP64 test of the cell path decides it.  m = 1e-3 + 4e-7 * ext bounds
+// the FP32 error of a distance between coordinates of magnitude <= ext (each
+// coordinate carries <= ext * 2^-24; the differences, the periodic shift and
+// the squares add a few ulp more), so both paths keep exactly the same pairs.
+// Rows come out ordered by j (ballot compaction in lane order).
+constexpr int TL_CH = 128;
+constexpr int TL_THREADS = 256;
+constexpr int TL_WARPS = TL_THREADS / 32;
+constexpr int TILE_MAX = 4096;
+
+__device__ __forceinline__ float tl_rel(const RepDev &rp, int a, double x, double ref) {
+    if (rp.per[a]) return (float)(x - rp.box.cell[a] * floor(x * rp.box.cell_inv[a]));
+    return (float)(x - ref);
+}
+
+struct Band {
+    float lo, hi;   // squared FP32 distance: below lo -> inside, above hi -> outside
+};
+__device__ __forceinline__ Band make_band(double T, double m) {
+    double a = T - m, b = T + m;
+    return Band{a > 0.0 ? __double2float_rd(a * a) : -1.0f, __double2float_ru(b * b)};
+}
+__device__ __forceinline__ bool in_band(const Band &B, float d2) { return d2 >= B.lo && d2 <= B.hi; }
+
+__global__ void __launch_bounds__(TL_THREADS) k_nl_tile(Dev d, TermP p, int cur) {
+    if (blockIdx.x == 0 && threadIdx.x == 0 && !d.any_cell) atomicAdd(d.ctr, 1ull);
+    const int2 chk = d.chunks[blockIdx.x];
+    const int r = chk.x;
+    RepDev &rp = d.rep[r];
+    if (!rp.rebuild || !rp.tile) return;
+    extern __shared__ float4 tl_smem[];
+    const int b = rp.begin, n = rp.n;
+    float4 *sq = tl_smem;
+    int2 *scs = (int2 *)(sq + n);
+    __shared__ float ext_s[TL_WARPS];
+    const double4_32a *pos = d.pos[cur];
+    const BoxD bx = rp.box;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const double4_32a p0 = pos[b];
+
+    float ext = 0.0f;
+    for (int k = t; k < n; k += TL_THREADS) {
+        double4_32a q = pos[b + k];
+        float x = tl_rel(rp, 0, q.x, p0.x), y = tl_rel(rp, 1, q.y, p0.y), z = tl_rel(rp, 2, q.z, p0.z);
+        sq[k] = make_float4(x, y, z, (float)q.w);
+        scs[k] = make_int2(d.chain[b + k], d.seq[b + k]);
+        ext = fmaxf(ext, fmaxf(fabsf(x), fmaxf(fabsf(y), fabsf(z))));
+    }
+    for (int o = 16; o; o >>= 1) ext = fmaxf(ext, __shfl_xor_sync(0xffffffffu, ext, o));
+    if (lane == 0) ext_s[w] = ext;
+    __syncthreads();
+    ext = 0.0f;
+    for (int q = 0; q < TL_WARPS; ++q) ext = fmaxf(ext, ext_s[q]);
+    double exd = (double)ext;
+    for (int a = 0; a < 3; ++a) exd = fmax(exd, bx.cell[a]);
+    const double m = 1e-3 + 4e-7 * exd;
+
+    const bool pauli_on = p.on[XMD_TERM_PAULI] != 0;
+    const bool go_on = p.on[XMD_TERM_GO] != 0;
+    const bool es_on = (p.on[XMD_TERM_CONST_ES] || p.on[XMD_TERM_REL_ES]);
+    const bool qa_on = d.qa_on && p.on[XMD_TERM_QA];
+    const Band Breq = make_band(rp.req_r, m);
+    const Band Bpa = make_band(1.0 / rp.pauli_min_inv, m);
+    const Band Bes = make_band(1.0 / rp.es_min_inv, m);
+    const Band Bqa = make_band(1.0 / rp.qa_min_inv, m);
+    const float Lx = (float)bx.cell[0], Ly = (float)bx.cell[1], Lz = (float)bx.cell[2];
+    const float Lix = (float)bx.cell_inv[0], Liy = (float)bx.cell_inv[1], Liz = (float)bx.cell_inv[2];
+    const double pad = rp.pad;
+    const int cap = d.nl_cap;
+    const unsigned lt = (1u << lane) - 1u;
+
+    if (t == 0 && chk.y == b) {
+        rp.first = 0;
+        rp.rebuilds += 1;
+    }
+    const int i_end = min(chk.y + TL_CH, b + n);
+    for (int i = chk.y + w; i < i_end; i += TL_WARPS) {
+        const int li = i - b;
+        const float4 qi = sq[li];
+        const int2 ci = scs[li];
+        const double4_32a pi = pos[i];
+        const int n0 = d.nat_start[i], n1 = d.nat_start[i + 1];
+
+        // Go list: update_go_contacts, go.cpp:11-22
+        for (int k = n0 + lane; k < n1; k += 32) {
+            const int j = d.nat_j[k];
+            const float4 qj = sq[j - b];
+            float dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
+            dx -= Lx * rintf(dx * Lix);
+            dy -= Ly * rintf(dy * Liy);
+            dz -= Lz * rintf(dz * Liz);
+            const float d2 = dx * dx + dy * dy + dz * dz;
+            const double T = __dadd_rn(2.0 * d.nat_d[k], pad);
+            const Band B = make_band(T, m);
+            bool on;
+            if (in_band(B, d2)) on = dist_exact(bx, pi, pos[j]) < T;
+            else on = d2 < B.lo;
+            d.nat_on[k] = on;
+        }
+
+        int nref = 0;
+        if (qa_on) nref = min(d.qa.ref_cnt[i], QA_REF_CAP);
+        int cnt = 0, tcnt = 0;
+        for (int j0 = 0; j0 < n; j0 += 32) {
+            const int lj = j0 + lane;
+            int flags = 0;
+            bool qa_free = false;
+            if (lj < n && lj != li) {
+                const float4 qj = sq[lj];
+                float dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
+                dx -= Lx * rintf(dx * Lix);
+                dy -= Ly * rintf(dy * Liy);
+                dz -= Lz * rintf(dz * Liz);
+                const float d2 = dx * dx + dy * dy + dz * dz;
+                const int2 cj = scs[lj];
+                const int df = ci.y > cj.y ? ci.y - cj.y : cj.y - ci.y;
+                if (d2 <= Breq.hi && !(ci.x == cj.x && df < 3)) {
+                    bool in_req, pa, es, qa;
+                    if (in_band(Breq, d2) || (pauli_on && in_band(Bpa, d2)) || (es_on && in_band(Bes, d2)) ||
+                        (qa_on && in_band(Bqa, d2))) {
+                        const double dd = dist_exact(bx, pi, pos[b + lj]);
+                        const double inv = __ddiv_rn(1.0, dd);
+                        in_req = dd < rp.req_r;
+                        pa = inv > rp.pauli_min_inv;
+                        es = inv > rp.es_min_inv;
+                        qa = inv > rp.qa_min_inv;
+                    } else {
+                        in_req = d2 < Breq.lo;
+                        pa = d2 < Bpa.lo;
+                        es = d2 < Bes.lo;
+                        qa = d2 < Bqa.lo;
+                    }
+                    if (in_req) {
+                        if (pauli_on && pa) flags |= NL_PAULI;
+                        if (es_on && es && qi.w * qj.w != 0.0f) flags |= NL_ES;
+                        qa_free = qa_on && lj > li && qa;
+                    }
+                }
+            }
+            // natives leave the list only with native contacts enabled
+            // (main.cpp:504-530); the loop is warp-uniform
+            if (go_on && __any_sync(0xffffffffu, flags != 0 || qa_free)) {
+                for (int k = n0; k < n1; ++k)
+                    if (d.nat_j[k] == b + lj) { flags = 0; qa_free = false; }
+            }
+            if (qa_on && __any_sync(0xffffffffu, qa_free)) {
+                for (int k = 0; k < nref; ++k) {
+                    const int s = d.qa.ref[(size_t)k * d.N + i];
+                    const int other = d.qa.ct_i1[s] == i ? d.qa.ct_i2[s] : d.qa.ct_i1[s];
+                    if (other == b + lj) qa_free = false;
+                }
+            }
+            const unsigned km = __ballot_sync(0xffffffffu, flags != 0);
+            if (flags) {
+                const int at = cnt + __popc(km & lt);
+                if (at < cap) d.nl_row[(size_t)at * d.N + i] = (b + lj) | flags;
+            }
+            cnt += __popc(km);
+            if (qa_on) {
+                const unsigned qm = __ballot_sync(0xffffffffu, qa_free);
+                if (qa_free) {
+                    const int at = tcnt + __popc(qm & lt);
+                    if (at < QA_TMP_CAP) d.qa.tmp[(size_t)at * d.N + i] = b + lj;
+                }
+                tcnt += __popc(qm);
+            }
+        }
+        if (lane == 0) {
+            atomicMax(&d.ctr[1], (unsigned long long)cnt);
+            if (cnt > cap) {
+                atomicOr(d.status, ST_CAPACITY);
+                cnt = cap;
+            }
+            d.nl_cnt[i] = cnt;
+            d.orig[i] = pi;
+            if (qa_on) {
+                if (tcnt > QA_TMP_CAP) atomicOr(d.status, ST_CAPACITY);
+                d.qa.tmp_cnt[i] = min(tcnt, QA_TMP_CAP);
+            }
+        }
     }
 }
 
@@ -859,6 +1053,7 @@ void Engine::finalize() {
     std::vector<RepDev> rd(R);
     int fp_total = 0, ct_total = 0;
     std::vector<uint64_t> jumps(64 * (size_t)R);
+    std::vector<int2> chunks;
     int chain_base = 0;
     for (int k = 0; k < R; ++k) {
         RepHost &r = reps[k];
@@ -887,6 +1082,19 @@ void Engine::finalize() {
         derive_rep(k, rd[k]);
         rd[k].cell_off = cell_off[k];
         rd[k].cell_budget = cell_bud[k];
+        // Verlet build: whole-replica tiles up to TILE_MAX beads, else cells
+        rd[k].tile = p.nl_build == XMD_NL_BUILD_TILE ||
+                     (p.nl_build == XMD_NL_BUILD_AUTO && r.n <= TILE_MAX);
+        if (rd[k].tile && r.n > TILE_MAX)
+            throw std::invalid_argument("engine: nl build 'tile' takes replicas of at most " +
+                                        std::to_string(TILE_MAX) + " beads");
+        if (rd[k].tile) {
+            any_tile = true;
+            tile_smem = std::max(tile_smem, (sizeof(float4) + sizeof(int2)) * (size_t)r.n);
+            for (int c = 0; c < r.n; c += TL_CH) chunks.push_back(make_int2(k, r.begin + c));
+        } else {
+            any_cell = true;
+        }
         if (p.on[XMD_TERM_QA]) {
             rd[k].fp_off = fp_total;
             rd[k].fp_cap = r.n * QA_FP_PER_BEAD + 256;
@@ -906,6 +1114,13 @@ void Engine::finalize() {
         for (auto &e : nat[i]) { nat_j.push_back(e.first); nat_d.push_back(e.second); }
     }
     nat_start[N] = (int)nat_j.size();
+    d.nchunks = (int)chunks.size();
+    d.chunks = (int2 *)dalloc(sizeof(int2) * std::max<size_t>(1, chunks.size()));
+    if (!chunks.empty())
+        CK(cudaMemcpyAsync(d.chunks, chunks.data(), sizeof(int2) * chunks.size(), cudaMemcpyHostToDevice, stream));
+    d.any_cell = any_cell;
+    if (tile_smem > 48 * 1024)
+        CK(cudaFuncSetAttribute(k_nl_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem));
     size_t NN = nat_j.size();
     d.nat_j = (int32_t *)dalloc(sizeof(int32_t) * (NN ? NN : 1));
     d.nat_d = (double *)dalloc(sizeof(double) * (NN ? NN : 1));
@@ -1171,8 +1386,11 @@ void Engine::record(std::vector<cudaEvent_t> &pool, size_t &n) {
 
 void Engine::launch_rebuild() {
     if (timing) record(ev_rebuild, n_ev_rebuild);
-    k_cells<<<d.R, CB, 0, stream>>>(d, cur);
-    k_nl_build<<<(d.N + 127) / 128, 128, 0, stream>>>(d, tp, cur);
+    if (any_cell) {
+        k_cells<<<d.R, CB, 0, stream>>>(d, cur);
+        k_nl_build<<<(d.N + 127) / 128, 128, 0, stream>>>(d, tp, cur);
+    }
+    if (any_tile) k_nl_tile<<<d.nchunks, TL_THREADS, tile_smem, stream>>>(d, tp, cur);
     if (d.qa_on) k_qa_rebuild<<<d.R, 1024, 0, stream>>>(d);
     if (timing) record(ev_rebuild, n_ev_rebuild);
 }
@@ -1188,6 +1406,11 @@ bool Engine::grow_rows(double frac) {
     int ncap = (int)(2 * need + 16);
     int32_t *rows = nullptr;
     CK(cudaMalloc(&rows, sizeof(int32_t) * (size_t)ncap * d.N));
+    // rows are slot-major ([k][N]), so the current lists keep their place:
+    // growing for headroom leaves them valid without a rebuild
+    CK(cudaMemcpyAsync(rows, d.nl_row, sizeof(int32_t) * (size_t)std::min(nl_cap, ncap) * d.N,
+                       cudaMemcpyDeviceToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
     for (auto &a : allocs)
         if (a == (void *)d.nl_row) {
             CK(cudaFree(a));
@@ -1300,36 +1523,55 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
         cp.conditional.type = cudaGraphCondTypeIf;
         cp.conditional.size = 1;
         CK(cudaGraphAddNode(&ncond, g, &nc, nullptr, 1, &cp));
-        cudaGraph_t body = cp.conditional.phGraph_out[0];
-        cudaKernelNodeParams k1{}, k2{};
-        void *a1[] = {&d, &cn};
-        k1.func = (void *)k_cells;
-        k1.gridDim = dim3(d.R);
-        k1.blockDim = dim3(CB);
-        k1.kernelParams = a1;
-        void *a2[] = {&d, &tp, &cn};
-        k2.func = (void *)k_nl_build;
-        k2.gridDim = dim3((d.N + 127) / 128);
-        k2.blockDim = dim3(128);
-        k2.kernelParams = a2;
-        cudaGraphNode_t b1, b2;
-        CK(cudaGraphAddKernelNode(&b1, body, nullptr, 0, &k1));
-        CK(cudaGraphAddKernelNode(&b2, body, &b1, 1, &k2));
-        if (d.qa_on) {
-            cudaKernelNodeParams k3{};
-            void *a3[] = {&d};
-            k3.func = (void *)k_qa_rebuild;
-            k3.gridDim = dim3(d.R);
-            k3.blockDim = dim3(1024);
-            k3.kernelParams = a3;
-            cudaGraphNode_t b3;
-            CK(cudaGraphAddKernelNode(&b3, body, &b2, 1, &k3));
-        }
+        add_rebuild_nodes(cp.conditional.phGraph_out[0], cn);
         prev = ncond;
     }
     CK(cudaGraphInstantiate(&gs.exec, g, 0));
     gs.graph = g;
     return gs.exec;
+}
+
+// the list rebuild as a chain of kernel nodes (body of the rebuild IF node)
+void Engine::add_rebuild_nodes(cudaGraph_t body, int cn) {
+    cudaGraphNode_t last = nullptr;
+    auto add = [&](cudaKernelNodeParams &kp) {
+        cudaGraphNode_t nn;
+        CK(cudaGraphAddKernelNode(&nn, body, last ? &last : nullptr, last ? 1 : 0, &kp));
+        last = nn;
+    };
+    void *a1[] = {&d, &cn};
+    void *a2[] = {&d, &tp, &cn};
+    void *a3[] = {&d};
+    if (any_cell) {
+        cudaKernelNodeParams k1{}, k2{};
+        k1.func = (void *)k_cells;
+        k1.gridDim = dim3(d.R);
+        k1.blockDim = dim3(CB);
+        k1.kernelParams = a1;
+        add(k1);
+        k2.func = (void *)k_nl_build;
+        k2.gridDim = dim3((d.N + 127) / 128);
+        k2.blockDim = dim3(128);
+        k2.kernelParams = a2;
+        add(k2);
+    }
+    if (any_tile) {
+        cudaKernelNodeParams kt{};
+        kt.func = (void *)k_nl_tile;
+        kt.gridDim = dim3(d.nchunks);
+        kt.blockDim = dim3(TL_THREADS);
+        kt.sharedMemBytes = (unsigned)tile_smem;
+        kt.kernelParams = a2;
+        add(kt);
+    }
+    if (d.qa_on) {
+        cudaKernelNodeParams k3{};
+        k3.func = (void *)k_qa_rebuild;
+        k3.gridDim = dim3(d.R);
+        k3.blockDim = dim3(1024);
+        k3.kernelParams = a3;
+        add(k3);
+    }
 }
 
 void Engine::check_status(const char *where) {

@@ -32,6 +32,7 @@ struct RepDev {
     int dims[3];             // cells along periodic axes
     double lo[3], cs[3];     // bounding-box minimum and 1/cell edge along open axes
     int hashed;              // cells hashed into the bucket budget
+    int tile;                // Verlet build by whole-replica tiles (no cell grid)
     float pre2;              // squared FP32 pre-filter radius of the Verlet build
     int first, rebuild;
     unsigned long long maxdisp;
@@ -91,6 +92,9 @@ struct Dev {
     int *any_rebuild;
     int *status;            // device error word
     unsigned long long *ctr;  // [0]: list-rebuild passes launched
+    int2 *chunks;           // (replica, first bead) of each tile-build block
+    int nchunks;
+    int any_cell;           // some replica uses the cell-grid build
     int qa_on;
     QaDev qa;
 };
@@ -175,6 +179,9 @@ private:
     bool use_graphs = true;
     bool auto_grow = true;       // grow Verlet rows instead of failing
     cudaGraphExec_t graph_for(int start_cur);
+    bool any_cell = false, any_tile = false;   // which Verlet builds the replicas use
+    size_t tile_smem = 0;                      // dynamic shared memory of k_nl_tile
+    void add_rebuild_nodes(cudaGraph_t body, int cn);
     bool grow_rows(double frac);
     void drop_graphs();
 
@@ -190,6 +197,7 @@ private:
 
 std::string &last_error();
 uint64_t rng_jump(uint64_t state, uint64_t n_draws);
+double fp64_peak(int device);
 int verlet_pairs_noalloc(const double *d_r, const int32_t *d_chain, const int32_t *d_seq, int32_t n,
                          const double cell[3], double cutoff, int32_t *d_pairs, int32_t cap, int32_t *d_count,
                          void *stream);
