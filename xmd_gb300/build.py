@@ -23,8 +23,11 @@ ORACLE_SRC = ROOT / "oracle" / "xmd_oracle.c"
 ORACLE_LIB = ROOT / "oracle" / "liboracle.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
-CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC"]
+# Host code derives list radii and integrator constants that the device
+# compares against: no multiply-add contraction, so x86 and Arm hosts give the
+# same bits as the oracle (which is built the same way).
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "--expt-relaxed-constexpr"]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off"]
 
 CUDA_SOURCES = ["engine.cu", "noalloc.cu", "probe.cu"]
 CXX_SOURCES = ["capi.cpp", "config.cpp", "defaults_yml.cpp"]

@@ -86,6 +86,10 @@ __device__ __forceinline__ double dist2_exact(const BoxD &b, double4_32a u, doub
     for (int a = 0; a < 3; ++a) d[a] = __dsub_rn(d[a], __dmul_rn(b.cell[a], rint(__dmul_rn(d[a], b.cell_inv[a]))));
     return __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
 }
+__device__ __forceinline__ double dist2_open(double4_32a u, double4_32a w) {
+    const double x = __dsub_rn(w.x, u.x), y = __dsub_rn(w.y, u.y), z = __dsub_rn(w.z, u.z);
+    return __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
+}
 __device__ __forceinline__ double dist_exact(const BoxD &b, double4_32a u, double4_32a w) {
     return __dsqrt_rn(dist2_exact(b, u, w));
 }
@@ -193,10 +197,23 @@ __device__ __forceinline__ V3<double> dsub(double4_32a u, double4_32a w) {
 }
 __device__ __forceinline__ V3<float> f3(V3<double> a) { return V3<float>{(float)a.x, (float)a.y, (float)a.z}; }
 
-__device__ __forceinline__ void angle_mixed(const TermP &p, V3<double> r12d, V3<double> r23d, V3<double> xd,
+// tether of the mixed path from the narrowed bond vector r12 = r2 - r1
+__device__ __forceinline__ V3<float> tether_vec(const TermP &p, V3<float> r12, float nat_dist, float *V) {
+    float r12_n = norm(r12);
+    float dr = r12_n - nat_dist, dr2 = dr * dr;
+    float H1 = (float)p.tether_H1, H2 = (float)p.tether_H2;
+    float V_ = 0.5f * dr2 * (H1 + H2 * dr2);
+    float dV_dr = dr * (H1 + 2.0f * H2 * dr2);
+    *V = clampv<float>(V_, -1.0e3f, 1.0e3f);
+    dV_dr = clampv<float>(dV_dr, -1.0e3f, 1.0e3f);
+    const float inv = 1.0f / r12_n;
+    return dV_dr * V3<float>{r12.x * inv, r12.y * inv, r12.z * inv};
+}
+
+// r12, r23: narrowed bond vectors; x12_23: narrowed FP64 cross product
+__device__ __forceinline__ void angle_mixed(const TermP &p, V3<float> r12, V3<float> r23, V3<float> x12_23,
                                             float nat_theta, V3<float> *f1, V3<float> *f2, V3<float> *f3o,
                                             float *V) {
-    V3<float> r12 = f3(r12d), r23 = f3(r23d), x12_23 = f3(xd);
     float r12_rn = 1.0f / norm(r12), r23_rn = 1.0f / norm(r23);
     V3<float> d1 = r12_rn * unit(cross(r12, x12_23));
     V3<float> d3 = r23_rn * unit(cross(r23, x12_23));
@@ -211,15 +228,14 @@ __device__ __forceinline__ void angle_mixed(const TermP &p, V3<double> r12d, V3<
     *f3o = -(dV * d3);
 }
 
-__device__ __forceinline__ void dihedral_mixed(const TermP &p, V3<double> r12d, V3<double> r23d, V3<double> r34d,
-                                               V3<double> x1d, float nat_phi, bool cnd, bool snd, V3<float> *f,
+// narrowed bond vectors and cross products; X = x12_23 . x23_34 and
+// T = x12_23 . r34 taken in FP64 by the caller
+__device__ __forceinline__ void dihedral_mixed(const TermP &p, V3<float> r12, V3<float> r23, V3<float> r34,
+                                               V3<float> x12_23, V3<float> x23_34, float X, float T,
+                                               float nat_phi, bool cnd, bool snd, V3<float> *f,
                                                float *Vc, float *Vs) {
-    V3<double> x2d = cross(r23d, r34d);
-    double X = dot(x1d, x2d);
-    double T = dot(x1d, r34d);
-    V3<float> r12 = f3(r12d), r23 = f3(r23d), r34 = f3(r34d), x12_23 = f3(x1d), x23_34 = f3(x2d);
     float r23_n = norm(r23);
-    float phi = atan2f(r23_n * (float)T, (float)X);
+    float phi = atan2f(r23_n * T, X);
     float diff_ = phi - nat_phi;
     float dV = 0.0f;
     *Vc = 0.0f;
@@ -360,6 +376,15 @@ __device__ __forceinline__ void noise3f(uint64_t st, double *nx, double *ny, dou
     float r2 = sqrtf(-2.0f * logf(u3));
     if (isnan(r2)) r2 = 0.0f;
     *nz = r2 * cosf((float)(2.0 * 3.141592653589793) * u4);
+}
+// The same product from 16 nibble tables of 16 entries (entry [q][v] = XOR of
+// the columns 4q..4q+3 selected by the bits of v): 16 lookups instead of 64
+constexpr int JUMP_WORDS = 256;
+__device__ __forceinline__ uint64_t gf2_apply_nib(const uint64_t *__restrict__ tab, uint64_t x) {
+    uint64_t y = 0;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) y ^= __ldg(tab + 16 * q + (int)((x >> (4 * q)) & 15ull));
+    return y;
 }
 // 64x64 GF(2) matrix (columns) times state: the xorshift jump-ahead
 __device__ __forceinline__ uint64_t gf2_apply(const uint64_t *__restrict__ col, uint64_t x) {

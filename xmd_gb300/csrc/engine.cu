@@ -111,12 +111,32 @@ __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
     const int N = d.N, t = threadIdx.x, i0 = blockIdx.x * FB;
     __shared__ double4_32a P[FB + 6];
     __shared__ V3<FT> Ct[FB + 3], Ca[3][FB + 3], Cd[4][FB + 3];
+    // mixed path: bond vectors e_k = P[k+1] - P[k] and cross products
+    // x_k = e_{k-1} x e_k, formed once per tile slot in FP64 and shared by the
+    // tether, angle and dihedral centres that use them
+    constexpr int NE = sizeof(FT) == 4 ? FB + 5 : 1;
+    __shared__ V3<double> Ed[NE], Xd[NE];
+    __shared__ V3<float> Ef[NE], Xf[NE];
 
     for (int k = t; k < FB + 6; k += FB) {
         int idx = i0 - 3 + k;
         P[k] = (idx >= 0 && idx < N) ? pin[idx] : make_double4_32a(0, 0, 0, 0);
     }
     __syncthreads();
+    if constexpr (sizeof(FT) == 4) {
+        for (int k = t; k < NE; k += FB) {
+            V3<double> e = dsub(P[k], P[k + 1]);
+            Ed[k] = e;
+            Ef[k] = f3(e);
+        }
+        __syncthreads();
+        for (int k = t + 1; k < NE; k += FB) {
+            V3<double> x = cross(Ed[k - 1], Ed[k]);
+            Xd[k] = x;
+            Xf[k] = f3(x);
+        }
+        __syncthreads();
+    }
 
     // bonded contributions of centres c in [i0-2, i0+FB]
     for (int sc = t; sc < FB + 3; sc += FB) {
@@ -129,7 +149,8 @@ __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
         int rc = own ? d.rep_of[c] : 0;
         if ((fl & BF_TETH) && p.on[XMD_TERM_TETHER]) {
             FT V_;
-            ft = tether_term<FT>(p, P[sp], P[sp + 1], (FT)d.teth_r0[c], &V_);
+            if constexpr (sizeof(FT) == 4) ft = tether_vec(p, Ef[sp], (float)d.teth_r0[c], &V_);
+            else ft = tether_term<FT>(p, P[sp], P[sp + 1], (FT)d.teth_r0[c], &V_);
             if (MODE == 0 && own) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_TETHER], (double)V_);
         }
         const bool do_ang = (fl & BF_ANG) && p.on[XMD_TERM_NAT_ANG];
@@ -150,17 +171,17 @@ __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
                 }
             }
         } else if (do_ang || do_dih) {
-            // mixed path: FP64 bond vectors and cross products, FP32 forces
-            V3<double> r12 = dsub(P[sp - 1], P[sp]), r23 = dsub(P[sp], P[sp + 1]);
-            V3<double> x12_23 = cross(r12, r23);
+            // mixed path: FP64 bond vectors and cross products (shared slots),
+            // FP32 forces
             if (do_ang) {
                 float V_;
-                angle_mixed(p, r12, r23, x12_23, (float)d.ang_t0[c], &a1, &a2, &a3, &V_);
+                angle_mixed(p, Ef[sp - 1], Ef[sp], Xf[sp], (float)d.ang_t0[c], &a1, &a2, &a3, &V_);
                 if (MODE == 0 && own) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_NAT_ANG], (double)V_);
             }
             if (do_dih) {
                 float Vc, Vs;
-                dihedral_mixed(p, r12, r23, dsub(P[sp + 1], P[sp + 2]), x12_23, (float)d.dih_p0[c],
+                const float X = (float)dot(Xd[sp], Xd[sp + 1]), T = (float)dot(Xd[sp], Ed[sp + 1]);
+                dihedral_mixed(p, Ef[sp - 1], Ef[sp], Ef[sp + 1], Xf[sp], Xf[sp + 1], X, T, (float)d.dih_p0[c],
                                p.on[XMD_TERM_CND] != 0, p.on[XMD_TERM_SND] != 0, q, &Vc, &Vs);
                 if (MODE == 0 && own) {
                     if (p.on[XMD_TERM_CND]) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_CND], (double)Vc);
@@ -178,15 +199,23 @@ __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
     if (i >= N) return;
     const int s = t + 2;   // centre slot of bead i
     double fx = 0, fy = 0, fz = 0;
-    add3(fx, fy, fz, Ct[s]);
-    add3(fx, fy, fz, -Ct[s - 1]);
-    add3(fx, fy, fz, Ca[2][s - 1]);
-    add3(fx, fy, fz, Ca[1][s]);
-    add3(fx, fy, fz, Ca[0][s + 1]);
-    add3(fx, fy, fz, Cd[0][s + 1]);
-    add3(fx, fy, fz, Cd[1][s]);
-    add3(fx, fy, fz, Cd[2][s - 1]);
-    add3(fx, fy, fz, Cd[3][s - 2]);
+    if constexpr (sizeof(FT) == 4) {
+        // the bonded contributions, computed in FP32, are summed in FP32 and
+        // enter the FP64 accumulator once
+        V3<float> bsum = Ct[s] - Ct[s - 1] + Ca[2][s - 1] + Ca[1][s] + Ca[0][s + 1] + Cd[0][s + 1] + Cd[1][s] +
+                         Cd[2][s - 1] + Cd[3][s - 2];
+        add3(fx, fy, fz, bsum);
+    } else {
+        add3(fx, fy, fz, Ct[s]);
+        add3(fx, fy, fz, -Ct[s - 1]);
+        add3(fx, fy, fz, Ca[2][s - 1]);
+        add3(fx, fy, fz, Ca[1][s]);
+        add3(fx, fy, fz, Ca[0][s + 1]);
+        add3(fx, fy, fz, Cd[0][s + 1]);
+        add3(fx, fy, fz, Cd[1][s]);
+        add3(fx, fy, fz, Cd[2][s - 1]);
+        add3(fx, fy, fz, Cd[3][s - 2]);
+    }
 
     const double4_32a pi = P[t + 3];
     const int r = d.rep_of[i];
@@ -286,8 +315,8 @@ __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
     double nz[3];
     if (sizeof(FT) == 8) noise3(st, &nz[0], &nz[1], &nz[2]);
     else noise3f(st, &nz[0], &nz[1], &nz[2]);
-    d.rng[i] = gf2_apply(d.jump + 64 * r, st);
-    const double dt = p.dt, dt_inv = 1.0 / dt, h = dt * dt / 2.0;
+    d.rng[i] = gf2_apply_nib(d.jump + JUMP_WORDS * r, st);
+    const double dt_inv = p.dt_inv, h = p.dt2_half;
     const double gamma = p.gamma_factor * 1.0;
     const double nsd = d.rep[r].noise_sd;
     const double F3[3] = {fx, fy, fz};
@@ -324,7 +353,19 @@ __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
     // skin test displacement: norm(box->r_uv(r_, orig_r_)), verify.cpp:12-14
     // squared; the check takes one square root of the maximum (sqrt is
     // monotone and correctly rounded, so that equals the max of the norms)
-    double disp = dist2_exact(bx, pn, d.orig[i]);
+    double disp;
+    if constexpr (sizeof(FT) == 4) {
+        // mixed path: the FP64 displacement narrowed, squared in FP32
+        const double4_32a o = d.orig[i];
+        float ex = (float)(pn.x - o.x), ey = (float)(pn.y - o.y), ez = (float)(pn.z - o.z);
+        ex -= (float)bx.cell[0] * rintf(ex * (float)bx.cell_inv[0]);
+        ey -= (float)bx.cell[1] * rintf(ey * (float)bx.cell_inv[1]);
+        ez -= (float)bx.cell[2] * rintf(ez * (float)bx.cell_inv[2]);
+        disp = (double)(ex * ex + ey * ey + ez * ez);
+    } else {
+        // on open axes the wrap subtracts exactly zero: skipping it changes no bit
+        disp = per ? dist2_exact(bx, pn, d.orig[i]) : dist2_open(pn, d.orig[i]);
+    }
     const unsigned lane = t & 31;
     int r0 = __shfl_sync(0xffffffffu & __activemask(), r, 0);
     unsigned mask = __activemask();
@@ -1038,7 +1079,7 @@ void Engine::finalize() {
     d.bead_cell = (int32_t *)dalloc(sizeof(int32_t) * N);
     d.cell_pos = (float4 *)dalloc(sizeof(float4) * N);
     d.rng = (uint64_t *)dalloc(sizeof(uint64_t) * N);
-    d.jump = (uint64_t *)dalloc(sizeof(uint64_t) * 64 * R);
+    d.jump = (uint64_t *)dalloc(sizeof(uint64_t) * JUMP_WORDS * R);
     d.rep = (RepDev *)dalloc(sizeof(RepDev) * R);
     d.any_rebuild = (int *)dalloc(sizeof(int) * 4);
     d.status = (int *)dalloc(sizeof(int) * 4);
@@ -1052,7 +1093,7 @@ void Engine::finalize() {
     std::vector<std::vector<std::pair<int, double>>> nat(N);
     std::vector<RepDev> rd(R);
     int fp_total = 0, ct_total = 0;
-    std::vector<uint64_t> jumps(64 * (size_t)R);
+    std::vector<uint64_t> jumps(JUMP_WORDS * (size_t)R);
     std::vector<int2> chunks;
     int chain_base = 0;
     for (int k = 0; k < R; ++k) {
@@ -1104,7 +1145,14 @@ void Engine::finalize() {
             ct_total += rd[k].ct_cap;
         }
         GF2 j = gf2_jump(4ull * (uint64_t)r.n);
-        std::copy(j.begin(), j.end(), jumps.begin() + 64 * (size_t)k);
+        // nibble tables: entry [q][v] = XOR of the columns 4q+b for the bits b of v
+        for (int q = 0; q < 16; ++q)
+            for (int v = 0; v < 16; ++v) {
+                uint64_t e = 0;
+                for (int bb = 0; bb < 4; ++bb)
+                    if ((v >> bb) & 1) e ^= j[4 * q + bb];
+                jumps[JUMP_WORDS * (size_t)k + 16 * q + v] = e;
+            }
     }
     std::vector<int32_t> nat_j;
     std::vector<double> nat_d;
@@ -1140,13 +1188,15 @@ void Engine::finalize() {
         CK(cudaMemcpyAsync(d.nat_d, nat_d.data(), sizeof(double) * NN, cudaMemcpyHostToDevice, stream));
     }
     CK(cudaMemcpyAsync(d.rep, rd.data(), sizeof(RepDev) * R, cudaMemcpyHostToDevice, stream));
-    CK(cudaMemcpyAsync(d.jump, jumps.data(), sizeof(uint64_t) * 64 * R, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d.jump, jumps.data(), sizeof(uint64_t) * JUMP_WORDS * R, cudaMemcpyHostToDevice, stream));
     CK(cudaStreamSynchronize(stream));
 
     // term parameters
     std::memset(&tp, 0, sizeof tp);
     for (int k = 0; k < XMD_NUM_TERMS; ++k) tp.on[k] = p.on[k];
     tp.dt = p.dt;
+    tp.dt_inv = 1.0 / p.dt;
+    tp.dt2_half = p.dt * p.dt / 2.0;
     tp.gamma_factor = p.gamma_factor;
     tp.tether_H1 = p.tether_H1; tp.tether_H2 = p.tether_H2;
     tp.nat_ang_k = p.nat_ang_k; tp.cnd_CDA = p.cnd_CDA; tp.cnd_CDB = p.cnd_CDB; tp.snd_CDH = p.snd_CDH;

@@ -87,7 +87,7 @@ struct Dev {
     int32_t *cell_cnt, *cell_start, *cell_fill, *cell_items, *bead_cell;
     float4 *cell_pos;       // bucket-sorted FP32 coordinates (+ bead index bits)
     uint64_t *rng;          // per-bead generator state
-    uint64_t *jump;         // [R][64] GF(2) jump matrices (4 N_r draws)
+    uint64_t *jump;         // [R][16][16] nibble tables of the GF(2) jump (4 N_r draws)
     RepDev *rep;
     int *any_rebuild;
     int *status;            // device error word

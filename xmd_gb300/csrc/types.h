@@ -15,6 +15,7 @@ struct BoxD {
 struct TermP {
     int on[XMD_NUM_TERMS];
     double dt, gamma_factor;
+    double dt_inv, dt2_half;     // 1.0 / dt and dt * dt / 2.0, as lang_pc.cpp:8, 21 round them
     double tether_H1, tether_H2;
     double nat_ang_k, cnd_CDA, cnd_CDB, snd_CDH;
     double go_depth;
