@@ -250,6 +250,65 @@ int xmd_gpu_kernel_times(xmd_gpu_ctx *ctx, double *force_ms, int64_t *force_laun
  * step kernels are reported.  Takes about 0.1 s. */
 int xmd_gpu_fp64_peak(int32_t device, double *tflops);
 
+/* ---- dynamic membership ----------------------------------------------------- */
+/* No counterpart in the reference (its driver simulates one system).  After
+ * xmd_gpu_reserve the context holds fixed device capacities; replicas can then
+ * be added (placed at the next eval/step, or by xmd_gpu_server admission) and
+ * removed between steps, their slots and device ranges reused.  A replica's
+ * results do not depend on which other replicas share the context. */
+int xmd_gpu_reserve(xmd_gpu_ctx *ctx, int32_t beads, int32_t replicas, int32_t native_entries);
+int xmd_gpu_remove_replica(xmd_gpu_ctx *ctx, int32_t rep);
+/* per-replica step budget: the replica stops (state kept) after nsteps more
+ * steps; -1 = no bound (the default) */
+int xmd_gpu_set_steps(xmd_gpu_ctx *ctx, int32_t rep, int64_t nsteps);
+/* out[k] = steps left for replica slot k (-1 unbounded, -2 free slot);
+ * out holds the reserved replica capacity (or the replica count) */
+int xmd_gpu_steps_left(xmd_gpu_ctx *ctx, int64_t *out);
+
+/* ---- serving: continuous batching ------------------------------------------- */
+/* No counterpart in the reference.  A server owns one context and a worker
+ * thread.  Requests (one independent system each: any number of chains, its
+ * own temperature, seed and step count) are admitted first come first served
+ * into replica slots while the capacity reserved from `hbm_budget_bytes`
+ * (and at most `max_beads` beads) has room; every admitted request advances
+ * in the same batched launches, `chunk_steps` steps at a time, and leaves as
+ * soon as its steps are done.  Input arrays are copied at submission. */
+typedef struct xmd_gpu_server xmd_gpu_server;
+typedef struct {
+    int32_t n;                                   /* beads */
+    const int32_t *chain_idx, *seq_idx;          /* [n] */
+    const uint8_t *atype;                        /* [n] amino-acid codes */
+    const double *cell;                          /* [3] box (0 = open), NULL = open */
+    double temperature;                          /* eps/kB; <= 0: langevin: temperature */
+    uint64_t seed;
+    int32_t n_tethers;  const int32_t *teth_i1, *teth_i2;  const double *teth_d;
+    int32_t n_angles;   const int32_t *ang_i1, *ang_i2, *ang_i3;  const double *ang_theta;
+    int32_t n_dihedrals; const int32_t *dih_i1, *dih_i2, *dih_i3, *dih_i4; const double *dih_phi;
+    int32_t n_natives;  const int32_t *nat_i1, *nat_i2;  const double *nat_d;
+    const double *r, *v;                         /* [3n] initial positions, velocities (NULL = 0) */
+    int64_t nsteps;
+} xmd_request;
+enum { XMD_REQ_QUEUED = 0, XMD_REQ_RUNNING = 1, XMD_REQ_DONE = 2, XMD_REQ_FAILED = -1 };
+enum {
+    XMD_SRV_P50_S = 0, XMD_SRV_P99_S, XMD_SRV_BEAD_STEPS_PER_S, XMD_SRV_COMPLETED, XMD_SRV_QUEUED,
+    XMD_SRV_RUNNING, XMD_SRV_CHUNKS, XMD_SRV_PEAK_RUNNING, XMD_SRV_CAP_BEADS, XMD_SRV_BEAD_STEPS,
+    XMD_SRV_SPAN_S, XMD_SRV_NUM
+};
+int xmd_gpu_server_create(const char *yaml_text, int64_t hbm_budget_bytes, int32_t max_beads,
+                          int32_t chunk_steps, xmd_gpu_server **out);
+int xmd_gpu_server_submit(xmd_gpu_server *srv, const xmd_request *req, int64_t *id);
+/* *state = XMD_REQ_* */
+int xmd_gpu_server_poll(xmd_gpu_server *srv, int64_t id, int32_t *state);
+/* waits for the request, copies its final state ([3n] each, NULL skips) and
+ * latency (submission to completion, s), and forgets it */
+int xmd_gpu_server_result(xmd_gpu_server *srv, int64_t id, double *r, double *v, double *t, double *latency_s);
+int xmd_gpu_server_wait_all(xmd_gpu_server *srv);
+/* out[XMD_SRV_NUM]: latency percentiles of completed requests, throughput
+ * (bead-steps of completed requests over first submission to last
+ * completion), counters */
+int xmd_gpu_server_stats(xmd_gpu_server *srv, double *out);
+int xmd_gpu_server_destroy(xmd_gpu_server *srv);
+
 /* ---- allocation-free pair search --------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device
  * memory where they need a pair list: code running while a CUDA graph is

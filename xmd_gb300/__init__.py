@@ -4,5 +4,6 @@ include/xmd_gpu.h."""
 from . import abi, synth
 from .abi import parse_params, XmdError
 from .engine import Engine
+from .server import Server
 
-__all__ = ["abi", "synth", "parse_params", "XmdError", "Engine"]
+__all__ = ["abi", "synth", "parse_params", "XmdError", "Engine", "Server"]

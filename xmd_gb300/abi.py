@@ -57,6 +57,25 @@ class Params(C.Structure):
         return out
 
 
+class Request(C.Structure):
+    """xmd_request (include/xmd_gpu.h)."""
+    _pi, _pdd, _pu = C.POINTER(C.c_int32), C.POINTER(C.c_double), C.POINTER(C.c_uint8)
+    _fields_ = [
+        ("n", _i), ("chain_idx", _pi), ("seq_idx", _pi), ("atype", _pu), ("cell", _pdd),
+        ("temperature", _d), ("seed", C.c_uint64),
+        ("n_tethers", _i), ("teth_i1", _pi), ("teth_i2", _pi), ("teth_d", _pdd),
+        ("n_angles", _i), ("ang_i1", _pi), ("ang_i2", _pi), ("ang_i3", _pi), ("ang_theta", _pdd),
+        ("n_dihedrals", _i), ("dih_i1", _pi), ("dih_i2", _pi), ("dih_i3", _pi), ("dih_i4", _pi),
+        ("dih_phi", _pdd),
+        ("n_natives", _i), ("nat_i1", _pi), ("nat_i2", _pi), ("nat_d", _pdd),
+        ("r", _pdd), ("v", _pdd), ("nsteps", C.c_int64),
+    ]
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, -1
+SRV_KEYS = ["p50_s", "p99_s", "bead_steps_per_s", "completed", "queued", "running", "chunks", "peak_running",
+            "cap_beads", "bead_steps", "span_s"]
+
 LIB_PATH = Path(__file__).resolve().parent / "libxmdgpu.so"
 
 P = C.POINTER
@@ -104,6 +123,17 @@ SIGNATURES = [
     ("xmd_gpu_kernel_times", C.c_int, [C.c_void_p, _pd, P(C.c_int64), _pd, P(C.c_int64)]),
     ("xmd_gpu_synchronize", C.c_int, [C.c_void_p]),
     ("xmd_gpu_fp64_peak", C.c_int, [C.c_int32, _pd]),
+    ("xmd_gpu_reserve", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
+    ("xmd_gpu_remove_replica", C.c_int, [C.c_void_p, C.c_int32]),
+    ("xmd_gpu_set_steps", C.c_int, [C.c_void_p, C.c_int32, C.c_int64]),
+    ("xmd_gpu_steps_left", C.c_int, [C.c_void_p, P(C.c_int64)]),
+    ("xmd_gpu_server_create", C.c_int, [C.c_char_p, C.c_int64, C.c_int32, C.c_int32, P(C.c_void_p)]),
+    ("xmd_gpu_server_submit", C.c_int, [C.c_void_p, P(Request), P(C.c_int64)]),
+    ("xmd_gpu_server_poll", C.c_int, [C.c_void_p, C.c_int64, _pi32]),
+    ("xmd_gpu_server_result", C.c_int, [C.c_void_p, C.c_int64, _pd, _pd, _pd, _pd]),
+    ("xmd_gpu_server_wait_all", C.c_int, [C.c_void_p]),
+    ("xmd_gpu_server_stats", C.c_int, [C.c_void_p, _pd]),
+    ("xmd_gpu_server_destroy", C.c_int, [C.c_void_p]),
 ]
 
 _lib = None

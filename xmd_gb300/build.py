@@ -30,7 +30,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contra
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off"]
 
 CUDA_SOURCES = ["engine.cu", "noalloc.cu", "probe.cu"]
-CXX_SOURCES = ["capi.cpp", "config.cpp", "defaults_yml.cpp"]
+CXX_SOURCES = ["capi.cpp", "config.cpp", "defaults_yml.cpp", "server.cpp"]
 
 
 def _nvcc() -> str:

@@ -5,13 +5,20 @@
 #include <sstream>
 #include <stdexcept>
 #include <string>
+#include <vector>
+#include <memory>
+#include <algorithm>
 
 #include "../../include/xmd_gpu.h"
 #include "config.h"
 #include "engine.h"
+#include "server.h"
 
 struct xmd_gpu_ctx {
     xmdg::Engine *eng = nullptr;
+};
+struct xmd_gpu_server {
+    xmdg::Server *srv = nullptr;
 };
 
 namespace {
@@ -240,6 +247,127 @@ int xmd_gpu_stats(xmd_gpu_ctx *ctx, int64_t *out) {
 int xmd_gpu_set_kernel_timing(xmd_gpu_ctx *ctx, int on) {
     NEED_CTX;
     return guard([&] { ctx->eng->use_device(); ctx->eng->set_kernel_timing(on != 0); });
+}
+
+int xmd_gpu_reserve(xmd_gpu_ctx *ctx, int32_t beads, int32_t replicas, int32_t native_entries) {
+    NEED_CTX;
+    return guard([&] {
+        ctx->eng->use_device();
+        ctx->eng->reserve(beads, replicas, native_entries);
+    });
+}
+
+int xmd_gpu_remove_replica(xmd_gpu_ctx *ctx, int32_t rep) {
+    NEED_CTX;
+    return guard([&] { ctx->eng->remove_replica(rep); });
+}
+
+int xmd_gpu_set_steps(xmd_gpu_ctx *ctx, int32_t rep, int64_t nsteps) {
+    NEED_CTX;
+    return guard([&] { ctx->eng->set_steps(rep, nsteps); });
+}
+
+int xmd_gpu_steps_left(xmd_gpu_ctx *ctx, int64_t *out) {
+    NEED_CTX;
+    if (!out) return fail(XMD_ERR_ARG, "null output");
+    return guard([&] {
+        std::vector<long long> v(std::max<size_t>(1, ctx->eng->reps.size()));
+        ctx->eng->steps_left(v.data());
+        for (size_t k = 0; k < ctx->eng->reps.size(); ++k) out[k] = v[k];
+    });
+}
+
+#define NEED_SRV \
+    if (!srv || !srv->srv) return fail(XMD_ERR_ARG, "null server");
+
+int xmd_gpu_server_create(const char *yaml_text, int64_t hbm_budget_bytes, int32_t max_beads, int32_t chunk_steps,
+                          xmd_gpu_server **out) {
+    if (!out) return fail(XMD_ERR_ARG, "null output");
+    *out = nullptr;
+    xmd_params p;
+    int rc = guard([&] { xmdg::params_from_yaml(yaml_text ? yaml_text : "", &p); });
+    if (rc) return rc;
+    return guard([&] {
+        auto *h = new xmd_gpu_server;
+        try {
+            h->srv = new xmdg::Server(p, hbm_budget_bytes, max_beads, chunk_steps);
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *out = h;
+    });
+}
+
+int xmd_gpu_server_submit(xmd_gpu_server *srv, const xmd_request *q, int64_t *id) {
+    NEED_SRV;
+    if (!q || !id) return fail(XMD_ERR_ARG, "null request");
+    if (q->n <= 0 || !q->chain_idx || !q->seq_idx || !q->atype || !q->r)
+        return fail(XMD_ERR_ARG, "request needs n > 0, topology and positions");
+    return guard([&] {
+        auto r = std::make_unique<xmdg::Request>();
+        const int n = q->n;
+        r->n = n;
+        r->chain.assign(q->chain_idx, q->chain_idx + n);
+        r->seq.assign(q->seq_idx, q->seq_idx + n);
+        r->atype.assign(q->atype, q->atype + n);
+        for (int a = 0; a < 3; ++a) r->cell[a] = q->cell ? q->cell[a] : 0.0;
+        r->temperature = q->temperature;
+        r->seed = q->seed;
+        auto cp = [](std::vector<int32_t> &dst, const int32_t *src, int m) {
+            if (m > 0 && !src) throw std::invalid_argument("null topology array");
+            dst.assign(src, src + std::max(0, m));
+        };
+        auto cpd = [](std::vector<double> &dst, const double *src, int m) {
+            if (m > 0 && src) dst.assign(src, src + m);
+            else dst.assign(std::max(0, m), 0.0);
+        };
+        cp(r->t1, q->teth_i1, q->n_tethers); cp(r->t2, q->teth_i2, q->n_tethers); cpd(r->td, q->teth_d, q->n_tethers);
+        cp(r->a1, q->ang_i1, q->n_angles); cp(r->a2, q->ang_i2, q->n_angles); cp(r->a3, q->ang_i3, q->n_angles);
+        if (q->n_angles > 0 && !q->ang_theta) throw std::invalid_argument("null native angles");
+        cpd(r->ath, q->ang_theta, q->n_angles);
+        cp(r->d1, q->dih_i1, q->n_dihedrals); cp(r->d2, q->dih_i2, q->n_dihedrals);
+        cp(r->d3, q->dih_i3, q->n_dihedrals); cp(r->d4, q->dih_i4, q->n_dihedrals);
+        if (q->n_dihedrals > 0 && !q->dih_phi) throw std::invalid_argument("null native dihedrals");
+        cpd(r->dph, q->dih_phi, q->n_dihedrals);
+        cp(r->n1, q->nat_i1, q->n_natives); cp(r->n2, q->nat_i2, q->n_natives);
+        if (q->n_natives > 0 && !q->nat_d) throw std::invalid_argument("null native distances");
+        cpd(r->nd, q->nat_d, q->n_natives);
+        r->r.assign(q->r, q->r + 3 * (size_t)n);
+        if (q->v) r->v.assign(q->v, q->v + 3 * (size_t)n);
+        r->nsteps = q->nsteps;
+        *id = srv->srv->submit(std::move(r));
+    });
+}
+
+int xmd_gpu_server_poll(xmd_gpu_server *srv, int64_t id, int32_t *state) {
+    NEED_SRV;
+    if (!state) return fail(XMD_ERR_ARG, "null output");
+    return guard([&] { *state = srv->srv->poll(id); });
+}
+
+int xmd_gpu_server_result(xmd_gpu_server *srv, int64_t id, double *r, double *v, double *t, double *latency_s) {
+    NEED_SRV;
+    return guard([&] { srv->srv->result(id, r, v, t, latency_s); });
+}
+
+int xmd_gpu_server_wait_all(xmd_gpu_server *srv) {
+    NEED_SRV;
+    return guard([&] { srv->srv->wait_all(); });
+}
+
+int xmd_gpu_server_stats(xmd_gpu_server *srv, double *out) {
+    NEED_SRV;
+    if (!out) return fail(XMD_ERR_ARG, "null output");
+    return guard([&] { srv->srv->stats(out); });
+}
+
+int xmd_gpu_server_destroy(xmd_gpu_server *srv) {
+    if (!srv) return XMD_OK;
+    return guard([&] {
+        delete srv->srv;
+        delete srv;
+    });
 }
 
 int xmd_gpu_fp64_peak(int32_t device, double *tflops) {

@@ -107,6 +107,7 @@ __device__ __forceinline__ void add3(double &fx, double &fy, double &fz, V3<FT> 
 //         displacement (verify.cpp:10-15).
 template <class FT, int MODE>
 __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
+    if (!d.blk_on[blockIdx.x]) return;   // no placed bead in this block (uniform)
     const double4_32a *__restrict__ pin = d.pos[cur];
     const int N = d.N, t = threadIdx.x, i0 = blockIdx.x * FB;
     __shared__ double4_32a P[FB + 6];
@@ -197,6 +198,13 @@ __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
 
     const int i = i0 + t;
     if (i >= N) return;
+    const int r = d.rep_of[i];
+    if (r < 0) return;     // free bead slot
+    if (MODE == 1 && d.rep[r].steps_left == 0) {
+        // the replica has taken its steps: it keeps its state (both buffers)
+        d.pos[cur ^ 1][i] = P[t + 3];
+        return;
+    }
     const int s = t + 2;   // centre slot of bead i
     double fx = 0, fy = 0, fz = 0;
     if constexpr (sizeof(FT) == 4) {
@@ -218,13 +226,12 @@ __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
     }
 
     const double4_32a pi = P[t + 3];
-    const int r = d.rep_of[i];
     const BoxD bx = d.rep[r].box;
     const bool per = bx.cell_inv[0] != 0.0 || bx.cell_inv[1] != 0.0 || bx.cell_inv[2] != 0.0;
     double vgo = 0, vpa = 0, ves = 0;
 
     if (p.on[XMD_TERM_GO]) {
-        const int k1 = d.nat_start[i + 1];
+        const int k1 = d.nat_end[i];
         for (int k = d.nat_start[i]; k < k1; ++k) {
             if (!d.nat_on[k]) continue;
             int j = d.nat_j[k];
@@ -386,10 +393,19 @@ __global__ void k_nl_check(Dev d, int advance, double dt, cudaGraphConditionalHa
     int any = 0;
     for (int r = threadIdx.x; r < d.R; r += blockDim.x) {
         RepDev &rp = d.rep[r];
-        if (advance) rp.t += dt;                       // *t = (*true_t += dt)
+        if (!rp.active) continue;
+        if (advance && rp.steps_left == 0) {           // took no step (k_force kept it)
+            rp.rebuild = 0;
+            continue;
+        }
+        if (advance) {
+            rp.t += dt;                                // *t = (*true_t += dt)
+            if (rp.steps_left > 0) rp.steps_left -= 1;
+        }
         double md = __dsqrt_rn(__longlong_as_double((long long)rp.maxdisp));
         rp.maxdisp = 0ull;
         int rb = rp.first || (2.0 * md + 0.0 > rp.pad);
+        if (advance && rp.steps_left == 0 && !rp.first) rb = 0;   // no further step uses a list
         rp.rebuild = rb;
         any |= rb;
     }
@@ -401,10 +417,11 @@ __global__ void k_nl_check(Dev d, int advance, double dt, cudaGraphConditionalHa
     }
 }
 
-// every replica rebuilds at the next check (after the rows were reallocated)
+// the replicas whose rebuild overflowed the rows rebuild again at the next
+// check (after the rows were reallocated); the others keep their lists
 __global__ void k_mark_all(Dev d) {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r < d.R) d.rep[r].first = 1;
+    if (r < d.R && d.rep[r].active && d.rep[r].rebuild) d.rep[r].first = 1;
 }
 
 // ---- cell lists: one block per flagged replica -----------------------------------
@@ -443,7 +460,7 @@ __global__ void __launch_bounds__(CB) k_cells(Dev d, int cur) {
     const int r = blockIdx.x;
     if (r == 0 && threadIdx.x == 0) atomicAdd(d.ctr, 1ull);
     RepDev &rp = d.rep[r];
-    if (!rp.rebuild || rp.tile) return;
+    if (!rp.active || !rp.rebuild || rp.tile) return;
     const double4_32a *pos = d.pos[cur];
     const int b = rp.begin, n = rp.n, off = rp.cell_off, bud = rp.cell_budget;
     __shared__ double red_lo[3][32], red_hi[3][32];
@@ -562,13 +579,14 @@ __global__ void __launch_bounds__(128) k_nl_build(Dev d, TermP p, int cur) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.N) return;
     const int r = d.rep_of[i];
+    if (r < 0) return;
     const RepDev &rp = d.rep[r];
     if (!rp.rebuild || rp.tile) return;
     const double4_32a *pos = d.pos[cur];
     const double4_32a pi = pos[i];
     const BoxD bx = rp.box;
     const int ci = d.chain[i], si = d.seq[i];
-    const int n0 = d.nat_start[i], n1 = d.nat_start[i + 1];
+    const int n0 = d.nat_start[i], n1 = d.nat_end[i];
     const double pad = rp.pad;
 
     // Go list: update_go_contacts, go.cpp:11-22
@@ -710,8 +728,9 @@ __global__ void __launch_bounds__(TL_THREADS) k_nl_tile(Dev d, TermP p, int cur)
     if (blockIdx.x == 0 && threadIdx.x == 0 && !d.any_cell) atomicAdd(d.ctr, 1ull);
     const int2 chk = d.chunks[blockIdx.x];
     const int r = chk.x;
+    if (r < 0) return;   // free chunk slot
     RepDev &rp = d.rep[r];
-    if (!rp.rebuild || !rp.tile) return;
+    if (!rp.active || !rp.rebuild || !rp.tile) return;
     extern __shared__ float4 tl_smem[];
     const int b = rp.begin, n = rp.n;
     float4 *sq = tl_smem;
@@ -763,7 +782,7 @@ __global__ void __launch_bounds__(TL_THREADS) k_nl_tile(Dev d, TermP p, int cur)
         const float4 qi = sq[li];
         const int2 ci = scs[li];
         const double4_32a pi = pos[i];
-        const int n0 = d.nat_start[i], n1 = d.nat_start[i + 1];
+        const int n0 = d.nat_start[i], n1 = d.nat_end[i];
 
         // Go list: update_go_contacts, go.cpp:11-22
         for (int k = n0 + lane; k < n1; k += 32) {
@@ -909,7 +928,8 @@ void Engine::release() {
 
 int Engine::add_replica(int n, const int32_t *chain, const int32_t *seq, const uint8_t *atype,
                         const double cell[3], double temperature, uint64_t seed) {
-    if (finalized) throw std::invalid_argument("replicas must be added before the first eval/step");
+    if (finalized && !dynamic)
+        throw std::invalid_argument("replicas must be added before the first eval/step (or reserve capacity)");
     if (n <= 0 || n > NL_MASK) throw std::invalid_argument("bead count out of range");
     if (!chain || !seq || !atype) throw std::invalid_argument("null topology array");
     RepHost r;
@@ -929,12 +949,100 @@ int Engine::add_replica(int n, const int32_t *chain, const int32_t *seq, const u
     r.teth_r0.assign(n, nan);
     r.ang_t0.assign(n, nan);
     r.dih_p0.assign(n, nan);
+    if (dynamic) {
+        // reuse a free slot; the replica is placed at the next eval/step
+        for (int k = 0; k < (int)reps.size(); ++k)
+            if (!reps[k].in_use) {
+                reps[k] = std::move(r);
+                return k;
+            }
+        if ((int)reps.size() >= cap.reps) throw std::length_error("engine: every reserved replica slot is taken");
+    }
     reps.push_back(std::move(r));
     return (int)reps.size() - 1;
 }
 
 static void check_rep(const std::vector<RepHost> &reps, int rep) {
-    if (rep < 0 || rep >= (int)reps.size()) throw std::invalid_argument("replica id out of range");
+    if (rep < 0 || rep >= (int)reps.size() || !reps[rep].in_use)
+        throw std::invalid_argument("replica id out of range");
+}
+
+void Engine::reserve(int beads, int replicas, int natives) {
+    if (finalized) throw std::logic_error("reserve must precede the first eval/step");
+    if (params.on[XMD_TERM_QA]) throw std::invalid_argument("reserve: the quasi-adiabatic term needs a static context");
+    if (beads < 1 || replicas < 1 || natives < 0) throw std::invalid_argument("reserve: bad capacity");
+    int nb = 0;
+    for (auto &r : reps) nb += r.n;
+    if (nb > beads || (int)reps.size() > replicas) throw std::invalid_argument("reserve: replicas already exceed it");
+    dynamic = true;
+    cap = Caps{};
+    cap.beads = beads;
+    cap.reps = replicas;
+    cap.nat = natives;
+    // bucket pool for replicas above the tile limit; chunk slots for the rest
+    cap.cells = params.nl_build == XMD_NL_BUILD_TILE ? 0 : std::max(64, 2 * beads);
+    cap.chunks = params.nl_build == XMD_NL_BUILD_CELL ? 0 : beads / TL_CH + replicas;
+    finalize();
+}
+
+void Engine::remove_replica(int rep) {
+    check_rep(reps, rep);
+    if (!dynamic) throw std::logic_error("remove_replica needs a context with reserved capacity");
+    RepHost &r = reps[rep];
+    if (r.placed) {
+        use_device();
+        const int b = r.begin, n = r.n;
+        CK(cudaStreamSynchronize(stream));
+        CK(cudaMemsetAsync(d.rep_of + b, 0xff, sizeof(int32_t) * n, stream));
+        CK(cudaMemsetAsync(d.bflags + b, 0, sizeof(uint32_t) * n, stream));
+        CK(cudaMemsetAsync(d.nl_cnt + b, 0, sizeof(int32_t) * n, stream));
+        if (r.nat_len) CK(cudaMemsetAsync(d.nat_on + r.nat_off, 0, r.nat_len, stream));
+        if (r.chunk_len) CK(cudaMemsetAsync(d.chunks + r.chunk_off, 0xff, sizeof(int2) * r.chunk_len, stream));
+        CK(cudaMemsetAsync(d.rep + rep, 0, sizeof(RepDev), stream));
+        CK(cudaStreamSynchronize(stream));
+        for (int i = 0; i < n; ++i) owner_h[b + i] = -1;
+        update_blocks(b, b + n);
+        a_beads.release(b, n);
+        a_nat.release(r.nat_off, r.nat_len);
+        a_cells.release(r.cell_off, r.cell_len);
+        a_chunks.release(r.chunk_off, r.chunk_len);
+    }
+    r = RepHost{};
+    r.in_use = false;
+}
+
+void Engine::set_steps(int rep, long long nsteps) {
+    check_rep(reps, rep);
+    if (params.on[XMD_TERM_QA]) throw std::invalid_argument("per-replica step budgets exclude the quasi-adiabatic term");
+    reps[rep].steps_left = nsteps < 0 ? -1 : nsteps;
+    if (reps[rep].placed) {
+        use_device();
+        long long v = reps[rep].steps_left;
+        CK(cudaMemcpyAsync((char *)(d.rep + rep) + offsetof(RepDev, steps_left), &v, sizeof v,
+                           cudaMemcpyHostToDevice, stream));
+        CK(cudaStreamSynchronize(stream));
+    }
+}
+
+void Engine::place_now(int rep) {
+    check_rep(reps, rep);
+    ready_alloc();
+    if (!reps[rep].placed) {
+        if (!reps[rep].have_state) throw std::logic_error("set_state must precede placement");
+        use_device();
+        place(rep);
+    }
+}
+
+void Engine::steps_left(long long *out) {
+    use_device();
+    std::vector<RepDev> rd(std::max(1, d.R));
+    if (finalized) {
+        CK(cudaMemcpyAsync(rd.data(), d.rep, sizeof(RepDev) * d.R, cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+    }
+    for (int k = 0; k < (int)reps.size(); ++k)
+        out[k] = !reps[k].in_use ? -2 : (reps[k].placed ? rd[k].steps_left : reps[k].steps_left);
 }
 static bool consecutive(const RepHost &r, int a, int b) {
     return a >= 0 && b < r.n && b == a + 1 && r.chain[a] == r.chain[b] && r.seq[b] == r.seq[a] + 1;
@@ -942,7 +1050,7 @@ static bool consecutive(const RepHost &r, int a, int b) {
 
 void Engine::set_tethers(int rep, int n, const int32_t *i1, const int32_t *i2, const double *dd) {
     check_rep(reps, rep);
-    if (finalized) throw std::invalid_argument("topology is fixed after the first eval/step");
+    if (reps[rep].placed) throw std::invalid_argument("topology is fixed once the replica is on the device");
     RepHost &r = reps[rep];
     std::fill(r.teth_r0.begin(), r.teth_r0.end(), std::nan(""));
     for (int k = 0; k < n; ++k) {
@@ -956,7 +1064,7 @@ void Engine::set_tethers(int rep, int n, const int32_t *i1, const int32_t *i2, c
 void Engine::set_angles(int rep, int n, const int32_t *i1, const int32_t *i2, const int32_t *i3,
                         const double *th) {
     check_rep(reps, rep);
-    if (finalized) throw std::invalid_argument("topology is fixed after the first eval/step");
+    if (reps[rep].placed) throw std::invalid_argument("topology is fixed once the replica is on the device");
     RepHost &r = reps[rep];
     std::fill(r.ang_t0.begin(), r.ang_t0.end(), std::nan(""));
     for (int k = 0; k < n; ++k) {
@@ -970,7 +1078,7 @@ void Engine::set_angles(int rep, int n, const int32_t *i1, const int32_t *i2, co
 void Engine::set_dihedrals(int rep, int n, const int32_t *i1, const int32_t *i2, const int32_t *i3,
                            const int32_t *i4, const double *ph) {
     check_rep(reps, rep);
-    if (finalized) throw std::invalid_argument("topology is fixed after the first eval/step");
+    if (reps[rep].placed) throw std::invalid_argument("topology is fixed once the replica is on the device");
     RepHost &r = reps[rep];
     std::fill(r.dih_p0.begin(), r.dih_p0.end(), std::nan(""));
     for (int k = 0; k < n; ++k) {
@@ -983,7 +1091,7 @@ void Engine::set_dihedrals(int rep, int n, const int32_t *i1, const int32_t *i2,
 }
 void Engine::set_native(int rep, int n, const int32_t *i1, const int32_t *i2, const double *dd) {
     check_rep(reps, rep);
-    if (finalized) throw std::invalid_argument("topology is fixed after the first eval/step");
+    if (reps[rep].placed) throw std::invalid_argument("topology is fixed once the replica is on the device");
     RepHost &r = reps[rep];
     std::vector<std::tuple<int, int, double>> v;
     for (int k = 0; k < n; ++k) {
@@ -1033,28 +1141,45 @@ void Engine::derive_rep(int ri, RepDev &rd) {
     rd.first = 1;
 }
 
+// Capacities: exact totals of the replicas added so far (static contexts), or
+// the reservation (dynamic contexts, where replicas come and go between steps).
 void Engine::finalize() {
     if (finalized) return;
-    if (reps.empty()) throw std::logic_error("no replica added");
-    for (auto &r : reps)
-        if (!r.have_state) throw std::logic_error("set_state must be called for every replica");
-    const xmd_params &p = params;
-    int N = 0;
-    int R = (int)reps.size();
-    long cells = 0;
-    std::vector<int> cell_off(R), cell_bud(R);
-    for (int k = 0; k < R; ++k) {
-        reps[k].begin = N;
-        N += reps[k].n;
-        cell_off[k] = (int)cells;
-        cell_bud[k] = std::max(64, 2 * reps[k].n);
-        cells += cell_bud[k];
+    if (!dynamic) {
+        if (reps.empty()) throw std::logic_error("no replica added");
+        for (auto &r : reps)
+            if (!r.have_state) throw std::logic_error("set_state must be called for every replica");
+        cap = Caps{};
+        cap.reps = (int)reps.size();
+        for (auto &r : reps) {
+            cap.beads += r.n;
+            cap.nat += 2 * (int)r.nat_i1.size();
+            const bool tile = params.nl_build == XMD_NL_BUILD_TILE ||
+                              (params.nl_build == XMD_NL_BUILD_AUTO && r.n <= TILE_MAX);
+            if (tile) cap.chunks += (r.n + TL_CH - 1) / TL_CH;
+            else cap.cells += std::max(64, 2 * r.n);
+            if (params.on[XMD_TERM_QA]) {
+                cap.fp += r.n * QA_FP_PER_BEAD + 256;
+                cap.ct += r.n * QA_CT_PER_BEAD + 256;
+            }
+        }
     }
+    allocate();
+    finalized = true;
+    place_pending();
+}
+
+// every device array at capacity; slots start empty (rep_of = -1)
+void Engine::allocate() {
+    const xmd_params &p = params;
+    const int N = cap.beads, R = cap.reps;
     nl_cap = p.nl_capacity > 0 ? p.nl_capacity : 64;
     auto_grow = p.nl_grow != 0;
     d.N = N;
     d.R = R;
     d.nl_cap = nl_cap;
+    const size_t cells = (size_t)std::max(1, cap.cells);
+    const size_t NN = (size_t)std::max(1, cap.nat);
     d.pos[0] = (double4_32a *)dalloc(sizeof(double4_32a) * N);
     d.pos[1] = (double4_32a *)dalloc(sizeof(double4_32a) * N);
     d.yh = (double *)dalloc(sizeof(double) * 15 * (size_t)N);
@@ -1062,6 +1187,7 @@ void Engine::finalize() {
     d.F = (double *)dalloc(sizeof(double) * 3 * (size_t)N);
     d.Vrep = (double *)dalloc(sizeof(double) * XMD_NUM_TERMS * R);
     d.rep_of = (int32_t *)dalloc(sizeof(int32_t) * N);
+    CK(cudaMemsetAsync(d.rep_of, 0xff, sizeof(int32_t) * N, stream));
     d.bflags = (uint32_t *)dalloc(sizeof(uint32_t) * N);
     d.chain = (int32_t *)dalloc(sizeof(int32_t) * N);
     d.seq = (int32_t *)dalloc(sizeof(int32_t) * N);
@@ -1069,7 +1195,11 @@ void Engine::finalize() {
     d.teth_r0 = (double *)dalloc(sizeof(double) * N);
     d.ang_t0 = (double *)dalloc(sizeof(double) * N);
     d.dih_p0 = (double *)dalloc(sizeof(double) * N);
-    d.nat_start = (int32_t *)dalloc(sizeof(int32_t) * (N + 1));
+    d.nat_start = (int32_t *)dalloc(sizeof(int32_t) * N);
+    d.nat_end = (int32_t *)dalloc(sizeof(int32_t) * N);
+    d.nat_j = (int32_t *)dalloc(sizeof(int32_t) * NN);
+    d.nat_d = (double *)dalloc(sizeof(double) * NN);
+    d.nat_on = (uint8_t *)dalloc(NN);
     d.nl_row = (int32_t *)dalloc(sizeof(int32_t) * (size_t)nl_cap * N);
     d.nl_cnt = (int32_t *)dalloc(sizeof(int32_t) * N);
     d.cell_cnt = (int32_t *)dalloc(sizeof(int32_t) * cells);
@@ -1084,112 +1214,26 @@ void Engine::finalize() {
     d.any_rebuild = (int *)dalloc(sizeof(int) * 4);
     d.status = (int *)dalloc(sizeof(int) * 4);
     d.ctr = (unsigned long long *)dalloc(sizeof(unsigned long long) * 4);
-
-    // host staging of the static per-bead data
-    std::vector<int32_t> rep_of(N), chain(N), seq(N), nat_start(N + 1, 0);
-    std::vector<uint32_t> bfl(N, 0);
-    std::vector<uint8_t> at(N);
-    std::vector<double> tr(N, 0.0), ar(N, 0.0), dr(N, 0.0);
-    std::vector<std::vector<std::pair<int, double>>> nat(N);
-    std::vector<RepDev> rd(R);
-    int fp_total = 0, ct_total = 0;
-    std::vector<uint64_t> jumps(JUMP_WORDS * (size_t)R);
-    std::vector<int2> chunks;
-    int chain_base = 0;
-    for (int k = 0; k < R; ++k) {
-        RepHost &r = reps[k];
-        int maxc = 0;
-        for (int i = 0; i < r.n; ++i) {
-            int g = r.begin + i;
-            rep_of[g] = k;
-            chain[g] = chain_base + r.chain[i];
-            maxc = std::max(maxc, r.chain[i] + 1);
-            seq[g] = r.seq[i];
-            at[g] = r.atype[i];
-            uint32_t f = 0;
-            if (!std::isnan(r.teth_r0[i])) { f |= BF_TETH; tr[g] = r.teth_r0[i]; }
-            if (!std::isnan(r.ang_t0[i])) { f |= BF_ANG; ar[g] = r.ang_t0[i]; }
-            if (!std::isnan(r.dih_p0[i])) { f |= BF_DIH; dr[g] = r.dih_p0[i]; }
-            if (i > 0 && consecutive(r, i - 1, i)) f |= BF_PREV;
-            if (i + 1 < r.n && consecutive(r, i, i + 1)) f |= BF_NEXT;
-            bfl[g] = f;
-        }
-        chain_base += maxc;
-        for (size_t q = 0; q < r.nat_i1.size(); ++q) {
-            int a = r.begin + r.nat_i1[q], b = r.begin + r.nat_i2[q];
-            nat[a].push_back({b, r.nat_d[q]});
-            nat[b].push_back({a, r.nat_d[q]});
-        }
-        derive_rep(k, rd[k]);
-        rd[k].cell_off = cell_off[k];
-        rd[k].cell_budget = cell_bud[k];
-        // Verlet build: whole-replica tiles up to TILE_MAX beads, else cells
-        rd[k].tile = p.nl_build == XMD_NL_BUILD_TILE ||
-                     (p.nl_build == XMD_NL_BUILD_AUTO && r.n <= TILE_MAX);
-        if (rd[k].tile && r.n > TILE_MAX)
-            throw std::invalid_argument("engine: nl build 'tile' takes replicas of at most " +
-                                        std::to_string(TILE_MAX) + " beads");
-        if (rd[k].tile) {
-            any_tile = true;
-            tile_smem = std::max(tile_smem, (sizeof(float4) + sizeof(int2)) * (size_t)r.n);
-            for (int c = 0; c < r.n; c += TL_CH) chunks.push_back(make_int2(k, r.begin + c));
-        } else {
-            any_cell = true;
-        }
-        if (p.on[XMD_TERM_QA]) {
-            rd[k].fp_off = fp_total;
-            rd[k].fp_cap = r.n * QA_FP_PER_BEAD + 256;
-            fp_total += rd[k].fp_cap;
-            rd[k].ct_off = ct_total;
-            rd[k].ct_cap = r.n * QA_CT_PER_BEAD + 256;
-            ct_total += rd[k].ct_cap;
-        }
-        GF2 j = gf2_jump(4ull * (uint64_t)r.n);
-        // nibble tables: entry [q][v] = XOR of the columns 4q+b for the bits b of v
-        for (int q = 0; q < 16; ++q)
-            for (int v = 0; v < 16; ++v) {
-                uint64_t e = 0;
-                for (int bb = 0; bb < 4; ++bb)
-                    if ((v >> bb) & 1) e ^= j[4 * q + bb];
-                jumps[JUMP_WORDS * (size_t)k + 16 * q + v] = e;
-            }
-    }
-    std::vector<int32_t> nat_j;
-    std::vector<double> nat_d;
-    for (int i = 0; i < N; ++i) {
-        std::sort(nat[i].begin(), nat[i].end());
-        nat_start[i] = (int)nat_j.size();
-        for (auto &e : nat[i]) { nat_j.push_back(e.first); nat_d.push_back(e.second); }
-    }
-    nat_start[N] = (int)nat_j.size();
-    d.nchunks = (int)chunks.size();
-    d.chunks = (int2 *)dalloc(sizeof(int2) * std::max<size_t>(1, chunks.size()));
-    if (!chunks.empty())
-        CK(cudaMemcpyAsync(d.chunks, chunks.data(), sizeof(int2) * chunks.size(), cudaMemcpyHostToDevice, stream));
+    d.nchunks = std::max(1, cap.chunks);
+    d.chunks = (int2 *)dalloc(sizeof(int2) * d.nchunks);
+    CK(cudaMemsetAsync(d.chunks, 0xff, sizeof(int2) * d.nchunks, stream));
+    d.blk_on = (uint8_t *)dalloc((N + FB - 1) / FB);
+    owner_h.assign(N, -1);
+    a_beads.init(N);
+    a_nat.init(cap.nat);
+    a_cells.init(cap.cells);
+    a_chunks.init(cap.chunks);
+    a_fp.init(cap.fp);
+    a_ct.init(cap.ct);
+    any_cell = cap.cells > 0;
+    any_tile = cap.chunks > 0;
     d.any_cell = any_cell;
+    tile_smem = 0;
+    for (auto &r : reps)
+        if (r.in_use && r.n <= TILE_MAX) tile_smem = std::max(tile_smem, (sizeof(float4) + sizeof(int2)) * (size_t)r.n);
+    if (dynamic) tile_smem = (sizeof(float4) + sizeof(int2)) * (size_t)std::min(TILE_MAX, cap.beads);
     if (tile_smem > 48 * 1024)
         CK(cudaFuncSetAttribute(k_nl_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem));
-    size_t NN = nat_j.size();
-    d.nat_j = (int32_t *)dalloc(sizeof(int32_t) * (NN ? NN : 1));
-    d.nat_d = (double *)dalloc(sizeof(double) * (NN ? NN : 1));
-    d.nat_on = (uint8_t *)dalloc(NN ? NN : 1);
-
-    CK(cudaMemcpyAsync(d.rep_of, rep_of.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, stream));
-    CK(cudaMemcpyAsync(d.chain, chain.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, stream));
-    CK(cudaMemcpyAsync(d.seq, seq.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, stream));
-    CK(cudaMemcpyAsync(d.atype, at.data(), N, cudaMemcpyHostToDevice, stream));
-    CK(cudaMemcpyAsync(d.bflags, bfl.data(), sizeof(uint32_t) * N, cudaMemcpyHostToDevice, stream));
-    CK(cudaMemcpyAsync(d.teth_r0, tr.data(), sizeof(double) * N, cudaMemcpyHostToDevice, stream));
-    CK(cudaMemcpyAsync(d.ang_t0, ar.data(), sizeof(double) * N, cudaMemcpyHostToDevice, stream));
-    CK(cudaMemcpyAsync(d.dih_p0, dr.data(), sizeof(double) * N, cudaMemcpyHostToDevice, stream));
-    CK(cudaMemcpyAsync(d.nat_start, nat_start.data(), sizeof(int32_t) * (N + 1), cudaMemcpyHostToDevice, stream));
-    if (NN) {
-        CK(cudaMemcpyAsync(d.nat_j, nat_j.data(), sizeof(int32_t) * NN, cudaMemcpyHostToDevice, stream));
-        CK(cudaMemcpyAsync(d.nat_d, nat_d.data(), sizeof(double) * NN, cudaMemcpyHostToDevice, stream));
-    }
-    CK(cudaMemcpyAsync(d.rep, rd.data(), sizeof(RepDev) * R, cudaMemcpyHostToDevice, stream));
-    CK(cudaMemcpyAsync(d.jump, jumps.data(), sizeof(uint64_t) * JUMP_WORDS * R, cudaMemcpyHostToDevice, stream));
-    CK(cudaStreamSynchronize(stream));
 
     // term parameters
     std::memset(&tp, 0, sizeof tp);
@@ -1220,9 +1264,7 @@ void Engine::finalize() {
     tp.lj_bs_r_min = p.lj_bs_r_min; tp.lj_bs_depth = p.lj_bs_depth;
     tp.ss_sinking = p.ss_sinking;
     if (p.on[XMD_TERM_QA]) {
-        // quasi-adiabatic state: valences start at the residue limits
-        // (intended main.cpp:662-672), tables of main.cpp:681-700 and
-        // lj_variants.cpp:59-62
+        // quasi-adiabatic state (tables of main.cpp:681-700, lj_variants.cpp:59-62)
         d.qa_on = 1;
         QaDev &q = d.qa;
         q.nh = (double *)dalloc(sizeof(double) * 6 * (size_t)N);
@@ -1231,6 +1273,7 @@ void Engine::finalize() {
         q.ref = (int32_t *)dalloc(sizeof(int32_t) * QA_REF_CAP * (size_t)N);
         q.tmp_cnt = (int32_t *)dalloc(sizeof(int32_t) * N);
         q.tmp = (int32_t *)dalloc(sizeof(int32_t) * QA_TMP_CAP * (size_t)N);
+        const int fp_total = std::max(1, cap.fp), ct_total = std::max(1, cap.ct);
         q.fp_total = fp_total;
         q.ct_total = ct_total;
         q.fp_i1 = (int32_t *)dalloc(sizeof(int32_t) * fp_total);
@@ -1277,21 +1320,159 @@ void Engine::finalize() {
         q.min_cos_hr = p.qa_min_cos_hr;
         q.min_cos_hh = p.qa_min_cos_hh;
         q.max_cos_nr = p.qa_max_cos_nr;
-        std::vector<int32_t> fprep(fp_total);
-        for (int k = 0; k < R; ++k)
-            for (int s = 0; s < rd[k].fp_cap; ++s) fprep[rd[k].fp_off + s] = k;
-        CK(cudaMemcpyAsync(q.fp_rep, fprep.data(), sizeof(int32_t) * fp_total, cudaMemcpyHostToDevice, stream));
-        std::vector<int32_t> sy(N);
-        for (int i = 0; i < N; ++i) {
-            const int32_t *lim = p.limits[at[i]];
+    }
+    CK(cudaStreamSynchronize(stream));
+}
+
+void Engine::ready() {
+    finalize();
+    place_pending();
+}
+void Engine::ready_alloc() {
+    if (!finalized) finalize();
+}
+
+void Engine::place_pending() {
+    for (int k = 0; k < (int)reps.size(); ++k)
+        if (reps[k].in_use && !reps[k].placed) {
+            if (!reps[k].have_state) throw std::logic_error("set_state must be called for every replica");
+            place(k);
+        }
+}
+
+// force blocks [b0/FB, (b1-1)/FB] on when any bead slot in them is placed
+void Engine::update_blocks(int b0, int b1) {
+    if (b1 <= b0) return;
+    const int k0 = b0 / FB, k1 = (b1 - 1) / FB;
+    std::vector<uint8_t> on(k1 - k0 + 1, 0);
+    for (int k = k0; k <= k1; ++k)
+        for (int i = k * FB; i < std::min(cap.beads, (k + 1) * FB); ++i)
+            if (owner_h[i] >= 0) { on[k - k0] = 1; break; }
+    CK(cudaMemcpyAsync(d.blk_on + k0, on.data(), on.size(), cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+}
+
+// static data, lists and state of replica slot k onto the device
+void Engine::place(int k) {
+    const xmd_params &p = params;
+    RepHost &r = reps[k];
+    const int n = r.n;
+    const bool tile = p.nl_build == XMD_NL_BUILD_TILE || (p.nl_build == XMD_NL_BUILD_AUTO && n <= TILE_MAX);
+    if (tile && n > TILE_MAX)
+        throw std::invalid_argument("engine: nl build 'tile' takes replicas of at most " +
+                                    std::to_string(TILE_MAX) + " beads");
+    const int nnat = 2 * (int)r.nat_i1.size();
+    const int nchunk = tile ? (n + TL_CH - 1) / TL_CH : 0;
+    const int ncell = tile ? 0 : std::max(64, 2 * n);
+    const bool qa = p.on[XMD_TERM_QA] != 0;
+    const int nfp = qa ? n * QA_FP_PER_BEAD + 256 : 0, nct = qa ? n * QA_CT_PER_BEAD + 256 : 0;
+    // device ranges (all or nothing)
+    int b = a_beads.alloc(n), no = a_nat.alloc(nnat), co = a_cells.alloc(ncell), ho = a_chunks.alloc(nchunk);
+    int fo = a_fp.alloc(nfp), to = a_ct.alloc(nct);
+    if (b < 0 || no < 0 || co < 0 || ho < 0 || fo < 0 || to < 0) {
+        if (b >= 0) a_beads.release(b, n);
+        if (no >= 0) a_nat.release(no, nnat);
+        if (co >= 0) a_cells.release(co, ncell);
+        if (ho >= 0) a_chunks.release(ho, nchunk);
+        if (fo >= 0) a_fp.release(fo, nfp);
+        if (to >= 0) a_ct.release(to, nct);
+        throw std::length_error("engine: the reserved capacity has no room for this replica");
+    }
+    r.begin = b;
+    r.nat_off = no; r.nat_len = nnat;
+    r.cell_off = co; r.cell_len = ncell;
+    r.chunk_off = ho; r.chunk_len = nchunk;
+    r.fp_off = fo; r.fp_len = nfp;
+    r.ct_off = to; r.ct_len = nct;
+
+    // per-bead static data; chain ids are local (pairs never cross replicas)
+    std::vector<int32_t> rep_of(n, k), seq(r.seq), chain(r.chain), ns(n), ne(n);
+    std::vector<uint32_t> bfl(n, 0);
+    std::vector<double> tr(n, 0.0), ar(n, 0.0), dr(n, 0.0);
+    for (int i = 0; i < n; ++i) {
+        uint32_t f = 0;
+        if (!std::isnan(r.teth_r0[i])) { f |= BF_TETH; tr[i] = r.teth_r0[i]; }
+        if (!std::isnan(r.ang_t0[i])) { f |= BF_ANG; ar[i] = r.ang_t0[i]; }
+        if (!std::isnan(r.dih_p0[i])) { f |= BF_DIH; dr[i] = r.dih_p0[i]; }
+        if (i > 0 && consecutive(r, i - 1, i)) f |= BF_PREV;
+        if (i + 1 < r.n && consecutive(r, i, i + 1)) f |= BF_NEXT;
+        bfl[i] = f;
+    }
+    // natives of each bead (both directions), ordered by partner: a CSR
+    // segment of the replica
+    std::vector<std::vector<std::pair<int, double>>> nat(n);
+    for (size_t q = 0; q < r.nat_i1.size(); ++q) {
+        nat[r.nat_i1[q]].push_back({b + r.nat_i2[q], r.nat_d[q]});
+        nat[r.nat_i2[q]].push_back({b + r.nat_i1[q], r.nat_d[q]});
+    }
+    std::vector<int32_t> nj;
+    std::vector<double> nd;
+    for (int i = 0; i < n; ++i) {
+        std::sort(nat[i].begin(), nat[i].end());
+        ns[i] = no + (int)nj.size();
+        for (auto &e : nat[i]) { nj.push_back(e.first); nd.push_back(e.second); }
+        ne[i] = no + (int)nj.size();
+    }
+    auto up = [&](void *dst, const void *src, size_t bytes_) {
+        if (bytes_) CK(cudaMemcpyAsync(dst, src, bytes_, cudaMemcpyHostToDevice, stream));
+    };
+    up(d.rep_of + b, rep_of.data(), sizeof(int32_t) * n);
+    up(d.chain + b, chain.data(), sizeof(int32_t) * n);
+    up(d.seq + b, seq.data(), sizeof(int32_t) * n);
+    up(d.atype + b, r.atype.data(), n);
+    up(d.bflags + b, bfl.data(), sizeof(uint32_t) * n);
+    up(d.teth_r0 + b, tr.data(), sizeof(double) * n);
+    up(d.ang_t0 + b, ar.data(), sizeof(double) * n);
+    up(d.dih_p0 + b, dr.data(), sizeof(double) * n);
+    up(d.nat_start + b, ns.data(), sizeof(int32_t) * n);
+    up(d.nat_end + b, ne.data(), sizeof(int32_t) * n);
+    up(d.nat_j + no, nj.data(), sizeof(int32_t) * nj.size());
+    up(d.nat_d + no, nd.data(), sizeof(double) * nd.size());
+    CK(cudaMemsetAsync(d.nat_on + no, 0, nnat, stream));
+    CK(cudaMemsetAsync(d.nl_cnt + b, 0, sizeof(int32_t) * n, stream));
+    std::vector<int2> ch(nchunk);
+    for (int c = 0; c < nchunk; ++c) ch[c] = make_int2(k, b + c * TL_CH);
+    up(d.chunks + ho, ch.data(), sizeof(int2) * nchunk);
+
+    RepDev rd;
+    derive_rep(k, rd);
+    rd.cell_off = co;
+    rd.cell_budget = ncell;
+    rd.tile = tile;
+    rd.active = 1;
+    rd.steps_left = r.steps_left;
+    if (qa) {
+        rd.fp_off = fo;
+        rd.fp_cap = nfp;
+        rd.ct_off = to;
+        rd.ct_cap = nct;
+        std::vector<int32_t> fprep(nfp, k), sy(n);
+        up(d.qa.fp_rep + fo, fprep.data(), sizeof(int32_t) * nfp);
+        // valences start at the residue limits (intended main.cpp:662-672)
+        for (int i = 0; i < n; ++i) {
+            const int32_t *lim = p.limits[r.atype[i]];
             sy[i] = (lim[0] & 0xff) | ((lim[1] & 0xff) << 8) | ((lim[2] & 0xff) << 16) | ((lim[3] & 0xff) << 24);
         }
-        CK(cudaMemcpyAsync(q.sync, sy.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, stream));
-        CK(cudaStreamSynchronize(stream));
+        up(d.qa.sync + b, sy.data(), sizeof(int32_t) * n);
+        CK(cudaMemsetAsync(d.qa.ref_cnt + b, 0, sizeof(int32_t) * n, stream));
     }
-
-    finalized = true;
-    for (int k = 0; k < R; ++k) upload_state(k);
+    up(d.rep + k, &rd, sizeof(RepDev));
+    GF2 j = gf2_jump(4ull * (uint64_t)n);
+    std::vector<uint64_t> jt(JUMP_WORDS);
+    // nibble tables: entry [q][v] = XOR of the columns 4q+b for the bits b of v
+    for (int q = 0; q < 16; ++q)
+        for (int v = 0; v < 16; ++v) {
+            uint64_t e = 0;
+            for (int bb = 0; bb < 4; ++bb)
+                if ((v >> bb) & 1) e ^= j[4 * q + bb];
+            jt[16 * q + v] = e;
+        }
+    up(d.jump + (size_t)JUMP_WORDS * k, jt.data(), sizeof(uint64_t) * JUMP_WORDS);
+    CK(cudaStreamSynchronize(stream));
+    for (int i = 0; i < n; ++i) owner_h[b + i] = k;
+    update_blocks(b, b + n);
+    r.placed = true;
+    upload_state(k);
 }
 
 void Engine::upload_state(int k) {
@@ -1336,12 +1517,12 @@ void Engine::set_state(int rep, const double *r, const double *v) {
     else h.v.assign(3 * (size_t)h.n, 0.0);
     for (double x : h.r) if (!std::isfinite(x)) throw std::invalid_argument("non-finite position");
     h.have_state = true;
-    if (finalized) upload_state(rep);
+    if (h.placed) upload_state(rep);
 }
 
 void Engine::set_history(int rep, const double *y, double t, uint64_t rngs) {
     check_rep(reps, rep);
-    if (!finalized) finalize();
+    ready();
     RepHost &h = reps[rep];
     int n = h.n, b = h.begin;
     size_t n3 = 3 * (size_t)n;
@@ -1375,7 +1556,7 @@ void Engine::set_history(int rep, const double *y, double t, uint64_t rngs) {
 
 void Engine::get_state(int rep, double *r, double *v, double *t) {
     check_rep(reps, rep);
-    if (!finalized) finalize();
+    ready();
     const RepHost &h = reps[rep];
     int n = h.n, b = h.begin;
     std::vector<double4_32a> pos(n);
@@ -1397,7 +1578,7 @@ void Engine::get_state(int rep, double *r, double *v, double *t) {
 
 void Engine::get_history(int rep, double *y, double *t, uint64_t *rngs) {
     check_rep(reps, rep);
-    if (!finalized) finalize();
+    ready();
     const RepHost &h = reps[rep];
     int n = h.n, b = h.begin;
     size_t n3 = 3 * (size_t)n;
@@ -1636,7 +1817,7 @@ void Engine::check_status(const char *where) {
 
 void Engine::eval_forces(int rep, double *F, double *V) {
     check_rep(reps, rep);
-    finalize();
+    ready();
     ensure_nl();
     CK(cudaMemsetAsync(d.Vrep, 0, sizeof(double) * XMD_NUM_TERMS * d.R, stream));
     int nb = (d.N + FB - 1) / FB;
@@ -1652,7 +1833,7 @@ void Engine::eval_forces(int rep, double *F, double *V) {
 
 void Engine::step(int nsteps) {
     use_device();
-    finalize();
+    ready();
     if (!params.langevin_on) throw std::invalid_argument("langevin: enabled is false; nothing integrates");
     ensure_nl();
     int s = 0;
@@ -1675,7 +1856,9 @@ void Engine::step(int nsteps) {
         if (*h_any) launch_rebuild();
     }
     check_status("step");
-    if (auto_grow && grow_rows(0.6)) k_mark_all<<<(d.R + 255) / 256, 256, 0, stream>>>(d);
+    // rows keep their contents when they grow: no list needs rebuilding, so
+    // no replica's trajectory depends on another's row lengths
+    if (auto_grow) grow_rows(0.6);
 }
 
 // ---- packed host-buffer path ----------------------------------------------------
@@ -1693,6 +1876,7 @@ __global__ void k_unpack_history(Dev d, const double *__restrict__ y, int cur) {
             d.yh[(size_t)((ord - 1) * 3 + a) * d.N + i] = y[ord * n3 + 3 * (size_t)i + a];
     // the skin test sees the new positions like any other displacement
     int r = d.rep_of[i];
+    if (r < 0) return;
     double disp = dist2_exact(d.rep[r].box, p, d.orig[i]);   // squared, as k_force records it
     atomicMax(&d.rep[r].maxdisp, (unsigned long long)__double_as_longlong(disp));
 }
@@ -1707,7 +1891,7 @@ __global__ void k_pack_positions(Dev d, double *__restrict__ r, int cur) {
 
 void Engine::upload_history_all(const double *y) {
     use_device();
-    finalize();
+    ready();
     if (!staging) staging = (double *)dalloc(sizeof(double) * 18 * (size_t)d.N);
     CK(cudaMemcpyAsync(staging, y, sizeof(double) * 18 * (size_t)d.N, cudaMemcpyHostToDevice, stream));
     k_unpack_history<<<(d.N + 255) / 256, 256, 0, stream>>>(d, staging, cur);
@@ -1716,7 +1900,7 @@ void Engine::upload_history_all(const double *y) {
 
 void Engine::download_positions_all(double *r) {
     use_device();
-    finalize();
+    ready();
     if (!staging) staging = (double *)dalloc(sizeof(double) * 18 * (size_t)d.N);
     k_pack_positions<<<(d.N + 255) / 256, 256, 0, stream>>>(d, staging, cur);
     ++launches;
@@ -1728,17 +1912,17 @@ void Engine::stats(int64_t *out) {
     use_device();
     for (int k = 0; k < XMD_NUM_STATS; ++k) out[k] = 0;
     int64_t nb = 0;
-    for (auto &r : reps) nb += r.n;
+    int64_t nr = 0;
+    for (auto &r : reps)
+        if (r.in_use) { nb += r.n; ++nr; }
     out[XMD_STAT_BEADS] = nb;
-    out[XMD_STAT_REPLICAS] = (int64_t)reps.size();
+    out[XMD_STAT_REPLICAS] = nr;
     out[XMD_STAT_LAUNCHES] = launches;
     out[XMD_STAT_MD_STEPS] = md_steps;
     if (!finalized) return;
     std::vector<int32_t> cnt(d.N);
     CK(cudaMemcpyAsync(cnt.data(), d.nl_cnt, sizeof(int32_t) * d.N, cudaMemcpyDeviceToHost, stream));
-    int32_t nn = 0;
-    CK(cudaMemcpyAsync(&nn, d.nat_start + d.N, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
-    CK(cudaStreamSynchronize(stream));
+    const int32_t nn = cap.nat;   // entries of free native ranges are kept at 0
     std::vector<uint8_t> on(nn > 0 ? nn : 1);
     if (nn) CK(cudaMemcpyAsync(on.data(), d.nat_on, nn, cudaMemcpyDeviceToHost, stream));
     std::vector<RepDev> rd(d.R);
@@ -1747,15 +1931,17 @@ void Engine::stats(int64_t *out) {
     unsigned long long passes = 0;
     CK(cudaMemcpyAsync(&passes, d.ctr, sizeof(passes), cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
-    out[XMD_STAT_LAUNCHES] = launches + 2 * (int64_t)passes;   // k_cells + k_nl_build per pass
-    for (int32_t c : cnt) out[XMD_STAT_NL_ENTRIES] += c;
+    out[XMD_STAT_LAUNCHES] = launches + (int64_t)((any_cell ? 2 : 0) + (any_tile ? 1 : 0) + (d.qa_on ? 1 : 0)) * (int64_t)passes;
+    for (int i = 0; i < d.N; ++i)
+        if (owner_h[i] >= 0) out[XMD_STAT_NL_ENTRIES] += cnt[i];
     for (int k = 0; k < nn; ++k) out[XMD_STAT_GO_ACTIVE] += on[k];
-    for (auto &r : rd) out[XMD_STAT_REBUILDS] += (int64_t)r.rebuilds;
+    for (auto &r : rd)
+        if (r.active) out[XMD_STAT_REBUILDS] += (int64_t)r.rebuilds;
 }
 
 int Engine::qa_contacts(int rep, int cap, int32_t *out4, double *ref_time) {
     check_rep(reps, rep);
-    finalize();
+    ready();
     if (!d.qa_on) return 0;
     RepDev rd;
     CK(cudaMemcpyAsync(&rd, d.rep + rep, sizeof(RepDev), cudaMemcpyDeviceToHost, stream));
@@ -1791,7 +1977,7 @@ int Engine::qa_contacts(int rep, int cap, int32_t *out4, double *ref_time) {
 
 int Engine::verlet_pairs(int rep, int cap, int32_t *out2, uint8_t *flags) {
     check_rep(reps, rep);
-    finalize();
+    ready();
     ensure_nl();
     const RepHost &h = reps[rep];
     std::vector<int32_t> cnt(h.n), rows((size_t)nl_cap * h.n);
@@ -1818,7 +2004,7 @@ int Engine::verlet_pairs(int rep, int cap, int32_t *out2, uint8_t *flags) {
 
 void Engine::qa_sync(int rep, int8_t *out) {
     check_rep(reps, rep);
-    finalize();
+    ready();
     const RepHost &h = reps[rep];
     if (!d.qa_on) {
         for (int i = 0; i < h.n; ++i)

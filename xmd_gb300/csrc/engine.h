@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -35,6 +36,8 @@ struct RepDev {
     int tile;                // Verlet build by whole-replica tiles (no cell grid)
     float pre2;              // squared FP32 pre-filter radius of the Verlet build
     int first, rebuild;
+    int active;              // slot holds a placed replica
+    long long steps_left;    // steps this replica still takes (-1: no bound)
     unsigned long long maxdisp;
     unsigned long long rebuilds;
     // quasi-adiabatic lists: free pairs [fp_off, fp_off + fp_n) of capacity
@@ -80,7 +83,7 @@ struct Dev {
     int32_t *chain, *seq;
     uint8_t *atype;
     double *teth_r0, *ang_t0, *dih_p0;
-    int32_t *nat_start, *nat_j;
+    int32_t *nat_start, *nat_end, *nat_j;   // natives of bead i: [nat_start[i], nat_end[i])
     double *nat_d;
     uint8_t *nat_on;
     int32_t *nl_row, *nl_cnt;
@@ -95,11 +98,14 @@ struct Dev {
     int2 *chunks;           // (replica, first bead) of each tile-build block
     int nchunks;
     int any_cell;           // some replica uses the cell-grid build
+    uint8_t *blk_on;        // force blocks (FB beads) holding at least one placed bead
     int qa_on;
     QaDev qa;
 };
 
 struct RepHost {
+    bool in_use = true;      // slot taken (false after remove)
+    bool placed = false;     // static data and state are on the device
     int n = 0;
     std::vector<int32_t> chain, seq;
     std::vector<uint8_t> atype;
@@ -112,6 +118,55 @@ struct RepHost {
     std::vector<double> r, v;                      // initial state
     bool have_state = false;
     int begin = 0;
+    int nat_off = 0, nat_len = 0;       // native CSR entries
+    int cell_off = 0, cell_len = 0;     // cell buckets (cell-grid build)
+    int chunk_off = 0, chunk_len = 0;   // tile-build chunks
+    int fp_off = 0, fp_len = 0, ct_off = 0, ct_len = 0;   // quasi-adiabatic slots
+    long long steps_left = -1;
+};
+
+// first-fit allocator of index ranges [0, n)
+class RangeAlloc {
+public:
+    void init(int n) {
+        free_.clear();
+        if (n > 0) free_[0] = n;
+    }
+    int alloc(int n) {
+        if (n <= 0) return 0;
+        for (auto it = free_.begin(); it != free_.end(); ++it)
+            if (it->second >= n) {
+                int s = it->first, l = it->second;
+                free_.erase(it);
+                if (l > n) free_[s + n] = l - n;
+                return s;
+            }
+        return -1;
+    }
+    void release(int s, int n) {
+        if (n <= 0) return;
+        auto it = free_.emplace(s, n).first;
+        auto nx = std::next(it);
+        if (nx != free_.end() && s + n == nx->first) {
+            it->second += nx->second;
+            free_.erase(nx);
+        }
+        if (it != free_.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+    int largest() const {
+        int m = 0;
+        for (auto &kv : free_) m = std::max(m, kv.second);
+        return m;
+    }
+
+private:
+    std::map<int, int> free_;   // start -> length
 };
 
 class Engine {
@@ -126,6 +181,15 @@ public:
 
     int add_replica(int n, const int32_t *chain, const int32_t *seq, const uint8_t *atype,
                     const double cell[3], double temperature, uint64_t seed);
+    // dynamic membership: fixed capacities, replicas placed and removed
+    // between steps (slots and device ranges are reused)
+    void reserve(int beads, int replicas, int natives);
+    void remove_replica(int rep);
+    void set_steps(int rep, long long nsteps);
+    void steps_left(long long *out);   // per replica slot, -2 for a free slot
+    void place_now(int rep);           // place a replica now (XMD_ERR_CAPACITY: no room yet)
+    int capacity_replicas() const { return cap.reps; }
+    size_t device_bytes() const { return bytes; }
     void set_tethers(int rep, int n, const int32_t *i1, const int32_t *i2, const double *d);
     void set_angles(int rep, int n, const int32_t *i1, const int32_t *i2, const int32_t *i3,
                     const double *th);
@@ -185,6 +249,19 @@ private:
     bool grow_rows(double frac);
     void drop_graphs();
 
+    struct Caps {
+        int beads = 0, reps = 0, nat = 0, cells = 0, chunks = 0, fp = 0, ct = 0;
+    } cap;
+    bool dynamic = false;
+    size_t bytes = 0;                          // device memory held
+    RangeAlloc a_beads, a_nat, a_cells, a_chunks, a_fp, a_ct;
+    std::vector<int32_t> owner_h;              // bead slot -> replica (or -1)
+    void allocate();
+    void place(int k);
+    void place_pending();
+    void ready();                              // allocated, every replica placed
+    void ready_alloc();
+    void update_blocks(int b0, int b1);
     void *dalloc(size_t bytes);
     void finalize();
     void release();

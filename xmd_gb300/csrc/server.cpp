@@ -1,0 +1,245 @@
+// server.cpp - continuous-batching request loop (see server.h).
+#include "server.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <stdexcept>
+
+namespace xmdg {
+
+double now_s() {
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+// device bytes a bead slot costs at the default row capacity (positions x2,
+// history, list origin, forces, topology, rows, cells, generator) plus its
+// share of native-contact entries; the reservation is sized from it
+constexpr int64_t BYTES_PER_BEAD = 1024;
+constexpr int NATIVES_PER_BEAD = 8;
+
+Server::Server(const xmd_params &p, int64_t hbm_budget, int max_beads, int chunk_steps) : params(p) {
+    if (!params.langevin_on) throw std::invalid_argument("server: langevin must be enabled");
+    if (params.on[XMD_TERM_QA]) throw std::invalid_argument("server: the quasi-adiabatic term needs a static context");
+    if (hbm_budget <= 0 || max_beads <= 0) throw std::invalid_argument("server: bad budget");
+    chunk = chunk_steps > 0 ? chunk_steps : 256;
+    cap_beads = (int)std::min<int64_t>(max_beads, hbm_budget / BYTES_PER_BEAD);
+    if (cap_beads < 1) throw std::invalid_argument("server: the HBM budget holds no bead");
+    cap_reps = std::min(1024, std::max(16, cap_beads / 30));
+    cap_nat = NATIVES_PER_BEAD * cap_beads;
+    eng = std::make_unique<Engine>(params);
+    eng->reserve(cap_beads, cap_reps, cap_nat);
+    worker = std::thread([this] { loop(); });
+}
+
+Server::~Server() {
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        stop = true;
+    }
+    cv.notify_all();
+    if (worker.joinable()) worker.join();
+    eng.reset();
+}
+
+int64_t Server::submit(std::unique_ptr<Request> req) {
+    if (req->n <= 0 || req->nsteps < 0) throw std::invalid_argument("server: empty request");
+    if (req->n > cap_beads)
+        throw std::length_error("server: the request has more beads than the reserved capacity");
+    std::lock_guard<std::mutex> lk(mu);
+    if (!fatal.empty()) throw std::runtime_error("server stopped: " + fatal);
+    req->id = next_id++;
+    req->t_submit = now_s();
+    if (t_first < 0) t_first = req->t_submit;
+    Request *q = req.get();
+    const int64_t id = req->id;
+    all[id] = std::move(req);
+    queue.push_back(q);
+    cv.notify_all();
+    return id;
+}
+
+int Server::poll(int64_t id) {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = all.find(id);
+    if (it == all.end()) throw std::invalid_argument("server: unknown request id");
+    return it->second->state;
+}
+
+void Server::result(int64_t id, double *r, double *v, double *t, double *latency) {
+    std::unique_lock<std::mutex> lk(mu);
+    auto it = all.find(id);
+    if (it == all.end()) throw std::invalid_argument("server: unknown request id");
+    Request *q = it->second.get();
+    cv_done.wait(lk, [&] { return q->state == XMD_REQ_DONE || q->state == XMD_REQ_FAILED; });
+    if (q->state == XMD_REQ_FAILED) {
+        std::string e = q->error;
+        all.erase(it);
+        throw std::runtime_error("request failed: " + e);
+    }
+    if (r) std::copy(q->r_out.begin(), q->r_out.end(), r);
+    if (v) std::copy(q->v_out.begin(), q->v_out.end(), v);
+    if (t) *t = q->t_out;
+    if (latency) *latency = q->t_done - q->t_submit;
+    all.erase(it);
+}
+
+void Server::wait_all() {
+    std::unique_lock<std::mutex> lk(mu);
+    cv_done.wait(lk, [&] { return (queue.empty() && running.empty()) || !fatal.empty(); });
+    if (!fatal.empty()) throw std::runtime_error("server stopped: " + fatal);
+}
+
+void Server::stats(double *out) {
+    std::lock_guard<std::mutex> lk(mu);
+    for (int k = 0; k < XMD_SRV_NUM; ++k) out[k] = 0.0;
+    std::vector<double> l = latencies;
+    std::sort(l.begin(), l.end());
+    auto pct = [&](double q) {
+        if (l.empty()) return 0.0;
+        // nearest-rank percentile
+        size_t k = (size_t)std::ceil(q * l.size());
+        return l[std::min(l.size(), std::max<size_t>(1, k)) - 1];
+    };
+    out[XMD_SRV_P50_S] = pct(0.50);
+    out[XMD_SRV_P99_S] = pct(0.99);
+    const double span = t_last - t_first;
+    out[XMD_SRV_BEAD_STEPS_PER_S] = (span > 0 && !l.empty()) ? bead_steps / span : 0.0;
+    out[XMD_SRV_COMPLETED] = (double)l.size();
+    out[XMD_SRV_QUEUED] = (double)queue.size();
+    out[XMD_SRV_RUNNING] = (double)running.size();
+    out[XMD_SRV_CHUNKS] = (double)chunks;
+    out[XMD_SRV_PEAK_RUNNING] = (double)peak_running;
+    out[XMD_SRV_CAP_BEADS] = (double)cap_beads;
+    out[XMD_SRV_BEAD_STEPS] = bead_steps;
+    out[XMD_SRV_SPAN_S] = span;
+}
+
+// place a queued request into a free slot; false when the capacity has no
+// room for it now (it stays queued)
+bool Server::admit(Request *q) {
+    Engine &e = *eng;
+    int slot;
+    try {
+        slot = e.add_replica(q->n, q->chain.data(), q->seq.data(), q->atype.data(), q->cell, q->temperature,
+                             q->seed);
+    } catch (std::length_error &) {
+        return false;   // every replica slot is taken
+    }
+    try {
+        e.set_tethers(slot, (int)q->t1.size(), q->t1.data(), q->t2.data(), q->td.data());
+        e.set_angles(slot, (int)q->a1.size(), q->a1.data(), q->a2.data(), q->a3.data(), q->ath.data());
+        e.set_dihedrals(slot, (int)q->d1.size(), q->d1.data(), q->d2.data(), q->d3.data(), q->d4.data(),
+                        q->dph.data());
+        e.set_native(slot, (int)q->n1.size(), q->n1.data(), q->n2.data(), q->nd.data());
+        e.set_state(slot, q->r.data(), q->v.empty() ? nullptr : q->v.data());
+        e.set_steps(slot, q->nsteps);
+        e.place_now(slot);
+    } catch (std::length_error &) {
+        e.remove_replica(slot);
+        return false;   // no contiguous room in the reserved capacity yet
+    } catch (std::exception &ex) {
+        e.remove_replica(slot);
+        std::lock_guard<std::mutex> lk(mu);
+        q->state = XMD_REQ_FAILED;
+        q->error = ex.what();
+        return true;   // consumed (failed)
+    }
+    q->slot = slot;
+    return true;
+}
+
+void Server::retire(Request *q) {
+    Engine &e = *eng;
+    q->r_out.resize(3 * (size_t)q->n);
+    q->v_out.resize(3 * (size_t)q->n);
+    e.get_state(q->slot, q->r_out.data(), q->v_out.data(), &q->t_out);
+    e.remove_replica(q->slot);
+    std::lock_guard<std::mutex> lk(mu);
+    q->t_done = now_s();
+    q->state = XMD_REQ_DONE;
+    latencies.push_back(q->t_done - q->t_submit);
+    bead_steps += (double)q->n * (double)q->nsteps;
+    t_last = q->t_done;
+}
+
+void Server::loop() {
+    try {
+        eng->use_device();
+        std::vector<long long> left;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                cv.wait(lk, [&] { return stop || !queue.empty() || !running.empty(); });
+                if (stop) break;
+            }
+            // admission, first come first served
+            for (;;) {
+                Request *q;
+                {
+                    std::lock_guard<std::mutex> lk(mu);
+                    if (queue.empty()) break;
+                    q = queue.front();
+                }
+                if (!admit(q)) break;
+                std::lock_guard<std::mutex> lk(mu);
+                queue.pop_front();
+                if (q->state == XMD_REQ_FAILED) {
+                    cv_done.notify_all();
+                    continue;
+                }
+                q->state = XMD_REQ_RUNNING;
+                q->t_start = now_s();
+                running.push_back(q);
+                peak_running = std::max(peak_running, (int)running.size());
+            }
+            if (running.empty()) {
+                // the head of the queue does not fit an empty context: it never will
+                std::lock_guard<std::mutex> lk(mu);
+                if (!queue.empty()) {
+                    Request *q = queue.front();
+                    queue.pop_front();
+                    q->state = XMD_REQ_FAILED;
+                    q->error = "the request does not fit the reserved capacity";
+                    cv_done.notify_all();
+                }
+                continue;
+            }
+            bool pending_zero = false;
+            for (Request *q : running) pending_zero |= q->nsteps == 0;
+            if (!pending_zero) {
+                eng->step(chunk);
+                ++chunks;
+            }
+            left.assign(eng->capacity_replicas(), -2);
+            eng->steps_left(left.data());
+            std::vector<Request *> keep;
+            for (Request *q : running) {
+                if (left[q->slot] == 0) retire(q);
+                else keep.push_back(q);
+            }
+            {
+                std::lock_guard<std::mutex> lk(mu);
+                running.swap(keep);
+            }
+            cv_done.notify_all();
+        }
+    } catch (std::exception &ex) {
+        std::lock_guard<std::mutex> lk(mu);
+        fatal = ex.what();
+        for (Request *q : running) {
+            q->state = XMD_REQ_FAILED;
+            q->error = fatal;
+        }
+        for (Request *q : queue) {
+            q->state = XMD_REQ_FAILED;
+            q->error = fatal;
+        }
+        running.clear();
+        queue.clear();
+        cv_done.notify_all();
+    }
+}
+
+}  // namespace xmdg

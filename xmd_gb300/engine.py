@@ -20,7 +20,7 @@ class Engine:
         h = C.c_void_p()
         check(self.lib.xmd_gpu_create(yaml_text.encode(), C.byref(h)))
         self.h = h
-        self.sizes: list[int] = []
+        self.sizes: dict[int, int] = {}
 
     def close(self):
         if self.h:
@@ -71,7 +71,7 @@ class Engine:
         check(self.lib.xmd_gpu_set_native_contacts(self.h, r, len(n1), iptr(n1), iptr(n2), dptr(nd)))
         rr = np.ascontiguousarray(s.r, dtype=np.float64).reshape(-1)
         check(self.lib.xmd_gpu_set_state(self.h, r, dptr(rr), None))
-        self.sizes.append(s.n)
+        self.sizes[r] = s.n
         return r
 
     def eval_forces(self, rep: int = 0):
@@ -128,6 +128,17 @@ class Engine:
         s = C.c_int32()
         check(self.lib.xmd_gpu_device_status(self.h, C.byref(s)))
         return s.value
+
+    def reserve(self, beads: int, replicas: int, native_entries: int):
+        """Fixed device capacities; replicas can then come and go between steps."""
+        check(self.lib.xmd_gpu_reserve(self.h, int(beads), int(replicas), int(native_entries)))
+
+    def remove_replica(self, rep: int):
+        check(self.lib.xmd_gpu_remove_replica(self.h, int(rep)))
+        self.sizes.pop(rep, None)
+
+    def set_steps(self, rep: int, nsteps: int):
+        check(self.lib.xmd_gpu_set_steps(self.h, int(rep), int(nsteps)))
 
     def synchronize(self):
         check(self.lib.xmd_gpu_synchronize(self.h))

@@ -326,3 +326,32 @@ def config_c4(seed=4, count=256, workers=0):
         with ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
             return list(ex.map(_c4_one, jobs, chunksize=4))
     return [_c4_one(j) for j in jobs]
+
+
+def c5_request(seed: int, max_chains=64, lo=30, hi=1500, max_beads=200_000):
+    """One serving request: 1-64 chains with lengths log-uniform in [30, 1500]
+    beads (total capped), open boundaries, Go + Debye-Hueckel topology, seeded
+    temperature uniform in [0.3, 0.6]."""
+    rng = np.random.default_rng(10_000 + seed)
+    nch = int(rng.integers(1, max_chains + 1))
+    lens = np.floor(np.exp(rng.uniform(math.log(lo), math.log(hi), size=nch))).astype(int)
+    lens = lens[np.cumsum(lens) <= max_beads]
+    T = float(rng.uniform(0.3, 0.6))
+    return make_system([int(L) for L in lens], 20_000 + seed, box=None, types="charged10", temperature=T,
+                       rng_seed=30_000 + seed)
+
+
+def _c5_one(args):
+    return c5_request(*args)
+
+
+def config_c5(count=24, seed=5, workers=0, max_chains=64):
+    """`count` serving requests (config 5), optionally generated in a spawned
+    process pool (same requests, same order)."""
+    jobs = [(seed * 1000 + k, max_chains) for k in range(count)]
+    if workers and workers > 1:
+        import multiprocessing as mp
+        from concurrent.futures import ProcessPoolExecutor
+        with ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+            return list(ex.map(_c5_one, jobs, chunksize=1))
+    return [_c5_one(j) for j in jobs]
