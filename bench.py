@@ -291,6 +291,17 @@ def run_engine(args, rank, local, world):
             Fd, _ = ed.eval_forces(r)
             errs.append(float(np.abs(Fm - Fd).max() / max(np.abs(Fd).max(), 1e-300)))
 
+    # serving (config 5): Poisson arrivals offered at ~70% of the batched
+    # mixed throughput, mixed and plain FP64 on the same request stream
+    serving = None
+    if args.serve_requests > 0:
+        from xmd_gb300 import synth as _s
+        reqs = _s.config_c5(count=args.serve_requests, seed=5 + rank, workers=min(16, os.cpu_count() or 1))
+        mean_work = float(np.mean([rq.n for rq in reqs])) * args.serve_steps
+        rate = 0.7 * (value / world) / mean_work
+        serving = {"mixed": serve_bench(reqs, "mixed", args.serve_steps, rate, dev),
+                   "fp64": serve_bench(reqs, "fp64", args.serve_steps, rate, dev)}
+
     cpu = cpu_baseline(systems, sample_steps=args.cpu_sample_steps) if rank == 0 else None
     rt.cudaFree(flush)
     rt.cudaFreeHost(hbuf)
@@ -311,7 +322,8 @@ def run_engine(args, rank, local, world):
             "mixed_over_plain_fp64": value / world / plain64["value"],
             "batched_fp64_value": value64, "mixed_over_batched_fp64": value / world / value64,
             "mixed_force_rel_err_max": max(errs), "graph_steps_per_launch": 16,
-            "p99_req_latency_ms": None,
+            "p99_req_latency_ms": serving["mixed"]["p99_ms"] if serving else None,
+            "serving": serving,
         },
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
@@ -354,6 +366,34 @@ def plain_fp64(systems, yaml_fp64, md, warmup, rt, flush, sample=16):
     return {"value": work / (t_ms / 1e3),
             "sample": f"{len(pick)} size-stratified replicas ({nb} beads), each alone in an FP64 context, "
                       f"{md} steps each"}
+
+
+def serve_bench(requests, precision, nsteps, rate_hz, device, seed=0):
+    """Config 5: requests arrive as a Poisson process at `rate_hz` and are
+    served by the continuous-batching loop (HBM-budget admission, state
+    resident on the device).  Returns latency percentiles and throughput."""
+    from xmd_gb300 import Server, synth
+    yaml = synth.yaml_for("c5", precision) + f"  device: {device}\n"
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate_hz, size=len(requests))
+    with Server(yaml, hbm_budget=8 << 30, max_beads=200_000, chunk_steps=256) as srv:
+        # warm-up request (graph capture, first list builds) outside the clock
+        srv.result(srv.submit(requests[0], 256))
+        t0 = time.perf_counter()
+        ids = []
+        for g, rq in zip(gaps, requests):
+            time.sleep(g)
+            ids.append(srv.submit(rq, nsteps))
+        lat = [srv.result(i)[3] for i in ids]
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+    lat = np.sort(np.asarray(lat))
+    work = float(sum(rq.n for rq in requests)) * nsteps
+    return {"p50_ms": 1e3 * float(np.percentile(lat, 50, method="inverted_cdf")),
+            "p99_ms": 1e3 * float(np.percentile(lat, 99, method="inverted_cdf")),
+            "bead_steps_per_s": work / wall, "wall_s": wall, "peak_concurrent": int(st["peak_running"]),
+            "requests": len(requests), "steps_per_request": nsteps, "rate_hz": rate_hz,
+            "beads_total": int(sum(rq.n for rq in requests))}
 
 
 # ------------------------------------------------------------- CPU arms --
@@ -439,6 +479,8 @@ def main():
     ap.add_argument("--md-steps", type=int, default=96)
     ap.add_argument("--md-steps-ref", type=int, default=5)
     ap.add_argument("--cpu-sample-steps", type=int, default=100)
+    ap.add_argument("--serve-requests", type=int, default=12)
+    ap.add_argument("--serve-steps", type=int, default=20000)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, local, world = dist_env()

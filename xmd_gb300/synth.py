@@ -69,11 +69,12 @@ def _sphere(rng):
     return _unit(v)
 
 
-def saw_chain(rng, n, bond, start, min_sep=4.0 * ANGSTROM, tries=16, others=None):
+def saw_chain(rng, n, bond, start, min_sep=4.0 * ANGSTROM, tries=16, others=None, window=None):
     """A persistent random walk as in morph_into_saw with overlap rejection:
     each step turns the direction by a spread angle about perp_v(dir) and an
     around angle about dir; `tries` turns are drawn at once and the first
-    whose bead keeps min_sep from earlier beads is taken (else the best)."""
+    whose bead keeps min_sep from earlier beads (the last `window` of them,
+    or all) is taken (else the best)."""
     max_spread, max_around = math.pi / 12.0, math.pi
     pos = np.empty((n, 3))
     pos[0] = start
@@ -90,7 +91,8 @@ def saw_chain(rng, n, bond, start, min_sep=4.0 * ANGSTROM, tries=16, others=None
         cand = pos[k - 1] + bond * v2
         dmin = np.full(tries, np.inf)
         if k >= 3:
-            dmin = np.sqrt(((cand[:, None, :] - pos[None, :k - 2, :]) ** 2).sum(axis=2).min(axis=1))
+            lo = 0 if window is None else max(0, k - 2 - window)
+            dmin = np.sqrt(((cand[:, None, :] - pos[None, lo:k - 2, :]) ** 2).sum(axis=2).min(axis=1))
         if others is not None and len(others):
             do = np.sqrt(((cand[:, None, :] - others[None, :, :]) ** 2).sum(axis=2).min(axis=1))
             dmin = np.minimum(dmin, do)
@@ -170,7 +172,8 @@ def _types(rng, n, mode):
 
 
 def make_system(chain_lengths, seed, box=None, density=1e-3, types="charged10",
-                bond=3.8 * ANGSTROM, native=True, temperature=0.0, rng_seed=None, start="saw"):
+                bond=3.8 * ANGSTROM, native=True, temperature=0.0, rng_seed=None, start="saw",
+                saw_window=None, avoid_others=True):
     """Build one replica.  box: edge in internal units (periodic cube) or None
     for open boundaries; density (per A^3) sizes the starting cube.
     start="saw" begins from the extended walk (far from the native structure,
@@ -195,8 +198,8 @@ def make_system(chain_lengths, seed, box=None, density=1e-3, types="charged10",
     off = 0
     for c, L in enumerate(lens):
         start_pt = rng.uniform(-a / 2.0, a / 2.0, size=3)
-        others = r[max(0, off - 2000):off] if off else None
-        r[off:off + L] = saw_chain(rng, L, bond, start_pt, others=others)
+        others = r[max(0, off - 2000):off] if (off and avoid_others) else None
+        r[off:off + L] = saw_chain(rng, L, bond, start_pt, others=others, window=saw_window)
         if L >= 2:
             tet_i1 += list(range(off, off + L - 1))
             tet_i2 += list(range(off + 1, off + L))
@@ -328,6 +331,139 @@ def config_c4(seed=4, count=256, workers=0):
     return [_c4_one(j) for j in jobs]
 
 
+def _perp_batch(d):
+    # perp_v (model.cpp:93-99) of each row
+    p1 = np.cross(d, [1.0, 0.0, 0.0])
+    p2 = np.cross(d, [0.0, 1.0, 0.0])
+    pick = (np.linalg.norm(p1, axis=1) > np.linalg.norm(p2, axis=1))[:, None]
+    p = np.where(pick, p1, p2)
+    return p / np.linalg.norm(p, axis=1, keepdims=True)
+
+
+def _min_dist(cand, seg):
+    """min over j of |cand[a, t] - seg[a, j]| for each chain a and try t
+    (|c|^2 + |s|^2 - 2 c.s through batched matrix products)."""
+    c2 = (cand * cand).sum(axis=2)[:, :, None]
+    s2 = (seg * seg).sum(axis=2)[:, None, :]
+    d2 = c2 + s2 - 2.0 * np.matmul(cand, seg.transpose(0, 2, 1))
+    return np.sqrt(np.maximum(d2.min(axis=2), 0.0))
+
+
+def saw_chains(rng, lens, bond, starts, window=256, min_sep=4.0 * ANGSTROM, tries=16):
+    """saw_chain for many chains at once (each step advances every chain that
+    is still growing); self-avoidance over the last `window` beads."""
+    lens = np.asarray(lens)
+    C, Lm = len(lens), int(lens.max())
+    pos = np.zeros((C, Lm, 3))
+    pos[:, 0] = starts
+    d = rng.normal(size=(C, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    ms, ma = math.pi / 12.0, math.pi
+    for k in range(1, Lm):
+        act = np.nonzero(lens > k)[0]
+        A = len(act)
+        dd = d[act][:, None, :]
+        sp = rng.uniform(-ms, ms, size=(A, tries, 1))
+        ar = rng.uniform(-ma, ma, size=(A, tries, 1))
+        p = _perp_batch(d[act])[:, None, :]
+        v1 = dd * np.cos(sp) + np.cross(p, dd) * np.sin(sp)
+        dv = (v1 * dd).sum(axis=2, keepdims=True)
+        v2 = v1 * np.cos(ar) + np.cross(dd, v1) * np.sin(ar) + dd * dv * (1.0 - np.cos(ar))
+        v2 /= np.linalg.norm(v2, axis=2, keepdims=True)
+        cand = pos[act, k - 1][:, None, :] + bond * v2
+        if k >= 3:
+            lo = max(0, k - 2 - window)
+            dmin = _min_dist(cand, pos[act, lo:k - 2])
+        else:
+            dmin = np.full((A, tries), np.inf)
+        ok = dmin >= min_sep
+        pick = np.where(ok.any(axis=1), ok.argmax(axis=1), dmin.argmax(axis=1))
+        ar_ = np.arange(A)
+        pos[act, k] = cand[ar_, pick]
+        d[act] = v2[ar_, pick]
+    return [pos[c, :lens[c]] for c in range(C)]
+
+
+def compact_walks(rng, lens, bond, density=1.0 / 120.0, min_sep=4.2 * ANGSTROM, tries=48, batch=8):
+    """compact_walk for many chains at once."""
+    lens = np.asarray(lens)
+    C, Lm = len(lens), int(lens.max())
+    radius = np.maximum((3.0 * lens / (4.0 * math.pi * density)) ** (1.0 / 3.0) * ANGSTROM, 2.0 * bond)
+    pos = np.zeros((C, Lm, 3))
+    for k in range(1, Lm):
+        act = np.nonzero(lens > k)[0]
+        A = len(act)
+        best = np.zeros((A, 3))
+        best_score = np.full(A, -np.inf)
+        done = np.zeros(A, dtype=bool)
+        for _ in range(0, tries, batch):
+            todo = np.nonzero(~done)[0]
+            if not len(todo):
+                break
+            ch = act[todo]
+            dirs = rng.normal(size=(len(todo), batch, 3))
+            dirs /= np.linalg.norm(dirs, axis=2, keepdims=True)
+            cand = pos[ch, k - 1][:, None, :] + bond * dirs
+            if k >= 2:
+                dmin = _min_dist(cand, pos[ch, :k - 1])
+            else:
+                dmin = np.full((len(todo), batch), np.inf)
+            out = np.maximum(0.0, np.linalg.norm(cand, axis=2) - radius[ch][:, None])
+            score = np.minimum(dmin - min_sep, 0.0) - out
+            ok = score >= 0.0
+            has = ok.any(axis=1)
+            j = np.where(has, ok.argmax(axis=1), score.argmax(axis=1))
+            sj = score[np.arange(len(todo)), j]
+            cj = cand[np.arange(len(todo)), j]
+            better = has | (sj > best_score[todo])
+            best[todo[better]] = cj[better]
+            best_score[todo[better]] = sj[better]
+            done[todo[has]] = True
+        pos[act, k] = best
+    return [pos[c, :lens[c]] for c in range(C)]
+
+
+def make_request_system(chain_lengths, seed, temperature, rng_seed, density=1e-3, bond=3.8 * ANGSTROM):
+    """A multi-chain open system built with the batched walks (config 5)."""
+    rng = np.random.default_rng(seed)
+    lens = [int(x) for x in chain_lengths]
+    n = sum(lens)
+    chain = np.concatenate([np.full(L, c, dtype=np.int32) for c, L in enumerate(lens)])
+    seq = np.concatenate([np.arange(L, dtype=np.int32) for L in lens])
+    atype = _types(rng, n, "charged10")
+    a = (n / density) ** (1.0 / 3.0) * ANGSTROM
+    starts = rng.uniform(-a / 2.0, a / 2.0, size=(len(lens), 3))
+    walks = saw_chains(rng, lens, bond, starts)
+    natives = compact_walks(rng, lens, bond)
+    r = np.concatenate(walks)
+    tet, ang, dih, nat = ([], [], []), ([], [], [], []), ([], [], [], [], []), ([], [], [])
+    off = 0
+    for L, npos in zip(lens, natives):
+        if L >= 2:
+            tet[0].append(np.arange(off, off + L - 1)); tet[1].append(np.arange(off + 1, off + L))
+            tet[2].append(np.full(L - 1, bond))
+        if L >= 3:
+            th, ph = bonded_natives(npos)
+            k = np.arange(len(th))
+            ang[0].append(off + k); ang[1].append(off + k + 1); ang[2].append(off + k + 2); ang[3].append(th)
+            k = np.arange(len(ph))
+            dih[0].append(off + k); dih[1].append(off + k + 1); dih[2].append(off + k + 2)
+            dih[3].append(off + k + 3); dih[4].append(ph)
+            i1, i2, dd = native_map(npos)
+            nat[0].append(i1 + off); nat[1].append(i2 + off); nat[2].append(dd)
+        off += L
+    cat32 = lambda xs: np.concatenate(xs).astype(np.int32) if xs else np.zeros(0, np.int32)
+    catf = lambda xs: np.concatenate(xs).astype(np.float64) if xs else np.zeros(0)
+    return System(
+        n=n, chain=chain, seq=seq, atype=atype, cell=np.zeros(3), r=r,
+        tethers=(cat32(tet[0]), cat32(tet[1]), catf(tet[2])),
+        angles=(cat32(ang[0]), cat32(ang[1]), cat32(ang[2]), catf(ang[3])),
+        dihedrals=(cat32(dih[0]), cat32(dih[1]), cat32(dih[2]), cat32(dih[3]), catf(dih[4])),
+        natives=(cat32(nat[0]), cat32(nat[1]), catf(nat[2])),
+        temperature=temperature, seed=int(rng_seed), meta={"chains": lens},
+    )
+
+
 def c5_request(seed: int, max_chains=64, lo=30, hi=1500, max_beads=200_000):
     """One serving request: 1-64 chains with lengths log-uniform in [30, 1500]
     beads (total capped), open boundaries, Go + Debye-Hueckel topology, seeded
@@ -337,8 +473,9 @@ def c5_request(seed: int, max_chains=64, lo=30, hi=1500, max_beads=200_000):
     lens = np.floor(np.exp(rng.uniform(math.log(lo), math.log(hi), size=nch))).astype(int)
     lens = lens[np.cumsum(lens) <= max_beads]
     T = float(rng.uniform(0.3, 0.6))
-    return make_system([int(L) for L in lens], 20_000 + seed, box=None, types="charged10", temperature=T,
-                       rng_seed=30_000 + seed)
+    # self-avoidance over the last 256 beads of a chain; chains start at
+    # random points of the density-sized cube and may meet (Pauli separates them)
+    return make_request_system([int(L) for L in lens], 20_000 + seed, T, 30_000 + seed)
 
 
 def _c5_one(args):
