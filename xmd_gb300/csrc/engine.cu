@@ -513,6 +513,7 @@ __global__ void __launch_bounds__(CB) k_cells(Dev d, int cur) {
         // rounding each, so this margin never rejects a pair inside req_r
         double m = rp.req_r + 1e-3 + 4e-7 * ext;
         rp.pre2 = (float)(m * m);
+        rp.band_m = 1e-3 + 4e-7 * ext;
         rp.first = 0;
         rp.rebuilds += 1;
     }
@@ -575,6 +576,16 @@ __global__ void __launch_bounds__(CB) k_cells(Dev d, int cur) {
 }
 
 // ---- Verlet rows (legacy_update.cpp:16-62 + the update_* filters) ---------------
+// FP32 decision band around a distance threshold T (error bound m)
+struct Band {
+    float lo, hi;   // squared FP32 distance: below lo -> inside, above hi -> outside
+};
+__device__ __forceinline__ Band make_band(double T, double m) {
+    double a = T - m, b = T + m;
+    return Band{a > 0.0 ? __double2float_rd(a * a) : -1.0f, __double2float_ru(b * b)};
+}
+__device__ __forceinline__ bool in_band(const Band &B, float d2) { return d2 >= B.lo && d2 <= B.hi; }
+
 __global__ void __launch_bounds__(128) k_nl_build(Dev d, TermP p, int cur) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.N) return;
@@ -591,8 +602,15 @@ __global__ void __launch_bounds__(128) k_nl_build(Dev d, TermP p, int cur) {
 
     // Go list: update_go_contacts, go.cpp:11-22
     for (int k = n0; k < n1; ++k) {
-        double dd = dist_exact(bx, pi, pos[d.nat_j[k]]);
-        d.nat_on[k] = dd < __dadd_rn(2.0 * d.nat_d[k], pad);
+        const double4_32a pj = pos[d.nat_j[k]];
+        const double T = __dadd_rn(2.0 * d.nat_d[k], pad);
+        float ex = (float)(pj.x - pi.x), ey = (float)(pj.y - pi.y), ez = (float)(pj.z - pi.z);
+        ex -= (float)bx.cell[0] * rintf(ex * (float)bx.cell_inv[0]);
+        ey -= (float)bx.cell[1] * rintf(ey * (float)bx.cell_inv[1]);
+        ez -= (float)bx.cell[2] * rintf(ez * (float)bx.cell_inv[2]);
+        const float d2 = ex * ex + ey * ey + ez * ez;
+        const Band B = make_band(T, 1e-3 + 1e-6 * T);
+        d.nat_on[k] = in_band(B, d2) ? dist_exact(bx, pi, pj) < T : d2 < B.lo;
     }
 
     int cc[3];
@@ -625,6 +643,11 @@ __global__ void __launch_bounds__(128) k_nl_build(Dev d, TermP p, int cur) {
     const float Lx = (float)bx.cell[0], Ly = (float)bx.cell[1], Lz = (float)bx.cell[2];
     const float Lix = (float)bx.cell_inv[0], Liy = (float)bx.cell_inv[1], Liz = (float)bx.cell_inv[2];
     const float pre2 = rp.pre2;
+    const double bm = rp.band_m;
+    const Band Breq = make_band(rp.req_r, bm);
+    const Band Bpa = make_band(1.0 / rp.pauli_min_inv, bm);
+    const Band Bes = make_band(1.0 / rp.es_min_inv, bm);
+    const Band Bqa = make_band(1.0 / rp.qa_min_inv, bm);
     const bool pauli_on = p.on[XMD_TERM_PAULI] != 0;
     const bool go_on = p.on[XMD_TERM_GO] != 0;
     const bool es_on = (p.on[XMD_TERM_CONST_ES] || p.on[XMD_TERM_REL_ES]);
@@ -644,23 +667,38 @@ __global__ void __launch_bounds__(128) k_nl_build(Dev d, TermP p, int cur) {
                     ddx -= Lx * rintf(ddx * Lix);
                     ddy -= Ly * rintf(ddy * Liy);
                     ddz -= Lz * rintf(ddz * Liz);
-                    if (ddx * ddx + ddy * ddy + ddz * ddz > pre2) continue;
+                    const float d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+                    if (d2 > pre2) continue;
                     int cj = d.chain[j], sj = d.seq[j];
                     int df = si > sj ? si - sj : sj - si;
                     if (ci == cj && df < 3) continue;
-                    double4_32a pj = pos[j];
-                    double dd = dist_exact(bx, pi, pj);
-                    if (!(dd < rp.req_r)) continue;
+                    // decided in FP32 away from every threshold, exactly near one
+                    // (the margin argument of k_nl_tile)
+                    bool in_req, pa, es, qa;
+                    if (in_band(Breq, d2) || (pauli_on && in_band(Bpa, d2)) || (es_on && in_band(Bes, d2)) ||
+                        (qa_on && in_band(Bqa, d2))) {
+                        const double dd = dist_exact(bx, pi, pos[j]);
+                        const double inv = __ddiv_rn(1.0, dd);
+                        in_req = dd < rp.req_r;
+                        pa = inv > rp.pauli_min_inv;
+                        es = inv > rp.es_min_inv;
+                        qa = inv > rp.qa_min_inv;
+                    } else {
+                        in_req = d2 < Breq.lo;
+                        pa = d2 < Bpa.lo;
+                        es = d2 < Bes.lo;
+                        qa = d2 < Bqa.lo;
+                    }
+                    if (!in_req) continue;
                     // natives leave the list only when native contacts are
                     // enabled (main.cpp:504-530 wires all_nat_cont there)
                     bool native = false;
                     if (go_on)
                         for (int k = n0; k < n1; ++k) native |= d.nat_j[k] == j;
                     if (native) continue;
-                    double inv = __ddiv_rn(1.0, dd);
                     // quasi-adiabatic free pairs (update_free_pairs, free_pair.cpp:9-19),
                     // j > i, minus pairs already in contact
-                    if (qa_on && j > i && inv > rp.qa_min_inv) {
+                    if (qa_on && j > i && qa) {
                         bool in_contact = false;
                         for (int k = 0; k < nref; ++k) {
                             int s = d.qa.ref[(size_t)k * d.N + i];
@@ -673,8 +711,8 @@ __global__ void __launch_bounds__(128) k_nl_build(Dev d, TermP p, int cur) {
                         }
                     }
                     int flags = 0;
-                    if (pauli_on && inv > rp.pauli_min_inv) flags |= NL_PAULI;
-                    if (es_on && inv > rp.es_min_inv && pi.w * pj.w != 0.0) flags |= NL_ES;
+                    if (pauli_on && pa) flags |= NL_PAULI;
+                    if (es_on && es && pi.w * pos[j].w != 0.0) flags |= NL_ES;
                     if (!flags) continue;
                     if (cnt < cap) d.nl_row[(size_t)cnt * d.N + i] = j | flags;
                     ++cnt;
@@ -715,14 +753,7 @@ __device__ __forceinline__ float tl_rel(const RepDev &rp, int a, double x, doubl
     return (float)(x - ref);
 }
 
-struct Band {
-    float lo, hi;   // squared FP32 distance: below lo -> inside, above hi -> outside
-};
-__device__ __forceinline__ Band make_band(double T, double m) {
-    double a = T - m, b = T + m;
-    return Band{a > 0.0 ? __double2float_rd(a * a) : -1.0f, __double2float_ru(b * b)};
-}
-__device__ __forceinline__ bool in_band(const Band &B, float d2) { return d2 >= B.lo && d2 <= B.hi; }
+
 
 __global__ void __launch_bounds__(TL_THREADS) k_nl_tile(Dev d, TermP p, int cur) {
     if (blockIdx.x == 0 && threadIdx.x == 0 && !d.any_cell) atomicAdd(d.ctr, 1ull);

@@ -35,6 +35,7 @@ struct RepDev {
     int hashed;              // cells hashed into the bucket budget
     int tile;                // Verlet build by whole-replica tiles (no cell grid)
     float pre2;              // squared FP32 pre-filter radius of the Verlet build
+    double band_m;           // FP32 distance error bound of the cell build
     int first, rebuild;
     int active;              // slot holds a placed replica
     long long steps_left;    // steps this replica still takes (-1: no bound)
