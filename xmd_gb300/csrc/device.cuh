@@ -106,7 +106,7 @@ __device__ __forceinline__ V3<T> tether_term(const TermP &p, double4_32a r1, dou
     V3<T> r12 = diff<T>(r1, r2);
     T r12_n = norm(r12);
     T dr = r12_n - nat_dist, dr2 = dr * dr;
-    T H1 = T(p.tether_H1), H2 = T(p.tether_H2);
+    T H1 = tpar<T>(p.tether_H1, p.f.tether_H1), H2 = tpar<T>(p.tether_H2, p.f.tether_H2);
     T V_ = T(0.5) * dr2 * (H1 + H2 * dr2);
     T dV_dr = dr * (H1 + T(2) * H2 * dr2);
     V_ = clampv<T>(V_, T(-1.0e3), T(1.0e3));
@@ -201,7 +201,7 @@ __device__ __forceinline__ V3<float> f3(V3<double> a) { return V3<float>{(float)
 __device__ __forceinline__ V3<float> tether_vec(const TermP &p, V3<float> r12, float nat_dist, float *V) {
     float r12_n = norm(r12);
     float dr = r12_n - nat_dist, dr2 = dr * dr;
-    float H1 = (float)p.tether_H1, H2 = (float)p.tether_H2;
+    float H1 = p.f.tether_H1, H2 = p.f.tether_H2;
     float V_ = 0.5f * dr2 * (H1 + H2 * dr2);
     float dV_dr = dr * (H1 + 2.0f * H2 * dr2);
     *V = clampv<float>(V_, -1.0e3f, 1.0e3f);
@@ -220,7 +220,7 @@ __device__ __forceinline__ void angle_mixed(const TermP &p, V3<float> r12, V3<fl
     V3<float> d2 = (-d1) - d3;
     float theta = atan2f(norm(x12_23), -dot(r12, r23));
     float dtheta = theta - nat_theta;
-    float k = (float)p.nat_ang_k;
+    float k = p.f.nat_ang_k;
     *V = 0.5f * k * dtheta * dtheta;
     float dV = k * dtheta;
     *f1 = -(dV * d1);
@@ -244,12 +244,12 @@ __device__ __forceinline__ void dihedral_mixed(const TermP &p, V3<float> r12, V3
         float s1, c1, s3, c3;
         sincosf(diff_, &s1, &c1);
         sincosf(3.0f * diff_, &s3, &c3);
-        float CDA = (float)p.cnd_CDA, CDB = (float)p.cnd_CDB;
+        float CDA = p.f.cnd_CDA, CDB = p.f.cnd_CDB;
         *Vc = CDA * (1.0f - c1) + CDB * (1.0f - c3);
         dV += CDA * s1 + CDB * 3.0f * s3;
     }
     if (snd) {
-        float CDH = (float)p.snd_CDH;
+        float CDH = p.f.snd_CDH;
         *Vs = 0.5f * CDH * diff_ * diff_;
         dV += CDH * diff_;
     }
@@ -285,7 +285,7 @@ __device__ __forceinline__ V3<T> go_pair(const TermP &p, V3<T> r12, T nat_dist, 
     T r12_rn = ninv(r12);
     V3<T> u = r12_rn * r12;
     T dV;
-    lj_eval<T>(T(p.go_depth), nat_dist, r12_rn, V, &dV);
+    lj_eval<T>(tpar<T>(p.go_depth, p.f.go_depth), nat_dist, r12_rn, V, &dV);
     return dV * u;
 }
 
@@ -294,10 +294,10 @@ __device__ __forceinline__ V3<T> go_pair(const TermP &p, V3<T> r12, T nat_dist, 
 template <class T>
 __device__ __forceinline__ V3<T> pauli_pair(const TermP &p, V3<T> r12, T *V) {
     T r12_rn = ninv(r12);
-    T r_excl = T(p.pauli_r_excl);
+    T r_excl = tpar<T>(p.pauli_r_excl, p.f.pauli_r_excl);
     if (T(1) < r12_rn * r_excl) {
         V3<T> u = r12_rn * r12;
-        T depth = T(p.pauli_depth);
+        T depth = tpar<T>(p.pauli_depth, p.f.pauli_depth);
         T s = r12_rn * r_excl, s6 = ipow6(s), s12 = s6 * s6;
         T V_ = depth * (s12 - T(2) * s6 + T(1));
         T dV_dr = T(12) * depth * r12_rn * (s6 - s12);
@@ -315,8 +315,8 @@ template <class T>
 __device__ __forceinline__ V3<T> es_pair(const TermP &p, V3<T> r12, T q1_x_q2, T *V) {
     T r12_n = norm(r12), r12_rn = T(1) / r12_n;
     V3<T> u = r12_rn * r12;
-    T sdi = T(p.es_sdi);
-    T Vij = T(p.es_Vf) * q1_x_q2 * exp_(-r12_n * sdi) * r12_rn * r12_rn;
+    T sdi = tpar<T>(p.es_sdi, p.f.es_sdi);
+    T Vij = tpar<T>(p.es_Vf, p.f.es_Vf) * q1_x_q2 * exp_(-r12_n * sdi) * r12_rn * r12_rn;
     T dVij_dr = p.es_rel ? -Vij * (sdi + T(2) * r12_rn) : -Vij * (sdi + r12_rn);
     *V = Vij;
     return dVij_dr * u;

@@ -100,14 +100,18 @@ __device__ __forceinline__ void add3(double &fx, double &fy, double &fz, V3<FT> 
     fz += (double)f.z;
 }
 
+// finiteness from the exponent bits (integer pipe)
+__device__ __forceinline__ bool finite_bits(double x) {
+    return ((unsigned long long)__double_as_longlong(x) & 0x7ff0000000000000ull) != 0x7ff0000000000000ull;
+}
+
 // ---- force (+ integrate) kernel --------------------------------------------------
 // MODE 0: forces and per-term energies at pos[cur] (eval).
 // MODE 1: forces, then one Langevin predictor-corrector step (lang_pc.cpp:5-41)
 //         writing pos[cur^1], y1..y5, the generator state and the skin-test
 //         displacement (verify.cpp:10-15).
 template <class FT, int MODE>
-__global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
-    if (!d.blk_on[blockIdx.x]) return;   // no placed bead in this block (uniform)
+__device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cur) {
     const double4_32a *__restrict__ pin = d.pos[cur];
     const int N = d.N, t = threadIdx.x, i0 = blockIdx.x * FB;
     __shared__ double4_32a P[FB + 6];
@@ -150,7 +154,7 @@ __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
         int rc = own ? d.rep_of[c] : 0;
         if ((fl & BF_TETH) && p.on[XMD_TERM_TETHER]) {
             FT V_;
-            if constexpr (sizeof(FT) == 4) ft = tether_vec(p, Ef[sp], (float)d.teth_r0[c], &V_);
+            if constexpr (sizeof(FT) == 4) ft = tether_vec(p, Ef[sp], d.bond_f[c].x, &V_);
             else ft = tether_term<FT>(p, P[sp], P[sp + 1], (FT)d.teth_r0[c], &V_);
             if (MODE == 0 && own) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_TETHER], (double)V_);
         }
@@ -176,13 +180,13 @@ __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
             // FP32 forces
             if (do_ang) {
                 float V_;
-                angle_mixed(p, Ef[sp - 1], Ef[sp], Xf[sp], (float)d.ang_t0[c], &a1, &a2, &a3, &V_);
+                angle_mixed(p, Ef[sp - 1], Ef[sp], Xf[sp], d.bond_f[c].y, &a1, &a2, &a3, &V_);
                 if (MODE == 0 && own) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_NAT_ANG], (double)V_);
             }
             if (do_dih) {
                 float Vc, Vs;
                 const float X = (float)dot(Xd[sp], Xd[sp + 1]), T = (float)dot(Xd[sp], Ed[sp + 1]);
-                dihedral_mixed(p, Ef[sp - 1], Ef[sp], Ef[sp + 1], Xf[sp], Xf[sp + 1], X, T, (float)d.dih_p0[c],
+                dihedral_mixed(p, Ef[sp - 1], Ef[sp], Ef[sp + 1], Xf[sp], Xf[sp + 1], X, T, d.bond_f[c].z,
                                p.on[XMD_TERM_CND] != 0, p.on[XMD_TERM_SND] != 0, q, &Vc, &Vs);
                 if (MODE == 0 && own) {
                     if (p.on[XMD_TERM_CND]) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_CND], (double)Vc);
@@ -227,7 +231,7 @@ __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
 
     const double4_32a pi = P[t + 3];
     const BoxD bx = d.rep[r].box;
-    const bool per = bx.cell_inv[0] != 0.0 || bx.cell_inv[1] != 0.0 || bx.cell_inv[2] != 0.0;
+    const bool per = (d.rep[r].per[0] | d.rep[r].per[1] | d.rep[r].per[2]) != 0;
     double vgo = 0, vpa = 0, ves = 0;
 
     if (p.on[XMD_TERM_GO]) {
@@ -236,7 +240,10 @@ __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
             if (!d.nat_on[k]) continue;
             int j = d.nat_j[k];
             FT V_;
-            V3<FT> f = go_pair<FT>(p, r_uv_p<FT>(bx, per, pi, pin[j]), (FT)d.nat_d[k], &V_);
+            FT nd;
+            if constexpr (sizeof(FT) == 4) nd = d.nat_df[k];
+            else nd = d.nat_d[k];
+            V3<FT> f = go_pair<FT>(p, r_uv_p<FT>(bx, per, pi, pin[j]), nd, &V_);
             add3(fx, fy, fz, f);
             if (MODE == 0 && i < j) vgo += (double)V_;
         }
@@ -303,7 +310,7 @@ __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
         }
     }
 
-    if (!(isfinite(fx) && isfinite(fy) && isfinite(fz))) atomicOr(d.status, ST_NONFINITE);
+    if (!(finite_bits(fx) && finite_bits(fy) && finite_bits(fz))) atomicOr(d.status, ST_NONFINITE);
 
     if (MODE == 0) {
         d.F[3 * i] = fx;
@@ -365,9 +372,11 @@ __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
         // mixed path: the FP64 displacement narrowed, squared in FP32
         const double4_32a o = d.orig[i];
         float ex = (float)(pn.x - o.x), ey = (float)(pn.y - o.y), ez = (float)(pn.z - o.z);
-        ex -= (float)bx.cell[0] * rintf(ex * (float)bx.cell_inv[0]);
-        ey -= (float)bx.cell[1] * rintf(ey * (float)bx.cell_inv[1]);
-        ez -= (float)bx.cell[2] * rintf(ez * (float)bx.cell_inv[2]);
+        if (per) {
+            ex -= (float)bx.cell[0] * rintf(ex * (float)bx.cell_inv[0]);
+            ey -= (float)bx.cell[1] * rintf(ey * (float)bx.cell_inv[1]);
+            ez -= (float)bx.cell[2] * rintf(ez * (float)bx.cell_inv[2]);
+        }
         disp = (double)(ex * ex + ey * ey + ez * ez);
     } else {
         // on open axes the wrap subtracts exactly zero: skipping it changes no bit
@@ -386,7 +395,8 @@ __global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur) {
 
 // ---- skin decision (nl::verify, verify.cpp:4-23) --------------------------------
 // setc: also set the conditional handle of the graph's rebuild IF node
-__global__ void k_nl_check(Dev d, int advance, double dt, cudaGraphConditionalHandle h, int setc) {
+__device__ __forceinline__ void nl_check_block(const Dev &d, int advance, double dt, cudaGraphConditionalHandle h,
+                                               int setc) {
     __shared__ int any_s;
     if (threadIdx.x == 0) any_s = 0;
     __syncthreads();
@@ -414,6 +424,32 @@ __global__ void k_nl_check(Dev d, int advance, double dt, cudaGraphConditionalHa
     if (threadIdx.x == 0) {
         *d.any_rebuild = any_s;
         if (setc) cudaGraphSetConditional(h, any_s ? 1u : 0u);
+    }
+}
+__global__ void k_nl_check(Dev d, int advance, double dt, cudaGraphConditionalHandle h, int setc) {
+    nl_check_block(d, advance, dt, h, setc);
+}
+
+// The step kernel.  With `fuse` (graph steps without the quasi-adiabatic
+// term) the last block to finish also takes the skin decision of every
+// replica and sets the graph's rebuild condition, so a step is one launch
+// plus the conditional rebuild.
+template <class FT, int MODE>
+__global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur, cudaGraphConditionalHandle h, int fuse) {
+    __shared__ int last_s;
+    if (d.blk_on[blockIdx.x]) force_block<FT, MODE>(d, p, cur);   // uniform per block
+    if (MODE == 1 && fuse) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            last_s = atomicAdd(&d.ctr[2], 1ull) == (unsigned long long)(gridDim.x - 1);
+        }
+        __syncthreads();
+        if (last_s) {
+            __threadfence();
+            nl_check_block(d, 1, p.dt, h, 1);
+            if (threadIdx.x == 0) d.ctr[2] = 0ull;
+        }
     }
 }
 
@@ -1226,10 +1262,12 @@ void Engine::allocate() {
     d.teth_r0 = (double *)dalloc(sizeof(double) * N);
     d.ang_t0 = (double *)dalloc(sizeof(double) * N);
     d.dih_p0 = (double *)dalloc(sizeof(double) * N);
+    d.bond_f = (float4 *)dalloc(sizeof(float4) * N);
     d.nat_start = (int32_t *)dalloc(sizeof(int32_t) * N);
     d.nat_end = (int32_t *)dalloc(sizeof(int32_t) * N);
     d.nat_j = (int32_t *)dalloc(sizeof(int32_t) * NN);
     d.nat_d = (double *)dalloc(sizeof(double) * NN);
+    d.nat_df = (float *)dalloc(sizeof(float) * NN);
     d.nat_on = (uint8_t *)dalloc(NN);
     d.nl_row = (int32_t *)dalloc(sizeof(int32_t) * (size_t)nl_cap * N);
     d.nl_cnt = (int32_t *)dalloc(sizeof(int32_t) * N);
@@ -1294,6 +1332,9 @@ void Engine::allocate() {
     tp.lj_bb_r_min = p.lj_bb_r_min; tp.lj_bb_depth = p.lj_bb_depth;
     tp.lj_bs_r_min = p.lj_bs_r_min; tp.lj_bs_depth = p.lj_bs_depth;
     tp.ss_sinking = p.ss_sinking;
+    tp.f = TermP::F32{(float)tp.tether_H1, (float)tp.tether_H2, (float)tp.nat_ang_k, (float)tp.cnd_CDA,
+                      (float)tp.cnd_CDB, (float)tp.snd_CDH, (float)tp.go_depth, (float)tp.pauli_r_excl,
+                      (float)tp.pauli_depth, (float)tp.es_Vf, (float)tp.es_sdi};
     if (p.on[XMD_TERM_QA]) {
         // quasi-adiabatic state (tables of main.cpp:681-700, lj_variants.cpp:59-62)
         d.qa_on = 1;
@@ -1455,10 +1496,15 @@ void Engine::place(int k) {
     up(d.teth_r0 + b, tr.data(), sizeof(double) * n);
     up(d.ang_t0 + b, ar.data(), sizeof(double) * n);
     up(d.dih_p0 + b, dr.data(), sizeof(double) * n);
+    std::vector<float4> bf(n);
+    for (int i = 0; i < n; ++i) bf[i] = make_float4((float)tr[i], (float)ar[i], (float)dr[i], 0.0f);
+    up(d.bond_f + b, bf.data(), sizeof(float4) * n);
     up(d.nat_start + b, ns.data(), sizeof(int32_t) * n);
     up(d.nat_end + b, ne.data(), sizeof(int32_t) * n);
     up(d.nat_j + no, nj.data(), sizeof(int32_t) * nj.size());
     up(d.nat_d + no, nd.data(), sizeof(double) * nd.size());
+    std::vector<float> ndf(nd.begin(), nd.end());
+    up(d.nat_df + no, ndf.data(), sizeof(float) * ndf.size());
     CK(cudaMemsetAsync(d.nat_on + no, 0, nnat, stream));
     CK(cudaMemsetAsync(d.nl_cnt + b, 0, sizeof(int32_t) * n, stream));
     std::vector<int2> ch(nchunk);
@@ -1718,8 +1764,9 @@ void Engine::ensure_nl() {
 void Engine::launch_force_step() {
     int nb = (d.N + FB - 1) / FB;
     if (timing) record(ev_force, n_ev_force);
-    if (params.precision == XMD_PREC_MIXED) k_force<float, 1><<<nb, FB, 0, stream>>>(d, tp, cur);
-    else k_force<double, 1><<<nb, FB, 0, stream>>>(d, tp, cur);
+    const cudaGraphConditionalHandle none = 0;
+    if (params.precision == XMD_PREC_MIXED) k_force<float, 1><<<nb, FB, 0, stream>>>(d, tp, cur, none, 0);
+    else k_force<double, 1><<<nb, FB, 0, stream>>>(d, tp, cur, none, 0);
     if (timing) record(ev_force, n_ev_force);
     ++launches;
     if (d.qa_on) {
@@ -1743,11 +1790,18 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
     const int nb = (d.N + FB - 1) / FB;
     void *fk = params.precision == XMD_PREC_MIXED ? (void *)k_force<float, 1> : (void *)k_force<double, 1>;
     double dt = params.dt;
+    // without the quasi-adiabatic term the step kernel takes the skin
+    // decision itself (its last block), so a step is one kernel node
+    const int fuse = d.qa_on ? 0 : 1;
     for (int s = 0; s < GRAPH_STEPS; ++s) {
         int c = start_cur ^ (s & 1), cn = c ^ 1;
         int adv = 1, setc = 1;
+        cudaGraphConditionalHandle h;
+        CK(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
         cudaKernelNodeParams kf{};
-        void *fargs[] = {&d, &tp, &c};
+        cudaGraphConditionalHandle hf = fuse ? h : 0;
+        int ff = fuse;
+        void *fargs[] = {&d, &tp, &c, &hf, &ff};
         kf.func = fk;
         kf.gridDim = dim3(nb);
         kf.blockDim = dim3(FB);
@@ -1770,15 +1824,17 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
             CK(cudaGraphAddKernelNode(&n2, g, &n1, 1, &kq));
             nf = n2;
         }
-        cudaGraphConditionalHandle h;
-        CK(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
-        cudaKernelNodeParams kc{};
-        void *cargs[] = {&d, &adv, &dt, &h, &setc};
-        kc.func = (void *)k_nl_check;
-        kc.gridDim = dim3(1);
-        kc.blockDim = dim3(1024);
-        kc.kernelParams = cargs;
-        CK(cudaGraphAddKernelNode(&nc, g, &nf, 1, &kc));
+        if (fuse) {
+            nc = nf;
+        } else {
+            cudaKernelNodeParams kc{};
+            void *cargs[] = {&d, &adv, &dt, &h, &setc};
+            kc.func = (void *)k_nl_check;
+            kc.gridDim = dim3(1);
+            kc.blockDim = dim3(1024);
+            kc.kernelParams = cargs;
+            CK(cudaGraphAddKernelNode(&nc, g, &nf, 1, &kc));
+        }
         cudaGraphNodeParams cp{};
         cp.type = cudaGraphNodeTypeConditional;
         cp.conditional.handle = h;
@@ -1852,8 +1908,9 @@ void Engine::eval_forces(int rep, double *F, double *V) {
     ensure_nl();
     CK(cudaMemsetAsync(d.Vrep, 0, sizeof(double) * XMD_NUM_TERMS * d.R, stream));
     int nb = (d.N + FB - 1) / FB;
-    if (params.precision == XMD_PREC_MIXED) k_force<float, 0><<<nb, FB, 0, stream>>>(d, tp, cur);
-    else k_force<double, 0><<<nb, FB, 0, stream>>>(d, tp, cur);
+    const cudaGraphConditionalHandle none = 0;
+    if (params.precision == XMD_PREC_MIXED) k_force<float, 0><<<nb, FB, 0, stream>>>(d, tp, cur, none, 0);
+    else k_force<double, 0><<<nb, FB, 0, stream>>>(d, tp, cur, none, 0);
     const RepHost &h = reps[rep];
     if (F) CK(cudaMemcpyAsync(F, d.F + 3 * (size_t)h.begin, sizeof(double) * 3 * h.n, cudaMemcpyDeviceToHost, stream));
     if (V) CK(cudaMemcpyAsync(V, d.Vrep + (size_t)rep * XMD_NUM_TERMS, sizeof(double) * XMD_NUM_TERMS,
@@ -1871,8 +1928,10 @@ void Engine::step(int nsteps) {
     if (!timing && use_graphs) {
         for (; s + GRAPH_STEPS <= nsteps; s += GRAPH_STEPS) {
             CK(cudaGraphLaunch(graph_for(cur), stream));
-            // per step: force, check, and (when taken) two rebuild kernels
-            launches += 2 * GRAPH_STEPS;
+            // per step: the step kernel (plus the separate check and the
+            // quasi-adiabatic kernels with that term); rebuild kernels are
+            // counted per pass in stats()
+            launches += (d.qa_on ? 4 : 1) * GRAPH_STEPS;
             md_steps += GRAPH_STEPS;
         }
     }

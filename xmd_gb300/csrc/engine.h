@@ -84,8 +84,10 @@ struct Dev {
     int32_t *chain, *seq;
     uint8_t *atype;
     double *teth_r0, *ang_t0, *dih_p0;
+    float4 *bond_f;         // (r0, theta0, phi0) in FP32 for the mixed path
     int32_t *nat_start, *nat_end, *nat_j;   // natives of bead i: [nat_start[i], nat_end[i])
     double *nat_d;
+    float *nat_df;          // nat_d in FP32 for the mixed path
     uint8_t *nat_on;
     int32_t *nl_row, *nl_cnt;
     int32_t *cell_cnt, *cell_start, *cell_fill, *cell_items, *bead_cell;

@@ -25,6 +25,17 @@ struct TermP {
     double qa_cycle, qa_cycle_inv, qa_factor;
     double lj_bb_r_min, lj_bb_depth, lj_bs_r_min, lj_bs_depth;
     int ss_sinking;
+    // FP32 copies of the constants the mixed path's FP32 terms use (no
+    // FP64-to-FP32 conversion per interaction)
+    struct F32 {
+        float tether_H1, tether_H2, nat_ang_k, cnd_CDA, cnd_CDB, snd_CDH, go_depth;
+        float pauli_r_excl, pauli_depth, es_Vf, es_sdi;
+    } f;
 };
+
+// the constant in the interaction's arithmetic type
+template <class T> __host__ __device__ __forceinline__ T tpar(double d, float f);
+template <> __host__ __device__ __forceinline__ double tpar<double>(double d, float) { return d; }
+template <> __host__ __device__ __forceinline__ float tpar<float>(double, float f) { return f; }
 
 }  // namespace xmdg
