@@ -360,23 +360,6 @@ __device__ __forceinline__ void noise3(uint64_t st, double *nx, double *ny, doub
     if (isnan(r2)) r2 = 0.0;
     *nz = r2 * cos((2.0 * 3.141592653589793) * u4);
 }
-// The same draws in FP32, as the reference's float build takes them
-__device__ __forceinline__ void noise3f(uint64_t st, double *nx, double *ny, double *nz) {
-    const float inv = 1.0f / 4294967296.0f;
-    float u1 = (float)(rng_next(st) >> 32) * inv;
-    float u2 = (float)(rng_next(st) >> 32) * inv;
-    float u3 = (float)(rng_next(st) >> 32) * inv;
-    float u4 = (float)(rng_next(st) >> 32) * inv;
-    float r = sqrtf(-2.0f * logf(u1));
-    if (isnan(r)) r = 0.0f;
-    float s, c;
-    sincosf((float)(2.0 * 3.141592653589793) * u2, &s, &c);
-    *nx = r * c;
-    *ny = r * s;
-    float r2 = sqrtf(-2.0f * logf(u3));
-    if (isnan(r2)) r2 = 0.0f;
-    *nz = r2 * cosf((float)(2.0 * 3.141592653589793) * u4);
-}
 // The same product from 16 nibble tables of 16 entries (entry [q][v] = XOR of
 // the columns 4q..4q+3 selected by the bits of v): 16 lookups instead of 64
 constexpr int JUMP_WORDS = 256;
@@ -385,6 +368,28 @@ __device__ __forceinline__ uint64_t gf2_apply_nib(const uint64_t *__restrict__ t
 #pragma unroll
     for (int q = 0; q < 16; ++q) y ^= __ldg(tab + 16 * q + (int)((x >> (4 * q)) & 15ull));
     return y;
+}
+// Mixed-path noise: the same four draws per bead, turned into three
+// normals without the conversion pipe (which runs at a fraction of the FP64
+// rate on GB300).  A uniform in (0, 1) is built from the top 23 bits of a draw
+// as a float in [1, 2) minus (1 - 2^-24), which is exact (Sterbenz) and never
+// 0 or 1; Box-Muller then uses the hardware log and sine/cosine on
+// t - pi in [-pi, pi), whose sine and cosine are those of t negated - the
+// same distribution.
+__device__ __forceinline__ float u01_bits(uint64_t v) {
+    return __uint_as_float(0x3f800000u | (unsigned)(v >> 41)) - __uint_as_float(0x3f7fffffu);
+}
+__device__ __forceinline__ void noise3m(uint64_t st, float *nx, float *ny, float *nz) {
+    const float u1 = u01_bits(rng_next(st)), u2 = u01_bits(rng_next(st));
+    const float u3 = u01_bits(rng_next(st)), u4 = u01_bits(rng_next(st));
+    const float two_pi = 6.283185307179586f;
+    const float r = sqrtf(-2.0f * __logf(u1));
+    float s, c;
+    __sincosf(two_pi * u2 - 3.141592653589793f, &s, &c);
+    *nx = r * c;
+    *ny = r * s;
+    const float r2 = sqrtf(-2.0f * __logf(u3));
+    *nz = r2 * __cosf(two_pi * u4 - 3.141592653589793f);
 }
 // 64x64 GF(2) matrix (columns) times state: the xorshift jump-ahead
 __device__ __forceinline__ uint64_t gf2_apply(const uint64_t *__restrict__ col, uint64_t x) {

@@ -327,8 +327,15 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
     // ---- lang_pc_step::operator(), lang_pc.cpp:11-37, mass = 1 (main.cpp:156) ----
     uint64_t st = d.rng[i];
     double nz[3];
-    if (sizeof(FT) == 8) noise3(st, &nz[0], &nz[1], &nz[2]);
-    else noise3f(st, &nz[0], &nz[1], &nz[2]);
+    if constexpr (sizeof(FT) == 8) {
+        noise3(st, &nz[0], &nz[1], &nz[2]);
+    } else {
+        float a, b, c;
+        noise3m(st, &a, &b, &c);
+        nz[0] = a;
+        nz[1] = b;
+        nz[2] = c;
+    }
     d.rng[i] = gf2_apply_nib(d.jump + JUMP_WORDS * r, st);
     const double dt_inv = p.dt_inv, h = p.dt2_half;
     const double gamma = p.gamma_factor * 1.0;
@@ -612,6 +619,15 @@ __global__ void __launch_bounds__(CB) k_cells(Dev d, int cur) {
 }
 
 // ---- Verlet rows (legacy_update.cpp:16-62 + the update_* filters) ---------------
+// Minimum image of a difference of coordinates wrapped into [0, L) (so
+// |d| < L) by compare and select: rintf runs on the slow conversion pipe.
+// L = 0 (open axis) leaves d unchanged.
+__device__ __forceinline__ float min_image_f(float d, float L) {
+    const float h = 0.5f * L;
+    d = d > h ? d - L : d;
+    return d < -h ? d + L : d;
+}
+
 // FP32 decision band around a distance threshold T (error bound m)
 struct Band {
     float lo, hi;   // squared FP32 distance: below lo -> inside, above hi -> outside
@@ -677,7 +693,7 @@ __global__ void __launch_bounds__(128) k_nl_build(Dev d, TermP p, int cur) {
             }
     const float mx = rel_coord(rp, 0, pi.x), my = rel_coord(rp, 1, pi.y), mz = rel_coord(rp, 2, pi.z);
     const float Lx = (float)bx.cell[0], Ly = (float)bx.cell[1], Lz = (float)bx.cell[2];
-    const float Lix = (float)bx.cell_inv[0], Liy = (float)bx.cell_inv[1], Liz = (float)bx.cell_inv[2];
+    const bool periodic = (rp.per[0] | rp.per[1] | rp.per[2]) != 0;
     const float pre2 = rp.pre2;
     const double bm = rp.band_m;
     const Band Breq = make_band(rp.req_r, bm);
@@ -700,9 +716,11 @@ __global__ void __launch_bounds__(128) k_nl_build(Dev d, TermP p, int cur) {
                     if (j == i) continue;
                     // FP32 pre-filter (min image on periodic axes)
                     float ddx = f.x - mx, ddy = f.y - my, ddz = f.z - mz;
-                    ddx -= Lx * rintf(ddx * Lix);
-                    ddy -= Ly * rintf(ddy * Liy);
-                    ddz -= Lz * rintf(ddz * Liz);
+                    if (periodic) {
+                        ddx = min_image_f(ddx, Lx);
+                        ddy = min_image_f(ddy, Ly);
+                        ddz = min_image_f(ddz, Lz);
+                    }
                     const float d2 = ddx * ddx + ddy * ddy + ddz * ddz;
                     if (d2 > pre2) continue;
                     int cj = d.chain[j], sj = d.seq[j];
@@ -834,7 +852,7 @@ __global__ void __launch_bounds__(TL_THREADS) k_nl_tile(Dev d, TermP p, int cur)
     const Band Bes = make_band(1.0 / rp.es_min_inv, m);
     const Band Bqa = make_band(1.0 / rp.qa_min_inv, m);
     const float Lx = (float)bx.cell[0], Ly = (float)bx.cell[1], Lz = (float)bx.cell[2];
-    const float Lix = (float)bx.cell_inv[0], Liy = (float)bx.cell_inv[1], Liz = (float)bx.cell_inv[2];
+    const bool periodic = (rp.per[0] | rp.per[1] | rp.per[2]) != 0;
     const double pad = rp.pad;
     const int cap = d.nl_cap;
     const unsigned lt = (1u << lane) - 1u;
@@ -856,9 +874,11 @@ __global__ void __launch_bounds__(TL_THREADS) k_nl_tile(Dev d, TermP p, int cur)
             const int j = d.nat_j[k];
             const float4 qj = sq[j - b];
             float dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
-            dx -= Lx * rintf(dx * Lix);
-            dy -= Ly * rintf(dy * Liy);
-            dz -= Lz * rintf(dz * Liz);
+            if (periodic) {
+                dx = min_image_f(dx, Lx);
+                dy = min_image_f(dy, Ly);
+                dz = min_image_f(dz, Lz);
+            }
             const float d2 = dx * dx + dy * dy + dz * dz;
             const double T = __dadd_rn(2.0 * d.nat_d[k], pad);
             const Band B = make_band(T, m);
@@ -878,9 +898,11 @@ __global__ void __launch_bounds__(TL_THREADS) k_nl_tile(Dev d, TermP p, int cur)
             if (lj < n && lj != li) {
                 const float4 qj = sq[lj];
                 float dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
-                dx -= Lx * rintf(dx * Lix);
-                dy -= Ly * rintf(dy * Liy);
-                dz -= Lz * rintf(dz * Liz);
+                if (periodic) {
+                    dx = min_image_f(dx, Lx);
+                    dy = min_image_f(dy, Ly);
+                    dz = min_image_f(dz, Lz);
+                }
                 const float d2 = dx * dx + dy * dy + dz * dz;
                 const int2 cj = scs[lj];
                 const int df = ci.y > cj.y ? ci.y - cj.y : cj.y - ci.y;
