@@ -404,8 +404,8 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
 // setc: also set the conditional handle of the graph's rebuild IF node
 __device__ __forceinline__ void nl_check_block(const Dev &d, int advance, double dt, cudaGraphConditionalHandle h,
                                                int setc) {
-    __shared__ int any_s;
-    if (threadIdx.x == 0) any_s = 0;
+    __shared__ int any_s, nwork_s;
+    if (threadIdx.x == 0) any_s = nwork_s = 0;
     __syncthreads();
     int any = 0;
     for (int r = threadIdx.x; r < d.R; r += blockDim.x) {
@@ -425,11 +425,18 @@ __device__ __forceinline__ void nl_check_block(const Dev &d, int advance, double
         if (advance && rp.steps_left == 0 && !rp.first) rb = 0;   // no further step uses a list
         rp.rebuild = rb;
         any |= rb;
+        // the tile build's work list: every chunk of the flagged replicas
+        // (order is free: each chunk writes its own rows)
+        if (rb && rp.tile) {
+            const int at = atomicAdd(&nwork_s, rp.nchunk);
+            for (int c = 0; c < rp.nchunk; ++c) d.work[at + c] = rp.chunk_off + c;
+        }
     }
     if (any) atomicOr(&any_s, 1);
     __syncthreads();
     if (threadIdx.x == 0) {
         *d.any_rebuild = any_s;
+        *d.nwork = nwork_s;
         if (setc) cudaGraphSetConditional(h, any_s ? 1u : 0u);
     }
 }
@@ -786,7 +793,8 @@ __global__ void __launch_bounds__(128) k_nl_build(Dev d, TermP p, int cur) {
 }
 
 // ---- Verlet build for replicas of at most TILE_MAX beads ---------------------------
-// One block per chunk of TL_CH beads i; the block holds the whole replica in
+// A block takes chunks of TL_CH beads i from the work list of the last skin
+// check (the chunks of every flagged replica); for each it holds the whole replica in
 // shared memory (FP32 coordinates relative to the replica, chain and sequence
 // index) and each warp scans every bead j of the replica for one bead i at a
 // time, lane k taking j = j0 + k.  A pair is decided in FP32 when its FP32
@@ -797,7 +805,7 @@ __global__ void __launch_bounds__(128) k_nl_build(Dev d, TermP p, int cur) {
 // coordinate carries <= ext * 2^-24; the differences, the periodic shift and
 // the squares add a few ulp more), so both paths keep exactly the same pairs.
 // Rows come out ordered by j (ballot compaction in lane order).
-constexpr int TL_CH = 128;
+constexpr int TL_CH = 16;      // rows per chunk: two per warp
 constexpr int TL_THREADS = 256;
 constexpr int TL_WARPS = TL_THREADS / 32;
 constexpr int TILE_MAX = 4096;
@@ -809,9 +817,7 @@ __device__ __forceinline__ float tl_rel(const RepDev &rp, int a, double x, doubl
 
 
 
-__global__ void __launch_bounds__(TL_THREADS) k_nl_tile(Dev d, TermP p, int cur) {
-    if (blockIdx.x == 0 && threadIdx.x == 0 && !d.any_cell) atomicAdd(d.ctr, 1ull);
-    const int2 chk = d.chunks[blockIdx.x];
+__device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, const int2 chk) {
     const int r = chk.x;
     if (r < 0) return;   // free chunk slot
     RepDev &rp = d.rep[r];
@@ -970,6 +976,15 @@ __global__ void __launch_bounds__(TL_THREADS) k_nl_tile(Dev d, TermP p, int cur)
                 d.qa.tmp_cnt[i] = min(tcnt, QA_TMP_CAP);
             }
         }
+    }
+}
+
+__global__ void __launch_bounds__(TL_THREADS) k_nl_tile(Dev d, TermP p, int cur) {
+    if (blockIdx.x == 0 && threadIdx.x == 0 && !d.any_cell) atomicAdd(d.ctr, 1ull);
+    const int nw = *d.nwork;
+    for (int w = blockIdx.x; w < nw; w += gridDim.x) {
+        tl_chunk(d, p, cur, d.chunks[d.work[w]]);
+        __syncthreads();   // the next chunk overwrites the shared tile
     }
 }
 
@@ -1307,6 +1322,9 @@ void Engine::allocate() {
     d.ctr = (unsigned long long *)dalloc(sizeof(unsigned long long) * 4);
     d.nchunks = std::max(1, cap.chunks);
     d.chunks = (int2 *)dalloc(sizeof(int2) * d.nchunks);
+    d.work = (int *)dalloc(sizeof(int) * d.nchunks);
+    d.nwork = (int *)dalloc(sizeof(int));
+    CK(cudaMemsetAsync(d.nwork, 0, sizeof(int), stream));
     CK(cudaMemsetAsync(d.chunks, 0xff, sizeof(int2) * d.nchunks, stream));
     d.blk_on = (uint8_t *)dalloc((N + FB - 1) / FB);
     owner_h.assign(N, -1);
@@ -1325,6 +1343,14 @@ void Engine::allocate() {
     if (dynamic) tile_smem = (sizeof(float4) + sizeof(int2)) * (size_t)std::min(TILE_MAX, cap.beads);
     if (tile_smem > 48 * 1024)
         CK(cudaFuncSetAttribute(k_nl_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem));
+    {
+        // the tile build runs as many blocks as are resident at once; they
+        // take the work list's chunks in turn
+        int sms = 0, per_sm = 0;
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_nl_tile, TL_THREADS, tile_smem));
+        tile_grid = std::max(1, std::min(d.nchunks, sms * std::max(1, per_sm)));
+    }
 
     // term parameters
     std::memset(&tp, 0, sizeof tp);
@@ -1538,6 +1564,8 @@ void Engine::place(int k) {
     rd.cell_off = co;
     rd.cell_budget = ncell;
     rd.tile = tile;
+    rd.chunk_off = tile ? ho : 0;
+    rd.nchunk = nchunk;
     rd.active = 1;
     rd.steps_left = r.steps_left;
     if (qa) {
@@ -1720,7 +1748,7 @@ void Engine::launch_rebuild() {
         k_cells<<<d.R, CB, 0, stream>>>(d, cur);
         k_nl_build<<<(d.N + 127) / 128, 128, 0, stream>>>(d, tp, cur);
     }
-    if (any_tile) k_nl_tile<<<d.nchunks, TL_THREADS, tile_smem, stream>>>(d, tp, cur);
+    if (any_tile) k_nl_tile<<<tile_grid, TL_THREADS, tile_smem, stream>>>(d, tp, cur);
     if (d.qa_on) k_qa_rebuild<<<d.R, 1024, 0, stream>>>(d);
     if (timing) record(ev_rebuild, n_ev_rebuild);
 }
@@ -1898,7 +1926,7 @@ void Engine::add_rebuild_nodes(cudaGraph_t body, int cn) {
     if (any_tile) {
         cudaKernelNodeParams kt{};
         kt.func = (void *)k_nl_tile;
-        kt.gridDim = dim3(d.nchunks);
+        kt.gridDim = dim3(tile_grid);
         kt.blockDim = dim3(TL_THREADS);
         kt.sharedMemBytes = (unsigned)tile_smem;
         kt.kernelParams = a2;

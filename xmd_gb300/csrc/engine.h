@@ -37,6 +37,7 @@ struct RepDev {
     float pre2;              // squared FP32 pre-filter radius of the Verlet build
     double band_m;           // FP32 distance error bound of the cell build
     int first, rebuild;
+    int chunk_off, nchunk;   // tile-build chunks of the replica in Dev::chunks
     int active;              // slot holds a placed replica
     long long steps_left;    // steps this replica still takes (-1: no bound)
     unsigned long long maxdisp;
@@ -100,6 +101,8 @@ struct Dev {
     unsigned long long *ctr;  // [0]: list-rebuild passes launched
     int2 *chunks;           // (replica, first bead) of each tile-build block
     int nchunks;
+    int *work;              // chunks of the replicas flagged at the last skin check
+    int *nwork;             // number of entries in `work`
     int any_cell;           // some replica uses the cell-grid build
     uint8_t *blk_on;        // force blocks (FB beads) holding at least one placed bead
     int qa_on;
@@ -248,6 +251,7 @@ private:
     cudaGraphExec_t graph_for(int start_cur);
     bool any_cell = false, any_tile = false;   // which Verlet builds the replicas use
     size_t tile_smem = 0;                      // dynamic shared memory of k_nl_tile
+    int tile_grid = 1;                         // resident blocks of k_nl_tile over all SMs
     void add_rebuild_nodes(cudaGraph_t body, int cn);
     bool grow_rows(double frac);
     void drop_graphs();
