@@ -51,6 +51,128 @@ template <class T> __device__ __forceinline__ T acos_c(T x) {
 }
 template <class T> __device__ __forceinline__ T ipow6(T s) { return s * (s * (s * (s * (s * s)))); }
 
+// ---- FP32 <-> FP64 on the integer pipe --------------------------------------------
+// On GB300 FP64 arithmetic AND the FP32<->FP64 conversion instructions run at
+// 2 lanes per clock per SM (FP32: 128).  The mixed path therefore keeps FP64
+// instructions out of its per-pair and per-bond work: it moves between the
+// formats with integer operations on the bit patterns, and carries extended
+// precision as pairs of FP32 values (float-float).
+//   narrow_f: round-to-nearest-even, equal to the hardware conversion for
+//             results in the normal FP32 range; smaller magnitudes give a
+//             signed zero (the hardware would give a denormal); overflow gives
+//             infinity and NaN stays NaN.
+//   widen_f:  exact for normal values, zeros and infinities; FP32 denormals
+//             give a signed zero; NaN stays NaN.
+__device__ __forceinline__ float narrow_f(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const int e = (int)((hi >> 20) & 0x7ffu) - 896;   // FP32 biased exponent
+    const unsigned sign = hi & 0x80000000u;
+    const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned rem = lo & 0x1fffffffu;
+    unsigned f = sign | ((unsigned)e << 23) | m;
+    f += (unsigned)(rem > 0x10000000u) | ((unsigned)(rem == 0x10000000u) & (m & 1u));
+    const bool nan = e == 1151 && (m | rem) != 0u;
+    f = e >= 255 ? (sign | 0x7f800000u | (nan ? 0x400000u : 0u)) : f;
+    f = e <= 0 ? sign : f;
+    return __uint_as_float(f);
+}
+__device__ __forceinline__ double widen_f(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned ex = (u >> 23) & 0xffu;
+    const unsigned sign = u & 0x80000000u;
+    const unsigned dex = ex == 0xffu ? 0x7ffu : ex + 896u;
+    unsigned hi = sign | (dex << 20) | ((u & 0x7fffffu) >> 3), lo = u << 29;
+    hi = ex == 0u ? sign : hi;
+    lo = ex == 0u ? 0u : lo;
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+// A double as an unevaluated sum h + l of two floats: h holds the leading 24
+// significant bits (truncated), l the next 24 of the remaining 29 (truncated),
+// so |x - (h + l)| <= 2^-47 |x|.  Integer operations only.  Magnitudes below
+// the FP32 normal range give 0 + 0 (positions there are zero for every purpose
+// of a pair distance); non-finite input gives a non-finite h.
+struct F2 { float h, l; };
+__device__ __forceinline__ F2 split_d(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const int E = (int)((hi >> 20) & 0x7ffu);
+    const int e = E - 896;
+    const unsigned sign = hi & 0x80000000u;
+    const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned rem = lo & 0x1fffffffu;
+    unsigned h = sign | ((unsigned)e << 23) | m;
+    // remainder rem * 2^(E - 1075): leading one at bit p = 31 - clz
+    const int lz = __clz(rem);
+    const int el = (31 - lz) + E - 948;                 // FP32 biased exponent of l
+    const unsigned ml = lz >= 8 ? rem << (lz - 8) : rem >> (8 - lz);
+    unsigned l = sign | ((unsigned)el << 23) | (ml & 0x7fffffu);
+    l = (rem == 0u || el <= 0) ? sign : l;
+    const bool big = e >= 255;
+    h = big ? (sign | 0x7f800000u | ((E == 0x7ff && (m | rem)) ? 0x400000u : 0u)) : h;
+    l = big ? 0u : l;
+    h = e <= 0 ? sign : h;
+    l = e <= 0 ? sign : l;
+    return F2{__uint_as_float(h), __uint_as_float(l)};
+}
+
+// ---- float-float arithmetic (error-free transformations) ---------------------
+// two_sum (Knuth): s + e == a + b exactly.  two_prod: p + e == a * b exactly
+// (one FMA).  FF values are unevaluated sums h + l with |l| <= ulp(h).
+struct FF { float h, l; };
+__device__ __forceinline__ FF two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return FF{s, e};
+}
+__device__ __forceinline__ FF fast_two_sum(float a, float b) {   // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return FF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ FF two_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    return FF{p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+    FF s = two_sum(a.h, b.h);
+    return fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ FF ff_neg(FF a) { return FF{-a.h, -a.l}; }
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+    FF p = two_prod(a.h, b.h);
+    return fast_two_sum(p.h, __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, p.l)));
+}
+// w - u of two split doubles, as float-float (error <= 2^-46 of the larger
+// magnitude of w, u)
+__device__ __forceinline__ FF ff_diff(F2 u, F2 w) {
+    FF s = two_sum(w.h, -u.h);
+    return fast_two_sum(s.h, __fadd_rn(s.l, __fsub_rn(w.l, u.l)));
+}
+// accumulation of FP32 terms into a float-float sum (error per addition
+// <= 2^-47 of the running magnitude)
+__device__ __forceinline__ void ff_acc(FF &acc, float v) {
+    FF s = two_sum(acc.h, v);
+    acc.h = s.h;
+    acc.l = __fadd_rn(acc.l, s.l);
+}
+__device__ __forceinline__ double ff_to_d(FF a) { return widen_f(a.h) + widen_f(a.l); }
+
+__device__ __forceinline__ FF ff_sub(FF a, FF b) { return ff_add(a, ff_neg(b)); }
+// float-float cross and dot products of float-float vectors
+__device__ __forceinline__ V3<FF> ff_cross(const V3<FF> &a, const V3<FF> &b) {
+    return V3<FF>{ff_sub(ff_mul(a.y, b.z), ff_mul(a.z, b.y)), ff_sub(ff_mul(a.z, b.x), ff_mul(a.x, b.z)),
+                  ff_sub(ff_mul(a.x, b.y), ff_mul(a.y, b.x))};
+}
+__device__ __forceinline__ FF ff_dot(const V3<FF> &a, const V3<FF> &b) {
+    return ff_add(ff_add(ff_mul(a.x, b.x), ff_mul(a.y, b.y)), ff_mul(a.z, b.z));
+}
+
+// position of a bead split per axis (mixed path)
+struct P2 { F2 x, y, z; };
+__device__ __forceinline__ P2 split_p(double4_32a p) { return P2{split_d(p.x), split_d(p.y), split_d(p.z)}; }
+
 // FP64 difference, narrowed to FT
 template <class T>
 __device__ __forceinline__ V3<T> diff(double4_32a u, double4_32a w) {
@@ -398,5 +520,77 @@ __device__ __forceinline__ uint64_t gf2_apply(const uint64_t *__restrict__ col, 
     for (int k = 0; k < 64; ++k) y ^= col[k] & (0ull - ((x >> k) & 1ull));
     return y;
 }
+
+// ---- per-bead force accumulation and pair geometry, by path -------------------
+// FP64 path: FP64 sums in the reference's term order; r_uv in FP64.
+// Mixed path: FP32 terms summed per bead in float-float (each addition exact
+// to 2^-47 of the running sum, below the FP32 rounding of the terms by ~10^7)
+// and widened once; pair vectors from split positions in FP32 (the minimum
+// image subtracted in float-float), with no FP64 instruction per pair.
+template <class FT> struct Acc3;
+template <> struct Acc3<double> {
+    double x = 0, y = 0, z = 0;
+    __device__ __forceinline__ void add(V3<double> f) { x += f.x; y += f.y; z += f.z; }
+    __device__ __forceinline__ void sub(V3<double> f) { x += -f.x; y += -f.y; z += -f.z; }
+    __device__ __forceinline__ V3<double> total() const { return V3<double>{x, y, z}; }
+};
+template <> struct Acc3<float> {
+    FF x{0.0f, 0.0f}, y{0.0f, 0.0f}, z{0.0f, 0.0f};
+    __device__ __forceinline__ void add(V3<float> f) { ff_acc(x, f.x); ff_acc(y, f.y); ff_acc(z, f.z); }
+    __device__ __forceinline__ void sub(V3<float> f) { ff_acc(x, -f.x); ff_acc(y, -f.y); ff_acc(z, -f.z); }
+    __device__ __forceinline__ V3<double> total() const { return V3<double>{ff_to_d(x), ff_to_d(y), ff_to_d(z)}; }
+};
+
+// w - u of split coordinates along one axis of length L = Lh + Ll (0 when open)
+__device__ __forceinline__ float mi_axis(F2 u, F2 w, float Lh, float Ll, float Linv, bool per) {
+    if (!per) return __fadd_rn(__fsub_rn(w.h, u.h), __fsub_rn(w.l, u.l));
+    const FF dd = ff_diff(u, w);
+    const float n = rintf(__fmul_rn(dd.h, Linv));
+    const FF q = ff_sub(dd, two_prod(n, Lh));
+    return __fadd_rn(q.h, __fsub_rn(q.l, __fmul_rn(n, Ll)));
+}
+
+// q_i q_j of the Debye-Hueckel pair (es_pair.cpp:17): an FP64 product on the
+// FP64 path; the charges are small integers, so the FP32 product of the
+// narrowed charges is the same value on the mixed path
+template <class FT> __device__ __forceinline__ FT charge_prod(double qi, double qj);
+template <> __device__ __forceinline__ double charge_prod<double>(double qi, double qj) { return qi * qj; }
+template <> __device__ __forceinline__ float charge_prod<float>(double qi, double qj) {
+    return __fmul_rn(narrow_f(qi), narrow_f(qj));
+}
+
+template <class FT> struct PairGeo;
+template <> struct PairGeo<double> {
+    BoxD bx;
+    bool per;
+    double4_32a pi;
+    __device__ __forceinline__ PairGeo(const BoxD &b, bool periodic, double4_32a p) : bx(b), per(periodic), pi(p) {}
+    __device__ __forceinline__ V3<double> to(double4_32a pj) const { return r_uv_p<double>(bx, per, pi, pj); }
+    __device__ __forceinline__ V3<double> between(double4_32a a, double4_32a b) const {
+        return r_uv_p<double>(bx, per, a, b);
+    }
+};
+template <> struct PairGeo<float> {
+    float Lh[3], Ll[3], Li[3];
+    bool per;
+    P2 si;
+    __device__ __forceinline__ PairGeo(const BoxD &b, bool periodic, double4_32a p) : per(periodic), si(split_p(p)) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const F2 L = split_d(b.cell[a]);
+            Lh[a] = L.h;
+            Ll[a] = L.l;
+            Li[a] = narrow_f(b.cell_inv[a]);
+        }
+    }
+    __device__ __forceinline__ V3<float> diff2(const P2 &u, const P2 &w) const {
+        return V3<float>{mi_axis(u.x, w.x, Lh[0], Ll[0], Li[0], per), mi_axis(u.y, w.y, Lh[1], Ll[1], Li[1], per),
+                         mi_axis(u.z, w.z, Lh[2], Ll[2], Li[2], per)};
+    }
+    __device__ __forceinline__ V3<float> to(double4_32a pj) const { return diff2(si, split_p(pj)); }
+    __device__ __forceinline__ V3<float> between(double4_32a a, double4_32a b) const {
+        return diff2(split_p(a), split_p(b));
+    }
+};
 
 }  // namespace xmdg

@@ -88,8 +88,13 @@ static GF2 gf2_jump(uint64_t draws) {
 uint64_t rng_jump(uint64_t state, uint64_t n_draws) { return gf2_apply_h(gf2_jump(n_draws), state); }
 
 // ---- device helpers -----------------------------------------------------------
-__device__ __forceinline__ double warp_max(double v) {
-    for (int o = 16; o; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+// maximum over the warp of non-negative doubles, compared as their bit
+// patterns (the same order) on the integer pipe
+__device__ __forceinline__ unsigned long long warp_max_bits(unsigned long long v) {
+    for (int o = 16; o; o >>= 1) {
+        const unsigned long long u = __shfl_xor_sync(0xffffffffu, v, o);
+        v = u > v ? u : v;
+    }
     return v;
 }
 
@@ -116,29 +121,34 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
     const int N = d.N, t = threadIdx.x, i0 = blockIdx.x * FB;
     __shared__ double4_32a P[FB + 6];
     __shared__ V3<FT> Ct[FB + 3], Ca[3][FB + 3], Cd[4][FB + 3];
-    // mixed path: bond vectors e_k = P[k+1] - P[k] and cross products
-    // x_k = e_{k-1} x e_k, formed once per tile slot in FP64 and shared by the
-    // tether, angle and dihedral centres that use them
+    // mixed path: every position of the tile split into float-float parts
+    // (integer operations); bond vectors e_k = P[k+1] - P[k] and cross
+    // products x_k = e_{k-1} x e_k formed once per tile slot in float-float
+    // arithmetic (~2^-44 relative, FP64-class where the FP32 forms lose
+    // everything: nearly straight triples) and shared by the tether, angle and
+    // dihedral centres that use them
     constexpr int NE = sizeof(FT) == 4 ? FB + 5 : 1;
-    __shared__ V3<double> Ed[NE], Xd[NE];
+    __shared__ P2 S[sizeof(FT) == 4 ? FB + 6 : 1];
+    __shared__ V3<FF> Eff[NE], Xff[NE];
     __shared__ V3<float> Ef[NE], Xf[NE];
 
     for (int k = t; k < FB + 6; k += FB) {
         int idx = i0 - 3 + k;
         P[k] = (idx >= 0 && idx < N) ? pin[idx] : make_double4_32a(0, 0, 0, 0);
+        if constexpr (sizeof(FT) == 4) S[k] = split_p(P[k]);
     }
     __syncthreads();
     if constexpr (sizeof(FT) == 4) {
         for (int k = t; k < NE; k += FB) {
-            V3<double> e = dsub(P[k], P[k + 1]);
-            Ed[k] = e;
-            Ef[k] = f3(e);
+            const V3<FF> e{ff_diff(S[k].x, S[k + 1].x), ff_diff(S[k].y, S[k + 1].y), ff_diff(S[k].z, S[k + 1].z)};
+            Eff[k] = e;
+            Ef[k] = V3<float>{e.x.h, e.y.h, e.z.h};
         }
         __syncthreads();
         for (int k = t + 1; k < NE; k += FB) {
-            V3<double> x = cross(Ed[k - 1], Ed[k]);
-            Xd[k] = x;
-            Xf[k] = f3(x);
+            const V3<FF> x = ff_cross(Eff[k - 1], Eff[k]);
+            Xff[k] = x;
+            Xf[k] = V3<float>{x.x.h, x.y.h, x.z.h};
         }
         __syncthreads();
     }
@@ -185,7 +195,7 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
             }
             if (do_dih) {
                 float Vc, Vs;
-                const float X = (float)dot(Xd[sp], Xd[sp + 1]), T = (float)dot(Xd[sp], Ed[sp + 1]);
+                const float X = dot(Xf[sp], Xf[sp + 1]), T = ff_dot(Xff[sp], Eff[sp + 1]).h;
                 dihedral_mixed(p, Ef[sp - 1], Ef[sp], Ef[sp + 1], Xf[sp], Xf[sp + 1], X, T, d.bond_f[c].z,
                                p.on[XMD_TERM_CND] != 0, p.on[XMD_TERM_SND] != 0, q, &Vc, &Vs);
                 if (MODE == 0 && own) {
@@ -210,28 +220,29 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
         return;
     }
     const int s = t + 2;   // centre slot of bead i
-    double fx = 0, fy = 0, fz = 0;
+    Acc3<FT> acc;
     if constexpr (sizeof(FT) == 4) {
         // the bonded contributions, computed in FP32, are summed in FP32 and
-        // enter the FP64 accumulator once
+        // enter the float-float accumulator once
         V3<float> bsum = Ct[s] - Ct[s - 1] + Ca[2][s - 1] + Ca[1][s] + Ca[0][s + 1] + Cd[0][s + 1] + Cd[1][s] +
                          Cd[2][s - 1] + Cd[3][s - 2];
-        add3(fx, fy, fz, bsum);
+        acc.add(bsum);
     } else {
-        add3(fx, fy, fz, Ct[s]);
-        add3(fx, fy, fz, -Ct[s - 1]);
-        add3(fx, fy, fz, Ca[2][s - 1]);
-        add3(fx, fy, fz, Ca[1][s]);
-        add3(fx, fy, fz, Ca[0][s + 1]);
-        add3(fx, fy, fz, Cd[0][s + 1]);
-        add3(fx, fy, fz, Cd[1][s]);
-        add3(fx, fy, fz, Cd[2][s - 1]);
-        add3(fx, fy, fz, Cd[3][s - 2]);
+        acc.add(Ct[s]);
+        acc.sub(Ct[s - 1]);
+        acc.add(Ca[2][s - 1]);
+        acc.add(Ca[1][s]);
+        acc.add(Ca[0][s + 1]);
+        acc.add(Cd[0][s + 1]);
+        acc.add(Cd[1][s]);
+        acc.add(Cd[2][s - 1]);
+        acc.add(Cd[3][s - 2]);
     }
 
     const double4_32a pi = P[t + 3];
     const BoxD bx = d.rep[r].box;
     const bool per = (d.rep[r].per[0] | d.rep[r].per[1] | d.rep[r].per[2]) != 0;
+    const PairGeo<FT> geo(bx, per, pi);
     double vgo = 0, vpa = 0, ves = 0;
 
     if (p.on[XMD_TERM_GO]) {
@@ -243,8 +254,8 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
             FT nd;
             if constexpr (sizeof(FT) == 4) nd = d.nat_df[k];
             else nd = d.nat_d[k];
-            V3<FT> f = go_pair<FT>(p, r_uv_p<FT>(bx, per, pi, pin[j]), nd, &V_);
-            add3(fx, fy, fz, f);
+            V3<FT> f = go_pair<FT>(p, geo.to(pin[j]), nd, &V_);
+            acc.add(f);
             if (MODE == 0 && i < j) vgo += (double)V_;
         }
     }
@@ -253,17 +264,17 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
         int e = d.nl_row[(size_t)k * N + i];
         int j = e & NL_MASK;
         double4_32a pj = pin[j];
-        V3<FT> r12 = r_uv_p<FT>(bx, per, pi, pj);
+        V3<FT> r12 = geo.to(pj);
         if (e & NL_PAULI) {
             FT V_;
             V3<FT> f = pauli_pair<FT>(p, r12, &V_);
-            add3(fx, fy, fz, f);
+            acc.add(f);
             if (MODE == 0 && i < j) vpa += (double)V_;
         }
         if (e & NL_ES) {
             FT V_;
-            V3<FT> f = es_pair<FT>(p, r12, (FT)(pi.w * pj.w), &V_);
-            add3(fx, fy, fz, f);
+            V3<FT> f = es_pair<FT>(p, r12, charge_prod<FT>(pi.w, pj.w), &V_);
+            acc.add(f);
             if (MODE == 0 && i < j) ves += (double)V_;
         }
     }
@@ -285,7 +296,7 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
         for (int k = 0; k < nref; ++k) {
             int slot = sl[k];
             int i1 = q.ct_i1[slot], i2 = q.ct_i2[slot];
-            V3<FT> r12 = r_uv_p<FT>(bx, per, pin[i1], pin[i2]);
+            V3<FT> r12 = geo.between(pin[i1], pin[i2]);
             FT r12_rn = ninv(r12);
             V3<FT> u = r12_rn * r12;
             double sat = fmin(tnow - q.ct_ref[slot], p.qa_cycle) * p.qa_cycle_inv;
@@ -295,8 +306,8 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
             FT V_, dV_;
             sink_lj_eval<FT>((FT)depth, (FT)rmin, (FT)rmax, r12_rn * nsq(r12), r12_rn, &V_, &dV_);
             V3<FT> f = ((FT)sat * dV_) * u;
-            if (i == i1) add3(fx, fy, fz, f);
-            else add3(fx, fy, fz, -f);
+            if (i == i1) acc.add(f);
+            else acc.sub(f);
             if (MODE == 0 && i == i1) vqa += sat * (double)V_;
         }
         if (MODE == 1) {
@@ -310,6 +321,8 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
         }
     }
 
+    const V3<double> ftot = acc.total();
+    const double fx = ftot.x, fy = ftot.y, fz = ftot.z;
     if (!(finite_bits(fx) && finite_bits(fy) && finite_bits(fz))) atomicOr(d.status, ST_NONFINITE);
 
     if (MODE == 0) {
@@ -332,9 +345,9 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
     } else {
         float a, b, c;
         noise3m(st, &a, &b, &c);
-        nz[0] = a;
-        nz[1] = b;
-        nz[2] = c;
+        nz[0] = widen_f(a);
+        nz[1] = widen_f(b);
+        nz[2] = widen_f(c);
     }
     d.rng[i] = gf2_apply_nib(d.jump + JUMP_WORDS * r, st);
     const double dt_inv = p.dt_inv, h = p.dt2_half;
@@ -376,15 +389,10 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
     // monotone and correctly rounded, so that equals the max of the norms)
     double disp;
     if constexpr (sizeof(FT) == 4) {
-        // mixed path: the FP64 displacement narrowed, squared in FP32
-        const double4_32a o = d.orig[i];
-        float ex = (float)(pn.x - o.x), ey = (float)(pn.y - o.y), ez = (float)(pn.z - o.z);
-        if (per) {
-            ex -= (float)bx.cell[0] * rintf(ex * (float)bx.cell_inv[0]);
-            ey -= (float)bx.cell[1] * rintf(ey * (float)bx.cell_inv[1]);
-            ez -= (float)bx.cell[2] * rintf(ez * (float)bx.cell_inv[2]);
-        }
-        disp = (double)(ex * ex + ey * ey + ez * ez);
+        // mixed path: the displacement from split positions (the FP64
+        // difference to FP32 accuracy), squared in FP32
+        const V3<float> e = geo.between(d.orig[i], pn);
+        disp = widen_f(e.x * e.x + e.y * e.y + e.z * e.z);
     } else {
         // on open axes the wrap subtracts exactly zero: skipping it changes no bit
         disp = per ? dist2_exact(bx, pn, d.orig[i]) : dist2_open(pn, d.orig[i]);
@@ -393,8 +401,8 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
     int r0 = __shfl_sync(0xffffffffu & __activemask(), r, 0);
     unsigned mask = __activemask();
     if (__all_sync(mask, r == r0) && mask == 0xffffffffu) {
-        double m = warp_max(disp);
-        if (lane == 0) atomicMax(&d.rep[r].maxdisp, (unsigned long long)__double_as_longlong(m));
+        const unsigned long long m = warp_max_bits((unsigned long long)__double_as_longlong(disp));
+        if (lane == 0) atomicMax(&d.rep[r].maxdisp, m);
     } else {
         atomicMax(&d.rep[r].maxdisp, (unsigned long long)__double_as_longlong(disp));
     }
@@ -810,6 +818,13 @@ constexpr int TL_THREADS = 256;
 constexpr int TL_WARPS = TL_THREADS / 32;
 constexpr int TILE_MAX = 4096;
 
+// dynamic shared memory of a tile block for a replica of n beads: the box of
+// each group of 32 consecutive beads (lo, hi), then the FP32 coordinates, then
+// chain and sequence indices
+__host__ __device__ constexpr size_t tile_bytes(int n) {
+    return 2 * sizeof(float4) * (size_t)((n + 31) / 32) + (sizeof(float4) + sizeof(int2)) * (size_t)n;
+}
+
 __device__ __forceinline__ float tl_rel(const RepDev &rp, int a, double x, double ref) {
     if (rp.per[a]) return (float)(x - rp.box.cell[a] * floor(x * rp.box.cell_inv[a]));
     return (float)(x - ref);
@@ -824,7 +839,9 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
     if (!rp.active || !rp.rebuild || !rp.tile) return;
     extern __shared__ float4 tl_smem[];
     const int b = rp.begin, n = rp.n;
-    float4 *sq = tl_smem;
+    const int ng = (n + 31) / 32;
+    float4 *gbox = tl_smem;
+    float4 *sq = gbox + 2 * ng;
     int2 *scs = (int2 *)(sq + n);
     __shared__ float ext_s[TL_WARPS];
     const double4_32a *pos = d.pos[cur];
@@ -845,23 +862,51 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
     __syncthreads();
     ext = 0.0f;
     for (int q = 0; q < TL_WARPS; ++q) ext = fmaxf(ext, ext_s[q]);
-    double exd = (double)ext;
-    for (int a = 0; a < 3; ++a) exd = fmax(exd, bx.cell[a]);
-    const double m = 1e-3 + 4e-7 * exd;
+    // bounding box of each group of 32 beads j (one warp per group)
+    for (int g = w; g < ng; g += TL_WARPS) {
+        const float4 q = sq[min(g * 32 + lane, n - 1)];
+        float lx = q.x, ly = q.y, lz = q.z, hx = q.x, hy = q.y, hz = q.z;
+        for (int o = 16; o; o >>= 1) {
+            lx = fminf(lx, __shfl_xor_sync(0xffffffffu, lx, o));
+            ly = fminf(ly, __shfl_xor_sync(0xffffffffu, ly, o));
+            lz = fminf(lz, __shfl_xor_sync(0xffffffffu, lz, o));
+            hx = fmaxf(hx, __shfl_xor_sync(0xffffffffu, hx, o));
+            hy = fmaxf(hy, __shfl_xor_sync(0xffffffffu, hy, o));
+            hz = fmaxf(hz, __shfl_xor_sync(0xffffffffu, hz, o));
+        }
+        if (lane == 0) {
+            gbox[2 * g] = make_float4(lx, ly, lz, 0.0f);
+            gbox[2 * g + 1] = make_float4(hx, hy, hz, 0.0f);
+        }
+    }
+    __syncthreads();
+    // decision bands of the chunk, formed once (FP64 work off the scan)
+    __shared__ Band bands_s[4];
+    __shared__ float mf_s;
+    if (t == 0) {
+        double exd = (double)ext;
+        for (int a = 0; a < 3; ++a) exd = fmax(exd, bx.cell[a]);
+        const double m = 1e-3 + 4e-7 * exd;
+        bands_s[0] = make_band(rp.req_r, m);
+        bands_s[1] = make_band(1.0 / rp.pauli_min_inv, m);
+        bands_s[2] = make_band(1.0 / rp.es_min_inv, m);
+        bands_s[3] = make_band(1.0 / rp.qa_min_inv, m);
+        mf_s = __double2float_ru(m);
+    }
+    __syncthreads();
+    const float mf = mf_s;
 
     const bool pauli_on = p.on[XMD_TERM_PAULI] != 0;
     const bool go_on = p.on[XMD_TERM_GO] != 0;
     const bool es_on = (p.on[XMD_TERM_CONST_ES] || p.on[XMD_TERM_REL_ES]);
     const bool qa_on = d.qa_on && p.on[XMD_TERM_QA];
-    const Band Breq = make_band(rp.req_r, m);
-    const Band Bpa = make_band(1.0 / rp.pauli_min_inv, m);
-    const Band Bes = make_band(1.0 / rp.es_min_inv, m);
-    const Band Bqa = make_band(1.0 / rp.qa_min_inv, m);
+    const Band Breq = bands_s[0], Bpa = bands_s[1], Bes = bands_s[2], Bqa = bands_s[3];
     const float Lx = (float)bx.cell[0], Ly = (float)bx.cell[1], Lz = (float)bx.cell[2];
     const bool periodic = (rp.per[0] | rp.per[1] | rp.per[2]) != 0;
     const double pad = rp.pad;
     const int cap = d.nl_cap;
     const unsigned lt = (1u << lane) - 1u;
+    const float skip2 = Breq.hi * 1.0001f;
 
     if (t == 0 && chk.y == b) {
         rp.first = 0;
@@ -886,8 +931,14 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
                 dz = min_image_f(dz, Lz);
             }
             const float d2 = dx * dx + dy * dy + dz * dz;
-            const double T = __dadd_rn(2.0 * d.nat_d[k], pad);
-            const Band B = make_band(T, m);
+            // band around T = 2 r_nat + pad in FP32 with directed rounding,
+            // widened by the narrowing error of T: at least as wide as the
+            // FP64-formed band, so the exact test decides the same pairs
+            const double T = d.nat_T[k];
+            const float Tf = narrow_f(T);
+            const float mm = __fmaf_ru(Tf, 1.2e-7f, mf);
+            const float blo = __fsub_rd(Tf, mm), bhi = __fadd_ru(Tf, mm);
+            const Band B{blo > 0.0f ? __fmul_rd(blo, blo) : -1.0f, __fmul_ru(bhi, bhi)};
             bool on;
             if (in_band(B, d2)) on = dist_exact(bx, pi, pos[j]) < T;
             else on = d2 < B.lo;
@@ -898,6 +949,16 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
         if (qa_on) nref = min(d.qa.ref_cnt[i], QA_REF_CAP);
         int cnt = 0, tcnt = 0;
         for (int j0 = 0; j0 < n; j0 += 32) {
+            if (!periodic) {
+                // a group whose box is beyond the list radius holds no pair
+                // (FP32 rounding is monotone, so the box distance never exceeds
+                // a member's distance; the factor covers contraction order)
+                const float4 lo = gbox[2 * (j0 >> 5)], hi = gbox[2 * (j0 >> 5) + 1];
+                const float gx = fmaxf(fmaxf(lo.x - qi.x, qi.x - hi.x), 0.0f);
+                const float gy = fmaxf(fmaxf(lo.y - qi.y, qi.y - hi.y), 0.0f);
+                const float gz = fmaxf(fmaxf(lo.z - qi.z, qi.z - hi.z), 0.0f);
+                if (gx * gx + gy * gy + gz * gz > skip2) continue;
+            }
             const int lj = j0 + lane;
             int flags = 0;
             bool qa_free = false;
@@ -1305,6 +1366,7 @@ void Engine::allocate() {
     d.nat_j = (int32_t *)dalloc(sizeof(int32_t) * NN);
     d.nat_d = (double *)dalloc(sizeof(double) * NN);
     d.nat_df = (float *)dalloc(sizeof(float) * NN);
+    d.nat_T = (double *)dalloc(sizeof(double) * NN);
     d.nat_on = (uint8_t *)dalloc(NN);
     d.nl_row = (int32_t *)dalloc(sizeof(int32_t) * (size_t)nl_cap * N);
     d.nl_cnt = (int32_t *)dalloc(sizeof(int32_t) * N);
@@ -1339,8 +1401,8 @@ void Engine::allocate() {
     d.any_cell = any_cell;
     tile_smem = 0;
     for (auto &r : reps)
-        if (r.in_use && r.n <= TILE_MAX) tile_smem = std::max(tile_smem, (sizeof(float4) + sizeof(int2)) * (size_t)r.n);
-    if (dynamic) tile_smem = (sizeof(float4) + sizeof(int2)) * (size_t)std::min(TILE_MAX, cap.beads);
+        if (r.in_use && r.n <= TILE_MAX) tile_smem = std::max(tile_smem, tile_bytes(r.n));
+    if (dynamic) tile_smem = tile_bytes(std::min(TILE_MAX, cap.beads));
     if (tile_smem > 48 * 1024)
         CK(cudaFuncSetAttribute(k_nl_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem));
     {
@@ -1561,6 +1623,11 @@ void Engine::place(int k) {
 
     RepDev rd;
     derive_rep(k, rd);
+    {
+        std::vector<double> nT(nd.size());
+        for (size_t q = 0; q < nd.size(); ++q) nT[q] = 2.0 * nd[q] + rd.pad;   // 2 r_nat is exact
+        up(d.nat_T + no, nT.data(), sizeof(double) * nT.size());
+    }
     rd.cell_off = co;
     rd.cell_budget = ncell;
     rd.tile = tile;

@@ -89,6 +89,7 @@ struct Dev {
     int32_t *nat_start, *nat_end, *nat_j;   // natives of bead i: [nat_start[i], nat_end[i])
     double *nat_d;
     float *nat_df;          // nat_d in FP32 for the mixed path
+    double *nat_T;          // Go-list threshold 2 r_nat + pad of each entry (go.cpp:11-22)
     uint8_t *nat_on;
     int32_t *nl_row, *nl_cnt;
     int32_t *cell_cnt, *cell_start, *cell_fill, *cell_items, *bead_cell;
