@@ -1,5 +1,7 @@
 """The mixed path's integer-pipe FP64 <-> FP32 conversions equal the hardware
-conversions bit for bit over the normal FP32 range."""
+conversions bit for bit over the normal FP32 range, and its float-float
+toolkit (position splits, differences, products, sums, accumulation) stays
+within 2^-44 of FP64 references."""
 import shutil
 import subprocess
 from pathlib import Path
@@ -18,3 +20,4 @@ def test_narrow_and_widen_match_hardware(tmp_path):
     res = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
     assert res.returncode == 0, res.stdout + res.stderr
     assert "narrow mismatches 0 widen mismatches 0" in res.stdout
+    assert "split mismatches 0 diff mismatches 0 ffop mismatches 0 acc mismatches 0" in res.stdout
