@@ -302,6 +302,8 @@ def run_engine(args, rank, local, world):
         serving = {"mixed": serve_bench(reqs, "mixed", args.serve_steps, rate, dev),
                    "fp64": serve_bench(reqs, "fp64", args.serve_steps, rate, dev)}
 
+    accuracy = accuracy_c3(args.accuracy_steps, args.accuracy_every, dev) \
+        if (rank == 0 and args.accuracy_steps > 0) else None
     cpu = cpu_baseline(systems, sample_steps=args.cpu_sample_steps) if rank == 0 else None
     rt.cudaFree(flush)
     rt.cudaFreeHost(hbuf)
@@ -324,6 +326,7 @@ def run_engine(args, rank, local, world):
             "mixed_force_rel_err_max": max(errs), "graph_steps_per_launch": 16,
             "p99_req_latency_ms": serving["mixed"]["p99_ms"] if serving else None,
             "serving": serving,
+            "mixed_vs_fp64_c3": accuracy,
         },
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
@@ -366,6 +369,35 @@ def plain_fp64(systems, yaml_fp64, md, warmup, rt, flush, sample=16):
     return {"value": work / (t_ms / 1e3),
             "sample": f"{len(pick)} size-stratified replicas ({nb} beads), each alone in an FP64 context, "
                       f"{md} steps each"}
+
+
+def accuracy_c3(steps, every, device):
+    """Config 3: mixed precision against plain FP64 on 512 chains x 60 beads at
+    1e-3 A^-3 (periodic; Go + Debye-Hueckel + quasi-adiabatic contacts).
+    Forces are compared on the starting state; then each precision runs
+    `steps` steps from that state with the same generator seed, and the
+    energy (mean and drift), Rg and Q are compared over the second half of
+    the run (block-averaged standard errors)."""
+    from xmd_gb300 import Engine, observe, synth
+    s = synth.config_c3()
+    runs, forces, wall = {}, {}, {}
+    for prec in ("fp64", "mixed"):
+        with Engine(synth.yaml_for("c3", prec) + f"  device: {device}\n") as e:
+            e.add_system(s)
+            forces[prec], _ = e.eval_forces(0)
+            t0 = time.perf_counter()
+            runs[prec] = observe.sample(e, steps, every)
+            wall[prec] = time.perf_counter() - t0
+    res = observe.compare(runs["mixed"], runs["fp64"], skip=0.5)
+    ferr = float(np.abs(forces["mixed"] - forces["fp64"]).max() / np.abs(forces["fp64"]).max())
+    return {"system": f"512 x 60 beads ({s.n}), periodic, Go + Debye-Hueckel + quasi-adiabatic",
+            "steps": steps, "sample_every": every, "force_rel_err_t0": ferr,
+            "E_mean_rel_diff": res["E"]["rel_diff"], "E_mean_diff": res["E"]["diff"], "E_se": res["E"]["se"],
+            "E_drift_mixed": res["E_drift"]["drift"], "E_drift_fp64": res["E_drift"]["ref_drift"],
+            "E_drift_diff_rel_to_energy_scale": res["E_drift"]["rel_to_ref_energy"],
+            "Rg_mean_rel_diff": res["Rg"]["rel_diff"], "Rg_se": res["Rg"]["se"],
+            "Q_mean_diff": res["Q"]["diff"], "Q_se": res["Q"]["se"],
+            "wall_s": wall, "reference": "plain FP64 engine (pinned to the oracle by the parity tests)"}
 
 
 def serve_bench(requests, precision, nsteps, rate_hz, device, seed=0):
@@ -481,6 +513,8 @@ def main():
     ap.add_argument("--cpu-sample-steps", type=int, default=100)
     ap.add_argument("--serve-requests", type=int, default=12)
     ap.add_argument("--serve-steps", type=int, default=20000)
+    ap.add_argument("--accuracy-steps", type=int, default=100000)
+    ap.add_argument("--accuracy-every", type=int, default=1000)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, local, world = dist_env()

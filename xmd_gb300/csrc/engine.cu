@@ -132,6 +132,22 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
     __shared__ V3<FF> Eff[NE], Xff[NE];
     __shared__ V3<float> Ef[NE], Xf[NE];
 
+    // mixed path: the integrator's per-bead state does not depend on the
+    // forces, so its loads are issued first and their latency passes under
+    // the force work (the FP64 path is bound by its FP64 pipe instead and
+    // loads them where they are used)
+    constexpr bool EARLY = MODE == 1 && sizeof(FT) == 4;
+    double yv[15];
+    uint64_t st0 = 0;
+    double4_32a o_i = make_double4_32a(0, 0, 0, 0);
+    if (EARLY && i0 + t < N) {
+        const size_t Ns = (size_t)N;
+#pragma unroll
+        for (int q = 0; q < 15; ++q) yv[q] = d.yh[q * Ns + i0 + t];
+        st0 = d.rng[i0 + t];
+        o_i = d.orig[i0 + t];
+    }
+
     for (int k = t; k < FB + 6; k += FB) {
         int idx = i0 - 3 + k;
         P[k] = (idx >= 0 && idx < N) ? pin[idx] : make_double4_32a(0, 0, 0, 0);
@@ -338,7 +354,11 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
     }
 
     // ---- lang_pc_step::operator(), lang_pc.cpp:11-37, mass = 1 (main.cpp:156) ----
-    uint64_t st = d.rng[i];
+    if (!EARLY) {
+        st0 = d.rng[i];
+        o_i = d.orig[i];
+    }
+    uint64_t st = st0;
     double nz[3];
     if constexpr (sizeof(FT) == 8) {
         noise3(st, &nz[0], &nz[1], &nz[2]);
@@ -359,9 +379,13 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
     const size_t Ns = (size_t)N;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        double y1 = yh[(0 * 3 + a) * Ns + i], y2 = yh[(1 * 3 + a) * Ns + i];
-        double y3 = yh[(2 * 3 + a) * Ns + i], y4 = yh[(3 * 3 + a) * Ns + i];
-        double y5 = yh[(4 * 3 + a) * Ns + i];
+        double y1, y2, y3, y4, y5;
+        if constexpr (EARLY) {
+            y1 = yv[0 * 3 + a]; y2 = yv[1 * 3 + a]; y3 = yv[2 * 3 + a]; y4 = yv[3 * 3 + a]; y5 = yv[4 * 3 + a];
+        } else {
+            y1 = yh[(0 * 3 + a) * Ns + i]; y2 = yh[(1 * 3 + a) * Ns + i]; y3 = yh[(2 * 3 + a) * Ns + i];
+            y4 = yh[(3 * 3 + a) * Ns + i]; y5 = yh[(4 * 3 + a) * Ns + i];
+        }
         double v = y1 * dt_inv;
         double a_ = F3[a] * 1.0 - gamma * v + nsd * nz[a];
         double error = y2 - a_ * h;
@@ -391,11 +415,11 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
     if constexpr (sizeof(FT) == 4) {
         // mixed path: the displacement from split positions (the FP64
         // difference to FP32 accuracy), squared in FP32
-        const V3<float> e = geo.between(d.orig[i], pn);
+        const V3<float> e = geo.between(o_i, pn);
         disp = widen_f(e.x * e.x + e.y * e.y + e.z * e.z);
     } else {
         // on open axes the wrap subtracts exactly zero: skipping it changes no bit
-        disp = per ? dist2_exact(bx, pn, d.orig[i]) : dist2_open(pn, d.orig[i]);
+        disp = per ? dist2_exact(bx, pn, o_i) : dist2_open(pn, o_i);
     }
     const unsigned lane = t & 31;
     int r0 = __shfl_sync(0xffffffffu & __activemask(), r, 0);
@@ -825,9 +849,12 @@ __host__ __device__ constexpr size_t tile_bytes(int n) {
     return 2 * sizeof(float4) * (size_t)((n + 31) / 32) + (sizeof(float4) + sizeof(int2)) * (size_t)n;
 }
 
-__device__ __forceinline__ float tl_rel(const RepDev &rp, int a, double x, double ref) {
+// FP32 coordinate of the pre-filter: wrapped into [0, L) on periodic axes,
+// else relative to the replica's first bead (from split positions: the FP64
+// difference to within 2^-46, then rounded to FP32, with no FP64 instruction)
+__device__ __forceinline__ float tl_rel(const RepDev &rp, int a, double x, F2 ref) {
     if (rp.per[a]) return (float)(x - rp.box.cell[a] * floor(x * rp.box.cell_inv[a]));
-    return (float)(x - ref);
+    return ff_diff(ref, split_d(x)).h;
 }
 
 
@@ -847,13 +874,13 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
     const double4_32a *pos = d.pos[cur];
     const BoxD bx = rp.box;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-    const double4_32a p0 = pos[b];
+    const P2 p0 = split_p(pos[b]);
 
     float ext = 0.0f;
     for (int k = t; k < n; k += TL_THREADS) {
         double4_32a q = pos[b + k];
         float x = tl_rel(rp, 0, q.x, p0.x), y = tl_rel(rp, 1, q.y, p0.y), z = tl_rel(rp, 2, q.z, p0.z);
-        sq[k] = make_float4(x, y, z, (float)q.w);
+        sq[k] = make_float4(x, y, z, narrow_f(q.w));
         scs[k] = make_int2(d.chain[b + k], d.seq[b + k]);
         ext = fmaxf(ext, fmaxf(fabsf(x), fmaxf(fabsf(y), fabsf(z))));
     }
@@ -862,6 +889,19 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
     __syncthreads();
     ext = 0.0f;
     for (int q = 0; q < TL_WARPS; ++q) ext = fmaxf(ext, ext_s[q]);
+    // decision bands of the chunk, formed once (FP64 work off the scan)
+    __shared__ Band bands_s[4];
+    __shared__ float mf_s;
+    if (t == 0) {
+        double exd = (double)ext;
+        for (int a = 0; a < 3; ++a) exd = fmax(exd, bx.cell[a]);
+        const double m = 1e-3 + 4e-7 * exd;
+        bands_s[0] = make_band(rp.req_r, m);
+        bands_s[1] = make_band(1.0 / rp.pauli_min_inv, m);
+        bands_s[2] = make_band(1.0 / rp.es_min_inv, m);
+        bands_s[3] = make_band(1.0 / rp.qa_min_inv, m);
+        mf_s = __double2float_ru(m);
+    }
     // bounding box of each group of 32 beads j (one warp per group)
     for (int g = w; g < ng; g += TL_WARPS) {
         const float4 q = sq[min(g * 32 + lane, n - 1)];
@@ -880,20 +920,6 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
         }
     }
     __syncthreads();
-    // decision bands of the chunk, formed once (FP64 work off the scan)
-    __shared__ Band bands_s[4];
-    __shared__ float mf_s;
-    if (t == 0) {
-        double exd = (double)ext;
-        for (int a = 0; a < 3; ++a) exd = fmax(exd, bx.cell[a]);
-        const double m = 1e-3 + 4e-7 * exd;
-        bands_s[0] = make_band(rp.req_r, m);
-        bands_s[1] = make_band(1.0 / rp.pauli_min_inv, m);
-        bands_s[2] = make_band(1.0 / rp.es_min_inv, m);
-        bands_s[3] = make_band(1.0 / rp.qa_min_inv, m);
-        mf_s = __double2float_ru(m);
-    }
-    __syncthreads();
     const float mf = mf_s;
 
     const bool pauli_on = p.on[XMD_TERM_PAULI] != 0;
@@ -901,9 +927,8 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
     const bool es_on = (p.on[XMD_TERM_CONST_ES] || p.on[XMD_TERM_REL_ES]);
     const bool qa_on = d.qa_on && p.on[XMD_TERM_QA];
     const Band Breq = bands_s[0], Bpa = bands_s[1], Bes = bands_s[2], Bqa = bands_s[3];
-    const float Lx = (float)bx.cell[0], Ly = (float)bx.cell[1], Lz = (float)bx.cell[2];
+    const float Lx = narrow_f(bx.cell[0]), Ly = narrow_f(bx.cell[1]), Lz = narrow_f(bx.cell[2]);
     const bool periodic = (rp.per[0] | rp.per[1] | rp.per[2]) != 0;
-    const double pad = rp.pad;
     const int cap = d.nl_cap;
     const unsigned lt = (1u << lane) - 1u;
     const float skip2 = Breq.hi * 1.0001f;
@@ -1040,7 +1065,7 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
     }
 }
 
-__global__ void __launch_bounds__(TL_THREADS) k_nl_tile(Dev d, TermP p, int cur) {
+__global__ void __launch_bounds__(TL_THREADS, 4) k_nl_tile(Dev d, TermP p, int cur) {
     if (blockIdx.x == 0 && threadIdx.x == 0 && !d.any_cell) atomicAdd(d.ctr, 1ull);
     const int nw = *d.nwork;
     for (int w = blockIdx.x; w < nw; w += gridDim.x) {
