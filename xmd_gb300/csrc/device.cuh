@@ -154,8 +154,7 @@ __device__ __forceinline__ FF ff_diff(F2 u, F2 w) {
 // <= 2^-47 of the running magnitude)
 __device__ __forceinline__ void ff_acc(FF &acc, float v) {
     FF s = two_sum(acc.h, v);
-    acc.h = s.h;
-    acc.l = __fadd_rn(acc.l, s.l);
+    acc = fast_two_sum(s.h, __fadd_rn(s.l, acc.l));
 }
 __device__ __forceinline__ double ff_to_d(FF a) { return widen_f(a.h) + widen_f(a.l); }
 

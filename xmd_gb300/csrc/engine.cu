@@ -506,6 +506,25 @@ __global__ void k_mark_all(Dev d) {
     if (r < d.R && d.rep[r].active && d.rep[r].rebuild) d.rep[r].first = 1;
 }
 
+// Minimum image of a difference of coordinates wrapped into [0, L) (so
+// |d| < L) by compare and select: rintf runs on the slow conversion pipe.
+// L = 0 (open axis) leaves d unchanged.
+__device__ __forceinline__ float min_image_f(float d, float L) {
+    const float h = 0.5f * L;
+    d = d > h ? d - L : d;
+    return d < -h ? d + L : d;
+}
+
+// FP32 decision band around a distance threshold T (error bound m)
+struct Band {
+    float lo, hi;   // squared FP32 distance: below lo -> inside, above hi -> outside
+};
+__device__ __forceinline__ Band make_band(double T, double m) {
+    double a = T - m, b = T + m;
+    return Band{a > 0.0 ? __double2float_rd(a * a) : -1.0f, __double2float_ru(b * b)};
+}
+__device__ __forceinline__ bool in_band(const Band &B, float d2) { return d2 >= B.lo && d2 <= B.hi; }
+
 // ---- cell lists: one block per flagged replica -----------------------------------
 // Cells have an edge of at least the Verlet radius.  Periodic axes are cut
 // into dims = floor(L / r) cells (wrapped); open axes count cells from the
@@ -546,7 +565,6 @@ __global__ void __launch_bounds__(CB) k_cells(Dev d, int cur) {
     const double4_32a *pos = d.pos[cur];
     const int b = rp.begin, n = rp.n, off = rp.cell_off, bud = rp.cell_budget;
     __shared__ double red_lo[3][32], red_hi[3][32];
-    __shared__ int scan_s[CB];
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
 
     // bounding box along open axes
@@ -596,6 +614,13 @@ __global__ void __launch_bounds__(CB) k_cells(Dev d, int cur) {
         double m = rp.req_r + 1e-3 + 4e-7 * ext;
         rp.pre2 = (float)(m * m);
         rp.band_m = 1e-3 + 4e-7 * ext;
+        const double T[4] = {rp.req_r, 1.0 / rp.pauli_min_inv, 1.0 / rp.es_min_inv, 1.0 / rp.qa_min_inv};
+        for (int k = 0; k < 4; ++k) {
+            const Band B = make_band(T[k], rp.band_m);
+            rp.band_lo[k] = B.lo;
+            rp.band_hi[k] = B.hi;
+        }
+        rp.band_mf = __double2float_ru(rp.band_m);
         rp.first = 0;
         rp.rebuilds += 1;
     }
@@ -605,14 +630,34 @@ __global__ void __launch_bounds__(CB) k_cells(Dev d, int cur) {
         d.cell_cnt[off + c] = 0;
         d.cell_fill[off + c] = 0;
     }
-    __syncthreads();
-    for (int i = b + t; i < b + n; i += CB) {
-        double4_32a q = pos[i];
-        int c = cell_key(rp, cell_coord(rp, 0, q.x), cell_coord(rp, 1, q.y), cell_coord(rp, 2, q.z));
-        d.bead_cell[i] = off + c;
-        atomicAdd(&d.cell_cnt[off + c], 1);
-    }
-    __syncthreads();
+}
+
+// The bucket sort of the flagged replicas, over the whole grid: count, scan
+// (one block per replica, over its buckets), scatter, then per bucket a
+// deterministic order (ascending bead index) and the FP32 coordinates.
+__device__ __forceinline__ bool cell_flagged(const Dev &d, int r) {
+    if (r < 0) return false;
+    const RepDev &rp = d.rep[r];
+    return rp.active && rp.rebuild && !rp.tile;
+}
+__global__ void k_cell_count(Dev d, int cur) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.N) return;
+    const int r = d.rep_of[i];
+    if (!cell_flagged(d, r)) return;
+    const RepDev &rp = d.rep[r];
+    const double4_32a q = d.pos[cur][i];
+    const int c = rp.cell_off + cell_key(rp, cell_coord(rp, 0, q.x), cell_coord(rp, 1, q.y), cell_coord(rp, 2, q.z));
+    d.bead_cell[i] = c;
+    atomicAdd(&d.cell_cnt[c], 1);
+}
+__global__ void __launch_bounds__(CB) k_cell_scan(Dev d) {
+    const int r = blockIdx.x;
+    if (!cell_flagged(d, r)) return;
+    const RepDev &rp = d.rep[r];
+    __shared__ int scan_s[CB];
+    const int t = threadIdx.x, off = rp.cell_off;
+    const int ncell = rp.hashed ? rp.cell_budget : rp.dims[0] * rp.dims[1] * rp.dims[2];
     // exclusive scan of the counts, contiguous chunk per thread
     const int chunk = (ncell + CB - 1) / CB;
     const int c0 = t * chunk, c1 = min(ncell, c0 + chunk);
@@ -626,60 +671,93 @@ __global__ void __launch_bounds__(CB) k_cells(Dev d, int cur) {
         scan_s[t] += v;
         __syncthreads();
     }
-    int run = b + scan_s[t] - sum;
+    int run = rp.begin + scan_s[t] - sum;
     for (int c = c0; c < c1; ++c) {
         d.cell_start[off + c] = run;
         run += d.cell_cnt[off + c];
     }
-    __syncthreads();
-    for (int i = b + t; i < b + n; i += CB) {
-        int c = d.bead_cell[i];
-        int slot = atomicAdd(&d.cell_fill[c], 1);
-        d.cell_items[d.cell_start[c] + slot] = i;
-    }
-    __syncthreads();
-    // deterministic order inside each bucket, then the FP32 coordinates
-    for (int c = t; c < ncell; c += CB) {
-        int s0 = d.cell_start[off + c], m = d.cell_cnt[off + c];
-        int *it = d.cell_items + s0;
+}
+__global__ void k_cell_scatter(Dev d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.N) return;
+    if (!cell_flagged(d, d.rep_of[i])) return;
+    const int c = d.bead_cell[i];
+    const int slot = atomicAdd(&d.cell_fill[c], 1);
+    d.cell_items[d.cell_start[c] + slot] = i;
+}
+// one warp per bucket of the pool: the bucket's beads put in ascending index
+// order (each item's rank among the bucket's items; buckets of more than
+// 8 x 32 beads are sorted by one lane), then their FP32 coordinates
+constexpr int CF_WARPS = 8, CF_HOLD = 8;
+__global__ void __launch_bounds__(CF_WARPS * 32) k_cell_finish(Dev d, int cur) {
+    const int lane = threadIdx.x & 31;
+    const int c = blockIdx.x * CF_WARPS + (threadIdx.x >> 5);
+    if (c >= d.ncells) return;   // warp-uniform exits
+    const int r = d.cell_rep[c];
+    if (!cell_flagged(d, r)) return;
+    const RepDev &rp = d.rep[r];
+    const int ncell = rp.hashed ? rp.cell_budget : rp.dims[0] * rp.dims[1] * rp.dims[2];
+    if (c - rp.cell_off >= ncell) return;
+    const int s0 = d.cell_start[c], m = d.cell_cnt[c];
+    int *it = d.cell_items + s0;
+    const unsigned FULL = 0xffffffffu;
+    if (m <= 32 * CF_HOLD) {
+        int v[CF_HOLD], rk[CF_HOLD];
+#pragma unroll
+        for (int u = 0; u < CF_HOLD; ++u) {
+            v[u] = u * 32 + lane < m ? it[u * 32 + lane] : 0x7fffffff;
+            rk[u] = 0;
+        }
+        for (int k = 0; k < m; ++k) {
+            int x = 0;
+#pragma unroll
+            for (int u = 0; u < CF_HOLD; ++u)
+                if ((k >> 5) == u) x = __shfl_sync(FULL, v[u], k & 31);
+#pragma unroll
+            for (int u = 0; u < CF_HOLD; ++u) rk[u] += x < v[u];
+        }
+        __syncwarp();
+#pragma unroll
+        for (int u = 0; u < CF_HOLD; ++u)
+            if (u * 32 + lane < m) it[rk[u]] = v[u];
+    } else if (lane == 0) {
         for (int x = 1; x < m; ++x) {
-            int v = it[x], y = x - 1;
-            while (y >= 0 && it[y] > v) { it[y + 1] = it[y]; --y; }
-            it[y + 1] = v;
+            int vv = it[x], y = x - 1;
+            while (y >= 0 && it[y] > vv) { it[y + 1] = it[y]; --y; }
+            it[y + 1] = vv;
         }
     }
-    __syncthreads();
-    for (int k = b + t; k < b + n; k += CB) {
-        int i = d.cell_items[k];
-        double4_32a q = pos[i];
+    __syncwarp();
+    const double4_32a *pos = d.pos[cur];
+    for (int k = s0 + lane; k < s0 + m; k += 32) {
+        const int i = d.cell_items[k];
+        const double4_32a q = pos[i];
         d.cell_pos[k] = make_float4(rel_coord(rp, 0, q.x), rel_coord(rp, 1, q.y), rel_coord(rp, 2, q.z),
                                     __int_as_float(i));
+        d.cell_cs[k] = make_int2(d.chain[i], d.seq[i]);
+        d.bead_slot[i] = k;
     }
 }
 
 // ---- Verlet rows (legacy_update.cpp:16-62 + the update_* filters) ---------------
-// Minimum image of a difference of coordinates wrapped into [0, L) (so
-// |d| < L) by compare and select: rintf runs on the slow conversion pipe.
-// L = 0 (open axis) leaves d unchanged.
-__device__ __forceinline__ float min_image_f(float d, float L) {
-    const float h = 0.5f * L;
-    d = d > h ? d - L : d;
-    return d < -h ? d + L : d;
-}
 
-// FP32 decision band around a distance threshold T (error bound m)
-struct Band {
-    float lo, hi;   // squared FP32 distance: below lo -> inside, above hi -> outside
-};
-__device__ __forceinline__ Band make_band(double T, double m) {
-    double a = T - m, b = T + m;
-    return Band{a > 0.0 ? __double2float_rd(a * a) : -1.0f, __double2float_ru(b * b)};
-}
-__device__ __forceinline__ bool in_band(const Band &B, float d2) { return d2 >= B.lo && d2 <= B.hi; }
-
-__global__ void __launch_bounds__(128) k_nl_build(Dev d, TermP p, int cur) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= d.N) return;
+// ---- Verlet rows of the cell build (legacy_update.cpp:16-62 + the update_*
+// filters), one warp per bead i --------------------------------------------------
+// A pair is decided in FP32 when its FP32 distance is outside the bands of
+// the replica (k_cells: the list radius, r_excl + pad, 2D + pad, the QA
+// formation radius + pad, each widened by the FP32 error bound), and by the
+// exact FP64 test inside them.  The candidates of each neighbouring bucket
+// are taken 32 at a time by the lanes: loads of a bucket are contiguous, the
+// row is compacted by ballot, and the bead's latency chain is one bucket deep
+// instead of one candidate deep.  Buckets are visited z, then y, then x
+// offset (first occurrence of each key).  Quasi-adiabatic partners are ranked
+// by j within the warp at the end, so the free-pair source list is ordered as
+// update_free_pairs (free_pair.cpp:9-19) walks it.
+constexpr int NC_WARPS = 8;
+__global__ void __launch_bounds__(NC_WARPS * 32, 3) k_nl_cells(Dev d, TermP p, int cur) {
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * NC_WARPS + (threadIdx.x >> 5);
+    if (i >= d.N) return;   // warp-uniform exits
     const int r = d.rep_of[i];
     if (r < 0) return;
     const RepDev &rp = d.rep[r];
@@ -689,138 +767,182 @@ __global__ void __launch_bounds__(128) k_nl_build(Dev d, TermP p, int cur) {
     const BoxD bx = rp.box;
     const int ci = d.chain[i], si = d.seq[i];
     const int n0 = d.nat_start[i], n1 = d.nat_end[i];
-    const double pad = rp.pad;
+    const unsigned FULL = 0xffffffffu, lt = (1u << lane) - 1u;
+    const PairGeo<float> geo(bx, (rp.per[0] | rp.per[1] | rp.per[2]) != 0, pi);
+    const float mf = rp.band_mf;
 
-    // Go list: update_go_contacts, go.cpp:11-22
-    for (int k = n0; k < n1; ++k) {
+    // Go list: update_go_contacts, go.cpp:11-22 (lanes over the natives)
+    for (int k = n0 + lane; k < n1; k += 32) {
         const double4_32a pj = pos[d.nat_j[k]];
-        const double T = __dadd_rn(2.0 * d.nat_d[k], pad);
-        float ex = (float)(pj.x - pi.x), ey = (float)(pj.y - pi.y), ez = (float)(pj.z - pi.z);
-        ex -= (float)bx.cell[0] * rintf(ex * (float)bx.cell_inv[0]);
-        ey -= (float)bx.cell[1] * rintf(ey * (float)bx.cell_inv[1]);
-        ez -= (float)bx.cell[2] * rintf(ez * (float)bx.cell_inv[2]);
-        const float d2 = ex * ex + ey * ey + ez * ez;
-        const Band B = make_band(T, 1e-3 + 1e-6 * T);
+        const V3<float> e = geo.to(pj);
+        const float d2 = e.x * e.x + e.y * e.y + e.z * e.z;
+        // band around T = 2 r_nat + pad, as in the tile build (split
+        // differences carry <= 1 ulp, inside the margin)
+        const double T = d.nat_T[k];
+        const float Tf = narrow_f(T);
+        const float mm = __fmaf_ru(Tf, 1.2e-7f, mf);
+        const float blo = __fsub_rd(Tf, mm), bhi = __fadd_ru(Tf, mm);
+        const Band B{blo > 0.0f ? __fmul_rd(blo, blo) : -1.0f, __fmul_ru(bhi, bhi)};
         d.nat_on[k] = in_band(B, d2) ? dist_exact(bx, pi, pj) < T : d2 < B.lo;
     }
 
-    int cc[3];
-    cc[0] = cell_coord(rp, 0, pi.x);
-    cc[1] = cell_coord(rp, 1, pi.y);
-    cc[2] = cell_coord(rp, 2, pi.z);
-    int offs[3][3], noff[3];
-    for (int a = 0; a < 3; ++a) {
-        noff[a] = 0;
-        for (int dlt = -1; dlt <= 1; ++dlt) {
-            int k = cc[a] + dlt;
+    // neighbouring buckets: lane l < 27 takes offsets (l/9, l/3 % 3, l % 3) - 1
+    int key = -1;
+    if (lane < 27) {
+        const int off[3] = {lane % 3 - 1, (lane / 3) % 3 - 1, lane / 9 - 1};
+        int cc[3];
+        bool ok = true;
+        for (int a = 0; a < 3; ++a) {
+            int k = cell_coord(rp, a, a == 0 ? pi.x : (a == 1 ? pi.y : pi.z)) + off[a];
             if (rp.per[a]) k = ((k % rp.dims[a]) + rp.dims[a]) % rp.dims[a];
-            else if (k < 0) continue;
-            bool dup = false;
-            for (int q = 0; q < noff[a]; ++q) dup |= offs[a][q] == k;
-            if (!dup) offs[a][noff[a]++] = k;
+            else if (k < 0) ok = false;
+            cc[a] = k;
         }
+        if (ok) key = cell_key(rp, cc[0], cc[1], cc[2]);
     }
-    // distinct buckets of the neighbouring cells
-    int keys[27], nk = 0;
-    for (int az = 0; az < noff[2]; ++az)
-        for (int ay = 0; ay < noff[1]; ++ay)
-            for (int ax = 0; ax < noff[0]; ++ax) {
-                int key = cell_key(rp, offs[0][ax], offs[1][ay], offs[2][az]);
-                bool dup = false;
-                for (int q = 0; q < nk; ++q) dup |= keys[q] == key;
-                if (!dup) keys[nk++] = key;
-            }
-    const float mx = rel_coord(rp, 0, pi.x), my = rel_coord(rp, 1, pi.y), mz = rel_coord(rp, 2, pi.z);
-    const float Lx = (float)bx.cell[0], Ly = (float)bx.cell[1], Lz = (float)bx.cell[2];
+    // first occurrence of each key in lane order
+    const unsigned same = __match_any_sync(FULL, key);
+    const bool lead = key >= 0 && (same & lt) == 0u;
+    unsigned todo = __ballot_sync(FULL, lead);
+    // each lead lane fetches its bucket's range up front
+    int kq0 = 0, kq1 = 0;
+    if (lead) {
+        const int c = rp.cell_off + key;
+        kq0 = d.cell_start[c];
+        kq1 = kq0 + d.cell_cnt[c];
+    }
+
+    const float4 me = d.cell_pos[d.bead_slot[i]];
+    const float mx = me.x, my = me.y, mz = me.z;
+    const float Lx = narrow_f(bx.cell[0]), Ly = narrow_f(bx.cell[1]), Lz = narrow_f(bx.cell[2]);
     const bool periodic = (rp.per[0] | rp.per[1] | rp.per[2]) != 0;
     const float pre2 = rp.pre2;
-    const double bm = rp.band_m;
-    const Band Breq = make_band(rp.req_r, bm);
-    const Band Bpa = make_band(1.0 / rp.pauli_min_inv, bm);
-    const Band Bes = make_band(1.0 / rp.es_min_inv, bm);
-    const Band Bqa = make_band(1.0 / rp.qa_min_inv, bm);
+    const Band Breq{rp.band_lo[0], rp.band_hi[0]}, Bpa{rp.band_lo[1], rp.band_hi[1]};
+    const Band Bes{rp.band_lo[2], rp.band_hi[2]}, Bqa{rp.band_lo[3], rp.band_hi[3]};
     const bool pauli_on = p.on[XMD_TERM_PAULI] != 0;
     const bool go_on = p.on[XMD_TERM_GO] != 0;
     const bool es_on = (p.on[XMD_TERM_CONST_ES] || p.on[XMD_TERM_REL_ES]);
     const bool qa_on = d.qa_on && p.on[XMD_TERM_QA];
     const int nref = qa_on ? min(d.qa.ref_cnt[i], QA_REF_CAP) : 0;
-    int cnt = 0, tcnt = 0;
+    const float qi_w = narrow_f(pi.w);
     const int cap = d.nl_cap;
-    for (int kk = 0; kk < nk; ++kk) {
-                int c = rp.cell_off + keys[kk];
-                int q0 = d.cell_start[c], q1 = q0 + d.cell_cnt[c];
-                for (int q = q0; q < q1; ++q) {
-                    const float4 f = d.cell_pos[q];
-                    int j = __float_as_int(f.w);
-                    if (j == i) continue;
-                    // FP32 pre-filter (min image on periodic axes)
-                    float ddx = f.x - mx, ddy = f.y - my, ddz = f.z - mz;
-                    if (periodic) {
-                        ddx = min_image_f(ddx, Lx);
-                        ddy = min_image_f(ddy, Ly);
-                        ddz = min_image_f(ddz, Lz);
-                    }
-                    const float d2 = ddx * ddx + ddy * ddy + ddz * ddz;
-                    if (d2 > pre2) continue;
-                    int cj = d.chain[j], sj = d.seq[j];
-                    int df = si > sj ? si - sj : sj - si;
-                    if (ci == cj && df < 3) continue;
-                    // decided in FP32 away from every threshold, exactly near one
-                    // (the margin argument of k_nl_tile)
-                    bool in_req, pa, es, qa;
-                    if (in_band(Breq, d2) || (pauli_on && in_band(Bpa, d2)) || (es_on && in_band(Bes, d2)) ||
-                        (qa_on && in_band(Bqa, d2))) {
-                        const double dd = dist_exact(bx, pi, pos[j]);
-                        const double inv = __ddiv_rn(1.0, dd);
-                        in_req = dd < rp.req_r;
-                        pa = inv > rp.pauli_min_inv;
-                        es = inv > rp.es_min_inv;
-                        qa = inv > rp.qa_min_inv;
-                    } else {
-                        in_req = d2 < Breq.lo;
-                        pa = d2 < Bpa.lo;
-                        es = d2 < Bes.lo;
-                        qa = d2 < Bqa.lo;
-                    }
-                    if (!in_req) continue;
-                    // natives leave the list only when native contacts are
-                    // enabled (main.cpp:504-530 wires all_nat_cont there)
-                    bool native = false;
-                    if (go_on)
-                        for (int k = n0; k < n1; ++k) native |= d.nat_j[k] == j;
-                    if (native) continue;
-                    // quasi-adiabatic free pairs (update_free_pairs, free_pair.cpp:9-19),
-                    // j > i, minus pairs already in contact
-                    if (qa_on && j > i && qa) {
-                        bool in_contact = false;
-                        for (int k = 0; k < nref; ++k) {
-                            int s = d.qa.ref[(size_t)k * d.N + i];
-                            int other = d.qa.ct_i1[s] == i ? d.qa.ct_i2[s] : d.qa.ct_i1[s];
-                            in_contact |= other == j;
+    int cnt = 0, tcnt = 0;
+    while (todo) {
+        const int src = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const int q0 = __shfl_sync(FULL, kq0, src), q1 = __shfl_sync(FULL, kq1, src);
+        for (int qb = q0; qb < q1; qb += 32) {
+            const int q = qb + lane;
+            int flags = 0;
+            bool qa_free = false;
+            int j = -1;
+            if (q < q1) {
+                const float4 f = d.cell_pos[q];
+                j = __float_as_int(f.w);
+                float ddx = f.x - mx, ddy = f.y - my, ddz = f.z - mz;
+                if (periodic) {
+                    ddx = min_image_f(ddx, Lx);
+                    ddy = min_image_f(ddy, Ly);
+                    ddz = min_image_f(ddz, Lz);
+                }
+                const float d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+                if (j != i && d2 <= pre2) {
+                    const int2 cs = d.cell_cs[q];
+                    const int cj = cs.x, sj = cs.y;
+                    const int df = si > sj ? si - sj : sj - si;
+                    if (!(ci == cj && df < 3)) {
+                        bool in_req, pa, es, qa;
+                        if (in_band(Breq, d2) || (pauli_on && in_band(Bpa, d2)) || (es_on && in_band(Bes, d2)) ||
+                            (qa_on && in_band(Bqa, d2))) {
+                            const double dd = dist_exact(bx, pi, pos[j]);
+                            const double inv = __ddiv_rn(1.0, dd);
+                            in_req = dd < rp.req_r;
+                            pa = inv > rp.pauli_min_inv;
+                            es = inv > rp.es_min_inv;
+                            qa = inv > rp.qa_min_inv;
+                        } else {
+                            in_req = d2 < Breq.lo;
+                            pa = d2 < Bpa.lo;
+                            es = d2 < Bes.lo;
+                            qa = d2 < Bqa.lo;
                         }
-                        if (!in_contact) {
-                            if (tcnt < QA_TMP_CAP) d.qa.tmp[(size_t)tcnt * d.N + i] = j;
-                            ++tcnt;
+                        if (in_req) {
+                            if (pauli_on && pa) flags |= NL_PAULI;
+                            if (es_on && es && qi_w * narrow_f(pos[j].w) != 0.0f) flags |= NL_ES;
+                            qa_free = qa_on && j > i && qa;
+                            // the pair is a native contact: it leaves every list
+                            // (natives leave only with native contacts enabled,
+                            // main.cpp:504-530)
+                            if (go_on)
+                                for (int k = n0; k < n1; ++k)
+                                    if (d.nat_j[k] == j) { flags = 0; qa_free = false; }
+                            if (qa_free)
+                                for (int k = 0; k < nref; ++k) {
+                                    const int s = d.qa.ref[(size_t)k * d.N + i];
+                                    const int other = d.qa.ct_i1[s] == i ? d.qa.ct_i2[s] : d.qa.ct_i1[s];
+                                    if (other == j) qa_free = false;
+                                }
                         }
                     }
-                    int flags = 0;
-                    if (pauli_on && pa) flags |= NL_PAULI;
-                    if (es_on && es && pi.w * pos[j].w != 0.0) flags |= NL_ES;
-                    if (!flags) continue;
-                    if (cnt < cap) d.nl_row[(size_t)cnt * d.N + i] = j | flags;
-                    ++cnt;
                 }
             }
-    atomicMax(&d.ctr[1], (unsigned long long)cnt);   // longest row needed
-    if (cnt > cap) {
-        atomicOr(d.status, ST_CAPACITY);
-        cnt = cap;
+            const unsigned km = __ballot_sync(FULL, flags != 0);
+            if (flags) {
+                const int at = cnt + __popc(km & lt);
+                if (at < cap) d.nl_row[(size_t)at * d.N + i] = j | flags;
+            }
+            cnt += __popc(km);
+            if (qa_on) {
+                const unsigned qm = __ballot_sync(FULL, qa_free);
+                if (qa_free) {
+                    const int at = tcnt + __popc(qm & lt);
+                    if (at < QA_TMP_CAP) d.qa.tmp[(size_t)at * d.N + i] = j;
+                }
+                tcnt += __popc(qm);
+            }
+        }
     }
-    d.nl_cnt[i] = cnt;
-    d.orig[i] = pi;
-    if (qa_on) {
-        if (tcnt > QA_TMP_CAP) atomicOr(d.status, ST_CAPACITY);
-        d.qa.tmp_cnt[i] = min(tcnt, QA_TMP_CAP);
+    if (qa_on && tcnt > 1) {
+        // order the partners by j: each entry's rank is the number of smaller
+        // ones (partners are distinct beads)
+        const int m = min(tcnt, QA_TMP_CAP);
+        __syncwarp();
+        int vals[QA_TMP_CAP / 32];
+#pragma unroll
+        for (int u = 0; u < QA_TMP_CAP / 32; ++u) {
+            const int k = u * 32 + lane;
+            vals[u] = k < m ? d.qa.tmp[(size_t)k * d.N + i] : 0x7fffffff;
+        }
+        int rank[QA_TMP_CAP / 32];
+#pragma unroll
+        for (int u = 0; u < QA_TMP_CAP / 32; ++u) rank[u] = 0;
+        for (int k = 0; k < m; ++k) {
+            int v = 0;
+#pragma unroll
+            for (int u = 0; u < QA_TMP_CAP / 32; ++u)
+                if (k / 32 == u) v = __shfl_sync(FULL, vals[u], k & 31);
+#pragma unroll
+            for (int u = 0; u < QA_TMP_CAP / 32; ++u) rank[u] += v < vals[u];
+        }
+        __syncwarp();
+#pragma unroll
+        for (int u = 0; u < QA_TMP_CAP / 32; ++u) {
+            const int k = u * 32 + lane;
+            if (k < m) d.qa.tmp[(size_t)rank[u] * d.N + i] = vals[u];
+        }
+    }
+    if (lane == 0) {
+        atomicMax(&d.ctr[1], (unsigned long long)cnt);   // longest row needed
+        if (cnt > cap) {
+            atomicOr(d.status, ST_CAPACITY);
+            cnt = cap;
+        }
+        d.nl_cnt[i] = cnt;
+        d.orig[i] = pi;
+        if (qa_on) {
+            if (tcnt > QA_TMP_CAP) atomicOr(d.status, ST_CAPACITY);
+            d.qa.tmp_cnt[i] = min(tcnt, QA_TMP_CAP);
+        }
     }
 }
 
@@ -1188,6 +1310,7 @@ void Engine::remove_replica(int rep) {
         CK(cudaMemsetAsync(d.nl_cnt + b, 0, sizeof(int32_t) * n, stream));
         if (r.nat_len) CK(cudaMemsetAsync(d.nat_on + r.nat_off, 0, r.nat_len, stream));
         if (r.chunk_len) CK(cudaMemsetAsync(d.chunks + r.chunk_off, 0xff, sizeof(int2) * r.chunk_len, stream));
+        if (r.cell_len) CK(cudaMemsetAsync(d.cell_rep + r.cell_off, 0xff, sizeof(int32_t) * r.cell_len, stream));
         CK(cudaMemsetAsync(d.rep + rep, 0, sizeof(RepDev), stream));
         CK(cudaStreamSynchronize(stream));
         for (int i = 0; i < n; ++i) owner_h[b + i] = -1;
@@ -1350,6 +1473,7 @@ void Engine::finalize() {
             else cap.cells += std::max(64, 2 * r.n);
             if (params.on[XMD_TERM_QA]) {
                 cap.fp += r.n * QA_FP_PER_BEAD + 256;
+                cap.qab += (r.n + QA_BCHUNK - 1) / QA_BCHUNK;
                 cap.ct += r.n * QA_CT_PER_BEAD + 256;
             }
         }
@@ -1401,6 +1525,11 @@ void Engine::allocate() {
     d.cell_items = (int32_t *)dalloc(sizeof(int32_t) * N);
     d.bead_cell = (int32_t *)dalloc(sizeof(int32_t) * N);
     d.cell_pos = (float4 *)dalloc(sizeof(float4) * N);
+    d.bead_slot = (int32_t *)dalloc(sizeof(int32_t) * N);
+    d.cell_cs = (int2 *)dalloc(sizeof(int2) * N);
+    d.ncells = (int)cells;
+    d.cell_rep = (int32_t *)dalloc(sizeof(int32_t) * cells);
+    CK(cudaMemsetAsync(d.cell_rep, 0xff, sizeof(int32_t) * cells, stream));
     d.rng = (uint64_t *)dalloc(sizeof(uint64_t) * N);
     d.jump = (uint64_t *)dalloc(sizeof(uint64_t) * JUMP_WORDS * R);
     d.rep = (RepDev *)dalloc(sizeof(RepDev) * R);
@@ -1480,6 +1609,13 @@ void Engine::allocate() {
         q.ref = (int32_t *)dalloc(sizeof(int32_t) * QA_REF_CAP * (size_t)N);
         q.tmp_cnt = (int32_t *)dalloc(sizeof(int32_t) * N);
         q.tmp = (int32_t *)dalloc(sizeof(int32_t) * QA_TMP_CAP * (size_t)N);
+        q.tmp_off = (int32_t *)dalloc(sizeof(int32_t) * N);
+        q.nbchunk = std::max(1, cap.qab);
+        q.bchunk = (int2 *)dalloc(sizeof(int2) * q.nbchunk);
+        CK(cudaMemsetAsync(q.bchunk, 0, sizeof(int2) * q.nbchunk, stream));
+        q.bcsum = (int32_t *)dalloc(sizeof(int32_t) * q.nbchunk);
+        q.bcbase = (int32_t *)dalloc(sizeof(int32_t) * q.nbchunk);
+        qa_bchunk_next = 0;
         const int fp_total = std::max(1, cap.fp), ct_total = std::max(1, cap.ct);
         q.fp_total = fp_total;
         q.ct_total = ct_total;
@@ -1490,6 +1626,10 @@ void Engine::allocate() {
         q.cand_type = (int32_t *)dalloc(sizeof(int32_t) * fp_total);
         q.cand_d1 = (int32_t *)dalloc(sizeof(int32_t) * fp_total);
         q.cand_d2 = (int32_t *)dalloc(sizeof(int32_t) * fp_total);
+        const int nsift = (fp_total + QA_SIFT - 1) / QA_SIFT;
+        q.cand_list = (int32_t *)dalloc(sizeof(int32_t) * (size_t)nsift * QA_SIFT);
+        q.cand_blk = (int32_t *)dalloc(sizeof(int32_t) * nsift);
+        CK(cudaMemsetAsync(q.cand_blk, 0, sizeof(int32_t) * nsift, stream));
         q.ct_i1 = (int32_t *)dalloc(sizeof(int32_t) * ct_total);
         q.ct_i2 = (int32_t *)dalloc(sizeof(int32_t) * ct_total);
         q.ct_type = (int32_t *)dalloc(sizeof(int32_t) * ct_total);
@@ -1497,6 +1637,10 @@ void Engine::allocate() {
         q.ct_d2 = (int32_t *)dalloc(sizeof(int32_t) * ct_total);
         q.ct_status = (uint8_t *)dalloc(ct_total);
         q.ct_vac = (uint8_t *)dalloc(ct_total);
+        q.ct_rm = (uint8_t *)dalloc(ct_total);
+        CK(cudaMemsetAsync(q.ct_rm, 0, ct_total, stream));
+        q.ct_rep = (int32_t *)dalloc(sizeof(int32_t) * ct_total);
+        CK(cudaMemsetAsync(q.ct_rep, 0xff, sizeof(int32_t) * ct_total, stream));
         q.ct_ref = (double *)dalloc(sizeof(double) * ct_total);
         std::vector<double> req(4 + XMD_NUM_SS, 0.0), sd(XMD_NUM_SS), smin(XMD_NUM_SS), smax(XMD_NUM_SS);
         req[1] = p.lj_bb_r_min;
@@ -1642,6 +1786,10 @@ void Engine::place(int k) {
     up(d.nat_df + no, ndf.data(), sizeof(float) * ndf.size());
     CK(cudaMemsetAsync(d.nat_on + no, 0, nnat, stream));
     CK(cudaMemsetAsync(d.nl_cnt + b, 0, sizeof(int32_t) * n, stream));
+    if (ncell) {
+        std::vector<int32_t> cr(ncell, k);
+        up(d.cell_rep + co, cr.data(), sizeof(int32_t) * ncell);
+    }
     std::vector<int2> ch(nchunk);
     for (int c = 0; c < nchunk; ++c) ch[c] = make_int2(k, b + c * TL_CH);
     up(d.chunks + ho, ch.data(), sizeof(int2) * nchunk);
@@ -1667,6 +1815,16 @@ void Engine::place(int k) {
         rd.ct_cap = nct;
         std::vector<int32_t> fprep(nfp, k), sy(n);
         up(d.qa.fp_rep + fo, fprep.data(), sizeof(int32_t) * nfp);
+        std::vector<int32_t> ctrep(nct, k);
+        up(d.qa.ct_rep + to, ctrep.data(), sizeof(int32_t) * nct);
+        const int nbc = (n + QA_BCHUNK - 1) / QA_BCHUNK;
+        if (qa_bchunk_next + nbc > d.qa.nbchunk) throw std::logic_error("engine: QA chunk table full");
+        std::vector<int2> bch(nbc);
+        for (int c = 0; c < nbc; ++c) bch[c] = make_int2(k, b + c * QA_BCHUNK);
+        up(d.qa.bchunk + qa_bchunk_next, bch.data(), sizeof(int2) * nbc);
+        rd.qa_bchunk_off = qa_bchunk_next;
+        rd.qa_nbchunk = nbc;
+        qa_bchunk_next += nbc;
         // valences start at the residue limits (intended main.cpp:662-672)
         for (int i = 0; i < n; ++i) {
             const int32_t *lim = p.limits[r.atype[i]];
@@ -1837,15 +1995,25 @@ void Engine::record(std::vector<cudaEvent_t> &pool, size_t &n) {
 void Engine::launch_rebuild() {
     if (timing) record(ev_rebuild, n_ev_rebuild);
     if (any_cell) {
+        const int gb = (d.N + 255) / 256;
         k_cells<<<d.R, CB, 0, stream>>>(d, cur);
-        k_nl_build<<<(d.N + 127) / 128, 128, 0, stream>>>(d, tp, cur);
+        k_cell_count<<<gb, 256, 0, stream>>>(d, cur);
+        k_cell_scan<<<d.R, CB, 0, stream>>>(d);
+        k_cell_scatter<<<gb, 256, 0, stream>>>(d);
+        k_cell_finish<<<(d.ncells + CF_WARPS - 1) / CF_WARPS, CF_WARPS * 32, 0, stream>>>(d, cur);
+        k_nl_cells<<<(d.N + NC_WARPS - 1) / NC_WARPS, NC_WARPS * 32, 0, stream>>>(d, tp, cur);
     }
     if (any_tile) k_nl_tile<<<tile_grid, TL_THREADS, tile_smem, stream>>>(d, tp, cur);
-    if (d.qa_on) k_qa_rebuild<<<d.R, 1024, 0, stream>>>(d);
+    if (d.qa_on) {
+        k_qa_fp_scan<<<d.qa.nbchunk, QA_BCHUNK, 0, stream>>>(d);
+        k_qa_fp_base<<<d.R, 1024, 0, stream>>>(d);
+        k_qa_fp_fill<<<d.qa.nbchunk, QA_BCHUNK, 0, stream>>>(d);
+        k_qa_compact<<<d.R, 1024, 0, stream>>>(d);
+    }
     if (timing) record(ev_rebuild, n_ev_rebuild);
 }
 
-// Grow the Verlet rows when the longest row needed (recorded by k_nl_build)
+// Grow the Verlet rows when the longest row needed (recorded by the builds)
 // reaches `frac` of the capacity.  Returns true when the rows were
 // reallocated (lists must then be rebuilt; captured graphs are dropped).
 bool Engine::grow_rows(double frac) {
@@ -1913,9 +2081,13 @@ void Engine::launch_force_step() {
     ++launches;
     if (d.qa_on) {
         // sift + acceptance + transitions at this step's positions (qa.cpp:20-31)
-        k_qa_sift<<<(d.qa.fp_total + 255) / 256, 256, 0, stream>>>(d, tp, cur);
+        k_qa_sift<<<(d.qa.fp_total + QA_SIFT - 1) / QA_SIFT, QA_SIFT, 0, stream>>>(d, tp, cur);
         k_qa_step<<<d.R, 1024, 0, stream>>>(d, tp, cur);
-        launches += 2;
+        const int gc = (d.qa.ct_total + 255) / 256;
+        k_qa_trans<<<gc, 256, 0, stream>>>(d, tp, cur);
+        k_qa_refree<<<d.R, 1024, 0, stream>>>(d);
+        k_qa_refs<<<gc, 256, 0, stream>>>(d);
+        launches += 5;
     }
 }
 
@@ -1954,17 +2126,35 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
             cudaKernelNodeParams ks{}, kq{};
             void *sargs[] = {&d, &tp, &c};
             ks.func = (void *)k_qa_sift;
-            ks.gridDim = dim3((d.qa.fp_total + 255) / 256);
-            ks.blockDim = dim3(256);
+            ks.gridDim = dim3((d.qa.fp_total + QA_SIFT - 1) / QA_SIFT);
+            ks.blockDim = dim3(QA_SIFT);
             ks.kernelParams = sargs;
             kq.func = (void *)k_qa_step;
             kq.gridDim = dim3(d.R);
             kq.blockDim = dim3(1024);
             kq.kernelParams = sargs;
-            cudaGraphNode_t n1, n2;
+            cudaKernelNodeParams kt{}, kr{}, kf2{};
+            void *dargs[] = {&d};
+            const unsigned gc = (unsigned)((d.qa.ct_total + 255) / 256);
+            kt.func = (void *)k_qa_trans;
+            kt.gridDim = dim3(gc);
+            kt.blockDim = dim3(256);
+            kt.kernelParams = sargs;
+            kr.func = (void *)k_qa_refree;
+            kr.gridDim = dim3(d.R);
+            kr.blockDim = dim3(1024);
+            kr.kernelParams = dargs;
+            kf2.func = (void *)k_qa_refs;
+            kf2.gridDim = dim3(gc);
+            kf2.blockDim = dim3(256);
+            kf2.kernelParams = dargs;
+            cudaGraphNode_t n1, n2, n3, n4, n5;
             CK(cudaGraphAddKernelNode(&n1, g, &nf, 1, &ks));
             CK(cudaGraphAddKernelNode(&n2, g, &n1, 1, &kq));
-            nf = n2;
+            CK(cudaGraphAddKernelNode(&n3, g, &n2, 1, &kt));
+            CK(cudaGraphAddKernelNode(&n4, g, &n3, 1, &kr));
+            CK(cudaGraphAddKernelNode(&n5, g, &n4, 1, &kf2));
+            nf = n5;
         }
         if (fuse) {
             nc = nf;
@@ -2003,15 +2193,36 @@ void Engine::add_rebuild_nodes(cudaGraph_t body, int cn) {
     void *a2[] = {&d, &tp, &cn};
     void *a3[] = {&d};
     if (any_cell) {
-        cudaKernelNodeParams k1{}, k2{};
+        cudaKernelNodeParams k1{}, k2{}, kc{}, ks{}, kx{}, kf{};
         k1.func = (void *)k_cells;
         k1.gridDim = dim3(d.R);
         k1.blockDim = dim3(CB);
         k1.kernelParams = a1;
         add(k1);
-        k2.func = (void *)k_nl_build;
-        k2.gridDim = dim3((d.N + 127) / 128);
-        k2.blockDim = dim3(128);
+        const unsigned gb = (unsigned)((d.N + 255) / 256);
+        kc.func = (void *)k_cell_count;
+        kc.gridDim = dim3(gb);
+        kc.blockDim = dim3(256);
+        kc.kernelParams = a1;
+        add(kc);
+        ks.func = (void *)k_cell_scan;
+        ks.gridDim = dim3(d.R);
+        ks.blockDim = dim3(CB);
+        ks.kernelParams = a3;
+        add(ks);
+        kx.func = (void *)k_cell_scatter;
+        kx.gridDim = dim3(gb);
+        kx.blockDim = dim3(256);
+        kx.kernelParams = a3;
+        add(kx);
+        kf.func = (void *)k_cell_finish;
+        kf.gridDim = dim3((unsigned)((d.ncells + CF_WARPS - 1) / CF_WARPS));
+        kf.blockDim = dim3(CF_WARPS * 32);
+        kf.kernelParams = a1;
+        add(kf);
+        k2.func = (void *)k_nl_cells;
+        k2.gridDim = dim3((d.N + NC_WARPS - 1) / NC_WARPS);
+        k2.blockDim = dim3(NC_WARPS * 32);
         k2.kernelParams = a2;
         add(k2);
     }
@@ -2025,12 +2236,27 @@ void Engine::add_rebuild_nodes(cudaGraph_t body, int cn) {
         add(kt);
     }
     if (d.qa_on) {
-        cudaKernelNodeParams k3{};
-        k3.func = (void *)k_qa_rebuild;
-        k3.gridDim = dim3(d.R);
-        k3.blockDim = dim3(1024);
+        cudaKernelNodeParams k3{}, k4{}, k5{}, k6{};
+        k3.func = (void *)k_qa_fp_scan;
+        k3.gridDim = dim3(d.qa.nbchunk);
+        k3.blockDim = dim3(QA_BCHUNK);
         k3.kernelParams = a3;
         add(k3);
+        k4.func = (void *)k_qa_fp_base;
+        k4.gridDim = dim3(d.R);
+        k4.blockDim = dim3(1024);
+        k4.kernelParams = a3;
+        add(k4);
+        k5.func = (void *)k_qa_fp_fill;
+        k5.gridDim = dim3(d.qa.nbchunk);
+        k5.blockDim = dim3(QA_BCHUNK);
+        k5.kernelParams = a3;
+        add(k5);
+        k6.func = (void *)k_qa_compact;
+        k6.gridDim = dim3(d.R);
+        k6.blockDim = dim3(1024);
+        k6.kernelParams = a3;
+        add(k6);
     }
 }
 
@@ -2073,7 +2299,7 @@ void Engine::step(int nsteps) {
             // per step: the step kernel (plus the separate check and the
             // quasi-adiabatic kernels with that term); rebuild kernels are
             // counted per pass in stats()
-            launches += (d.qa_on ? 4 : 1) * GRAPH_STEPS;
+            launches += (d.qa_on ? 7 : 1) * GRAPH_STEPS;
             md_steps += GRAPH_STEPS;
         }
     }
@@ -2163,7 +2389,7 @@ void Engine::stats(int64_t *out) {
     unsigned long long passes = 0;
     CK(cudaMemcpyAsync(&passes, d.ctr, sizeof(passes), cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
-    out[XMD_STAT_LAUNCHES] = launches + (int64_t)((any_cell ? 2 : 0) + (any_tile ? 1 : 0) + (d.qa_on ? 1 : 0)) * (int64_t)passes;
+    out[XMD_STAT_LAUNCHES] = launches + (int64_t)((any_cell ? 6 : 0) + (any_tile ? 1 : 0) + (d.qa_on ? 4 : 0)) * (int64_t)passes;
     for (int i = 0; i < d.N; ++i)
         if (owner_h[i] >= 0) out[XMD_STAT_NL_ENTRIES] += cnt[i];
     for (int k = 0; k < nn; ++k) out[XMD_STAT_GO_ACTIVE] += on[k];

@@ -36,6 +36,8 @@ struct RepDev {
     int tile;                // Verlet build by whole-replica tiles (no cell grid)
     float pre2;              // squared FP32 pre-filter radius of the Verlet build
     double band_m;           // FP32 distance error bound of the cell build
+    float band_lo[4], band_hi[4];   // cell build: FP32 bands of the list radius, r_excl + pad, 2D + pad, QA radius + pad
+    float band_mf;           // band_m rounded up to FP32
     int first, rebuild;
     int chunk_off, nchunk;   // tile-build chunks of the replica in Dev::chunks
     int active;              // slot holds a placed replica
@@ -45,6 +47,7 @@ struct RepDev {
     // quasi-adiabatic lists: free pairs [fp_off, fp_off + fp_n) of capacity
     // fp_cap, contacts [ct_off, ct_off + ct_n) of capacity ct_cap
     int fp_off, fp_cap, fp_n;
+    int qa_bchunk_off, qa_nbchunk;   // chunks of QA_BCHUNK beads in QaDev::bchunk
     int ct_off, ct_cap, ct_n;
 };
 
@@ -52,6 +55,8 @@ constexpr int QA_REF_CAP = 16;   // contacts per bead (valence bounds it by 10)
 constexpr int QA_TMP_CAP = 256;  // free-pair partners j > i per bead at a rebuild
 constexpr int QA_FP_PER_BEAD = 96;   // free-pair slots per bead of a replica (+256)
 constexpr int QA_CT_PER_BEAD = 8;    // contact slots per bead of a replica (+256)
+constexpr int QA_SIFT = 256;         // free-pair slots per block of the candidate sift
+constexpr int QA_BCHUNK = 1024;      // beads per chunk of the free-pair re-listing
 
 // device record of the quasi-adiabatic state
 struct QaDev {
@@ -59,11 +64,18 @@ struct QaDev {
     int32_t *sync;               // [N] packed int8 x4: back | side_all | side_polar | side_hydrophobic
     int32_t *ref_cnt, *ref;      // [N], [QA_REF_CAP][N] contact slots per bead
     int32_t *tmp_cnt, *tmp;      // [N], [QA_TMP_CAP][N] partners collected at a rebuild
+    int32_t *tmp_off;            // [N] offset of a bead's partners within its chunk
+    int2 *bchunk;                // (replica, first bead) of each chunk of QA_BCHUNK beads
+    int32_t *bcsum, *bcbase;     // per chunk: partners, first free-pair slot
+    int nbchunk;
     int32_t *fp_i1, *fp_i2, *fp_rep;   // free-pair slots
     uint8_t *fp_vac;
     int32_t *cand_type, *cand_d1, *cand_d2;   // per free-pair slot, 0 = not a candidate
+    int32_t *cand_list, *cand_blk;   // per sift block of QA_SIFT slots: its candidates in slot order, their count
     int32_t *ct_i1, *ct_i2, *ct_type, *ct_d1, *ct_d2;
     uint8_t *ct_status, *ct_vac;
+    uint8_t *ct_rm;              // removed at this step (re-freed by k_qa_refree)
+    int32_t *ct_rep;             // contact slot -> replica owning it
     double *ct_ref;
     const double *req_min_dist;  // [404] by contact type (main.cpp:681-697)
     const double *ss_depth, *ss_rmin, *ss_rmax;   // [400] ss potentials (lj_variants.cpp)
@@ -94,6 +106,10 @@ struct Dev {
     int32_t *nl_row, *nl_cnt;
     int32_t *cell_cnt, *cell_start, *cell_fill, *cell_items, *bead_cell;
     float4 *cell_pos;       // bucket-sorted FP32 coordinates (+ bead index bits)
+    int32_t *bead_slot;     // bead -> its slot in cell_pos
+    int2 *cell_cs;          // (chain, sequence index) of each slot of cell_pos
+    int32_t *cell_rep;      // bucket of the pool -> replica owning it (-1: free)
+    int ncells;             // buckets in the pool
     uint64_t *rng;          // per-bead generator state
     uint64_t *jump;         // [R][16][16] nibble tables of the GF(2) jump (4 N_r draws)
     RepDev *rep;
@@ -258,11 +274,12 @@ private:
     void drop_graphs();
 
     struct Caps {
-        int beads = 0, reps = 0, nat = 0, cells = 0, chunks = 0, fp = 0, ct = 0;
+        int beads = 0, reps = 0, nat = 0, cells = 0, chunks = 0, fp = 0, ct = 0, qab = 0;
     } cap;
     bool dynamic = false;
     size_t bytes = 0;                          // device memory held
     RangeAlloc a_beads, a_nat, a_cells, a_chunks, a_fp, a_ct;
+    int qa_bchunk_next = 0;   // next free chunk of the QA re-listing (static contexts)
     std::vector<int32_t> owner_h;              // bead slot -> replica (or -1)
     void allocate();
     void place(int k);

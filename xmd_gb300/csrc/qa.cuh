@@ -97,16 +97,18 @@ __device__ __forceinline__ int block_exscan(int v, int *out, int *s_warp) {
 }
 
 // ---- sift_candidates::iter (sift_candidates.cpp:15-77), one thread per slot ----
-__global__ void __launch_bounds__(256) k_qa_sift(Dev d, TermP p, int cur) {
+// Each block also lists its candidates in slot order (cand_list, cand_blk),
+// so the acceptance visits candidates instead of every free-pair slot.
+__global__ void __launch_bounds__(QA_SIFT) k_qa_sift(Dev d, TermP p, int cur) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     const QaDev &q = d.qa;
-    if (slot >= q.fp_total) return;
-    const int r = q.fp_rep[slot];
+    bool live = slot < q.fp_total;
+    const int r = live ? q.fp_rep[slot] : 0;
     const RepDev &rp = d.rep[r];
-    if (slot - rp.fp_off >= rp.fp_n) return;
+    live = live && slot - rp.fp_off < rp.fp_n;
     int type = 0;
     int32_t d1p = 0, d2p = 0;
-    if (!q.fp_vac[slot]) {
+    if (live && !q.fp_vac[slot]) {
         const int i1 = q.fp_i1[slot], i2 = q.fp_i2[slot];
         const double4_32a *pos = d.pos[cur];
         D3 r12 = d3ruv(rp.box, pos[i1], pos[i2]);
@@ -134,15 +136,30 @@ __global__ void __launch_bounds__(256) k_qa_sift(Dev d, TermP p, int cur) {
             if (!sync_ok_after(q.sync[i1], d1p) || !sync_ok_after(q.sync[i2], d2p)) type = 0;
         }
     }
-    q.cand_type[slot] = type;
-    q.cand_d1[slot] = d1p;
-    q.cand_d2[slot] = d2p;
+    if (live) {
+        q.cand_type[slot] = type;
+        q.cand_d1[slot] = d1p;
+        q.cand_d2[slot] = d2p;
+    }
+    // ordered compaction of the block's candidates
+    __shared__ int s_wc[QA_SIFT / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned bal = __ballot_sync(0xffffffffu, type != 0);
+    if (lane == 0) s_wc[w] = __popc(bal);
+    __syncthreads();
+    int before = 0, total = 0;
+#pragma unroll
+    for (int k = 0; k < QA_SIFT / 32; ++k) {
+        before += k < w ? s_wc[k] : 0;
+        total += s_wc[k];
+    }
+    if (type != 0) q.cand_list[(size_t)blockIdx.x * QA_SIFT + before + __popc(bal & ((1u << lane) - 1u))] = slot;
+    if (threadIdx.x == 0) q.cand_blk[blockIdx.x] = total;
 }
 
-// ---- acceptance, contact transitions and per-bead references: block/replica ----
-// process_candidates::iter (process_candidates.cpp:10-29) in candidate order,
-// then process_contacts::iter's state part (process_contacts.cpp:42-56) in
-// contact-slot order.
+// ---- acceptance: process_candidates::iter (process_candidates.cpp:10-29) in
+// candidate order, one block per replica (the greedy choice of shared
+// valences is sequential); the transitions follow in k_qa_trans.
 __global__ void __launch_bounds__(1024) k_qa_step(Dev d, TermP p, int cur) {
     const int r = blockIdx.x, t = threadIdx.x;
     RepDev &rp = d.rep[r];
@@ -155,24 +172,41 @@ __global__ void __launch_bounds__(1024) k_qa_step(Dev d, TermP p, int cur) {
     const double tnow = rp.t;
     const int fp_off = rp.fp_off, ct_off = rp.ct_off;
     const int fp_n0 = s_fp_n;
-    // 1. greedy acceptance in free-pair slot order
-    for (int base = 0; base < fp_n0; base += 1024) {
-        int slot = fp_off + base + t;
-        int flag = (base + t < fp_n0) && q.cand_type[slot] != 0;
+    // 1. greedy acceptance in free-pair slot order, over the sift blocks'
+    //    ordered candidate lists (slots outside this replica's live range are
+    //    skipped: blocks at the edges are shared)
+    __shared__ int s_i1[1024], s_i2[1024], s_d1[1024], s_d2[1024], s_ty[1024];
+    const int sb0 = fp_off / QA_SIFT, sb1 = (fp_off + fp_n0 + QA_SIFT - 1) / QA_SIFT;
+    for (int bb = sb0; bb < sb1; bb += 1024) {
+        const int blk = bb + t;
+        const int cnt = blk < sb1 ? q.cand_blk[blk] : 0;
         int pos;
-        int total = block_exscan(flag, &pos, s_warp);
-        if (flag) s_slots[pos] = slot;
+        const int total = block_exscan(cnt, &pos, s_warp);
+        for (int g0 = 0; g0 < total; g0 += 1024) {
+        // gather candidates [g0, g0 + 1024) of this round with their data
+        for (int k = max(0, g0 - pos); k < cnt && pos + k < g0 + 1024; ++k) {
+            const int s = q.cand_list[(size_t)blk * QA_SIFT + k];
+            const int o = pos + k - g0;
+            const bool mine = s >= fp_off && s < fp_off + fp_n0;
+            s_slots[o] = mine ? s : -1;
+            if (mine) {
+                s_i1[o] = q.fp_i1[s]; s_i2[o] = q.fp_i2[s];
+                s_d1[o] = q.cand_d1[s]; s_d2[o] = q.cand_d2[s]; s_ty[o] = q.cand_type[s];
+            }
+        }
         __syncthreads();
         if (t == 0) {
-            for (int k = 0; k < total; ++k) {
+            const int m = min(1024, total - g0);
+            for (int k = 0; k < m; ++k) {
                 int s = s_slots[k];
-                int i1 = q.fp_i1[s], i2 = q.fp_i2[s];
-                int32_t d1p = q.cand_d1[s], d2p = q.cand_d2[s];
+                if (s < 0) continue;
+                int i1 = s_i1[k], i2 = s_i2[k];
+                int32_t d1p = s_d1[k], d2p = s_d2[k];
                 int32_t y1 = q.sync[i1], y2 = q.sync[i2];
                 if (sync_ok_after(y1, d1p) && sync_ok_after(y2, d2p)) {
                     if (s_ct_n >= rp.ct_cap) { s_err = 1; break; }
                     int c = ct_off + s_ct_n++;
-                    q.ct_i1[c] = i1; q.ct_i2[c] = i2; q.ct_type[c] = q.cand_type[s];
+                    q.ct_i1[c] = i1; q.ct_i2[c] = i2; q.ct_type[c] = s_ty[k];
                     q.ct_status[c] = QA_FORMING; q.ct_ref[c] = tnow; q.ct_vac[c] = 0;
                     q.ct_d1[c] = d1p; q.ct_d2[c] = d2p;
                     q.sync[i1] = y1 - d1p;   // bytes never borrow: each stays >= 0
@@ -182,38 +216,67 @@ __global__ void __launch_bounds__(1024) k_qa_step(Dev d, TermP p, int cur) {
             }
         }
         __syncthreads();
-    }
-    // 2. transitions in contact-slot order; removals re-free the pair at the
-    //    end of the free-pair list, in slot order
-    const int ct_n = s_ct_n;
-    for (int base = 0; base < ct_n; base += 1024) {
-        int slot = ct_off + base + t;
-        int removed = 0;
-        if (base + t < ct_n && !q.ct_vac[slot]) {
-            int i1 = q.ct_i1[slot], i2 = q.ct_i2[slot];
-            D3 r12 = d3ruv(rp.box, d.pos[cur][i1], d.pos[cur][i2]);
-            double r12_rn = __ddiv_rn(1.0, __dsqrt_rn(d3dot(r12, r12)));
-            int status = q.ct_status[slot];
-            double sat = __dmul_rn(fmin(__dsub_rn(tnow, q.ct_ref[slot]), p.qa_cycle), p.qa_cycle_inv);
-            if (status == QA_BREAKING) sat = __dsub_rn(1.0, sat);
-            double depth, rmin, rmax;
-            qa_lj(p, q, q.ct_type[slot], &depth, &rmin, &rmax);
-            if (status == QA_FORMING && sat == 1.0) {
-                if (__dmul_rn(__dmul_rn(p.qa_factor, rmin), r12_rn) < 1.0) {
-                    q.ct_status[slot] = QA_BREAKING;
-                    q.ct_ref[slot] = tnow;
-                }
-            } else if (status == QA_BREAKING && sat == 0.0) {
-                q.ct_vac[slot] = 1;
-                atomicAdd(&q.sync[i1], q.ct_d1[slot]);   // bytes stay <= 127: no carry
-                atomicAdd(&q.sync[i2], q.ct_d2[slot]);
-                removed = 1;
-            }
         }
+    }
+    __syncthreads();
+    if (t == 0) rp.ct_n = s_ct_n;
+    if (t == 0 && s_err) atomicOr(d.status, 4);
+}
+
+// ---- process_contacts::iter, state part (process_contacts.cpp:42-56) -----------
+// One thread per contact slot of the pool: saturation, forming -> breaking,
+// and removal (valence returned, slot vacated, flagged for re-freeing).
+// Contacts accepted at this step have saturation 0 and stay as they are.
+__global__ void __launch_bounds__(256) k_qa_trans(Dev d, TermP p, int cur) {
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    const QaDev &q = d.qa;
+    if (slot >= q.ct_total) return;
+    q.ct_rm[slot] = 0;
+    const int r = q.ct_rep[slot];
+    if (r < 0) return;
+    const RepDev &rp = d.rep[r];
+    if (!rp.active || slot - rp.ct_off >= rp.ct_n || q.ct_vac[slot]) return;
+    const double tnow = rp.t;
+    const int i1 = q.ct_i1[slot], i2 = q.ct_i2[slot];
+    D3 r12 = d3ruv(rp.box, d.pos[cur][i1], d.pos[cur][i2]);
+    double r12_rn = __ddiv_rn(1.0, __dsqrt_rn(d3dot(r12, r12)));
+    int status = q.ct_status[slot];
+    double sat = __dmul_rn(fmin(__dsub_rn(tnow, q.ct_ref[slot]), p.qa_cycle), p.qa_cycle_inv);
+    if (status == QA_BREAKING) sat = __dsub_rn(1.0, sat);
+    double depth, rmin, rmax;
+    qa_lj(p, q, q.ct_type[slot], &depth, &rmin, &rmax);
+    if (status == QA_FORMING && sat == 1.0) {
+        if (__dmul_rn(__dmul_rn(p.qa_factor, rmin), r12_rn) < 1.0) {
+            q.ct_status[slot] = QA_BREAKING;
+            q.ct_ref[slot] = tnow;
+        }
+    } else if (status == QA_BREAKING && sat == 0.0) {
+        q.ct_vac[slot] = 1;
+        atomicAdd(&q.sync[i1], q.ct_d1[slot]);   // bytes stay <= 127: no carry
+        atomicAdd(&q.sync[i2], q.ct_d2[slot]);
+        q.ct_rm[slot] = 1;
+    }
+}
+
+// Removed pairs re-freed at the end of the free-pair list in contact-slot
+// order (process_contacts.cpp:48-55), and the per-bead contact lists cleared.
+__global__ void __launch_bounds__(1024) k_qa_refree(Dev d) {
+    const int r = blockIdx.x, t = threadIdx.x;
+    RepDev &rp = d.rep[r];
+    if (!rp.active || rp.ct_cap == 0) return;
+    const QaDev &q = d.qa;
+    __shared__ int s_warp[33];
+    __shared__ int s_fp_n, s_err;
+    if (t == 0) { s_fp_n = rp.fp_n; s_err = 0; }
+    __syncthreads();
+    const int fp_off = rp.fp_off, ct_off = rp.ct_off, ct_n = rp.ct_n;
+    for (int base = 0; base < ct_n; base += 1024) {
+        const int slot = ct_off + base + t;
+        const int removed = base + t < ct_n ? q.ct_rm[slot] : 0;
         int pos;
-        int total = block_exscan(removed, &pos, s_warp);
+        const int total = block_exscan(removed, &pos, s_warp);
         if (removed) {
-            int fs = fp_off + s_fp_n + pos;
+            const int fs = fp_off + s_fp_n + pos;
             if (s_fp_n + pos < rp.fp_cap) {
                 q.fp_i1[fs] = q.ct_i1[slot];
                 q.fp_i2[fs] = q.ct_i2[slot];
@@ -226,71 +289,107 @@ __global__ void __launch_bounds__(1024) k_qa_step(Dev d, TermP p, int cur) {
         if (t == 0) s_fp_n = min(s_fp_n + total, rp.fp_cap);
         __syncthreads();
     }
-    // 3. per-bead contact references
     for (int i = rp.begin + t; i < rp.begin + rp.n; i += 1024) q.ref_cnt[i] = 0;
     __syncthreads();
-    for (int base = 0; base < ct_n; base += 1024) {
-        int slot = ct_off + base + t;
-        if (base + t < ct_n && !q.ct_vac[slot]) {
-            int i1 = q.ct_i1[slot], i2 = q.ct_i2[slot];
-            int k1 = atomicAdd(&q.ref_cnt[i1], 1), k2 = atomicAdd(&q.ref_cnt[i2], 1);
-            if (k1 < QA_REF_CAP) q.ref[(size_t)k1 * d.N + i1] = slot; else s_err = 1;
-            if (k2 < QA_REF_CAP) q.ref[(size_t)k2 * d.N + i2] = slot; else s_err = 1;
-        }
-    }
-    __syncthreads();
     if (t == 0) {
-        rp.ct_n = s_ct_n;
         rp.fp_n = s_fp_n;
         if (s_err) atomicOr(d.status, 4);
     }
 }
 
-// ---- after a Verlet rebuild: free pairs re-listed, contacts compacted -----------
+// per-bead contact references, one thread per contact slot of the pool
+__global__ void __launch_bounds__(256) k_qa_refs(Dev d) {
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    const QaDev &q = d.qa;
+    if (slot >= q.ct_total) return;
+    const int r = q.ct_rep[slot];
+    if (r < 0) return;
+    const RepDev &rp = d.rep[r];
+    if (!rp.active || slot - rp.ct_off >= rp.ct_n || q.ct_vac[slot]) return;
+    const int i1 = q.ct_i1[slot], i2 = q.ct_i2[slot];
+    const int k1 = atomicAdd(&q.ref_cnt[i1], 1), k2 = atomicAdd(&q.ref_cnt[i2], 1);
+    if (k1 < QA_REF_CAP) q.ref[(size_t)k1 * d.N + i1] = slot;
+    if (k2 < QA_REF_CAP) q.ref[(size_t)k2 * d.N + i2] = slot;
+    if (k1 >= QA_REF_CAP || k2 >= QA_REF_CAP) atomicOr(d.status, 4);
+}
+
+// ---- after a Verlet rebuild: the free-pair list re-listed ------------------------
 // update_free_pairs (free_pair.cpp:6-21): non-native list pairs within
 // max_formation_min_dist + pad, in (i1, i2) order, minus pairs in contact.
-__global__ void __launch_bounds__(1024) k_qa_rebuild(Dev d) {
+// The builds leave each bead's partners in ascending j (tmp rows); the list
+// is their concatenation in bead order, placed by a scan over chunks of
+// QA_BCHUNK beads of each replica (grid-wide: the writes are spread over
+// every SM).
+__global__ void __launch_bounds__(QA_BCHUNK) k_qa_fp_scan(Dev d) {
+    const QaDev &q = d.qa;
+    const int2 ch = q.bchunk[blockIdx.x];
+    const RepDev &rp = d.rep[ch.x];
+    if (!rp.active || !rp.rebuild) return;
+    __shared__ int s_warp[33];
+    const int i = ch.y + threadIdx.x, end = rp.begin + rp.n;
+    const int cnt = i < end ? min(q.tmp_cnt[i], QA_TMP_CAP) : 0;
+    int pos;
+    const int total = block_exscan(cnt, &pos, s_warp);
+    if (i < end) q.tmp_off[i] = pos;
+    if (threadIdx.x == 0) q.bcsum[blockIdx.x] = total;
+}
+__global__ void __launch_bounds__(1024) k_qa_fp_base(Dev d) {
     const int r = blockIdx.x, t = threadIdx.x;
     RepDev &rp = d.rep[r];
-    if (!rp.rebuild) return;
+    if (!rp.active || !rp.rebuild) return;
     const QaDev &q = d.qa;
     __shared__ int s_warp[33];
-    __shared__ int s_base, s_err;
-    if (t == 0) { s_base = 0; s_err = 0; }
+    __shared__ int s_run;
+    if (t == 0) s_run = 0;
     __syncthreads();
-    const int b = rp.begin, n = rp.n, fp_off = rp.fp_off;
-    for (int c0 = 0; c0 < n; c0 += 1024) {
-        int i = b + c0 + t;
-        int cnt = (c0 + t < n) ? min(q.tmp_cnt[i], QA_TMP_CAP) : 0;
+    const int off = rp.qa_bchunk_off, nb = rp.qa_nbchunk;
+    for (int base = 0; base < nb; base += 1024) {
+        const int c = base + t;
+        const int v = c < nb ? q.bcsum[off + c] : 0;
         int pos;
-        int total = block_exscan(cnt, &pos, s_warp);
-        if (cnt) {
-            int loc[QA_TMP_CAP];
-            for (int k = 0; k < cnt; ++k) loc[k] = q.tmp[(size_t)k * d.N + i];
-            for (int x = 1; x < cnt; ++x) {   // ascending j
-                int v = loc[x], y = x - 1;
-                while (y >= 0 && loc[y] > v) { loc[y + 1] = loc[y]; --y; }
-                loc[y + 1] = v;
-            }
-            for (int k = 0; k < cnt; ++k) {
-                int o = s_base + pos + k;
-                if (o < rp.fp_cap) {
-                    q.fp_i1[fp_off + o] = i;
-                    q.fp_i2[fp_off + o] = loc[k];
-                    q.fp_vac[fp_off + o] = 0;
-                } else {
-                    s_err = 1;
-                }
-            }
-        }
+        const int total = block_exscan(v, &pos, s_warp);
+        if (c < nb) q.bcbase[off + c] = s_run + pos;
         __syncthreads();
-        if (t == 0) s_base += total;
+        if (t == 0) s_run += total;
         __syncthreads();
     }
-    if (t == 0) rp.fp_n = min(s_base, rp.fp_cap);
-    // in-place ordered compaction of the contact slots
-    const int ct_off = rp.ct_off, ct_n = rp.ct_n;
+    if (t == 0) {
+        if (s_run > rp.fp_cap) atomicOr(d.status, 4);
+        rp.fp_n = min(s_run, rp.fp_cap);
+    }
+}
+__global__ void __launch_bounds__(QA_BCHUNK) k_qa_fp_fill(Dev d) {
+    const QaDev &q = d.qa;
+    const int2 ch = q.bchunk[blockIdx.x];
+    const RepDev &rp = d.rep[ch.x];
+    if (!rp.active || !rp.rebuild) return;
+    const int i = ch.y + threadIdx.x;
+    if (i >= rp.begin + rp.n) return;
+    const int cnt = min(q.tmp_cnt[i], QA_TMP_CAP);
+    const int o0 = q.bcbase[blockIdx.x] + q.tmp_off[i];
+    for (int k = 0; k < cnt; ++k) {
+        const int o = o0 + k;
+        if (o < rp.fp_cap) {
+            q.fp_i1[rp.fp_off + o] = i;
+            q.fp_i2[rp.fp_off + o] = q.tmp[(size_t)k * d.N + i];
+            q.fp_vac[rp.fp_off + o] = 0;
+        }
+    }
+}
+
+// Contact slots compacted in order when the replica's region is three
+// quarters used (tombstones of removed contacts accumulate between; the order
+// of the live contacts, which decides transitions and re-freeing, is kept),
+// with the per-bead references rebuilt for the moved slots.
+__global__ void __launch_bounds__(1024) k_qa_compact(Dev d) {
+    const int r = blockIdx.x, t = threadIdx.x;
+    RepDev &rp = d.rep[r];
+    if (!rp.active || !rp.rebuild || 4 * rp.ct_n <= 3 * rp.ct_cap) return;
+    const QaDev &q = d.qa;
+    __shared__ int s_warp[33];
     __shared__ int s_out;
+    const int b = rp.begin, n = rp.n;
+    const int ct_off = rp.ct_off, ct_n = rp.ct_n;
     if (t == 0) s_out = 0;
     __syncthreads();
     for (int base = 0; base < ct_n; base += 1024) {
@@ -325,10 +424,7 @@ __global__ void __launch_bounds__(1024) k_qa_rebuild(Dev d) {
         if (k2 < QA_REF_CAP) q.ref[(size_t)k2 * d.N + i2] = slot;
     }
     __syncthreads();
-    if (t == 0) {
-        rp.ct_n = nct;
-        if (s_err) atomicOr(d.status, 4);
-    }
+    if (t == 0) rp.ct_n = nct;
 }
 
 }  // namespace xmdg
