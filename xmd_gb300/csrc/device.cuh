@@ -576,10 +576,13 @@ template <> struct PairGeo<float> {
     __device__ __forceinline__ PairGeo(const BoxD &b, bool periodic, double4_32a p) : per(periodic), si(split_p(p)) {
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            const F2 L = split_d(b.cell[a]);
-            Lh[a] = L.h;
-            Ll[a] = L.l;
-            Li[a] = narrow_f(b.cell_inv[a]);
+            Lh[a] = Ll[a] = Li[a] = 0.0f;
+            if (periodic) {
+                const F2 L = split_d(b.cell[a]);
+                Lh[a] = L.h;
+                Ll[a] = L.l;
+                Li[a] = narrow_f(b.cell_inv[a]);
+            }
         }
     }
     __device__ __forceinline__ V3<float> diff2(const P2 &u, const P2 &w) const {

@@ -824,6 +824,13 @@ __global__ void __launch_bounds__(NC_WARPS * 32, 3) k_nl_cells(Dev d, TermP p, i
     const bool es_on = (p.on[XMD_TERM_CONST_ES] || p.on[XMD_TERM_REL_ES]);
     const bool qa_on = d.qa_on && p.on[XMD_TERM_QA];
     const int nref = qa_on ? min(d.qa.ref_cnt[i], QA_REF_CAP) : 0;
+    const int nnat = n1 - n0;
+    const int my_nat = lane < nnat ? d.nat_j[n0 + lane] : -1;
+    int my_qa = -1;
+    if (lane < nref) {
+        const int s = d.qa.ref[(size_t)lane * d.N + i];
+        my_qa = d.qa.ct_i1[s] == i ? d.qa.ct_i2[s] : d.qa.ct_i1[s];
+    }
     const float qi_w = narrow_f(pi.w);
     const int cap = d.nl_cap;
     int cnt = 0, tcnt = 0;
@@ -870,22 +877,26 @@ __global__ void __launch_bounds__(NC_WARPS * 32, 3) k_nl_cells(Dev d, TermP p, i
                             if (pauli_on && pa) flags |= NL_PAULI;
                             if (es_on && es && qi_w * narrow_f(pos[j].w) != 0.0f) flags |= NL_ES;
                             qa_free = qa_on && j > i && qa;
-                            // the pair is a native contact: it leaves every list
-                            // (natives leave only with native contacts enabled,
-                            // main.cpp:504-530)
-                            if (go_on)
-                                for (int k = n0; k < n1; ++k)
-                                    if (d.nat_j[k] == j) { flags = 0; qa_free = false; }
-                            if (qa_free)
-                                for (int k = 0; k < nref; ++k) {
-                                    const int s = d.qa.ref[(size_t)k * d.N + i];
-                                    const int other = d.qa.ct_i1[s] == i ? d.qa.ct_i2[s] : d.qa.ct_i1[s];
-                                    if (other == j) qa_free = false;
-                                }
                         }
                     }
                 }
             }
+            // a native contact leaves every list (natives leave only with
+            // native contacts enabled, main.cpp:504-530); a pair in contact
+            // is no free pair.  The bead's natives and contact partners are
+            // held one per lane and broadcast.
+            if (go_on && __any_sync(FULL, flags != 0 || qa_free)) {
+                if (nnat <= 32) {
+                    for (int k = 0; k < nnat; ++k)
+                        if (__shfl_sync(FULL, my_nat, k) == j) { flags = 0; qa_free = false; }
+                } else {
+                    for (int k = n0; k < n1; ++k)
+                        if (d.nat_j[k] == j) { flags = 0; qa_free = false; }
+                }
+            }
+            if (qa_on && __any_sync(FULL, qa_free))
+                for (int k = 0; k < nref; ++k)
+                    if (__shfl_sync(FULL, my_qa, k) == j) qa_free = false;
             const unsigned km = __ballot_sync(FULL, flags != 0);
             if (flags) {
                 const int at = cnt + __popc(km & lt);
@@ -1094,6 +1105,15 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
 
         int nref = 0;
         if (qa_on) nref = min(d.qa.ref_cnt[i], QA_REF_CAP);
+        // the row's natives and contact partners, one per lane (broadcast by
+        // shuffle in the exclusion checks)
+        const int nnat = n1 - n0;
+        const int my_nat = lane < nnat ? d.nat_j[n0 + lane] : -1;
+        int my_qa = -1;
+        if (lane < nref) {
+            const int s = d.qa.ref[(size_t)lane * d.N + i];
+            my_qa = d.qa.ct_i1[s] == i ? d.qa.ct_i2[s] : d.qa.ct_i1[s];
+        }
         int cnt = 0, tcnt = 0;
         for (int j0 = 0; j0 < n; j0 += 32) {
             if (!periodic) {
@@ -1146,16 +1166,17 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
             // natives leave the list only with native contacts enabled
             // (main.cpp:504-530); the loop is warp-uniform
             if (go_on && __any_sync(0xffffffffu, flags != 0 || qa_free)) {
-                for (int k = n0; k < n1; ++k)
-                    if (d.nat_j[k] == b + lj) { flags = 0; qa_free = false; }
-            }
-            if (qa_on && __any_sync(0xffffffffu, qa_free)) {
-                for (int k = 0; k < nref; ++k) {
-                    const int s = d.qa.ref[(size_t)k * d.N + i];
-                    const int other = d.qa.ct_i1[s] == i ? d.qa.ct_i2[s] : d.qa.ct_i1[s];
-                    if (other == b + lj) qa_free = false;
+                if (nnat <= 32) {
+                    for (int k = 0; k < nnat; ++k)
+                        if (__shfl_sync(0xffffffffu, my_nat, k) == b + lj) { flags = 0; qa_free = false; }
+                } else {
+                    for (int k = n0; k < n1; ++k)
+                        if (d.nat_j[k] == b + lj) { flags = 0; qa_free = false; }
                 }
             }
+            if (qa_on && __any_sync(0xffffffffu, qa_free))
+                for (int k = 0; k < nref; ++k)
+                    if (__shfl_sync(0xffffffffu, my_qa, k) == b + lj) qa_free = false;
             const unsigned km = __ballot_sync(0xffffffffu, flags != 0);
             if (flags) {
                 const int at = cnt + __popc(km & lt);
