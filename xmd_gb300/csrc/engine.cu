@@ -87,6 +87,29 @@ static GF2 gf2_jump(uint64_t draws) {
 
 uint64_t rng_jump(uint64_t state, uint64_t n_draws) { return gf2_apply_h(gf2_jump(n_draws), state); }
 
+// ---- exact squared-distance thresholds (host) ---------------------------------
+// The list tests of the reference take a square root (and a reciprocal) of
+// the squared distance and compare.  Both are correctly rounded and monotone
+// in IEEE FP64, so each test equals s < S for one threshold S on the squared
+// distance, found here by stepping through adjacent doubles; the builds then
+// compare squared distances (no FP64 square root or division per pair).
+// smallest s with RN(sqrt(s)) >= T: sqrt(s) < T <=> s < sq_below(T)
+static double sq_below(double T) {
+    if (!(T > 0.0)) return 0.0;
+    double s = T * T;
+    while (s > 0.0 && std::sqrt(s) >= T) s = std::nextafter(s, 0.0);
+    while (std::sqrt(s) < T) s = std::nextafter(s, INFINITY);
+    return s;
+}
+// smallest x with RN(1/x) <= v: 1/x > v <=> x < inv_above(v)
+static double inv_above(double v) {
+    if (!(v > 0.0)) return INFINITY;
+    double x = 1.0 / v;
+    while (x > 0.0 && 1.0 / x <= v) x = std::nextafter(x, 0.0);
+    while (1.0 / x > v) x = std::nextafter(x, INFINITY);
+    return x;
+}
+
 // ---- device helpers -----------------------------------------------------------
 // maximum over the warp of non-negative doubles, compared as their bit
 // patterns (the same order) on the integer pipe
@@ -109,6 +132,11 @@ __device__ __forceinline__ void add3(double &fx, double &fy, double &fz, V3<FT> 
 __device__ __forceinline__ bool finite_bits(double x) {
     return ((unsigned long long)__double_as_longlong(x) & 0x7ff0000000000000ull) != 0x7ff0000000000000ull;
 }
+
+// native distance of Go-list entry k in the path's type
+template <class FT> __device__ __forceinline__ FT nat_dist(const Dev &d, int k);
+template <> __device__ __forceinline__ double nat_dist<double>(const Dev &d, int k) { return d.nat_d[k]; }
+template <> __device__ __forceinline__ float nat_dist<float>(const Dev &d, int k) { return d.nat_df[k]; }
 
 // ---- force (+ integrate) kernel --------------------------------------------------
 // MODE 0: forces and per-term energies at pos[cur] (eval).
@@ -140,6 +168,12 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
     double yv[15];
     uint64_t st0 = 0;
     double4_32a o_i = make_double4_32a(0, 0, 0, 0);
+    int pf_n0 = 0, pf_n1 = 0, pf_cnt = 0;   // the pair loops' bounds, loaded first too
+    if (i0 + t < N) {
+        pf_n0 = d.nat_start[i0 + t];
+        pf_n1 = d.nat_end[i0 + t];
+        pf_cnt = d.nl_cnt[i0 + t];
+    }
     if (EARLY && i0 + t < N) {
         const size_t Ns = (size_t)N;
 #pragma unroll
@@ -261,23 +295,46 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
     const PairGeo<FT> geo(bx, per, pi);
     double vgo = 0, vpa = 0, ves = 0;
 
+    // Both pair loops are software-pipelined: the next entry (native index
+    // data, or row entry) is loaded while the current partner's position is
+    // fetched, so each iteration waits on one load instead of a chain.  The
+    // summation order is unchanged.
     if (p.on[XMD_TERM_GO]) {
-        const int k1 = d.nat_end[i];
-        for (int k = d.nat_start[i]; k < k1; ++k) {
-            if (!d.nat_on[k]) continue;
-            int j = d.nat_j[k];
-            FT V_;
-            FT nd;
-            if constexpr (sizeof(FT) == 4) nd = d.nat_df[k];
-            else nd = d.nat_d[k];
-            V3<FT> f = go_pair<FT>(p, geo.to(pin[j]), nd, &V_);
-            acc.add(f);
-            if (MODE == 0 && i < j) vgo += (double)V_;
+        int k = pf_n0;
+        const int k1 = pf_n1;
+        int j = 0;
+        bool on = false;
+        FT nd = FT(0);
+        if (k < k1) {
+            j = d.nat_j[k];
+            on = d.nat_on[k] != 0;
+            nd = nat_dist<FT>(d, k);
+        }
+        for (; k < k1; ++k) {
+            int jn = 0;
+            bool onn = false;
+            FT ndn = FT(0);
+            if (k + 1 < k1) {
+                jn = d.nat_j[k + 1];
+                onn = d.nat_on[k + 1] != 0;
+                ndn = nat_dist<FT>(d, k + 1);
+            }
+            if (on) {
+                FT V_;
+                V3<FT> f = go_pair<FT>(p, geo.to(pin[j]), nd, &V_);
+                acc.add(f);
+                if (MODE == 0 && i < j) vgo += (double)V_;
+            }
+            j = jn;
+            on = onn;
+            nd = ndn;
         }
     }
-    const int cnt = d.nl_cnt[i];
+    const int cnt = pf_cnt;
+    int e_next = cnt > 0 ? d.nl_row[i] : 0;
     for (int k = 0; k < cnt; ++k) {
-        int e = d.nl_row[(size_t)k * N + i];
+        const int e = e_next;
+        if (k + 1 < cnt) e_next = d.nl_row[(size_t)(k + 1) * N + i];
         int j = e & NL_MASK;
         double4_32a pj = pin[j];
         V3<FT> r12 = geo.to(pj);
@@ -515,6 +572,16 @@ __device__ __forceinline__ float min_image_f(float d, float L) {
     return d < -h ? d + L : d;
 }
 
+// FP32 error bound of a distance d <= ext between FP32 coordinates of
+// magnitude <= ext (relative coordinates, or wrapped into [0, L) with L <=
+// ext).  Each coordinate is the FP64 value rounded once (<= 2^-24 ext); a
+// difference adds one rounding and the minimum-image shift by the rounded
+// box length two more (<= 4 * 2^-24 ext per axis); the three squares and
+// their sum add <= 3 * 2^-24 relative to d^2.  In distance terms that is
+// <= sqrt(3) * 4 * 2^-24 ext + 1.5 * 2^-24 d < 5e-7 ext; the bound used is
+// twice that plus an absolute 1e-5.
+__host__ __device__ __forceinline__ double band_margin(double ext) { return 1e-5 + 1e-6 * ext; }
+
 // FP32 decision band around a distance threshold T (error bound m)
 struct Band {
     float lo, hi;   // squared FP32 distance: below lo -> inside, above hi -> outside
@@ -609,11 +676,11 @@ __global__ void __launch_bounds__(CB) k_cells(Dev d, int cur) {
             }
         }
         rp.hashed = !(all_per && total <= bud);
-        // FP32 pre-filter radius: relative coordinates carry <= ext * 2^-24
-        // rounding each, so this margin never rejects a pair inside req_r
-        double m = rp.req_r + 1e-3 + 4e-7 * ext;
-        rp.pre2 = (float)(m * m);
-        rp.band_m = 1e-3 + 4e-7 * ext;
+        // FP32 error bound of a distance (see band_margin); the pre-filter
+        // radius req_r + m never rejects a pair inside req_r
+        rp.band_m = band_margin(fmax(ext, rp.req_r));
+        double m = rp.req_r + rp.band_m;
+        rp.pre2 = __double2float_ru(m * m);
         const double T[4] = {rp.req_r, 1.0 / rp.pauli_min_inv, 1.0 / rp.es_min_inv, 1.0 / rp.qa_min_inv};
         for (int k = 0; k < 4; ++k) {
             const Band B = make_band(T[k], rp.band_m);
@@ -783,7 +850,7 @@ __global__ void __launch_bounds__(NC_WARPS * 32, 3) k_nl_cells(Dev d, TermP p, i
         const float mm = __fmaf_ru(Tf, 1.2e-7f, mf);
         const float blo = __fsub_rd(Tf, mm), bhi = __fadd_ru(Tf, mm);
         const Band B{blo > 0.0f ? __fmul_rd(blo, blo) : -1.0f, __fmul_ru(bhi, bhi)};
-        d.nat_on[k] = in_band(B, d2) ? dist_exact(bx, pi, pj) < T : d2 < B.lo;
+        d.nat_on[k] = in_band(B, d2) ? dist2_exact(bx, pi, pj) < d.nat_S[k] : d2 < B.lo;
     }
 
     // neighbouring buckets: lane l < 27 takes offsets (l/9, l/3 % 3, l % 3) - 1
@@ -861,12 +928,11 @@ __global__ void __launch_bounds__(NC_WARPS * 32, 3) k_nl_cells(Dev d, TermP p, i
                         bool in_req, pa, es, qa;
                         if (in_band(Breq, d2) || (pauli_on && in_band(Bpa, d2)) || (es_on && in_band(Bes, d2)) ||
                             (qa_on && in_band(Bqa, d2))) {
-                            const double dd = dist_exact(bx, pi, pos[j]);
-                            const double inv = __ddiv_rn(1.0, dd);
-                            in_req = dd < rp.req_r;
-                            pa = inv > rp.pauli_min_inv;
-                            es = inv > rp.es_min_inv;
-                            qa = inv > rp.qa_min_inv;
+                            const double s2 = dist2_exact(bx, pi, pos[j]);
+                            in_req = s2 < rp.s_req;
+                            pa = s2 < rp.s_pa;
+                            es = s2 < rp.s_es;
+                            qa = s2 < rp.s_qa;
                         } else {
                             in_req = d2 < Breq.lo;
                             pa = d2 < Bpa.lo;
@@ -965,10 +1031,9 @@ __global__ void __launch_bounds__(NC_WARPS * 32, 3) k_nl_cells(Dev d, TermP p, i
 // time, lane k taking j = j0 + k.  A pair is decided in FP32 when its FP32
 // distance is farther than the error margin m from every threshold (the list
 // radius, r_excl + pad, 2D + pad, the QA formation radius + pad); otherwise the
-// exact FP64 test of the cell path decides it.  m = 1e-3 + 4e-7 * ext bounds
-// the FP32 error of a distance between coordinates of magnitude <= ext (each
-// coordinate carries <= ext * 2^-24; the differences, the periodic shift and
-// the squares add a few ulp more), so both paths keep exactly the same pairs.
+// exact FP64 test decides it.  The margin (band_margin) bounds the FP32 error
+// of a distance between coordinates of magnitude <= ext, so both paths keep
+// exactly the same pairs.
 // Rows come out ordered by j (ballot compaction in lane order).
 constexpr int TL_CH = 16;      // rows per chunk: two per warp
 constexpr int TL_THREADS = 256;
@@ -1026,9 +1091,9 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
     __shared__ Band bands_s[4];
     __shared__ float mf_s;
     if (t == 0) {
-        double exd = (double)ext;
+        double exd = fmax((double)ext, rp.req_r);
         for (int a = 0; a < 3; ++a) exd = fmax(exd, bx.cell[a]);
-        const double m = 1e-3 + 4e-7 * exd;
+        const double m = band_margin(exd);
         bands_s[0] = make_band(rp.req_r, m);
         bands_s[1] = make_band(1.0 / rp.pauli_min_inv, m);
         bands_s[2] = make_band(1.0 / rp.es_min_inv, m);
@@ -1098,7 +1163,7 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
             const float blo = __fsub_rd(Tf, mm), bhi = __fadd_ru(Tf, mm);
             const Band B{blo > 0.0f ? __fmul_rd(blo, blo) : -1.0f, __fmul_ru(bhi, bhi)};
             bool on;
-            if (in_band(B, d2)) on = dist_exact(bx, pi, pos[j]) < T;
+            if (in_band(B, d2)) on = dist2_exact(bx, pi, pos[j]) < d.nat_S[k];
             else on = d2 < B.lo;
             d.nat_on[k] = on;
         }
@@ -1144,12 +1209,11 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
                     bool in_req, pa, es, qa;
                     if (in_band(Breq, d2) || (pauli_on && in_band(Bpa, d2)) || (es_on && in_band(Bes, d2)) ||
                         (qa_on && in_band(Bqa, d2))) {
-                        const double dd = dist_exact(bx, pi, pos[b + lj]);
-                        const double inv = __ddiv_rn(1.0, dd);
-                        in_req = dd < rp.req_r;
-                        pa = inv > rp.pauli_min_inv;
-                        es = inv > rp.es_min_inv;
-                        qa = inv > rp.qa_min_inv;
+                        const double s2 = dist2_exact(bx, pi, pos[b + lj]);
+                        in_req = s2 < rp.s_req;
+                        pa = s2 < rp.s_pa;
+                        es = s2 < rp.s_es;
+                        qa = s2 < rp.s_qa;
                     } else {
                         in_req = d2 < Breq.lo;
                         pa = d2 < Bpa.lo;
@@ -1469,6 +1533,10 @@ void Engine::derive_rep(int ri, RepDev &rd) {
     rd.es_min_inv = 1.0 / (es_cut + rd.pad);                      // es_pair.cpp:9
     rd.pauli_min_inv = 1.0 / (p.pauli_r_excl + rd.pad);           // pauli.cpp:12-13
     rd.qa_min_inv = 1.0 / (max_form + rd.pad);                     // free_pair.cpp:9-10
+    rd.s_req = sq_below(rd.req_r);
+    rd.s_pa = sq_below(inv_above(rd.pauli_min_inv));
+    rd.s_es = sq_below(inv_above(rd.es_min_inv));
+    rd.s_qa = sq_below(inv_above(rd.qa_min_inv));
     rd.noise_sd = std::sqrt(2.0 * 1.0 * r.temperature) * std::sqrt(p.gamma_factor) * 1.0;
     rd.begin = r.begin;
     rd.n = r.n;
@@ -1537,6 +1605,7 @@ void Engine::allocate() {
     d.nat_d = (double *)dalloc(sizeof(double) * NN);
     d.nat_df = (float *)dalloc(sizeof(float) * NN);
     d.nat_T = (double *)dalloc(sizeof(double) * NN);
+    d.nat_S = (double *)dalloc(sizeof(double) * NN);
     d.nat_on = (uint8_t *)dalloc(NN);
     d.nl_row = (int32_t *)dalloc(sizeof(int32_t) * (size_t)nl_cap * N);
     d.nl_cnt = (int32_t *)dalloc(sizeof(int32_t) * N);
@@ -1821,6 +1890,9 @@ void Engine::place(int k) {
         std::vector<double> nT(nd.size());
         for (size_t q = 0; q < nd.size(); ++q) nT[q] = 2.0 * nd[q] + rd.pad;   // 2 r_nat is exact
         up(d.nat_T + no, nT.data(), sizeof(double) * nT.size());
+        std::vector<double> nS(nT.size());
+        for (size_t q = 0; q < nT.size(); ++q) nS[q] = sq_below(nT[q]);
+        up(d.nat_S + no, nS.data(), sizeof(double) * nS.size());
     }
     rd.cell_off = co;
     rd.cell_budget = ncell;

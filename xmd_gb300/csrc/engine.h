@@ -26,6 +26,9 @@ struct RepDev {
     BoxD box;
     double pad, req_r, noise_sd;
     double es_min_inv, pauli_min_inv, qa_min_inv;
+    // squared-distance forms of the list tests: s < s_req <=> sqrt(s) < req_r,
+    // s < s_pa <=> 1/sqrt(s) > pauli_min_inv, etc. (correctly rounded FP64)
+    double s_req, s_pa, s_es, s_qa;
     double t;
     int begin, n;
     int cell_off, cell_budget;
@@ -102,6 +105,7 @@ struct Dev {
     double *nat_d;
     float *nat_df;          // nat_d in FP32 for the mixed path
     double *nat_T;          // Go-list threshold 2 r_nat + pad of each entry (go.cpp:11-22)
+    double *nat_S;          // its squared form: s < nat_S <=> sqrt(s) < nat_T
     uint8_t *nat_on;
     int32_t *nl_row, *nl_cnt;
     int32_t *cell_cnt, *cell_start, *cell_fill, *cell_items, *bead_cell;
