@@ -124,19 +124,25 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """Per-launch DRAM traffic of the dominant kernel from the committed ncu
-    summary (line `traffic_bytes_per_launch: <int>`), or None."""
+def profile_value(key):
+    """A figure of the dominant kernel's committed ncu summary (a line
+    `<key>: <number>`), or None."""
     p = ROOT / "profiles" / "k_force_mixed_c4.md"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
-        if line.strip().startswith("traffic_bytes_per_launch:"):
+        if line.strip().startswith(key + ":"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
                 return None
     return None
+
+
+def profile_traffic():
+    """Per-launch DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum)
+    of the dominant kernel from the committed ncu summary, or None."""
+    return profile_value("traffic_bytes_per_launch")
 
 
 def dist_env():
@@ -331,7 +337,11 @@ def run_engine(args, rank, local, world):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "kernel": "k_force<float,1> (force+integrate)", "kernel_ms": force_ms,
-                     "alg_bytes_per_launch": alg_bytes, "peak_source": peak_kind},
+                     "alg_bytes_per_launch": alg_bytes, "peak_source": peak_kind,
+                     "fp64_pipe_active": profile_value("fp64_pipe_active_pct"),
+                     "note": "working set (~30 MB) is L2-resident between steps; the step kernel is "
+                             "latency-bound at 16 warps/SM with its FP64 integrator on GB300's 2-lane/clk FP64 "
+                             "pipe (fp64_pipe_active: % of active cycles, ncu, profiles/k_force_mixed_c4.md)"},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "bead-steps/s", "h2d_bytes_per_step": int(yh.nbytes),
                 "d2h_bytes_per_step": int(24 * nbeads)},
@@ -404,7 +414,7 @@ def serve_bench(requests, precision, nsteps, rate_hz, device, seed=0):
     """Config 5: requests arrive as a Poisson process at `rate_hz` and are
     served by the continuous-batching loop (HBM-budget admission, state
     resident on the device).  Returns latency percentiles and throughput."""
-    from xmd_gb300 import Server, synth
+    from xmd_gb300 import Server, XmdError, synth
     yaml = synth.yaml_for("c5", precision) + f"  device: {device}\n"
     rng = np.random.default_rng(seed)
     gaps = rng.exponential(1.0 / rate_hz, size=len(requests))
@@ -416,15 +426,24 @@ def serve_bench(requests, precision, nsteps, rate_hz, device, seed=0):
         for g, rq in zip(gaps, requests):
             time.sleep(g)
             ids.append(srv.submit(rq, nsteps))
-        lat = [srv.result(i)[3] for i in ids]
+        # a request whose trajectory diverges (non-finite force, as the
+        # reference's own kernels do for some states) fails alone
+        lat, done_beads, failed = [], 0, []
+        for k, i in enumerate(ids):
+            try:
+                lat.append(srv.result(i)[3])
+                done_beads += requests[k].n
+            except XmdError as ex:
+                failed.append({"request": k, "beads": int(requests[k].n), "error": str(ex)[:120]})
         wall = time.perf_counter() - t0
         st = srv.stats()
     lat = np.sort(np.asarray(lat))
-    work = float(sum(rq.n for rq in requests)) * nsteps
-    return {"p50_ms": 1e3 * float(np.percentile(lat, 50, method="inverted_cdf")),
-            "p99_ms": 1e3 * float(np.percentile(lat, 99, method="inverted_cdf")),
+    work = float(done_beads) * nsteps
+    pct = (lambda q: 1e3 * float(np.percentile(lat, q, method="inverted_cdf"))) if len(lat) else (lambda q: None)
+    return {"p50_ms": pct(50), "p99_ms": pct(99),
             "bead_steps_per_s": work / wall, "wall_s": wall, "peak_concurrent": int(st["peak_running"]),
-            "requests": len(requests), "steps_per_request": nsteps, "rate_hz": rate_hz,
+            "requests": len(requests), "completed": len(lat), "failed": failed,
+            "steps_per_request": nsteps, "rate_hz": rate_hz,
             "beads_total": int(sum(rq.n for rq in requests))}
 
 

@@ -292,7 +292,7 @@ enum { XMD_REQ_QUEUED = 0, XMD_REQ_RUNNING = 1, XMD_REQ_DONE = 2, XMD_REQ_FAILED
 enum {
     XMD_SRV_P50_S = 0, XMD_SRV_P99_S, XMD_SRV_BEAD_STEPS_PER_S, XMD_SRV_COMPLETED, XMD_SRV_QUEUED,
     XMD_SRV_RUNNING, XMD_SRV_CHUNKS, XMD_SRV_PEAK_RUNNING, XMD_SRV_CAP_BEADS, XMD_SRV_BEAD_STEPS,
-    XMD_SRV_SPAN_S, XMD_SRV_NUM
+    XMD_SRV_SPAN_S, XMD_SRV_FAILED, XMD_SRV_NUM
 };
 int xmd_gpu_server_create(const char *yaml_text, int64_t hbm_budget_bytes, int32_t max_beads,
                           int32_t chunk_steps, xmd_gpu_server **out);

@@ -96,3 +96,49 @@ def test_server_rejects_oversized_request():
         with pytest.raises(abi.XmdError) as ei:
             srv.submit(big, 10)
         assert ei.value.code == -5
+
+
+def diverging(seed=610):
+    """A chain with two beads far apart in sequence placed on the same spot:
+    its first pair force is non-finite."""
+    s = synth.make_system([80], seed, box=None, types="charged10", temperature=0.4, rng_seed=seed)
+    s.r[40] = s.r[10]
+    return s
+
+
+def test_diverged_request_fails_alone():
+    """A request whose trajectory goes non-finite is frozen and failed; the
+    requests sharing the context finish with the state each reaches alone."""
+    ss = systems()[:3]
+    bad = diverging()
+    steps = [96, 160, 64]
+    with Server(YAML, hbm_budget=64 << 20, max_beads=4000, chunk_steps=32) as srv:
+        ids = [srv.submit(ss[0], steps[0]), srv.submit(bad, 128), srv.submit(ss[1], steps[1]),
+               srv.submit(ss[2], steps[2])]
+        with pytest.raises(abi.XmdError) as ei:
+            srv.result(ids[1])
+        assert "non-finite" in str(ei.value)
+        res = [srv.result(i) for i in (ids[0], ids[2], ids[3])]
+        st = srv.stats()
+    assert st["failed"] == 1 and st["completed"] == 3
+    for k, s in enumerate(ss):
+        r, v, t = alone(s, steps[k])
+        assert np.array_equal(res[k][0], r), k
+        assert np.array_equal(res[k][1], v), k
+
+
+def test_static_context_reports_non_finite_and_freezes():
+    """Outside the server a non-finite force fails the step call; the
+    replica is frozen with finite positions and thaws on a new state."""
+    bad = diverging()
+    with Engine(YAML) as e:
+        e.add_system(bad)
+        with pytest.raises(abi.XmdError):
+            e.step(8)
+        r, _, _ = e.get_state(0)
+        assert np.isfinite(r).all()
+        good = synth.make_system([80], 611, box=None, types="charged10", temperature=0.4, rng_seed=611)
+        e.set_state(0, good.r)
+        e.step(8)
+        r2, _, _ = e.get_state(0)
+        assert np.isfinite(r2).all() and not np.array_equal(r2, good.r)

@@ -396,7 +396,17 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
 
     const V3<double> ftot = acc.total();
     const double fx = ftot.x, fy = ftot.y, fz = ftot.z;
-    if (!(finite_bits(fx) && finite_bits(fy) && finite_bits(fz))) atomicOr(d.status, ST_NONFINITE);
+    if (!(finite_bits(fx) && finite_bits(fy) && finite_bits(fz))) {
+        // the replica is frozen from the next step on (its skin check sets
+        // steps_left = 0); this bead keeps its state, so no non-finite
+        // position ever reaches a list build
+        atomicOr(d.status, ST_NONFINITE);
+        if (MODE == 1) {
+            d.rep[r].fault = 1;
+            d.pos[cur ^ 1][i] = pi;
+            return;
+        }
+    }
 
     if (MODE == 0) {
         d.F[3 * i] = fx;
@@ -500,6 +510,11 @@ __device__ __forceinline__ void nl_check_block(const Dev &d, int advance, double
     for (int r = threadIdx.x; r < d.R; r += blockDim.x) {
         RepDev &rp = d.rep[r];
         if (!rp.active) continue;
+        if (rp.fault) {   // frozen: no further step, no list
+            rp.steps_left = 0;
+            rp.rebuild = 0;
+            continue;
+        }
         if (advance && rp.steps_left == 0) {           // took no step (k_force kept it)
             rp.rebuild = 0;
             continue;
@@ -928,7 +943,7 @@ __global__ void __launch_bounds__(NC_WARPS * 32, 3) k_nl_cells(Dev d, TermP p, i
                         bool in_req, pa, es, qa;
                         if (in_band(Breq, d2) || (pauli_on && in_band(Bpa, d2)) || (es_on && in_band(Bes, d2)) ||
                             (qa_on && in_band(Bqa, d2))) {
-                            const double s2 = dist2_exact(bx, pi, pos[j]);
+                            const double s2 = periodic ? dist2_exact(bx, pi, pos[j]) : dist2_open(pi, pos[j]);
                             in_req = s2 < rp.s_req;
                             pa = s2 < rp.s_pa;
                             es = s2 < rp.s_es;
@@ -1075,12 +1090,25 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
     const P2 p0 = split_p(pos[b]);
 
     float ext = 0.0f;
-    for (int k = t; k < n; k += TL_THREADS) {
-        double4_32a q = pos[b + k];
-        float x = tl_rel(rp, 0, q.x, p0.x), y = tl_rel(rp, 1, q.y, p0.y), z = tl_rel(rp, 2, q.z, p0.z);
-        sq[k] = make_float4(x, y, z, narrow_f(q.w));
-        scs[k] = make_int2(d.chain[b + k], d.seq[b + k]);
-        ext = fmaxf(ext, fmaxf(fabsf(x), fmaxf(fabsf(y), fabsf(z))));
+    // two loops on a block-uniform flag, so the open-box loop carries no
+    // FP64 work (a select between the two forms would execute both)
+    if ((rp.per[0] | rp.per[1] | rp.per[2]) == 0) {
+        for (int k = t; k < n; k += TL_THREADS) {
+            const double4_32a q = pos[b + k];
+            const float x = ff_diff(p0.x, split_d(q.x)).h, y = ff_diff(p0.y, split_d(q.y)).h,
+                        z = ff_diff(p0.z, split_d(q.z)).h;
+            sq[k] = make_float4(x, y, z, narrow_f(q.w));
+            scs[k] = make_int2(d.chain[b + k], d.seq[b + k]);
+            ext = fmaxf(ext, fmaxf(fabsf(x), fmaxf(fabsf(y), fabsf(z))));
+        }
+    } else {
+        for (int k = t; k < n; k += TL_THREADS) {
+            const double4_32a q = pos[b + k];
+            const float x = tl_rel(rp, 0, q.x, p0.x), y = tl_rel(rp, 1, q.y, p0.y), z = tl_rel(rp, 2, q.z, p0.z);
+            sq[k] = make_float4(x, y, z, narrow_f(q.w));
+            scs[k] = make_int2(d.chain[b + k], d.seq[b + k]);
+            ext = fmaxf(ext, fmaxf(fabsf(x), fmaxf(fabsf(y), fabsf(z))));
+        }
     }
     for (int o = 16; o; o >>= 1) ext = fmaxf(ext, __shfl_xor_sync(0xffffffffu, ext, o));
     if (lane == 0) ext_s[w] = ext;
@@ -1209,7 +1237,7 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
                     bool in_req, pa, es, qa;
                     if (in_band(Breq, d2) || (pauli_on && in_band(Bpa, d2)) || (es_on && in_band(Bes, d2)) ||
                         (qa_on && in_band(Bqa, d2))) {
-                        const double s2 = dist2_exact(bx, pi, pos[b + lj]);
+                        const double s2 = periodic ? dist2_exact(bx, pi, pos[b + lj]) : dist2_open(pi, pos[b + lj]);
                         in_req = s2 < rp.s_req;
                         pa = s2 < rp.s_pa;
                         es = s2 < rp.s_es;
@@ -1440,7 +1468,8 @@ void Engine::steps_left(long long *out) {
         CK(cudaStreamSynchronize(stream));
     }
     for (int k = 0; k < (int)reps.size(); ++k)
-        out[k] = !reps[k].in_use ? -2 : (reps[k].placed ? rd[k].steps_left : reps[k].steps_left);
+        out[k] = !reps[k].in_use ? -2
+                 : (reps[k].placed ? (rd[k].fault ? -3 : rd[k].steps_left) : reps[k].steps_left);
 }
 static bool consecutive(const RepHost &r, int a, int b) {
     return a >= 0 && b < r.n && b == a + 1 && r.chain[a] == r.chain[b] && r.seq[b] == r.seq[a] + 1;
@@ -1897,6 +1926,7 @@ void Engine::place(int k) {
     rd.cell_off = co;
     rd.cell_budget = ncell;
     rd.tile = tile;
+    rd.fault = 0;
     rd.chunk_off = tile ? ho : 0;
     rd.nchunk = nchunk;
     rd.active = 1;
@@ -1974,6 +2004,10 @@ void Engine::upload_state(int k) {
     rd.t = 0.0;
     rd.first = 1;
     rd.maxdisp = 0;
+    if (rd.fault) {   // a new state thaws a frozen replica
+        rd.fault = 0;
+        rd.steps_left = reps[k].steps_left;
+    }
     CK(cudaMemcpyAsync(d.rep + k, &rd, sizeof(RepDev), cudaMemcpyHostToDevice, stream));
     CK(cudaStreamSynchronize(stream));
 }
@@ -2020,6 +2054,10 @@ void Engine::set_history(int rep, const double *y, double t, uint64_t rngs) {
     rd.t = t;
     rd.first = 1;
     rd.maxdisp = 0;
+    if (rd.fault) {   // a new state thaws a frozen replica
+        rd.fault = 0;
+        rd.steps_left = reps[rep].steps_left;
+    }
     CK(cudaMemcpyAsync(d.rep + rep, &rd, sizeof(RepDev), cudaMemcpyHostToDevice, stream));
     CK(cudaStreamSynchronize(stream));
 }
@@ -2360,7 +2398,14 @@ void Engine::check_status(const char *where) {
     CK(cudaGetLastError());
     if (st & ST_CAPACITY)
         throw std::length_error(std::string(where) + ": Verlet row capacity exceeded (raise `engine: nl capacity`)");
-    if (st & ST_NONFINITE) throw std::domain_error(std::string(where) + ": non-finite force");
+    if (st & ST_NONFINITE) {
+        // reported once: the faulted replicas are frozen (a new state thaws
+        // them); the other replicas of the context go on
+        const int keep = st & ~ST_NONFINITE;
+        CK(cudaMemcpyAsync(d.status, &keep, sizeof(int), cudaMemcpyHostToDevice, stream));
+        CK(cudaStreamSynchronize(stream));
+        if (!isolate_faults) throw std::domain_error(std::string(where) + ": non-finite force");
+    }
 }
 
 void Engine::eval_forces(int rep, double *F, double *V) {

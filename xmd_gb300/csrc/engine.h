@@ -44,6 +44,7 @@ struct RepDev {
     int first, rebuild;
     int chunk_off, nchunk;   // tile-build chunks of the replica in Dev::chunks
     int active;              // slot holds a placed replica
+    int fault;               // a bead's force was non-finite: the replica is frozen
     long long steps_left;    // steps this replica still takes (-1: no bound)
     unsigned long long maxdisp;
     unsigned long long rebuilds;
@@ -216,6 +217,9 @@ public:
     void steps_left(long long *out);   // per replica slot, -2 for a free slot
     void place_now(int rep);           // place a replica now (XMD_ERR_CAPACITY: no room yet)
     int capacity_replicas() const { return cap.reps; }
+    // a non-finite force freezes its replica (steps_left reports -3) instead
+    // of failing the step, so a serving loop can retire it alone
+    void set_isolate_faults(bool on) { isolate_faults = on; }
     size_t device_bytes() const { return bytes; }
     void set_tethers(int rep, int n, const int32_t *i1, const int32_t *i2, const double *d);
     void set_angles(int rep, int n, const int32_t *i1, const int32_t *i2, const int32_t *i3,
@@ -254,6 +258,7 @@ private:
     int64_t launches = 0, md_steps = 0;
     double *staging = nullptr;   // packed host-layout buffer [18 N]
     bool timing = false;
+    bool isolate_faults = false;
     std::vector<cudaEvent_t> ev_force, ev_rebuild;   // start/stop pairs
     size_t n_ev_force = 0, n_ev_rebuild = 0;
 

@@ -29,6 +29,8 @@ Server::Server(const xmd_params &p, int64_t hbm_budget, int max_beads, int chunk
     cap_reps = std::min(1024, std::max(16, cap_beads / 30));
     cap_nat = NATIVES_PER_BEAD * cap_beads;
     eng = std::make_unique<Engine>(params);
+    // one request whose trajectory diverges fails alone; the others go on
+    eng->set_isolate_faults(true);
     eng->reserve(cap_beads, cap_reps, cap_nat);
     worker = std::thread([this] { loop(); });
 }
@@ -114,6 +116,7 @@ void Server::stats(double *out) {
     out[XMD_SRV_CAP_BEADS] = (double)cap_beads;
     out[XMD_SRV_BEAD_STEPS] = bead_steps;
     out[XMD_SRV_SPAN_S] = span;
+    out[XMD_SRV_FAILED] = (double)failed;
 }
 
 // place a queued request into a free slot; false when the capacity has no
@@ -162,6 +165,16 @@ void Server::retire(Request *q) {
     latencies.push_back(q->t_done - q->t_submit);
     bead_steps += (double)q->n * (double)q->nsteps;
     t_last = q->t_done;
+}
+
+// a request whose replica was frozen by a non-finite force
+void Server::fail(Request *q, const char *why) {
+    eng->remove_replica(q->slot);
+    std::lock_guard<std::mutex> lk(mu);
+    q->t_done = now_s();
+    q->state = XMD_REQ_FAILED;
+    q->error = why;
+    ++failed;
 }
 
 void Server::loop() {
@@ -216,7 +229,8 @@ void Server::loop() {
             eng->steps_left(left.data());
             std::vector<Request *> keep;
             for (Request *q : running) {
-                if (left[q->slot] == 0) retire(q);
+                if (left[q->slot] == -3) fail(q, "non-finite force: the trajectory diverged");
+                else if (left[q->slot] == 0) retire(q);
                 else keep.push_back(q);
             }
             {

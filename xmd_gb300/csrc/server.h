@@ -73,10 +73,12 @@ private:
     std::vector<double> latencies;
     int64_t chunks = 0;
     int peak_running = 0;
+    int64_t failed = 0;     // requests retired by a diverged trajectory
 
     void loop();
     bool admit(Request *q);
     void retire(Request *q);
+    void fail(Request *q, const char *why);
 };
 
 double now_s();

@@ -90,6 +90,14 @@ class Engine:
         check(self.lib.xmd_gpu_get_state(self.h, rep, dptr(r), dptr(v), C.byref(t)))
         return r.reshape(n, 3), v.reshape(n, 3), t.value
 
+    def set_state(self, rep: int, r: np.ndarray, v: np.ndarray | None = None):
+        r = np.ascontiguousarray(r, dtype=np.float64).reshape(-1)
+        vp = None
+        if v is not None:
+            v = np.ascontiguousarray(v, dtype=np.float64).reshape(-1)
+            vp = dptr(v)
+        check(self.lib.xmd_gpu_set_state(self.h, rep, dptr(r), vp))
+
     def get_history(self, rep: int = 0):
         n = self.sizes[rep]
         y, t, st = np.zeros(18 * n), C.c_double(), C.c_uint64()
