@@ -197,6 +197,9 @@ def run_engine(args, rank, local, world):
             dist.barrier()
 
     md = args.md_steps
+    # launch shapes chosen by the autotuner on a clone (not timed; the
+    # trajectory does not depend on them)
+    tuned = eng.autotune(md) if args.autotune else None
     # warm-up (also builds the graphs and the first lists)
     for _ in range(args.warmup):
         eng.step(md)
@@ -270,6 +273,7 @@ def run_engine(args, rank, local, world):
     eng64 = Engine(y_fp64)
     for s in systems:
         eng64.add_system(s)
+    tuned64 = eng64.autotune(md) if args.autotune else None   # its own best shape
     for _ in range(args.warmup):
         eng64.step(md)
     eng64.synchronize()
@@ -329,7 +333,9 @@ def run_engine(args, rank, local, world):
             "plain_fp64_value": plain64["value"], "plain_fp64_sample": plain64["sample"],
             "mixed_over_plain_fp64": value / world / plain64["value"],
             "batched_fp64_value": value64, "mixed_over_batched_fp64": value / world / value64,
-            "mixed_force_rel_err_max": max(errs), "graph_steps_per_launch": 16,
+            "mixed_force_rel_err_max": max(errs),
+            "graph_steps_per_launch": (tuned or {}).get("graph_steps", 16),
+            "autotuned_shape": tuned, "autotuned_shape_fp64": tuned64,
             "p99_req_latency_ms": serving["mixed"]["p99_ms"] if serving else None,
             "serving": serving,
             "mixed_vs_fp64_c3": accuracy,
@@ -534,6 +540,7 @@ def main():
     ap.add_argument("--serve-steps", type=int, default=20000)
     ap.add_argument("--accuracy-steps", type=int, default=100000)
     ap.add_argument("--accuracy-every", type=int, default=1000)
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, local, world = dist_env()

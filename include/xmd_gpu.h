@@ -241,6 +241,18 @@ int xmd_gpu_stats(xmd_gpu_ctx *ctx, int64_t *out);
 /* When on, CUDA events bracket every force and list-rebuild launch; the sums
  * are returned (ms, launches) by xmd_gpu_kernel_times and reset on enabling. */
 int xmd_gpu_set_kernel_timing(xmd_gpu_ctx *ctx, int on);
+
+/* ---- launch shapes and the autotuner ------------------------------------------
+ * No counterpart in the reference (its OpenMP loop has no launch shape).
+ * shape[3] = {beads per step-kernel block (64, 96, 128), resident tile-build
+ * blocks per SM (0 = as many as fit), steps per captured graph (8, 16, 32)}.
+ * Results never depend on the shape.  xmd_gpu_autotune times every candidate
+ * on a clone of the context (same replicas, same starting state; the
+ * context's own state is untouched), keeps the fastest and returns it with
+ * its time per step.  Static contexts only (replicas added, states set). */
+int xmd_gpu_autotune(xmd_gpu_ctx *ctx, int32_t steps, int32_t *shape, double *ms_per_step);
+int xmd_gpu_set_tuning(xmd_gpu_ctx *ctx, const int32_t *shape);
+int xmd_gpu_get_tuning(xmd_gpu_ctx *ctx, int32_t *shape);
 int xmd_gpu_kernel_times(xmd_gpu_ctx *ctx, double *force_ms, int64_t *force_launches,
                          double *rebuild_ms, int64_t *rebuild_launches);
 

@@ -1,0 +1,60 @@
+"""Launch shapes and the autotuner: the trajectory never depends on the shape
+(step-kernel block size, resident tile-build blocks, steps per graph), and
+autotuning leaves the context's state as it was."""
+import numpy as np
+import pytest
+
+from xmd_gb300 import Engine, abi, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def replicas():
+    lens = [57, 130, 301, 75, 612]
+    return [synth.make_system([L], 700 + k, box=None, types="charged10", temperature=0.3 + 0.05 * k,
+                              rng_seed=800 + k) for k, L in enumerate(lens)]
+
+
+def run(prec, shape, nsteps=200):
+    with Engine(synth.yaml_for("c4", prec)) as e:
+        for s in replicas():
+            e.add_system(s)
+        if shape is not None:
+            e.set_tuning(*shape)
+        e.step(nsteps)
+        return [e.get_state(r)[0] for r in range(5)]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_shapes_give_identical_trajectories(prec):
+    ref = run(prec, None)
+    for shape in [(64, 0, 8), (96, 2, 32), (128, 1, 16)]:
+        got = run(prec, shape)
+        for r in range(5):
+            assert np.array_equal(got[r], ref[r]), (shape, r)
+
+
+def test_autotune_keeps_state_and_picks_a_valid_shape():
+    with Engine(synth.yaml_for("c4", "mixed")) as e, Engine(synth.yaml_for("c4", "mixed")) as f:
+        for s in replicas():
+            e.add_system(s)
+            f.add_system(s)
+        e.step(32)
+        f.step(32)
+        best = e.autotune(64)
+        assert best["fb"] in (64, 96, 128) and best["graph_steps"] in (8, 16, 32)
+        assert best["ms_per_step"] > 0
+        assert e.tuning() == {k: best[k] for k in ("fb", "tile_per_sm", "graph_steps")}
+        e.step(96)
+        f.step(96)
+        for r in range(5):
+            assert np.array_equal(e.get_state(r)[0], f.get_state(r)[0]), r
+
+
+def test_bad_shape_rejected():
+    with Engine(synth.yaml_for("c4", "mixed")) as e:
+        e.add_system(replicas()[0])
+        with pytest.raises(abi.XmdError):
+            e.set_tuning(100, 0, 16)
+        with pytest.raises(abi.XmdError):
+            e.set_tuning(64, 0, 12)

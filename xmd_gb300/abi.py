@@ -120,6 +120,9 @@ SIGNATURES = [
     ("xmd_gpu_get_stream", C.c_int, [C.c_void_p, P(C.c_void_p)]),
     ("xmd_gpu_stats", C.c_int, [C.c_void_p, P(C.c_int64)]),
     ("xmd_gpu_set_kernel_timing", C.c_int, [C.c_void_p, C.c_int]),
+    ("xmd_gpu_autotune", C.c_int, [C.c_void_p, C.c_int32, _pi32, _pd]),
+    ("xmd_gpu_set_tuning", C.c_int, [C.c_void_p, _pi32]),
+    ("xmd_gpu_get_tuning", C.c_int, [C.c_void_p, _pi32]),
     ("xmd_gpu_kernel_times", C.c_int, [C.c_void_p, _pd, P(C.c_int64), _pd, P(C.c_int64)]),
     ("xmd_gpu_synchronize", C.c_int, [C.c_void_p]),
     ("xmd_gpu_fp64_peak", C.c_int, [C.c_int32, _pd]),

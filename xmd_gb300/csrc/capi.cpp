@@ -249,6 +249,37 @@ int xmd_gpu_set_kernel_timing(xmd_gpu_ctx *ctx, int on) {
     return guard([&] { ctx->eng->use_device(); ctx->eng->set_kernel_timing(on != 0); });
 }
 
+int xmd_gpu_autotune(xmd_gpu_ctx *ctx, int32_t steps, int32_t *shape, double *ms_per_step) {
+    NEED_CTX;
+    return guard([&] {
+        ctx->eng->use_device();
+        const xmdg::Engine::Tune t = ctx->eng->autotune(steps, ms_per_step);
+        if (shape) { shape[0] = t.fb; shape[1] = t.tile_per_sm; shape[2] = t.graph_steps; }
+    });
+}
+
+int xmd_gpu_set_tuning(xmd_gpu_ctx *ctx, const int32_t *shape) {
+    NEED_CTX;
+    if (!shape) return XMD_ERR_ARG;
+    return guard([&] {
+        ctx->eng->use_device();
+        xmdg::Engine::Tune t;
+        t.fb = shape[0];
+        t.tile_per_sm = shape[1];
+        t.graph_steps = shape[2];
+        ctx->eng->set_tuning(t);
+    });
+}
+
+int xmd_gpu_get_tuning(xmd_gpu_ctx *ctx, int32_t *shape) {
+    NEED_CTX;
+    if (!shape) return XMD_ERR_ARG;
+    return guard([&] {
+        const xmdg::Engine::Tune t = ctx->eng->tuning();
+        shape[0] = t.fb; shape[1] = t.tile_per_sm; shape[2] = t.graph_steps;
+    });
+}
+
 int xmd_gpu_reserve(xmd_gpu_ctx *ctx, int32_t beads, int32_t replicas, int32_t native_entries) {
     NEED_CTX;
     return guard([&] {

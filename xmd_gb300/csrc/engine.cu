@@ -44,7 +44,7 @@ std::string &last_error() {
                                      " at " #call);                                  \
     } while (0)
 
-constexpr int FB = 128;              // beads per force block
+constexpr int BLK_ON = 32;           // beads per granule of the force blocks' occupancy map
 constexpr int NL_MASK = 0x3FFFFFFF;
 constexpr int NL_PAULI = 1 << 30;
 constexpr int NL_ES = (int)(1u << 31);
@@ -143,20 +143,20 @@ template <> __device__ __forceinline__ float nat_dist<float>(const Dev &d, int k
 // MODE 1: forces, then one Langevin predictor-corrector step (lang_pc.cpp:5-41)
 //         writing pos[cur^1], y1..y5, the generator state and the skin-test
 //         displacement (verify.cpp:10-15).
-template <class FT, int MODE>
+template <class FT, int MODE, int FBT>
 __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cur) {
     const double4_32a *__restrict__ pin = d.pos[cur];
-    const int N = d.N, t = threadIdx.x, i0 = blockIdx.x * FB;
-    __shared__ double4_32a P[FB + 6];
-    __shared__ V3<FT> Ct[FB + 3], Ca[3][FB + 3], Cd[4][FB + 3];
+    const int N = d.N, t = threadIdx.x, i0 = blockIdx.x * FBT;
+    __shared__ double4_32a P[FBT + 6];
+    __shared__ V3<FT> Ct[FBT + 3], Ca[3][FBT + 3], Cd[4][FBT + 3];
     // mixed path: every position of the tile split into float-float parts
     // (integer operations); bond vectors e_k = P[k+1] - P[k] and cross
     // products x_k = e_{k-1} x e_k formed once per tile slot in float-float
     // arithmetic (~2^-44 relative, FP64-class where the FP32 forms lose
     // everything: nearly straight triples) and shared by the tether, angle and
     // dihedral centres that use them
-    constexpr int NE = sizeof(FT) == 4 ? FB + 5 : 1;
-    __shared__ P2 S[sizeof(FT) == 4 ? FB + 6 : 1];
+    constexpr int NE = sizeof(FT) == 4 ? FBT + 5 : 1;
+    __shared__ P2 S[sizeof(FT) == 4 ? FBT + 6 : 1];
     __shared__ V3<FF> Eff[NE], Xff[NE];
     __shared__ V3<float> Ef[NE], Xf[NE];
 
@@ -182,20 +182,20 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
         o_i = d.orig[i0 + t];
     }
 
-    for (int k = t; k < FB + 6; k += FB) {
+    for (int k = t; k < FBT + 6; k += FBT) {
         int idx = i0 - 3 + k;
         P[k] = (idx >= 0 && idx < N) ? pin[idx] : make_double4_32a(0, 0, 0, 0);
         if constexpr (sizeof(FT) == 4) S[k] = split_p(P[k]);
     }
     __syncthreads();
     if constexpr (sizeof(FT) == 4) {
-        for (int k = t; k < NE; k += FB) {
+        for (int k = t; k < NE; k += FBT) {
             const V3<FF> e{ff_diff(S[k].x, S[k + 1].x), ff_diff(S[k].y, S[k + 1].y), ff_diff(S[k].z, S[k + 1].z)};
             Eff[k] = e;
             Ef[k] = V3<float>{e.x.h, e.y.h, e.z.h};
         }
         __syncthreads();
-        for (int k = t + 1; k < NE; k += FB) {
+        for (int k = t + 1; k < NE; k += FBT) {
             const V3<FF> x = ff_cross(Eff[k - 1], Eff[k]);
             Xff[k] = x;
             Xf[k] = V3<float>{x.x.h, x.y.h, x.z.h};
@@ -203,14 +203,14 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
         __syncthreads();
     }
 
-    // bonded contributions of centres c in [i0-2, i0+FB]
-    for (int sc = t; sc < FB + 3; sc += FB) {
+    // bonded contributions of centres c in [i0-2, i0+FBT]
+    for (int sc = t; sc < FBT + 3; sc += FBT) {
         int c = i0 - 2 + sc;
         uint32_t fl = (c >= 0 && c < N) ? d.bflags[c] : 0u;
         V3<FT> z{FT(0), FT(0), FT(0)};
         V3<FT> ft = z, a1 = z, a2 = z, a3 = z, q[4] = {z, z, z, z};
         int sp = c - (i0 - 3);
-        bool own = (c >= i0 && c < i0 + FB && c < N);
+        bool own = (c >= i0 && c < i0 + FBT && c < N);
         int rc = own ? d.rep_of[c] : 0;
         if ((fl & BF_TETH) && p.on[XMD_TERM_TETHER]) {
             FT V_;
@@ -552,10 +552,14 @@ __global__ void k_nl_check(Dev d, int advance, double dt, cudaGraphConditionalHa
 // term) the last block to finish also takes the skin decision of every
 // replica and sets the graph's rebuild condition, so a step is one launch
 // plus the conditional rebuild.
-template <class FT, int MODE>
-__global__ void __launch_bounds__(FB) k_force(Dev d, TermP p, int cur, cudaGraphConditionalHandle h, int fuse) {
+template <class FT, int MODE, int FBT>
+__global__ void __launch_bounds__(FBT) k_force(Dev d, TermP p, int cur, cudaGraphConditionalHandle h, int fuse) {
     __shared__ int last_s;
-    if (d.blk_on[blockIdx.x]) force_block<FT, MODE>(d, p, cur);   // uniform per block
+    static_assert(FBT % BLK_ON == 0, "force blocks are whole multiples of the occupancy granule");
+    bool on = false;
+#pragma unroll
+    for (int q = 0; q < FBT / BLK_ON; ++q) on |= d.blk_on[blockIdx.x * (FBT / BLK_ON) + q] != 0;
+    if (on) force_block<FT, MODE, FBT>(d, p, cur);   // uniform per block
     if (MODE == 1 && fuse) {
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -1311,6 +1315,34 @@ __global__ void __launch_bounds__(TL_THREADS, 4) k_nl_tile(Dev d, TermP p, int c
 
 // =================================================================== host ==
 
+// the step kernel of a precision, mode and block size (the block sizes the
+// autotuner chooses from)
+static void *force_kernel(bool mixed, int mode, int fb) {
+#define XMD_FK(M, B) (mixed ? (void *)k_force<float, M, B> : (void *)k_force<double, M, B>)
+    if (mode == 0) {
+        switch (fb) {
+        case 64: return XMD_FK(0, 64);
+        case 96: return XMD_FK(0, 96);
+        default: return XMD_FK(0, 128);
+        }
+    }
+    switch (fb) {
+    case 64: return XMD_FK(1, 64);
+    case 96: return XMD_FK(1, 96);
+    default: return XMD_FK(1, 128);
+    }
+#undef XMD_FK
+}
+
+void Engine::launch_force(int mode, int c) {
+    const int nb = (d.N + tune.fb - 1) / tune.fb;
+    cudaGraphConditionalHandle none = 0;
+    int fuse = 0;
+    void *args[] = {&d, &tp, &c, &none, &fuse};
+    CK(cudaLaunchKernel(force_kernel(params.precision == XMD_PREC_MIXED, mode, tune.fb), dim3(nb), dim3(tune.fb),
+                        args, 0, stream));
+}
+
 Engine::Engine(const xmd_params &p) : params(p) {
     int ndev = 0;
     CK(cudaGetDeviceCount(&ndev));
@@ -1661,7 +1693,8 @@ void Engine::allocate() {
     d.nwork = (int *)dalloc(sizeof(int));
     CK(cudaMemsetAsync(d.nwork, 0, sizeof(int), stream));
     CK(cudaMemsetAsync(d.chunks, 0xff, sizeof(int2) * d.nchunks, stream));
-    d.blk_on = (uint8_t *)dalloc((N + FB - 1) / FB);
+    d.blk_on = (uint8_t *)dalloc((N + BLK_ON - 1) / BLK_ON + 8);
+    CK(cudaMemsetAsync(d.blk_on, 0, (N + BLK_ON - 1) / BLK_ON + 8, stream));
     owner_h.assign(N, -1);
     a_beads.init(N);
     a_nat.init(cap.nat);
@@ -1679,12 +1712,15 @@ void Engine::allocate() {
     if (tile_smem > 48 * 1024)
         CK(cudaFuncSetAttribute(k_nl_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem));
     {
-        // the tile build runs as many blocks as are resident at once; they
-        // take the work list's chunks in turn
+        // the tile build runs as many blocks as are resident at once (or the
+        // tuned number per SM); they take the work list's chunks in turn
         int sms = 0, per_sm = 0;
         CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_nl_tile, TL_THREADS, tile_smem));
-        tile_grid = std::max(1, std::min(d.nchunks, sms * std::max(1, per_sm)));
+        tile_sms = std::max(1, sms);
+        tile_max_per_sm = std::max(1, per_sm);
+        const int k = tune.tile_per_sm > 0 ? std::min(tune.tile_per_sm, tile_max_per_sm) : tile_max_per_sm;
+        tile_grid = std::max(1, std::min(d.nchunks, tile_sms * k));
     }
 
     // term parameters
@@ -1810,13 +1846,14 @@ void Engine::place_pending() {
         }
 }
 
-// force blocks [b0/FB, (b1-1)/FB] on when any bead slot in them is placed
+// occupancy granules [b0/BLK_ON, (b1-1)/BLK_ON] on when any bead slot in them
+// is placed (a force block runs when any of its granules is on)
 void Engine::update_blocks(int b0, int b1) {
     if (b1 <= b0) return;
-    const int k0 = b0 / FB, k1 = (b1 - 1) / FB;
+    const int k0 = b0 / BLK_ON, k1 = (b1 - 1) / BLK_ON;
     std::vector<uint8_t> on(k1 - k0 + 1, 0);
     for (int k = k0; k <= k1; ++k)
-        for (int i = k * FB; i < std::min(cap.beads, (k + 1) * FB); ++i)
+        for (int i = k * BLK_ON; i < std::min(cap.beads, (k + 1) * BLK_ON); ++i)
             if (owner_h[i] >= 0) { on[k - k0] = 1; break; }
     CK(cudaMemcpyAsync(d.blk_on + k0, on.data(), on.size(), cudaMemcpyHostToDevice, stream));
     CK(cudaStreamSynchronize(stream));
@@ -2171,6 +2208,78 @@ bool Engine::grow_rows(double frac) {
     return true;
 }
 
+void Engine::set_tuning(const Tune &t) {
+    if (t.fb != 64 && t.fb != 96 && t.fb != 128)
+        throw std::invalid_argument("tuning: step-kernel block size must be 64, 96 or 128");
+    if (t.graph_steps != 8 && t.graph_steps != 16 && t.graph_steps != 32)
+        throw std::invalid_argument("tuning: steps per graph must be 8, 16 or 32");
+    if (t.tile_per_sm < 0) throw std::invalid_argument("tuning: tile blocks per SM must be >= 0");
+    tune = t;
+    if (finalized) {
+        const int k = tune.tile_per_sm > 0 ? std::min(tune.tile_per_sm, tile_max_per_sm) : tile_max_per_sm;
+        tile_grid = std::max(1, std::min(d.nchunks, tile_sms * k));
+        drop_graphs();
+    }
+}
+
+// The autotuner.  Every candidate launch shape (step-kernel block size,
+// resident tile-build blocks per SM, steps per graph) runs on a fresh clone of
+// this context: the same replicas from the same starting state, so each is
+// timed on the same trajectory (the trajectory does not depend on the shape).
+// A candidate's time is CUDA-event time per step over `steps` graph steps
+// after one warm-up graph (which builds the first lists and captures the
+// graph).  This context's device state is not touched.
+Engine::Tune Engine::autotune(int steps, double *ms_out) {
+    if (dynamic) throw std::logic_error("autotune needs a static context (replicas added before the first step)");
+    int live = 0;
+    for (auto &r : reps) live += r.in_use ? 1 : 0;
+    if (!live) throw std::logic_error("autotune: the context has no replica");
+    for (auto &r : reps)
+        if (r.in_use && !r.have_state) throw std::logic_error("autotune: set_state must be called for every replica");
+    steps = std::max(32, (steps + 31) / 32 * 32);
+    std::vector<Tune> cands;
+    for (int fb : {64, 96, 128})
+        for (int gs : {8, 16, 32})
+            for (int tps : {0, 2}) cands.push_back(Tune{fb, tps, gs});
+    Tune best = tune;
+    double best_ms = 1e300;
+    for (const Tune &cand : cands) {
+        Engine c(params);
+        for (auto &r : reps)
+            if (r.in_use) {
+                RepHost h = r;
+                h.placed = false;
+                c.reps.push_back(std::move(h));
+            }
+        c.tune = cand;
+        c.use_device();
+        c.ready();
+        c.set_tuning(cand);
+        c.step(cand.graph_steps);   // first lists, graph capture
+        c.sync();
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        CK(cudaEventRecord(e0, c.stream));
+        c.step(steps);
+        CK(cudaEventRecord(e1, c.stream));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0.0f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        const double per = (double)ms / steps;
+        if (per < best_ms) {
+            best_ms = per;
+            best = cand;
+        }
+    }
+    use_device();
+    set_tuning(best);
+    if (ms_out) *ms_out = best_ms;
+    return best;
+}
+
 void Engine::drop_graphs() {
     for (auto &row : graphs)
         for (auto &g : row) {
@@ -2203,11 +2312,8 @@ void Engine::ensure_nl() {
 }
 
 void Engine::launch_force_step() {
-    int nb = (d.N + FB - 1) / FB;
     if (timing) record(ev_force, n_ev_force);
-    const cudaGraphConditionalHandle none = 0;
-    if (params.precision == XMD_PREC_MIXED) k_force<float, 1><<<nb, FB, 0, stream>>>(d, tp, cur, none, 0);
-    else k_force<double, 1><<<nb, FB, 0, stream>>>(d, tp, cur, none, 0);
+    launch_force(1, cur);
     if (timing) record(ev_force, n_ev_force);
     ++launches;
     if (d.qa_on) {
@@ -2222,7 +2328,7 @@ void Engine::launch_force_step() {
     }
 }
 
-// One graph runs GRAPH_STEPS steps: per step a force+integrate node, a skin
+// One graph runs tune.graph_steps steps: per step a force+integrate node, a skin
 // check that sets a conditional handle on the device, and an IF node whose
 // body rebuilds the lists of the flagged replicas (cells, then rows).  An
 // even step count leaves the position double buffer where it started.
@@ -2232,13 +2338,13 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
     cudaGraph_t g;
     CK(cudaGraphCreate(&g, 0));
     cudaGraphNode_t prev = nullptr;
-    const int nb = (d.N + FB - 1) / FB;
-    void *fk = params.precision == XMD_PREC_MIXED ? (void *)k_force<float, 1> : (void *)k_force<double, 1>;
+    const int nb = (d.N + tune.fb - 1) / tune.fb;
+    void *fk = force_kernel(params.precision == XMD_PREC_MIXED, 1, tune.fb);
     double dt = params.dt;
     // without the quasi-adiabatic term the step kernel takes the skin
     // decision itself (its last block), so a step is one kernel node
     const int fuse = d.qa_on ? 0 : 1;
-    for (int s = 0; s < GRAPH_STEPS; ++s) {
+    for (int s = 0; s < tune.graph_steps; ++s) {
         int c = start_cur ^ (s & 1), cn = c ^ 1;
         int adv = 1, setc = 1;
         cudaGraphConditionalHandle h;
@@ -2249,7 +2355,7 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
         void *fargs[] = {&d, &tp, &c, &hf, &ff};
         kf.func = fk;
         kf.gridDim = dim3(nb);
-        kf.blockDim = dim3(FB);
+        kf.blockDim = dim3(tune.fb);
         kf.kernelParams = fargs;
         cudaGraphNode_t nf, nc, ncond;
         CK(cudaGraphAddKernelNode(&nf, g, prev ? &prev : nullptr, prev ? 1 : 0, &kf));
@@ -2413,10 +2519,7 @@ void Engine::eval_forces(int rep, double *F, double *V) {
     ready();
     ensure_nl();
     CK(cudaMemsetAsync(d.Vrep, 0, sizeof(double) * XMD_NUM_TERMS * d.R, stream));
-    int nb = (d.N + FB - 1) / FB;
-    const cudaGraphConditionalHandle none = 0;
-    if (params.precision == XMD_PREC_MIXED) k_force<float, 0><<<nb, FB, 0, stream>>>(d, tp, cur, none, 0);
-    else k_force<double, 0><<<nb, FB, 0, stream>>>(d, tp, cur, none, 0);
+    launch_force(0, cur);
     const RepHost &h = reps[rep];
     if (F) CK(cudaMemcpyAsync(F, d.F + 3 * (size_t)h.begin, sizeof(double) * 3 * h.n, cudaMemcpyDeviceToHost, stream));
     if (V) CK(cudaMemcpyAsync(V, d.Vrep + (size_t)rep * XMD_NUM_TERMS, sizeof(double) * XMD_NUM_TERMS,
@@ -2432,13 +2535,14 @@ void Engine::step(int nsteps) {
     ensure_nl();
     int s = 0;
     if (!timing && use_graphs) {
-        for (; s + GRAPH_STEPS <= nsteps; s += GRAPH_STEPS) {
+        const int gsteps = tune.graph_steps;
+        for (; s + gsteps <= nsteps; s += gsteps) {
             CK(cudaGraphLaunch(graph_for(cur), stream));
             // per step: the step kernel (plus the separate check and the
             // quasi-adiabatic kernels with that term); rebuild kernels are
             // counted per pass in stats()
-            launches += (d.qa_on ? 7 : 1) * GRAPH_STEPS;
-            md_steps += GRAPH_STEPS;
+            launches += (d.qa_on ? 7 : 1) * gsteps;
+            md_steps += gsteps;
         }
     }
     for (; s < nsteps; ++s) {

@@ -220,6 +220,20 @@ public:
     // a non-finite force freezes its replica (steps_left reports -3) instead
     // of failing the step, so a serving loop can retire it alone
     void set_isolate_faults(bool on) { isolate_faults = on; }
+    // launch shapes (the trajectory does not depend on them), chosen by
+    // autotune() or set directly
+    struct Tune {
+        int fb = 128;            // beads (threads) per step-kernel block: 64, 96 or 128
+        int tile_per_sm = 0;     // resident tile-build blocks per SM (0: as many as fit)
+        int graph_steps = 16;    // steps per captured graph: 8, 16 or 32
+    };
+    Tune tuning() const { return tune; }
+    void set_tuning(const Tune &t);
+    // times every candidate shape on a clone of this context (same replicas,
+    // same starting state) and keeps the fastest; this context's state is
+    // not touched.  ms_out (optional) receives the best time per step.
+    Tune autotune(int steps, double *ms_out = nullptr);
+    Tune tune;
     size_t device_bytes() const { return bytes; }
     void set_tethers(int rep, int n, const int32_t *i1, const int32_t *i2, const double *d);
     void set_angles(int rep, int n, const int32_t *i1, const int32_t *i2, const int32_t *i3,
@@ -259,6 +273,8 @@ private:
     double *staging = nullptr;   // packed host-layout buffer [18 N]
     bool timing = false;
     bool isolate_faults = false;
+    void launch_force(int mode, int c);
+    int tile_sms = 1, tile_max_per_sm = 1;     // for the tile build's resident grid
     std::vector<cudaEvent_t> ev_force, ev_rebuild;   // start/stop pairs
     size_t n_ev_force = 0, n_ev_rebuild = 0;
 
@@ -266,7 +282,6 @@ private:
     void launch_force_step();
 
     // graph-captured step chunks, per precision and starting buffer
-    static constexpr int GRAPH_STEPS = 16;
     struct GraphSet {
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;

@@ -90,6 +90,24 @@ class Engine:
         check(self.lib.xmd_gpu_get_state(self.h, rep, dptr(r), dptr(v), C.byref(t)))
         return r.reshape(n, 3), v.reshape(n, 3), t.value
 
+    def autotune(self, steps: int = 96) -> dict:
+        """Times every launch shape on a clone of this context and keeps the
+        fastest (results never depend on the shape)."""
+        shape = np.zeros(3, dtype=np.int32)
+        ms = C.c_double()
+        check(self.lib.xmd_gpu_autotune(self.h, int(steps), iptr(shape), C.byref(ms)))
+        return {"fb": int(shape[0]), "tile_per_sm": int(shape[1]), "graph_steps": int(shape[2]),
+                "ms_per_step": ms.value}
+
+    def tuning(self) -> dict:
+        shape = np.zeros(3, dtype=np.int32)
+        check(self.lib.xmd_gpu_get_tuning(self.h, iptr(shape)))
+        return {"fb": int(shape[0]), "tile_per_sm": int(shape[1]), "graph_steps": int(shape[2])}
+
+    def set_tuning(self, fb: int, tile_per_sm: int, graph_steps: int):
+        shape = np.array([fb, tile_per_sm, graph_steps], dtype=np.int32)
+        check(self.lib.xmd_gpu_set_tuning(self.h, iptr(shape)))
+
     def set_state(self, rep: int, r: np.ndarray, v: np.ndarray | None = None):
         r = np.ascontiguousarray(r, dtype=np.float64).reshape(-1)
         vp = None
