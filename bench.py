@@ -150,6 +150,22 @@ def dist_env():
             int(os.environ.get("WORLD_SIZE", 1)))
 
 
+def job_rate(nbeads: int, md_steps: int, steps: int, t_ms: float, world: int):
+    """Whole-job bead-steps/s: the beads of every rank (each rank steps its own
+    replicas) over the slowest rank's time.  Returns (value, t_max_ms,
+    beads_all_ranks)."""
+    t_max, beads = float(t_ms), float(nbeads)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        tt = torch.tensor([t_ms], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        bb = torch.tensor([float(nbeads)], dtype=torch.float64)
+        dist.all_reduce(bb, op=dist.ReduceOp.SUM)
+        t_max, beads = float(tt.item()), float(bb.item())
+    return beads * md_steps * steps / (t_max / 1e3), t_max, int(beads)
+
+
 def make_workload(rank: int, workers: int):
     from xmd_gb300 import synth
     return synth.config_c4(seed=4 + 1000 * rank, workers=workers)
@@ -219,14 +235,7 @@ def run_engine(args, rank, local, world):
     clk = clocks.stop()
     s1 = stats()
     launches = int(s1[5] - s0[5])
-    t_max = t_ms
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        tt = torch.tensor([t_ms], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
-    value = world * nbeads * md * args.steps / (t_max / 1e3)
+    value, t_max, beads_all = job_rate(nbeads, md, args.steps, t_ms, world)
 
     # dominant kernel: force+integrate, timed with events around each launch
     abi.check(eng.lib.xmd_gpu_set_kernel_timing(eng.h, 1))
@@ -267,7 +276,7 @@ def run_engine(args, rank, local, world):
         abi.check(eng.lib.xmd_gpu_download_positions_all(eng.h, hr.ctypes.data_as(pd)))
     barrier()
     e2e_s = time.perf_counter() - t0
-    e2e_value = world * nbeads * md * e2e_steps / e2e_s
+    e2e_value = job_rate(nbeads, md, e2e_steps, 1e3 * e2e_s, world)[0]
 
     # plain FP64 on the same replicas (same protocol), and the mixed force error
     eng64 = Engine(y_fp64)

@@ -58,7 +58,9 @@ enum {
     XMD_TERM_CONST_ES = 6,  /* eval_const_es_forces src/forces/es/const.cpp:13-32             */
     XMD_TERM_REL_ES = 7,    /* eval_relative_es_forces src/forces/es/relative.cpp:13-32       */
     XMD_TERM_QA = 8,        /* qa::process_contacts src/forces/qa/process_contacts.cpp:13-57  */
-    XMD_NUM_TERMS = 9
+    XMD_TERM_CHIR = 9,      /* eval_chiral_forces src/forces/chiral.cpp:15-37                 */
+    XMD_TERM_NAT_SS = 10,   /* eval_nat_ssbond_forces src/forces/native_ss.cpp:27-40          */
+    XMD_NUM_TERMS = 11
 };
 
 enum { XMD_PREC_FP64 = 0, XMD_PREC_MIXED = 1 };
@@ -118,6 +120,10 @@ typedef struct xmd_params {
     /* engine: Verlet build, XMD_NL_BUILD_* ("nl build: auto | cell | tile");
        both builds keep exactly the same pairs */
     int32_t nl_build;
+    /* chirality (chiral.h: e_chi) */
+    double chir_e_chi;
+    /* native ssbonds (native_ss.h: H1, nat_r = `equilibrium dist`) */
+    double nat_ss_H1, nat_ss_dist;
 } xmd_params;
 
 enum { XMD_NL_BUILD_AUTO = 0, XMD_NL_BUILD_CELL = 1, XMD_NL_BUILD_TILE = 2 };
@@ -180,6 +186,14 @@ int xmd_gpu_set_angles(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *
 int xmd_gpu_set_dihedrals(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1,
                           const int32_t *i2, const int32_t *i3, const int32_t *i4,
                           const double *nat_phi);
+/* Chiral quadruplets (chiral_quad{i1..i4, nat_factor, nat_chir},
+ * main.cpp:372-398): consecutive beads of one chain; nat_factor = |r23|^-3
+ * and nat_chir = r12 . (r23 x r34) * nat_factor of the native structure. */
+int xmd_gpu_set_chirals(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1,
+                        const int32_t *i2, const int32_t *i3, const int32_t *i4,
+                        const double *nat_factor, const double *nat_chir);
+/* Native disulfide bonds (model contacts of type NAT_SS, main.cpp:554-598). */
+int xmd_gpu_set_ssbonds(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1, const int32_t *i2);
 /* All native contacts (nat_cont{i1,i2,nat_dist}, main.cpp:505-552). */
 int xmd_gpu_set_native_contacts(xmd_gpu_ctx *ctx, int32_t rep, int32_t n,
                                 const int32_t *i1, const int32_t *i2,

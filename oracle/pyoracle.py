@@ -37,6 +37,8 @@ def _load(path: Path, pfx: str, params_type):
         "set_angles": (C.c_int, [C.c_void_p, C.c_int32, _pi, _pi, _pi, _pd]),
         "set_dihedrals": (C.c_int, [C.c_void_p, C.c_int32, _pi, _pi, _pi, _pi, _pd]),
         "set_native_contacts": (C.c_int, [C.c_void_p, C.c_int32, _pi, _pi, _pd]),
+        "set_chirals": (C.c_int, [C.c_void_p, C.c_int32, _pi, _pi, _pi, _pi, _pd, _pd]),
+        "set_ssbonds": (C.c_int, [C.c_void_p, C.c_int32, _pi, _pi]),
         "set_state": (C.c_int, [C.c_void_p, _pd, _pd]),
         "set_history": (C.c_int, [C.c_void_p, _pd, C.c_double, C.c_uint64]),
         "get_state": (C.c_int, [C.c_void_p, _pd, _pd, _pd]),
@@ -99,6 +101,12 @@ class Oracle:
         self.fn("set_dihedrals")(self.h, len(d[0]), ip(d[0]), ip(d[1]), ip(d[2]), ip(d[3]), dp(d[4]))
         nc = s.natives
         self.fn("set_native_contacts")(self.h, len(nc[0]), ip(nc[0]), ip(nc[1]), dp(nc[2]))
+        q = getattr(s, "chirals", None)
+        if q is not None:
+            self.fn("set_chirals")(self.h, len(q[0]), ip(q[0]), ip(q[1]), ip(q[2]), ip(q[3]), dp(q[4]), dp(q[5]))
+        b = getattr(s, "ssbonds", None)
+        if b is not None:
+            self.fn("set_ssbonds")(self.h, len(b[0]), ip(b[0]), ip(b[1]))
         self.fn("set_state")(self.h, dp(np.asarray(s.r).reshape(-1)), None)
 
     def fn(self, name):
@@ -117,7 +125,8 @@ class Oracle:
 
     def eval_forces(self):
         F = np.zeros(3 * self.n)
-        V = np.zeros(9)
+        from xmd_gb300.abi import NUM_TERMS
+        V = np.zeros(NUM_TERMS)
         self.fn("eval_forces")(self.h, F.ctypes.data_as(_pd), V.ctypes.data_as(_pd))
         return F.reshape(self.n, 3), V
 

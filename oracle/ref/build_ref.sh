@@ -35,14 +35,14 @@ sed -i '/class sync_diff_expr:/{n;s/sync_data_expr<sync_sum_expr<E1, E2>>/sync_d
   "$OUT/fp64/include/xmd/forces/qa/sync_data.h"
 grep -A1 'class sync_diff_expr:' "$OUT/fp64/include/xmd/forces/qa/sync_data.h" | grep -q 'sync_data_expr<sync_diff_expr<E1, E2>>'
 INC=(-I"$OUT/fp64/include" -I"$OUT/fp64/include/xmd" -I"$REF/src"
-     -I"$REF/ext/gentypes/include" -I"$REF/ext/yaml-cpp-0.7.0/include" -I"$HERE/stub")
+     -I"$REF/ext/gentypes/include" -I"$REF/ext/yaml-cpp-0.7.0/include" -I"$REF/ext/eigen-3.4.0" -I"$HERE/stub")
 FLAGS=(-std=c++17 -O2 -fPIC -Wno-changes-meaning -Dparticle_pairs=non_native)
 TUS=(forces/tether forces/go forces/primitives/lj forces/primitives/sink_lj
      forces/primitives/harmonic forces/angle/native forces/dihedral/complex_native
      forces/dihedral/simple_native forces/pauli forces/es/const forces/es/relative
      forces/es/es_pair forces/qa/precompute_nh forces/qa/sift_candidates
      forces/qa/process_candidates forces/qa/process_contacts forces/qa/free_pair
-     dynamics/lang_pc nl/verify)
+     dynamics/lang_pc nl/verify forces/chiral forces/native_ss)
 OBJS=()
 pids=()
 for tu in "${TUS[@]}"; do

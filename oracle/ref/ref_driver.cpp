@@ -28,6 +28,8 @@
 #include <xmd/forces/dihedral/complex_native.h>
 #include <xmd/forces/dihedral/simple_native.h>
 #include <xmd/forces/go.h>
+#include <xmd/forces/chiral.h>
+#include <xmd/forces/native_ss.h>
 #include <xmd/forces/pauli.h>
 #include <xmd/forces/es/const.h>
 #include <xmd/forces/es/relative.h>
@@ -76,6 +78,9 @@ struct xr_sys {
     ::vector<nat_dih> dihedrals;
     ::vector<nat_cont> all_nat_cont, go_contacts;
     std::vector<std::pair<int, int>> nat_sorted;
+    ::vector<chiral_quad> quads;
+    ::vector<nat_ss> all_ss, cur_ss;
+    std::vector<std::pair<int, int>> ss_sorted;
 
     nl::nl_data nl, nl_qa;
     bool invalid = true, first_time = true;
@@ -98,6 +103,7 @@ void derive(xr_sys *s) {
     auto &p = s->p;
     real mc = 0;
     if (p.on[XMD_TERM_PAULI]) mc = std::max(mc, (real)p.pauli_r_excl);
+    if (p.on[XMD_TERM_NAT_SS]) mc = std::max(mc, harmonic::cutoff((real)p.nat_ss_dist));   // main.cpp:596-597
     if (p.on[XMD_TERM_GO]) {
         real c = 0;
         for (int k = 0; k < s->all_nat_cont.size(); ++k)
@@ -130,7 +136,7 @@ void legacy_update_restated(xr_sys *s) {
     s->nl.native_contacts.clear();
     s->nl.native_ssbonds.clear();
     s->nl.non_native.clear();
-    size_t nat_idx = 0;
+    size_t nat_idx = 0, ss_idx = 0;
     for (int i1 = 0; i1 < s->n; ++i1) {
         auto r1 = s->r[i1];
         auto chain1 = s->chain[i1], seq1 = s->seq[i1];
@@ -148,6 +154,12 @@ void legacy_update_restated(xr_sys *s) {
                 while (s->p.on[XMD_TERM_GO] && nat_idx < s->nat_sorted.size() && s->nat_sorted[nat_idx] < key) ++nat_idx;
                 if (s->p.on[XMD_TERM_GO] && nat_idx < s->nat_sorted.size() && s->nat_sorted[nat_idx] == key) {
                     s->nl.native_contacts.emplace_back(i1, i2, orig_dist);
+                    non_native = false;
+                }
+                // all_nat_ss is wired with native ssbonds enabled (main.cpp:579-580)
+                while (s->p.on[XMD_TERM_NAT_SS] && ss_idx < s->ss_sorted.size() && s->ss_sorted[ss_idx] < key) ++ss_idx;
+                if (s->p.on[XMD_TERM_NAT_SS] && ss_idx < s->ss_sorted.size() && s->ss_sorted[ss_idx] == key) {
+                    s->nl.native_ssbonds.emplace_back(i1, i2, orig_dist);
                     non_native = false;
                 }
                 if (non_native) s->nl.non_native.emplace_back(i1, i2, orig_dist);
@@ -175,6 +187,18 @@ void rebuild_lists(xr_sys *s) {
         up();
     } else {
         s->pauli_pairs.clear();
+    }
+    if (p.on[XMD_TERM_NAT_SS]) {
+        update_nat_ssbonds us;
+        us.cutoff = harmonic::cutoff((real)p.nat_ss_dist);   // never set by main.cpp:588-594 [D14]
+        us.r = s->r.data();
+        us.box = &s->bx;
+        us.nl = &s->nl;
+        us.all_ssbonds = &s->all_ss;
+        us.ssbonds = &s->cur_ss;
+        us();
+    } else {
+        s->cur_ss.clear();
     }
     // restated update_go_contacts::operator() (go.cpp:8-23) [D1]
     s->go_contacts.clear();
@@ -313,6 +337,18 @@ void term_forces(xr_sys *s, ::vector<vec3r> &F, real *V) {
         e.r = s->r.data(); e.F = F.data(); e.box = &s->bx; e.es_pairs = &s->es_pairs; e.V = &V[XMD_TERM_REL_ES];
         e();
     }
+    if (p.on[XMD_TERM_CHIR]) {
+        eval_chiral_forces e;
+        e.e_chi = p.chir_e_chi;
+        e.r = s->r.data(); e.F = F.data(); e.quads = s->quads.view(); e.V = &V[XMD_TERM_CHIR];
+        e();
+    }
+    if (p.on[XMD_TERM_NAT_SS]) {
+        eval_nat_ssbond_forces e;
+        e.H1 = p.nat_ss_H1; e.nat_r = p.nat_ss_dist;
+        e.r = s->r.data(); e.F = F.data(); e.box = &s->bx; e.ssbonds = &s->cur_ss; e.V = &V[XMD_TERM_NAT_SS];
+        e();
+    }
 }
 
 void setup_proc_contacts(xr_sys *s, qa::process_contacts &pc, ::vector<vec3r> &F, real *V,
@@ -422,6 +458,26 @@ int xr_set_dihedrals(void *h, int32_t n, const int32_t *i1, const int32_t *i2, c
     auto *s = (xr_sys *)h;
     s->dihedrals.clear();
     for (int k = 0; k < n; ++k) s->dihedrals.emplace_back(i1[k], i2[k], i3[k], i4[k], (real)ph[k]);
+    return 0;
+}
+// chiral quads by field name (main.cpp:391 passes nat_factor where the
+// gentype's fifth field is nat_chir, chiral.h:9 [D15])
+int xr_set_chirals(void *h, int32_t n, const int32_t *i1, const int32_t *i2, const int32_t *i3, const int32_t *i4,
+                   const double *nat_factor, const double *nat_chir) {
+    auto *s = (xr_sys *)h;
+    s->quads.clear();
+    for (int k = 0; k < n; ++k) s->quads.emplace_back(i1[k], i2[k], i3[k], i4[k], (real)nat_chir[k], (real)nat_factor[k]);
+    return 0;
+}
+int xr_set_ssbonds(void *h, int32_t n, const int32_t *i1, const int32_t *i2) {
+    auto *s = (xr_sys *)h;
+    std::vector<std::pair<int, int>> v;
+    for (int k = 0; k < n; ++k) v.emplace_back(std::min(i1[k], i2[k]), std::max(i1[k], i2[k]));
+    std::sort(v.begin(), v.end());
+    s->all_ss.clear();
+    s->ss_sorted = v;
+    for (auto &[a, b] : v) s->all_ss.emplace_back(a, b);
+    s->first_time = true;
     return 0;
 }
 int xr_set_native_contacts(void *h, int32_t n, const int32_t *i1, const int32_t *i2, const double *d) {

@@ -120,6 +120,9 @@ struct xo_sys {
     int32_t n_ang; int32_t *ang_i; double *ang_t;
     int32_t n_dih; int32_t *dih_i; double *dih_p;
     int32_t n_nat; pair_d *nat;
+    int32_t n_chir; int32_t *chir_i; double *chir_f, *chir_n;   /* chiral_quad (chiral.h) */
+    int32_t n_ss_all; pair_i *ss_all;                           /* native ssbonds (nat_ss) */
+    pair_i *ss; int32_t n_ss;                                   /* update_nat_ssbonds' list */
     /* state */
     double *r, *v, *y[6], *F;
     double t, true_t;
@@ -175,6 +178,7 @@ static void derive_cutoffs(xo_sys *s) {
     /* max_cutoff accumulation: main.cpp:500, 545-551, 628-630, 642-644, 742-746 */
     double mc = 0.0;
     if (p->on[XMD_TERM_PAULI]) mc = fmax(mc, p->pauli_r_excl);
+    if (p->on[XMD_TERM_NAT_SS]) mc = fmax(mc, 2.0 * p->nat_ss_dist);   /* harmonic::cutoff, main.cpp:596-597 */
     if (p->on[XMD_TERM_GO]) {
         double c = 0.0;
         for (int k = 0; k < s->n_nat; ++k) c = fmax(c, 2.0 * s->nat[k].d); /* lj::cutoff lj.cpp:8-10 */
@@ -257,6 +261,7 @@ void xo_destroy(xo_sys *s) {
     free(s->chain); free(s->seq); free(s->prev); free(s->next); free(s->atype);
     free(s->teth_i); free(s->teth_d); free(s->ang_i); free(s->ang_t);
     free(s->dih_i); free(s->dih_p); free(s->nat);
+    free(s->chir_i); free(s->chir_f); free(s->chir_n); free(s->ss_all); free(s->ss);
     free(s->r); free(s->v); free(s->F);
     for (int k = 0; k < 6; ++k) free(s->y[k]);
     free(s->orig_r); free(s->nl); free(s->go); free(s->pauli); free(s->es);
@@ -322,6 +327,42 @@ int xo_set_native_contacts(xo_sys *s, int32_t n, const int32_t *i1, const int32_
     /* the merge of legacy_update.cpp:33-43 needs the list sorted (nl/pair.h:19-25) */
     qsort(s->nat, n, sizeof(pair_d), cmp_pair_d);
     derive_cutoffs(s);
+    s->first_time = 1;
+    return 0;
+}
+
+/* chiral quads (main.cpp:372-398): parameters from the native structure */
+int xo_set_chirals(xo_sys *s, int32_t n, const int32_t *i1, const int32_t *i2, const int32_t *i3,
+                   const int32_t *i4, const double *nat_factor, const double *nat_chir) {
+    free(s->chir_i); free(s->chir_f); free(s->chir_n);
+    s->n_chir = n;
+    s->chir_i = (int32_t *)malloc(sizeof(int32_t) * 4 * (n ? n : 1));
+    s->chir_f = (double *)malloc(sizeof(double) * (n ? n : 1));
+    s->chir_n = (double *)malloc(sizeof(double) * (n ? n : 1));
+    for (int k = 0; k < n; ++k) {
+        s->chir_i[4 * k] = i1[k]; s->chir_i[4 * k + 1] = i2[k];
+        s->chir_i[4 * k + 2] = i3[k]; s->chir_i[4 * k + 3] = i4[k];
+        s->chir_f[k] = nat_factor[k];
+        s->chir_n[k] = nat_chir[k];
+    }
+    return 0;
+}
+static int cmp_pair_i0(const void *a, const void *b) {
+    const pair_i *x = (const pair_i *)a, *y = (const pair_i *)b;
+    if (x->i1 != y->i1) return x->i1 < y->i1 ? -1 : 1;
+    if (x->i2 != y->i2) return x->i2 < y->i2 ? -1 : 1;
+    return 0;
+}
+/* native disulfides (model contacts of type NAT_SS, main.cpp:554-598) */
+int xo_set_ssbonds(xo_sys *s, int32_t n, const int32_t *i1, const int32_t *i2) {
+    free(s->ss_all);
+    s->n_ss_all = n;
+    s->ss_all = (pair_i *)malloc(sizeof(pair_i) * (n ? n : 1));
+    for (int k = 0; k < n; ++k) {
+        s->ss_all[k].i1 = i1[k] < i2[k] ? i1[k] : i2[k];
+        s->ss_all[k].i2 = i1[k] < i2[k] ? i2[k] : i1[k];
+    }
+    qsort(s->ss_all, n, sizeof(pair_i), cmp_pair_i0);
     s->first_time = 1;
     return 0;
 }
@@ -527,7 +568,7 @@ static void nl_rebuild(xo_sys *s) {
     cgrid g;
     grid_build(s, &g);
     int *part = (int *)malloc(sizeof(int) * s->n);
-    int64_t nat_idx = 0;
+    int64_t nat_idx = 0, ss_idx = 0;
     for (int i1 = 0; i1 < s->n; ++i1) {
         v3 r1 = ld(s->r, i1);
         int chain1 = s->chain[i1], seq1 = s->seq[i1];
@@ -547,6 +588,14 @@ static void nl_rebuild(xo_sys *s) {
                        (s->nat[nat_idx].i1 < i1 || (s->nat[nat_idx].i1 == i1 && s->nat[nat_idx].i2 < i2)))
                     ++nat_idx;
                 if (p->on[XMD_TERM_GO] && nat_idx < s->n_nat && s->nat[nat_idx].i1 == i1 && s->nat[nat_idx].i2 == i2)
+                    non_native = 0;
+                /* the same merge against the native disulfides, which take
+                   part with that term enabled (main.cpp:579-580) */
+                while (p->on[XMD_TERM_NAT_SS] && ss_idx < s->n_ss_all &&
+                       (s->ss_all[ss_idx].i1 < i1 || (s->ss_all[ss_idx].i1 == i1 && s->ss_all[ss_idx].i2 < i2)))
+                    ++ss_idx;
+                if (p->on[XMD_TERM_NAT_SS] && ss_idx < s->n_ss_all && s->ss_all[ss_idx].i1 == i1 &&
+                    s->ss_all[ss_idx].i2 == i2)
                     non_native = 0;
                 if (non_native) {                                       /* [D3] */
                     GROW(s->nl, s->n_nl, s->cap_nl, pair_i);
@@ -578,6 +627,16 @@ static void nl_rebuild(xo_sys *s) {
                 s->n_pauli++;
             }
         }
+    }
+    /* update_nat_ssbonds: native_ss.cpp:8-19, cutoff = harmonic::cutoff(nat_r)
+       = 2 nat_r [D14] */
+    free(s->ss);
+    s->ss = (pair_i *)malloc(sizeof(pair_i) * (s->n_ss_all ? s->n_ss_all : 1));
+    s->n_ss = 0;
+    if (p->on[XMD_TERM_NAT_SS]) {
+        for (int k = 0; k < s->n_ss_all; ++k)
+            if (nrm(r_uv(s, ld(s->r, s->ss_all[k].i1), ld(s->r, s->ss_all[k].i2))) < 2.0 * p->nat_ss_dist + s->orig_pad)
+                s->ss[s->n_ss++] = s->ss_all[k];
     }
     /* update_go_contacts: go.cpp:8-23 */
     free(s->go);
@@ -950,6 +1009,40 @@ static void qa_contact_transition(xo_sys *s, int64_t idx) {
 
 /* ---- force phase ------------------------------------------------------------- */
 
+/* eval_chiral_forces::iter: src/forces/chiral.cpp:15-37 */
+static void chiral_iter(const xo_sys *s, int idx, double *F, double *V) {
+    int i1 = s->chir_i[4 * idx], i2 = s->chir_i[4 * idx + 1], i3 = s->chir_i[4 * idx + 2], i4 = s->chir_i[4 * idx + 3];
+    double nat_chir = s->chir_n[idx], nat_factor = s->chir_f[idx];
+    v3 r1 = ld(s->r, i1), r2 = ld(s->r, i2), r3 = ld(s->r, i3), r4 = ld(s->r, i4);
+    v3 r12 = sub(r2, r1), r23 = sub(r3, r2), r34 = sub(r4, r3);
+    v3 x12_23 = cross(r12, r23), x12_34 = cross(r12, r34), x23_34 = cross(r23, r34);
+    double chir = dot(r12, x23_34) * nat_factor;
+    double chir_diff = chir - nat_chir;
+    *V += 0.5 * s->p.chir_e_chi * chir_diff * chir_diff;
+    double f = s->p.chir_e_chi * chir_diff * nat_factor;
+    acc(F, i1, scl(f, x12_23));
+    dec(F, i2, scl(f, add(x12_34, x23_34)));
+    acc(F, i3, scl(f, add(x12_23, x12_34)));
+    dec(F, i4, scl(f, x12_23));
+}
+
+/* eval_nat_ssbond_forces::iter: src/forces/native_ss.cpp:27-40 */
+static void ss_iter(const xo_sys *s, int idx, double *F, double *V) {
+    int i1 = s->ss[idx].i1, i2 = s->ss[idx].i2;
+    v3 r12 = r_uv(s, ld(s->r, i1), ld(s->r, i2));
+    double r12_n = nrm(r12);
+    /* harmonic(H1, 0, nat_r): harmonic.h:18-25 */
+    double dr = r12_n - s->p.nat_ss_dist, dr2 = dr * dr;
+    double V_ = 0.5 * dr2 * (s->p.nat_ss_H1 + 0.0 * dr2);
+    double dV_dr = dr * (s->p.nat_ss_H1 + 2.0 * 0.0 * dr2);
+    V_ = clampd(V_, -1.0e3, 1.0e3);
+    dV_dr = clampd(dV_dr, -1.0e3, 1.0e3);
+    v3 r12_u = {r12.x / r12_n, r12.y / r12_n, r12.z / r12_n};   /* r12 / r12_n: per component */
+    *V += V_;
+    acc(F, i1, scl(dV_dr, r12_u));
+    dec(F, i2, scl(dV_dr, r12_u));
+}
+
 static void pure_forces(const xo_sys *s, double *F, double *V) {
     const xmd_params *p = &s->p;
     memset(F, 0, sizeof(double) * 3 * (size_t)s->n);
@@ -963,6 +1056,8 @@ static void pure_forces(const xo_sys *s, double *F, double *V) {
     if (p->on[XMD_TERM_CONST_ES]) for (int64_t k = 0; k < s->n_es; ++k) es_iter(s, k, 0, F, &V[XMD_TERM_CONST_ES]);
     if (p->on[XMD_TERM_REL_ES]) for (int64_t k = 0; k < s->n_es; ++k) es_iter(s, k, 1, F, &V[XMD_TERM_REL_ES]);
     if (p->on[XMD_TERM_QA]) for (int64_t k = 0; k < s->n_cont; ++k) qa_contact_force(s, k, F, &V[XMD_TERM_QA]);
+    if (p->on[XMD_TERM_CHIR]) for (int k = 0; k < s->n_chir; ++k) chiral_iter(s, k, F, &V[XMD_TERM_CHIR]);
+    if (p->on[XMD_TERM_NAT_SS]) for (int k = 0; k < s->n_ss; ++k) ss_iter(s, k, F, &V[XMD_TERM_NAT_SS]);
 }
 
 int xo_eval_forces(xo_sys *s, double *F, double *V) {
@@ -1103,6 +1198,14 @@ int xo_step_omp(xo_sys *s, int32_t nsteps, int32_t nthreads) {
             if (p->on[XMD_TERM_REL_ES]) {
 #pragma omp for schedule(static) nowait
                 for (int64_t k = 0; k < s->n_es; ++k) es_iter(s, k, 1, F, &V[XMD_TERM_REL_ES]);
+            }
+            if (p->on[XMD_TERM_CHIR]) {
+#pragma omp for schedule(static) nowait
+                for (int k = 0; k < s->n_chir; ++k) chiral_iter(s, k, F, &V[XMD_TERM_CHIR]);
+            }
+            if (p->on[XMD_TERM_NAT_SS]) {
+#pragma omp for schedule(static) nowait
+                for (int k = 0; k < s->n_ss; ++k) ss_iter(s, k, F, &V[XMD_TERM_NAT_SS]);
             }
             if (p->on[XMD_TERM_QA]) {
 #pragma omp for schedule(static) nowait

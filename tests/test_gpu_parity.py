@@ -282,10 +282,12 @@ def test_per_term_forces(case, term):
     normalised by that term's own force scale."""
     s, y, _ = load_golden(case)
     names = ["tether forces", "native angles", "complex native dihedrals", "simple native dihedrals",
-             "native contacts", "Pauli exclusion", "const ES", "relative ES", "quasi-adiabatic potential"]
+             "native contacts", "Pauli exclusion", "const ES", "relative ES", "quasi-adiabatic potential",
+             "chirality", "native ssbonds"]
     full = abi.parse_params(y)
     mc = Oracle(full, s, "port").cutoffs()
-    yy = y + "".join(f"\n{names[k]}:\n  enabled: {'true' if k == term else 'false'}\n" for k in range(9))
+    yy = y + "".join(f"\n{names[k]}:\n  enabled: {'true' if k == term else 'false'}\n"
+                     for k in range(abi.NUM_TERMS))
     yy += f"\nneighbor list:\n  cutoff: {float(mc[0] / ANGSTROM)!r} A\n  skin: {float(mc[1] / ANGSTROM)!r} A\n"
     p = abi.parse_params(yy)
     Fo, Vo = Oracle(p, s, "port").eval_forces()

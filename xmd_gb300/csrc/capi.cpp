@@ -159,6 +159,20 @@ int xmd_gpu_set_angles(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *
     return guard([&] { ctx->eng->use_device(); ctx->eng->set_angles(rep, n, i1, i2, i3, nat_theta); });
 }
 
+int xmd_gpu_set_chirals(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1, const int32_t *i2,
+                        const int32_t *i3, const int32_t *i4, const double *nat_factor, const double *nat_chir) {
+    NEED_CTX;
+    if (n < 0 || (n > 0 && (!i1 || !i2 || !i3 || !i4 || !nat_factor || !nat_chir)))
+        return fail(XMD_ERR_ARG, "set_chirals: null array");
+    return guard([&] { ctx->eng->set_chirals(rep, n, i1, i2, i3, i4, nat_factor, nat_chir); });
+}
+
+int xmd_gpu_set_ssbonds(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1, const int32_t *i2) {
+    NEED_CTX;
+    if (n < 0 || (n > 0 && (!i1 || !i2))) return fail(XMD_ERR_ARG, "set_ssbonds: null array");
+    return guard([&] { ctx->eng->set_ssbonds(rep, n, i1, i2); });
+}
+
 int xmd_gpu_set_dihedrals(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1, const int32_t *i2,
                           const int32_t *i3, const int32_t *i4, const double *nat_phi) {
     NEED_CTX;

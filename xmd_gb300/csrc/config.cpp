@@ -527,6 +527,11 @@ void resolve_params(const YNode &root, xmd_params *o) {
     o->on[XMD_TERM_REL_ES] = enabled(root, "relative ES");
     o->rel_es_screen_dist = qval(section(root, "relative ES"), "screening distance", "relative ES: ");
     o->rel_es_factor = qval(section(root, "relative ES"), "factor", "relative ES: ");
+    o->on[XMD_TERM_CHIR] = enabled(root, "chirality");
+    o->chir_e_chi = qval(section(root, "chirality"), "e_chi", "chirality: ");
+    o->on[XMD_TERM_NAT_SS] = enabled(root, "native ssbonds");
+    o->nat_ss_H1 = qval(section(root, "native ssbonds"), "H1", "native ssbonds: ");
+    o->nat_ss_dist = qval(section(root, "native ssbonds"), "equilibrium dist", "native ssbonds: ");
     o->on[XMD_TERM_QA] = enabled(root, "quasi-adiabatic potential");
     {
         const YNode &q = section(root, "quasi-adiabatic potential");

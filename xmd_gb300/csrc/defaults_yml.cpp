@@ -48,6 +48,15 @@ native contacts:
   lj depth: 1 eps
   active threshold: 1.5
 
+chirality:
+  enabled: false
+  e_chi: 1 eps
+
+native ssbonds:
+  enabled: true
+  H1: 100 eps/A**2
+  equilibrium dist: 6.0 A
+
 Pauli exclusion:
   enabled: true
   r_excl: 4.0 A

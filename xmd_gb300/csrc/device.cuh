@@ -302,6 +302,42 @@ __device__ __forceinline__ void dihedral_term(const TermP &p, double4_32a q1, do
     f[3] = -(dV * d4);
 }
 
+// chiral quad (c-1, c, c+1, c+2): eval_chiral_forces::iter chiral.cpp:15-37.
+// Writes the forces on the four beads.
+template <class T>
+__device__ __forceinline__ void chiral_term(const TermP &p, double4_32a q1, double4_32a q2, double4_32a q3,
+                                            double4_32a q4, T nat_factor, T nat_chir, V3<T> *f, T *V) {
+    V3<T> r12 = diff<T>(q1, q2), r23 = diff<T>(q2, q3), r34 = diff<T>(q3, q4);
+    V3<T> x12_23 = cross(r12, r23), x12_34 = cross(r12, r34), x23_34 = cross(r23, r34);
+    T chir = dot(r12, x23_34) * nat_factor;
+    T chir_diff = chir - nat_chir;
+    T e_chi = T(p.chir_e_chi);
+    *V = T(0.5) * e_chi * chir_diff * chir_diff;
+    T g = e_chi * chir_diff * nat_factor;
+    f[0] = g * x12_23;
+    f[1] = -(g * (x12_34 + x23_34));
+    f[2] = g * (x12_23 + x12_34);
+    f[3] = -(g * x12_23);
+}
+
+// the same on the mixed path: r12, r23, r34 the narrowed bond vectors,
+// x12_23, x23_34 their narrowed float-float crosses, triple = r12 . x23_34
+// taken in float-float
+__device__ __forceinline__ void chiral_mixed(const TermP &p, V3<float> r12, V3<float> r23, V3<float> r34,
+                                             V3<float> x12_23, V3<float> x23_34, float triple, float nat_factor,
+                                             float nat_chir, V3<float> *f, float *V) {
+    (void)r23;
+    const V3<float> x12_34 = cross(r12, r34);
+    const float chir_diff = triple * nat_factor - nat_chir;
+    const float e_chi = p.f.chir_e_chi;
+    *V = 0.5f * e_chi * chir_diff * chir_diff;
+    const float g = e_chi * chir_diff * nat_factor;
+    f[0] = g * x12_23;
+    f[1] = -(g * (x12_34 + x23_34));
+    f[2] = g * (x12_23 + x12_34);
+    f[3] = -(g * x12_23);
+}
+
 // ---- bonded terms of the mixed path -------------------------------------------
 // The reference formulation (acos of a clamped cosine; cross products of bond
 // vectors) loses all accuracy in FP32 near straight triples, where the stiff
@@ -408,6 +444,21 @@ __device__ __forceinline__ V3<T> go_pair(const TermP &p, V3<T> r12, T nat_dist, 
     T dV;
     lj_eval<T>(tpar<T>(p.go_depth, p.f.go_depth), nat_dist, r12_rn, V, &dV);
     return dV * u;
+}
+
+// native disulfide: eval_nat_ssbond_forces::iter native_ss.cpp:27-40,
+// harmonic(H1, 0, nat_r) (harmonic.h:18-25) on the bond length
+template <class T>
+__device__ __forceinline__ V3<T> ss_pair(const TermP &p, V3<T> r12, T *V) {
+    const T r12_n = norm(r12);
+    const T nat_r = tpar<T>(p.nat_ss_dist, p.f.nat_ss_dist), H1 = tpar<T>(p.nat_ss_H1, p.f.nat_ss_H1);
+    const T dr = r12_n - nat_r, dr2 = dr * dr;
+    T V_ = T(0.5) * dr2 * (H1 + T(0) * dr2);
+    T dV_dr = dr * (H1 + T(2) * T(0) * dr2);
+    *V = clampv<T>(V_, T(-1.0e3), T(1.0e3));
+    dV_dr = clampv<T>(dV_dr, T(-1.0e3), T(1.0e3));
+    const V3<T> u{r12.x / r12_n, r12.y / r12_n, r12.z / r12_n};
+    return dV_dr * u;
 }
 
 // Pauli exclusion: eval_pauli_exclusion_forces::iter pauli.cpp:32-48,

@@ -254,6 +254,24 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
                 }
             }
         }
+        // chirality of the quad (c-1, c, c+1, c+2): eval_chiral_forces::iter,
+        // chiral.cpp:15-37; its forces join the dihedral slots of the centre
+        if ((fl & BF_CHIR) && p.on[XMD_TERM_CHIR]) {
+            V3<FT> g[4];
+            FT Vch;
+            if constexpr (sizeof(FT) == 8) {
+                const double2 cp = d.chir[c];
+                chiral_term<FT>(p, P[sp - 1], P[sp], P[sp + 1], P[sp + 2], (FT)cp.x, (FT)cp.y, g, &Vch);
+            } else {
+                const float2 cp = d.chir_f32[c];
+                // the triple product in float-float: planar quads are well conditioned
+                const float tp = ff_dot(Eff[sp - 1], Xff[sp + 1]).h;
+                chiral_mixed(p, Ef[sp - 1], Ef[sp], Ef[sp + 1], Xf[sp], Xf[sp + 1], tp, cp.x, cp.y, g, &Vch);
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) q[k] = q[k] + g[k];
+            if (MODE == 0 && own) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_CHIR], (double)Vch);
+        }
         Ct[sc] = ft;
         Ca[0][sc] = a1; Ca[1][sc] = a2; Ca[2][sc] = a3;
         Cd[0][sc] = q[0]; Cd[1][sc] = q[1]; Cd[2][sc] = q[2]; Cd[3][sc] = q[3];
@@ -328,6 +346,18 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
             j = jn;
             on = onn;
             nd = ndn;
+        }
+    }
+    double vss = 0;
+    if (p.on[XMD_TERM_NAT_SS]) {
+        const int s1 = d.ss_end[i];
+        for (int k = d.ss_start[i]; k < s1; ++k) {
+            if (!d.ss_on[k]) continue;
+            const int j = d.ss_j[k];
+            FT V_;
+            V3<FT> f = ss_pair<FT>(p, geo.to(pin[j]), &V_);
+            acc.add(f);
+            if (MODE == 0 && i < j) vss += (double)V_;
         }
     }
     const int cnt = pf_cnt;
@@ -417,6 +447,7 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
         if (vpa != 0.0) atomicAdd(&Vr[XMD_TERM_PAULI], vpa);
         if (ves != 0.0) atomicAdd(&Vr[p.es_rel ? XMD_TERM_REL_ES : XMD_TERM_CONST_ES], ves);
         if (vqa != 0.0) atomicAdd(&Vr[XMD_TERM_QA], vqa);
+        if (vss != 0.0) atomicAdd(&Vr[XMD_TERM_NAT_SS], vss);
         return;
     }
 
@@ -912,6 +943,14 @@ __global__ void __launch_bounds__(NC_WARPS * 32, 3) k_nl_cells(Dev d, TermP p, i
     const int nref = qa_on ? min(d.qa.ref_cnt[i], QA_REF_CAP) : 0;
     const int nnat = n1 - n0;
     const int my_nat = lane < nnat ? d.nat_j[n0 + lane] : -1;
+    // disulfide list (update_nat_ssbonds, native_ss.cpp:8-19) and partners
+    const bool ss_on = p.on[XMD_TERM_NAT_SS] != 0;
+    const int ss0 = d.ss_start[i], ss1 = d.ss_end[i];
+    if (ss_on)
+        for (int k = ss0 + lane; k < ss1; k += 32)
+            d.ss_on[k] = dist2_exact(bx, pi, pos[d.ss_j[k]]) < rp.s_ss;
+    const int nss = ss_on ? ss1 - ss0 : 0;
+    const int my_ss = lane < nss ? d.ss_j[ss0 + lane] : -1;
     int my_qa = -1;
     if (lane < nref) {
         const int s = d.qa.ref[(size_t)lane * d.N + i];
@@ -982,6 +1021,16 @@ __global__ void __launch_bounds__(NC_WARPS * 32, 3) k_nl_cells(Dev d, TermP p, i
             if (qa_on && __any_sync(FULL, qa_free))
                 for (int k = 0; k < nref; ++k)
                     if (__shfl_sync(FULL, my_qa, k) == j) qa_free = false;
+            // a native disulfide is in no non-native list (main.cpp:579-580)
+            if (nss && __any_sync(FULL, flags != 0 || qa_free)) {
+                if (nss <= 32) {
+                    for (int k = 0; k < nss; ++k)
+                        if (__shfl_sync(FULL, my_ss, k) == j) { flags = 0; qa_free = false; }
+                } else {
+                    for (int k = ss0; k < ss1; ++k)
+                        if (d.ss_j[k] == j) { flags = 0; qa_free = false; }
+                }
+            }
             const unsigned km = __ballot_sync(FULL, flags != 0);
             if (flags) {
                 const int at = cnt + __popc(km & lt);
@@ -1156,6 +1205,7 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
     const bool go_on = p.on[XMD_TERM_GO] != 0;
     const bool es_on = (p.on[XMD_TERM_CONST_ES] || p.on[XMD_TERM_REL_ES]);
     const bool qa_on = d.qa_on && p.on[XMD_TERM_QA];
+    const bool ss_on = p.on[XMD_TERM_NAT_SS] != 0;
     const Band Breq = bands_s[0], Bpa = bands_s[1], Bes = bands_s[2], Bqa = bands_s[3];
     const float Lx = narrow_f(bx.cell[0]), Ly = narrow_f(bx.cell[1]), Lz = narrow_f(bx.cell[2]);
     const bool periodic = (rp.per[0] | rp.per[1] | rp.per[2]) != 0;
@@ -1199,6 +1249,17 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
             else on = d2 < B.lo;
             d.nat_on[k] = on;
         }
+
+        // disulfide list: update_nat_ssbonds, native_ss.cpp:8-19 (exact test;
+        // a bead has at most a few disulfides)
+        const int ss0 = d.ss_start[i], ss1 = d.ss_end[i];
+        if (ss_on)
+            for (int k = ss0 + lane; k < ss1; k += 32) {
+                const double4_32a pj = pos[d.ss_j[k]];
+                d.ss_on[k] = (periodic ? dist2_exact(bx, pi, pj) : dist2_open(pi, pj)) < rp.s_ss;
+            }
+        const int nss = ss_on ? ss1 - ss0 : 0;
+        const int my_ss = lane < nss ? d.ss_j[ss0 + lane] : -1;
 
         int nref = 0;
         if (qa_on) nref = min(d.qa.ref_cnt[i], QA_REF_CAP);
@@ -1273,6 +1334,17 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
             if (qa_on && __any_sync(0xffffffffu, qa_free))
                 for (int k = 0; k < nref; ++k)
                     if (__shfl_sync(0xffffffffu, my_qa, k) == b + lj) qa_free = false;
+            // a native disulfide is in no non-native list (legacy_update's
+            // merge against all_nat_ss, main.cpp:579-580)
+            if (nss && __any_sync(0xffffffffu, flags != 0 || qa_free)) {
+                if (nss <= 32) {
+                    for (int k = 0; k < nss; ++k)
+                        if (__shfl_sync(0xffffffffu, my_ss, k) == b + lj) { flags = 0; qa_free = false; }
+                } else {
+                    for (int k = ss0; k < ss1; ++k)
+                        if (d.ss_j[k] == b + lj) { flags = 0; qa_free = false; }
+                }
+            }
             const unsigned km = __ballot_sync(0xffffffffu, flags != 0);
             if (flags) {
                 const int at = cnt + __popc(km & lt);
@@ -1406,6 +1478,8 @@ int Engine::add_replica(int n, const int32_t *chain, const int32_t *seq, const u
     r.teth_r0.assign(n, nan);
     r.ang_t0.assign(n, nan);
     r.dih_p0.assign(n, nan);
+    r.chir_f.assign(n, nan);
+    r.chir_n.assign(n, nan);
     if (dynamic) {
         // reuse a free slot; the replica is placed at the next eval/step
         for (int k = 0; k < (int)reps.size(); ++k)
@@ -1436,6 +1510,7 @@ void Engine::reserve(int beads, int replicas, int natives) {
     cap.beads = beads;
     cap.reps = replicas;
     cap.nat = natives;
+    cap.ss = natives;   // disulfide entries share the native budget
     // bucket pool for replicas above the tile limit; chunk slots for the rest
     cap.cells = params.nl_build == XMD_NL_BUILD_TILE ? 0 : std::max(64, 2 * beads);
     cap.chunks = params.nl_build == XMD_NL_BUILD_CELL ? 0 : beads / TL_CH + replicas;
@@ -1462,6 +1537,9 @@ void Engine::remove_replica(int rep) {
         update_blocks(b, b + n);
         a_beads.release(b, n);
         a_nat.release(r.nat_off, r.nat_len);
+        a_ss.release(r.ss_off, r.ss_len);
+        CK(cudaMemsetAsync(d.ss_start + b, 0, sizeof(int32_t) * n, stream));
+        CK(cudaMemsetAsync(d.ss_end + b, 0, sizeof(int32_t) * n, stream));
         a_cells.release(r.cell_off, r.cell_len);
         a_chunks.release(r.chunk_off, r.chunk_len);
     }
@@ -1567,6 +1645,38 @@ void Engine::set_native(int rep, int n, const int32_t *i1, const int32_t *i2, co
     for (auto &[a, b, x] : v) { r.nat_i1.push_back(a); r.nat_i2.push_back(b); r.nat_d.push_back(x); }
 }
 
+void Engine::set_chirals(int rep, int n, const int32_t *i1, const int32_t *i2, const int32_t *i3,
+                         const int32_t *i4, const double *f, const double *c) {
+    check_rep(reps, rep);
+    if (reps[rep].placed) throw std::invalid_argument("topology is fixed once the replica is on the device");
+    RepHost &r = reps[rep];
+    std::fill(r.chir_f.begin(), r.chir_f.end(), std::nan(""));
+    std::fill(r.chir_n.begin(), r.chir_n.end(), std::nan(""));
+    for (int k = 0; k < n; ++k) {
+        if (!consecutive(r, i1[k], i2[k]) || !consecutive(r, i2[k], i3[k]) || !consecutive(r, i3[k], i4[k]))
+            throw std::invalid_argument("chiral quad must be (i-1, i, i+1, i+2) of one chain");
+        if (!std::isnan(r.chir_f[i2[k]])) throw std::invalid_argument("duplicate chiral quad");
+        if (!std::isfinite(f[k]) || !std::isfinite(c[k])) throw std::invalid_argument("non-finite chiral parameter");
+        r.chir_f[i2[k]] = f[k];
+        r.chir_n[i2[k]] = c[k];
+    }
+}
+void Engine::set_ssbonds(int rep, int n, const int32_t *i1, const int32_t *i2) {
+    check_rep(reps, rep);
+    if (reps[rep].placed) throw std::invalid_argument("topology is fixed once the replica is on the device");
+    RepHost &r = reps[rep];
+    std::vector<std::pair<int, int>> v;
+    for (int k = 0; k < n; ++k) {
+        int a = std::min(i1[k], i2[k]), b = std::max(i1[k], i2[k]);
+        if (a < 0 || b >= r.n || a == b) throw std::invalid_argument("disulfide index out of range");
+        v.emplace_back(a, b);
+    }
+    std::sort(v.begin(), v.end());
+    if (std::adjacent_find(v.begin(), v.end()) != v.end()) throw std::invalid_argument("duplicate disulfide");
+    r.ss_i1.clear(); r.ss_i2.clear();
+    for (auto &[a, b] : v) { r.ss_i1.push_back(a); r.ss_i2.push_back(b); }
+}
+
 void Engine::derive_rep(int ri, RepDev &rd) {
     const RepHost &r = reps[ri];
     const xmd_params &p = params;
@@ -1579,6 +1689,7 @@ void Engine::derive_rep(int ri, RepDev &rd) {
     // max_cutoff: main.cpp:500, 545-551, 628-630, 642-644, 742-746
     double mc = 0.0;
     if (p.on[XMD_TERM_PAULI]) mc = std::max(mc, p.pauli_r_excl);
+    if (p.on[XMD_TERM_NAT_SS]) mc = std::max(mc, 2.0 * p.nat_ss_dist);   // harmonic::cutoff, main.cpp:596-597
     if (p.on[XMD_TERM_GO]) for (double x : r.nat_d) mc = std::max(mc, 2.0 * x);
     if (p.on[XMD_TERM_CONST_ES]) mc = std::max(mc, 2.0 * p.const_es_screen_dist);
     if (p.on[XMD_TERM_REL_ES]) mc = std::max(mc, 2.0 * p.rel_es_screen_dist);
@@ -1598,6 +1709,7 @@ void Engine::derive_rep(int ri, RepDev &rd) {
     rd.s_pa = sq_below(inv_above(rd.pauli_min_inv));
     rd.s_es = sq_below(inv_above(rd.es_min_inv));
     rd.s_qa = sq_below(inv_above(rd.qa_min_inv));
+    rd.s_ss = sq_below(2.0 * p.nat_ss_dist + rd.pad);   // update_nat_ssbonds, native_ss.cpp:15
     rd.noise_sd = std::sqrt(2.0 * 1.0 * r.temperature) * std::sqrt(p.gamma_factor) * 1.0;
     rd.begin = r.begin;
     rd.n = r.n;
@@ -1617,6 +1729,7 @@ void Engine::finalize() {
         for (auto &r : reps) {
             cap.beads += r.n;
             cap.nat += 2 * (int)r.nat_i1.size();
+            cap.ss += 2 * (int)r.ss_i1.size();
             const bool tile = params.nl_build == XMD_NL_BUILD_TILE ||
                               (params.nl_build == XMD_NL_BUILD_AUTO && r.n <= TILE_MAX);
             if (tile) cap.chunks += (r.n + TL_CH - 1) / TL_CH;
@@ -1668,6 +1781,18 @@ void Engine::allocate() {
     d.nat_T = (double *)dalloc(sizeof(double) * NN);
     d.nat_S = (double *)dalloc(sizeof(double) * NN);
     d.nat_on = (uint8_t *)dalloc(NN);
+    {
+        const size_t SS = (size_t)std::max(1, cap.ss);
+        d.ss_start = (int32_t *)dalloc(sizeof(int32_t) * N);
+        d.ss_end = (int32_t *)dalloc(sizeof(int32_t) * N);
+        CK(cudaMemsetAsync(d.ss_start, 0, sizeof(int32_t) * N, stream));
+        CK(cudaMemsetAsync(d.ss_end, 0, sizeof(int32_t) * N, stream));
+        d.ss_j = (int32_t *)dalloc(sizeof(int32_t) * SS);
+        d.ss_on = (uint8_t *)dalloc(SS);
+        CK(cudaMemsetAsync(d.ss_on, 0, SS, stream));
+        d.chir = (double2 *)dalloc(sizeof(double2) * N);
+        d.chir_f32 = (float2 *)dalloc(sizeof(float2) * N);
+    }
     d.nl_row = (int32_t *)dalloc(sizeof(int32_t) * (size_t)nl_cap * N);
     d.nl_cnt = (int32_t *)dalloc(sizeof(int32_t) * N);
     d.cell_cnt = (int32_t *)dalloc(sizeof(int32_t) * cells);
@@ -1698,6 +1823,7 @@ void Engine::allocate() {
     owner_h.assign(N, -1);
     a_beads.init(N);
     a_nat.init(cap.nat);
+    a_ss.init(cap.ss);
     a_cells.init(cap.cells);
     a_chunks.init(cap.chunks);
     a_fp.init(cap.fp);
@@ -1751,9 +1877,13 @@ void Engine::allocate() {
     tp.lj_bb_r_min = p.lj_bb_r_min; tp.lj_bb_depth = p.lj_bb_depth;
     tp.lj_bs_r_min = p.lj_bs_r_min; tp.lj_bs_depth = p.lj_bs_depth;
     tp.ss_sinking = p.ss_sinking;
+    tp.chir_e_chi = p.chir_e_chi;
+    tp.nat_ss_H1 = p.nat_ss_H1;
+    tp.nat_ss_dist = p.nat_ss_dist;
     tp.f = TermP::F32{(float)tp.tether_H1, (float)tp.tether_H2, (float)tp.nat_ang_k, (float)tp.cnd_CDA,
                       (float)tp.cnd_CDB, (float)tp.snd_CDH, (float)tp.go_depth, (float)tp.pauli_r_excl,
-                      (float)tp.pauli_depth, (float)tp.es_Vf, (float)tp.es_sdi};
+                      (float)tp.pauli_depth, (float)tp.es_Vf, (float)tp.es_sdi, (float)tp.chir_e_chi,
+                      (float)tp.nat_ss_H1, (float)tp.nat_ss_dist};
     if (p.on[XMD_TERM_QA]) {
         // quasi-adiabatic state (tables of main.cpp:681-700, lj_variants.cpp:59-62)
         d.qa_on = 1;
@@ -1869,14 +1999,16 @@ void Engine::place(int k) {
         throw std::invalid_argument("engine: nl build 'tile' takes replicas of at most " +
                                     std::to_string(TILE_MAX) + " beads");
     const int nnat = 2 * (int)r.nat_i1.size();
+    const int nss = 2 * (int)r.ss_i1.size();
     const int nchunk = tile ? (n + TL_CH - 1) / TL_CH : 0;
     const int ncell = tile ? 0 : std::max(64, 2 * n);
     const bool qa = p.on[XMD_TERM_QA] != 0;
     const int nfp = qa ? n * QA_FP_PER_BEAD + 256 : 0, nct = qa ? n * QA_CT_PER_BEAD + 256 : 0;
     // device ranges (all or nothing)
     int b = a_beads.alloc(n), no = a_nat.alloc(nnat), co = a_cells.alloc(ncell), ho = a_chunks.alloc(nchunk);
-    int fo = a_fp.alloc(nfp), to = a_ct.alloc(nct);
-    if (b < 0 || no < 0 || co < 0 || ho < 0 || fo < 0 || to < 0) {
+    int fo = a_fp.alloc(nfp), to = a_ct.alloc(nct), so = a_ss.alloc(nss);
+    if (b < 0 || no < 0 || co < 0 || ho < 0 || fo < 0 || to < 0 || so < 0) {
+        if (so >= 0) a_ss.release(so, nss);
         if (b >= 0) a_beads.release(b, n);
         if (no >= 0) a_nat.release(no, nnat);
         if (co >= 0) a_cells.release(co, ncell);
@@ -1887,6 +2019,7 @@ void Engine::place(int k) {
     }
     r.begin = b;
     r.nat_off = no; r.nat_len = nnat;
+    r.ss_off = so; r.ss_len = nss;
     r.cell_off = co; r.cell_len = ncell;
     r.chunk_off = ho; r.chunk_len = nchunk;
     r.fp_off = fo; r.fp_len = nfp;
@@ -1901,6 +2034,7 @@ void Engine::place(int k) {
         if (!std::isnan(r.teth_r0[i])) { f |= BF_TETH; tr[i] = r.teth_r0[i]; }
         if (!std::isnan(r.ang_t0[i])) { f |= BF_ANG; ar[i] = r.ang_t0[i]; }
         if (!std::isnan(r.dih_p0[i])) { f |= BF_DIH; dr[i] = r.dih_p0[i]; }
+        if (!std::isnan(r.chir_f[i])) f |= BF_CHIR;
         if (i > 0 && consecutive(r, i - 1, i)) f |= BF_PREV;
         if (i + 1 < r.n && consecutive(r, i, i + 1)) f |= BF_NEXT;
         bfl[i] = f;
@@ -1931,6 +2065,34 @@ void Engine::place(int k) {
     up(d.teth_r0 + b, tr.data(), sizeof(double) * n);
     up(d.ang_t0 + b, ar.data(), sizeof(double) * n);
     up(d.dih_p0 + b, dr.data(), sizeof(double) * n);
+    {
+        std::vector<double2> ch(n);
+        std::vector<float2> chf(n);
+        for (int i = 0; i < n; ++i) {
+            const bool on = !std::isnan(r.chir_f[i]);
+            ch[i] = make_double2(on ? r.chir_f[i] : 0.0, on ? r.chir_n[i] : 0.0);
+            chf[i] = make_float2((float)ch[i].x, (float)ch[i].y);
+        }
+        up(d.chir + b, ch.data(), sizeof(double2) * n);
+        up(d.chir_f32 + b, chf.data(), sizeof(float2) * n);
+        // disulfide partners per bead, both directions, ordered by partner
+        std::vector<std::vector<int>> sp(n);
+        for (size_t q = 0; q < r.ss_i1.size(); ++q) {
+            sp[r.ss_i1[q]].push_back(b + r.ss_i2[q]);
+            sp[r.ss_i2[q]].push_back(b + r.ss_i1[q]);
+        }
+        std::vector<int32_t> sst(n), sse(n), sj;
+        for (int i = 0; i < n; ++i) {
+            std::sort(sp[i].begin(), sp[i].end());
+            sst[i] = so + (int)sj.size();
+            for (int x : sp[i]) sj.push_back(x);
+            sse[i] = so + (int)sj.size();
+        }
+        up(d.ss_start + b, sst.data(), sizeof(int32_t) * n);
+        up(d.ss_end + b, sse.data(), sizeof(int32_t) * n);
+        up(d.ss_j + so, sj.data(), sizeof(int32_t) * sj.size());
+        if (nss) CK(cudaMemsetAsync(d.ss_on + so, 0, nss, stream));
+    }
     std::vector<float4> bf(n);
     for (int i = 0; i < n; ++i) bf[i] = make_float4((float)tr[i], (float)ar[i], (float)dr[i], 0.0f);
     up(d.bond_f + b, bf.data(), sizeof(float4) * n);

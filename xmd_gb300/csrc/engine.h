@@ -17,6 +17,7 @@ enum : uint32_t {
     BF_TETH = 1u,  // bond (i, i+1)
     BF_ANG = 2u,   // angle (i-1, i, i+1)
     BF_DIH = 4u,   // dihedral (i-1, i, i+1, i+2)
+    BF_CHIR = 32u, // chiral quad (i-1, i, i+1, i+2)
     BF_PREV = 8u,  // i-1 is the previous bead of the same chain
     BF_NEXT = 16u  // i+1 is the next bead of the same chain
 };
@@ -29,6 +30,7 @@ struct RepDev {
     // squared-distance forms of the list tests: s < s_req <=> sqrt(s) < req_r,
     // s < s_pa <=> 1/sqrt(s) > pauli_min_inv, etc. (correctly rounded FP64)
     double s_req, s_pa, s_es, s_qa;
+    double s_ss;             // disulfide list: s < s_ss <=> r < 2 nat_r + pad (native_ss.cpp:15)
     double t;
     int begin, n;
     int cell_off, cell_budget;
@@ -101,6 +103,10 @@ struct Dev {
     int32_t *chain, *seq;
     uint8_t *atype;
     double *teth_r0, *ang_t0, *dih_p0;
+    double2 *chir;          // (nat_factor, nat_chir) per centre i2 of a chiral quad
+    float2 *chir_f32;       // the same in FP32 (mixed path)
+    int32_t *ss_start, *ss_end, *ss_j;   // native disulfide partners per bead (CSR, both directions)
+    uint8_t *ss_on;         // in the list of the last rebuild (update_nat_ssbonds, native_ss.cpp:8-19)
     float4 *bond_f;         // (r0, theta0, phi0) in FP32 for the mixed path
     int32_t *nat_start, *nat_end, *nat_j;   // natives of bead i: [nat_start[i], nat_end[i])
     double *nat_d;
@@ -141,12 +147,15 @@ struct RepHost {
     double temperature = 0;
     uint64_t seed = 0;
     std::vector<double> teth_r0, ang_t0, dih_p0;   // per centre, NaN = absent
+    std::vector<double> chir_f, chir_n;            // chirality per centre (i2), NaN = absent
+    std::vector<int32_t> ss_i1, ss_i2;             // native disulfides
     std::vector<int32_t> nat_i1, nat_i2;
     std::vector<double> nat_d;
     std::vector<double> r, v;                      // initial state
     bool have_state = false;
     int begin = 0;
     int nat_off = 0, nat_len = 0;       // native CSR entries
+    int ss_off = 0, ss_len = 0;         // disulfide CSR entries
     int cell_off = 0, cell_len = 0;     // cell buckets (cell-grid build)
     int chunk_off = 0, chunk_len = 0;   // tile-build chunks
     int fp_off = 0, fp_len = 0, ct_off = 0, ct_len = 0;   // quasi-adiabatic slots
@@ -241,6 +250,9 @@ public:
     void set_dihedrals(int rep, int n, const int32_t *i1, const int32_t *i2, const int32_t *i3,
                        const int32_t *i4, const double *ph);
     void set_native(int rep, int n, const int32_t *i1, const int32_t *i2, const double *d);
+    void set_chirals(int rep, int n, const int32_t *i1, const int32_t *i2, const int32_t *i3, const int32_t *i4,
+                     const double *factor, const double *chir);
+    void set_ssbonds(int rep, int n, const int32_t *i1, const int32_t *i2);
     void set_state(int rep, const double *r, const double *v);
     void set_history(int rep, const double *y, double t, uint64_t rng);
     void get_state(int rep, double *r, double *v, double *t);
@@ -298,11 +310,11 @@ private:
     void drop_graphs();
 
     struct Caps {
-        int beads = 0, reps = 0, nat = 0, cells = 0, chunks = 0, fp = 0, ct = 0, qab = 0;
+        int beads = 0, reps = 0, nat = 0, cells = 0, chunks = 0, fp = 0, ct = 0, qab = 0, ss = 0;
     } cap;
     bool dynamic = false;
     size_t bytes = 0;                          // device memory held
-    RangeAlloc a_beads, a_nat, a_cells, a_chunks, a_fp, a_ct;
+    RangeAlloc a_beads, a_nat, a_cells, a_chunks, a_fp, a_ct, a_ss;
     int qa_bchunk_next = 0;   // next free chunk of the QA re-listing (static contexts)
     std::vector<int32_t> owner_h;              // bead slot -> replica (or -1)
     void allocate();

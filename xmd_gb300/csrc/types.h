@@ -25,11 +25,14 @@ struct TermP {
     double qa_cycle, qa_cycle_inv, qa_factor;
     double lj_bb_r_min, lj_bb_depth, lj_bs_r_min, lj_bs_depth;
     int ss_sinking;
+    double chir_e_chi;                       // chirality (chiral.h)
+    double nat_ss_H1, nat_ss_dist;           // native ssbonds (native_ss.h: H1, nat_r)
     // FP32 copies of the constants the mixed path's FP32 terms use (no
     // FP64-to-FP32 conversion per interaction)
     struct F32 {
         float tether_H1, tether_H2, nat_ang_k, cnd_CDA, cnd_CDB, snd_CDH, go_depth;
         float pauli_r_excl, pauli_depth, es_Vf, es_sdi;
+        float chir_e_chi, nat_ss_H1, nat_ss_dist;
     } f;
 };
 

@@ -69,6 +69,13 @@ class Engine:
                                              dptr(dp)))
         n1, n2, nd = (np.ascontiguousarray(x) for x in s.natives)
         check(self.lib.xmd_gpu_set_native_contacts(self.h, r, len(n1), iptr(n1), iptr(n2), dptr(nd)))
+        if getattr(s, "chirals", None) is not None:
+            q = [np.ascontiguousarray(x, dtype=np.int32) for x in s.chirals[:4]]
+            qf, qc = (np.ascontiguousarray(x, dtype=np.float64) for x in s.chirals[4:])
+            check(self.lib.xmd_gpu_set_chirals(self.h, r, len(q[0]), *(iptr(x) for x in q), dptr(qf), dptr(qc)))
+        if getattr(s, "ssbonds", None) is not None:
+            s1, s2 = (np.ascontiguousarray(x, dtype=np.int32) for x in s.ssbonds)
+            check(self.lib.xmd_gpu_set_ssbonds(self.h, r, len(s1), iptr(s1), iptr(s2)))
         rr = np.ascontiguousarray(s.r, dtype=np.float64).reshape(-1)
         check(self.lib.xmd_gpu_set_state(self.h, r, dptr(rr), None))
         self.sizes[r] = s.n

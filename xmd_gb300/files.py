@@ -33,7 +33,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from .abi import AA
-from .synth import ANGSTROM, System, bonded_natives
+from .synth import ANGSTROM, System, bonded_natives, chirals_of
 
 # CA radii of the residue types (defaults.yml amino-acid data, `radius`), in A
 # (MET's entry, defaults.yml:183, lacks its unit; it is read as 4.5 A)
@@ -211,15 +211,18 @@ def to_system(pdb: Pdb, temperature: float = 0.35, seed: int = 1, contacts: str 
     nat = sorted(pairs.items())
     as32 = lambda x: np.asarray(x, dtype=np.int32)
     asf = lambda x: np.asarray(x, dtype=np.float64)
+    dihs = (as32(dih[0]), as32(dih[1]), as32(dih[2]), as32(dih[3]), asf(dih[4]))
     return System(
         n=n, chain=chain, seq=seq, atype=np.asarray(atype, dtype=np.uint8), cell=np.asarray(pdb.cell, dtype=np.float64),
         r=pos.copy(),
         tethers=(as32(t1), as32(t2), asf(td)),
         angles=(as32(ang[0]), as32(ang[1]), as32(ang[2]), asf(ang[3])),
-        dihedrals=(as32(dih[0]), as32(dih[1]), as32(dih[2]), as32(dih[3]), asf(dih[4])),
+        dihedrals=dihs,
         natives=(as32([p[0][0] for p in nat]), as32([p[0][1] for p in nat]), asf([p[1] for p in nat])),
         temperature=float(temperature), seed=int(seed),
         meta={"ssbonds": ss, "chains": [int((chain == c).sum()) for c in np.unique(chain)]},
+        chirals=chirals_of(dihs, pos),
+        ssbonds=(as32([x[0] for x in ss]), as32([x[1] for x in ss])),
     )
 
 

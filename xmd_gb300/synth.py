@@ -44,6 +44,8 @@ class System:
     temperature: float = 0.0
     seed: int = 0
     meta: dict = field(default_factory=dict)
+    chirals: tuple | None = None  # (i1, i2, i3, i4, nat_factor, nat_chir)
+    ssbonds: tuple | None = None  # (i1, i2) native disulfide bonds
 
 
 def _unit(v):
@@ -150,6 +152,18 @@ def bonded_natives(pos):
     return th, ph
 
 
+def chirals_of(dihedrals, pos):
+    """Chiral quads over the dihedral quadruplets (i1..i4) with native
+    positions pos[n, 3]: nat_factor = |r23|^-3 and nat_chir = r12 . (r23 x r34)
+    * nat_factor, as main.cpp builds them from the model's dihedrals
+    (src/freeform/main.cpp:376-393)."""
+    i1, i2, i3, i4 = (np.asarray(x, dtype=np.int32) for x in dihedrals[:4])
+    r12, r23, r34 = pos[i2] - pos[i1], pos[i3] - pos[i2], pos[i4] - pos[i3]
+    fac = np.linalg.norm(r23, axis=1) ** -3 if len(i1) else np.zeros(0)
+    chi = (r12 * np.cross(r23, r34)).sum(axis=1) * fac if len(i1) else np.zeros(0)
+    return i1, i2, i3, i4, np.asarray(fac, dtype=np.float64), np.asarray(chi, dtype=np.float64)
+
+
 def native_map(pos, cutoff=7.5 * ANGSTROM, min_sep=3):
     n = len(pos)
     d = np.linalg.norm(pos[:, None, :] - pos[None, :, :], axis=2)
@@ -195,6 +209,7 @@ def make_system(chain_lengths, seed, box=None, density=1e-3, types="charged10",
     ang = ([], [], [], [])
     dih = ([], [], [], [], [])
     nat = ([], [], [])
+    natpos = np.zeros((n, 3))
     off = 0
     for c, L in enumerate(lens):
         start_pt = rng.uniform(-a / 2.0, a / 2.0, size=3)
@@ -206,6 +221,7 @@ def make_system(chain_lengths, seed, box=None, density=1e-3, types="charged10",
             tet_d += [bond] * (L - 1)
         if native and L >= 3:
             npos = compact_walk(rng, L, bond)
+            natpos[off:off + L] = npos
             if start == "native":
                 r[off:off + L] = npos - npos.mean(axis=0) + start_pt
             th, ph = bonded_natives(npos)
@@ -220,14 +236,15 @@ def make_system(chain_lengths, seed, box=None, density=1e-3, types="charged10",
     cell = np.array([box, box, box], dtype=np.float64) if box is not None else np.zeros(3)
     as32 = lambda x: np.asarray(x, dtype=np.int32)
     asf = lambda x: np.asarray(x, dtype=np.float64)
+    dihs = (as32(dih[0]), as32(dih[1]), as32(dih[2]), as32(dih[3]), asf(dih[4]))
     return System(
         n=n, chain=chain, seq=seq, atype=atype, cell=cell, r=r,
         tethers=(as32(tet_i1), as32(tet_i2), asf(tet_d)),
         angles=(as32(ang[0]), as32(ang[1]), as32(ang[2]), asf(ang[3])),
-        dihedrals=(as32(dih[0]), as32(dih[1]), as32(dih[2]), as32(dih[3]), asf(dih[4])),
+        dihedrals=dihs,
         natives=(as32(nat[0]), as32(nat[1]), asf(nat[2])),
         temperature=temperature, seed=int(rng_seed if rng_seed is not None else seed * 7919 + 17),
-        meta={"chains": lens},
+        meta={"chains": lens}, chirals=chirals_of(dihs, natpos),
     )
 
 
@@ -454,13 +471,15 @@ def make_request_system(chain_lengths, seed, temperature, rng_seed, density=1e-3
         off += L
     cat32 = lambda xs: np.concatenate(xs).astype(np.int32) if xs else np.zeros(0, np.int32)
     catf = lambda xs: np.concatenate(xs).astype(np.float64) if xs else np.zeros(0)
+    dihs = (cat32(dih[0]), cat32(dih[1]), cat32(dih[2]), cat32(dih[3]), catf(dih[4]))
     return System(
         n=n, chain=chain, seq=seq, atype=atype, cell=np.zeros(3), r=r,
         tethers=(cat32(tet[0]), cat32(tet[1]), catf(tet[2])),
         angles=(cat32(ang[0]), cat32(ang[1]), cat32(ang[2]), catf(ang[3])),
-        dihedrals=(cat32(dih[0]), cat32(dih[1]), cat32(dih[2]), cat32(dih[3]), catf(dih[4])),
+        dihedrals=dihs,
         natives=(cat32(nat[0]), cat32(nat[1]), catf(nat[2])),
         temperature=temperature, seed=int(rng_seed), meta={"chains": lens},
+        chirals=chirals_of(dihs, np.concatenate(natives)),
     )
 
 
