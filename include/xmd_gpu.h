@@ -60,7 +60,9 @@ enum {
     XMD_TERM_QA = 8,        /* qa::process_contacts src/forces/qa/process_contacts.cpp:13-57  */
     XMD_TERM_CHIR = 9,      /* eval_chiral_forces src/forces/chiral.cpp:15-37                 */
     XMD_TERM_NAT_SS = 10,   /* eval_nat_ssbond_forces src/forces/native_ss.cpp:27-40          */
-    XMD_NUM_TERMS = 11
+    XMD_TERM_HEUR_ANG = 11, /* eval_heurestic_angle_forces src/forces/angle/heurestic.cpp:29-59 */
+    XMD_TERM_HEUR_DIH = 12, /* eval_heurestic_dihedral_forces src/forces/dihedral/heurestic.cpp:29-70 */
+    XMD_NUM_TERMS = 13
 };
 
 enum { XMD_PREC_FP64 = 0, XMD_PREC_MIXED = 1 };
@@ -124,6 +126,14 @@ typedef struct xmd_params {
     double chir_e_chi;
     /* native ssbonds (native_ss.h: H1, nat_r = `equilibrium dist`) */
     double nat_ss_H1, nat_ss_dist;
+    /* heuristic angles: V(theta) = sum_d a_d theta^d, d = 0..6, per pair
+       type 3 t1 + t2 of the angle's first two residues (G = 0, P = 1, other
+       = 2); `heurestic angles: coefficients`, angle/heurestic.h:40-41 */
+    double heur_ang_coeffs[9][7];
+    /* heuristic dihedrals: V(phi) = c0 + c1 sin + c2 cos + c3 sin^2 + c4 cos^2
+       + c5 sin cos, per pair type of the dihedral's middle residues;
+       `heurestic dihedrals: coefficients`, dihedral/heurestic.h:37-38 */
+    double heur_dih_coeffs[9][6];
 } xmd_params;
 
 enum { XMD_NL_BUILD_AUTO = 0, XMD_NL_BUILD_CELL = 1, XMD_NL_BUILD_TILE = 2 };
@@ -192,6 +202,15 @@ int xmd_gpu_set_dihedrals(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_
 int xmd_gpu_set_chirals(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1,
                         const int32_t *i2, const int32_t *i3, const int32_t *i4,
                         const double *nat_factor, const double *nat_chir);
+/* Heuristic angles heur_ang{i1, i2, i3, type} (angle/heurestic.h:27-31),
+ * (k, k+1, k+2) of one chain; the type follows from the residues i1 and i2.
+ * A centre has either a native or a heuristic angle. */
+int xmd_gpu_set_heuristic_angles(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1,
+                                 const int32_t *i2, const int32_t *i3);
+/* Heuristic dihedrals heur_dih{i1..i4, type} (dihedral/heurestic.h:27-31),
+ * (k, ..., k+3) of one chain; the type follows from the residues i2 and i3. */
+int xmd_gpu_set_heuristic_dihedrals(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1,
+                                    const int32_t *i2, const int32_t *i3, const int32_t *i4);
 /* Native disulfide bonds (model contacts of type NAT_SS, main.cpp:554-598). */
 int xmd_gpu_set_ssbonds(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1, const int32_t *i2);
 /* All native contacts (nat_cont{i1,i2,nat_dist}, main.cpp:505-552). */

@@ -39,6 +39,8 @@ def _load(path: Path, pfx: str, params_type):
         "set_native_contacts": (C.c_int, [C.c_void_p, C.c_int32, _pi, _pi, _pd]),
         "set_chirals": (C.c_int, [C.c_void_p, C.c_int32, _pi, _pi, _pi, _pi, _pd, _pd]),
         "set_ssbonds": (C.c_int, [C.c_void_p, C.c_int32, _pi, _pi]),
+        "set_heuristic_angles": (C.c_int, [C.c_void_p, C.c_int32, _pi, _pi, _pi]),
+        "set_heuristic_dihedrals": (C.c_int, [C.c_void_p, C.c_int32, _pi, _pi, _pi, _pi]),
         "set_state": (C.c_int, [C.c_void_p, _pd, _pd]),
         "set_history": (C.c_int, [C.c_void_p, _pd, C.c_double, C.c_uint64]),
         "get_state": (C.c_int, [C.c_void_p, _pd, _pd, _pd]),
@@ -107,6 +109,12 @@ class Oracle:
         b = getattr(s, "ssbonds", None)
         if b is not None:
             self.fn("set_ssbonds")(self.h, len(b[0]), ip(b[0]), ip(b[1]))
+        h = getattr(s, "heur_angles", None)
+        if h is not None:
+            self.fn("set_heuristic_angles")(self.h, len(h[0]), ip(h[0]), ip(h[1]), ip(h[2]))
+        h = getattr(s, "heur_dihedrals", None)
+        if h is not None:
+            self.fn("set_heuristic_dihedrals")(self.h, len(h[0]), ip(h[0]), ip(h[1]), ip(h[2]), ip(h[3]))
         self.fn("set_state")(self.h, dp(np.asarray(s.r).reshape(-1)), None)
 
     def fn(self, name):
@@ -190,3 +198,21 @@ def rng_stream(kind: str, state: int, n: int):
     fn = getattr(lib, ("xo_" if kind == "port" else "xr_") + "rng_next")
     st = C.c_uint64(state)
     return np.array([fn(C.byref(st)) for _ in range(n)], dtype=np.uint64), st.value
+
+
+def ref_morph_into_saw(lens, bond, density, infer_box, seed):
+    """model::morph_into_saw of the reference itself (its model.cpp compiled
+    into the reference driver): (r[n, 3], generator state after, cell[3])."""
+    from xmd_gb300.abi import Params
+    lib = _load(REF_LIB, "xr_", Params)
+    fn = lib.xr_morph_into_saw
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_int32, _pi, C.c_double, C.c_double, C.c_int32, C.c_uint64, _pd, _pu64, _pd]
+    L = np.ascontiguousarray(lens, dtype=np.int32)
+    n = int(L.sum())
+    r = np.zeros(3 * max(n, 1))
+    cell = np.zeros(3)
+    st = np.zeros(1, dtype=np.uint64)
+    fn(len(L), L.ctypes.data_as(_pi), float(bond if bond is not None else 0.0), float(density), int(infer_box),
+       int(seed) & (2**64 - 1), r.ctypes.data_as(_pd), st.ctypes.data_as(_pu64), cell.ctypes.data_as(_pd))
+    return r[:3 * n].reshape(n, 3), int(st[0]), cell

@@ -30,6 +30,9 @@
 #include <xmd/forces/go.h>
 #include <xmd/forces/chiral.h>
 #include <xmd/forces/native_ss.h>
+#include <xmd/model/model.h>
+#include <xmd/forces/angle/heurestic.h>
+#include <xmd/forces/dihedral/heurestic.h>
 #include <xmd/forces/pauli.h>
 #include <xmd/forces/es/const.h>
 #include <xmd/forces/es/relative.h>
@@ -79,6 +82,8 @@ struct xr_sys {
     ::vector<nat_cont> all_nat_cont, go_contacts;
     std::vector<std::pair<int, int>> nat_sorted;
     ::vector<chiral_quad> quads;
+    ::vector<heur_ang> heur_angles;
+    ::vector<heur_dih> heur_dihedrals;
     ::vector<nat_ss> all_ss, cur_ss;
     std::vector<std::pair<int, int>> ss_sorted;
 
@@ -343,6 +348,26 @@ void term_forces(xr_sys *s, ::vector<vec3r> &F, real *V) {
         e.r = s->r.data(); e.F = F.data(); e.quads = s->quads.view(); e.V = &V[XMD_TERM_CHIR];
         e();
     }
+    if (p.on[XMD_TERM_HEUR_ANG]) {
+        // main.cpp builds no heuristic term; the kernel gets all 7 table
+        // coefficients (freeform/params.cpp:77-80 reads a0..a5 only) [D17]
+        eval_heurestic_angle_forces e;
+        for (int d = 0; d <= eval_heurestic_angle_forces::POLY_DEG; ++d)
+            for (int t = 0; t < eval_heurestic_angle_forces::NUM_TYPES; ++t)
+                e.poly_coeffs[d][t] = (real)p.heur_ang_coeffs[t][d];
+        e.r = s->r.data(); e.F = F.data(); e.angles = s->heur_angles.view(); e.V = &V[XMD_TERM_HEUR_ANG];
+        e();
+    }
+    if (p.on[XMD_TERM_HEUR_DIH]) {
+        // the shipped kernel as it is: phi = cos(cos_phi) and +2 c4 sin cos
+        // (dihedral/heurestic.cpp:43, 52-54); the restatement departs [D18]
+        eval_heurestic_dihedral_forces e;
+        for (int k = 0; k < eval_heurestic_dihedral_forces::NUM_TERMS; ++k)
+            for (int t = 0; t < eval_heurestic_dihedral_forces::NUM_TYPES; ++t)
+                e.coeffs[k][t] = (real)p.heur_dih_coeffs[t][k];
+        e.r = s->r.data(); e.F = F.data(); e.dihedrals = s->heur_dihedrals.view(); e.V = &V[XMD_TERM_HEUR_DIH];
+        e();
+    }
     if (p.on[XMD_TERM_NAT_SS]) {
         eval_nat_ssbond_forces e;
         e.H1 = p.nat_ss_H1; e.nat_r = p.nat_ss_dist;
@@ -467,6 +492,57 @@ int xr_set_chirals(void *h, int32_t n, const int32_t *i1, const int32_t *i2, con
     auto *s = (xr_sys *)h;
     s->quads.clear();
     for (int k = 0; k < n; ++k) s->quads.emplace_back(i1[k], i2[k], i3[k], i4[k], (real)nat_chir[k], (real)nat_factor[k]);
+    return 0;
+}
+// heuristic angle and dihedral types from the residues (heur_ang_type(a1, a2)
+// of the angle's i1, i2; heur_dih_type(a2, a3) of the dihedral's i2, i3)
+int xr_set_heuristic_angles(void *h, int32_t n, const int32_t *i1, const int32_t *i2, const int32_t *i3) {
+    auto *s = (xr_sys *)h;
+    s->heur_angles.clear();
+    for (int k = 0; k < n; ++k)
+        s->heur_angles.emplace_back(i1[k], i2[k], i3[k], heur_ang_type(s->atype[i1[k]], s->atype[i2[k]]));
+    return 0;
+}
+int xr_set_heuristic_dihedrals(void *h, int32_t n, const int32_t *i1, const int32_t *i2, const int32_t *i3,
+                               const int32_t *i4) {
+    auto *s = (xr_sys *)h;
+    s->heur_dihedrals.clear();
+    for (int k = 0; k < n; ++k)
+        s->heur_dihedrals.emplace_back(i1[k], i2[k], i3[k], i4[k], heur_dih_type(s->atype[i2[k]], s->atype[i3[k]]));
+    return 0;
+}
+// model::morph_into_saw (model.cpp:101-173) on chains of the given lengths
+// (positions zero, as seq_file leaves them), with rand_gen(seed); writes the
+// positions in residue order and the generator's state afterwards.
+// bond <= 0: the optional bond length is absent.
+int xr_morph_into_saw(int32_t nchains, const int32_t *lens, double bond, double density, int32_t infer_box,
+                      uint64_t seed, double *r_out, uint64_t *state_out, double *cell_out) {
+    xmd::model m;
+    for (int c = 0; c < nchains; ++c) {
+        auto &ch = m.chains.emplace_back(std::make_unique<xmd::model::chain>());
+        ch->residues.resize(lens[c]);
+        for (int k = 0; k < lens[c]; ++k) {
+            auto &res = m.residues.emplace_back(std::make_unique<xmd::model::residue>());
+            res->seq_idx = k;
+            res->parent = &*ch;
+            res->type = amino_acid(GLY);
+            res->pos = {0.0, 0.0, 0.0};
+            ch->residues[k] = &*res;
+        }
+    }
+    xmd::rand_gen gen(seed);
+    std::optional<true_real> bl;
+    if (bond > 0) bl = bond;
+    m.morph_into_saw(gen, bl, density, infer_box != 0);
+    size_t q = 0;
+    for (auto const &res : m.residues) {
+        r_out[3 * q] = res->pos.x(); r_out[3 * q + 1] = res->pos.y(); r_out[3 * q + 2] = res->pos.z();
+        ++q;
+    }
+    *state_out = gen.state;
+    if (cell_out) {
+        cell_out[0] = m.model_box.cell.x(); cell_out[1] = m.model_box.cell.y(); cell_out[2] = m.model_box.cell.z();
+    }
     return 0;
 }
 int xr_set_ssbonds(void *h, int32_t n, const int32_t *i1, const int32_t *i2) {

@@ -123,6 +123,8 @@ struct xo_sys {
     int32_t n_chir; int32_t *chir_i; double *chir_f, *chir_n;   /* chiral_quad (chiral.h) */
     int32_t n_ss_all; pair_i *ss_all;                           /* native ssbonds (nat_ss) */
     pair_i *ss; int32_t n_ss;                                   /* update_nat_ssbonds' list */
+    int32_t n_hang; int32_t *hang_i; int8_t *hang_t;            /* heur_ang (angle/heurestic.h) */
+    int32_t n_hdih; int32_t *hdih_i; int8_t *hdih_t;            /* heur_dih (dihedral/heurestic.h) */
     /* state */
     double *r, *v, *y[6], *F;
     double t, true_t;
@@ -262,6 +264,7 @@ void xo_destroy(xo_sys *s) {
     free(s->teth_i); free(s->teth_d); free(s->ang_i); free(s->ang_t);
     free(s->dih_i); free(s->dih_p); free(s->nat);
     free(s->chir_i); free(s->chir_f); free(s->chir_n); free(s->ss_all); free(s->ss);
+    free(s->hang_i); free(s->hang_t); free(s->hdih_i); free(s->hdih_t);
     free(s->r); free(s->v); free(s->F);
     for (int k = 0; k < 6; ++k) free(s->y[k]);
     free(s->orig_r); free(s->nl); free(s->go); free(s->pauli); free(s->es);
@@ -344,6 +347,38 @@ int xo_set_chirals(xo_sys *s, int32_t n, const int32_t *i1, const int32_t *i2, c
         s->chir_i[4 * k + 2] = i3[k]; s->chir_i[4 * k + 3] = i4[k];
         s->chir_f[k] = nat_factor[k];
         s->chir_n[k] = nat_chir[k];
+    }
+    return 0;
+}
+/* heur_ang_type / heur_dih_type: GLY = 0, PRO = 1, others = 2 and
+   type = 3 t1 + t2 (angle/heurestic.cpp:9-15, dihedral/heurestic.cpp:8-14) */
+static int8_t heur_type(uint8_t a, uint8_t b) {
+    int ca = a == 7 ? 0 : (a == 14 ? 1 : 2), cb = b == 7 ? 0 : (b == 14 ? 1 : 2);
+    return (int8_t)(3 * ca + cb);
+}
+/* heuristic angles: type of (i1, i2) */
+int xo_set_heuristic_angles(xo_sys *s, int32_t n, const int32_t *i1, const int32_t *i2, const int32_t *i3) {
+    free(s->hang_i); free(s->hang_t);
+    s->n_hang = n;
+    s->hang_i = (int32_t *)malloc(sizeof(int32_t) * 3 * (n ? n : 1));
+    s->hang_t = (int8_t *)malloc(n ? n : 1);
+    for (int k = 0; k < n; ++k) {
+        s->hang_i[3 * k] = i1[k]; s->hang_i[3 * k + 1] = i2[k]; s->hang_i[3 * k + 2] = i3[k];
+        s->hang_t[k] = heur_type(s->atype[i1[k]], s->atype[i2[k]]);
+    }
+    return 0;
+}
+/* heuristic dihedrals: type of (i2, i3) */
+int xo_set_heuristic_dihedrals(xo_sys *s, int32_t n, const int32_t *i1, const int32_t *i2, const int32_t *i3,
+                               const int32_t *i4) {
+    free(s->hdih_i); free(s->hdih_t);
+    s->n_hdih = n;
+    s->hdih_i = (int32_t *)malloc(sizeof(int32_t) * 4 * (n ? n : 1));
+    s->hdih_t = (int8_t *)malloc(n ? n : 1);
+    for (int k = 0; k < n; ++k) {
+        s->hdih_i[4 * k] = i1[k]; s->hdih_i[4 * k + 1] = i2[k];
+        s->hdih_i[4 * k + 2] = i3[k]; s->hdih_i[4 * k + 3] = i4[k];
+        s->hdih_t[k] = heur_type(s->atype[i2[k]], s->atype[i3[k]]);
     }
     return 0;
 }
@@ -1009,6 +1044,62 @@ static void qa_contact_transition(xo_sys *s, int64_t idx) {
 
 /* ---- force phase ------------------------------------------------------------- */
 
+/* eval_heurestic_angle_forces::iter: src/forces/angle/heurestic.cpp:29-59,
+   with the 7 coefficients a0..a6 of the type's table row */
+static void heur_angle_iter(const xo_sys *s, int idx, double *F, double *V) {
+    int i1 = s->hang_i[3 * idx], i2 = s->hang_i[3 * idx + 1], i3 = s->hang_i[3 * idx + 2];
+    const double *a = s->p.heur_ang_coeffs[s->hang_t[idx]];
+    v3 r1 = ld(s->r, i1), r2 = ld(s->r, i2), r3 = ld(s->r, i3);
+    v3 r12 = sub(r2, r1), r23 = sub(r3, r2);
+    v3 x12_23 = cross(r12, r23);
+    double r12_rn = ninv(r12), r23_rn = ninv(r23);
+    v3 d1 = scl(r12_rn, unit(cross(r12, x12_23)));
+    v3 d3 = scl(r23_rn, unit(cross(r23, x12_23)));
+    v3 d2 = sub(neg(d1), d3);
+    double cos_theta = -dot(r12, r23) * r12_rn * r23_rn;
+    double theta = acos_c(cos_theta);
+    double angle_V = 0.0, dV = 0.0;
+    for (int d = 6; d >= 0; --d) {
+        if (d > 0) dV = (double)d * a[d] + theta * dV;
+        angle_V = a[d] + theta * angle_V;
+    }
+    *V += angle_V;
+    dec(F, i1, scl(dV, d1));
+    dec(F, i2, scl(dV, d2));
+    dec(F, i3, scl(dV, d3));
+}
+
+/* eval_heurestic_dihedral_forces::iter: src/forces/dihedral/heurestic.cpp:29-70,
+   with phi = acos(cos_phi) (line 43 takes cos) and dV/dphi the derivative
+   of V (lines 52-54 add 2 c4 sin cos where d(cos^2)/dphi = -2 sin cos) */
+static void heur_dihedral_iter(const xo_sys *s, int idx, double *F, double *V) {
+    int i1 = s->hdih_i[4 * idx], i2 = s->hdih_i[4 * idx + 1], i3 = s->hdih_i[4 * idx + 2],
+        i4 = s->hdih_i[4 * idx + 3];
+    const double *c = s->p.heur_dih_coeffs[s->hdih_t[idx]];
+    v3 r1 = ld(s->r, i1), r2 = ld(s->r, i2), r3 = ld(s->r, i3), r4 = ld(s->r, i4);
+    v3 r12 = sub(r2, r1), r23 = sub(r3, r2), r34 = sub(r4, r3);
+    v3 x12_23 = cross(r12, r23), x23_34 = cross(r23, r34);
+    double x12_23_rn = ninv(x12_23), x23_34_rn = ninv(x23_34);
+    v3 x12_23_u = scl(x12_23_rn, x12_23), x23_34_u = scl(x23_34_rn, x23_34);
+    double cos_phi = dot(x12_23_u, x23_34_u);
+    double phi = acos_c(cos_phi);
+    if (dot(x12_23, r34) < 0.0) phi = -phi;
+    double sin_phi = sin(phi);
+    double sin2 = sin_phi * sin_phi, cos2 = cos_phi * cos_phi, sc = sin_phi * cos_phi;
+    *V += c[0] + c[1] * sin_phi + c[2] * cos_phi + c[3] * sin2 + c[4] * cos2 + c[5] * sc;
+    double dV = c[1] * cos_phi - c[2] * sin_phi + 2.0 * (c[3] - c[4]) * sc + c[5] * (cos2 - sin2);
+    double r23_n = nrm(r23);
+    v3 d1 = scl(x12_23_rn, scl(r23_n, neg(x12_23_u)));
+    v3 d4 = scl(x23_34_rn, scl(r23_n, x23_34_u));
+    double k1 = dot(r12, r23), k4 = dot(r23, r34), den = r23_n * r23_n;
+    v3 df = mk((-d1.x * k1 + d4.x * k4) / den, (-d1.y * k1 + d4.y * k4) / den, (-d1.z * k1 + d4.z * k4) / den);
+    v3 d2 = add(neg(d1), df), d3 = sub(neg(d4), df);
+    dec(F, i1, scl(dV, d1));
+    dec(F, i2, scl(dV, d2));
+    dec(F, i3, scl(dV, d3));
+    dec(F, i4, scl(dV, d4));
+}
+
 /* eval_chiral_forces::iter: src/forces/chiral.cpp:15-37 */
 static void chiral_iter(const xo_sys *s, int idx, double *F, double *V) {
     int i1 = s->chir_i[4 * idx], i2 = s->chir_i[4 * idx + 1], i3 = s->chir_i[4 * idx + 2], i4 = s->chir_i[4 * idx + 3];
@@ -1058,6 +1149,8 @@ static void pure_forces(const xo_sys *s, double *F, double *V) {
     if (p->on[XMD_TERM_QA]) for (int64_t k = 0; k < s->n_cont; ++k) qa_contact_force(s, k, F, &V[XMD_TERM_QA]);
     if (p->on[XMD_TERM_CHIR]) for (int k = 0; k < s->n_chir; ++k) chiral_iter(s, k, F, &V[XMD_TERM_CHIR]);
     if (p->on[XMD_TERM_NAT_SS]) for (int k = 0; k < s->n_ss; ++k) ss_iter(s, k, F, &V[XMD_TERM_NAT_SS]);
+    if (p->on[XMD_TERM_HEUR_ANG]) for (int k = 0; k < s->n_hang; ++k) heur_angle_iter(s, k, F, &V[XMD_TERM_HEUR_ANG]);
+    if (p->on[XMD_TERM_HEUR_DIH]) for (int k = 0; k < s->n_hdih; ++k) heur_dihedral_iter(s, k, F, &V[XMD_TERM_HEUR_DIH]);
 }
 
 int xo_eval_forces(xo_sys *s, double *F, double *V) {
@@ -1206,6 +1299,14 @@ int xo_step_omp(xo_sys *s, int32_t nsteps, int32_t nthreads) {
             if (p->on[XMD_TERM_NAT_SS]) {
 #pragma omp for schedule(static) nowait
                 for (int k = 0; k < s->n_ss; ++k) ss_iter(s, k, F, &V[XMD_TERM_NAT_SS]);
+            }
+            if (p->on[XMD_TERM_HEUR_ANG]) {
+#pragma omp for schedule(static) nowait
+                for (int k = 0; k < s->n_hang; ++k) heur_angle_iter(s, k, F, &V[XMD_TERM_HEUR_ANG]);
+            }
+            if (p->on[XMD_TERM_HEUR_DIH]) {
+#pragma omp for schedule(static) nowait
+                for (int k = 0; k < s->n_hdih; ++k) heur_dihedral_iter(s, k, F, &V[XMD_TERM_HEUR_DIH]);
             }
             if (p->on[XMD_TERM_QA]) {
 #pragma omp for schedule(static) nowait

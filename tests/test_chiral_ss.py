@@ -8,17 +8,12 @@ import numpy as np
 import pytest
 
 from oracle.pyoracle import REF_LIB, Oracle
-from tests.util import ANGSTROM, energy_rel, rel_err
+from tests.util import ANGSTROM, energy_rel, only_term, rel_err
 from xmd_gb300 import abi, synth
 
 have_ref = REF_LIB.exists()
 E_CHI = 1.0                             # chirality: e_chi = 1 eps
 H1, NAT_R = 100.0 / ANGSTROM**2, 6.0 * ANGSTROM   # native ssbonds: H1 = 100 eps/A^2, 6 A
-
-ONLY = ["tether forces", "native angles", "complex native dihedrals", "simple native dihedrals",
-        "native contacts", "Pauli exclusion", "const ES", "relative ES", "quasi-adiabatic potential",
-        "chirality", "native ssbonds"]
-
 
 def system(seed=21, n_ss=5, noise=0.25, lens=(60, 45)):
     """Chains near their native structure (so chirality and the disulfides sit
@@ -53,8 +48,7 @@ def yaml(prec="fp64", chir=True, ss=True):
 
 
 def only(term, y):
-    return y + "".join(f"\n{ONLY[k]}:\n  enabled: {'true' if k == term else 'false'}\n"
-                       for k in range(abi.NUM_TERMS))
+    return only_term(term, y)
 
 
 def chiral_energy(s, r):

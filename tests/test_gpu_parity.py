@@ -17,7 +17,7 @@ import numpy as np
 import pytest
 
 from oracle.pyoracle import Oracle
-from tests.util import ANGSTROM, FP64_CASES, energy_rel, horizon_snapshot, load_golden, rel_err
+from tests.util import ANGSTROM, FP64_CASES, energy_rel, horizon_snapshot, load_golden, only_term, rel_err
 from xmd_gb300 import Engine, abi, synth
 
 pytestmark = pytest.mark.gpu
@@ -281,13 +281,9 @@ def test_per_term_forces(case, term):
     forces and energy of that term alone within 1e-10 of the oracle,
     normalised by that term's own force scale."""
     s, y, _ = load_golden(case)
-    names = ["tether forces", "native angles", "complex native dihedrals", "simple native dihedrals",
-             "native contacts", "Pauli exclusion", "const ES", "relative ES", "quasi-adiabatic potential",
-             "chirality", "native ssbonds"]
     full = abi.parse_params(y)
     mc = Oracle(full, s, "port").cutoffs()
-    yy = y + "".join(f"\n{names[k]}:\n  enabled: {'true' if k == term else 'false'}\n"
-                     for k in range(abi.NUM_TERMS))
+    yy = only_term(term, y)
     yy += f"\nneighbor list:\n  cutoff: {float(mc[0] / ANGSTROM)!r} A\n  skin: {float(mc[1] / ANGSTROM)!r} A\n"
     p = abi.parse_params(yy)
     Fo, Vo = Oracle(p, s, "port").eval_forces()

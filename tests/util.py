@@ -11,6 +11,16 @@ GOLDEN = Path(__file__).resolve().parent / "golden"
 GOLDEN_CASES = ["c1_chain100", "c1_native100", "c2_periodic480", "c2_sparse240", "c3_qa600"]
 FP64_CASES = ["c1_chain100", "c1_native100", "c2_periodic480", "c2_sparse240"]
 ANGSTROM = 0.2
+# YAML section of each force term, in xmd_gb300.abi.TERM_* order
+SECTIONS = ["tether forces", "native angles", "complex native dihedrals", "simple native dihedrals",
+            "native contacts", "Pauli exclusion", "const ES", "relative ES", "quasi-adiabatic potential",
+            "chirality", "native ssbonds", "heurestic angles", "heurestic dihedrals"]
+
+
+def only_term(term: int, y: str) -> str:
+    """y with every force term off but `term`."""
+    return y + "".join(f"\n{SECTIONS[k]}:\n  enabled: {'true' if k == term else 'false'}\n"
+                       for k in range(len(SECTIONS)))
 
 
 def horizon_snapshot(z):

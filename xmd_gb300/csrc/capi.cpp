@@ -167,6 +167,21 @@ int xmd_gpu_set_chirals(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t 
     return guard([&] { ctx->eng->set_chirals(rep, n, i1, i2, i3, i4, nat_factor, nat_chir); });
 }
 
+int xmd_gpu_set_heuristic_angles(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1, const int32_t *i2,
+                                 const int32_t *i3) {
+    NEED_CTX;
+    if (n < 0 || (n > 0 && (!i1 || !i2 || !i3))) return fail(XMD_ERR_ARG, "set_heuristic_angles: null array");
+    return guard([&] { ctx->eng->set_heuristic_angles(rep, n, i1, i2, i3); });
+}
+
+int xmd_gpu_set_heuristic_dihedrals(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1, const int32_t *i2,
+                                    const int32_t *i3, const int32_t *i4) {
+    NEED_CTX;
+    if (n < 0 || (n > 0 && (!i1 || !i2 || !i3 || !i4)))
+        return fail(XMD_ERR_ARG, "set_heuristic_dihedrals: null array");
+    return guard([&] { ctx->eng->set_heuristic_dihedrals(rep, n, i1, i2, i3, i4); });
+}
+
 int xmd_gpu_set_ssbonds(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1, const int32_t *i2) {
     NEED_CTX;
     if (n < 0 || (n > 0 && (!i1 || !i2))) return fail(XMD_ERR_ARG, "set_ssbonds: null array");

@@ -470,6 +470,32 @@ void read_ss_table(const std::string &csv, double def_unit, double *out) {
         }
     }
 }
+// Heuristic coefficient tables (freeform/params.cpp:69-83, 101-118): two
+// residue-class columns (G, P, anything else = X), then the coefficients by
+// position.  The shipped header names fewer columns than the rows hold
+// (a0..a5 for 7 angle coefficients; no constant column for the dihedral's
+// 6), so the coefficients are read in row order: a0..a6 and c0..c5, the
+// orders eval_heurestic_angle_forces / eval_heurestic_dihedral_forces use.
+int heur_class(const std::string &s) {
+    if (s.empty()) throw std::runtime_error("empty residue class in a heuristic table");
+    return s[0] == 'G' ? 0 : (s[0] == 'P' ? 1 : 2);
+}
+
+void read_heur_table(const std::string &csv, int ncoef, double *out, const std::string &where) {
+    auto rows = read_csv(csv);
+    for (size_t r = 1; r < rows.size(); ++r) {
+        const auto &f = rows[r];
+        if (f.size() < 2) throw std::runtime_error(where + "short row");
+        const int type = 3 * heur_class(f[0]) + heur_class(f[1]);
+        int k = 0;
+        for (size_t c = 2; c < f.size(); ++c) {
+            if (f[c].empty()) continue;
+            if (k == ncoef) throw std::runtime_error(where + "too many coefficients in a row");
+            out[type * ncoef + k++] = parse_quantity(f[c], 1.0);
+        }
+        if (k != ncoef) throw std::runtime_error(where + "too few coefficients in a row");
+    }
+}
 }  // namespace
 
 void resolve_params(const YNode &root, xmd_params *o) {
@@ -532,6 +558,12 @@ void resolve_params(const YNode &root, xmd_params *o) {
     o->on[XMD_TERM_NAT_SS] = enabled(root, "native ssbonds");
     o->nat_ss_H1 = qval(section(root, "native ssbonds"), "H1", "native ssbonds: ");
     o->nat_ss_dist = qval(section(root, "native ssbonds"), "equilibrium dist", "native ssbonds: ");
+    o->on[XMD_TERM_HEUR_ANG] = enabled(root, "heurestic angles");
+    read_heur_table(sval(section(root, "heurestic angles"), "coefficients", "heurestic angles: "), 7,
+                    &o->heur_ang_coeffs[0][0], "heurestic angles: ");
+    o->on[XMD_TERM_HEUR_DIH] = enabled(root, "heurestic dihedrals");
+    read_heur_table(sval(section(root, "heurestic dihedrals"), "coefficients", "heurestic dihedrals: "), 6,
+                    &o->heur_dih_coeffs[0][0], "heurestic dihedrals: ");
     o->on[XMD_TERM_QA] = enabled(root, "quasi-adiabatic potential");
     {
         const YNode &q = section(root, "quasi-adiabatic potential");

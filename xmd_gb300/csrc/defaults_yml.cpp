@@ -43,6 +43,34 @@ simple native dihedrals:
   enabled: false
   CDH: 3.33 eps/rad**2
 
+heurestic angles:
+  enabled: true
+  coefficients: |-
+    type1,type2,a0,a1,a2,a3,a4,a5
+    G,G,20872.75597,-63260.52963,79318.301,-52680.17088,19554.21897,-3847.670279,313.6716916
+    G,P,8222.83155,-25178.89003,31841.70634,-21290.04519,7941.501624,-1567.87285,128.0761621
+    G,X,20872.75597,-63260.52963,79318.301,-52680.17088,19554.21897,-3847.670279,313.6716916
+    P,G,34646.70029,-109957.2324,144423.9036,-100525.9874,39127.31928,-8079.214542,691.8417699
+    P,P,10744.12043,-34148.94233,44818.66284,-31110.67875,12060.69185,-2479.723349,211.6367439
+    P,X,34646.70029,-109957.2324,144423.9036,-100525.9874,39127.31928,-8079.214542,691.8417699
+    X,G,15883.02041,-48923.1471,62360.6974,-42110.86572,15891.78309,-3178.490602,263.2916319
+    X,P,16912.27207,-53570.09757,70150.19389,-48602.41198,18791.04978,-3844.690523,325.3085829
+    X,X,15883.02041,-48923.1471,62360.6974,-42110.86572,15891.78309,-3178.490602,263.2916319
+
+heurestic dihedrals:
+  enabled: true
+  coefficients: |-
+    type2,type3,sin,cos,sin2,cos2,sin_cos
+    G,G,0.133672207,-0.007576316,0.003786907,-0.124627339,0.425373566,-0.060606303,
+    G,P,0.935285048,0.928786712,-0.18516837,0.015857805,0.2861951,0.072728001
+    G,X,0.210489196,-0.00606094,0.202709724,-0.160512736,0.461339767,0.13333598
+    P,G,0.233402207,-0.101516187,0.109235732,0.14906496,0.151803103,-0.742423775
+    P,P,1.810497634,1.171212546,0.091084321,-0.254152251,0.557619284,-1.569694253
+    P,X,0.661379307,0.115151794,0.428904959,0.200723546,0.100490651,-0.803028162
+    X,P,0.198889776,0.018181703,-0.070746181,0.122076238,0.178719533,-0.624241103
+    X,G,1.254229713,0.739393723,0.686217752,0.219188398,0.083115678,-0.790909154
+    X,X,0.275933756,0.00606063,0.257226522,0.15460117,0.146208844,-0.448484074
+
 native contacts:
   enabled: true
   lj depth: 1 eps

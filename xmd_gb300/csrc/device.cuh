@@ -237,11 +237,40 @@ __device__ __forceinline__ V3<T> tether_term(const TermP &p, double4_32a r1, dou
     return dV_dr * u;
 }
 
+// ---- heuristic angles and dihedrals -----------------------------------------
+
+// Horner sums of V(theta) = sum_{d=0..6} a_d theta^d and its derivative, in
+// the order of eval_heurestic_angle_forces::iter (angle/heurestic.cpp:45-50)
+__device__ __forceinline__ void heur_poly(const double *a, double theta, double *V, double *dV) {
+    double v = 0.0, dv = 0.0;
+#pragma unroll
+    for (int d = 6; d >= 0; --d) {
+        const double c = __ldg(a + d);
+        if (d > 0) dv = (double)d * c + theta * dv;
+        v = c + theta * v;
+    }
+    *V = v;
+    *dV = dv;
+}
+
+// V(phi) = c0 + c1 sin + c2 cos + c3 sin^2 + c4 cos^2 + c5 sin cos
+// (dihedral/heurestic.cpp:48-50) and dV/dphi, its derivative [the shipped
+// line 52-54 has +2 c4 sin cos where d(cos^2)/dphi = -2 sin cos]
+template <class T>
+__device__ __forceinline__ void heur_dih_V(const T *c, T s, T co, T *V, T *dV) {
+    const T s2 = s * s, c2 = co * co, sc = s * co;
+    *V = c[0] + c[1] * s + c[2] * co + c[3] * s2 + c[4] * c2 + c[5] * sc;
+    *dV = c[1] * co - c[2] * s + T(2) * (c[3] - c[4]) * sc + c[5] * (c2 - s2);
+}
+
 // native angle (c-1, c, c+1): eval_native_angle_forces::iter
-// angle/native.cpp:13-39.  Writes the forces on the three beads.
+// angle/native.cpp:13-39; or, with hc (the type's 7 coefficients), the
+// heuristic angle of eval_heurestic_angle_forces::iter
+// angle/heurestic.cpp:29-59, whose geometry is the same.  Writes the forces
+// on the three beads.
 template <class T>
 __device__ __forceinline__ void angle_term(const TermP &p, double4_32a q1, double4_32a q2, double4_32a q3, T nat_theta,
-                                           V3<T> *f1, V3<T> *f2, V3<T> *f3, T *V) {
+                                           const double *hc, V3<T> *f1, V3<T> *f2, V3<T> *f3, T *V) {
     V3<T> r12 = diff<T>(q1, q2), r23 = diff<T>(q2, q3);
     V3<T> x12_23 = cross(r12, r23);
     T r12_rn = ninv(r12), r23_rn = ninv(r23);
@@ -250,10 +279,18 @@ __device__ __forceinline__ void angle_term(const TermP &p, double4_32a q1, doubl
     V3<T> d2 = (-d1) - d3;
     T cos_theta = -dot(r12, r23) * r12_rn * r23_rn;
     T theta = acos_c(cos_theta);
-    T dtheta = theta - nat_theta;
-    T k = T(p.nat_ang_k);
-    *V = T(0.5) * k * dtheta * dtheta;
-    T dV = k * dtheta;
+    T dV;
+    if (hc) {
+        double Vd, dVd;
+        heur_poly(hc, (double)theta, &Vd, &dVd);
+        *V = (T)Vd;
+        dV = (T)dVd;
+    } else {
+        T dtheta = theta - nat_theta;
+        T k = T(p.nat_ang_k);
+        *V = T(0.5) * k * dtheta * dtheta;
+        dV = k * dtheta;
+    }
     *f1 = -(dV * d1);
     *f2 = -(dV * d2);
     *f3 = -(dV * d3);
@@ -261,10 +298,13 @@ __device__ __forceinline__ void angle_term(const TermP &p, double4_32a q1, doubl
 
 // native dihedral (c-1, c, c+1, c+2): eval_cnd_forces::iter
 // dihedral/complex_native.cpp:13-49 and eval_snd_forces::iter
-// dihedral/simple_native.cpp:13-45
+// dihedral/simple_native.cpp:13-45; or, with hc (the type's 6
+// coefficients), the heuristic dihedral of
+// eval_heurestic_dihedral_forces::iter dihedral/heurestic.cpp:29-70 with
+// phi = acos(cos_phi) [line 43 takes cos(cos_phi)], its energy in *Vc
 template <class T>
 __device__ __forceinline__ void dihedral_term(const TermP &p, double4_32a q1, double4_32a q2, double4_32a q3, double4_32a q4,
-                                              T nat_phi, bool cnd, bool snd, V3<T> *f, T *Vc, T *Vs) {
+                                              T nat_phi, bool cnd, bool snd, const T *hc, V3<T> *f, T *Vc, T *Vs) {
     V3<T> r12 = diff<T>(q1, q2), r23 = diff<T>(q2, q3), r34 = diff<T>(q3, q4);
     V3<T> x12_23 = cross(r12, r23), x23_34 = cross(r23, r34);
     T x12_23_rn = ninv(x12_23), x23_34_rn = ninv(x23_34);
@@ -276,7 +316,12 @@ __device__ __forceinline__ void dihedral_term(const TermP &p, double4_32a q1, do
     T dV = T(0);
     *Vc = T(0);
     *Vs = T(0);
-    if (cnd) {
+    if (hc) {
+        T c[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) c[k] = __ldg(hc + k);
+        heur_dih_V<T>(c, sin(phi), cos_phi, Vc, &dV);
+    } else if (cnd) {
         T sin_diff, cos_diff, sin_3diff, cos_3diff;
         sincos_(diff_, &sin_diff, &cos_diff);
         sincos_(T(3) * diff_, &sin_3diff, &cos_3diff);
@@ -284,7 +329,7 @@ __device__ __forceinline__ void dihedral_term(const TermP &p, double4_32a q1, do
         *Vc = CDA * (T(1) - cos_diff) + CDB * (T(1) - cos_3diff);
         dV += CDA * sin_diff + CDB * T(3) * sin_3diff;
     }
-    if (snd) {
+    if (snd && !hc) {
         T CDH = T(p.snd_CDH);
         *Vs = T(0.5) * CDH * diff_ * diff_;
         dV += CDH * diff_;
@@ -367,19 +412,29 @@ __device__ __forceinline__ V3<float> tether_vec(const TermP &p, V3<float> r12, f
     return dV_dr * V3<float>{r12.x * inv, r12.y * inv, r12.z * inv};
 }
 
-// r12, r23: narrowed bond vectors; x12_23: narrowed FP64 cross product
+// r12, r23: narrowed bond vectors; x12_23: narrowed FP64 cross product.
+// hc: heuristic angle coefficients (or null); their polynomial, whose terms
+// cancel to ~1e-5 of their size, is summed in FP64
 __device__ __forceinline__ void angle_mixed(const TermP &p, V3<float> r12, V3<float> r23, V3<float> x12_23,
-                                            float nat_theta, V3<float> *f1, V3<float> *f2, V3<float> *f3o,
-                                            float *V) {
+                                            float nat_theta, const double *hc, V3<float> *f1, V3<float> *f2,
+                                            V3<float> *f3o, float *V) {
     float r12_rn = 1.0f / norm(r12), r23_rn = 1.0f / norm(r23);
     V3<float> d1 = r12_rn * unit(cross(r12, x12_23));
     V3<float> d3 = r23_rn * unit(cross(r23, x12_23));
     V3<float> d2 = (-d1) - d3;
     float theta = atan2f(norm(x12_23), -dot(r12, r23));
-    float dtheta = theta - nat_theta;
-    float k = p.f.nat_ang_k;
-    *V = 0.5f * k * dtheta * dtheta;
-    float dV = k * dtheta;
+    float dV;
+    if (hc) {
+        double Vd, dVd;
+        heur_poly(hc, (double)theta, &Vd, &dVd);
+        *V = (float)Vd;
+        dV = (float)dVd;
+    } else {
+        float dtheta = theta - nat_theta;
+        float k = p.f.nat_ang_k;
+        *V = 0.5f * k * dtheta * dtheta;
+        dV = k * dtheta;
+    }
     *f1 = -(dV * d1);
     *f2 = -(dV * d2);
     *f3o = -(dV * d3);
@@ -387,9 +442,10 @@ __device__ __forceinline__ void angle_mixed(const TermP &p, V3<float> r12, V3<fl
 
 // narrowed bond vectors and cross products; X = x12_23 . x23_34 and
 // T = x12_23 . r34 taken in FP64 by the caller
+// (hc: heuristic dihedral coefficients or null, as dihedral_term)
 __device__ __forceinline__ void dihedral_mixed(const TermP &p, V3<float> r12, V3<float> r23, V3<float> r34,
                                                V3<float> x12_23, V3<float> x23_34, float X, float T,
-                                               float nat_phi, bool cnd, bool snd, V3<float> *f,
+                                               float nat_phi, bool cnd, bool snd, const float *hc, V3<float> *f,
                                                float *Vc, float *Vs) {
     float r23_n = norm(r23);
     float phi = atan2f(r23_n * T, X);
@@ -397,7 +453,13 @@ __device__ __forceinline__ void dihedral_mixed(const TermP &p, V3<float> r12, V3
     float dV = 0.0f;
     *Vc = 0.0f;
     *Vs = 0.0f;
-    if (cnd) {
+    if (hc) {
+        float c[6], sp, cp;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) c[k] = __ldg(hc + k);
+        sincosf(phi, &sp, &cp);
+        heur_dih_V<float>(c, sp, cp, Vc, &dV);
+    } else if (cnd) {
         float s1, c1, s3, c3;
         sincosf(diff_, &s1, &c1);
         sincosf(3.0f * diff_, &s3, &c3);
@@ -405,7 +467,7 @@ __device__ __forceinline__ void dihedral_mixed(const TermP &p, V3<float> r12, V3
         *Vc = CDA * (1.0f - c1) + CDB * (1.0f - c3);
         dV += CDA * s1 + CDB * 3.0f * s3;
     }
-    if (snd) {
+    if (snd && !hc) {
         float CDH = p.f.snd_CDH;
         *Vs = 0.5f * CDH * diff_ * diff_;
         dV += CDH * diff_;

@@ -218,21 +218,32 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
             else ft = tether_term<FT>(p, P[sp], P[sp + 1], (FT)d.teth_r0[c], &V_);
             if (MODE == 0 && own) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_TETHER], (double)V_);
         }
-        const bool do_ang = (fl & BF_ANG) && p.on[XMD_TERM_NAT_ANG];
-        const bool do_dih = (fl & BF_DIH) && (p.on[XMD_TERM_CND] || p.on[XMD_TERM_SND]);
+        // a centre's angle and dihedral are native or heuristic (seq-file
+        // models: those without a native value); both kinds share one call
+        const bool h_ang = (fl & BF_HANG) && p.on[XMD_TERM_HEUR_ANG];
+        const bool h_dih = (fl & BF_HDIH) && p.on[XMD_TERM_HEUR_DIH];
+        const bool do_ang = ((fl & BF_ANG) && p.on[XMD_TERM_NAT_ANG]) || h_ang;
+        const bool do_dih = ((fl & BF_DIH) && (p.on[XMD_TERM_CND] || p.on[XMD_TERM_SND])) || h_dih;
+        const double *hac = h_ang ? d.heur_ang + 7 * ((fl >> BF_HANG_SHIFT) & 15u) : nullptr;
+        const int hdt = (int)((fl >> BF_HDIH_SHIFT) & 15u);
+        const int ang_slot = h_ang ? XMD_TERM_HEUR_ANG : XMD_TERM_NAT_ANG;
         if constexpr (sizeof(FT) == 8) {
             if (do_ang) {
                 FT V_;
-                angle_term<FT>(p, P[sp - 1], P[sp], P[sp + 1], (FT)d.ang_t0[c], &a1, &a2, &a3, &V_);
-                if (MODE == 0 && own) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_NAT_ANG], (double)V_);
+                angle_term<FT>(p, P[sp - 1], P[sp], P[sp + 1], (FT)d.ang_t0[c], hac, &a1, &a2, &a3, &V_);
+                if (MODE == 0 && own) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + ang_slot], (double)V_);
             }
             if (do_dih) {
                 FT Vc, Vs;
                 dihedral_term<FT>(p, P[sp - 1], P[sp], P[sp + 1], P[sp + 2], (FT)d.dih_p0[c],
-                                  p.on[XMD_TERM_CND] != 0, p.on[XMD_TERM_SND] != 0, q, &Vc, &Vs);
+                                  p.on[XMD_TERM_CND] != 0, p.on[XMD_TERM_SND] != 0,
+                                  h_dih ? d.heur_dih + 6 * hdt : nullptr, q, &Vc, &Vs);
                 if (MODE == 0 && own) {
-                    if (p.on[XMD_TERM_CND]) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_CND], (double)Vc);
-                    if (p.on[XMD_TERM_SND]) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_SND], (double)Vs);
+                    if (h_dih) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_HEUR_DIH], (double)Vc);
+                    else {
+                        if (p.on[XMD_TERM_CND]) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_CND], (double)Vc);
+                        if (p.on[XMD_TERM_SND]) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_SND], (double)Vs);
+                    }
                 }
             }
         } else if (do_ang || do_dih) {
@@ -240,17 +251,21 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
             // FP32 forces
             if (do_ang) {
                 float V_;
-                angle_mixed(p, Ef[sp - 1], Ef[sp], Xf[sp], d.bond_f[c].y, &a1, &a2, &a3, &V_);
-                if (MODE == 0 && own) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_NAT_ANG], (double)V_);
+                angle_mixed(p, Ef[sp - 1], Ef[sp], Xf[sp], d.bond_f[c].y, hac, &a1, &a2, &a3, &V_);
+                if (MODE == 0 && own) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + ang_slot], (double)V_);
             }
             if (do_dih) {
                 float Vc, Vs;
                 const float X = dot(Xf[sp], Xf[sp + 1]), T = ff_dot(Xff[sp], Eff[sp + 1]).h;
                 dihedral_mixed(p, Ef[sp - 1], Ef[sp], Ef[sp + 1], Xf[sp], Xf[sp + 1], X, T, d.bond_f[c].z,
-                               p.on[XMD_TERM_CND] != 0, p.on[XMD_TERM_SND] != 0, q, &Vc, &Vs);
+                               p.on[XMD_TERM_CND] != 0, p.on[XMD_TERM_SND] != 0,
+                               h_dih ? d.heur_dih_f + 6 * hdt : nullptr, q, &Vc, &Vs);
                 if (MODE == 0 && own) {
-                    if (p.on[XMD_TERM_CND]) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_CND], (double)Vc);
-                    if (p.on[XMD_TERM_SND]) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_SND], (double)Vs);
+                    if (h_dih) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_HEUR_DIH], (double)Vc);
+                    else {
+                        if (p.on[XMD_TERM_CND]) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_CND], (double)Vc);
+                        if (p.on[XMD_TERM_SND]) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_SND], (double)Vs);
+                    }
                 }
             }
         }
@@ -1480,6 +1495,8 @@ int Engine::add_replica(int n, const int32_t *chain, const int32_t *seq, const u
     r.dih_p0.assign(n, nan);
     r.chir_f.assign(n, nan);
     r.chir_n.assign(n, nan);
+    r.hang_t.assign(n, -1);
+    r.hdih_t.assign(n, -1);
     if (dynamic) {
         // reuse a free slot; the replica is placed at the next eval/step
         for (int k = 0; k < (int)reps.size(); ++k)
@@ -1608,6 +1625,7 @@ void Engine::set_angles(int rep, int n, const int32_t *i1, const int32_t *i2, co
         if (!consecutive(r, i1[k], i2[k]) || !consecutive(r, i2[k], i3[k]))
             throw std::invalid_argument("angle must be (i-1, i, i+1) of one chain");
         if (!std::isnan(r.ang_t0[i2[k]])) throw std::invalid_argument("duplicate angle");
+        if (r.hang_t[i2[k]] >= 0) throw std::invalid_argument("angle is already heuristic");
         if (!std::isfinite(th[k])) throw std::invalid_argument("non-finite native angle");
         r.ang_t0[i2[k]] = th[k];
     }
@@ -1622,6 +1640,7 @@ void Engine::set_dihedrals(int rep, int n, const int32_t *i1, const int32_t *i2,
         if (!consecutive(r, i1[k], i2[k]) || !consecutive(r, i2[k], i3[k]) || !consecutive(r, i3[k], i4[k]))
             throw std::invalid_argument("dihedral must be (i-1, i, i+1, i+2) of one chain");
         if (!std::isnan(r.dih_p0[i2[k]])) throw std::invalid_argument("duplicate dihedral");
+        if (r.hdih_t[i2[k]] >= 0) throw std::invalid_argument("dihedral is already heuristic");
         if (!std::isfinite(ph[k])) throw std::invalid_argument("non-finite native dihedral");
         r.dih_p0[i2[k]] = ph[k];
     }
@@ -1659,6 +1678,39 @@ void Engine::set_chirals(int rep, int n, const int32_t *i1, const int32_t *i2, c
         if (!std::isfinite(f[k]) || !std::isfinite(c[k])) throw std::invalid_argument("non-finite chiral parameter");
         r.chir_f[i2[k]] = f[k];
         r.chir_n[i2[k]] = c[k];
+    }
+}
+// heur_ang_type / heur_dih_type: G = 0, P = 1, any other residue = 2,
+// type = 3 t1 + t2 (angle/heurestic.cpp:9-15, dihedral/heurestic.cpp:8-14)
+static int8_t heur_type(uint8_t a, uint8_t b) {
+    auto cls = [](uint8_t x) { return x == 7 ? 0 : (x == 14 ? 1 : 2); };   // GLY, PRO of amino_acid.h:10-13
+    return (int8_t)(3 * cls(a) + cls(b));
+}
+void Engine::set_heuristic_angles(int rep, int n, const int32_t *i1, const int32_t *i2, const int32_t *i3) {
+    check_rep(reps, rep);
+    if (reps[rep].placed) throw std::invalid_argument("topology is fixed once the replica is on the device");
+    RepHost &r = reps[rep];
+    std::fill(r.hang_t.begin(), r.hang_t.end(), (int8_t)-1);
+    for (int k = 0; k < n; ++k) {
+        if (!consecutive(r, i1[k], i2[k]) || !consecutive(r, i2[k], i3[k]))
+            throw std::invalid_argument("heuristic angle must be (i-1, i, i+1) of one chain");
+        if (r.hang_t[i2[k]] >= 0) throw std::invalid_argument("duplicate heuristic angle");
+        if (!std::isnan(r.ang_t0[i2[k]])) throw std::invalid_argument("angle is already native");
+        r.hang_t[i2[k]] = heur_type(r.atype[i1[k]], r.atype[i2[k]]);
+    }
+}
+void Engine::set_heuristic_dihedrals(int rep, int n, const int32_t *i1, const int32_t *i2, const int32_t *i3,
+                                     const int32_t *i4) {
+    check_rep(reps, rep);
+    if (reps[rep].placed) throw std::invalid_argument("topology is fixed once the replica is on the device");
+    RepHost &r = reps[rep];
+    std::fill(r.hdih_t.begin(), r.hdih_t.end(), (int8_t)-1);
+    for (int k = 0; k < n; ++k) {
+        if (!consecutive(r, i1[k], i2[k]) || !consecutive(r, i2[k], i3[k]) || !consecutive(r, i3[k], i4[k]))
+            throw std::invalid_argument("heuristic dihedral must be (i-1, i, i+1, i+2) of one chain");
+        if (r.hdih_t[i2[k]] >= 0) throw std::invalid_argument("duplicate heuristic dihedral");
+        if (!std::isnan(r.dih_p0[i2[k]])) throw std::invalid_argument("dihedral is already native");
+        r.hdih_t[i2[k]] = heur_type(r.atype[i2[k]], r.atype[i3[k]]);
     }
 }
 void Engine::set_ssbonds(int rep, int n, const int32_t *i1, const int32_t *i2) {
@@ -1792,6 +1844,19 @@ void Engine::allocate() {
         CK(cudaMemsetAsync(d.ss_on, 0, SS, stream));
         d.chir = (double2 *)dalloc(sizeof(double2) * N);
         d.chir_f32 = (float2 *)dalloc(sizeof(float2) * N);
+    }
+    {
+        // heuristic coefficient tables: constants of the context
+        double *ha = (double *)dalloc(sizeof(double) * 9 * 7);
+        double *hd = (double *)dalloc(sizeof(double) * 9 * 6);
+        float *hdf = (float *)dalloc(sizeof(float) * 9 * 6);
+        float tf[9 * 6];
+        for (int k = 0; k < 9 * 6; ++k) tf[k] = (float)(&params.heur_dih_coeffs[0][0])[k];
+        CK(cudaMemcpyAsync(ha, &params.heur_ang_coeffs[0][0], sizeof(double) * 9 * 7, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(hd, &params.heur_dih_coeffs[0][0], sizeof(double) * 9 * 6, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(hdf, tf, sizeof(float) * 9 * 6, cudaMemcpyHostToDevice, stream));
+        CK(cudaStreamSynchronize(stream));
+        d.heur_ang = ha; d.heur_dih = hd; d.heur_dih_f = hdf;
     }
     d.nl_row = (int32_t *)dalloc(sizeof(int32_t) * (size_t)nl_cap * N);
     d.nl_cnt = (int32_t *)dalloc(sizeof(int32_t) * N);
@@ -2035,6 +2100,8 @@ void Engine::place(int k) {
         if (!std::isnan(r.ang_t0[i])) { f |= BF_ANG; ar[i] = r.ang_t0[i]; }
         if (!std::isnan(r.dih_p0[i])) { f |= BF_DIH; dr[i] = r.dih_p0[i]; }
         if (!std::isnan(r.chir_f[i])) f |= BF_CHIR;
+        if (r.hang_t[i] >= 0) f |= BF_HANG | ((uint32_t)r.hang_t[i] << BF_HANG_SHIFT);
+        if (r.hdih_t[i] >= 0) f |= BF_HDIH | ((uint32_t)r.hdih_t[i] << BF_HDIH_SHIFT);
         if (i > 0 && consecutive(r, i - 1, i)) f |= BF_PREV;
         if (i + 1 < r.n && consecutive(r, i, i + 1)) f |= BF_NEXT;
         bfl[i] = f;

@@ -19,8 +19,11 @@ enum : uint32_t {
     BF_DIH = 4u,   // dihedral (i-1, i, i+1, i+2)
     BF_CHIR = 32u, // chiral quad (i-1, i, i+1, i+2)
     BF_PREV = 8u,  // i-1 is the previous bead of the same chain
-    BF_NEXT = 16u  // i+1 is the next bead of the same chain
+    BF_NEXT = 16u, // i+1 is the next bead of the same chain
+    BF_HANG = 64u, // heuristic angle (i-1, i, i+1); type in bits 8-11
+    BF_HDIH = 128u // heuristic dihedral (i-1, i, i+1, i+2); type in bits 12-15
 };
+constexpr int BF_HANG_SHIFT = 8, BF_HDIH_SHIFT = 12;
 
 // per-replica device record
 struct RepDev {
@@ -105,6 +108,9 @@ struct Dev {
     double *teth_r0, *ang_t0, *dih_p0;
     double2 *chir;          // (nat_factor, nat_chir) per centre i2 of a chiral quad
     float2 *chir_f32;       // the same in FP32 (mixed path)
+    const double *heur_ang;     // [9][7] heuristic angle coefficients a0..a6
+    const double *heur_dih;     // [9][6] heuristic dihedral coefficients c0..c5
+    const float *heur_dih_f;    // the same in FP32 (mixed path)
     int32_t *ss_start, *ss_end, *ss_j;   // native disulfide partners per bead (CSR, both directions)
     uint8_t *ss_on;         // in the list of the last rebuild (update_nat_ssbonds, native_ss.cpp:8-19)
     float4 *bond_f;         // (r0, theta0, phi0) in FP32 for the mixed path
@@ -149,6 +155,7 @@ struct RepHost {
     std::vector<double> teth_r0, ang_t0, dih_p0;   // per centre, NaN = absent
     std::vector<double> chir_f, chir_n;            // chirality per centre (i2), NaN = absent
     std::vector<int32_t> ss_i1, ss_i2;             // native disulfides
+    std::vector<int8_t> hang_t, hdih_t;            // heuristic angle / dihedral type per centre, -1 = absent
     std::vector<int32_t> nat_i1, nat_i2;
     std::vector<double> nat_d;
     std::vector<double> r, v;                      // initial state
@@ -253,6 +260,9 @@ public:
     void set_chirals(int rep, int n, const int32_t *i1, const int32_t *i2, const int32_t *i3, const int32_t *i4,
                      const double *factor, const double *chir);
     void set_ssbonds(int rep, int n, const int32_t *i1, const int32_t *i2);
+    void set_heuristic_angles(int rep, int n, const int32_t *i1, const int32_t *i2, const int32_t *i3);
+    void set_heuristic_dihedrals(int rep, int n, const int32_t *i1, const int32_t *i2, const int32_t *i3,
+                                 const int32_t *i4);
     void set_state(int rep, const double *r, const double *v);
     void set_history(int rep, const double *y, double t, uint64_t rng);
     void get_state(int rep, double *r, double *v, double *t);

@@ -76,6 +76,12 @@ class Engine:
         if getattr(s, "ssbonds", None) is not None:
             s1, s2 = (np.ascontiguousarray(x, dtype=np.int32) for x in s.ssbonds)
             check(self.lib.xmd_gpu_set_ssbonds(self.h, r, len(s1), iptr(s1), iptr(s2)))
+        if getattr(s, "heur_angles", None) is not None:
+            h = [np.ascontiguousarray(x, dtype=np.int32) for x in s.heur_angles]
+            check(self.lib.xmd_gpu_set_heuristic_angles(self.h, r, len(h[0]), *(iptr(x) for x in h)))
+        if getattr(s, "heur_dihedrals", None) is not None:
+            h = [np.ascontiguousarray(x, dtype=np.int32) for x in s.heur_dihedrals]
+            check(self.lib.xmd_gpu_set_heuristic_dihedrals(self.h, r, len(h[0]), *(iptr(x) for x in h)))
         rr = np.ascontiguousarray(s.r, dtype=np.float64).reshape(-1)
         check(self.lib.xmd_gpu_set_state(self.h, r, dptr(rr), None))
         self.sizes[r] = s.n

@@ -46,6 +46,8 @@ class System:
     meta: dict = field(default_factory=dict)
     chirals: tuple | None = None  # (i1, i2, i3, i4, nat_factor, nat_chir)
     ssbonds: tuple | None = None  # (i1, i2) native disulfide bonds
+    heur_angles: tuple | None = None     # (i1, i2, i3): angles without a native value
+    heur_dihedrals: tuple | None = None  # (i1, i2, i3, i4): dihedrals without a native value
 
 
 def _unit(v):
