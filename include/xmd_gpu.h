@@ -226,6 +226,16 @@ int xmd_gpu_set_history(xmd_gpu_ctx *ctx, int32_t rep, const double *y, double t
 int xmd_gpu_get_state(xmd_gpu_ctx *ctx, int32_t rep, double *r, double *v, double *t);
 int xmd_gpu_get_history(xmd_gpu_ctx *ctx, int32_t rep, double *y, double *t,
                         uint64_t *rng_state);
+/* Snapshot of the replica's whole mutable state (positions, history, time,
+ * per-bead generators, Verlet rows, Go/disulfide activity, quasi-adiabatic
+ * contacts, free pairs and valences): the store of main.cpp's make_saved
+ * items (include/xmd/store/store.h), with the generator, so that a restored
+ * run continues bit for bit.  Restore into the same replica slot of a context
+ * built the same way (same parameters, systems added in the same order);
+ * another layout is XMD_ERR_ARG. */
+int xmd_gpu_snapshot_size(xmd_gpu_ctx *ctx, int32_t rep, int64_t *bytes);
+int xmd_gpu_snapshot(xmd_gpu_ctx *ctx, int32_t rep, void *buf, int64_t bytes);
+int xmd_gpu_restore(xmd_gpu_ctx *ctx, int32_t rep, const void *buf, int64_t bytes);
 
 /* ---- hot path ------------------------------------------------------------ */
 /* Forces and per-term energies at the current state of one replica (the

@@ -113,6 +113,9 @@ SIGNATURES = [
     ("xmd_gpu_set_history", C.c_int, [C.c_void_p, C.c_int32, _pd, C.c_double, C.c_uint64]),
     ("xmd_gpu_get_state", C.c_int, [C.c_void_p, C.c_int32, _pd, _pd, _pd]),
     ("xmd_gpu_get_history", C.c_int, [C.c_void_p, C.c_int32, _pd, _pd, _pu64]),
+    ("xmd_gpu_snapshot_size", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64)]),
+    ("xmd_gpu_snapshot", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64]),
+    ("xmd_gpu_restore", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64]),
     ("xmd_gpu_eval_forces", C.c_int, [C.c_void_p, C.c_int32, _pd, _pd]),
     ("xmd_gpu_step", C.c_int, [C.c_void_p, C.c_int32]),
     ("xmd_gpu_observables", C.c_int, [C.c_void_p, C.c_int32, _pd, _pd, _pd, _pd]),

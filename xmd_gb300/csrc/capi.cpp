@@ -224,6 +224,24 @@ int xmd_gpu_get_history(xmd_gpu_ctx *ctx, int32_t rep, double *y, double *t, uin
     return guard([&] { ctx->eng->use_device(); ctx->eng->get_history(rep, y, t, rng_state); });
 }
 
+int xmd_gpu_snapshot_size(xmd_gpu_ctx *ctx, int32_t rep, int64_t *bytes) {
+    NEED_CTX;
+    if (!bytes) return fail(XMD_ERR_ARG, "snapshot_size: null output");
+    return guard([&] { ctx->eng->use_device(); *bytes = (int64_t)ctx->eng->snapshot_size(rep); });
+}
+
+int xmd_gpu_snapshot(xmd_gpu_ctx *ctx, int32_t rep, void *buf, int64_t bytes) {
+    NEED_CTX;
+    if (!buf || bytes < 0) return fail(XMD_ERR_ARG, "snapshot: null buffer");
+    return guard([&] { ctx->eng->use_device(); ctx->eng->snapshot(rep, buf, (size_t)bytes); });
+}
+
+int xmd_gpu_restore(xmd_gpu_ctx *ctx, int32_t rep, const void *buf, int64_t bytes) {
+    NEED_CTX;
+    if (!buf || bytes < 0) return fail(XMD_ERR_ARG, "restore: null buffer");
+    return guard([&] { ctx->eng->use_device(); ctx->eng->restore(rep, buf, (size_t)bytes); });
+}
+
 int xmd_gpu_eval_forces(xmd_gpu_ctx *ctx, int32_t rep, double *F, double *V) {
     NEED_CTX;
     return guard([&] { ctx->eng->use_device(); ctx->eng->eval_forces(rep, F, V); });

@@ -2350,6 +2350,160 @@ void Engine::get_state(int rep, double *r, double *v, double *t) {
     if (t) *t = rd.t;
 }
 
+// ---- snapshots: the replica's whole mutable device state -----------------------
+// The reference's store (include/xmd/store/store.h; main.cpp's make_saved
+// items) keeps positions, the Gear history, time, the pair lists and the QA
+// sets, but not the generator (a make_temp), so a resumed run draws new
+// noise.  A snapshot here holds everything a step reads and writes:
+// positions, Gear history, time, per-bead generators, skin origins, the
+// Verlet rows, native and disulfide activity, and the quasi-adiabatic state
+// (sync, contacts with their slots, free pairs).  Restoring it continues
+// the run bit for bit.  It is taken and restored in place: the replica must
+// sit at the same slots of a context built the same way (same parameters,
+// the same systems added in the same order); the header checks this.
+
+namespace {
+struct SnapHeader {
+    char magic[8];
+    uint32_t version, precision;
+    int32_t rep, n, begin, nl_cap;
+    int32_t nat_off, nat_len, ss_off, ss_len;
+    int32_t qa_on, fp_off, fp_len, ct_off, ct_len;
+    int32_t pad_;
+    uint64_t topo;
+};
+constexpr uint32_t SNAP_VERSION = 1;
+constexpr char SNAP_MAGIC[8] = {'X', 'M', 'D', 'S', 'N', 'A', 'P', '1'};
+struct SnapRep {   // the mutable scalars of RepDev
+    double t;
+    int32_t first, rebuild, fault, fp_n, ct_n, pad_;
+    long long steps_left;
+    unsigned long long maxdisp, rebuilds;
+};
+
+uint64_t fnv(uint64_t h, const void *p, size_t bytes) {
+    const unsigned char *c = (const unsigned char *)p;
+    for (size_t k = 0; k < bytes; ++k) h = (h ^ c[k]) * 1099511628211ull;
+    return h;
+}
+}  // namespace
+
+uint64_t Engine::topo_hash(int rep) const {
+    const RepHost &r = reps[rep];
+    uint64_t h = 1469598103934665603ull;
+    h = fnv(h, r.chain.data(), r.chain.size() * sizeof(int32_t));
+    h = fnv(h, r.seq.data(), r.seq.size() * sizeof(int32_t));
+    h = fnv(h, r.atype.data(), r.atype.size());
+    h = fnv(h, r.nat_i1.data(), r.nat_i1.size() * sizeof(int32_t));
+    h = fnv(h, r.nat_i2.data(), r.nat_i2.size() * sizeof(int32_t));
+    h = fnv(h, r.ss_i1.data(), r.ss_i1.size() * sizeof(int32_t));
+    h = fnv(h, r.ss_i2.data(), r.ss_i2.size() * sizeof(int32_t));
+    return h;
+}
+
+size_t Engine::snapshot_io(int rep, unsigned char *buf, size_t bytes, bool save) {
+    check_rep(reps, rep);
+    ready();
+    RepHost &h = reps[rep];
+    const int n = h.n, b = h.begin;
+    const size_t N = (size_t)d.N;
+    SnapHeader hd{};
+    std::memcpy(hd.magic, SNAP_MAGIC, 8);
+    hd.version = SNAP_VERSION;
+    hd.precision = (uint32_t)params.precision;
+    hd.rep = rep; hd.n = n; hd.begin = b; hd.nl_cap = 0;   // the row capacity may differ (below)
+    hd.nat_off = h.nat_off; hd.nat_len = h.nat_len; hd.ss_off = h.ss_off; hd.ss_len = h.ss_len;
+    hd.qa_on = d.qa_on; hd.fp_off = h.fp_off; hd.fp_len = h.fp_len; hd.ct_off = h.ct_off; hd.ct_len = h.ct_len;
+    hd.topo = topo_hash(rep);
+    size_t off = 0;
+    auto host = [&](void *p, size_t nb) {
+        if (buf && off + nb <= bytes) {
+            if (save) std::memcpy(buf + off, p, nb);
+            else std::memcpy(p, buf + off, nb);
+        }
+        off += nb;
+    };
+    auto dev = [&](void *p, size_t nb) {
+        if (buf && nb && off + nb <= bytes)
+            CK(cudaMemcpyAsync(save ? (void *)(buf + off) : p, save ? p : (const void *)(buf + off), nb,
+                               save ? cudaMemcpyDeviceToHost : cudaMemcpyHostToDevice, stream));
+        off += nb;
+    };
+    // rows [k][N] of a per-bead array: the replica's n entries of each row
+    auto rows = [&](void *base, size_t elem, int nrows) {
+        for (int k = 0; k < nrows; ++k) dev((char *)base + ((size_t)k * N + b) * elem, elem * n);
+    };
+    if (!save) {
+        if (!buf || bytes < sizeof(SnapHeader)) throw std::invalid_argument("snapshot too short");
+        SnapHeader got;
+        std::memcpy(&got, buf, sizeof got);
+        if (std::memcmp(got.magic, SNAP_MAGIC, 8) != 0 || got.version != SNAP_VERSION)
+            throw std::invalid_argument("not a snapshot of this format");
+        if (std::memcmp(&got, &hd, sizeof hd) != 0)
+            throw std::invalid_argument("snapshot of another replica layout (parameters, systems or their order differ)");
+    }
+    host(&hd, sizeof hd);
+    // Verlet row capacity of the snapshot; a restore grows this context's rows
+    // to it (capacity does not change the trajectory)
+    int32_t cap = nl_cap;
+    host(&cap, sizeof cap);
+    if (buf && !save) {
+        if (cap <= 0 || cap > (1 << 20)) throw std::invalid_argument("snapshot: bad row capacity");
+        if (cap > nl_cap) resize_rows(cap);
+    }
+    CK(cudaStreamSynchronize(stream));
+    RepDev rd;
+    CK(cudaMemcpy(&rd, d.rep + rep, sizeof(RepDev), cudaMemcpyDeviceToHost));
+    SnapRep sr{rd.t, rd.first, rd.rebuild, rd.fault, rd.fp_n, rd.ct_n, 0, rd.steps_left, rd.maxdisp, rd.rebuilds};
+    host(&sr, sizeof sr);
+    dev(d.pos[cur] + b, sizeof(double4_32a) * n);
+    rows(d.yh, sizeof(double), 15);
+    dev(d.orig + b, sizeof(double4_32a) * n);
+    dev(d.rng + b, sizeof(uint64_t) * n);
+    dev(d.nl_cnt + b, sizeof(int32_t) * n);
+    rows(d.nl_row, sizeof(int32_t), cap);
+    dev(d.nat_on + h.nat_off, h.nat_len);
+    dev(d.ss_on + h.ss_off, h.ss_len);
+    if (d.qa_on) {
+        rows(d.qa.sync, sizeof(int32_t), 1);
+        rows(d.qa.ref_cnt, sizeof(int32_t), 1);
+        rows(d.qa.ref, sizeof(int32_t), QA_REF_CAP);
+        const int fo = h.fp_off, fl = h.fp_len, co = h.ct_off, cl = h.ct_len;
+        dev(d.qa.fp_i1 + fo, sizeof(int32_t) * fl);
+        dev(d.qa.fp_i2 + fo, sizeof(int32_t) * fl);
+        dev(d.qa.fp_rep + fo, sizeof(int32_t) * fl);
+        dev(d.qa.fp_vac + fo, fl);
+        dev(d.qa.ct_i1 + co, sizeof(int32_t) * cl);
+        dev(d.qa.ct_i2 + co, sizeof(int32_t) * cl);
+        dev(d.qa.ct_type + co, sizeof(int32_t) * cl);
+        dev(d.qa.ct_d1 + co, sizeof(int32_t) * cl);
+        dev(d.qa.ct_d2 + co, sizeof(int32_t) * cl);
+        dev(d.qa.ct_status + co, cl);
+        dev(d.qa.ct_vac + co, cl);
+        dev(d.qa.ct_rm + co, cl);
+        dev(d.qa.ct_rep + co, sizeof(int32_t) * cl);
+        dev(d.qa.ct_ref + co, sizeof(double) * cl);
+    }
+    CK(cudaStreamSynchronize(stream));
+    if (buf && !save) {
+        if (off > bytes) throw std::invalid_argument("snapshot truncated");
+        rd.t = sr.t; rd.first = sr.first; rd.rebuild = sr.rebuild; rd.fault = sr.fault;
+        rd.fp_n = sr.fp_n; rd.ct_n = sr.ct_n; rd.steps_left = sr.steps_left;
+        rd.maxdisp = sr.maxdisp; rd.rebuilds = sr.rebuilds;
+        CK(cudaMemcpy(d.rep + rep, &rd, sizeof(RepDev), cudaMemcpyHostToDevice));
+        h.steps_left = sr.steps_left;
+    }
+    return off;
+}
+size_t Engine::snapshot_size(int rep) { return snapshot_io(rep, nullptr, 0, true); }
+void Engine::snapshot(int rep, void *buf, size_t bytes) {
+    if (bytes < snapshot_size(rep)) throw std::invalid_argument("snapshot buffer too small");
+    snapshot_io(rep, (unsigned char *)buf, bytes, true);
+}
+void Engine::restore(int rep, const void *buf, size_t bytes) {
+    snapshot_io(rep, (unsigned char *)const_cast<void *>(buf), bytes, false);
+}
+
 void Engine::get_history(int rep, double *y, double *t, uint64_t *rngs) {
     check_rep(reps, rep);
     ready();
@@ -2418,7 +2572,12 @@ bool Engine::grow_rows(double frac) {
     CK(cudaMemcpyAsync(&need, d.ctr + 1, sizeof(need), cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
     if ((double)need < frac * nl_cap) return false;
-    int ncap = (int)(2 * need + 16);
+    resize_rows((int)(2 * need + 16));
+    return true;
+}
+
+// Reallocate the Verlet rows with ncap slots per bead, keeping the rows held.
+void Engine::resize_rows(int ncap) {
     int32_t *rows = nullptr;
     CK(cudaMalloc(&rows, sizeof(int32_t) * (size_t)ncap * d.N));
     // rows are slot-major ([k][N]), so the current lists keep their place:
@@ -2434,7 +2593,6 @@ bool Engine::grow_rows(double frac) {
     d.nl_row = rows;
     d.nl_cap = nl_cap = ncap;
     drop_graphs();
-    return true;
 }
 
 void Engine::set_tuning(const Tune &t) {

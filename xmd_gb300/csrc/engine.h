@@ -267,6 +267,15 @@ public:
     void set_history(int rep, const double *y, double t, uint64_t rng);
     void get_state(int rep, double *r, double *v, double *t);
     void get_history(int rep, double *y, double *t, uint64_t *rng);
+    // whole mutable state of a replica (positions, history, generators, lists,
+    // quasi-adiabatic state) for an exact resume; restore into the same slot
+    // of a context built the same way
+    size_t snapshot_size(int rep);
+    void snapshot(int rep, void *buf, size_t bytes);
+    void restore(int rep, const void *buf, size_t bytes);
+    uint64_t topo_hash(int rep) const;
+    size_t snapshot_io(int rep, unsigned char *buf, size_t bytes, bool save);
+    void resize_rows(int ncap);
     void eval_forces(int rep, double *F, double *V);
     void step(int nsteps);
     void observables(int rep, double *E, double *K, double *Rg, double *Q);

@@ -139,6 +139,19 @@ class Engine:
         y = np.ascontiguousarray(y, dtype=np.float64).reshape(-1)
         check(self.lib.xmd_gpu_set_history(self.h, rep, dptr(y), float(t), int(rng_state)))
 
+    def snapshot(self, rep: int = 0) -> bytes:
+        """The replica's whole mutable state (xmd_gpu_snapshot)."""
+        nb = C.c_int64()
+        check(self.lib.xmd_gpu_snapshot_size(self.h, rep, C.byref(nb)))
+        buf = C.create_string_buffer(nb.value)
+        check(self.lib.xmd_gpu_snapshot(self.h, rep, buf, nb.value))
+        return buf.raw
+
+    def restore(self, rep: int, snap: bytes):
+        """Continue from a snapshot of the same replica slot (xmd_gpu_restore)."""
+        buf = C.create_string_buffer(bytes(snap), len(snap))
+        check(self.lib.xmd_gpu_restore(self.h, rep, buf, len(snap)))
+
     def observables(self, rep: int = 0):
         E, K, Rg, Q = C.c_double(), C.c_double(), C.c_double(), C.c_double()
         check(self.lib.xmd_gpu_observables(self.h, rep, C.byref(E), C.byref(K), C.byref(Rg), C.byref(Q)))
