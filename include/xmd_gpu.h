@@ -62,7 +62,9 @@ enum {
     XMD_TERM_NAT_SS = 10,   /* eval_nat_ssbond_forces src/forces/native_ss.cpp:27-40          */
     XMD_TERM_HEUR_ANG = 11, /* eval_heurestic_angle_forces src/forces/angle/heurestic.cpp:29-59 */
     XMD_TERM_HEUR_DIH = 12, /* eval_heurestic_dihedral_forces src/forces/dihedral/heurestic.cpp:29-70 */
-    XMD_NUM_TERMS = 13
+    XMD_TERM_VEL_AFM = 13,  /* eval_velocity_afm_forces src/forces/velocity_afm.cpp (no energy) */
+    XMD_TERM_FORCE_AFM = 14,/* eval_force_afm_forces src/forces/force_afm.cpp (no energy)       */
+    XMD_NUM_TERMS = 15
 };
 
 enum { XMD_PREC_FP64 = 0, XMD_PREC_MIXED = 1 };
@@ -134,6 +136,8 @@ typedef struct xmd_params {
        + c5 sin cos, per pair type of the dihedral's middle residues;
        `heurestic dihedrals: coefficients`, dihedral/heurestic.h:37-38 */
     double heur_dih_coeffs[9][6];
+    /* velocity AFM (velocity_afm.h: afm_force = harmonic(H1, H2, 0)) */
+    double vel_afm_H1, vel_afm_H2;
 } xmd_params;
 
 enum { XMD_NL_BUILD_AUTO = 0, XMD_NL_BUILD_CELL = 1, XMD_NL_BUILD_TILE = 2 };
@@ -211,6 +215,14 @@ int xmd_gpu_set_heuristic_angles(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const
  * (k, ..., k+3) of one chain; the type follows from the residues i2 and i3. */
 int xmd_gpu_set_heuristic_dihedrals(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1,
                                     const int32_t *i2, const int32_t *i3, const int32_t *i4);
+/* AFM tips (main.cpp:876-906).  Velocity tips vel_afm_tip{res_idx,
+ * afm_orig, afm_vel}: orig[3k..3k+2] (NaN: the bead's position when the
+ * replica is placed, as main.cpp:884 takes r[pulled_idx]) and vel[3k..];
+ * at most one per bead.  Force tips force_afm_tip{res_idx, pull_force}:
+ * F[3k..]; several on one bead add up. */
+int xmd_gpu_set_velocity_afm(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *bead,
+                             const double *orig, const double *vel);
+int xmd_gpu_set_force_afm(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *bead, const double *F);
 /* Native disulfide bonds (model contacts of type NAT_SS, main.cpp:554-598). */
 int xmd_gpu_set_ssbonds(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1, const int32_t *i2);
 /* All native contacts (nat_cont{i1,i2,nat_dist}, main.cpp:505-552). */

@@ -40,6 +40,8 @@ def _load(path: Path, pfx: str, params_type):
         "set_chirals": (C.c_int, [C.c_void_p, C.c_int32, _pi, _pi, _pi, _pi, _pd, _pd]),
         "set_ssbonds": (C.c_int, [C.c_void_p, C.c_int32, _pi, _pi]),
         "set_heuristic_angles": (C.c_int, [C.c_void_p, C.c_int32, _pi, _pi, _pi]),
+        "set_velocity_afm": (C.c_int, [C.c_void_p, C.c_int32, _pi, _pd, _pd]),
+        "set_force_afm": (C.c_int, [C.c_void_p, C.c_int32, _pi, _pd]),
         "set_heuristic_dihedrals": (C.c_int, [C.c_void_p, C.c_int32, _pi, _pi, _pi, _pi]),
         "set_state": (C.c_int, [C.c_void_p, _pd, _pd]),
         "set_history": (C.c_int, [C.c_void_p, _pd, C.c_double, C.c_uint64]),
@@ -109,6 +111,17 @@ class Oracle:
         b = getattr(s, "ssbonds", None)
         if b is not None:
             self.fn("set_ssbonds")(self.h, len(b[0]), ip(b[0]), ip(b[1]))
+        a = getattr(s, "afm_vel", None)
+        if a is not None:
+            # a NaN origin is the bead's start position (main.cpp:884)
+            o = np.array(a[1], dtype=np.float64).reshape(-1, 3)
+            start = np.asarray(s.r, dtype=np.float64).reshape(-1, 3)[np.asarray(a[0])]
+            o = np.where(np.isnan(o), start, o)
+            self.fn("set_velocity_afm")(self.h, len(a[0]), ip(a[0]), dp(o.reshape(-1)),
+                                        dp(np.asarray(a[2]).reshape(-1)))
+        a = getattr(s, "afm_force", None)
+        if a is not None:
+            self.fn("set_force_afm")(self.h, len(a[0]), ip(a[0]), dp(np.asarray(a[1]).reshape(-1)))
         h = getattr(s, "heur_angles", None)
         if h is not None:
             self.fn("set_heuristic_angles")(self.h, len(h[0]), ip(h[0]), ip(h[1]), ip(h[2]))

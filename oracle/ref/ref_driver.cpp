@@ -32,6 +32,8 @@
 #include <xmd/forces/native_ss.h>
 #include <xmd/model/model.h>
 #include <xmd/forces/angle/heurestic.h>
+#include <xmd/forces/velocity_afm.h>
+#include <xmd/forces/force_afm.h>
 #include <xmd/forces/dihedral/heurestic.h>
 #include <xmd/forces/pauli.h>
 #include <xmd/forces/es/const.h>
@@ -84,6 +86,8 @@ struct xr_sys {
     ::vector<chiral_quad> quads;
     ::vector<heur_ang> heur_angles;
     ::vector<heur_dih> heur_dihedrals;
+    ::vector<vel_afm_tip> vafm;
+    ::vector<force_afm_tip> fafm;
     ::vector<nat_ss> all_ss, cur_ss;
     std::vector<std::pair<int, int>> ss_sorted;
 
@@ -368,6 +372,18 @@ void term_forces(xr_sys *s, ::vector<vec3r> &F, real *V) {
         e.r = s->r.data(); e.F = F.data(); e.dihedrals = s->heur_dihedrals.view(); e.V = &V[XMD_TERM_HEUR_DIH];
         e();
     }
+    if (p.on[XMD_TERM_VEL_AFM]) {
+        // afm_force's nat_r is never set (main.cpp:876-879): a zero-length spring [D21]
+        eval_velocity_afm_forces e;
+        e.afm_force = harmonic((real)p.vel_afm_H1, (real)p.vel_afm_H2, (real)0.0);
+        e.r = s->r.data(); e.F = F.data(); e.t = &s->t; e.afm_tips = s->vafm.view();
+        e();
+    }
+    if (p.on[XMD_TERM_FORCE_AFM]) {
+        eval_force_afm_forces e;
+        e.F = F.data(); e.afm_tips = s->fafm.view();
+        e();
+    }
     if (p.on[XMD_TERM_NAT_SS]) {
         eval_nat_ssbond_forces e;
         e.H1 = p.nat_ss_H1; e.nat_r = p.nat_ss_dist;
@@ -543,6 +559,20 @@ int xr_morph_into_saw(int32_t nchains, const int32_t *lens, double bond, double 
     if (cell_out) {
         cell_out[0] = m.model_box.cell.x(); cell_out[1] = m.model_box.cell.y(); cell_out[2] = m.model_box.cell.z();
     }
+    return 0;
+}
+int xr_set_velocity_afm(void *h, int32_t n, const int32_t *bead, const double *orig, const double *vel) {
+    auto *s = (xr_sys *)h;
+    s->vafm.clear();
+    for (int k = 0; k < n; ++k)
+        s->vafm.emplace_back(bead[k], vec3r(orig[3 * k], orig[3 * k + 1], orig[3 * k + 2]),
+                             vec3r(vel[3 * k], vel[3 * k + 1], vel[3 * k + 2]));
+    return 0;
+}
+int xr_set_force_afm(void *h, int32_t n, const int32_t *bead, const double *F) {
+    auto *s = (xr_sys *)h;
+    s->fafm.clear();
+    for (int k = 0; k < n; ++k) s->fafm.emplace_back(bead[k], vec3r(F[3 * k], F[3 * k + 1], F[3 * k + 2]));
     return 0;
 }
 int xr_set_ssbonds(void *h, int32_t n, const int32_t *i1, const int32_t *i2) {

@@ -125,6 +125,8 @@ struct xo_sys {
     pair_i *ss; int32_t n_ss;                                   /* update_nat_ssbonds' list */
     int32_t n_hang; int32_t *hang_i; int8_t *hang_t;            /* heur_ang (angle/heurestic.h) */
     int32_t n_hdih; int32_t *hdih_i; int8_t *hdih_t;            /* heur_dih (dihedral/heurestic.h) */
+    int32_t n_vafm; int32_t *vafm_i; double *vafm_o, *vafm_v;   /* vel_afm_tip (velocity_afm.h) */
+    int32_t n_fafm; int32_t *fafm_i; double *fafm_F;            /* force_afm_tip (force_afm.h) */
     /* state */
     double *r, *v, *y[6], *F;
     double t, true_t;
@@ -265,6 +267,7 @@ void xo_destroy(xo_sys *s) {
     free(s->dih_i); free(s->dih_p); free(s->nat);
     free(s->chir_i); free(s->chir_f); free(s->chir_n); free(s->ss_all); free(s->ss);
     free(s->hang_i); free(s->hang_t); free(s->hdih_i); free(s->hdih_t);
+    free(s->vafm_i); free(s->vafm_o); free(s->vafm_v); free(s->fafm_i); free(s->fafm_F);
     free(s->r); free(s->v); free(s->F);
     for (int k = 0; k < 6; ++k) free(s->y[k]);
     free(s->orig_r); free(s->nl); free(s->go); free(s->pauli); free(s->es);
@@ -379,6 +382,30 @@ int xo_set_heuristic_dihedrals(xo_sys *s, int32_t n, const int32_t *i1, const in
         s->hdih_i[4 * k] = i1[k]; s->hdih_i[4 * k + 1] = i2[k];
         s->hdih_i[4 * k + 2] = i3[k]; s->hdih_i[4 * k + 3] = i4[k];
         s->hdih_t[k] = heur_type(s->atype[i2[k]], s->atype[i3[k]]);
+    }
+    return 0;
+}
+/* AFM tips (main.cpp:876-906): origins given explicitly */
+int xo_set_velocity_afm(xo_sys *s, int32_t n, const int32_t *bead, const double *orig, const double *vel) {
+    free(s->vafm_i); free(s->vafm_o); free(s->vafm_v);
+    s->n_vafm = n;
+    s->vafm_i = (int32_t *)malloc(sizeof(int32_t) * (n ? n : 1));
+    s->vafm_o = (double *)malloc(sizeof(double) * 3 * (n ? n : 1));
+    s->vafm_v = (double *)malloc(sizeof(double) * 3 * (n ? n : 1));
+    for (int k = 0; k < n; ++k) {
+        s->vafm_i[k] = bead[k];
+        for (int a = 0; a < 3; ++a) { s->vafm_o[3 * k + a] = orig[3 * k + a]; s->vafm_v[3 * k + a] = vel[3 * k + a]; }
+    }
+    return 0;
+}
+int xo_set_force_afm(xo_sys *s, int32_t n, const int32_t *bead, const double *F) {
+    free(s->fafm_i); free(s->fafm_F);
+    s->n_fafm = n;
+    s->fafm_i = (int32_t *)malloc(sizeof(int32_t) * (n ? n : 1));
+    s->fafm_F = (double *)malloc(sizeof(double) * 3 * (n ? n : 1));
+    for (int k = 0; k < n; ++k) {
+        s->fafm_i[k] = bead[k];
+        for (int a = 0; a < 3; ++a) s->fafm_F[3 * k + a] = F[3 * k + a];
     }
     return 0;
 }
@@ -1100,6 +1127,26 @@ static void heur_dihedral_iter(const xo_sys *s, int idx, double *F, double *V) {
     dec(F, i4, scl(dV, d4));
 }
 
+/* eval_velocity_afm_forces::iter: src/forces/velocity_afm.cpp; afm_force is
+   harmonic(H1, H2, nat_r = 0) (main.cpp sets H1 and H2 only) */
+static void vel_afm_iter(const xo_sys *s, int idx, double *F) {
+    int i = s->vafm_i[idx];
+    v3 r_ = ld(s->r, i);
+    v3 cur = add(ld(s->vafm_o, idx), scl(s->t, ld(s->vafm_v, idx)));
+    v3 r_afm = sub(cur, r_);
+    double r_afm_n = nrm(r_afm), r_afm_rn = 1.0 / r_afm_n;
+    if (r_afm_n == 0.0) return;   /* the spring at rest: no force (the shipped code gives 0 * inf) [D21] */
+    v3 r_afm_u = scl(r_afm_rn, r_afm);
+    double dr = r_afm_n - 0.0, dr2 = dr * dr;
+    double dV_dr = dr * (s->p.vel_afm_H1 + 2.0 * s->p.vel_afm_H2 * dr2);
+    dV_dr = clampd(dV_dr, -1.0e3, 1.0e3);
+    acc(F, i, scl(dV_dr, r_afm_u));
+}
+/* eval_force_afm_forces::iter: src/forces/force_afm.cpp */
+static void force_afm_iter(const xo_sys *s, int idx, double *F) {
+    acc(F, s->fafm_i[idx], ld(s->fafm_F, idx));
+}
+
 /* eval_chiral_forces::iter: src/forces/chiral.cpp:15-37 */
 static void chiral_iter(const xo_sys *s, int idx, double *F, double *V) {
     int i1 = s->chir_i[4 * idx], i2 = s->chir_i[4 * idx + 1], i3 = s->chir_i[4 * idx + 2], i4 = s->chir_i[4 * idx + 3];
@@ -1151,6 +1198,8 @@ static void pure_forces(const xo_sys *s, double *F, double *V) {
     if (p->on[XMD_TERM_NAT_SS]) for (int k = 0; k < s->n_ss; ++k) ss_iter(s, k, F, &V[XMD_TERM_NAT_SS]);
     if (p->on[XMD_TERM_HEUR_ANG]) for (int k = 0; k < s->n_hang; ++k) heur_angle_iter(s, k, F, &V[XMD_TERM_HEUR_ANG]);
     if (p->on[XMD_TERM_HEUR_DIH]) for (int k = 0; k < s->n_hdih; ++k) heur_dihedral_iter(s, k, F, &V[XMD_TERM_HEUR_DIH]);
+    if (p->on[XMD_TERM_VEL_AFM]) for (int k = 0; k < s->n_vafm; ++k) vel_afm_iter(s, k, F);
+    if (p->on[XMD_TERM_FORCE_AFM]) for (int k = 0; k < s->n_fafm; ++k) force_afm_iter(s, k, F);
 }
 
 int xo_eval_forces(xo_sys *s, double *F, double *V) {
@@ -1307,6 +1356,14 @@ int xo_step_omp(xo_sys *s, int32_t nsteps, int32_t nthreads) {
             if (p->on[XMD_TERM_HEUR_DIH]) {
 #pragma omp for schedule(static) nowait
                 for (int k = 0; k < s->n_hdih; ++k) heur_dihedral_iter(s, k, F, &V[XMD_TERM_HEUR_DIH]);
+            }
+            if (p->on[XMD_TERM_VEL_AFM]) {
+#pragma omp for schedule(static) nowait
+                for (int k = 0; k < s->n_vafm; ++k) vel_afm_iter(s, k, F);
+            }
+            if (p->on[XMD_TERM_FORCE_AFM]) {
+#pragma omp for schedule(static) nowait
+                for (int k = 0; k < s->n_fafm; ++k) force_afm_iter(s, k, F);
             }
             if (p->on[XMD_TERM_QA]) {
 #pragma omp for schedule(static) nowait

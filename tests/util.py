@@ -14,7 +14,8 @@ ANGSTROM = 0.2
 # YAML section of each force term, in xmd_gb300.abi.TERM_* order
 SECTIONS = ["tether forces", "native angles", "complex native dihedrals", "simple native dihedrals",
             "native contacts", "Pauli exclusion", "const ES", "relative ES", "quasi-adiabatic potential",
-            "chirality", "native ssbonds", "heurestic angles", "heurestic dihedrals"]
+            "chirality", "native ssbonds", "heurestic angles", "heurestic dihedrals", "velocity AFM",
+            "force AFM"]
 
 
 def only_term(term: int, y: str) -> str:

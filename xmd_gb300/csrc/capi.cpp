@@ -182,6 +182,19 @@ int xmd_gpu_set_heuristic_dihedrals(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, co
     return guard([&] { ctx->eng->set_heuristic_dihedrals(rep, n, i1, i2, i3, i4); });
 }
 
+int xmd_gpu_set_velocity_afm(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *bead, const double *orig,
+                             const double *vel) {
+    NEED_CTX;
+    if (n < 0 || (n > 0 && (!bead || !orig || !vel))) return fail(XMD_ERR_ARG, "set_velocity_afm: null array");
+    return guard([&] { ctx->eng->set_velocity_afm(rep, n, bead, orig, vel); });
+}
+
+int xmd_gpu_set_force_afm(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *bead, const double *F) {
+    NEED_CTX;
+    if (n < 0 || (n > 0 && (!bead || !F))) return fail(XMD_ERR_ARG, "set_force_afm: null array");
+    return guard([&] { ctx->eng->set_force_afm(rep, n, bead, F); });
+}
+
 int xmd_gpu_set_ssbonds(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1, const int32_t *i2) {
     NEED_CTX;
     if (n < 0 || (n > 0 && (!i1 || !i2))) return fail(XMD_ERR_ARG, "set_ssbonds: null array");

@@ -564,6 +564,10 @@ void resolve_params(const YNode &root, xmd_params *o) {
     o->on[XMD_TERM_HEUR_DIH] = enabled(root, "heurestic dihedrals");
     read_heur_table(sval(section(root, "heurestic dihedrals"), "coefficients", "heurestic dihedrals: "), 6,
                     &o->heur_dih_coeffs[0][0], "heurestic dihedrals: ");
+    o->on[XMD_TERM_VEL_AFM] = enabled(root, "velocity AFM");
+    o->vel_afm_H1 = qval(section(root, "velocity AFM"), "H1", "velocity AFM: ");
+    o->vel_afm_H2 = qval(section(root, "velocity AFM"), "H2", "velocity AFM: ");
+    o->on[XMD_TERM_FORCE_AFM] = enabled(root, "force AFM");
     o->on[XMD_TERM_QA] = enabled(root, "quasi-adiabatic potential");
     {
         const YNode &q = section(root, "quasi-adiabatic potential");

@@ -85,6 +85,14 @@ native ssbonds:
   H1: 100 eps/A**2
   equilibrium dist: 6.0 A
 
+velocity AFM:
+  enabled: false
+  H1: 0.06 eps/A**2
+  H2: 0 eps/A**2
+
+force AFM:
+  enabled: false
+
 Pauli exclusion:
   enabled: true
   r_excl: 4.0 A

@@ -439,7 +439,26 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
         }
     }
 
-    const V3<double> ftot = acc.total();
+    V3<double> ftot = acc.total();
+    if (d.rep[r].afm) {
+        const uint32_t fl_i = d.bflags[i];
+        if (fl_i & BF_AFM) {
+            const AfmTip tp = d.afm[fl_i >> BF_AFM_SHIFT];
+            if (tp.has_vel && p.on[XMD_TERM_VEL_AFM]) {
+                // eval_velocity_afm_forces::iter (velocity_afm.cpp): a
+                // harmonic(H1, H2, 0) spring to the tip at orig + t vel
+                const double tt = d.rep[r].t;
+                const V3<double> ra{tp.ox + tt * tp.vx - pi.x, tp.oy + tt * tp.vy - pi.y, tp.oz + tt * tp.vz - pi.z};
+                const double rn = norm(ra), rrn = 1.0 / rn;
+                const double dr2 = rn * rn;
+                double dV = rn * (p.vel_afm_H1 + 2.0 * p.vel_afm_H2 * dr2);
+                dV = clampv<double>(dV, -1.0e3, 1.0e3);
+                // the spring at rest pulls nothing (0 * inf in the shipped code)
+                if (rn > 0.0) ftot = ftot + dV * (rrn * ra);
+            }
+            if (p.on[XMD_TERM_FORCE_AFM]) ftot = ftot + V3<double>{tp.fx, tp.fy, tp.fz};
+        }
+    }
     const double fx = ftot.x, fy = ftot.y, fz = ftot.z;
     if (!(finite_bits(fx) && finite_bits(fy) && finite_bits(fz))) {
         // the replica is frozen from the next step on (its skin check sets
@@ -1713,6 +1732,46 @@ void Engine::set_heuristic_dihedrals(int rep, int n, const int32_t *i1, const in
         r.hdih_t[i2[k]] = heur_type(r.atype[i2[k]], r.atype[i3[k]]);
     }
 }
+void Engine::set_velocity_afm(int rep, int n, const int32_t *bead, const double *orig, const double *vel) {
+    check_rep(reps, rep);
+    if (reps[rep].placed) throw std::invalid_argument("topology is fixed once the replica is on the device");
+    if (dynamic) throw std::invalid_argument("AFM tips need a static context");
+    RepHost &r = reps[rep];
+    std::vector<int32_t> seen;
+    for (int k = 0; k < n; ++k) {
+        if (bead[k] < 0 || bead[k] >= r.n) throw std::invalid_argument("AFM tip bead out of range");
+        if (std::find(seen.begin(), seen.end(), bead[k]) != seen.end())
+            throw std::invalid_argument("one velocity AFM tip per bead");
+        seen.push_back(bead[k]);
+        for (int a = 0; a < 3; ++a)
+            if (!std::isfinite(vel[3 * k + a]) || std::isinf(orig[3 * k + a]))
+                throw std::invalid_argument("non-finite AFM tip");
+    }
+    r.vafm_i.assign(bead, bead + n);
+    r.vafm_o.assign(orig, orig + 3 * n);
+    r.vafm_v.assign(vel, vel + 3 * n);
+}
+void Engine::set_force_afm(int rep, int n, const int32_t *bead, const double *F) {
+    check_rep(reps, rep);
+    if (reps[rep].placed) throw std::invalid_argument("topology is fixed once the replica is on the device");
+    if (dynamic) throw std::invalid_argument("AFM tips need a static context");
+    RepHost &r = reps[rep];
+    for (int k = 0; k < n; ++k) {
+        if (bead[k] < 0 || bead[k] >= r.n) throw std::invalid_argument("AFM tip bead out of range");
+        for (int a = 0; a < 3; ++a)
+            if (!std::isfinite(F[3 * k + a])) throw std::invalid_argument("non-finite AFM force");
+    }
+    r.fafm_i.assign(bead, bead + n);
+    r.fafm_F.assign(F, F + 3 * n);
+}
+// beads of replica r pulled by some AFM tip, in order
+static std::vector<int> afm_beads(const RepHost &r) {
+    std::vector<int> v(r.vafm_i.begin(), r.vafm_i.end());
+    v.insert(v.end(), r.fafm_i.begin(), r.fafm_i.end());
+    std::sort(v.begin(), v.end());
+    v.erase(std::unique(v.begin(), v.end()), v.end());
+    return v;
+}
 void Engine::set_ssbonds(int rep, int n, const int32_t *i1, const int32_t *i2) {
     check_rep(reps, rep);
     if (reps[rep].placed) throw std::invalid_argument("topology is fixed once the replica is on the device");
@@ -1782,6 +1841,7 @@ void Engine::finalize() {
             cap.beads += r.n;
             cap.nat += 2 * (int)r.nat_i1.size();
             cap.ss += 2 * (int)r.ss_i1.size();
+            cap.afm += (int)afm_beads(r).size();
             const bool tile = params.nl_build == XMD_NL_BUILD_TILE ||
                               (params.nl_build == XMD_NL_BUILD_AUTO && r.n <= TILE_MAX);
             if (tile) cap.chunks += (r.n + TL_CH - 1) / TL_CH;
@@ -1844,6 +1904,7 @@ void Engine::allocate() {
         CK(cudaMemsetAsync(d.ss_on, 0, SS, stream));
         d.chir = (double2 *)dalloc(sizeof(double2) * N);
         d.chir_f32 = (float2 *)dalloc(sizeof(float2) * N);
+        d.afm = (AfmTip *)dalloc(sizeof(AfmTip) * (size_t)std::max(1, cap.afm));
     }
     {
         // heuristic coefficient tables: constants of the context
@@ -1889,6 +1950,8 @@ void Engine::allocate() {
     a_beads.init(N);
     a_nat.init(cap.nat);
     a_ss.init(cap.ss);
+    if (cap.afm > AFM_MAX_TIPS) throw std::length_error("engine: more AFM-pulled beads than the tip table holds");
+    a_afm.init(cap.afm);
     a_cells.init(cap.cells);
     a_chunks.init(cap.chunks);
     a_fp.init(cap.fp);
@@ -1945,6 +2008,8 @@ void Engine::allocate() {
     tp.chir_e_chi = p.chir_e_chi;
     tp.nat_ss_H1 = p.nat_ss_H1;
     tp.nat_ss_dist = p.nat_ss_dist;
+    tp.vel_afm_H1 = p.vel_afm_H1;
+    tp.vel_afm_H2 = p.vel_afm_H2;
     tp.f = TermP::F32{(float)tp.tether_H1, (float)tp.tether_H2, (float)tp.nat_ang_k, (float)tp.cnd_CDA,
                       (float)tp.cnd_CDB, (float)tp.snd_CDH, (float)tp.go_depth, (float)tp.pauli_r_excl,
                       (float)tp.pauli_depth, (float)tp.es_Vf, (float)tp.es_sdi, (float)tp.chir_e_chi,
@@ -2071,8 +2136,11 @@ void Engine::place(int k) {
     const int nfp = qa ? n * QA_FP_PER_BEAD + 256 : 0, nct = qa ? n * QA_CT_PER_BEAD + 256 : 0;
     // device ranges (all or nothing)
     int b = a_beads.alloc(n), no = a_nat.alloc(nnat), co = a_cells.alloc(ncell), ho = a_chunks.alloc(nchunk);
-    int fo = a_fp.alloc(nfp), to = a_ct.alloc(nct), so = a_ss.alloc(nss);
-    if (b < 0 || no < 0 || co < 0 || ho < 0 || fo < 0 || to < 0 || so < 0) {
+    const std::vector<int> afm_b = afm_beads(r);
+    const int nafm = (int)afm_b.size();
+    int fo = a_fp.alloc(nfp), to = a_ct.alloc(nct), so = a_ss.alloc(nss), ao = a_afm.alloc(nafm);
+    if (b < 0 || no < 0 || co < 0 || ho < 0 || fo < 0 || to < 0 || so < 0 || ao < 0) {
+        if (ao >= 0) a_afm.release(ao, nafm);
         if (so >= 0) a_ss.release(so, nss);
         if (b >= 0) a_beads.release(b, n);
         if (no >= 0) a_nat.release(no, nnat);
@@ -2089,6 +2157,7 @@ void Engine::place(int k) {
     r.chunk_off = ho; r.chunk_len = nchunk;
     r.fp_off = fo; r.fp_len = nfp;
     r.ct_off = to; r.ct_len = nct;
+    r.afm_off = ao; r.afm_len = nafm;
 
     // per-bead static data; chain ids are local (pairs never cross replicas)
     std::vector<int32_t> rep_of(n, k), seq(r.seq), chain(r.chain), ns(n), ne(n);
@@ -2102,6 +2171,11 @@ void Engine::place(int k) {
         if (!std::isnan(r.chir_f[i])) f |= BF_CHIR;
         if (r.hang_t[i] >= 0) f |= BF_HANG | ((uint32_t)r.hang_t[i] << BF_HANG_SHIFT);
         if (r.hdih_t[i] >= 0) f |= BF_HDIH | ((uint32_t)r.hdih_t[i] << BF_HDIH_SHIFT);
+        {
+            auto it = std::lower_bound(afm_b.begin(), afm_b.end(), i);
+            if (it != afm_b.end() && *it == i)
+                f |= BF_AFM | ((uint32_t)(ao + (int)(it - afm_b.begin())) << BF_AFM_SHIFT);
+        }
         if (i > 0 && consecutive(r, i - 1, i)) f |= BF_PREV;
         if (i + 1 < r.n && consecutive(r, i, i + 1)) f |= BF_NEXT;
         bfl[i] = f;
@@ -2197,6 +2271,29 @@ void Engine::place(int k) {
     rd.nchunk = nchunk;
     rd.active = 1;
     rd.steps_left = r.steps_left;
+    rd.afm = nafm > 0;
+    if (nafm) {
+        // the tips of each pulled bead; a velocity tip's origin defaults to
+        // the bead's position when placed (main.cpp:884)
+        std::vector<AfmTip> tips(nafm);
+        for (auto &tp : tips) tp = AfmTip{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+        auto slot = [&](int i) { return (int)(std::lower_bound(afm_b.begin(), afm_b.end(), i) - afm_b.begin()); };
+        for (size_t q = 0; q < r.vafm_i.size(); ++q) {
+            const int i = r.vafm_i[q];
+            AfmTip &tp = tips[slot(i)];
+            const double *o = &r.vafm_o[3 * q], *v = &r.vafm_v[3 * q];
+            tp.ox = std::isnan(o[0]) ? r.r[3 * i] : o[0];
+            tp.oy = std::isnan(o[1]) ? r.r[3 * i + 1] : o[1];
+            tp.oz = std::isnan(o[2]) ? r.r[3 * i + 2] : o[2];
+            tp.vx = v[0]; tp.vy = v[1]; tp.vz = v[2];
+            tp.has_vel = 1;
+        }
+        for (size_t q = 0; q < r.fafm_i.size(); ++q) {
+            AfmTip &tp = tips[slot(r.fafm_i[q])];
+            tp.fx += r.fafm_F[3 * q]; tp.fy += r.fafm_F[3 * q + 1]; tp.fz += r.fafm_F[3 * q + 2];
+        }
+        up(d.afm + ao, tips.data(), sizeof(AfmTip) * nafm);
+    }
     if (qa) {
         rd.fp_off = fo;
         rd.fp_cap = nfp;

@@ -21,9 +21,20 @@ enum : uint32_t {
     BF_PREV = 8u,  // i-1 is the previous bead of the same chain
     BF_NEXT = 16u, // i+1 is the next bead of the same chain
     BF_HANG = 64u, // heuristic angle (i-1, i, i+1); type in bits 8-11
-    BF_HDIH = 128u // heuristic dihedral (i-1, i, i+1, i+2); type in bits 12-15
+    BF_HDIH = 128u, // heuristic dihedral (i-1, i, i+1, i+2); type in bits 12-15
+    BF_AFM = 65536u // the bead is pulled by AFM tips; their slot in bits 17-31
 };
-constexpr int BF_HANG_SHIFT = 8, BF_HDIH_SHIFT = 12;
+constexpr int BF_HANG_SHIFT = 8, BF_HDIH_SHIFT = 12, BF_AFM_SHIFT = 17;
+constexpr int AFM_MAX_TIPS = 1 << 15;
+
+// the AFM tips on one bead: a velocity tip (vel_afm_tip{res_idx, afm_orig,
+// afm_vel}, velocity_afm.h) and the sum of its force tips
+// (force_afm_tip{res_idx, pull_force}, force_afm.h)
+struct AfmTip {
+    double ox, oy, oz, vx, vy, vz;
+    double fx, fy, fz;
+    int has_vel, pad_;
+};
 
 // per-replica device record
 struct RepDev {
@@ -58,6 +69,7 @@ struct RepDev {
     int fp_off, fp_cap, fp_n;
     int qa_bchunk_off, qa_nbchunk;   // chunks of QA_BCHUNK beads in QaDev::bchunk
     int ct_off, ct_cap, ct_n;
+    int afm;                 // some bead of the replica is pulled by an AFM tip
 };
 
 constexpr int QA_REF_CAP = 16;   // contacts per bead (valence bounds it by 10)
@@ -111,6 +123,7 @@ struct Dev {
     const double *heur_ang;     // [9][7] heuristic angle coefficients a0..a6
     const double *heur_dih;     // [9][6] heuristic dihedral coefficients c0..c5
     const float *heur_dih_f;    // the same in FP32 (mixed path)
+    AfmTip *afm;            // AFM tips, one slot per pulled bead
     int32_t *ss_start, *ss_end, *ss_j;   // native disulfide partners per bead (CSR, both directions)
     uint8_t *ss_on;         // in the list of the last rebuild (update_nat_ssbonds, native_ss.cpp:8-19)
     float4 *bond_f;         // (r0, theta0, phi0) in FP32 for the mixed path
@@ -156,6 +169,9 @@ struct RepHost {
     std::vector<double> chir_f, chir_n;            // chirality per centre (i2), NaN = absent
     std::vector<int32_t> ss_i1, ss_i2;             // native disulfides
     std::vector<int8_t> hang_t, hdih_t;            // heuristic angle / dihedral type per centre, -1 = absent
+    std::vector<int32_t> vafm_i, fafm_i;           // AFM tips: pulled bead
+    std::vector<double> vafm_o, vafm_v, fafm_F;    // [3 per tip] origin (NaN: placed position), velocity, force
+    int afm_off = 0, afm_len = 0;       // AFM tip slots
     std::vector<int32_t> nat_i1, nat_i2;
     std::vector<double> nat_d;
     std::vector<double> r, v;                      // initial state
@@ -261,6 +277,8 @@ public:
                      const double *factor, const double *chir);
     void set_ssbonds(int rep, int n, const int32_t *i1, const int32_t *i2);
     void set_heuristic_angles(int rep, int n, const int32_t *i1, const int32_t *i2, const int32_t *i3);
+    void set_velocity_afm(int rep, int n, const int32_t *bead, const double *orig, const double *vel);
+    void set_force_afm(int rep, int n, const int32_t *bead, const double *F);
     void set_heuristic_dihedrals(int rep, int n, const int32_t *i1, const int32_t *i2, const int32_t *i3,
                                  const int32_t *i4);
     void set_state(int rep, const double *r, const double *v);
@@ -329,11 +347,11 @@ private:
     void drop_graphs();
 
     struct Caps {
-        int beads = 0, reps = 0, nat = 0, cells = 0, chunks = 0, fp = 0, ct = 0, qab = 0, ss = 0;
+        int beads = 0, reps = 0, nat = 0, cells = 0, chunks = 0, fp = 0, ct = 0, qab = 0, ss = 0, afm = 0;
     } cap;
     bool dynamic = false;
     size_t bytes = 0;                          // device memory held
-    RangeAlloc a_beads, a_nat, a_cells, a_chunks, a_fp, a_ct, a_ss;
+    RangeAlloc a_beads, a_nat, a_cells, a_chunks, a_fp, a_ct, a_ss, a_afm;
     int qa_bchunk_next = 0;   // next free chunk of the QA re-listing (static contexts)
     std::vector<int32_t> owner_h;              // bead slot -> replica (or -1)
     void allocate();

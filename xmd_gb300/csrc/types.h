@@ -27,6 +27,7 @@ struct TermP {
     int ss_sinking;
     double chir_e_chi;                       // chirality (chiral.h)
     double nat_ss_H1, nat_ss_dist;           // native ssbonds (native_ss.h: H1, nat_r)
+    double vel_afm_H1, vel_afm_H2;           // velocity AFM spring (velocity_afm.h)
     // FP32 copies of the constants the mixed path's FP32 terms use (no
     // FP64-to-FP32 conversion per interaction)
     struct F32 {

@@ -76,6 +76,14 @@ class Engine:
         if getattr(s, "ssbonds", None) is not None:
             s1, s2 = (np.ascontiguousarray(x, dtype=np.int32) for x in s.ssbonds)
             check(self.lib.xmd_gpu_set_ssbonds(self.h, r, len(s1), iptr(s1), iptr(s2)))
+        if getattr(s, "afm_vel", None) is not None:
+            b = np.ascontiguousarray(s.afm_vel[0], dtype=np.int32)
+            o, v = (np.ascontiguousarray(x, dtype=np.float64).reshape(-1) for x in s.afm_vel[1:])
+            check(self.lib.xmd_gpu_set_velocity_afm(self.h, r, len(b), iptr(b), dptr(o), dptr(v)))
+        if getattr(s, "afm_force", None) is not None:
+            b = np.ascontiguousarray(s.afm_force[0], dtype=np.int32)
+            f = np.ascontiguousarray(s.afm_force[1], dtype=np.float64).reshape(-1)
+            check(self.lib.xmd_gpu_set_force_afm(self.h, r, len(b), iptr(b), dptr(f)))
         if getattr(s, "heur_angles", None) is not None:
             h = [np.ascontiguousarray(x, dtype=np.int32) for x in s.heur_angles]
             check(self.lib.xmd_gpu_set_heuristic_angles(self.h, r, len(h[0]), *(iptr(x) for x in h)))

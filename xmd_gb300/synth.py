@@ -48,6 +48,8 @@ class System:
     ssbonds: tuple | None = None  # (i1, i2) native disulfide bonds
     heur_angles: tuple | None = None     # (i1, i2, i3): angles without a native value
     heur_dihedrals: tuple | None = None  # (i1, i2, i3, i4): dihedrals without a native value
+    afm_vel: tuple | None = None         # (bead, orig[k, 3] (NaN: start position), vel[k, 3]) velocity AFM tips
+    afm_force: tuple | None = None       # (bead, F[k, 3]) force AFM tips
 
 
 def _unit(v):
