@@ -263,6 +263,22 @@ __device__ __forceinline__ void heur_dih_V(const T *c, T s, T co, T *V, T *dV) {
     *dV = c[1] * co - c[2] * s + T(2) * (c[3] - c[4]) * sc + c[5] * (c2 - s2);
 }
 
+// Out-of-line forms of the two heuristic sums: called, they leave a real
+// branch around them, where inlined the compiler predicates their FP64
+// arithmetic into every angle and dihedral centre (2% of the mixed step)
+__device__ __noinline__ double2 heur_poly_nl(const double *a, double theta) {
+    double v, dv;
+    heur_poly(a, theta, &v, &dv);
+    return make_double2(v, dv);
+}
+template <class T>
+__device__ __noinline__ void heur_dih_nl(const T *hc, T s, T co, T *V, T *dV) {
+    T c[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) c[k] = __ldg(hc + k);
+    heur_dih_V<T>(c, s, co, V, dV);
+}
+
 // native angle (c-1, c, c+1): eval_native_angle_forces::iter
 // angle/native.cpp:13-39; or, with hc (the type's 7 coefficients), the
 // heuristic angle of eval_heurestic_angle_forces::iter
@@ -281,10 +297,9 @@ __device__ __forceinline__ void angle_term(const TermP &p, double4_32a q1, doubl
     T theta = acos_c(cos_theta);
     T dV;
     if (hc) {
-        double Vd, dVd;
-        heur_poly(hc, (double)theta, &Vd, &dVd);
-        *V = (T)Vd;
-        dV = (T)dVd;
+        const double2 vd = heur_poly_nl(hc, (double)theta);
+        *V = (T)vd.x;
+        dV = (T)vd.y;
     } else {
         T dtheta = theta - nat_theta;
         T k = T(p.nat_ang_k);
@@ -317,10 +332,7 @@ __device__ __forceinline__ void dihedral_term(const TermP &p, double4_32a q1, do
     *Vc = T(0);
     *Vs = T(0);
     if (hc) {
-        T c[6];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) c[k] = __ldg(hc + k);
-        heur_dih_V<T>(c, sin(phi), cos_phi, Vc, &dV);
+        heur_dih_nl<T>(hc, sin(phi), cos_phi, Vc, &dV);
     } else if (cnd) {
         T sin_diff, cos_diff, sin_3diff, cos_3diff;
         sincos_(diff_, &sin_diff, &cos_diff);
@@ -425,10 +437,9 @@ __device__ __forceinline__ void angle_mixed(const TermP &p, V3<float> r12, V3<fl
     float theta = atan2f(norm(x12_23), -dot(r12, r23));
     float dV;
     if (hc) {
-        double Vd, dVd;
-        heur_poly(hc, (double)theta, &Vd, &dVd);
-        *V = (float)Vd;
-        dV = (float)dVd;
+        const double2 vd = heur_poly_nl(hc, (double)theta);
+        *V = (float)vd.x;
+        dV = (float)vd.y;
     } else {
         float dtheta = theta - nat_theta;
         float k = p.f.nat_ang_k;
@@ -454,11 +465,9 @@ __device__ __forceinline__ void dihedral_mixed(const TermP &p, V3<float> r12, V3
     *Vc = 0.0f;
     *Vs = 0.0f;
     if (hc) {
-        float c[6], sp, cp;
-#pragma unroll
-        for (int k = 0; k < 6; ++k) c[k] = __ldg(hc + k);
+        float sp, cp;
         sincosf(phi, &sp, &cp);
-        heur_dih_V<float>(c, sp, cp, Vc, &dV);
+        heur_dih_nl<float>(hc, sp, cp, Vc, &dV);
     } else if (cnd) {
         float s1, c1, s3, c3;
         sincosf(diff_, &s1, &c1);
