@@ -64,8 +64,12 @@ enum {
     XMD_TERM_HEUR_DIH = 12, /* eval_heurestic_dihedral_forces src/forces/dihedral/heurestic.cpp:29-70 */
     XMD_TERM_VEL_AFM = 13,  /* eval_velocity_afm_forces src/forces/velocity_afm.cpp (no energy) */
     XMD_TERM_FORCE_AFM = 14,/* eval_force_afm_forces src/forces/force_afm.cpp (no energy)       */
-    XMD_NUM_TERMS = 15
+    XMD_TERM_SOLID_WALL = 15,  /* eval_solid_wall_forces src/forces/walls/solid.cpp:12-27      */
+    XMD_TERM_LJ_WALL = 16,     /* eval_lj_attr_wall_forces src/forces/walls/lj_attr.cpp:5-43    */
+    XMD_NUM_TERMS = 17
 };
+
+#define XMD_MAX_WALLS 8   /* planes per wall kind */
 
 enum { XMD_PREC_FP64 = 0, XMD_PREC_MIXED = 1 };
 
@@ -138,6 +142,12 @@ typedef struct xmd_params {
     double heur_dih_coeffs[9][6];
     /* velocity AFM (velocity_afm.h: afm_force = harmonic(H1, H2, 0)) */
     double vel_afm_H1, vel_afm_H2;
+    /* solid walls (walls/solid.h: eps = depth, cutoff) */
+    double solid_wall_depth, solid_wall_cutoff;
+    /* LJ attractive walls (walls/lj_attr.h: wall_min_dist, breaking_factor,
+       cycle_time = phase duration; lj_depth = `depth`, which the shipped
+       params never read) */
+    double lj_wall_min_dist, lj_wall_breaking_factor, lj_wall_phase_duration, lj_wall_depth;
 } xmd_params;
 
 enum { XMD_NL_BUILD_AUTO = 0, XMD_NL_BUILD_CELL = 1, XMD_NL_BUILD_TILE = 2 };
@@ -223,6 +233,11 @@ int xmd_gpu_set_heuristic_dihedrals(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, co
 int xmd_gpu_set_velocity_afm(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *bead,
                              const double *orig, const double *vel);
 int xmd_gpu_set_force_afm(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *bead, const double *F);
+/* Wall planes plane{origin, normal} of one kind (0 = solid walls, 1 = LJ
+ * attractive walls; `planes:` of their YAML sections, main.cpp:815-871),
+ * at most XMD_MAX_WALLS each; they act on every replica.  Set before the
+ * first replica is placed. */
+int xmd_gpu_set_walls(xmd_gpu_ctx *ctx, int32_t kind, int32_t n, const double *origin, const double *normal);
 /* Native disulfide bonds (model contacts of type NAT_SS, main.cpp:554-598). */
 int xmd_gpu_set_ssbonds(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1, const int32_t *i2);
 /* All native contacts (nat_cont{i1,i2,nat_dist}, main.cpp:505-552). */

@@ -42,6 +42,7 @@ def _load(path: Path, pfx: str, params_type):
         "set_heuristic_angles": (C.c_int, [C.c_void_p, C.c_int32, _pi, _pi, _pi]),
         "set_velocity_afm": (C.c_int, [C.c_void_p, C.c_int32, _pi, _pd, _pd]),
         "set_force_afm": (C.c_int, [C.c_void_p, C.c_int32, _pi, _pd]),
+        "set_walls": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _pd, _pd]),
         "set_heuristic_dihedrals": (C.c_int, [C.c_void_p, C.c_int32, _pi, _pi, _pi, _pi]),
         "set_state": (C.c_int, [C.c_void_p, _pd, _pd]),
         "set_history": (C.c_int, [C.c_void_p, _pd, C.c_double, C.c_uint64]),
@@ -77,7 +78,8 @@ class Oracle:
     """One system on a CPU oracle.  kind: 'port' (C restatement) or 'ref'
     (the reference's compiled kernels)."""
 
-    def __init__(self, params, system, kind: str = "port", temperature=None, seed=None):
+    def __init__(self, params, system, kind: str = "port", temperature=None, seed=None, walls=None):
+        """walls: {kind: (origin[k, 3], normal[k, 3])}, kind 0 solid, 1 LJ attractive."""
         from xmd_gb300.abi import Params
         self.kind = kind
         self.pfx = "xo_" if kind == "port" else "xr_"
@@ -122,6 +124,10 @@ class Oracle:
         a = getattr(s, "afm_force", None)
         if a is not None:
             self.fn("set_force_afm")(self.h, len(a[0]), ip(a[0]), dp(np.asarray(a[1]).reshape(-1)))
+        for wk, (wo, wn) in (walls or {}).items():
+            if self.fn("set_walls")(self.h, int(wk), len(wo), dp(np.asarray(wo).reshape(-1)),
+                                    dp(np.asarray(wn).reshape(-1))) != 0:
+                raise ValueError("bad walls")
         h = getattr(s, "heur_angles", None)
         if h is not None:
             self.fn("set_heuristic_angles")(self.h, len(h[0]), ip(h[0]), ip(h[1]), ip(h[2]))

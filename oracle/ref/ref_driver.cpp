@@ -34,6 +34,8 @@
 #include <xmd/forces/angle/heurestic.h>
 #include <xmd/forces/velocity_afm.h>
 #include <xmd/forces/force_afm.h>
+#include <xmd/forces/walls/solid.h>
+#include <xmd/forces/walls/lj_attr.h>
 #include <xmd/forces/dihedral/heurestic.h>
 #include <xmd/forces/pauli.h>
 #include <xmd/forces/es/const.h>
@@ -88,6 +90,9 @@ struct xr_sys {
     ::vector<heur_dih> heur_dihedrals;
     ::vector<vel_afm_tip> vafm;
     ::vector<force_afm_tip> fafm;
+    ::vector<plane> walls[2];
+    ::vector<vec3r> wall_F[2];
+    ::vector<lj_attr_pair> ljw_pairs;
     ::vector<nat_ss> all_ss, cur_ss;
     std::vector<std::pair<int, int>> ss_sorted;
 
@@ -384,6 +389,25 @@ void term_forces(xr_sys *s, ::vector<vec3r> &F, real *V) {
         e.F = F.data(); e.afm_tips = s->fafm.view();
         e();
     }
+    if (p.on[XMD_TERM_SOLID_WALL]) {
+        eval_solid_wall_forces e;
+        e.eps = p.solid_wall_depth; e.cutoff = p.solid_wall_cutoff;
+        e.r = s->r.data(); e.F = F.data(); e.wall_F = s->wall_F[0].data(); e.box = &s->bx;
+        e.walls = s->walls[0].view(); e.V = &V[XMD_TERM_SOLID_WALL]; e.num_particles = s->n;
+        e();
+    }
+    if (p.on[XMD_TERM_LJ_WALL]) {
+        // lj_depth is never set by main.cpp:836-843: `depth` [D22]; one state
+        // per (wall, bead), wall-major (main.cpp:848-854)
+        eval_lj_attr_wall_forces e;
+        e.wall_min_dist = p.lj_wall_min_dist; e.lj_depth = p.lj_wall_depth;
+        e.cycle_time = p.lj_wall_phase_duration; e.cycle_time_inv = 1.0 / e.cycle_time;
+        e.breaking_factor = p.lj_wall_breaking_factor; e.factor = e.breaking_factor * pow(2.0, -1.0 / 6.0);
+        e.r = s->r.data(); e.F = F.data(); e.wall_F = s->wall_F[1].data(); e.box = &s->bx;
+        e.walls = s->walls[1].view(); e.V = &V[XMD_TERM_LJ_WALL]; e.t = &s->t; e.num_particles = s->n;
+        e.pairs = s->ljw_pairs.view();
+        e();
+    }
     if (p.on[XMD_TERM_NAT_SS]) {
         eval_nat_ssbond_forces e;
         e.H1 = p.nat_ss_H1; e.nat_r = p.nat_ss_dist;
@@ -573,6 +597,22 @@ int xr_set_force_afm(void *h, int32_t n, const int32_t *bead, const double *F) {
     auto *s = (xr_sys *)h;
     s->fafm.clear();
     for (int k = 0; k < n; ++k) s->fafm.emplace_back(bead[k], vec3r(F[3 * k], F[3 * k + 1], F[3 * k + 2]));
+    return 0;
+}
+int xr_set_walls(void *h, int32_t kind, int32_t n, const double *origin, const double *normal) {
+    auto *s = (xr_sys *)h;
+    if (kind < 0 || kind > 1) return -1;
+    s->walls[kind].clear();
+    for (int k = 0; k < n; ++k)
+        s->walls[kind].emplace_back(vec3r(origin[3 * k], origin[3 * k + 1], origin[3 * k + 2]),
+                                    vec3r(normal[3 * k], normal[3 * k + 1], normal[3 * k + 2]));
+    s->wall_F[kind].clear();
+    for (int k = 0; k < std::max(n, 1); ++k) s->wall_F[kind].emplace_back(0, 0, 0);
+    if (kind == 1) {
+        s->ljw_pairs.clear();
+        for (int w = 0; w < n; ++w)
+            for (int i = 0; i < s->n; ++i) s->ljw_pairs.emplace_back(i, w, FREE, vec3r(0, 0, 0), (real)0);
+    }
     return 0;
 }
 int xr_set_ssbonds(void *h, int32_t n, const int32_t *i1, const int32_t *i2) {

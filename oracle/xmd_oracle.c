@@ -127,6 +127,8 @@ struct xo_sys {
     int32_t n_hdih; int32_t *hdih_i; int8_t *hdih_t;            /* heur_dih (dihedral/heurestic.h) */
     int32_t n_vafm; int32_t *vafm_i; double *vafm_o, *vafm_v;   /* vel_afm_tip (velocity_afm.h) */
     int32_t n_fafm; int32_t *fafm_i; double *fafm_F;            /* force_afm_tip (force_afm.h) */
+    int32_t n_wall[2]; double wall[2][XMD_MAX_WALLS][6];       /* planes (origin, normal): solid, LJ attractive */
+    int8_t *ljw_status; double *ljw_joint, *ljw_ref;           /* lj_attr_pair per (wall, bead) */
     /* state */
     double *r, *v, *y[6], *F;
     double t, true_t;
@@ -268,6 +270,7 @@ void xo_destroy(xo_sys *s) {
     free(s->chir_i); free(s->chir_f); free(s->chir_n); free(s->ss_all); free(s->ss);
     free(s->hang_i); free(s->hang_t); free(s->hdih_i); free(s->hdih_t);
     free(s->vafm_i); free(s->vafm_o); free(s->vafm_v); free(s->fafm_i); free(s->fafm_F);
+    free(s->ljw_status); free(s->ljw_joint); free(s->ljw_ref);
     free(s->r); free(s->v); free(s->F);
     for (int k = 0; k < 6; ++k) free(s->y[k]);
     free(s->orig_r); free(s->nl); free(s->go); free(s->pauli); free(s->es);
@@ -406,6 +409,21 @@ int xo_set_force_afm(xo_sys *s, int32_t n, const int32_t *bead, const double *F)
     for (int k = 0; k < n; ++k) {
         s->fafm_i[k] = bead[k];
         for (int a = 0; a < 3; ++a) s->fafm_F[3 * k + a] = F[3 * k + a];
+    }
+    return 0;
+}
+/* wall planes (main.cpp:815-871); the LJ attractive pairs start free */
+int xo_set_walls(xo_sys *s, int32_t kind, int32_t n, const double *origin, const double *normal) {
+    if (kind < 0 || kind > 1 || n < 0 || n > XMD_MAX_WALLS) return -1;
+    s->n_wall[kind] = n;
+    for (int k = 0; k < n; ++k)
+        for (int a = 0; a < 3; ++a) { s->wall[kind][k][a] = origin[3 * k + a]; s->wall[kind][k][3 + a] = normal[3 * k + a]; }
+    if (kind == 1) {
+        free(s->ljw_status); free(s->ljw_joint); free(s->ljw_ref);
+        size_t m = (size_t)(n ? n : 1) * (size_t)s->n;
+        s->ljw_status = (int8_t *)calloc(m, 1);
+        s->ljw_joint = (double *)calloc(3 * m, sizeof(double));
+        s->ljw_ref = (double *)calloc(m, sizeof(double));
     }
     return 0;
 }
@@ -1142,6 +1160,82 @@ static void vel_afm_iter(const xo_sys *s, int idx, double *F) {
     dV_dr = clampd(dV_dr, -1.0e3, 1.0e3);
     acc(F, i, scl(dV_dr, r_afm_u));
 }
+/* box::wrap (include/xmd/model/box.h:37-43) */
+static v3 wrap(const xo_sys *s, v3 v) {
+    v.x -= s->cell[0] * nearbyint(v.x * s->cell_inv[0]);
+    v.y -= s->cell[1] * nearbyint(v.y * s->cell_inv[1]);
+    v.z -= s->cell[2] * nearbyint(v.z * s->cell_inv[2]);
+    return v;
+}
+static double signed_dist(v3 p, const double *pl) {   /* utils/geometry.h:17-20 */
+    return dot(mk(pl[3], pl[4], pl[5]), sub(p, mk(pl[0], pl[1], pl[2])));
+}
+/* eval_solid_wall_forces::iter (walls/solid.cpp:12-27): V = eps / (9 x^9)
+   inside the cutoff, with the force -dV/dx along the normal (the shipped
+   dV_dx = V * (-9 x) is added along +normal) [D22] */
+static void solid_wall_iter(const xo_sys *s, int idx, double *F, double *V) {
+    v3 part_r = wrap(s, ld(s->r, idx));
+    for (int w = 0; w < s->n_wall[0]; ++w) {
+        const double *pl = s->wall[0][w];
+        double x = signed_dist(part_r, pl);
+        if (x < s->p.solid_wall_cutoff) {
+            double x3 = x * x * x;
+            double V_ = s->p.solid_wall_depth / (9.0 * (x3 * x3 * x3));
+            double dV_dx = -9.0 * V_ / x;
+            *V += V_;
+            acc(F, idx, scl(-dV_dx, mk(pl[3], pl[4], pl[5])));
+        }
+    }
+}
+/* Force part of eval_lj_attr_wall_forces::loop (walls/lj_attr.cpp:16-31),
+   lj_depth = `depth` (never set by main.cpp:836-843) [D22] */
+static void lj_wall_force(const xo_sys *s, int w, int idx, double *F, double *V) {
+    size_t q = (size_t)w * s->n + idx;
+    int st = s->ljw_status[q];
+    if (st == 0) return;
+    v3 r_ = wrap(s, ld(s->r, idx));
+    double sat = fmin(s->t - s->ljw_ref[q], s->p.lj_wall_phase_duration) * (1.0 / s->p.lj_wall_phase_duration);
+    if (st == 2) sat = 1.0 - sat;
+    v3 r12 = sub(ld(s->ljw_joint, (int)q), r_);
+    double r12_rn = ninv(r12);
+    double V_, dV_dr;
+    lj_eval(s->p.lj_wall_depth, s->p.lj_wall_min_dist, r12_rn, &V_, &dV_dr);
+    *V += V_ * sat;
+    v3 r12_u = scl(r12_rn, r12);
+    acc(F, idx, scl(sat * dV_dr, r12_u));
+}
+/* State part of the same loop (lj_attr.cpp:8-14, 32-40), after the forces */
+static void lj_wall_transition(xo_sys *s, int w, int idx) {
+    size_t q = (size_t)w * s->n + idx;
+    int st = s->ljw_status[q];
+    v3 r_ = wrap(s, ld(s->r, idx));
+    const double *pl = s->wall[1][w];
+    if (st == 0) {
+        double x = signed_dist(r_, pl);
+        if (fabs(x) < s->p.lj_wall_min_dist) {
+            s->ljw_status[q] = 1;
+            v3 j = sub(r_, scl(x, mk(pl[3], pl[4], pl[5])));
+            st3(s->ljw_joint, (int)q, j);
+            s->ljw_ref[q] = s->t;
+        }
+        return;
+    }
+    double sat = fmin(s->t - s->ljw_ref[q], s->p.lj_wall_phase_duration) * (1.0 / s->p.lj_wall_phase_duration);
+    if (st == 2) sat = 1.0 - sat;
+    double r12_rn = ninv(sub(ld(s->ljw_joint, (int)q), r_));
+    double factor = s->p.lj_wall_breaking_factor * pow(2.0, -1.0 / 6.0);
+    if (st == 1 && sat == 1.0) {
+        if (factor * s->p.lj_wall_min_dist * r12_rn < 1.0) { s->ljw_status[q] = 2; s->ljw_ref[q] = s->t; }
+    } else if (st == 2 && sat == 0.0) {
+        s->ljw_status[q] = 0;
+    }
+}
+static void lj_wall_phase(xo_sys *s) {
+    if (!s->p.on[XMD_TERM_LJ_WALL]) return;
+    for (int w = 0; w < s->n_wall[1]; ++w)
+        for (int i = 0; i < s->n; ++i) lj_wall_transition(s, w, i);
+}
+
 /* eval_force_afm_forces::iter: src/forces/force_afm.cpp */
 static void force_afm_iter(const xo_sys *s, int idx, double *F) {
     acc(F, s->fafm_i[idx], ld(s->fafm_F, idx));
@@ -1200,6 +1294,10 @@ static void pure_forces(const xo_sys *s, double *F, double *V) {
     if (p->on[XMD_TERM_HEUR_DIH]) for (int k = 0; k < s->n_hdih; ++k) heur_dihedral_iter(s, k, F, &V[XMD_TERM_HEUR_DIH]);
     if (p->on[XMD_TERM_VEL_AFM]) for (int k = 0; k < s->n_vafm; ++k) vel_afm_iter(s, k, F);
     if (p->on[XMD_TERM_FORCE_AFM]) for (int k = 0; k < s->n_fafm; ++k) force_afm_iter(s, k, F);
+    if (p->on[XMD_TERM_SOLID_WALL]) for (int k = 0; k < s->n; ++k) solid_wall_iter(s, k, F, &V[XMD_TERM_SOLID_WALL]);
+    if (p->on[XMD_TERM_LJ_WALL])
+        for (int w = 0; w < s->n_wall[1]; ++w)
+            for (int k = 0; k < s->n; ++k) lj_wall_force(s, w, k, F, &V[XMD_TERM_LJ_WALL]);
 }
 
 int xo_eval_forces(xo_sys *s, double *F, double *V) {
@@ -1277,6 +1375,7 @@ int xo_step(xo_sys *s, int32_t nsteps) {
     for (int32_t k = 0; k < nsteps; ++k) {
         pure_forces(s, s->F, s->V);
         if (s->p.on[XMD_TERM_QA]) qa_state_phase(s);
+        lj_wall_phase(s);
         if (s->p.langevin_on) lang_pc(s);
         ensure_nl(s);
     }
@@ -1365,6 +1464,16 @@ int xo_step_omp(xo_sys *s, int32_t nsteps, int32_t nthreads) {
 #pragma omp for schedule(static) nowait
                 for (int k = 0; k < s->n_fafm; ++k) force_afm_iter(s, k, F);
             }
+            if (p->on[XMD_TERM_SOLID_WALL]) {
+#pragma omp for schedule(static) nowait
+                for (int k = 0; k < s->n; ++k) solid_wall_iter(s, k, F, &V[XMD_TERM_SOLID_WALL]);
+            }
+            if (p->on[XMD_TERM_LJ_WALL]) {
+                for (int w = 0; w < s->n_wall[1]; ++w) {
+#pragma omp for schedule(static) nowait
+                    for (int k = 0; k < s->n; ++k) lj_wall_force(s, w, k, F, &V[XMD_TERM_LJ_WALL]);
+                }
+            }
             if (p->on[XMD_TERM_QA]) {
 #pragma omp for schedule(static) nowait
                 for (int64_t k = 0; k < s->n_cont; ++k) qa_contact_force(s, k, F, &V[XMD_TERM_QA]);
@@ -1408,6 +1517,7 @@ int xo_step_omp(xo_sys *s, int32_t nsteps, int32_t nthreads) {
                     int64_t n_before = s->n_cont;
                     for (int64_t k = 0; k < n_before; ++k) qa_contact_transition(s, k);
                 }
+                lj_wall_phase(s);
                 if (p->langevin_on) lang_pc(s);
                 ensure_nl(s);
             }

@@ -10,14 +10,14 @@ from pathlib import Path
 
 import numpy as np
 
-NUM_TERMS = 15
+NUM_TERMS = 17
 NUM_AA = 20
 NUM_SS = NUM_AA * NUM_AA
 TERM_NAMES = ["tether", "nat_ang", "cnd", "snd", "go", "pauli", "const_es", "rel_es", "qa",
-              "chir", "nat_ss", "heur_ang", "heur_dih", "vel_afm", "force_afm"]
+              "chir", "nat_ss", "heur_ang", "heur_dih", "vel_afm", "force_afm", "solid_wall", "lj_wall"]
 (TERM_TETHER, TERM_NAT_ANG, TERM_CND, TERM_SND, TERM_GO, TERM_PAULI, TERM_CONST_ES,
  TERM_REL_ES, TERM_QA, TERM_CHIR, TERM_NAT_SS, TERM_HEUR_ANG, TERM_HEUR_DIH,
- TERM_VEL_AFM, TERM_FORCE_AFM) = range(NUM_TERMS)
+ TERM_VEL_AFM, TERM_FORCE_AFM, TERM_SOLID_WALL, TERM_LJ_WALL) = range(NUM_TERMS)
 PREC_FP64, PREC_MIXED = 0, 1
 NOALLOC_MAX_BEADS = 65536   # XMD_NOALLOC_MAX_BEADS
 
@@ -54,6 +54,9 @@ class Params(C.Structure):
         ("chir_e_chi", _d), ("nat_ss_H1", _d), ("nat_ss_dist", _d),
         ("heur_ang_coeffs", (_d * 7) * 9), ("heur_dih_coeffs", (_d * 6) * 9),
         ("vel_afm_H1", _d), ("vel_afm_H2", _d),
+        ("solid_wall_depth", _d), ("solid_wall_cutoff", _d),
+        ("lj_wall_min_dist", _d), ("lj_wall_breaking_factor", _d), ("lj_wall_phase_duration", _d),
+        ("lj_wall_depth", _d),
     ]
 
     def copy(self) -> "Params":
@@ -111,6 +114,7 @@ SIGNATURES = [
     ("xmd_gpu_set_ssbonds", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _pi32, _pi32]),
     ("xmd_gpu_set_velocity_afm", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _pi32, _pd, _pd]),
     ("xmd_gpu_set_force_afm", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _pi32, _pd]),
+    ("xmd_gpu_set_walls", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _pd, _pd]),
     ("xmd_gpu_set_heuristic_angles", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _pi32, _pi32, _pi32]),
     ("xmd_gpu_set_heuristic_dihedrals", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _pi32, _pi32, _pi32, _pi32]),
     ("xmd_gpu_set_state", C.c_int, [C.c_void_p, C.c_int32, _pd, _pd]),

@@ -195,6 +195,12 @@ int xmd_gpu_set_force_afm(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_
     return guard([&] { ctx->eng->set_force_afm(rep, n, bead, F); });
 }
 
+int xmd_gpu_set_walls(xmd_gpu_ctx *ctx, int32_t kind, int32_t n, const double *origin, const double *normal) {
+    NEED_CTX;
+    if (n < 0 || (n > 0 && (!origin || !normal))) return fail(XMD_ERR_ARG, "set_walls: null array");
+    return guard([&] { ctx->eng->set_walls(kind, n, origin, normal); });
+}
+
 int xmd_gpu_set_ssbonds(xmd_gpu_ctx *ctx, int32_t rep, int32_t n, const int32_t *i1, const int32_t *i2) {
     NEED_CTX;
     if (n < 0 || (n > 0 && (!i1 || !i2))) return fail(XMD_ERR_ARG, "set_ssbonds: null array");

@@ -568,6 +568,18 @@ void resolve_params(const YNode &root, xmd_params *o) {
     o->vel_afm_H1 = qval(section(root, "velocity AFM"), "H1", "velocity AFM: ");
     o->vel_afm_H2 = qval(section(root, "velocity AFM"), "H2", "velocity AFM: ");
     o->on[XMD_TERM_FORCE_AFM] = enabled(root, "force AFM");
+    o->on[XMD_TERM_SOLID_WALL] = enabled(root, "solid walls");
+    o->solid_wall_depth = qval(section(root, "solid walls"), "depth", "solid walls: ");
+    o->solid_wall_cutoff = qval(section(root, "solid walls"), "cutoff", "solid walls: ");
+    {
+        const YNode &w = section(root, "LJ attractive walls");
+        const std::string ws = "LJ attractive walls: ";
+        o->on[XMD_TERM_LJ_WALL] = enabled(root, "LJ attractive walls");
+        o->lj_wall_min_dist = qval(w, "wall min dist", ws);
+        o->lj_wall_breaking_factor = qval(w, "breaking factor", ws);
+        o->lj_wall_phase_duration = qval(w, "phase duration", ws);
+        o->lj_wall_depth = qval(w, "depth", ws);
+    }
     o->on[XMD_TERM_QA] = enabled(root, "quasi-adiabatic potential");
     {
         const YNode &q = section(root, "quasi-adiabatic potential");

@@ -85,6 +85,18 @@ native ssbonds:
   H1: 100 eps/A**2
   equilibrium dist: 6.0 A
 
+solid walls:
+  enabled: false
+  depth: 1 eps
+  cutoff: 5.0 A
+
+LJ attractive walls:
+  enabled: false
+  wall min dist: 5.0 A
+  breaking factor: 1.5
+  phase duration: 10 tau
+  depth: 1 eps
+
 velocity AFM:
   enabled: false
   H1: 0.06 eps/A**2

@@ -143,6 +143,116 @@ template <> __device__ __forceinline__ float nat_dist<float>(const Dev &d, int k
 // MODE 1: forces, then one Langevin predictor-corrector step (lang_pc.cpp:5-41)
 //         writing pos[cur^1], y1..y5, the generator state and the skin-test
 //         displacement (verify.cpp:10-15).
+// Wall forces on one bead at its wrapped position rw.  ljw points at the bead's state for the first LJ attractive
+// wall (stride N); step = true advances the pair states.
+struct WallOut { double fx, fy, fz, vs, vl; };
+__device__ __forceinline__ WallOut wall_forces(const double *wall, LjWallState *ljw, size_t N, V3<double> rw,
+                                            double tt, bool step, int n_solid, int n_ljw, double solid_eps,
+                                            double solid_cutoff, double min_dist, double factor, double cycle,
+                                            double cycle_inv, double depth) {
+    WallOut o{0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int w = 0; w < n_solid; ++w) {
+        // eval_solid_wall_forces::iter (walls/solid.cpp:12-27): V = eps /
+        // (9 x^9) inside the cutoff, its force -dV/dx along the normal [the
+        // shipped dV_dx = V (-9 x), added along +normal]
+        const double *pl = wall + 6 * w;
+        const double x = pl[3] * (rw.x - pl[0]) + pl[4] * (rw.y - pl[1]) + pl[5] * (rw.z - pl[2]);
+        if (x < solid_cutoff) {
+            const double x3 = x * x * x, V_ = solid_eps / (9.0 * (x3 * x3 * x3));
+            const double mdV = 9.0 * V_ / x;   // -dV/dx
+            o.vs += V_;
+            o.fx += mdV * pl[3]; o.fy += mdV * pl[4]; o.fz += mdV * pl[5];
+        }
+    }
+    for (int w = 0; w < n_ljw; ++w) {
+        // eval_lj_attr_wall_forces::loop (walls/lj_attr.cpp:5-43)
+        const double *pl = wall + 6 * (XMD_MAX_WALLS + w);
+        LjWallState st = ljw[(size_t)w * N];
+        if (st.status == 0) {
+            const double x = pl[3] * (rw.x - pl[0]) + pl[4] * (rw.y - pl[1]) + pl[5] * (rw.z - pl[2]);
+            if (step && fabs(x) < min_dist) {
+                st.status = 1;
+                st.jx = rw.x - pl[3] * x; st.jy = rw.y - pl[4] * x; st.jz = rw.z - pl[5] * x;
+                st.ref_t = tt;
+                ljw[(size_t)w * N] = st;
+            }
+        } else {
+            double sat = fmin(tt - st.ref_t, cycle) * cycle_inv;
+            if (st.status == 2) sat = 1.0 - sat;
+            const V3<double> r12{st.jx - rw.x, st.jy - rw.y, st.jz - rw.z};
+            const double r12_rn = 1.0 / norm(r12);
+            double V_, dV;
+            lj_eval<double>(depth, min_dist, r12_rn, &V_, &dV);
+            o.vl += V_ * sat;
+            const double f = sat * dV;
+            o.fx += f * (r12_rn * r12.x); o.fy += f * (r12_rn * r12.y); o.fz += f * (r12_rn * r12.z);
+            if (step) {
+                if (st.status == 1 && sat == 1.0) {
+                    if (factor * min_dist * r12_rn < 1.0) { st.status = 2; st.ref_t = tt; }
+                } else if (st.status == 2 && sat == 0.0) {
+                    st.status = 0;
+                }
+                ljw[(size_t)w * N] = st;
+            }
+        }
+    }
+    return o;
+}
+
+// External forces of the step, one thread per bead, before the step kernel
+// (contexts with AFM tips or walls only): the AFM pulls and the wall forces
+// at the step's positions, into fext; MODE 0 adds their energies, MODE 1
+// advances the LJ attractive wall pairs.  Kept out of the step kernel, whose
+// registers they would raise for every context.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_ext(Dev d, TermP p, int cur) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.N) return;
+    double *fo = d.fext + 3 * (size_t)i;
+    fo[0] = fo[1] = fo[2] = 0.0;
+    const int r = d.rep_of[i];
+    if (r < 0) return;
+    if (MODE == 1 && d.rep[r].steps_left == 0) return;
+    const double4_32a pi = d.pos[cur][i];
+    const double tt = d.rep[r].t;
+    V3<double> f{0.0, 0.0, 0.0};
+    if (d.rep[r].afm) {
+        const uint32_t fl_i = d.bflags[i];
+        if (fl_i & BF_AFM) {
+            const AfmTip tp = d.afm[fl_i >> BF_AFM_SHIFT];
+            if (tp.has_vel && p.on[XMD_TERM_VEL_AFM]) {
+                // eval_velocity_afm_forces::iter (velocity_afm.cpp): a
+                // harmonic(H1, H2, 0) spring to the tip at orig + t vel
+                const V3<double> ra{tp.ox + tt * tp.vx - pi.x, tp.oy + tt * tp.vy - pi.y, tp.oz + tt * tp.vz - pi.z};
+                const double rn = norm(ra), rrn = 1.0 / rn;
+                const double dr2 = rn * rn;
+                double dV = rn * (p.vel_afm_H1 + 2.0 * p.vel_afm_H2 * dr2);
+                dV = clampv<double>(dV, -1.0e3, 1.0e3);
+                // the spring at rest pulls nothing (0 * inf in the shipped code)
+                if (rn > 0.0) f = f + dV * (rrn * ra);
+            }
+            if (p.on[XMD_TERM_FORCE_AFM]) f = f + V3<double>{tp.fx, tp.fy, tp.fz};
+        }
+    }
+    if (p.n_solid | p.n_ljw) {
+        // walls act on the position wrapped into the box (box::wrap)
+        const BoxD bx = d.rep[r].box;
+        V3<double> rw{pi.x, pi.y, pi.z};
+        rw.x -= bx.cell[0] * rint(rw.x * bx.cell_inv[0]);
+        rw.y -= bx.cell[1] * rint(rw.y * bx.cell_inv[1]);
+        rw.z -= bx.cell[2] * rint(rw.z * bx.cell_inv[2]);
+        const WallOut wo = wall_forces(d.wall, d.ljw + i, (size_t)d.N, rw, tt, MODE == 1, p.n_solid, p.n_ljw,
+                                       p.solid_eps, p.solid_cutoff, p.ljw_min_dist, p.ljw_factor, p.ljw_cycle,
+                                       p.ljw_cycle_inv, p.ljw_depth);
+        f = f + V3<double>{wo.fx, wo.fy, wo.fz};
+        if (MODE == 0) {
+            if (p.n_solid) atomicAdd(&d.Vrep[r * XMD_NUM_TERMS + XMD_TERM_SOLID_WALL], wo.vs);
+            if (p.n_ljw) atomicAdd(&d.Vrep[r * XMD_NUM_TERMS + XMD_TERM_LJ_WALL], wo.vl);
+        }
+    }
+    fo[0] = f.x; fo[1] = f.y; fo[2] = f.z;
+}
+
 template <class FT, int MODE, int FBT>
 __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cur) {
     const double4_32a *__restrict__ pin = d.pos[cur];
@@ -440,24 +550,9 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
     }
 
     V3<double> ftot = acc.total();
-    if (d.rep[r].afm) {
-        const uint32_t fl_i = d.bflags[i];
-        if (fl_i & BF_AFM) {
-            const AfmTip tp = d.afm[fl_i >> BF_AFM_SHIFT];
-            if (tp.has_vel && p.on[XMD_TERM_VEL_AFM]) {
-                // eval_velocity_afm_forces::iter (velocity_afm.cpp): a
-                // harmonic(H1, H2, 0) spring to the tip at orig + t vel
-                const double tt = d.rep[r].t;
-                const V3<double> ra{tp.ox + tt * tp.vx - pi.x, tp.oy + tt * tp.vy - pi.y, tp.oz + tt * tp.vz - pi.z};
-                const double rn = norm(ra), rrn = 1.0 / rn;
-                const double dr2 = rn * rn;
-                double dV = rn * (p.vel_afm_H1 + 2.0 * p.vel_afm_H2 * dr2);
-                dV = clampv<double>(dV, -1.0e3, 1.0e3);
-                // the spring at rest pulls nothing (0 * inf in the shipped code)
-                if (rn > 0.0) ftot = ftot + dV * (rrn * ra);
-            }
-            if (p.on[XMD_TERM_FORCE_AFM]) ftot = ftot + V3<double>{tp.fx, tp.fy, tp.fz};
-        }
+    if (p.ext_on) {
+        // AFM pulls and walls, from k_ext (launched just before)
+        ftot = ftot + V3<double>{d.fext[3 * (size_t)i], d.fext[3 * (size_t)i + 1], d.fext[3 * (size_t)i + 2]};
     }
     const double fx = ftot.x, fy = ftot.y, fz = ftot.z;
     if (!(finite_bits(fx) && finite_bits(fy) && finite_bits(fz))) {
@@ -1441,6 +1536,10 @@ static void *force_kernel(bool mixed, int mode, int fb) {
 }
 
 void Engine::launch_force(int mode, int c) {
+    if (tp.ext_on) {
+        if (mode == 0) k_ext<0><<<(d.N + 255) / 256, 256, 0, stream>>>(d, tp, c);
+        else k_ext<1><<<(d.N + 255) / 256, 256, 0, stream>>>(d, tp, c);
+    }
     const int nb = (d.N + tune.fb - 1) / tune.fb;
     cudaGraphConditionalHandle none = 0;
     int fuse = 0;
@@ -1764,6 +1863,20 @@ void Engine::set_force_afm(int rep, int n, const int32_t *bead, const double *F)
     r.fafm_i.assign(bead, bead + n);
     r.fafm_F.assign(F, F + 3 * n);
 }
+void Engine::set_walls(int kind, int n, const double *origin, const double *normal) {
+    if (kind != 0 && kind != 1) throw std::invalid_argument("wall kind must be 0 (solid) or 1 (LJ attractive)");
+    if (n < 0 || n > XMD_MAX_WALLS) throw std::invalid_argument("at most XMD_MAX_WALLS planes per wall kind");
+    if (finalized) throw std::invalid_argument("walls are set before the first replica is placed");
+    std::vector<double> w;
+    for (int k = 0; k < n; ++k) {
+        for (int a = 0; a < 3; ++a)
+            if (!std::isfinite(origin[3 * k + a]) || !std::isfinite(normal[3 * k + a]))
+                throw std::invalid_argument("non-finite wall plane");
+        for (int a = 0; a < 3; ++a) w.push_back(origin[3 * k + a]);
+        for (int a = 0; a < 3; ++a) w.push_back(normal[3 * k + a]);
+    }
+    walls[kind] = w;
+}
 // beads of replica r pulled by some AFM tip, in order
 static std::vector<int> afm_beads(const RepHost &r) {
     std::vector<int> v(r.vafm_i.begin(), r.vafm_i.end());
@@ -1905,6 +2018,17 @@ void Engine::allocate() {
         d.chir = (double2 *)dalloc(sizeof(double2) * N);
         d.chir_f32 = (float2 *)dalloc(sizeof(float2) * N);
         d.afm = (AfmTip *)dalloc(sizeof(AfmTip) * (size_t)std::max(1, cap.afm));
+        // wall planes, and the state of every (bead, LJ attractive wall) pair
+        double wt[2 * XMD_MAX_WALLS * 6] = {0};
+        for (int kind = 0; kind < 2; ++kind)
+            for (size_t q = 0; q < walls[kind].size(); ++q) wt[kind * XMD_MAX_WALLS * 6 + q] = walls[kind][q];
+        d.wall = (double *)dalloc(sizeof(wt));
+        CK(cudaMemcpyAsync(d.wall, wt, sizeof(wt), cudaMemcpyHostToDevice, stream));
+        const size_t nlj = walls[1].size() / 6;
+        d.fext = (double *)dalloc(sizeof(double) * 3 * N);
+        d.ljw = (LjWallState *)dalloc(sizeof(LjWallState) * std::max<size_t>(1, nlj * N));
+        CK(cudaMemsetAsync(d.ljw, 0, sizeof(LjWallState) * std::max<size_t>(1, nlj * N), stream));
+        CK(cudaStreamSynchronize(stream));
     }
     {
         // heuristic coefficient tables: constants of the context
@@ -2010,6 +2134,17 @@ void Engine::allocate() {
     tp.nat_ss_dist = p.nat_ss_dist;
     tp.vel_afm_H1 = p.vel_afm_H1;
     tp.vel_afm_H2 = p.vel_afm_H2;
+    tp.ext_on = (cap.afm > 0 && (p.on[XMD_TERM_VEL_AFM] || p.on[XMD_TERM_FORCE_AFM])) ||
+                (p.on[XMD_TERM_SOLID_WALL] && !walls[0].empty()) || (p.on[XMD_TERM_LJ_WALL] && !walls[1].empty());
+    tp.n_solid = p.on[XMD_TERM_SOLID_WALL] ? (int)walls[0].size() / 6 : 0;
+    tp.n_ljw = p.on[XMD_TERM_LJ_WALL] ? (int)walls[1].size() / 6 : 0;
+    tp.solid_eps = p.solid_wall_depth;
+    tp.solid_cutoff = p.solid_wall_cutoff;
+    tp.ljw_min_dist = p.lj_wall_min_dist;
+    tp.ljw_factor = p.lj_wall_breaking_factor * std::pow(2.0, -1.0 / 6.0);   // main.cpp:842
+    tp.ljw_cycle = p.lj_wall_phase_duration;
+    tp.ljw_cycle_inv = 1.0 / p.lj_wall_phase_duration;
+    tp.ljw_depth = p.lj_wall_depth;
     tp.f = TermP::F32{(float)tp.tether_H1, (float)tp.tether_H2, (float)tp.nat_ang_k, (float)tp.cnd_CDA,
                       (float)tp.cnd_CDB, (float)tp.snd_CDH, (float)tp.go_depth, (float)tp.pauli_r_excl,
                       (float)tp.pauli_depth, (float)tp.es_Vf, (float)tp.es_sdi, (float)tp.chir_e_chi,
@@ -2512,6 +2647,7 @@ size_t Engine::snapshot_io(int rep, unsigned char *buf, size_t bytes, bool save)
     hd.nat_off = h.nat_off; hd.nat_len = h.nat_len; hd.ss_off = h.ss_off; hd.ss_len = h.ss_len;
     hd.qa_on = d.qa_on; hd.fp_off = h.fp_off; hd.fp_len = h.fp_len; hd.ct_off = h.ct_off; hd.ct_len = h.ct_len;
     hd.topo = topo_hash(rep);
+    hd.pad_ = (int32_t)(walls[1].size() / 6);   // LJ attractive walls (their pair states are saved)
     size_t off = 0;
     auto host = [&](void *p, size_t nb) {
         if (buf && off + nb <= bytes) {
@@ -2561,6 +2697,7 @@ size_t Engine::snapshot_io(int rep, unsigned char *buf, size_t bytes, bool save)
     rows(d.nl_row, sizeof(int32_t), cap);
     dev(d.nat_on + h.nat_off, h.nat_len);
     dev(d.ss_on + h.ss_off, h.ss_len);
+    for (int w = 0; w < hd.pad_; ++w) dev(d.ljw + (size_t)w * N + b, sizeof(LjWallState) * n);
     if (d.qa_on) {
         rows(d.qa.sync, sizeof(int32_t), 1);
         rows(d.qa.ref_cnt, sizeof(int32_t), 1);
@@ -2842,6 +2979,18 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
         kf.blockDim = dim3(tune.fb);
         kf.kernelParams = fargs;
         cudaGraphNode_t nf, nc, ncond;
+        if (tp.ext_on) {
+            // the step's external forces first (AFM, walls)
+            cudaKernelNodeParams ke{};
+            void *eargs[] = {&d, &tp, &c};
+            ke.func = (void *)k_ext<1>;
+            ke.gridDim = dim3((d.N + 255) / 256);
+            ke.blockDim = dim3(256);
+            ke.kernelParams = eargs;
+            cudaGraphNode_t ne;
+            CK(cudaGraphAddKernelNode(&ne, g, prev ? &prev : nullptr, prev ? 1 : 0, &ke));
+            prev = ne;
+        }
         CK(cudaGraphAddKernelNode(&nf, g, prev ? &prev : nullptr, prev ? 1 : 0, &kf));
         if (d.qa_on) {
             cudaKernelNodeParams ks{}, kq{};

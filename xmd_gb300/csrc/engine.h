@@ -27,6 +27,13 @@ enum : uint32_t {
 constexpr int BF_HANG_SHIFT = 8, BF_HDIH_SHIFT = 12, BF_AFM_SHIFT = 17;
 constexpr int AFM_MAX_TIPS = 1 << 15;
 
+// one (bead, LJ attractive wall) pair: lj_attr_pair{status, joint_r, ref_t}
+// (walls/lj_attr.h); status 0 = free, 1 = forming or formed, 2 = breaking
+struct LjWallState {
+    double jx, jy, jz, ref_t;
+    int status, pad_;
+};
+
 // the AFM tips on one bead: a velocity tip (vel_afm_tip{res_idx, afm_orig,
 // afm_vel}, velocity_afm.h) and the sum of its force tips
 // (force_afm_tip{res_idx, pull_force}, force_afm.h)
@@ -124,6 +131,9 @@ struct Dev {
     const double *heur_dih;     // [9][6] heuristic dihedral coefficients c0..c5
     const float *heur_dih_f;    // the same in FP32 (mixed path)
     AfmTip *afm;            // AFM tips, one slot per pulled bead
+    double *wall;           // [2][XMD_MAX_WALLS][6] planes (origin, normal): solid, then LJ attractive
+    LjWallState *ljw;       // [n_ljw][N] LJ attractive wall pairs
+    double *fext;           // [3N] external force of the step (k_ext: AFM, walls)
     int32_t *ss_start, *ss_end, *ss_j;   // native disulfide partners per bead (CSR, both directions)
     uint8_t *ss_on;         // in the list of the last rebuild (update_nat_ssbonds, native_ss.cpp:8-19)
     float4 *bond_f;         // (r0, theta0, phi0) in FP32 for the mixed path
@@ -279,6 +289,8 @@ public:
     void set_heuristic_angles(int rep, int n, const int32_t *i1, const int32_t *i2, const int32_t *i3);
     void set_velocity_afm(int rep, int n, const int32_t *bead, const double *orig, const double *vel);
     void set_force_afm(int rep, int n, const int32_t *bead, const double *F);
+    void set_walls(int kind, int n, const double *origin, const double *normal);
+    std::vector<double> walls[2];           // planes (origin, normal) per kind
     void set_heuristic_dihedrals(int rep, int n, const int32_t *i1, const int32_t *i2, const int32_t *i3,
                                  const int32_t *i4);
     void set_state(int rep, const double *r, const double *v);

@@ -28,6 +28,10 @@ struct TermP {
     double chir_e_chi;                       // chirality (chiral.h)
     double nat_ss_H1, nat_ss_dist;           // native ssbonds (native_ss.h: H1, nat_r)
     double vel_afm_H1, vel_afm_H2;           // velocity AFM spring (velocity_afm.h)
+    int ext_on;                              // AFM tips or walls: k_ext runs before the step kernel
+    int n_solid, n_ljw;                      // wall planes of each kind (0 when the term is off)
+    double solid_eps, solid_cutoff;          // walls/solid.h
+    double ljw_min_dist, ljw_factor, ljw_cycle, ljw_cycle_inv, ljw_depth;   // walls/lj_attr.h
     // FP32 copies of the constants the mixed path's FP32 terms use (no
     // FP64-to-FP32 conversion per interaction)
     struct F32 {

@@ -95,6 +95,13 @@ class Engine:
         self.sizes[r] = s.n
         return r
 
+    def set_walls(self, kind: int, origin, normal):
+        """Wall planes of one kind (0 solid, 1 LJ attractive), before the
+        first step or evaluation."""
+        o = np.ascontiguousarray(origin, dtype=np.float64).reshape(-1)
+        n = np.ascontiguousarray(normal, dtype=np.float64).reshape(-1)
+        check(self.lib.xmd_gpu_set_walls(self.h, int(kind), len(o) // 3, dptr(o), dptr(n)))
+
     def eval_forces(self, rep: int = 0):
         n = self.sizes[rep]
         F = np.zeros(3 * n)
