@@ -66,7 +66,8 @@ enum {
     XMD_TERM_FORCE_AFM = 14,/* eval_force_afm_forces src/forces/force_afm.cpp (no energy)       */
     XMD_TERM_SOLID_WALL = 15,  /* eval_solid_wall_forces src/forces/walls/solid.cpp:12-27      */
     XMD_TERM_LJ_WALL = 16,     /* eval_lj_attr_wall_forces src/forces/walls/lj_attr.cpp:5-43    */
-    XMD_NUM_TERMS = 17
+    XMD_TERM_PID = 17,         /* pid::eval_pid_forces src/forces/pid/eval_forces.cpp:14-141      */
+    XMD_NUM_TERMS = 18
 };
 
 #define XMD_MAX_WALLS 8   /* planes per wall kind */
@@ -148,6 +149,11 @@ typedef struct xmd_params {
        cycle_time = phase duration; lj_depth = `depth`, which the shipped
        params never read) */
     double lj_wall_min_dist, lj_wall_breaking_factor, lj_wall_phase_duration, lj_wall_depth;
+    /* pseudo-improper dihedral potential (pid/eval_forces.h, lambda.h):
+       lambda version 0 = cosine, 1 = algebraic; bb+ / bb- (alpha, psi_0,
+       r_min, depth) and ss (alpha, psi_0) */
+    int32_t pid_lambda;
+    double pid_bbp[4], pid_bbm[4], pid_ss[2];
 } xmd_params;
 
 enum { XMD_NL_BUILD_AUTO = 0, XMD_NL_BUILD_CELL = 1, XMD_NL_BUILD_TILE = 2 };

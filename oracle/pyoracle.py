@@ -157,6 +157,16 @@ class Oracle:
         self.fn("eval_forces")(self.h, F.ctypes.data_as(_pd), V.ctypes.data_as(_pd))
         return F.reshape(self.n, 3), V
 
+    def eval_at(self, r):
+        """Forces and energies at positions r with the current lists (port only)."""
+        from xmd_gb300.abi import NUM_TERMS
+        fn = self.lib.xo_eval_at
+        fn.restype, fn.argtypes = C.c_int, [C.c_void_p, _pd, _pd, _pd]
+        rr = np.ascontiguousarray(r, dtype=np.float64).reshape(-1)
+        F, V = np.zeros(3 * self.n), np.zeros(NUM_TERMS)
+        fn(self.h, rr.ctypes.data_as(_pd), F.ctypes.data_as(_pd), V.ctypes.data_as(_pd))
+        return F.reshape(self.n, 3), V
+
     def step(self, nsteps: int):
         self.fn("step")(self.h, int(nsteps))
 

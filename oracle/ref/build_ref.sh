@@ -43,7 +43,8 @@ TUS=(forces/tether forces/go forces/primitives/lj forces/primitives/sink_lj
      forces/es/es_pair forces/qa/precompute_nh forces/qa/sift_candidates
      forces/qa/process_candidates forces/qa/process_contacts forces/qa/free_pair
      dynamics/lang_pc nl/verify forces/chiral forces/native_ss forces/angle/heurestic
-     forces/dihedral/heurestic model/model forces/velocity_afm forces/force_afm forces/walls/solid forces/walls/lj_attr)
+     forces/dihedral/heurestic model/model forces/velocity_afm forces/force_afm forces/walls/solid forces/walls/lj_attr
+     forces/pid/eval_forces forces/pid/bundle)
 OBJS=()
 pids=()
 for tu in "${TUS[@]}"; do

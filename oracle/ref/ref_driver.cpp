@@ -36,6 +36,8 @@
 #include <xmd/forces/force_afm.h>
 #include <xmd/forces/walls/solid.h>
 #include <xmd/forces/walls/lj_attr.h>
+#include <xmd/forces/pid/eval_forces.h>
+#include <xmd/forces/pid/bundle.h>
 #include <xmd/forces/dihedral/heurestic.h>
 #include <xmd/forces/pauli.h>
 #include <xmd/forces/es/const.h>
@@ -93,6 +95,9 @@ struct xr_sys {
     ::vector<plane> walls[2];
     ::vector<vec3r> wall_F[2];
     ::vector<lj_attr_pair> ljw_pairs;
+    ::vector<pid::pid_bundle> pid_bundles;
+    ::vector<sink_lj> ss_plain;          // lj_variants::ss, unshifted (PID's ss_ljs)
+    real pid_cut = 0;
     ::vector<nat_ss> all_ss, cur_ss;
     std::vector<std::pair<int, int>> ss_sorted;
 
@@ -139,6 +144,13 @@ void derive(xr_sys *s) {
     for (int k = 0; k < qa::contact_type::NUM_TYPES; ++k) mf = std::max(mf, s->req_min_dist[k]);
     s->max_form = mf;
     if (p.on[XMD_TERM_QA]) mc = std::max(mc, mf);
+    {
+        // PID cutoff: main.cpp:801-810
+        real c = std::max(lj::cutoff((real)p.lj_bb_r_min), lj::cutoff((real)p.lj_bs_r_min));
+        for (int k = 0; k < XMD_NUM_SS; ++k) c = std::max(c, sink_lj::cutoff((real)p.ss_r_max[k]));
+        s->pid_cut = c;
+        if (p.on[XMD_TERM_PID]) mc = std::max(mc, c);
+    }
     if (p.nl_cutoff > 0) mc = p.nl_cutoff;
     s->max_cutoff = mc;
     s->pad = p.nl_skin > 0 ? (real)p.nl_skin : (real)(p.pad_factor * mc);
@@ -201,6 +213,15 @@ void rebuild_lists(xr_sys *s) {
         up();
     } else {
         s->pauli_pairs.clear();
+    }
+    if (p.on[XMD_TERM_PID]) {
+        pid::update_pid_bundles ub;
+        ub.cutoff = s->pid_cut;
+        ub.r = s->r.data(); ub.prev = s->prev.data(); ub.next = s->next.data(); ub.atype = s->atype.data();
+        ub.box = &s->bx; ub.nl = &s->nl; ub.bundles = &s->pid_bundles;
+        ub();
+    } else {
+        s->pid_bundles.clear();
     }
     if (p.on[XMD_TERM_NAT_SS]) {
         update_nat_ssbonds us;
@@ -387,6 +408,29 @@ void term_forces(xr_sys *s, ::vector<vec3r> &F, real *V) {
     if (p.on[XMD_TERM_FORCE_AFM]) {
         eval_force_afm_forces e;
         e.F = F.data(); e.afm_tips = s->fafm.view();
+        e();
+    }
+    if (p.on[XMD_TERM_PID]) {
+        // the shipped kernel leaves dpsi2_* unset (eval_forces.cpp:64-98),
+        // so its forces are not compared; its energy is
+        pid::eval_pid_forces e;
+        auto lv = p.pid_lambda == 1 ? pid::lambda_version::ALGEBRAIC : pid::lambda_version::COSINE;
+        e.bb_plus_lam.version() = lv; e.bb_minus_lam.version() = lv; e.ss_lam.version() = lv;
+        e.bb_plus_lam.alpha() = p.pid_bbp[0]; e.bb_plus_lam.psi_0() = p.pid_bbp[1];
+        e.bb_plus_lj.r_min() = p.pid_bbp[2]; e.bb_plus_lj.depth() = p.pid_bbp[3];
+        e.bb_minus_lam.alpha() = p.pid_bbm[0]; e.bb_minus_lam.psi_0() = p.pid_bbm[1];
+        e.bb_minus_lj.r_min() = p.pid_bbm[2]; e.bb_minus_lj.depth() = p.pid_bbm[3];
+        e.ss_lam.alpha() = p.pid_ss[0]; e.ss_lam.psi_0() = p.pid_ss[1];
+        s->ss_plain.clear();
+        for (int k = 0; k < XMD_NUM_SS; ++k) {
+            real r_max = p.ss_r_max[k];
+            real r_min = p.ss_sinking ? (real)p.lj_bb_r_min : r_max;
+            s->ss_plain.emplace_back((real)p.ss_depth[k], r_min, r_max);
+        }
+        e.ss_ljs = s->ss_plain.data();
+        ::vector<vec3r> Fd(s->n, vec3r(0, 0, 0));
+        e.r = s->r.data(); e.F = Fd.data(); e.box = &s->bx; e.bundles = &s->pid_bundles;
+        e.prev = s->prev.data(); e.next = s->next.data(); e.V = &V[XMD_TERM_PID];
         e();
     }
     if (p.on[XMD_TERM_SOLID_WALL]) {

@@ -129,6 +129,8 @@ struct xo_sys {
     int32_t n_fafm; int32_t *fafm_i; double *fafm_F;            /* force_afm_tip (force_afm.h) */
     int32_t n_wall[2]; double wall[2][XMD_MAX_WALLS][6];       /* planes (origin, normal): solid, LJ attractive */
     int8_t *ljw_status; double *ljw_joint, *ljw_ref;           /* lj_attr_pair per (wall, bead) */
+    double pid_cut;                                            /* update_pid_bundles::cutoff */
+    pair_i *pid; int64_t n_pid, cap_pid;                       /* pid_bundle{i1, i2} (type from atype) */
     /* state */
     double *r, *v, *y[6], *F;
     double t, true_t;
@@ -204,6 +206,14 @@ static void derive_cutoffs(xo_sys *s) {
     for (int t = 0; t < 4 + XMD_NUM_SS; ++t) mf = fmax(mf, s->req_min_dist[t]);
     s->max_form = mf;                                              /* [D5] */
     if (p->on[XMD_TERM_QA]) mc = fmax(mc, mf);
+    /* PID: the largest LJ-variant cutoff (lj::cutoff = 2 r_min, sink_lj::cutoff
+       = 2 r_max), main.cpp:801-810 */
+    {
+        double c = fmax(2.0 * p->lj_bb_r_min, 2.0 * p->lj_bs_r_min);
+        for (int k = 0; k < XMD_NUM_SS; ++k) c = fmax(c, 2.0 * p->ss_r_max[k]);
+        s->pid_cut = c;
+        if (p->on[XMD_TERM_PID]) mc = fmax(mc, c);
+    }
     if (p->nl_cutoff > 0.0) mc = p->nl_cutoff;
     s->max_cutoff = mc;
     /* legacy_update.cpp:7-8 */
@@ -271,6 +281,7 @@ void xo_destroy(xo_sys *s) {
     free(s->hang_i); free(s->hang_t); free(s->hdih_i); free(s->hdih_t);
     free(s->vafm_i); free(s->vafm_o); free(s->vafm_v); free(s->fafm_i); free(s->fafm_F);
     free(s->ljw_status); free(s->ljw_joint); free(s->ljw_ref);
+    free(s->pid);
     free(s->r); free(s->v); free(s->F);
     for (int k = 0; k < 6; ++k) free(s->y[k]);
     free(s->orig_r); free(s->nl); free(s->go); free(s->pauli); free(s->es);
@@ -705,6 +716,22 @@ static void nl_rebuild(xo_sys *s) {
                 s->pauli[s->n_pauli].i1 = i1;
                 s->pauli[s->n_pauli].i2 = i2;
                 s->n_pauli++;
+            }
+        }
+    }
+    /* update_pid_bundles: pid/bundle.cpp:6-27 (beads with both chain
+       neighbours, r < cutoff + pad at the rebuild) */
+    s->n_pid = 0;
+    if (p->on[XMD_TERM_PID]) {
+        double min_norm_inv = 1.0 / (s->pid_cut + s->orig_pad);
+        for (int64_t k = 0; k < s->n_nl; ++k) {
+            int i1 = s->nl[k].i1, i2 = s->nl[k].i2;
+            if (ninv(r_uv(s, ld(s->r, i1), ld(s->r, i2))) > min_norm_inv) {
+                if (s->prev[i1] < 0 || s->next[i1] < 0 || s->prev[i2] < 0 || s->next[i2] < 0) continue;
+                GROW(s->pid, s->n_pid, s->cap_pid, pair_i);
+                s->pid[s->n_pid].i1 = i1;
+                s->pid[s->n_pid].i2 = i2;
+                s->n_pid++;
             }
         }
     }
@@ -1236,6 +1263,105 @@ static void lj_wall_phase(xo_sys *s) {
         for (int i = 0; i < s->n; ++i) lj_wall_transition(s, w, i);
 }
 
+/* pid::lambda_func (pid/lambda.h:29-56): support and (value, derivative) */
+static int pid_supp(double alpha, double psi0, double psi) { return fabs(alpha * (psi - psi0)) < M_PI; }
+static void pid_lam(int version, double alpha, double psi0, double psi, double *val, double *deriv) {
+    double sv = alpha * (psi - psi0);
+    if (version == 0) {
+        *val = 0.5 * cos(sv) + 0.5;
+        *deriv = -0.5 * alpha * sin(sv);
+    } else {
+        double t = fabs(sv / M_PI);
+        double x_inv = 1.0 / (2.0 * t * t - 2.0 * t - 1);
+        *val = (t * t - 2.0 * t + 1.0) * x_inv;
+        /* d val / d psi = 2 (t - 1)(t - 2) / den^2 * alpha / pi (the shipped
+           line 47 has 2 t (t - 1) and no alpha) [D23] */
+        *deriv = (2.0 * (t - 1.0) * (t - 2.0)) * x_inv * x_inv * alpha / M_PI;
+        *deriv *= (sv < 0.0 ? -1.0 : 1.0);
+    }
+}
+/* One side of eval_pid_forces::iter (eval_forces.cpp:27-62): the
+   pseudo-improper dihedral psi of (r1_, r2_, r3_; r4_) and its derivatives
+   along the four beads */
+static double pid_psi(const xo_sys *s, v3 r1_, v3 r2_, v3 r3_, v3 r4_, v3 *d1, v3 *d2, v3 *d3, v3 *d4) {
+    v3 r24 = r_uv(s, r2_, r4_);
+    v3 r12 = sub(r2_, r1_), r23 = sub(r3_, r2_), r13 = sub(r3_, r1_);
+    v3 r14 = add(r12, r24);
+    v3 rij = neg(r23), rkj = neg(r13), rkl = neg(r14);
+    v3 rm = cross(r23, r12), rn = cross(r13, r14);
+    double rm_rn = ninv(rm), rn_rn = ninv(rn), rkj_n = nrm(rkj);
+    /* atoms i = r2_, j = r3_, k = r1_, l = r4_ of rij = ri - rj, rkj, rkl;
+       the dihedral's gradient (Bekker): dpsi/dri = |rkj| m / |m|^2,
+       dpsi/drl = -|rkj| n / |n|^2, and j, k from them [D23] */
+    v3 gi = scl(rkj_n * rm_rn * rm_rn, rm);
+    v3 gl = neg(scl(rkj_n * rn_rn * rn_rn, rn));
+    double a = dot(rij, rkj) / (rkj_n * rkj_n), b = dot(rkl, rkj) / (rkj_n * rkj_n);
+    v3 gj = sub(scl(a - 1.0, gi), scl(b, gl));
+    v3 gk = sub(scl(b - 1.0, gl), scl(a, gi));
+    *d1 = gk;      /* r1_: previous bead */
+    *d2 = gi;      /* r2_: the bead */
+    *d3 = gj;      /* r3_: next bead */
+    *d4 = gl;      /* r4_: the partner */
+    double psi = acos(dot(rm, rn) * rm_rn * rn_rn);
+    if (dot(rij, rn) < 0.0) psi = -psi;
+    return psi;
+}
+/* eval_pid_forces::iter (eval_forces.cpp:14-141) with the forces the
+   energy's gradient [D23]: the shipped lines 64-98 write the second side's
+   derivatives into dpsi1_* (dpsi2_* stay unset), and each side's derivatives
+   go to the wrong beads with 1/|m|, 1/|n| for 1/|m|^2, 1/|n|^2; the pair
+   part's sign is that of the Go term (F1 = +dV/dr r12_u, go.cpp:42-44),
+   where the shipped lines 136-139 subtract it */
+static void pid_iter(const xo_sys *s, int64_t idx, double *F, double *V) {
+    const xmd_params *p = &s->p;
+    int i1 = s->pid[idx].i1, i2 = s->pid[idx].i2;
+    int i1p = s->prev[i1], i1n = s->next[i1], i2p = s->prev[i2], i2n = s->next[i2];
+    v3 r1p = ld(s->r, i1p), r1 = ld(s->r, i1), r1n = ld(s->r, i1n);
+    v3 r2p = ld(s->r, i2p), r2 = ld(s->r, i2), r2n = ld(s->r, i2n);
+    v3 a1p, a1, a1n, a2, b2p, b2, b2n, b1;
+    double psi1 = pid_psi(s, r1p, r1, r1n, r2, &a1p, &a1, &a1n, &a2);
+    double psi2 = pid_psi(s, r2p, r2, r2n, r1, &b2p, &b2, &b2n, &b1);
+    v3 r12 = r_uv(s, r1, r2);
+    double r12_n = nrm(r12), r12_rn = 1.0 / r12_n;
+    double A = 0.0, B = 0.0, C = 0.0, V_ = 0.0;
+    const double *bb[2] = {p->pid_bbp, p->pid_bbm};
+    for (int k = 0; k < 2; ++k) {
+        const double *q = bb[k];
+        if (pid_supp(q[0], q[1], psi1) && pid_supp(q[0], q[1], psi2)) {
+            double lam1, d1, lam2, d2, lV, ldV;
+            pid_lam(p->pid_lambda, q[0], q[1], psi1, &lam1, &d1);
+            pid_lam(p->pid_lambda, q[0], q[1], psi2, &lam2, &d2);
+            lj_eval(q[3], q[2], r12_rn, &lV, &ldV);
+            V_ += lam1 * lam2 * lV;
+            A += d1 * lam2 * lV;
+            B += d2 * lam1 * lV;
+            C += lam1 * lam2 * ldV;
+        }
+    }
+    if (pid_supp(p->pid_ss[0], p->pid_ss[1], psi1) && pid_supp(p->pid_ss[0], p->pid_ss[1], psi2)) {
+        /* ss_ljs[type], type = atype1 * NUM_AA + atype2 (bundle.cpp:20-22) */
+        int ss = (int)s->atype[i1] * XMD_NUM_AA + (int)s->atype[i2];
+        double depth = p->ss_depth[ss], r_max = p->ss_r_max[ss];
+        double r_min = p->ss_sinking ? p->lj_bb_r_min : r_max;
+        double lam1, d1, lam2, d2, lV, ldV;
+        pid_lam(p->pid_lambda, p->pid_ss[0], p->pid_ss[1], psi1, &lam1, &d1);
+        pid_lam(p->pid_lambda, p->pid_ss[0], p->pid_ss[1], psi2, &lam2, &d2);
+        sink_lj_eval(depth, r_min, r_max, r12_n, r12_rn, &lV, &ldV);
+        V_ += lam1 * lam2 * lV;
+        A += d1 * lam2 * lV;
+        B += d2 * lam1 * lV;
+        C += lam1 * lam2 * ldV;
+    }
+    *V += V_;
+    v3 r12_u = scl(r12_rn, r12);
+    dec(F, i1p, scl(A, a1p));
+    dec(F, i1, sub(add(scl(A, a1), scl(B, b1)), scl(C, r12_u)));
+    dec(F, i1n, scl(A, a1n));
+    dec(F, i2p, scl(B, b2p));
+    dec(F, i2, add(add(scl(A, a2), scl(B, b2)), scl(C, r12_u)));
+    dec(F, i2n, scl(B, b2n));
+}
+
 /* eval_force_afm_forces::iter: src/forces/force_afm.cpp */
 static void force_afm_iter(const xo_sys *s, int idx, double *F) {
     acc(F, s->fafm_i[idx], ld(s->fafm_F, idx));
@@ -1294,10 +1420,29 @@ static void pure_forces(const xo_sys *s, double *F, double *V) {
     if (p->on[XMD_TERM_HEUR_DIH]) for (int k = 0; k < s->n_hdih; ++k) heur_dihedral_iter(s, k, F, &V[XMD_TERM_HEUR_DIH]);
     if (p->on[XMD_TERM_VEL_AFM]) for (int k = 0; k < s->n_vafm; ++k) vel_afm_iter(s, k, F);
     if (p->on[XMD_TERM_FORCE_AFM]) for (int k = 0; k < s->n_fafm; ++k) force_afm_iter(s, k, F);
+    if (p->on[XMD_TERM_PID]) for (int64_t k = 0; k < s->n_pid; ++k) pid_iter(s, k, F, &V[XMD_TERM_PID]);
     if (p->on[XMD_TERM_SOLID_WALL]) for (int k = 0; k < s->n; ++k) solid_wall_iter(s, k, F, &V[XMD_TERM_SOLID_WALL]);
     if (p->on[XMD_TERM_LJ_WALL])
         for (int w = 0; w < s->n_wall[1]; ++w)
             for (int k = 0; k < s->n; ++k) lj_wall_force(s, w, k, F, &V[XMD_TERM_LJ_WALL]);
+}
+
+/* Forces at positions r with the current lists (no rebuild); the state is
+   left as it was (a checker of derivatives) */
+int xo_eval_at(xo_sys *s, const double *r, double *F, double *V) {
+    size_t nb = sizeof(double) * 3 * (size_t)s->n;
+    double *keep = (double *)malloc(nb);
+    memcpy(keep, s->r, nb);
+    memcpy(s->r, r, nb);
+    double Vl[XMD_NUM_TERMS];
+    double *Ft = (double *)malloc(nb);
+    pure_forces(s, Ft, Vl);
+    if (F) memcpy(F, Ft, nb);
+    if (V) memcpy(V, Vl, sizeof Vl);
+    memcpy(s->r, keep, nb);
+    free(keep);
+    free(Ft);
+    return 0;
 }
 
 int xo_eval_forces(xo_sys *s, double *F, double *V) {
@@ -1463,6 +1608,10 @@ int xo_step_omp(xo_sys *s, int32_t nsteps, int32_t nthreads) {
             if (p->on[XMD_TERM_FORCE_AFM]) {
 #pragma omp for schedule(static) nowait
                 for (int k = 0; k < s->n_fafm; ++k) force_afm_iter(s, k, F);
+            }
+            if (p->on[XMD_TERM_PID]) {
+#pragma omp for schedule(static) nowait
+                for (int64_t k = 0; k < s->n_pid; ++k) pid_iter(s, k, F, &V[XMD_TERM_PID]);
             }
             if (p->on[XMD_TERM_SOLID_WALL]) {
 #pragma omp for schedule(static) nowait

@@ -33,6 +33,7 @@ int xo_set_chirals(xo_sys *s, int32_t n, const int32_t *i1, const int32_t *i2, c
 int xo_set_ssbonds(xo_sys *s, int32_t n, const int32_t *i1, const int32_t *i2);
 int xo_set_velocity_afm(xo_sys *s, int32_t n, const int32_t *bead, const double *orig, const double *vel);
 int xo_set_force_afm(xo_sys *s, int32_t n, const int32_t *bead, const double *F);
+int xo_eval_at(xo_sys *s, const double *r, double *F, double *V);
 int xo_set_walls(xo_sys *s, int32_t kind, int32_t n, const double *origin, const double *normal);
 int xo_set_heuristic_angles(xo_sys *s, int32_t n, const int32_t *i1, const int32_t *i2, const int32_t *i3);
 int xo_set_heuristic_dihedrals(xo_sys *s, int32_t n, const int32_t *i1, const int32_t *i2, const int32_t *i3,

@@ -15,7 +15,8 @@ ANGSTROM = 0.2
 SECTIONS = ["tether forces", "native angles", "complex native dihedrals", "simple native dihedrals",
             "native contacts", "Pauli exclusion", "const ES", "relative ES", "quasi-adiabatic potential",
             "chirality", "native ssbonds", "heurestic angles", "heurestic dihedrals", "velocity AFM",
-            "force AFM", "solid walls", "LJ attractive walls"]
+            "force AFM", "solid walls", "LJ attractive walls",
+            "pseudo-improper dihedral potential"]
 
 
 def only_term(term: int, y: str) -> str:

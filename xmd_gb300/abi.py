@@ -10,14 +10,15 @@ from pathlib import Path
 
 import numpy as np
 
-NUM_TERMS = 17
+NUM_TERMS = 18
 NUM_AA = 20
 NUM_SS = NUM_AA * NUM_AA
 TERM_NAMES = ["tether", "nat_ang", "cnd", "snd", "go", "pauli", "const_es", "rel_es", "qa",
-              "chir", "nat_ss", "heur_ang", "heur_dih", "vel_afm", "force_afm", "solid_wall", "lj_wall"]
+              "chir", "nat_ss", "heur_ang", "heur_dih", "vel_afm", "force_afm", "solid_wall", "lj_wall",
+              "pid"]
 (TERM_TETHER, TERM_NAT_ANG, TERM_CND, TERM_SND, TERM_GO, TERM_PAULI, TERM_CONST_ES,
  TERM_REL_ES, TERM_QA, TERM_CHIR, TERM_NAT_SS, TERM_HEUR_ANG, TERM_HEUR_DIH,
- TERM_VEL_AFM, TERM_FORCE_AFM, TERM_SOLID_WALL, TERM_LJ_WALL) = range(NUM_TERMS)
+ TERM_VEL_AFM, TERM_FORCE_AFM, TERM_SOLID_WALL, TERM_LJ_WALL, TERM_PID) = range(NUM_TERMS)
 PREC_FP64, PREC_MIXED = 0, 1
 NOALLOC_MAX_BEADS = 65536   # XMD_NOALLOC_MAX_BEADS
 
@@ -57,6 +58,7 @@ class Params(C.Structure):
         ("solid_wall_depth", _d), ("solid_wall_cutoff", _d),
         ("lj_wall_min_dist", _d), ("lj_wall_breaking_factor", _d), ("lj_wall_phase_duration", _d),
         ("lj_wall_depth", _d),
+        ("pid_lambda", _i), ("pid_bbp", _d * 4), ("pid_bbm", _d * 4), ("pid_ss", _d * 2),
     ]
 
     def copy(self) -> "Params":

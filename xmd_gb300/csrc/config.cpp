@@ -568,6 +568,22 @@ void resolve_params(const YNode &root, xmd_params *o) {
     o->vel_afm_H1 = qval(section(root, "velocity AFM"), "H1", "velocity AFM: ");
     o->vel_afm_H2 = qval(section(root, "velocity AFM"), "H2", "velocity AFM: ");
     o->on[XMD_TERM_FORCE_AFM] = enabled(root, "force AFM");
+    {
+        // pid_params (freeform/params.cpp:132-158); an unknown lambda
+        // version is cosine (main.cpp:765-767)
+        const YNode &q = section(root, "pseudo-improper dihedral potential");
+        const std::string w = "pseudo-improper dihedral potential: ";
+        o->on[XMD_TERM_PID] = enabled(root, "pseudo-improper dihedral potential");
+        o->pid_lambda = sval(q, "lambda version", w) == "algebraic" ? 1 : 0;
+        const YNode &bp = need(q, "bb+", w), &bm = need(q, "bb-", w), &ss = need(q, "ss", w);
+        const char *keys[4] = {"alpha", "psi_0", "r_min", "depth"};
+        for (int k = 0; k < 4; ++k) {
+            o->pid_bbp[k] = qval(bp, keys[k], w + "bb+: ");
+            o->pid_bbm[k] = qval(bm, keys[k], w + "bb-: ");
+        }
+        o->pid_ss[0] = qval(ss, "alpha", w + "ss: ");
+        o->pid_ss[1] = qval(ss, "psi_0", w + "ss: ");
+    }
     o->on[XMD_TERM_SOLID_WALL] = enabled(root, "solid walls");
     o->solid_wall_depth = qval(section(root, "solid walls"), "depth", "solid walls: ");
     o->solid_wall_cutoff = qval(section(root, "solid walls"), "cutoff", "solid walls: ");

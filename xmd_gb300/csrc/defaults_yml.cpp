@@ -85,6 +85,23 @@ native ssbonds:
   H1: 100 eps/A**2
   equilibrium dist: 6.0 A
 
+pseudo-improper dihedral potential:
+  enabled: false
+  lambda version: cosine
+  bb+:
+    alpha: 6.4 1/rad
+    psi_0: 1.05 rad
+    r_min: 5.6 A
+    depth: 1 eps
+  bb-:
+    alpha: 6.0 1/rad
+    psi_0: -1.44 rad
+    r_min: 6.2 A
+    depth: 1 eps
+  ss:
+    alpha: 1.2 1/rad
+    psi_0: -0.23 rad
+
 solid walls:
   enabled: false
   depth: 1 eps

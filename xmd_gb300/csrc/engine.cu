@@ -1549,6 +1549,8 @@ void Engine::launch_force(int mode, int c) {
 }
 
 Engine::Engine(const xmd_params &p) : params(p) {
+    if (p.on[XMD_TERM_PID])
+        throw std::invalid_argument("the pseudo-improper dihedral potential has no engine path (CPU oracle only)");
     int ndev = 0;
     CK(cudaGetDeviceCount(&ndev));
     if (ndev < 1) throw std::runtime_error("no CUDA device");
