@@ -5,15 +5,18 @@ Workload (config 4 of the benchmark set): 256 independent single-chain
 systems, lengths log-uniform in [50, 800] beads, Go native contacts +
 Debye-Hueckel + Pauli + tether/angle/dihedral terms, per-replica temperature
 uniform in [0.3, 0.6], all packed into one engine context.  A bench "step" is
---md-steps Langevin predictor-corrector steps over every replica (one chunk
-of graph-captured device work); L2 is flushed (256 MiB device write) before
-each timed step and is excluded from the timing.
+--md-steps Langevin predictor-corrector steps of every replica.  The timed
+window is fixed by the step counts: W warm-up bench steps, then K timed ones,
+so MD steps [W*md, (W+K)*md) of every replica; the rebuild rate in that
+window is reported.  L2 is flushed (256 MiB device write, not timed) before
+each timed step.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
 
 One JSON line on rank 0.  --impl reference times the CPU implementation of
-the same path (the C restatement of the reference's kernels, all host
-threads, one thread per replica group) on the same workload.
+the same path (the C restatement of the reference's FP64 kernels, all host
+threads, one thread per replica group) on the same workload and window; that
+arm loads only the oracle's libraries.
 """
 from __future__ import annotations
 
@@ -35,6 +38,10 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "bead-steps/s mixed+batched vs plain FP64 at ≤1e-5 force err; p99 req latency"
 L2_FLUSH_BYTES = 256 << 20
+# ncu DRAM read + write of one k_force<float,1> launch on this workload (the
+# capture and its command are in profiles/k_force_mixed_c4.md); a committed
+# figure, not measured by this run
+FORCE_TRAFFIC_NCU = 25491200
 
 
 # ---------------------------------------------------------------- helpers --
@@ -48,8 +55,7 @@ def cudart():
             if "libcudart.so" in line:
                 path = line.split()[-1]
                 break
-    lib = C.CDLL(path or "libcudart.so")
-    return lib
+    return C.CDLL(path or "libcudart.so")
 
 
 class Events:
@@ -84,7 +90,7 @@ class Clocks:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
@@ -124,27 +130,6 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def profile_value(key):
-    """A figure of the dominant kernel's committed ncu summary (a line
-    `<key>: <number>`), or None."""
-    p = ROOT / "profiles" / "k_force_mixed_c4.md"
-    if not p.exists():
-        return None
-    for line in p.read_text().splitlines():
-        if line.strip().startswith(key + ":"):
-            try:
-                return float(line.split(":", 1)[1].split()[0])
-            except ValueError:
-                return None
-    return None
-
-
-def profile_traffic():
-    """Per-launch DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum)
-    of the dominant kernel from the committed ncu summary, or None."""
-    return profile_value("traffic_bytes_per_launch")
-
-
 def dist_env():
     return (int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)),
             int(os.environ.get("WORLD_SIZE", 1)))
@@ -171,17 +156,24 @@ def make_workload(rank: int, workers: int):
     return synth.config_c4(seed=4 + 1000 * rank, workers=workers)
 
 
-def pack_history(eng, nrep):
-    hs = [eng.get_history(r)[0] for r in range(nrep)]     # each [6, n, 3]
-    return np.ascontiguousarray(np.concatenate(hs, axis=1).reshape(6, -1))
+def workload_config(nbeads: int, nrep: int, md: int, warmup: int, steps: int) -> dict:
+    """The `config` of both arms (identical for the same arguments)."""
+    return {"workload": f"256 uneven single-chain replicas (log-uniform 50-800 beads, {nbeads} beads), "
+                        "Go+Debye-Hueckel+Pauli+tether/angle/dihedral, per-replica T in [0.3,0.6], "
+                        "seeded synthetic chains from extended starts",
+            "beads_per_gpu": nbeads, "replicas_per_gpu": nrep, "md_steps_per_step": md,
+            "window_md_steps": [warmup * md, (warmup + steps) * md]}
 
 
 # ------------------------------------------------------------ engine arm --
 def run_engine(args, rank, local, world):
     from xmd_gb300 import Engine, abi, synth
     dev = local
-    systems = make_workload(rank, workers=min(16, os.cpu_count() or 1))
+    workers = min(16, os.cpu_count() or 1)
+    systems = make_workload(rank, workers)
     nbeads = sum(s.n for s in systems)
+    nrep = len(systems)
+    md, K, W = args.md_steps, args.steps, args.warmup
     y_mixed = synth.yaml_for("c4", "mixed") + f"  device: {dev}\n"
     y_fp64 = synth.yaml_for("c4", "fp64") + f"  device: {dev}\n"
     eng = Engine(y_mixed)
@@ -194,17 +186,7 @@ def run_engine(args, rank, local, world):
     ev = Events(rt, stream)
     flush = C.c_void_p()
     assert rt.cudaMalloc(C.byref(flush), C.c_size_t(L2_FLUSH_BYTES)) == 0
-
-    def flush_l2():
-        rt.cudaMemsetAsync(flush, 1, C.c_size_t(L2_FLUSH_BYTES), stream)
-
-    def stats():
-        out = np.zeros(abi_n_stats(), dtype=np.int64)
-        abi.check(eng.lib.xmd_gpu_stats(eng.h, out.ctypes.data_as(C.POINTER(C.c_int64))))
-        return out
-
-    def abi_n_stats():
-        return 8
+    pd = C.POINTER(C.c_double)
 
     def barrier():
         eng.synchronize()
@@ -212,234 +194,237 @@ def run_engine(args, rank, local, world):
             import torch.distributed as dist
             dist.barrier()
 
-    md = args.md_steps
     # launch shapes chosen by the autotuner on a clone (not timed; the
     # trajectory does not depend on them)
-    tuned = eng.autotune(md) if args.autotune else None
-    # warm-up (also builds the graphs and the first lists)
-    for _ in range(args.warmup):
+    tuned = eng.autotune(min(md, 96)) if args.autotune else None
+    st_a = eng.stats()
+    for _ in range(W):
         eng.step(md)
     barrier()
-    s0 = stats()
+    st_w = eng.stats()
+    # the state at the window start: snapshots (the end-to-end loop replays
+    # the window from them) and histories (the CPU sample starts there)
+    snaps = [eng.snapshot(r) for r in range(nrep)]
+    hist0 = [eng.get_history(r) for r in range(nrep)]
+    s0 = eng.stats()
     clocks = Clocks(dev)
     clocks.start()
     e0, e1 = ev.new(), ev.new()
     t_ms = 0.0
-    for _ in range(args.steps):
-        flush_l2()
+    for _ in range(K):
+        rt.cudaMemsetAsync(flush, 1, C.c_size_t(L2_FLUSH_BYTES), stream)
         ev.record(e0)
         eng.step(md)
         ev.record(e1)
         t_ms += ev.ms(e0, e1)
     barrier()
     clk = clocks.stop()
-    s1 = stats()
-    launches = int(s1[5] - s0[5])
-    value, t_max, beads_all = job_rate(nbeads, md, args.steps, t_ms, world)
+    s1 = eng.stats()
+    r_end = np.zeros(3 * nbeads)
+    abi.check(eng.lib.xmd_gpu_download_positions_all(eng.h, r_end.ctypes.data_as(pd)))
+    launches = int(s1["launches"] - s0["launches"])
+    value, t_max, beads_all = job_rate(nbeads, md, K, t_ms, world)
+    window = {"md_steps": [W * md, (W + K) * md],
+              "replica_rebuilds_per_md_step": (s1["rebuilds"] - s0["rebuilds"]) / (K * md),
+              "replica_rebuilds_per_md_step_warmup": (st_w["rebuilds"] - st_a["rebuilds"]) / max(1, W * md)}
 
-    # dominant kernel: force+integrate, timed with events around each launch
+    # end to end through the C ABI over the SAME window: restore the
+    # window-start state, then every bench step uploads the whole state from
+    # pinned host memory, runs md steps and reads the whole state back
+    for r in range(nrep):
+        eng.restore(r, snaps[r])
+    ybytes = 18 * 8 * nbeads
+    hbuf = C.c_void_p()
+    assert rt.cudaHostAlloc(C.byref(hbuf), C.c_size_t(ybytes), 0) == 0
+    hy = np.ctypeslib.as_array((C.c_double * (18 * nbeads)).from_address(hbuf.value))
+    abi.check(eng.lib.xmd_gpu_download_history_all(eng.h, hy.ctypes.data_as(pd)))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        abi.check(eng.lib.xmd_gpu_upload_history_all(eng.h, hy.ctypes.data_as(pd)))
+        eng.step(md)
+        abi.check(eng.lib.xmd_gpu_download_history_all(eng.h, hy.ctypes.data_as(pd)))
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = job_rate(nbeads, md, K, 1e3 * e2e_s, world)[0]
+    e2e_same = bool(np.array_equal(hy[:3 * nbeads], r_end))
+
+    # the dominant kernel, timed with events around each launch (per-step
+    # path), continuing from the window's end
     abi.check(eng.lib.xmd_gpu_set_kernel_timing(eng.h, 1))
     eng.step(md)
     fms, nf, rms, nr = C.c_double(), C.c_int64(), C.c_double(), C.c_int64()
     abi.check(eng.lib.xmd_gpu_kernel_times(eng.h, C.byref(fms), C.byref(nf), C.byref(rms), C.byref(nr)))
     abi.check(eng.lib.xmd_gpu_set_kernel_timing(eng.h, 0))
     force_ms = fms.value / max(1, nf.value)
-    st = stats()
-    P = st[2] / 2.0          # unique pairs kept by the pair terms
-    Cg = st[3] / 2.0         # active Go contacts
+    rebuild_ms = rms.value / max(1, nr.value)
+    st = eng.stats()
+    P = st["nl_entries"] / 2.0          # unique pairs kept by the pair terms
+    Cg = st["go_active"] / 2.0          # active Go contacts
     alg_bytes = 325.0 * nbeads + 4.0 * P + 12.0 * Cg     # mixed, per MD step (Q = 0)
     peak, peak_kind = peaks()
     achieved = alg_bytes / (force_ms / 1e3) / 1e9
-    traffic = profile_traffic()
+    eng.close()
 
-    # end-to-end through the C ABI with pinned host buffers: every bench step
-    # uploads the packed history of all replicas, runs md steps, reads back
-    # all positions
-    nrep = len(systems)
-    yh = pack_history(eng, nrep)
-    hbuf = C.c_void_p()
-    assert rt.cudaHostAlloc(C.byref(hbuf), C.c_size_t(yh.nbytes + 24 * nbeads), 0) == 0
-    hy = np.ctypeslib.as_array((C.c_double * yh.size).from_address(hbuf.value))
-    hy[:] = yh.reshape(-1)
-    hr = np.ctypeslib.as_array((C.c_double * (3 * nbeads)).from_address(hbuf.value + yh.nbytes))
-    e2e_steps = max(2, args.steps // 2)
-    pd = C.POINTER(C.c_double)
-    for _ in range(1):
-        abi.check(eng.lib.xmd_gpu_upload_history_all(eng.h, hy.ctypes.data_as(pd)))
-        eng.step(md)
-        abi.check(eng.lib.xmd_gpu_download_positions_all(eng.h, hr.ctypes.data_as(pd)))
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        abi.check(eng.lib.xmd_gpu_upload_history_all(eng.h, hy.ctypes.data_as(pd)))
-        eng.step(md)
-        abi.check(eng.lib.xmd_gpu_download_positions_all(eng.h, hr.ctypes.data_as(pd)))
-    barrier()
-    e2e_s = time.perf_counter() - t0
-    e2e_value = job_rate(nbeads, md, e2e_steps, 1e3 * e2e_s, world)[0]
-
-    # plain FP64 on the same replicas (same protocol), and the mixed force error
+    # plain FP64 on the same replicas, batched, the same protocol and window
     eng64 = Engine(y_fp64)
     for s in systems:
         eng64.add_system(s)
-    tuned64 = eng64.autotune(md) if args.autotune else None   # its own best shape
-    for _ in range(args.warmup):
+    tuned64 = eng64.autotune(min(md, 96)) if args.autotune else None
+    for _ in range(W):
         eng64.step(md)
     eng64.synchronize()
     abi.check(eng64.lib.xmd_gpu_get_stream(eng64.h, C.byref(stream)))
     ev64 = Events(rt, stream)
     t64 = 0.0
-    k64 = max(2, args.steps // 2)
-    for _ in range(k64):
+    for _ in range(K):
         rt.cudaMemsetAsync(flush, 1, C.c_size_t(L2_FLUSH_BYTES), stream)
         ev64.record(e0)
         eng64.step(md)
         ev64.record(e1)
         t64 += ev64.ms(e0, e1)
-    value64 = nbeads * md * k64 / (t64 / 1e3)
+    value64 = nbeads * md * K / (t64 / 1e3)
     eng64.close()
-    plain64 = plain_fp64(systems, y_fp64, md, args.warmup, rt, flush)
-    # force error of the mixed path on identical states (fresh engines at t=0)
+    # mixed force error against FP64 on identical states (every replica at t = 0)
     errs = []
     with Engine(y_mixed) as em, Engine(y_fp64) as ed:
-        for s in systems[:16]:
+        for s in systems:
             em.add_system(s)
             ed.add_system(s)
-        for r in range(16):
+        for r in range(nrep):
             Fm, _ = em.eval_forces(r)
             Fd, _ = ed.eval_forces(r)
             errs.append(float(np.abs(Fm - Fd).max() / max(np.abs(Fd).max(), 1e-300)))
-
-    # serving (config 5): Poisson arrivals offered at ~70% of the batched
-    # mixed throughput, mixed and plain FP64 on the same request stream
-    serving = None
-    if args.serve_requests > 0:
-        from xmd_gb300 import synth as _s
-        reqs = _s.config_c5(count=args.serve_requests, seed=5 + rank, workers=min(16, os.cpu_count() or 1))
-        mean_work = float(np.mean([rq.n for rq in reqs])) * args.serve_steps
-        rate = 0.7 * (value / world) / mean_work
-        serving = {"mixed": serve_bench(reqs, "mixed", args.serve_steps, rate, dev),
-                   "fp64": serve_bench(reqs, "fp64", args.serve_steps, rate, dev)}
-
-    accuracy = accuracy_c3(args.accuracy_steps, args.accuracy_every, dev) \
-        if (rank == 0 and args.accuracy_steps > 0) else None
-    cpu = cpu_baseline(systems, sample_steps=args.cpu_sample_steps) if rank == 0 else None
     rt.cudaFree(flush)
     rt.cudaFreeHost(hbuf)
-    eng.close()
+
+    extras = {}
+    if rank == 0 and args.extras:
+        extras["c2_plain_fp64"] = bench_c2(args, dev, rt)
+        if args.serve_requests > 0:
+            extras["serving"] = serve_section(args, dev, workers)
+        if args.accuracy_steps > 0:
+            extras["mixed_vs_fp64_c3"] = accuracy_c3(args.accuracy_replicas, args.accuracy_steps,
+                                                    args.accuracy_every, dev)
+    cpu = cpu_baseline(systems, hist0, args.cpu_sample_steps) if rank == 0 else None
     if rank != 0:
         return
     out = {
-        "metric": METRIC, "value": value, "unit": "bead-steps/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+        "metric": METRIC, "value": value, "unit": "bead-steps/s", "n_gpus": world, "steps": K,
+        "warmup": W, "ms_per_step": t_max / K, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-        "config": {
-            "workload": f"256 uneven single-chain replicas (log-uniform 50-800 beads, {nbeads} beads), "
-                        "Go+Debye-Hueckel+Pauli+tether/angle/dihedral, per-replica T in [0.3,0.6], "
-                        "mixed precision (FP32 forces, FP64 accumulate/integrate), one context",
-            "md_steps_per_step": md, "beads_per_gpu": nbeads, "replicas_per_gpu": nrep,
-            "l2": "256 MiB device write before each timed step (not timed)",
-            "plain_fp64_value": plain64["value"], "plain_fp64_sample": plain64["sample"],
-            "mixed_over_plain_fp64": value / world / plain64["value"],
+        "config": workload_config(nbeads, nrep, md, W, K),
+        "precision": "mixed: FP32 pair/bond forces, float-float per-bead accumulation, FP64 positions, "
+                     "history, integrator, energies and skin test",
+        "l2": "256 MiB device write before each timed step (not timed)",
+        "window": window,
+        "comparisons": {
             "batched_fp64_value": value64, "mixed_over_batched_fp64": value / world / value64,
-            "mixed_force_rel_err_max": max(errs),
-            "graph_steps_per_launch": (tuned or {}).get("graph_steps", 16),
+            "mixed_force_rel_err_max": max(errs), "mixed_force_rel_err_replicas": len(errs),
             "autotuned_shape": tuned, "autotuned_shape_fp64": tuned64,
-            "p99_req_latency_ms": serving["mixed"]["p99_ms"] if serving else None,
-            "serving": serving,
-            "mixed_vs_fp64_c3": accuracy,
-        },
+            **extras},
+        "p99_req_latency_ms": (extras.get("serving") or {}).get("latency", {}).get("p99_ms"),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic,
+                     "frac": achieved / peak, "traffic": FORCE_TRAFFIC_NCU,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch, "
+                                       "committed capture (profiles/k_force_mixed_c4.md), not this run",
                      "kernel": "k_force<float,1> (force+integrate)", "kernel_ms": force_ms,
+                     "rebuild_pass_ms": rebuild_ms, "rebuild_passes_per_md_step": nr.value / md,
                      "alg_bytes_per_launch": alg_bytes, "peak_source": peak_kind,
-                     "fp64_pipe_active": profile_value("fp64_pipe_active_pct"),
-                     "note": "working set (~30 MB) is L2-resident between steps; the step kernel is "
-                             "latency-bound at 16 warps/SM with its FP64 integrator on GB300's 2-lane/clk FP64 "
-                             "pipe (fp64_pipe_active: % of active cycles, ncu, profiles/k_force_mixed_c4.md)"},
+                     "alg_bytes": "325 N + 4 P + 12 C (N beads, P kept pairs, C active Go contacts)"},
         "cpu_baseline": cpu,
-        "e2e": {"value": e2e_value, "unit": "bead-steps/s", "h2d_bytes_per_step": int(yh.nbytes),
-                "d2h_bytes_per_step": int(24 * nbeads)},
+        "e2e": {"value": e2e_value, "unit": "bead-steps/s", "h2d_bytes_per_step": ybytes,
+                "d2h_bytes_per_step": ybytes, "same_window_as_value": e2e_same,
+                "path": "xmd_gpu_upload_history_all + xmd_gpu_step + xmd_gpu_download_history_all, pinned host"},
         "gpu_launches": launches,
         "clocks": clk,
     }
     print(json.dumps(out), flush=True)
 
 
-def plain_fp64(systems, yaml_fp64, md, warmup, rt, flush, sample=16):
-    """The plain FP64 path: each system alone in its own context (no packing,
-    FP64 forces), over a size-stratified sample of the replicas.  Returns
-    summed bead-steps over summed device time."""
-    from xmd_gb300 import Engine, abi
-    order = sorted(range(len(systems)), key=lambda k: systems[k].n)
-    pick = [order[int(q)] for q in np.linspace(0, len(order) - 1, min(sample, len(order)))]
-    work, t_ms = 0, 0.0
-    stream = C.c_void_p()
-    for k in pick:
-        with Engine(yaml_fp64) as e:
-            e.add_system(systems[k])
-            for _ in range(max(1, warmup)):
-                e.step(md)
+def bench_c2(args, dev, rt):
+    """Config 2 (16 x 500 beads, 300 A periodic box, Debye-Hueckel): the
+    plain FP64 GPU path on one system, beside the CPU restatement on the same
+    system and window."""
+    from oracle.pyoracle import Oracle, parse_params
+    from xmd_gb300 import Engine, abi, synth
+    s = synth.config_c2()
+    y = synth.yaml_for("c2", "fp64") + f"  device: {dev}\n"
+    warm, timed = args.c2_warmup, args.c2_steps
+    out = {"system": f"16 x 500 beads ({s.n}), 300 A periodic, Go+Pauli+tether/angle/CND+Debye-Hueckel",
+           "window_md_steps": [warm, warm + timed]}
+    for prec in ("fp64", "mixed"):
+        with Engine(y.replace("precision: fp64", f"precision: {prec}")) as e:
+            e.add_system(s)
+            e.step(warm)
             e.synchronize()
+            stream = C.c_void_p()
             abi.check(e.lib.xmd_gpu_get_stream(e.h, C.byref(stream)))
             ev = Events(rt, stream)
             a, b = ev.new(), ev.new()
-            rt.cudaMemsetAsync(flush, 1, C.c_size_t(L2_FLUSH_BYTES), stream)
+            s0 = e.stats()
             ev.record(a)
-            e.step(md)
+            e.step(timed)
             ev.record(b)
-            t_ms += ev.ms(a, b)
-            work += systems[k].n * md
-    nb = sum(systems[k].n for k in pick)
-    return {"value": work / (t_ms / 1e3),
-            "sample": f"{len(pick)} size-stratified replicas ({nb} beads), each alone in an FP64 context, "
-                      f"{md} steps each"}
+            ms = ev.ms(a, b)
+            s1 = e.stats()
+            out[f"gpu_{prec}_value"] = s.n * timed / (ms / 1e3)
+            out[f"gpu_{prec}_rebuilds_per_md_step"] = (s1["rebuilds"] - s0["rebuilds"]) / timed
+            if prec == "fp64":
+                y0, t0, g0 = e.get_history(0)
+    # the CPU restatement from the same window-start state, all host threads
+    p = parse_params(synth.yaml_for("c2", "fp64"))
+    o = Oracle(p, s, "port")
+    o.set_history(y0, t0, g0)
+    threads = os.cpu_count() or 1
+    o.step_omp(1, threads)
+    t = time.perf_counter()
+    o.step_omp(args.c2_cpu_steps, threads)
+    dt = time.perf_counter() - t
+    out["cpu_port_value"] = s.n * args.c2_cpu_steps / dt
+    out["cpu_port_sample"] = f"{args.c2_cpu_steps} MD steps from the window start, {threads} host threads"
+    out["gpu_fp64_over_cpu"] = out["gpu_fp64_value"] / out["cpu_port_value"]
+    return out
 
 
-def accuracy_c3(steps, every, device):
-    """Config 3: mixed precision against plain FP64 on 512 chains x 60 beads at
-    1e-3 A^-3 (periodic; Go + Debye-Hueckel + quasi-adiabatic contacts).
-    Forces are compared on the starting state; then each precision runs
-    `steps` steps from that state with the same generator seed, and the
-    energy (mean and drift), Rg and Q are compared over the second half of
-    the run (block-averaged standard errors)."""
-    from xmd_gb300 import Engine, observe, synth
-    s = synth.config_c3()
-    runs, forces, wall = {}, {}, {}
-    for prec in ("fp64", "mixed"):
-        with Engine(synth.yaml_for("c3", prec) + f"  device: {device}\n") as e:
-            e.add_system(s)
-            forces[prec], _ = e.eval_forces(0)
-            t0 = time.perf_counter()
-            runs[prec] = observe.sample(e, steps, every)
-            wall[prec] = time.perf_counter() - t0
-    res = observe.compare(runs["mixed"], runs["fp64"], skip=0.5)
-    ferr = float(np.abs(forces["mixed"] - forces["fp64"]).max() / np.abs(forces["fp64"]).max())
-    return {"system": f"512 x 60 beads ({s.n}), periodic, Go + Debye-Hueckel + quasi-adiabatic",
-            "steps": steps, "sample_every": every, "force_rel_err_t0": ferr,
-            "E_mean_rel_diff": res["E"]["rel_diff"], "E_mean_diff": res["E"]["diff"], "E_se": res["E"]["se"],
-            "E_drift_mixed": res["E_drift"]["drift"], "E_drift_fp64": res["E_drift"]["ref_drift"],
-            "E_drift_diff_rel_to_energy_scale": res["E_drift"]["rel_to_ref_energy"],
-            "Rg_mean_rel_diff": res["Rg"]["rel_diff"], "Rg_se": res["Rg"]["se"],
-            "Q_mean_diff": res["Q"]["diff"], "Q_se": res["Q"]["se"],
-            "wall_s": wall, "reference": "plain FP64 engine (pinned to the oracle by the parity tests)"}
+def serve_section(args, device, workers):
+    """Config 5 serving: capacity of mixed and plain FP64 on the same request
+    stream (every request offered at once, so throughput is the server's
+    capacity, not the arrival rate), then latency percentiles of mixed under
+    Poisson arrivals at a fraction of that capacity."""
+    from xmd_gb300 import synth
+    reqs = synth.config_c5(count=args.serve_requests, seed=5, workers=workers)
+    cap_reqs = reqs[:args.serve_capacity_requests]
+    cap = {prec: serve_run(cap_reqs, prec, args.serve_steps, None, device) for prec in ("mixed", "fp64")}
+    mean_work = float(np.mean([rq.n for rq in reqs])) * args.serve_steps
+    rate = args.serve_load * cap["mixed"]["bead_steps_per_s"] / mean_work
+    lat = serve_run(reqs, "mixed", args.serve_steps, rate, device)
+    lat["offered_load"] = args.serve_load
+    return {"capacity": cap,
+            "capacity_mixed_over_fp64": cap["mixed"]["bead_steps_per_s"] / cap["fp64"]["bead_steps_per_s"],
+            "latency": lat}
 
 
-def serve_bench(requests, precision, nsteps, rate_hz, device, seed=0):
-    """Config 5: requests arrive as a Poisson process at `rate_hz` and are
-    served by the continuous-batching loop (HBM-budget admission, state
-    resident on the device).  Returns latency percentiles and throughput."""
+def serve_run(requests, precision, nsteps, rate_hz, device, seed=0):
+    """Requests arrive as a Poisson process at `rate_hz` (None: all at once)
+    and are served by the continuous-batching loop (HBM-budget admission,
+    state resident on the device).  Returns latency percentiles and
+    throughput."""
     from xmd_gb300 import Server, XmdError, synth
     yaml = synth.yaml_for("c5", precision) + f"  device: {device}\n"
     rng = np.random.default_rng(seed)
-    gaps = rng.exponential(1.0 / rate_hz, size=len(requests))
+    gaps = rng.exponential(1.0 / rate_hz, size=len(requests)) if rate_hz else np.zeros(len(requests))
     with Server(yaml, hbm_budget=8 << 30, max_beads=200_000, chunk_steps=256) as srv:
         # warm-up request (graph capture, first list builds) outside the clock
         srv.result(srv.submit(requests[0], 256))
         t0 = time.perf_counter()
         ids = []
+        due = t0
         for g, rq in zip(gaps, requests):
-            time.sleep(g)
+            due += g
+            d = due - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
             ids.append(srv.submit(rq, nsteps))
         # a request whose trajectory diverges (non-finite force, as the
         # reference's own kernels do for some states) fails alone
@@ -455,35 +440,92 @@ def serve_bench(requests, precision, nsteps, rate_hz, device, seed=0):
     lat = np.sort(np.asarray(lat))
     work = float(done_beads) * nsteps
     pct = (lambda q: 1e3 * float(np.percentile(lat, q, method="inverted_cdf"))) if len(lat) else (lambda q: None)
-    return {"p50_ms": pct(50), "p99_ms": pct(99),
+    return {"p50_ms": pct(50), "p99_ms": pct(99), "max_ms": pct(100),
             "bead_steps_per_s": work / wall, "wall_s": wall, "peak_concurrent": int(st["peak_running"]),
             "requests": len(requests), "completed": len(lat), "failed": failed,
             "steps_per_request": nsteps, "rate_hz": rate_hz,
             "beads_total": int(sum(rq.n for rq in requests))}
 
 
+def accuracy_c3(nrep, steps, every, device):
+    """Config 3 at full size (512 x 60 beads at 1e-3 A^-3, periodic, Go +
+    Debye-Hueckel + quasi-adiabatic contacts): `nrep` replicas of the system,
+    each with its own generator seed, run in mixed precision and in plain
+    FP64 (one batched context per precision) from the same states with the
+    same seeds.  Per replica: the energy change over the run and over its
+    second half (least-squares slope x duration), and the means of E, Rg and
+    Q over the second half.  Reported as paired mixed - FP64 differences,
+    their mean and standard error over the replicas, and the drift
+    criterion: |mean paired drift difference| <= 1 % of |FP64 drift|."""
+    from xmd_gb300 import Engine, observe, synth
+    s = synth.config_c3()
+    runs, forces, wall = {}, {}, {}
+    for prec in ("fp64", "mixed"):
+        with Engine(synth.yaml_for("c3", prec) + f"  device: {device}\n") as e:
+            for k in range(nrep):
+                e.add_system(s, seed=s.seed + 7919 * k)
+            forces[prec], _ = e.eval_forces(0)
+            t0 = time.perf_counter()
+            samples = [[(0.0, *[e.observables(k)[f] for f in observe.FIELDS])] for k in range(nrep)]
+            for t in range(every, steps + 1, every):
+                e.step(every)
+                for k in range(nrep):
+                    samples[k].append((float(t), *[e.observables(k)[f] for f in observe.FIELDS]))
+            wall[prec] = time.perf_counter() - t0
+            runs[prec] = [np.asarray(x) for x in samples]
+    half = len(runs["fp64"][0]) // 2
+
+    def per_rep(a):
+        return {"drift_run": observe.drift(a[:, 0], a[:, 1]), "drift_half": observe.drift(a[half:, 0], a[half:, 1]),
+                "E": a[half:, 1].mean(), "Rg": a[half:, 3].mean(), "Q": a[half:, 4].mean()}
+    m = [per_rep(a) for a in runs["mixed"]]
+    f = [per_rep(a) for a in runs["fp64"]]
+
+    def paired(key):
+        d = np.array([x[key] - y[key] for x, y in zip(m, f)])
+        ref = np.array([y[key] for y in f])
+        return {"fp64_mean": float(ref.mean()), "mixed_minus_fp64": float(d.mean()),
+                "se": float(d.std(ddof=1) / np.sqrt(len(d))) if len(d) > 1 else None}
+    res = {k: paired(k) for k in ("drift_run", "drift_half", "E", "Rg", "Q")}
+    ferr = float(np.abs(forces["mixed"] - forces["fp64"]).max() / np.abs(forces["fp64"]).max())
+    dr = res["drift_run"]
+    rel = abs(dr["mixed_minus_fp64"]) / abs(dr["fp64_mean"])
+    rel_hi = (abs(dr["mixed_minus_fp64"]) + 2.0 * (dr["se"] or 0.0)) / abs(dr["fp64_mean"])
+    return {"system": f"{nrep} replicas x 512 x 60 beads ({s.n} each), periodic, Go + Debye-Hueckel + "
+                      "quasi-adiabatic, own generator seed per replica",
+            "steps": steps, "sample_every": every, "force_rel_err_t0": ferr, "paired": res,
+            "drift_rel_diff": rel, "drift_rel_diff_95": rel_hi, "drift_within_1pct": bool(rel <= 0.01),
+            "drift_within_1pct_95": bool(rel_hi <= 0.01),
+            "drift_definition": "energy change over the whole run (least-squares slope x duration), "
+                                "per replica, paired mixed - FP64; 95 = mean + 2 SE",
+            "wall_s": wall, "reference": "plain FP64 engine (pinned to the oracle by the parity tests)"}
+
+
 # ------------------------------------------------------------- CPU arms --
-def _cpu_run(systems, steps, threads, warm=0):
-    """All replicas on the CPU restatement, replicas spread over `threads`
-    host threads (ctypes releases the GIL during each call)."""
-    from oracle.pyoracle import Oracle
-    from xmd_gb300 import abi, synth
-    p = abi.parse_params(synth.yaml_for("c4", "fp64"))
-    orcs = [Oracle(p, s, "port") for s in systems]
-    order = sorted(range(len(orcs)), key=lambda k: -systems[k].n)
-    groups = [[] for _ in range(threads)]
-    load = [0] * threads
-    for k in order:   # longest-first greedy balance
-        g = int(np.argmin(load))
-        groups[g].append(k)
-        load[g] += systems[k].n
+class CpuReplicas:
+    """All replicas on the CPU restatement of the reference's FP64 kernels,
+    spread over `threads` host threads (ctypes releases the GIL during each
+    call).  Loads only the oracle's library (parameters are parsed by the
+    parser linked into it)."""
 
-    def work(g, n):
-        for k in groups[g]:
-            orcs[k].step(n)
+    def __init__(self, systems, threads):
+        from oracle.pyoracle import Oracle, parse_params
+        from xmd_gb300 import synth
+        p = parse_params(synth.yaml_for("c4", "fp64"))
+        self.orcs = [Oracle(p, s, "port") for s in systems]
+        order = sorted(range(len(self.orcs)), key=lambda k: -systems[k].n)
+        self.groups = [[] for _ in range(threads)]
+        load = [0] * threads
+        for k in order:   # longest-first greedy balance
+            g = int(np.argmin(load))
+            self.groups[g].append(k)
+            load[g] += systems[k].n
 
-    def run(n):
-        ts = [threading.Thread(target=work, args=(g, n)) for g in range(threads)]
+    def run(self, n):
+        def work(g):
+            for k in self.groups[g]:
+                self.orcs[k].step(n)
+        ts = [threading.Thread(target=work, args=(g,)) for g in range(len(self.groups))]
         t0 = time.perf_counter()
         for t in ts:
             t.start()
@@ -491,19 +533,21 @@ def _cpu_run(systems, steps, threads, warm=0):
             t.join()
         return time.perf_counter() - t0
 
-    if warm:
-        run(warm)
-    return orcs, run
 
-
-def cpu_baseline(systems, sample_steps=200):
+def cpu_baseline(systems, hist0, steps):
+    """A bounded sample of the same workload on the CPU restatement: every
+    replica, `steps` MD steps from the state at the start of the timed
+    window (so the list-rebuild rate is the window's)."""
     threads = os.cpu_count() or 1
     nb = sum(s.n for s in systems)
-    _, run = _cpu_run(systems, sample_steps, threads, warm=1)
-    dt = run(sample_steps)
-    return {"value": nb * sample_steps / dt, "unit": "bead-steps/s", "cores": threads, "kind": "port",
-            "sample": f"all {len(systems)} replicas x {sample_steps} steps ({nb} beads), "
-                      f"{dt:.1f} s wall on {threads} host threads"}
+    cpu = CpuReplicas(systems, threads)
+    for o, (y, t, g) in zip(cpu.orcs, hist0):
+        o.set_history(y, t, g)
+    cpu.run(1)
+    dt = cpu.run(steps)
+    return {"value": nb * steps / dt, "unit": "bead-steps/s", "cores": threads, "kind": "port",
+            "sample": f"all {len(systems)} replicas x {steps} MD steps ({nb} beads) from the timed window's "
+                      f"start state, {dt:.1f} s wall on {threads} host threads"}
 
 
 def run_reference(args, rank, world):
@@ -512,25 +556,26 @@ def run_reference(args, rank, world):
     systems = make_workload(0, workers=min(16, os.cpu_count() or 1))
     nb = sum(s.n for s in systems)
     threads = os.cpu_count() or 1
-    md = args.md_steps_ref
-    _, run = _cpu_run(systems, md, threads)
-    for _ in range(args.warmup):
-        run(md)
+    md, K, W = args.md_steps, args.steps, args.warmup
+    cpu = CpuReplicas(systems, threads)
+    for _ in range(W):
+        cpu.run(md)
     t = 0.0
-    for _ in range(args.steps):
-        t += run(md)
-    value = nb * md * args.steps / t
+    for _ in range(K):
+        t += cpu.run(md)
+    value = nb * md * K / t
+    maps = [ln.split()[-1] for ln in open("/proc/self/maps") if ".so" in ln and str(ROOT) in ln]
     out = {
-        "metric": METRIC, "value": value, "unit": "bead-steps/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+        "metric": METRIC, "value": value, "unit": "bead-steps/s", "n_gpus": world, "steps": K,
+        "warmup": W, "ms_per_step": 1e3 * t / K, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-        "config": {"workload": f"256 uneven single-chain replicas (log-uniform 50-800 beads, {nb} beads), "
-                               "Go+Debye-Hueckel+Pauli+tether/angle/dihedral, per-replica T in [0.3,0.6]",
-                   "md_steps_per_step": md,
-                   "implementation": "C restatement of the reference's FP64 kernels (bit-exact to them), "
-                                     "one host thread per replica group"},
+        "config": workload_config(nb, len(systems), md, W, K),
+        "implementation": "C restatement of the reference's FP64 kernels (bit-exact to them on x86), "
+                          "one host thread per replica group",
+        "libraries_loaded": sorted(set(Path(m).name for m in maps)),
         "cpu_baseline": {"value": value, "unit": "bead-steps/s", "cores": threads, "kind": "port",
-                         "sample": f"all {len(systems)} replicas x {md} steps per bench step"},
+                         "sample": f"all {len(systems)} replicas x {md} MD steps per bench step, "
+                                   f"MD steps [{W * md}, {(W + K) * md})"},
         "e2e": {"value": value, "unit": "bead-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out), flush=True)
@@ -539,15 +584,22 @@ def run_reference(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--md-steps", type=int, default=96)
-    ap.add_argument("--md-steps-ref", type=int, default=5)
-    ap.add_argument("--cpu-sample-steps", type=int, default=100)
-    ap.add_argument("--serve-requests", type=int, default=12)
+    ap.add_argument("--md-steps", type=int, default=240)
+    ap.add_argument("--cpu-sample-steps", type=int, default=120)
+    ap.add_argument("--no-extras", dest="extras", action="store_false",
+                    help="skip the config-2, serving and config-3 sections")
+    ap.add_argument("--c2-warmup", type=int, default=480)
+    ap.add_argument("--c2-steps", type=int, default=2400)
+    ap.add_argument("--c2-cpu-steps", type=int, default=40)
+    ap.add_argument("--serve-requests", type=int, default=200)
+    ap.add_argument("--serve-capacity-requests", type=int, default=32)
+    ap.add_argument("--serve-load", type=float, default=0.7)
     ap.add_argument("--serve-steps", type=int, default=20000)
-    ap.add_argument("--accuracy-steps", type=int, default=100000)
+    ap.add_argument("--accuracy-replicas", type=int, default=8)
+    ap.add_argument("--accuracy-steps", type=int, default=20000)
     ap.add_argument("--accuracy-every", type=int, default=1000)
     ap.add_argument("--no-autotune", dest="autotune", action="store_false")
     args = ap.parse_args()
@@ -560,11 +612,10 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
-    if True:
-        from xmd_gb300 import build
-        build.build_engine()
-        build.build_oracle()
-        run_engine(args, rank, local, world)
+    from xmd_gb300 import build
+    build.build_engine()
+    build.build_oracle()
+    run_engine(args, rank, local, world)
     if world > 1:
         import torch.distributed as dist
         dist.barrier()

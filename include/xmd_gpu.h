@@ -310,6 +310,10 @@ int xmd_gpu_synchronize(xmd_gpu_ctx *ctx);
  * from the new positions (the next step verifies and rebuilds as needed). */
 int xmd_gpu_upload_history_all(xmd_gpu_ctx *ctx, const double *y);
 int xmd_gpu_download_positions_all(xmd_gpu_ctx *ctx, double *r);
+/* The whole [6][3*N] history of all replicas (the layout the upload takes):
+ * a host-driven loop can carry the state through host memory and upload it
+ * back unchanged without altering the trajectory. */
+int xmd_gpu_download_history_all(xmd_gpu_ctx *ctx, double *y);
 /* The CUDA stream (cudaStream_t) all work of the context is ordered on. */
 int xmd_gpu_get_stream(xmd_gpu_ctx *ctx, void **stream);
 /* Counters, see XMD_STAT_*; out[XMD_NUM_STATS]. */
@@ -331,12 +335,6 @@ int xmd_gpu_set_tuning(xmd_gpu_ctx *ctx, const int32_t *shape);
 int xmd_gpu_get_tuning(xmd_gpu_ctx *ctx, int32_t *shape);
 int xmd_gpu_kernel_times(xmd_gpu_ctx *ctx, double *force_ms, int64_t *force_launches,
                          double *rebuild_ms, int64_t *rebuild_launches);
-
-/* No counterpart in the reference.  Measures the FP64 fused multiply-add
- * rate of CUDA device `device` (TFLOP/s, 2 flops per FMA, best of four timed
- * launches of a kernel that fills every SM); the FP64 roof against which the
- * step kernels are reported.  Takes about 0.1 s. */
-int xmd_gpu_fp64_peak(int32_t device, double *tflops);
 
 /* ---- dynamic membership ----------------------------------------------------- */
 /* No counterpart in the reference (its driver simulates one system).  After
@@ -412,9 +410,12 @@ int xmd_gpu_server_destroy(xmd_gpu_server *srv);
  * pairs i < j of the engine's Verlet search: not in the same chain with
  * |seq_i - seq_j| < 3, minimum-image distance below `cutoff`
  * (legacy_update.cpp:24-29 semantics), written as (i, j) into d_pairs[2*k] in
- * (i, j) order, at most `cap` pairs; *d_count receives the number found
- * (which may exceed cap).  d_r = positions [3n], d_chain / d_seq = [n];
- * cell = host array, 0 = open along that axis.
+ * (i, j) order, at most `cap` pairs; *d_count receives the number found.
+ * When that number exceeds cap, d_pairs holds the first cap pairs of the
+ * full (i, j)-ordered list.  d_r = positions [3n], d_chain / d_seq = [n];
+ * cell = host array, 0 = open along that axis.  Each bead's row is kept sorted
+ * by insertion in one thread, O(m^2) for m partners: meant for Verlet-list
+ * densities, slow when most beads lie within the cutoff of most others.
  *
  * The first call on a device looks up the scratch's device address (once per
  * device, with that device current); make that first call before any stream

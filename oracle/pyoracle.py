@@ -220,6 +220,21 @@ class Oracle:
         return {"E": E.value, "K": K.value, "Rg": Rg.value, "Q": Q.value}
 
 
+def parse_params(yaml_text: str = ""):
+    """xmd_params of YAML overrides merged over the defaults, resolved by the
+    parser linked into liboracle.so (the engine library is not loaded)."""
+    from xmd_gb300.abi import Params, XmdError
+    lib = _load(PORT_LIB, "xo_", Params)
+    fn = lib.xo_parse_params
+    fn.restype, fn.argtypes = C.c_int, [C.c_char_p, C.POINTER(Params)]
+    lib.xo_last_error.restype = C.c_char_p
+    p = Params()
+    rc = fn(yaml_text.encode(), C.byref(p))
+    if rc != 0:
+        raise XmdError(rc, lib.xo_last_error().decode())
+    return p
+
+
 def rng_stream(kind: str, state: int, n: int):
     """n raw outputs of the reference generator from `state`."""
     from xmd_gb300.abi import Params

@@ -3,7 +3,10 @@
 # own hot-path translation units (TEST INFRASTRUCTURE; never shipped).
 #
 #   XMD_REF_ROOT   reference checkout (default /root/reference); its xmd/ tree
-#                  is read, never written.
+#                  is read, never written.  Exit status 2 when it is absent.
+#
+# The reference root used is recorded in oracle/_ref/ref_root.txt, where tests
+# that read the reference's example data find it.
 #
 # The FP64 oracle is the reference with `using real = double;`
 # (xmd/include/xmd/types/scalar.h:4).  The reference has no such switch, so the
@@ -57,4 +60,5 @@ g++ "${FLAGS[@]}" "${INC[@]}" -c "$HERE/ref_driver.cpp" -o "$OUT/obj/ref_driver.
 pids+=($!)
 for p in "${pids[@]}"; do wait "$p"; done
 g++ -shared -o "$OUT/libxmdref64.so" "${OBJS[@]}" "$OUT/obj/ref_driver.o"
+echo "${XMD_REF_ROOT:-/root/reference}" > "$OUT/ref_root.txt"
 echo "built $OUT/libxmdref64.so"

@@ -7,7 +7,13 @@ reference tree).  Each fixture stores the full input (topology, native
 structure, positions, YAML) and the reference's outputs, so the tests need
 neither the reference tree nor the synthetic generator to replay it.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]    (all cases by default)
+
+The full-size systems of the benchmark configurations (8,000 and 30,720
+beads) keep only what their tests read: the inputs, the forces and energies
+at step 0, the generator state and quasi-adiabatic contacts at each snapshot,
+and the state at the last snapshot inside the parity horizon (the whole
+predictor-corrector history for 8,000 beads, positions for 30,720).
 """
 from __future__ import annotations
 
@@ -25,6 +31,18 @@ from xmd_gb300 import abi, synth  # noqa: E402
 OUT = Path(__file__).resolve().parent
 
 QA_SHORT = "quasi-adiabatic potential:\n  phase duration: 0.25 tau\n"
+# relative ES instead of const ES, simple native dihedrals instead of complex
+REL_SND = """const ES:
+  enabled: false
+relative ES:
+  enabled: true
+  screening distance: 10.0 A
+  factor: 4.0 eps_0/A
+complex native dihedrals:
+  enabled: false
+simple native dihedrals:
+  enabled: true
+"""
 
 CASES = {
     # 100-bead chain from the extended start, open boundary, Go + Pauli +
@@ -45,6 +63,17 @@ CASES = {
     "c3_qa600": dict(sys=lambda: synth.make_system([30] * 20, 11, box=(600 / 1e-3) ** (1 / 3) * 0.2 * 0.5,
                                                    types="uniform20", temperature=0.35),
                      yaml=synth.yaml_for("c3") + QA_SHORT, steps=500),
+    # 8 x 60 beads from extended starts, 80 A periodic box, with the relative
+    # ES term (es/relative.cpp) and simple native dihedrals
+    # (dihedral/simple_native.cpp) in place of const ES and CND
+    "c2_relsnd480": dict(sys=lambda: synth.make_system([60] * 8, 6, box=80 * 0.2, temperature=0.35),
+                         yaml=synth.yaml_for("c2") + REL_SND, steps=1000),
+    # the plain FP64 benchmark system at full size: 16 x 500 beads in a
+    # 300 A periodic box, charges +-1 at p = 0.1 each, Debye-Hueckel
+    "c2_full8000": dict(sys=lambda: synth.config_c2(), yaml=synth.yaml_for("c2"), steps=200, big="history"),
+    # the mixed-precision benchmark system at full size: 512 x 60 beads at
+    # 1e-3 A^-3, periodic, Go + Debye-Hueckel + quasi-adiabatic contacts
+    "c3_full30720": dict(sys=lambda: synth.config_c3(), yaml=synth.yaml_for("c3"), steps=50, big="positions"),
 }
 
 
@@ -70,7 +99,7 @@ def parity_horizon(s, p, total):
     correct FP64 implementations is not defined."""
     a, b = Oracle(p, s, "port"), Oracle(p, s, "port")
     done, best = 0, 0
-    for n in list(SNAPSHOTS) + [total]:
+    for n in sorted({k for k in SNAPSHOTS if k <= total} | {total}):
         a.step(n - done)
         b.step_omp(n - done, 4)
         done = n
@@ -83,42 +112,57 @@ def parity_horizon(s, p, total):
     return best
 
 
-def main():
-    for name, c in CASES.items():
-        s = c["sys"]()
-        p = abi.parse_params(c["yaml"])
-        ref = Oracle(p, s, "ref")
-        F0, V0 = ref.eval_forces()
-        counts0 = ref.counts()
-        snaps = {}
-        done = 0
-        for k in SNAPSHOTS:
-            ref.step(k - done)
-            done = k
-            snaps[f"y_{k}"] = ref.get_history()[0]
-            snaps[f"rng_{k}"] = np.uint64(ref.get_history()[2])
-            qk, _ = ref.qa_contacts()
-            if qk.size:
-                snaps[f"qa_{k}"] = qk
-        ref.step(c["steps"] - done)
-        y, t, rng = ref.get_history()
-        snaps["parity_steps"] = np.int64(parity_horizon(s, p, c["steps"]))
+def make_case(name, c):
+    s = c["sys"]()
+    p = abi.parse_params(c["yaml"])
+    big = c.get("big")
+    horizon = parity_horizon(s, p, c["steps"])
+    ref = Oracle(p, s, "ref")
+    F0, V0 = ref.eval_forces()
+    counts0 = ref.counts()
+    snaps = {}
+    done = 0
+    keep = max([k for k in SNAPSHOTS + (c["steps"],) if k <= max(horizon, 50) and k <= c["steps"]])
+    for k in SNAPSHOTS:
+        if k > c["steps"]:
+            break
+        ref.step(k - done)
+        done = k
+        y, _, st = ref.get_history()
+        if not big or k == keep:
+            snaps[f"y_{k}"] = y if big != "positions" else y[0]
+        snaps[f"rng_{k}"] = np.uint64(st)
+        qk, _ = ref.qa_contacts()
+        if qk.size:
+            snaps[f"qa_{k}"] = qk
+    ref.step(c["steps"] - done)
+    y, t, rng = ref.get_history()
+    snaps["parity_steps"] = np.int64(horizon)
+    extra = {}
+    if not big:
         F1, V1 = ref.eval_forces()
         qa, qa_t = ref.qa_contacts()
-        extra = {}
+        extra = dict(F1=F1, V1=V1)
         if qa.size:
-            extra = dict(qa_contacts=qa, qa_ref_time=qa_t, sync=ref.sync())
-        np.savez_compressed(OUT / f"{name}.npz", yaml=np.array(c["yaml"]), steps=np.int64(c["steps"]),
-                            F0=F0, V0=V0, n_go0=np.int64(counts0["go"]), n_pauli0=np.int64(counts0["pauli"]),
-                            n_es0=np.int64(counts0["es"]), y=y, t=np.float64(t), rng=np.uint64(rng),
-                            F1=F1, V1=V1, rebuilds=np.int64(ref.counts()["rebuilds"]),
-                            **pack_system(s), **extra, **snaps)
-        print(name, s.n, "atoms,", c["steps"], "steps, V0 =", V0.sum(), "rebuilds", ref.counts()["rebuilds"],
-              "parity horizon", int(snaps["parity_steps"]))
-    raw, st = rng_stream("ref", 42, 64)
-    np.savez_compressed(OUT / "rng_seed42.npz", raw=raw, state_after=np.uint64(st))
-    print("rng", raw[:3])
+            extra.update(qa_contacts=qa, qa_ref_time=qa_t, sync=ref.sync())
+        extra.update(y=y)
+    np.savez_compressed(OUT / f"{name}.npz", yaml=np.array(c["yaml"]), steps=np.int64(c["steps"]),
+                        F0=F0, V0=V0, n_go0=np.int64(counts0["go"]), n_pauli0=np.int64(counts0["pauli"]),
+                        n_es0=np.int64(counts0["es"]), t=np.float64(t), rng=np.uint64(rng),
+                        rebuilds=np.int64(ref.counts()["rebuilds"]),
+                        **pack_system(s), **extra, **snaps)
+    print(name, s.n, "atoms,", c["steps"], "steps, V0 =", V0.sum(), "rebuilds", ref.counts()["rebuilds"],
+          "parity horizon", horizon, flush=True)
+
+
+def main(names):
+    for name in names or CASES:
+        make_case(name, CASES[name])
+    if not names:
+        raw, st = rng_stream("ref", 42, 64)
+        np.savez_compressed(OUT / "rng_seed42.npz", raw=raw, state_after=np.uint64(st))
+        print("rng", raw[:3])
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

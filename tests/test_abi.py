@@ -30,7 +30,7 @@ def declared():
 def test_header_declares_the_boundary():
     d = declared()
     for name in ("xmd_gpu_create", "xmd_gpu_eval_forces", "xmd_gpu_step", "xmd_gpu_get_state",
-                 "xmd_gpu_observables", "xmd_gpu_verlet_pairs_noalloc", "xmd_gpu_fp64_peak"):
+                 "xmd_gpu_observables", "xmd_gpu_verlet_pairs_noalloc"):
         assert name in d
 
 

@@ -112,7 +112,7 @@ def test_fresh_system_matches_port(seed):
     assert t == to
 
 
-@pytest.mark.parametrize("case", ["c1_chain100", "c2_periodic480"])
+@pytest.mark.parametrize("case", ["c1_chain100", "c2_periodic480", "c2_relsnd480"])
 def test_mixed_precision_force_error(case):
     s, y, z = load_golden(case)
     with Engine(y.replace("precision: fp64", "precision: mixed")) as e:
@@ -171,6 +171,31 @@ def test_packed_upload_download_roundtrip():
         r = np.zeros(3 * (40 + 75))
         abi.check(e.lib.xmd_gpu_download_positions_all(e.h, abi.dptr(r)))
         assert np.array_equal(r.reshape(-1, 3), np.concatenate([h[0] for h in hs]))
+        yall = np.zeros(18 * (40 + 75))
+        abi.check(e.lib.xmd_gpu_download_history_all(e.h, abi.dptr(yall)))
+        assert np.array_equal(yall, packed.reshape(-1))
+
+
+def test_host_round_trip_keeps_the_trajectory():
+    """Carrying the whole state through host memory between chunks
+    (download_history_all, upload_history_all) leaves the trajectory
+    bit-identical to a run that never leaves the device."""
+    systems = [synth.make_system([L], 600 + k, temperature=0.4) for k, L in enumerate([60, 90])]
+    y = synth.yaml_for("c2")
+    with Engine(y) as a, Engine(y) as b:
+        for s in systems:
+            a.add_system(s)
+            b.add_system(s)
+        a.step(200)
+        host = np.zeros(18 * 150)
+        for _ in range(5):
+            abi.check(b.lib.xmd_gpu_download_history_all(b.h, abi.dptr(host)))
+            abi.check(b.lib.xmd_gpu_upload_history_all(b.h, abi.dptr(host)))
+            b.step(40)
+        for k in range(2):
+            ya, ta, sa = a.get_history(k)
+            yb, tb, sb = b.get_history(k)
+            assert np.array_equal(ya, yb) and ta == tb and sa == sb
 
 
 def with_engine_key(y: str, line: str) -> str:
@@ -274,8 +299,13 @@ def test_verlet_rows_grow_on_demand():
     assert rel_err(F, z["F0"], floor=1.0) <= 1e-10
 
 
-@pytest.mark.parametrize("case", ["c1_chain100", "c2_periodic480", "c3_qa600"])
-@pytest.mark.parametrize("term", [0, 1, 2, 4, 5, 6])
+# one term at a time: tether 0, native angle 1, CND 2, SND 3, Go 4, Pauli 5,
+# const ES 6, relative ES 7
+PER_TERM = [(c, k) for c in ("c1_chain100", "c2_periodic480", "c3_qa600") for k in (0, 1, 2, 4, 5, 6)] + \
+           [("c2_relsnd480", k) for k in (0, 1, 3, 4, 5, 7)]
+
+
+@pytest.mark.parametrize("case,term", PER_TERM)
 def test_per_term_forces(case, term):
     """One term enabled at a time (the list cutoffs kept as with all terms):
     forces and energy of that term alone within 1e-10 of the oracle,

@@ -57,7 +57,7 @@ def test_reference_arm_prints_once_under_torchrun():
     port = free_port()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port), str(ROOT / "bench.py"),
-           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "3", "--md-steps-ref", "1"]
+           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "3", "--md-steps", "1"]
     res = subprocess.run(cmd, capture_output=True, text=True, timeout=900, cwd=str(ROOT))
     assert res.returncode == 0, res.stderr[-2000:]
     lines = [l for l in res.stdout.splitlines() if l.startswith("{")]
@@ -65,3 +65,8 @@ def test_reference_arm_prints_once_under_torchrun():
     rec = json.loads(lines[0])
     assert rec["impl"] == "reference" and rec["n_gpus"] == 2 and rec["value"] > 0
     assert rec["cpu_baseline"]["cores"] >= 1 and rec["e2e"]["h2d_bytes_per_step"] == 0
+    # the CPU arm maps the oracle's library only, never the engine's
+    assert rec["libraries_loaded"] == ["liboracle.so"], rec["libraries_loaded"]
+    # the same config as the engine arm would report for these arguments
+    import bench
+    assert rec["config"] == bench.workload_config(rec["config"]["beads_per_gpu"], 256, 1, 3, 1)

@@ -13,7 +13,10 @@ from tests.util import ANGSTROM, energy_rel, only_term, rel_err
 from xmd_gb300 import abi, seqfile, synth
 
 have_ref = REF_LIB.exists()
-EXAMPLES = Path("/root/reference/xmd/data/examples")
+# the reference checkout the reference oracle was built from (recorded by
+# oracle/ref/build_ref.sh); its example inputs are read where they lie
+_REF_ROOT = REF_LIB.parent / "ref_root.txt"
+EXAMPLES = Path(_REF_ROOT.read_text().strip() if _REF_ROOT.exists() else "/nonexistent") / "xmd/data/examples"
 
 
 def test_yaml_subset():

@@ -137,3 +137,53 @@ def test_snapshot_of_another_layout_rejected():
         with pytest.raises(abi.XmdError):
             a.restore(1, snap[:100])
         a.restore(1, snap)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cut", [1, 4096])
+def test_truncated_snapshot_leaves_replica_unchanged(cut):
+    """A snapshot cut short anywhere past its header is rejected before any
+    of the replica's state is written: the replica continues exactly as if no
+    restore had been tried."""
+    s, y, _ = load_golden("c3_qa600")
+    other = synth.make_system([40, 25], 8, box=None, types="charged10", temperature=0.4, rng_seed=3)
+    with build(y, [other, s]) as a, build(y, [other, s]) as b:
+        a.step(60)
+        b.step(60)
+        snap = a.snapshot(1)
+        a.step(30)
+        b.step(30)
+        before = b.get_history(1)
+        with pytest.raises(abi.XmdError):
+            b.restore(1, snap[:len(snap) - cut])
+        after = b.get_history(1)
+        assert np.array_equal(after[0], before[0]) and after[1:] == before[1:]
+        a.step(40)
+        b.step(40)
+        ga, gb = a.get_history(1), b.get_history(1)
+        assert np.array_equal(ga[0], gb[0]) and ga[1:] == gb[1:]
+        assert np.array_equal(a.qa_contacts(1)[0], b.qa_contacts(1)[0])
+
+
+@pytest.mark.gpu
+def test_snapshot_with_other_wall_planes_rejected():
+    """The saved LJ attractive wall states belong to the wall planes they
+    were taken with: a context with other planes refuses the snapshot."""
+    from xmd_gb300 import Engine
+    s = synth.make_system([30], 4, box=None, types="charged10", temperature=0.4)
+    y = synth.yaml_for("c1") + "LJ attractive walls:\n  enabled: true\n"
+    planes = [(np.array([0.0, 0.0, -5.0]), np.array([0.0, 0.0, 1.0])),
+              (np.array([0.0, 0.0, -6.0]), np.array([0.0, 0.0, 1.0]))]
+    snaps = []
+    for o, nrm in planes:
+        with Engine(y) as e:
+            e.set_walls(1, o[None, :], nrm[None, :])
+            e.add_system(s)
+            e.step(5)
+            snaps.append(e.snapshot(0))
+    with Engine(y) as e:
+        e.set_walls(1, planes[0][0][None, :], planes[0][1][None, :])
+        e.add_system(s)
+        e.restore(0, snaps[0])
+        with pytest.raises(abi.XmdError):
+            e.restore(0, snaps[1])

@@ -30,7 +30,8 @@ LYS = abi.AA.index("LYS")
 
 
 def all_charged_system(chains, length, seed, box_a):
-    s = synth.make_system([length] * chains, seed, box=box_a * ANGSTROM, temperature=0.35, native=False)
+    box = None if box_a is None else box_a * ANGSTROM
+    s = synth.make_system([length] * chains, seed, box=box, temperature=0.35, native=False)
     s.atype = np.full(s.n, LYS, dtype=np.uint8)
     return s
 
@@ -83,20 +84,21 @@ class DeviceBuffers:
         self.ptrs = []
 
 
-def noalloc_pairs(lib, rt, bufs, s, cutoff):
+def noalloc_pairs(lib, rt, bufs, s, cutoff, cap=None, want_count=False):
     d_r = bufs.put(np.asarray(s.r, dtype=np.float64).reshape(-1))
     d_chain = bufs.put(np.asarray(s.chain, dtype=np.int32))
     d_seq = bufs.put(np.asarray(s.seq, dtype=np.int32))
-    cap = 64 * s.n + 64
+    cap = 64 * s.n + 64 if cap is None else cap
     d_pairs = bufs.empty(8 * cap)
     d_count = bufs.empty(4)
     cell = np.ascontiguousarray(s.cell, dtype=np.float64)
     abi.check(lib.xmd_gpu_verlet_pairs_noalloc(d_r, d_chain, d_seq, s.n, abi.dptr(cell), cutoff,
                                                d_pairs, cap, d_count, None))
     assert rt.cudaDeviceSynchronize() == 0
-    k = int(bufs.get(d_count, np.int32, 1)[0])
-    assert k <= cap
-    return bufs.get(d_pairs, np.int32, 2 * k).reshape(k, 2)
+    total = int(bufs.get(d_count, np.int32, 1)[0])
+    k = min(total, cap)
+    got = bufs.get(d_pairs, np.int32, 2 * k).reshape(k, 2)
+    return (got, total) if want_count else got
 
 
 def test_noalloc_pairs_match_engine_two_calls():
@@ -125,3 +127,50 @@ def test_noalloc_rejects_oversize():
                                           None, 0, None, None)
     assert rc == -5
     assert b"XMD_NOALLOC_MAX_BEADS" in lib.xmd_gpu_last_error()
+
+
+def free_device_bytes(rt):
+    free, total = ctypes.c_size_t(), ctypes.c_size_t()
+    assert rt.cudaMemGetInfo(ctypes.byref(free), ctypes.byref(total)) == 0
+    return free.value
+
+
+def test_noalloc_open_boundary_truncation_and_no_allocation():
+    """An open (non-periodic) system, where cells clamp at the low corner and
+    out-of-range neighbour cells are skipped, against the engine's list; a
+    call whose cap is below the pair count returns the full count and the
+    first cap pairs of the (i, j)-ordered list; and repeated calls leave the
+    device's free memory unchanged (no allocation behind the caller's back)."""
+    lib = abi.load()
+    rt = cudart()
+    s = all_charged_system(4, 50, 91, None)
+    assert not np.asarray(s.cell).any()
+    want = engine_pairs(s)
+    assert len(want) > 100
+    verlet_radius = (20.0 + 5.0) * ANGSTROM
+    bufs = DeviceBuffers(rt)
+    try:
+        got, total = noalloc_pairs(lib, rt, bufs, s, verlet_radius, want_count=True)
+        assert total == len(want) and np.array_equal(got, want)
+        for cap in (len(want) // 3, len(want) - 1, 1):
+            part, total = noalloc_pairs(lib, rt, bufs, s, verlet_radius, cap=cap, want_count=True)
+            assert total == len(want)
+            assert np.array_equal(part, want[:cap])
+        # buffers of the next call first, then the free memory around it
+        d_r = bufs.put(np.asarray(s.r, dtype=np.float64).reshape(-1))
+        d_chain = bufs.put(np.asarray(s.chain, dtype=np.int32))
+        d_seq = bufs.put(np.asarray(s.seq, dtype=np.int32))
+        cap = 64 * s.n
+        d_pairs = bufs.empty(8 * cap)
+        d_count = bufs.empty(4)
+        cell = np.zeros(3)
+        assert rt.cudaDeviceSynchronize() == 0
+        before = free_device_bytes(rt)
+        for _ in range(3):
+            abi.check(lib.xmd_gpu_verlet_pairs_noalloc(d_r, d_chain, d_seq, s.n, abi.dptr(cell), verlet_radius,
+                                                       d_pairs, cap, d_count, None))
+        assert rt.cudaDeviceSynchronize() == 0
+        assert free_device_bytes(rt) == before
+        assert int(bufs.get(d_count, np.int32, 1)[0]) == len(want)
+    finally:
+        bufs.free()

@@ -8,8 +8,11 @@ import numpy as np
 from xmd_gb300.synth import System
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
-GOLDEN_CASES = ["c1_chain100", "c1_native100", "c2_periodic480", "c2_sparse240", "c3_qa600"]
-FP64_CASES = ["c1_chain100", "c1_native100", "c2_periodic480", "c2_sparse240"]
+GOLDEN_CASES = ["c1_chain100", "c1_native100", "c2_periodic480", "c2_sparse240", "c3_qa600", "c2_relsnd480"]
+FP64_CASES = ["c1_chain100", "c1_native100", "c2_periodic480", "c2_sparse240", "c2_relsnd480"]
+# the benchmark systems at full size (8,000 and 30,720 beads): inputs, step-0
+# forces, and the state at the last snapshot inside the parity horizon
+FULL_CASES = ["c2_full8000", "c3_full30720"]
 ANGSTROM = 0.2
 # YAML section of each force term, in xmd_gb300.abi.TERM_* order
 SECTIONS = ["tether forces", "native angles", "complex native dihedrals", "simple native dihedrals",
@@ -31,9 +34,9 @@ def horizon_snapshot(z):
     under a reordered force summation to 1e-11 A (beyond it the dynamics
     amplifies rounding, so no two FP64 implementations stay within 1e-8 A)."""
     h = int(z["parity_steps"])
-    if h >= int(z["steps"]):
+    if h >= int(z["steps"]) and "y" in z:
         return int(z["steps"]), z["y"], int(z["rng"])
-    best = max(k for k in (50, 100, 200) if k <= max(h, 50))
+    best = max(k for k in (50, 100, 200) if k <= max(h, 50) and f"y_{k}" in z)
     return best, z[f"y_{best}"], int(z[f"rng_{best}"])
 
 

@@ -137,6 +137,7 @@ SIGNATURES = [
                                                C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     ("xmd_gpu_upload_history_all", C.c_int, [C.c_void_p, _pd]),
     ("xmd_gpu_download_positions_all", C.c_int, [C.c_void_p, _pd]),
+    ("xmd_gpu_download_history_all", C.c_int, [C.c_void_p, _pd]),
     ("xmd_gpu_get_stream", C.c_int, [C.c_void_p, P(C.c_void_p)]),
     ("xmd_gpu_stats", C.c_int, [C.c_void_p, P(C.c_int64)]),
     ("xmd_gpu_set_kernel_timing", C.c_int, [C.c_void_p, C.c_int]),
@@ -145,7 +146,6 @@ SIGNATURES = [
     ("xmd_gpu_get_tuning", C.c_int, [C.c_void_p, _pi32]),
     ("xmd_gpu_kernel_times", C.c_int, [C.c_void_p, _pd, P(C.c_int64), _pd, P(C.c_int64)]),
     ("xmd_gpu_synchronize", C.c_int, [C.c_void_p]),
-    ("xmd_gpu_fp64_peak", C.c_int, [C.c_int32, _pd]),
     ("xmd_gpu_reserve", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
     ("xmd_gpu_remove_replica", C.c_int, [C.c_void_p, C.c_int32]),
     ("xmd_gpu_set_steps", C.c_int, [C.c_void_p, C.c_int32, C.c_int64]),

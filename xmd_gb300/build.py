@@ -29,7 +29,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "--expt-relaxed-constexpr"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off"]
 
-CUDA_SOURCES = ["engine.cu", "noalloc.cu", "probe.cu"]
+CUDA_SOURCES = ["engine.cu", "noalloc.cu"]
 CXX_SOURCES = ["capi.cpp", "config.cpp", "defaults_yml.cpp", "server.cpp"]
 
 
@@ -85,26 +85,45 @@ def build_engine(verbose: bool = False, force: bool = False) -> Path:
 
 
 def build_oracle(verbose: bool = False, force: bool = False) -> Path:
-    """The CPU restatement (test oracle and timed CPU baseline)."""
-    deps = [ORACLE_SRC, ORACLE_SRC.with_suffix(".h"), ROOT / "include" / "xmd_gpu.h"]
+    """The CPU restatement (test oracle and timed CPU baseline), with the
+    host-side YAML parser linked in (oracle/params.cpp), so that CPU-only
+    callers resolve parameters without the engine library."""
+    cfg = [CSRC / "config.cpp", CSRC / "defaults_yml.cpp", ROOT / "oracle" / "params.cpp"]
+    deps = [ORACLE_SRC, ORACLE_SRC.with_suffix(".h"), ROOT / "include" / "xmd_gpu.h", CSRC / "config.h", *cfg]
     if force or _stale(ORACLE_LIB, deps):
+        obj_dir = BUILD / "oracle"
+        obj_dir.mkdir(parents=True, exist_ok=True)
         # -ffp-contract=off: the same uncontracted arithmetic on every host, so
         # list-membership decisions are reproducible across x86 and Arm.
-        _run(["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-std=c11",
-              "-D_GNU_SOURCE", str(ORACLE_SRC), "-o", str(ORACLE_LIB), "-lm"], verbose)
+        jobs = [["gcc", "-O2", "-fPIC", "-fopenmp", "-ffp-contract=off", "-std=c11", "-D_GNU_SOURCE",
+                 "-c", str(ORACLE_SRC), "-o", str(obj_dir / "xmd_oracle.o")]]
+        objs = [obj_dir / "xmd_oracle.o"]
+        for src in cfg:
+            o = obj_dir / (src.stem + ".o")
+            objs.append(o)
+            jobs.append(["g++", *CXX_FLAGS, "-c", str(src), "-o", str(o)])
+        with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+            list(ex.map(lambda c: _run(c, verbose), jobs))
+        _run(["g++", "-shared", "-fopenmp", "-o", str(ORACLE_LIB), *map(str, objs), "-lm"], verbose)
     return ORACLE_LIB
 
 
 def build_reference_oracle(verbose: bool = False) -> Path | None:
-    """Compile the reference's own kernels when its source tree is present."""
-    ref_root = Path(os.environ.get("XMD_REF_ROOT", "/root/reference"))
-    if not (ref_root / "xmd" / "src").is_dir():
-        return None
+    """Compile the reference's own kernels when its source tree is present.
+    The recipe (oracle/ref/build_ref.sh) locates the tree and exits with
+    status 2 when there is none; then this returns None."""
     script = ROOT / "oracle" / "ref" / "build_ref.sh"
     out = ROOT / "oracle" / "_ref" / "libxmdref64.so"
     deps = [script, ROOT / "oracle" / "ref" / "ref_driver.cpp", ROOT / "include" / "xmd_gpu.h"]
-    if _stale(out, deps):
-        _run(["bash", str(script)], verbose)
+    if not _stale(out, deps):
+        return out
+    res = subprocess.run(["bash", str(script)], capture_output=True, text=True)
+    if res.returncode == 2:
+        return None
+    if res.returncode != 0:
+        raise RuntimeError(f"reference oracle build failed ({res.returncode}):\n{res.stdout}\n{res.stderr}")
+    if verbose:
+        print(res.stdout, end="")
     return out
 
 

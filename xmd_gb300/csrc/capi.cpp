@@ -297,6 +297,12 @@ int xmd_gpu_download_positions_all(xmd_gpu_ctx *ctx, double *r) {
     return guard([&] { ctx->eng->use_device(); ctx->eng->download_positions_all(r); });
 }
 
+int xmd_gpu_download_history_all(xmd_gpu_ctx *ctx, double *y) {
+    NEED_CTX;
+    if (!y) return fail(XMD_ERR_ARG, "null output");
+    return guard([&] { ctx->eng->use_device(); ctx->eng->download_history_all(y); });
+}
+
 int xmd_gpu_get_stream(xmd_gpu_ctx *ctx, void **stream) {
     NEED_CTX;
     if (!stream) return fail(XMD_ERR_ARG, "null output");
@@ -465,11 +471,6 @@ int xmd_gpu_server_destroy(xmd_gpu_server *srv) {
         delete srv->srv;
         delete srv;
     });
-}
-
-int xmd_gpu_fp64_peak(int32_t device, double *tflops) {
-    if (!tflops || device < 0) return fail(XMD_ERR_ARG, "bad argument");
-    return guard([&] { *tflops = xmdg::fp64_peak(device); });
 }
 
 int xmd_gpu_kernel_times(xmd_gpu_ctx *ctx, double *force_ms, int64_t *force_launches, double *rebuild_ms,

@@ -2635,7 +2635,7 @@ uint64_t Engine::topo_hash(int rep) const {
     return h;
 }
 
-size_t Engine::snapshot_io(int rep, unsigned char *buf, size_t bytes, bool save) {
+size_t Engine::snapshot_io(int rep, unsigned char *buf, size_t bytes, bool save, int cap_rows) {
     check_rep(reps, rep);
     ready();
     RepHost &h = reps[rep];
@@ -2648,7 +2648,10 @@ size_t Engine::snapshot_io(int rep, unsigned char *buf, size_t bytes, bool save)
     hd.rep = rep; hd.n = n; hd.begin = b; hd.nl_cap = 0;   // the row capacity may differ (below)
     hd.nat_off = h.nat_off; hd.nat_len = h.nat_len; hd.ss_off = h.ss_off; hd.ss_len = h.ss_len;
     hd.qa_on = d.qa_on; hd.fp_off = h.fp_off; hd.fp_len = h.fp_len; hd.ct_off = h.ct_off; hd.ct_len = h.ct_len;
-    hd.topo = topo_hash(rep);
+    // the topology, and the wall planes the saved LJ attractive wall states
+    // refer to
+    hd.topo = fnv(fnv(topo_hash(rep), walls[0].data(), walls[0].size() * sizeof(double)), walls[1].data(),
+                  walls[1].size() * sizeof(double));
     hd.pad_ = (int32_t)(walls[1].size() / 6);   // LJ attractive walls (their pair states are saved)
     size_t off = 0;
     auto host = [&](void *p, size_t nb) {
@@ -2675,12 +2678,20 @@ size_t Engine::snapshot_io(int rep, unsigned char *buf, size_t bytes, bool save)
         if (std::memcmp(got.magic, SNAP_MAGIC, 8) != 0 || got.version != SNAP_VERSION)
             throw std::invalid_argument("not a snapshot of this format");
         if (std::memcmp(&got, &hd, sizeof hd) != 0)
-            throw std::invalid_argument("snapshot of another replica layout (parameters, systems or their order differ)");
+            throw std::invalid_argument("snapshot of another replica layout (precision, replica sizes or order, "
+                                        "topology or wall planes differ)");
+        // the whole snapshot must be there before anything of the replica
+        // is overwritten: a short buffer leaves the replica as it was
+        int32_t scap;
+        if (bytes < sizeof(SnapHeader) + sizeof scap) throw std::invalid_argument("snapshot truncated");
+        std::memcpy(&scap, buf + sizeof(SnapHeader), sizeof scap);
+        if (scap <= 0 || scap > (1 << 20)) throw std::invalid_argument("snapshot: bad row capacity");
+        if (bytes < snapshot_io(rep, nullptr, 0, true, scap)) throw std::invalid_argument("snapshot truncated");
     }
     host(&hd, sizeof hd);
     // Verlet row capacity of the snapshot; a restore grows this context's rows
     // to it (capacity does not change the trajectory)
-    int32_t cap = nl_cap;
+    int32_t cap = cap_rows >= 0 ? cap_rows : nl_cap;
     host(&cap, sizeof cap);
     if (buf && !save) {
         if (cap <= 0 || cap > (1 << 20)) throw std::invalid_argument("snapshot: bad row capacity");
@@ -3224,6 +3235,19 @@ __global__ void k_pack_positions(Dev d, double *__restrict__ r, int cur) {
     r[3 * (size_t)i + 2] = p.z;
 }
 
+__global__ void k_pack_history(Dev d, double *__restrict__ y, int cur) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.N) return;
+    const size_t n3 = 3 * (size_t)d.N;
+    double4_32a p = d.pos[cur][i];
+    y[3 * (size_t)i] = p.x;
+    y[3 * (size_t)i + 1] = p.y;
+    y[3 * (size_t)i + 2] = p.z;
+    for (int ord = 1; ord < 6; ++ord)
+        for (int a = 0; a < 3; ++a)
+            y[ord * n3 + 3 * (size_t)i + a] = d.yh[(size_t)((ord - 1) * 3 + a) * d.N + i];
+}
+
 void Engine::upload_history_all(const double *y) {
     use_device();
     ready();
@@ -3231,6 +3255,16 @@ void Engine::upload_history_all(const double *y) {
     CK(cudaMemcpyAsync(staging, y, sizeof(double) * 18 * (size_t)d.N, cudaMemcpyHostToDevice, stream));
     k_unpack_history<<<(d.N + 255) / 256, 256, 0, stream>>>(d, staging, cur);
     ++launches;
+}
+
+void Engine::download_history_all(double *y) {
+    use_device();
+    ready();
+    if (!staging) staging = (double *)dalloc(sizeof(double) * 18 * (size_t)d.N);
+    k_pack_history<<<(d.N + 255) / 256, 256, 0, stream>>>(d, staging, cur);
+    ++launches;
+    CK(cudaMemcpyAsync(y, staging, sizeof(double) * 18 * (size_t)d.N, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
 }
 
 void Engine::download_positions_all(double *r) {

@@ -304,7 +304,8 @@ public:
     void snapshot(int rep, void *buf, size_t bytes);
     void restore(int rep, const void *buf, size_t bytes);
     uint64_t topo_hash(int rep) const;
-    size_t snapshot_io(int rep, unsigned char *buf, size_t bytes, bool save);
+    // cap_rows >= 0: size of a snapshot whose Verlet rows have that capacity
+    size_t snapshot_io(int rep, unsigned char *buf, size_t bytes, bool save, int cap_rows = -1);
     void resize_rows(int ncap);
     void eval_forces(int rep, double *F, double *V);
     void step(int nsteps);
@@ -313,6 +314,7 @@ public:
     void sync();
     void upload_history_all(const double *y);
     void download_positions_all(double *r);
+    void download_history_all(double *y);
     cudaStream_t get_stream() const { return stream; }
     void stats(int64_t *out);
     void set_kernel_timing(bool on);
@@ -384,7 +386,6 @@ private:
 
 std::string &last_error();
 uint64_t rng_jump(uint64_t state, uint64_t n_draws);
-double fp64_peak(int device);
 int verlet_pairs_noalloc(const double *d_r, const int32_t *d_chain, const int32_t *d_seq, int32_t n,
                          const double cell[3], double cutoff, int32_t *d_pairs, int32_t cap, int32_t *d_count,
                          void *stream);

@@ -17,6 +17,11 @@
 // (legacy_update.cpp:24-26), whose minimum-image distance is below the
 // cutoff (legacy_update.cpp:28-29), in (i, j) order.  Cells of the cutoff's
 // edge are hashed into n buckets, which bounds the scratch by the bead count.
+// One thread builds one bead's row and keeps it sorted by insertion, so a row
+// of m partners costs O(m^2): cheap at Verlet-list densities (tens to a few
+// hundred partners), slow when most beads are within the cutoff of most
+// others (a periodic box under two cutoffs wide, a cluster much denser than
+// a protein).
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -137,19 +142,10 @@ __global__ void __launch_bounds__(NA_BLOCK) k_na_grid(NaScratch *s, const double
         run += s->bucket_cnt[c];
     }
     __syncthreads();
+    // the order inside a bucket is free: each row is ordered by j below
     for (int i = t; i < n; i += NA_BLOCK) {
         int k = s->bead_bucket[i];
         s->items[s->bucket_start[k] + atomicAdd(&s->bucket_fill[k], 1)] = i;
-    }
-    __syncthreads();
-    for (int c = t; c < nb; c += NA_BLOCK) {
-        int *it = s->items + s->bucket_start[c];
-        int m = s->bucket_cnt[c];
-        for (int x = 1; x < m; ++x) {
-            int v = it[x], y = x - 1;
-            while (y >= 0 && it[y] > v) { it[y + 1] = it[y]; --y; }
-            it[y + 1] = v;
-        }
     }
 }
 
@@ -179,7 +175,14 @@ __global__ void __launch_bounds__(128) k_na_rows(NaScratch *s, const double *__r
             }
     const int ci = chain[i], si = seq[i];
     int cnt = 0;
+    // pass 1: the row's m smallest partners (m = what fits below cap: all of
+    // them, except in the row that straddles cap), kept sorted by j with
+    // insertion as they are found, so the output is always the (i, j)-ordered
+    // prefix of the full list
     const int base = pass ? s->row_off[i] : 0;
+    const int m = pass ? min(s->row_cnt[i], max(0, cap - base)) : 0;
+    int32_t *row = pairs + 2 * (size_t)base;
+    int kept = 0;
     for (int kk = 0; kk < nk; ++kk) {
         const int q0 = s->bucket_start[keys[kk]], q1 = q0 + s->bucket_cnt[keys[kk]];
         for (int q = q0; q < q1; ++q) {
@@ -189,24 +192,22 @@ __global__ void __launch_bounds__(128) k_na_rows(NaScratch *s, const double *__r
             int df = si > sj ? si - sj : sj - si;
             if (chain[j] == ci && df < 3) continue;
             if (!(na_dist(*s, r, i, j) < cutoff)) continue;
-            if (pass && base + cnt < cap) {
-                pairs[2 * (size_t)(base + cnt)] = i;
-                pairs[2 * (size_t)(base + cnt) + 1] = j;
-            }
             ++cnt;
+            if (m == 0 || (kept == m && j >= row[2 * (m - 1) + 1])) continue;
+            int y = kept < m ? kept : m - 1;   // the slot that opens (the largest drops out when full)
+            while (y > 0 && row[2 * (y - 1) + 1] > j) {
+                row[2 * y + 1] = row[2 * (y - 1) + 1];
+                --y;
+            }
+            row[2 * y + 1] = j;
+            if (kept < m) ++kept;
         }
     }
     if (!pass) {
         s->row_cnt[i] = cnt;
         return;
     }
-    const int m = min(cnt, max(0, cap - base));   // the part of the row that fit
-    int32_t *row = pairs + 2 * (size_t)base;
-    for (int x = 1; x < m; ++x) {
-        int v = row[2 * x + 1], y = x - 1;
-        while (y >= 0 && row[2 * y + 1] > v) { row[2 * y + 3] = row[2 * y + 1]; --y; }
-        row[2 * y + 3] = v;
-    }
+    for (int x = 0; x < m; ++x) row[2 * x] = i;
 }
 
 // exclusive scan of the row counts; total to the caller's counter
