@@ -324,7 +324,7 @@ int xmd_gpu_set_kernel_timing(xmd_gpu_ctx *ctx, int on);
 
 /* ---- launch shapes and the autotuner ------------------------------------------
  * No counterpart in the reference (its OpenMP loop has no launch shape).
- * shape[3] = {beads per step-kernel block (64, 96, 128), resident tile-build
+ * shape[3] = {beads per step-kernel block (32, 64, 128; four threads per bead), resident tile-build
  * blocks per SM (0 = as many as fit), steps per captured graph (8, 16, 32)}.
  * Results never depend on the shape.  xmd_gpu_autotune times every candidate
  * on a clone of the context (same replicas, same starting state; the
@@ -378,7 +378,13 @@ enum { XMD_REQ_QUEUED = 0, XMD_REQ_RUNNING = 1, XMD_REQ_DONE = 2, XMD_REQ_FAILED
 enum {
     XMD_SRV_P50_S = 0, XMD_SRV_P99_S, XMD_SRV_BEAD_STEPS_PER_S, XMD_SRV_COMPLETED, XMD_SRV_QUEUED,
     XMD_SRV_RUNNING, XMD_SRV_CHUNKS, XMD_SRV_PEAK_RUNNING, XMD_SRV_CAP_BEADS, XMD_SRV_BEAD_STEPS,
-    XMD_SRV_SPAN_S, XMD_SRV_FAILED, XMD_SRV_NUM
+    XMD_SRV_SPAN_S, XMD_SRV_FAILED,
+    XMD_SRV_DEVICE_BYTES,     /* device memory the serving context holds           */
+    XMD_SRV_BUDGET_BYTES,     /* the HBM budget it was created with                */
+    XMD_SRV_BYTES_PER_BEAD,   /* measured device cost of one reserved bead slot    */
+    XMD_SRV_ADMIT_S,          /* worker time between step chunks (admit, retire)   */
+    XMD_SRV_STEP_S,           /* worker time inside step chunks                    */
+    XMD_SRV_NUM
 };
 int xmd_gpu_server_create(const char *yaml_text, int64_t hbm_budget_bytes, int32_t max_beads,
                           int32_t chunk_steps, xmd_gpu_server **out);

@@ -28,7 +28,7 @@ def run(prec, shape, nsteps=200):
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
 def test_shapes_give_identical_trajectories(prec):
     ref = run(prec, None)
-    for shape in [(64, 0, 8), (96, 2, 32), (128, 1, 16)]:
+    for shape in [(32, 0, 8), (64, 2, 32), (128, 1, 16)]:
         got = run(prec, shape)
         for r in range(5):
             assert np.array_equal(got[r], ref[r]), (shape, r)
@@ -42,7 +42,7 @@ def test_autotune_keeps_state_and_picks_a_valid_shape():
         e.step(32)
         f.step(32)
         best = e.autotune(64)
-        assert best["fb"] in (64, 96, 128) and best["graph_steps"] in (8, 16, 32)
+        assert best["fb"] in (32, 64, 128) and best["graph_steps"] in (8, 16, 32)
         assert best["ms_per_step"] > 0
         assert e.tuning() == {k: best[k] for k in ("fb", "tile_per_sm", "graph_steps")}
         e.step(96)

@@ -142,3 +142,16 @@ def test_static_context_reports_non_finite_and_freezes():
         e.step(8)
         r2, _, _ = e.get_state(0)
         assert np.isfinite(r2).all() and not np.array_equal(r2, good.r)
+
+
+def test_budget_is_the_real_allocation():
+    """The server sizes its reservation from the engine's measured device
+    cost per bead slot, so the context it holds stays within the budget and
+    uses most of it; the per-bead figure is the allocation's, not a guess."""
+    budget = 1 << 30
+    with Server(YAML, hbm_budget=budget, max_beads=10_000_000, chunk_steps=64) as srv:
+        st = srv.stats()
+    assert st["budget_bytes"] == budget
+    assert 0.9 * budget <= st["device_bytes"] <= budget
+    assert st["cap_beads"] * st["bytes_per_bead"] <= budget
+    assert 500 <= st["bytes_per_bead"] <= 4096

@@ -36,7 +36,8 @@ def horizon_snapshot(z):
     h = int(z["parity_steps"])
     if h >= int(z["steps"]) and "y" in z:
         return int(z["steps"]), z["y"], int(z["rng"])
-    best = max(k for k in (50, 100, 200) if k <= max(h, 50) and f"y_{k}" in z)
+    shots = sorted(int(k[2:]) for k in z.files if k.startswith("y_"))
+    best = max(k for k in shots if k <= max(h, shots[0]))
     return best, z[f"y_{best}"], int(z[f"rng_{best}"])
 
 

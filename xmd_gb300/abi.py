@@ -84,7 +84,8 @@ class Request(C.Structure):
 
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, -1
 SRV_KEYS = ["p50_s", "p99_s", "bead_steps_per_s", "completed", "queued", "running", "chunks", "peak_running",
-            "cap_beads", "bead_steps", "span_s", "failed"]
+            "cap_beads", "bead_steps", "span_s", "failed", "device_bytes", "budget_bytes", "bytes_per_bead",
+            "admit_s", "step_s"]
 
 LIB_PATH = Path(__file__).resolve().parent / "libxmdgpu.so"
 

@@ -51,6 +51,43 @@ template <class T> __device__ __forceinline__ T acos_c(T x) {
 }
 template <class T> __device__ __forceinline__ T ipow6(T s) { return s * (s * (s * (s * (s * s)))); }
 
+// ---- FP64 without contraction ---------------------------------------------------
+// The plain FP64 path evaluates its bonded terms with every product, sum,
+// quotient and square root rounded on its own (no fused multiply-add), as the
+// uncontracted CPU build of the reference does.  On the extended starts some
+// triples are straight to ~1e-6 rad: a dihedral's derivatives there scale as
+// 1 / |r12 x r23|^2 and its force reaches ~1e6, so one contracted rounding
+// moves that force by ~1e-10 of itself and the first step carries the change
+// into the positions at ~1e-8 A.  DN is a double whose operators round each
+// operation separately; the bonded templates instantiated on it reproduce
+// the reference's arithmetic operation for operation.
+struct DN {
+    double v;
+    DN() = default;
+    __host__ __device__ __forceinline__ constexpr DN(double x) : v(x) {}
+    __host__ __device__ __forceinline__ explicit operator double() const { return v; }
+};
+__device__ __forceinline__ DN operator+(DN a, DN b) { return DN(__dadd_rn(a.v, b.v)); }
+__device__ __forceinline__ DN operator-(DN a, DN b) { return DN(__dsub_rn(a.v, b.v)); }
+__device__ __forceinline__ DN operator*(DN a, DN b) { return DN(__dmul_rn(a.v, b.v)); }
+__device__ __forceinline__ DN operator/(DN a, DN b) { return DN(__ddiv_rn(a.v, b.v)); }
+__device__ __forceinline__ DN operator-(DN a) { return DN(-a.v); }
+__device__ __forceinline__ DN &operator+=(DN &a, DN b) { return a = a + b; }
+__device__ __forceinline__ bool operator<(DN a, DN b) { return a.v < b.v; }
+__device__ __forceinline__ bool operator>(DN a, DN b) { return a.v > b.v; }
+__device__ __forceinline__ DN sqrt_(DN x) { return DN(__dsqrt_rn(x.v)); }
+__device__ __forceinline__ DN acos_(DN x) { return DN(acos(x.v)); }
+__device__ __forceinline__ DN exp_(DN x) { return DN(exp(x.v)); }
+__device__ __forceinline__ DN sin(DN x) { return DN(::sin(x.v)); }
+__device__ __forceinline__ void sincos_(DN x, DN *s, DN *c) { sincos(x.v, &s->v, &c->v); }
+template <> __host__ __device__ __forceinline__ DN tpar<DN>(double d, float) { return DN(d); }
+__device__ __forceinline__ float ldg_(const float *p) { return __ldg(p); }
+__device__ __forceinline__ double ldg_(const double *p) { return __ldg(p); }
+__device__ __forceinline__ DN ldg_(const DN *p) { return DN(__ldg(&p->v)); }
+template <class T> __device__ __forceinline__ V3<double> v3d(V3<T> a) {
+    return V3<double>{(double)a.x, (double)a.y, (double)a.z};
+}
+
 // ---- FP32 <-> FP64 on the integer pipe --------------------------------------------
 // On GB300 FP64 arithmetic AND the FP32<->FP64 conversion instructions run at
 // 2 lanes per clock per SM (FP32: 128).  The mixed path therefore keeps FP64
@@ -275,7 +312,7 @@ template <class T>
 __device__ __noinline__ void heur_dih_nl(const T *hc, T s, T co, T *V, T *dV) {
     T c[6];
 #pragma unroll
-    for (int k = 0; k < 6; ++k) c[k] = __ldg(hc + k);
+    for (int k = 0; k < 6; ++k) c[k] = ldg_(hc + k);
     heur_dih_V<T>(c, s, co, V, dV);
 }
 

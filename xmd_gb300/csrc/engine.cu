@@ -253,10 +253,42 @@ __global__ void __launch_bounds__(256) k_ext(Dev d, TermP p, int cur) {
     fo[0] = f.x; fo[1] = f.y; fo[2] = f.z;
 }
 
+// Threads per bead in the step kernel.  A bead's pair entries (native
+// contacts, disulfides, Verlet row, quasi-adiabatic contacts) are spread over
+// its LPB lanes and their partial forces combined by shuffles in a fixed
+// order; its bonded centres are split in two tasks; its integrator runs one
+// axis per lane, with the generator, the new position and the skin test on
+// the fourth.  The lanes of a bead are adjacent threads of one warp.
+constexpr int LPB = 4;
+
+// sum of the bead's four lane partials, the same bits on every lane
+// ((a0 + a1) + (a2 + a3): each step adds a lane's value to its partner's,
+// which is commutative bit for bit for FP64 and for the float-float sum)
+__device__ __forceinline__ double quad_sum(unsigned m, double v) {
+    v += __shfl_xor_sync(m, v, 1, LPB);
+    v += __shfl_xor_sync(m, v, 2, LPB);
+    return v;
+}
+__device__ __forceinline__ FF quad_sum(unsigned m, FF v) {
+    v = ff_add(v, FF{__shfl_xor_sync(m, v.h, 1, LPB), __shfl_xor_sync(m, v.l, 1, LPB)});
+    v = ff_add(v, FF{__shfl_xor_sync(m, v.h, 2, LPB), __shfl_xor_sync(m, v.l, 2, LPB)});
+    return v;
+}
+template <class FT> __device__ __forceinline__ void quad_sum(unsigned m, Acc3<FT> &a) {
+    a.x = quad_sum(m, a.x);
+    a.y = quad_sum(m, a.y);
+    a.z = quad_sum(m, a.z);
+}
+__device__ __forceinline__ double comp3(double4_32a v, int a) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); }
+
 template <class FT, int MODE, int FBT>
 __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cur) {
+    constexpr int NT = FBT * LPB;
     const double4_32a *__restrict__ pin = d.pos[cur];
     const int N = d.N, t = threadIdx.x, i0 = blockIdx.x * FBT;
+    const int bs = t / LPB, ln = t % LPB;   // bead slot in the block, lane of the bead
+    const int i = i0 + bs;
+    const unsigned qm = 0xFu << ((t & 31) & ~(LPB - 1));   // the bead's lanes in the warp
     __shared__ double4_32a P[FBT + 6];
     __shared__ V3<FT> Ct[FBT + 3], Ca[3][FBT + 3], Cd[4][FBT + 3];
     // mixed path: every position of the tile split into float-float parts
@@ -269,43 +301,50 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
     __shared__ P2 S[sizeof(FT) == 4 ? FBT + 6 : 1];
     __shared__ V3<FF> Eff[NE], Xff[NE];
     __shared__ V3<float> Ef[NE], Xf[NE];
+    // quasi-adiabatic contact slots of each bead, in ascending order
+    __shared__ int Qs[FBT][QA_REF_CAP];
 
     // mixed path: the integrator's per-bead state does not depend on the
     // forces, so its loads are issued first and their latency passes under
-    // the force work (the FP64 path is bound by its FP64 pipe instead and
-    // loads them where they are used)
+    // the force work (lanes 0-2 their axis of the history, lane 3 the
+    // generator and the list origin); the FP64 path is bound by its FP64
+    // pipe instead and loads them where they are used
     constexpr bool EARLY = MODE == 1 && sizeof(FT) == 4;
-    double yv[15];
+    const bool live = i < N;
+    double yv[5];
     uint64_t st0 = 0;
     double4_32a o_i = make_double4_32a(0, 0, 0, 0);
     int pf_n0 = 0, pf_n1 = 0, pf_cnt = 0;   // the pair loops' bounds, loaded first too
-    if (i0 + t < N) {
-        pf_n0 = d.nat_start[i0 + t];
-        pf_n1 = d.nat_end[i0 + t];
-        pf_cnt = d.nl_cnt[i0 + t];
+    if (live) {
+        pf_n0 = d.nat_start[i];
+        pf_n1 = d.nat_end[i];
+        pf_cnt = d.nl_cnt[i];
     }
-    if (EARLY && i0 + t < N) {
-        const size_t Ns = (size_t)N;
+    const size_t Ns = (size_t)N;
+    if (EARLY && live) {
+        if (ln < 3) {
 #pragma unroll
-        for (int q = 0; q < 15; ++q) yv[q] = d.yh[q * Ns + i0 + t];
-        st0 = d.rng[i0 + t];
-        o_i = d.orig[i0 + t];
+            for (int q = 0; q < 5; ++q) yv[q] = d.yh[(size_t)(q * 3 + ln) * Ns + i];
+        } else {
+            st0 = d.rng[i];
+            o_i = d.orig[i];
+        }
     }
 
-    for (int k = t; k < FBT + 6; k += FBT) {
+    for (int k = t; k < FBT + 6; k += NT) {
         int idx = i0 - 3 + k;
         P[k] = (idx >= 0 && idx < N) ? pin[idx] : make_double4_32a(0, 0, 0, 0);
         if constexpr (sizeof(FT) == 4) S[k] = split_p(P[k]);
     }
     __syncthreads();
     if constexpr (sizeof(FT) == 4) {
-        for (int k = t; k < NE; k += FBT) {
+        for (int k = t; k < NE; k += NT) {
             const V3<FF> e{ff_diff(S[k].x, S[k + 1].x), ff_diff(S[k].y, S[k + 1].y), ff_diff(S[k].z, S[k + 1].z)};
             Eff[k] = e;
             Ef[k] = V3<float>{e.x.h, e.y.h, e.z.h};
         }
         __syncthreads();
-        for (int k = t + 1; k < NE; k += FBT) {
+        for (int k = t + 1; k < NE; k += NT) {
             const V3<FF> x = ff_cross(Eff[k - 1], Eff[k]);
             Xff[k] = x;
             Xf[k] = V3<float>{x.x.h, x.y.h, x.z.h};
@@ -313,137 +352,163 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
         __syncthreads();
     }
 
-    // bonded contributions of centres c in [i0-2, i0+FBT]
-    for (int sc = t; sc < FBT + 3; sc += FBT) {
-        int c = i0 - 2 + sc;
-        uint32_t fl = (c >= 0 && c < N) ? d.bflags[c] : 0u;
-        V3<FT> z{FT(0), FT(0), FT(0)};
-        V3<FT> ft = z, a1 = z, a2 = z, a3 = z, q[4] = {z, z, z, z};
-        int sp = c - (i0 - 3);
-        bool own = (c >= i0 && c < i0 + FBT && c < N);
-        int rc = own ? d.rep_of[c] : 0;
-        if ((fl & BF_TETH) && p.on[XMD_TERM_TETHER]) {
-            FT V_;
-            if constexpr (sizeof(FT) == 4) ft = tether_vec(p, Ef[sp], d.bond_f[c].x, &V_);
-            else ft = tether_term<FT>(p, P[sp], P[sp + 1], (FT)d.teth_r0[c], &V_);
-            if (MODE == 0 && own) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_TETHER], (double)V_);
-        }
+    // bonded contributions of centres c in [i0-2, i0+FBT], two tasks per
+    // centre: (tether, angle) and (dihedral, chirality)
+    for (int w = t; w < 2 * (FBT + 3); w += NT) {
+        const int sc = w >> 1, task = w & 1;
+        const int c = i0 - 2 + sc;
+        const uint32_t fl = (c >= 0 && c < N) ? d.bflags[c] : 0u;
+        const V3<FT> z{FT(0), FT(0), FT(0)};
+        const int sp = c - (i0 - 3);
+        const bool own = (c >= i0 && c < i0 + FBT && c < N);
+        const int rc = own ? d.rep_of[c] : 0;
         // a centre's angle and dihedral are native or heuristic (seq-file
         // models: those without a native value); both kinds share one call
-        const bool h_ang = (fl & BF_HANG) && p.on[XMD_TERM_HEUR_ANG];
-        const bool h_dih = (fl & BF_HDIH) && p.on[XMD_TERM_HEUR_DIH];
-        const bool do_ang = ((fl & BF_ANG) && p.on[XMD_TERM_NAT_ANG]) || h_ang;
-        const bool do_dih = ((fl & BF_DIH) && (p.on[XMD_TERM_CND] || p.on[XMD_TERM_SND])) || h_dih;
-        const double *hac = h_ang ? d.heur_ang + 7 * ((fl >> BF_HANG_SHIFT) & 15u) : nullptr;
-        const int hdt = (int)((fl >> BF_HDIH_SHIFT) & 15u);
-        const int ang_slot = h_ang ? XMD_TERM_HEUR_ANG : XMD_TERM_NAT_ANG;
-        if constexpr (sizeof(FT) == 8) {
-            if (do_ang) {
+        if (task == 0) {
+            V3<FT> ft = z, a1 = z, a2 = z, a3 = z;
+            if ((fl & BF_TETH) && p.on[XMD_TERM_TETHER]) {
                 FT V_;
-                angle_term<FT>(p, P[sp - 1], P[sp], P[sp + 1], (FT)d.ang_t0[c], hac, &a1, &a2, &a3, &V_);
-                if (MODE == 0 && own) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + ang_slot], (double)V_);
-            }
-            if (do_dih) {
-                FT Vc, Vs;
-                dihedral_term<FT>(p, P[sp - 1], P[sp], P[sp + 1], P[sp + 2], (FT)d.dih_p0[c],
-                                  p.on[XMD_TERM_CND] != 0, p.on[XMD_TERM_SND] != 0,
-                                  h_dih ? d.heur_dih + 6 * hdt : nullptr, q, &Vc, &Vs);
-                if (MODE == 0 && own) {
-                    if (h_dih) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_HEUR_DIH], (double)Vc);
-                    else {
-                        if (p.on[XMD_TERM_CND]) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_CND], (double)Vc);
-                        if (p.on[XMD_TERM_SND]) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_SND], (double)Vs);
-                    }
+                if constexpr (sizeof(FT) == 4) ft = tether_vec(p, Ef[sp], d.bond_f[c].x, &V_);
+                else {
+                    DN Vn;
+                    ft = v3d(tether_term<DN>(p, P[sp], P[sp + 1], DN(d.teth_r0[c]), &Vn));
+                    V_ = (double)Vn;
                 }
+                if (MODE == 0 && own) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_TETHER], (double)V_);
             }
-        } else if (do_ang || do_dih) {
-            // mixed path: FP64 bond vectors and cross products (shared slots),
-            // FP32 forces
+            const bool h_ang = (fl & BF_HANG) && p.on[XMD_TERM_HEUR_ANG];
+            const bool do_ang = ((fl & BF_ANG) && p.on[XMD_TERM_NAT_ANG]) || h_ang;
+            const double *hac = h_ang ? d.heur_ang + 7 * ((fl >> BF_HANG_SHIFT) & 15u) : nullptr;
+            const int ang_slot = h_ang ? XMD_TERM_HEUR_ANG : XMD_TERM_NAT_ANG;
             if (do_ang) {
-                float V_;
-                angle_mixed(p, Ef[sp - 1], Ef[sp], Xf[sp], d.bond_f[c].y, hac, &a1, &a2, &a3, &V_);
-                if (MODE == 0 && own) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + ang_slot], (double)V_);
+                double V_;
+                if constexpr (sizeof(FT) == 8) {
+                    // every operation rounded on its own (DN), as the
+                    // reference's uncontracted build: near-straight triples
+                    // make the bonded terms ill-conditioned
+                    V3<DN> b1, b2, b3;
+                    DN Vn;
+                    angle_term<DN>(p, P[sp - 1], P[sp], P[sp + 1], DN(d.ang_t0[c]), hac, &b1, &b2, &b3, &Vn);
+                    a1 = v3d(b1); a2 = v3d(b2); a3 = v3d(b3);
+                    V_ = (double)Vn;
+                } else {
+                    // mixed path: float-float bond vectors and cross products
+                    // (shared slots), FP32 forces
+                    float Vf;
+                    angle_mixed(p, Ef[sp - 1], Ef[sp], Xf[sp], d.bond_f[c].y, hac, &a1, &a2, &a3, &Vf);
+                    V_ = (double)Vf;
+                }
+                if (MODE == 0 && own) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + ang_slot], V_);
             }
+            Ct[sc] = ft;
+            Ca[0][sc] = a1; Ca[1][sc] = a2; Ca[2][sc] = a3;
+        } else {
+            V3<FT> q[4] = {z, z, z, z};
+            const bool h_dih = (fl & BF_HDIH) && p.on[XMD_TERM_HEUR_DIH];
+            const bool do_dih = ((fl & BF_DIH) && (p.on[XMD_TERM_CND] || p.on[XMD_TERM_SND])) || h_dih;
+            const int hdt = (int)((fl >> BF_HDIH_SHIFT) & 15u);
             if (do_dih) {
-                float Vc, Vs;
-                const float X = dot(Xf[sp], Xf[sp + 1]), T = ff_dot(Xff[sp], Eff[sp + 1]).h;
-                dihedral_mixed(p, Ef[sp - 1], Ef[sp], Ef[sp + 1], Xf[sp], Xf[sp + 1], X, T, d.bond_f[c].z,
-                               p.on[XMD_TERM_CND] != 0, p.on[XMD_TERM_SND] != 0,
-                               h_dih ? d.heur_dih_f + 6 * hdt : nullptr, q, &Vc, &Vs);
+                double Vc, Vs;
+                if constexpr (sizeof(FT) == 8) {
+                    V3<DN> qn[4];
+                    DN Vcn, Vsn;
+                    dihedral_term<DN>(p, P[sp - 1], P[sp], P[sp + 1], P[sp + 2], DN(d.dih_p0[c]),
+                                      p.on[XMD_TERM_CND] != 0, p.on[XMD_TERM_SND] != 0,
+                                      h_dih ? reinterpret_cast<const DN *>(d.heur_dih) + 6 * hdt : nullptr, qn,
+                                      &Vcn, &Vsn);
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) q[k] = v3d(qn[k]);
+                    Vc = (double)Vcn;
+                    Vs = (double)Vsn;
+                } else {
+                    float Vcf, Vsf;
+                    const float X = dot(Xf[sp], Xf[sp + 1]), T = ff_dot(Xff[sp], Eff[sp + 1]).h;
+                    dihedral_mixed(p, Ef[sp - 1], Ef[sp], Ef[sp + 1], Xf[sp], Xf[sp + 1], X, T, d.bond_f[c].z,
+                                   p.on[XMD_TERM_CND] != 0, p.on[XMD_TERM_SND] != 0,
+                                   h_dih ? d.heur_dih_f + 6 * hdt : nullptr, q, &Vcf, &Vsf);
+                    Vc = (double)Vcf;
+                    Vs = (double)Vsf;
+                }
                 if (MODE == 0 && own) {
-                    if (h_dih) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_HEUR_DIH], (double)Vc);
+                    if (h_dih) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_HEUR_DIH], Vc);
                     else {
-                        if (p.on[XMD_TERM_CND]) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_CND], (double)Vc);
-                        if (p.on[XMD_TERM_SND]) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_SND], (double)Vs);
+                        if (p.on[XMD_TERM_CND]) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_CND], Vc);
+                        if (p.on[XMD_TERM_SND]) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_SND], Vs);
                     }
                 }
             }
-        }
-        // chirality of the quad (c-1, c, c+1, c+2): eval_chiral_forces::iter,
-        // chiral.cpp:15-37; its forces join the dihedral slots of the centre
-        if ((fl & BF_CHIR) && p.on[XMD_TERM_CHIR]) {
-            V3<FT> g[4];
-            FT Vch;
-            if constexpr (sizeof(FT) == 8) {
-                const double2 cp = d.chir[c];
-                chiral_term<FT>(p, P[sp - 1], P[sp], P[sp + 1], P[sp + 2], (FT)cp.x, (FT)cp.y, g, &Vch);
-            } else {
-                const float2 cp = d.chir_f32[c];
-                // the triple product in float-float: planar quads are well conditioned
-                const float tp = ff_dot(Eff[sp - 1], Xff[sp + 1]).h;
-                chiral_mixed(p, Ef[sp - 1], Ef[sp], Ef[sp + 1], Xf[sp], Xf[sp + 1], tp, cp.x, cp.y, g, &Vch);
-            }
+            // chirality of the quad (c-1, c, c+1, c+2): eval_chiral_forces::iter,
+            // chiral.cpp:15-37; its forces join the dihedral slots of the centre
+            if ((fl & BF_CHIR) && p.on[XMD_TERM_CHIR]) {
+                V3<FT> g[4];
+                double Vch;
+                if constexpr (sizeof(FT) == 8) {
+                    const double2 cp = d.chir[c];
+                    V3<DN> gn[4];
+                    DN Vn;
+                    chiral_term<DN>(p, P[sp - 1], P[sp], P[sp + 1], P[sp + 2], DN(cp.x), DN(cp.y), gn, &Vn);
 #pragma unroll
-            for (int k = 0; k < 4; ++k) q[k] = q[k] + g[k];
-            if (MODE == 0 && own) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_CHIR], (double)Vch);
+                    for (int k = 0; k < 4; ++k) g[k] = v3d(gn[k]);
+                    Vch = (double)Vn;
+                } else {
+                    const float2 cp = d.chir_f32[c];
+                    // the triple product in float-float: planar quads are well conditioned
+                    const float tp = ff_dot(Eff[sp - 1], Xff[sp + 1]).h;
+                    float Vf;
+                    chiral_mixed(p, Ef[sp - 1], Ef[sp], Ef[sp + 1], Xf[sp], Xf[sp + 1], tp, cp.x, cp.y, g, &Vf);
+                    Vch = (double)Vf;
+                }
+#pragma unroll
+                for (int k = 0; k < 4; ++k) q[k] = q[k] + g[k];
+                if (MODE == 0 && own) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_CHIR], Vch);
+            }
+            Cd[0][sc] = q[0]; Cd[1][sc] = q[1]; Cd[2][sc] = q[2]; Cd[3][sc] = q[3];
         }
-        Ct[sc] = ft;
-        Ca[0][sc] = a1; Ca[1][sc] = a2; Ca[2][sc] = a3;
-        Cd[0][sc] = q[0]; Cd[1][sc] = q[1]; Cd[2][sc] = q[2]; Cd[3][sc] = q[3];
     }
     __syncthreads();
 
-    const int i = i0 + t;
-    if (i >= N) return;
+    // from here on, the four lanes of a bead take the same branches
+    if (!live) return;
     const int r = d.rep_of[i];
     if (r < 0) return;     // free bead slot
     if (MODE == 1 && d.rep[r].steps_left == 0) {
         // the replica has taken its steps: it keeps its state (both buffers)
-        d.pos[cur ^ 1][i] = P[t + 3];
+        if (ln == LPB - 1) d.pos[cur ^ 1][i] = P[bs + 3];
         return;
     }
-    const int s = t + 2;   // centre slot of bead i
+    const int s = bs + 2;   // centre slot of bead i
     Acc3<FT> acc;
-    if constexpr (sizeof(FT) == 4) {
-        // the bonded contributions, computed in FP32, are summed in FP32 and
-        // enter the float-float accumulator once
-        V3<float> bsum = Ct[s] - Ct[s - 1] + Ca[2][s - 1] + Ca[1][s] + Ca[0][s + 1] + Cd[0][s + 1] + Cd[1][s] +
-                         Cd[2][s - 1] + Cd[3][s - 2];
-        acc.add(bsum);
-    } else {
-        acc.add(Ct[s]);
-        acc.sub(Ct[s - 1]);
-        acc.add(Ca[2][s - 1]);
-        acc.add(Ca[1][s]);
-        acc.add(Ca[0][s + 1]);
-        acc.add(Cd[0][s + 1]);
-        acc.add(Cd[1][s]);
-        acc.add(Cd[2][s - 1]);
-        acc.add(Cd[3][s - 2]);
+    if (ln == 0) {
+        if constexpr (sizeof(FT) == 4) {
+            // the bonded contributions, computed in FP32, are summed in FP32
+            // and enter the float-float accumulator once
+            V3<float> bsum = Ct[s] - Ct[s - 1] + Ca[2][s - 1] + Ca[1][s] + Ca[0][s + 1] + Cd[0][s + 1] +
+                             Cd[1][s] + Cd[2][s - 1] + Cd[3][s - 2];
+            acc.add(bsum);
+        } else {
+            acc.add(Ct[s]);
+            acc.sub(Ct[s - 1]);
+            acc.add(Ca[2][s - 1]);
+            acc.add(Ca[1][s]);
+            acc.add(Ca[0][s + 1]);
+            acc.add(Cd[0][s + 1]);
+            acc.add(Cd[1][s]);
+            acc.add(Cd[2][s - 1]);
+            acc.add(Cd[3][s - 2]);
+        }
     }
 
-    const double4_32a pi = P[t + 3];
+    const double4_32a pi = P[bs + 3];
     const BoxD bx = d.rep[r].box;
     const bool per = (d.rep[r].per[0] | d.rep[r].per[1] | d.rep[r].per[2]) != 0;
     const PairGeo<FT> geo(bx, per, pi);
     double vgo = 0, vpa = 0, ves = 0;
 
-    // Both pair loops are software-pipelined: the next entry (native index
-    // data, or row entry) is loaded while the current partner's position is
-    // fetched, so each iteration waits on one load instead of a chain.  The
-    // summation order is unchanged.
+    // Each lane takes every LPB-th entry of the bead's lists.  The loops are
+    // software-pipelined: the next entry (native index data, or row entry)
+    // is loaded while the current partner's position is fetched.
     if (p.on[XMD_TERM_GO]) {
-        int k = pf_n0;
+        int k = pf_n0 + ln;
         const int k1 = pf_n1;
         int j = 0;
         bool on = false;
@@ -453,14 +518,14 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
             on = d.nat_on[k] != 0;
             nd = nat_dist<FT>(d, k);
         }
-        for (; k < k1; ++k) {
+        for (; k < k1; k += LPB) {
             int jn = 0;
             bool onn = false;
             FT ndn = FT(0);
-            if (k + 1 < k1) {
-                jn = d.nat_j[k + 1];
-                onn = d.nat_on[k + 1] != 0;
-                ndn = nat_dist<FT>(d, k + 1);
+            if (k + LPB < k1) {
+                jn = d.nat_j[k + LPB];
+                onn = d.nat_on[k + LPB] != 0;
+                ndn = nat_dist<FT>(d, k + LPB);
             }
             if (on) {
                 FT V_;
@@ -476,7 +541,7 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
     double vss = 0;
     if (p.on[XMD_TERM_NAT_SS]) {
         const int s1 = d.ss_end[i];
-        for (int k = d.ss_start[i]; k < s1; ++k) {
+        for (int k = d.ss_start[i] + ln; k < s1; k += LPB) {
             if (!d.ss_on[k]) continue;
             const int j = d.ss_j[k];
             FT V_;
@@ -486,10 +551,10 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
         }
     }
     const int cnt = pf_cnt;
-    int e_next = cnt > 0 ? d.nl_row[i] : 0;
-    for (int k = 0; k < cnt; ++k) {
+    int e_next = ln < cnt ? d.nl_row[(size_t)ln * N + i] : 0;
+    for (int k = ln; k < cnt; k += LPB) {
         const int e = e_next;
-        if (k + 1 < cnt) e_next = d.nl_row[(size_t)(k + 1) * N + i];
+        if (k + LPB < cnt) e_next = d.nl_row[(size_t)(k + LPB) * N + i];
         int j = e & NL_MASK;
         double4_32a pj = pin[j];
         V3<FT> r12 = geo.to(pj);
@@ -508,21 +573,38 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
     }
 
     // quasi-adiabatic contacts: the force part of process_contacts::iter
-    // (process_contacts.cpp:25-40), summed in contact-slot order
+    // (process_contacts.cpp:25-40).  The bead's contact slots (at most
+    // QA_REF_CAP, held four per lane) are put in ascending order by rank, and
+    // lane l takes the l-th, (l+4)-th, ... of them.
     double vqa = 0;
     if (d.qa_on && p.on[XMD_TERM_QA]) {
         const QaDev &q = d.qa;
-        int nref = min(q.ref_cnt[i], QA_REF_CAP);
-        int sl[QA_REF_CAP];
-        for (int k = 0; k < nref; ++k) sl[k] = q.ref[(size_t)k * N + i];
-        for (int x = 1; x < nref; ++x) {
-            int v = sl[x], y = x - 1;
-            while (y >= 0 && sl[y] > v) { sl[y + 1] = sl[y]; --y; }
-            sl[y + 1] = v;
+        const int nref = min(q.ref_cnt[i], QA_REF_CAP);
+        constexpr int HOLD = QA_REF_CAP / LPB;
+        int v[HOLD], rk[HOLD];
+#pragma unroll
+        for (int u = 0; u < HOLD; ++u) {
+            const int k = u * LPB + ln;
+            v[u] = k < nref ? q.ref[(size_t)k * N + i] : INT_MAX;
+            rk[u] = 0;
         }
+        for (int m = 0; m < nref; ++m) {
+            int x = 0;
+#pragma unroll
+            for (int u = 0; u < HOLD; ++u) {
+                const int y = __shfl_sync(qm, v[u], m % LPB, LPB);
+                if (m / LPB == u) x = y;
+            }
+#pragma unroll
+            for (int u = 0; u < HOLD; ++u) rk[u] += x < v[u];
+        }
+#pragma unroll
+        for (int u = 0; u < HOLD; ++u)
+            if (u * LPB + ln < nref) Qs[bs][rk[u]] = v[u];
+        __syncwarp(qm);
         const double tnow = d.rep[r].t;
-        for (int k = 0; k < nref; ++k) {
-            int slot = sl[k];
+        for (int k = ln; k < nref; k += LPB) {
+            const int slot = Qs[bs][k];
             int i1 = q.ct_i1[slot], i2 = q.ct_i2[slot];
             V3<FT> r12 = geo.between(pin[i1], pin[i2]);
             FT r12_rn = ninv(r12);
@@ -538,17 +620,18 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
             else acc.sub(f);
             if (MODE == 0 && i == i1) vqa += sat * (double)V_;
         }
-        if (MODE == 1) {
+        if (MODE == 1 && ln == LPB - 1) {
             // n and h at this step's positions (precompute_nh.cpp:12-20)
             D3 n{0, 0, 0}, h{0, 0, 0};
             const uint32_t fl = d.bflags[i];
-            if ((fl & BF_PREV) && (fl & BF_NEXT)) qa_nh(P[t + 2], P[t + 3], P[t + 4], &n, &h);
-            const size_t Ns = (size_t)N;
+            if ((fl & BF_PREV) && (fl & BF_NEXT)) qa_nh(P[bs + 2], P[bs + 3], P[bs + 4], &n, &h);
             q.nh[i] = n.x; q.nh[Ns + i] = n.y; q.nh[2 * Ns + i] = n.z;
             q.nh[3 * Ns + i] = h.x; q.nh[4 * Ns + i] = h.y; q.nh[5 * Ns + i] = h.z;
         }
     }
 
+    // the bead's force: its lanes' partial sums combined (every lane holds it)
+    quad_sum(qm, acc);
     V3<double> ftot = acc.total();
     if (p.ext_on) {
         // AFM pulls and walls, from k_ext (launched just before)
@@ -559,94 +642,114 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
         // the replica is frozen from the next step on (its skin check sets
         // steps_left = 0); this bead keeps its state, so no non-finite
         // position ever reaches a list build
-        atomicOr(d.status, ST_NONFINITE);
+        if (ln == 0) atomicOr(d.status, ST_NONFINITE);
         if (MODE == 1) {
-            d.rep[r].fault = 1;
-            d.pos[cur ^ 1][i] = pi;
+            if (ln == LPB - 1) {
+                d.rep[r].fault = 1;
+                d.pos[cur ^ 1][i] = pi;
+            }
             return;
         }
     }
 
     if (MODE == 0) {
-        d.F[3 * i] = fx;
-        d.F[3 * i + 1] = fy;
-        d.F[3 * i + 2] = fz;
-        double *Vr = d.Vrep + r * XMD_NUM_TERMS;
-        if (vgo != 0.0) atomicAdd(&Vr[XMD_TERM_GO], vgo);
-        if (vpa != 0.0) atomicAdd(&Vr[XMD_TERM_PAULI], vpa);
-        if (ves != 0.0) atomicAdd(&Vr[p.es_rel ? XMD_TERM_REL_ES : XMD_TERM_CONST_ES], ves);
-        if (vqa != 0.0) atomicAdd(&Vr[XMD_TERM_QA], vqa);
-        if (vss != 0.0) atomicAdd(&Vr[XMD_TERM_NAT_SS], vss);
+        if (ln < 3) d.F[3 * (size_t)i + ln] = ln == 0 ? fx : (ln == 1 ? fy : fz);
+        vgo = quad_sum(qm, vgo);
+        vpa = quad_sum(qm, vpa);
+        ves = quad_sum(qm, ves);
+        vqa = quad_sum(qm, vqa);
+        vss = quad_sum(qm, vss);
+        if (ln == 0) {
+            double *Vr = d.Vrep + r * XMD_NUM_TERMS;
+            if (vgo != 0.0) atomicAdd(&Vr[XMD_TERM_GO], vgo);
+            if (vpa != 0.0) atomicAdd(&Vr[XMD_TERM_PAULI], vpa);
+            if (ves != 0.0) atomicAdd(&Vr[p.es_rel ? XMD_TERM_REL_ES : XMD_TERM_CONST_ES], ves);
+            if (vqa != 0.0) atomicAdd(&Vr[XMD_TERM_QA], vqa);
+            if (vss != 0.0) atomicAdd(&Vr[XMD_TERM_NAT_SS], vss);
+        }
         return;
     }
 
     // ---- lang_pc_step::operator(), lang_pc.cpp:11-37, mass = 1 (main.cpp:156) ----
-    if (!EARLY) {
-        st0 = d.rng[i];
-        o_i = d.orig[i];
+    // lane 3: the bead's four generator draws, three normals
+    double nz0 = 0.0, nz1 = 0.0, nz2 = 0.0;
+    if (ln == LPB - 1) {
+        if (!EARLY) {
+            st0 = d.rng[i];
+            o_i = d.orig[i];
+        }
+        uint64_t st = st0;
+        if constexpr (sizeof(FT) == 8) {
+            noise3(st, &nz0, &nz1, &nz2);
+        } else {
+            float a, b, c;
+            noise3m(st, &a, &b, &c);
+            nz0 = widen_f(a);
+            nz1 = widen_f(b);
+            nz2 = widen_f(c);
+        }
+        d.rng[i] = gf2_apply_nib(d.jump + JUMP_WORDS * r, st);
     }
-    uint64_t st = st0;
-    double nz[3];
-    if constexpr (sizeof(FT) == 8) {
-        noise3(st, &nz[0], &nz[1], &nz[2]);
-    } else {
-        float a, b, c;
-        noise3m(st, &a, &b, &c);
-        nz[0] = widen_f(a);
-        nz[1] = widen_f(b);
-        nz[2] = widen_f(c);
-    }
-    d.rng[i] = gf2_apply_nib(d.jump + JUMP_WORDS * r, st);
-    const double dt_inv = p.dt_inv, h = p.dt2_half;
-    const double gamma = p.gamma_factor * 1.0;
-    const double nsd = d.rep[r].noise_sd;
-    const double F3[3] = {fx, fy, fz};
-    double y0[3] = {pi.x, pi.y, pi.z};
-    double *yh = d.yh;
-    const size_t Ns = (size_t)N;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
+    nz0 = __shfl_sync(qm, nz0, LPB - 1, LPB);
+    nz1 = __shfl_sync(qm, nz1, LPB - 1, LPB);
+    nz2 = __shfl_sync(qm, nz2, LPB - 1, LPB);
+    // lanes 0-2: the Gear-5 corrector and predictor of their axis
+    double y0 = 0.0;
+    if (ln < 3) {
+        const double dt_inv = p.dt_inv, h = p.dt2_half;
+        const double gamma = p.gamma_factor * 1.0;
+        const double nsd = d.rep[r].noise_sd;
+        const double Fa = ln == 0 ? fx : (ln == 1 ? fy : fz);
+        const double nza = ln == 0 ? nz0 : (ln == 1 ? nz1 : nz2);
+        double *yh = d.yh;
+        y0 = comp3(pi, ln);
         double y1, y2, y3, y4, y5;
         if constexpr (EARLY) {
-            y1 = yv[0 * 3 + a]; y2 = yv[1 * 3 + a]; y3 = yv[2 * 3 + a]; y4 = yv[3 * 3 + a]; y5 = yv[4 * 3 + a];
+            y1 = yv[0]; y2 = yv[1]; y3 = yv[2]; y4 = yv[3]; y5 = yv[4];
         } else {
-            y1 = yh[(0 * 3 + a) * Ns + i]; y2 = yh[(1 * 3 + a) * Ns + i]; y3 = yh[(2 * 3 + a) * Ns + i];
-            y4 = yh[(3 * 3 + a) * Ns + i]; y5 = yh[(4 * 3 + a) * Ns + i];
+            y1 = yh[(size_t)(0 * 3 + ln) * Ns + i]; y2 = yh[(size_t)(1 * 3 + ln) * Ns + i];
+            y3 = yh[(size_t)(2 * 3 + ln) * Ns + i]; y4 = yh[(size_t)(3 * 3 + ln) * Ns + i];
+            y5 = yh[(size_t)(4 * 3 + ln) * Ns + i];
         }
         double v = y1 * dt_inv;
-        double a_ = F3[a] * 1.0 - gamma * v + nsd * nz[a];
+        double a_ = Fa * 1.0 - gamma * v + nsd * nza;
         double error = y2 - a_ * h;
-        y0[a] -= 3.0 / 16.0 * error;
+        y0 -= 3.0 / 16.0 * error;
         y1 -= 251.0 / 360.0 * error;
         y2 -= 1.0 * error;
         y3 -= 11.0 / 18.0 * error;
         y4 -= 1.0 / 6.0 * error;
         y5 -= 1.0 / 60.0 * error;
-        y0[a] += y1 + y2 + y3 + y4 + y5;
+        y0 += y1 + y2 + y3 + y4 + y5;
         y1 += 2.0 * y2 + 3.0 * y3 + 4.0 * y4 + 5.0 * y5;
         y2 += 3.0 * y3 + 6.0 * y4 + 10.0 * y5;
         y3 += 4.0 * y4 + 10.0 * y5;
         y4 += 5.0 * y5;
-        yh[(0 * 3 + a) * Ns + i] = y1;
-        yh[(1 * 3 + a) * Ns + i] = y2;
-        yh[(2 * 3 + a) * Ns + i] = y3;
-        yh[(3 * 3 + a) * Ns + i] = y4;
-        yh[(4 * 3 + a) * Ns + i] = y5;
+        yh[(size_t)(0 * 3 + ln) * Ns + i] = y1;
+        yh[(size_t)(1 * 3 + ln) * Ns + i] = y2;
+        yh[(size_t)(2 * 3 + ln) * Ns + i] = y3;
+        yh[(size_t)(3 * 3 + ln) * Ns + i] = y4;
+        yh[(size_t)(4 * 3 + ln) * Ns + i] = y5;
     }
-    double4_32a pn = make_double4_32a(y0[0], y0[1], y0[2], pi.w);
-    d.pos[cur ^ 1][i] = pn;
-    // skin test displacement: norm(box->r_uv(r_, orig_r_)), verify.cpp:12-14
-    // squared; the check takes one square root of the maximum (sqrt is
-    // monotone and correctly rounded, so that equals the max of the norms)
-    double disp;
-    if constexpr (sizeof(FT) == 4) {
-        // mixed path: the displacement from split positions (the FP64
-        // difference to FP32 accuracy), squared in FP32
-        const V3<float> e = geo.between(o_i, pn);
-        disp = widen_f(e.x * e.x + e.y * e.y + e.z * e.z);
-    } else {
-        // on open axes the wrap subtracts exactly zero: skipping it changes no bit
-        disp = per ? dist2_exact(bx, pn, o_i) : dist2_open(pn, o_i);
+    // lane 3: the new position and the skin-test displacement
+    const double px = __shfl_sync(qm, y0, 0, LPB), py = __shfl_sync(qm, y0, 1, LPB);
+    const double pz = __shfl_sync(qm, y0, 2, LPB);
+    double disp = 0.0;
+    if (ln == LPB - 1) {
+        const double4_32a pn = make_double4_32a(px, py, pz, pi.w);
+        d.pos[cur ^ 1][i] = pn;
+        // skin test displacement: norm(box->r_uv(r_, orig_r_)), verify.cpp:12-14
+        // squared; the check takes one square root of the maximum (sqrt is
+        // monotone and correctly rounded, so that equals the max of the norms)
+        if constexpr (sizeof(FT) == 4) {
+            // mixed path: the displacement from split positions (the FP64
+            // difference to FP32 accuracy), squared in FP32
+            const V3<float> e = geo.between(o_i, pn);
+            disp = widen_f(e.x * e.x + e.y * e.y + e.z * e.z);
+        } else {
+            // on open axes the wrap subtracts exactly zero: skipping it changes no bit
+            disp = per ? dist2_exact(bx, pn, o_i) : dist2_open(pn, o_i);
+        }
     }
     const unsigned lane = t & 31;
     int r0 = __shfl_sync(0xffffffffu & __activemask(), r, 0);
@@ -654,7 +757,7 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
     if (__all_sync(mask, r == r0) && mask == 0xffffffffu) {
         const unsigned long long m = warp_max_bits((unsigned long long)__double_as_longlong(disp));
         if (lane == 0) atomicMax(&d.rep[r].maxdisp, m);
-    } else {
+    } else if (ln == LPB - 1) {
         atomicMax(&d.rep[r].maxdisp, (unsigned long long)__double_as_longlong(disp));
     }
 }
@@ -713,7 +816,7 @@ __global__ void k_nl_check(Dev d, int advance, double dt, cudaGraphConditionalHa
 // replica and sets the graph's rebuild condition, so a step is one launch
 // plus the conditional rebuild.
 template <class FT, int MODE, int FBT>
-__global__ void __launch_bounds__(FBT) k_force(Dev d, TermP p, int cur, cudaGraphConditionalHandle h, int fuse) {
+__global__ void __launch_bounds__(FBT * LPB) k_force(Dev d, TermP p, int cur, cudaGraphConditionalHandle h, int fuse) {
     __shared__ int last_s;
     static_assert(FBT % BLK_ON == 0, "force blocks are whole multiples of the occupancy granule");
     bool on = false;
@@ -1049,7 +1152,6 @@ __global__ void __launch_bounds__(NC_WARPS * 32, 3) k_nl_cells(Dev d, TermP p, i
     // first occurrence of each key in lane order
     const unsigned same = __match_any_sync(FULL, key);
     const bool lead = key >= 0 && (same & lt) == 0u;
-    unsigned todo = __ballot_sync(FULL, lead);
     // each lead lane fetches its bucket's range up front
     int kq0 = 0, kq1 = 0;
     if (lead) {
@@ -1088,16 +1190,33 @@ __global__ void __launch_bounds__(NC_WARPS * 32, 3) k_nl_cells(Dev d, TermP p, i
     const float qi_w = narrow_f(pi.w);
     const int cap = d.nl_cap;
     int cnt = 0, tcnt = 0;
-    while (todo) {
-        const int src = __ffs(todo) - 1;
-        todo &= todo - 1;
-        const int q0 = __shfl_sync(FULL, kq0, src), q1 = __shfl_sync(FULL, kq1, src);
-        for (int qb = q0; qb < q1; qb += 32) {
-            const int q = qb + lane;
+    // the buckets' candidates as one sequence (lead lanes in lane order, each
+    // bucket in its ascending bead order), taken 32 at a time: lane l takes
+    // entry g = base + l, which lies in the bucket of the last lane whose
+    // exclusive prefix of bucket sizes is <= g
+    const int csz = kq1 - kq0;
+    int pre = csz;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL, pre, o);
+        if (lane >= o) pre += y;
+    }
+    const int total = __shfl_sync(FULL, pre, 31);
+    pre -= csz;   // exclusive
+    for (int base = 0; base < total; base += 32) {
+        {
+            const int g = base + lane;
+            int lo = 0;
+#pragma unroll
+            for (int step = 16; step; step >>= 1) {
+                const int pm = __shfl_sync(FULL, pre, lo + step);
+                if (pm <= g) lo += step;
+            }
+            const int q = __shfl_sync(FULL, kq0, lo) + (g - __shfl_sync(FULL, pre, lo));
             int flags = 0;
             bool qa_free = false;
             int j = -1;
-            if (q < q1) {
+            if (g < total) {
                 const float4 f = d.cell_pos[q];
                 j = __float_as_int(f.w);
                 float ddx = f.x - mx, ddy = f.y - my, ddz = f.z - mz;
@@ -1522,14 +1641,14 @@ static void *force_kernel(bool mixed, int mode, int fb) {
 #define XMD_FK(M, B) (mixed ? (void *)k_force<float, M, B> : (void *)k_force<double, M, B>)
     if (mode == 0) {
         switch (fb) {
+        case 32: return XMD_FK(0, 32);
         case 64: return XMD_FK(0, 64);
-        case 96: return XMD_FK(0, 96);
         default: return XMD_FK(0, 128);
         }
     }
     switch (fb) {
+    case 32: return XMD_FK(1, 32);
     case 64: return XMD_FK(1, 64);
-    case 96: return XMD_FK(1, 96);
     default: return XMD_FK(1, 128);
     }
 #undef XMD_FK
@@ -1544,8 +1663,8 @@ void Engine::launch_force(int mode, int c) {
     cudaGraphConditionalHandle none = 0;
     int fuse = 0;
     void *args[] = {&d, &tp, &c, &none, &fuse};
-    CK(cudaLaunchKernel(force_kernel(params.precision == XMD_PREC_MIXED, mode, tune.fb), dim3(nb), dim3(tune.fb),
-                        args, 0, stream));
+    CK(cudaLaunchKernel(force_kernel(params.precision == XMD_PREC_MIXED, mode, tune.fb), dim3(nb),
+                        dim3(tune.fb * LPB), args, 0, stream));
 }
 
 Engine::Engine(const xmd_params &p) : params(p) {
@@ -1580,12 +1699,14 @@ void *Engine::dalloc(size_t bytes) {
     CK(cudaMalloc(&p, bytes < 16 ? 16 : bytes));
     CK(cudaMemsetAsync(p, 0, bytes < 16 ? 16 : bytes, stream));
     allocs.push_back(p);
+    alloc_bytes += bytes < 16 ? 16 : bytes;
     return p;
 }
 
 void Engine::release() {
     for (void *p : allocs) cudaFree(p);
     allocs.clear();
+    alloc_bytes = 0;
     d = Dev{};
     finalized = false;
 }
@@ -2223,6 +2344,10 @@ void Engine::allocate() {
         q.min_cos_hr = p.qa_min_cos_hr;
         q.min_cos_hh = p.qa_min_cos_hh;
         q.max_cos_nr = p.qa_max_cos_nr;
+        double rmax = 0.0;
+        for (double v : req) rmax = std::max(rmax, v);
+        const double w = rmax * (1.0 + 1e-9);
+        q.req_out2 = w * w;
     }
     CK(cudaStreamSynchronize(stream));
 }
@@ -2837,14 +2962,16 @@ void Engine::resize_rows(int ncap) {
             CK(cudaFree(a));
             a = rows;
         }
+    alloc_bytes += sizeof(int32_t) * (size_t)d.N * ncap;
+    alloc_bytes -= std::max<size_t>(16, sizeof(int32_t) * (size_t)nl_cap * d.N);
     d.nl_row = rows;
     d.nl_cap = nl_cap = ncap;
     drop_graphs();
 }
 
 void Engine::set_tuning(const Tune &t) {
-    if (t.fb != 64 && t.fb != 96 && t.fb != 128)
-        throw std::invalid_argument("tuning: step-kernel block size must be 64, 96 or 128");
+    if (t.fb != 32 && t.fb != 64 && t.fb != 128)
+        throw std::invalid_argument("tuning: step-kernel block size must be 32, 64 or 128 beads");
     if (t.graph_steps != 8 && t.graph_steps != 16 && t.graph_steps != 32)
         throw std::invalid_argument("tuning: steps per graph must be 8, 16 or 32");
     if (t.tile_per_sm < 0) throw std::invalid_argument("tuning: tile blocks per SM must be >= 0");
@@ -2872,7 +2999,7 @@ Engine::Tune Engine::autotune(int steps, double *ms_out) {
         if (r.in_use && !r.have_state) throw std::logic_error("autotune: set_state must be called for every replica");
     steps = std::max(32, (steps + 31) / 32 * 32);
     std::vector<Tune> cands;
-    for (int fb : {64, 96, 128})
+    for (int fb : {32, 64, 128})
         for (int gs : {8, 16, 32})
             for (int tps : {0, 2}) cands.push_back(Tune{fb, tps, gs});
     Tune best = tune;
@@ -2989,7 +3116,7 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
         void *fargs[] = {&d, &tp, &c, &hf, &ff};
         kf.func = fk;
         kf.gridDim = dim3(nb);
-        kf.blockDim = dim3(tune.fb);
+        kf.blockDim = dim3(tune.fb * LPB);
         kf.kernelParams = fargs;
         cudaGraphNode_t nf, nc, ncond;
         if (tp.ext_on) {

@@ -110,6 +110,9 @@ struct QaDev {
     const int32_t *ptype;        // [20] polarization
     int fp_total, ct_total;
     double min_cos_hr, min_cos_hh, max_cos_nr;
+    // a squared distance above which no contact type passes the formation
+    // distance test (the largest req_min_dist, widened by 1e-9)
+    double req_out2;
 };
 
 // everything a kernel needs, passed by value
@@ -259,13 +262,15 @@ public:
     void steps_left(long long *out);   // per replica slot, -2 for a free slot
     void place_now(int rep);           // place a replica now (XMD_ERR_CAPACITY: no room yet)
     int capacity_replicas() const { return cap.reps; }
+    // device memory this context holds (its allocations, rows at their current capacity)
+    size_t device_bytes() const { return alloc_bytes; }
     // a non-finite force freezes its replica (steps_left reports -3) instead
     // of failing the step, so a serving loop can retire it alone
     void set_isolate_faults(bool on) { isolate_faults = on; }
     // launch shapes (the trajectory does not depend on them), chosen by
     // autotune() or set directly
     struct Tune {
-        int fb = 128;            // beads (threads) per step-kernel block: 64, 96 or 128
+        int fb = 64;             // beads per step-kernel block (4 threads each): 32, 64 or 128
         int tile_per_sm = 0;     // resident tile-build blocks per SM (0: as many as fit)
         int graph_steps = 16;    // steps per captured graph: 8, 16 or 32
     };
@@ -276,7 +281,6 @@ public:
     // not touched.  ms_out (optional) receives the best time per step.
     Tune autotune(int steps, double *ms_out = nullptr);
     Tune tune;
-    size_t device_bytes() const { return bytes; }
     void set_tethers(int rep, int n, const int32_t *i1, const int32_t *i2, const double *d);
     void set_angles(int rep, int n, const int32_t *i1, const int32_t *i2, const int32_t *i3,
                     const double *th);
@@ -330,6 +334,7 @@ private:
     int device = 0;
     cudaStream_t stream = nullptr;
     std::vector<void *> allocs;
+    size_t alloc_bytes = 0;   // device memory held by this context
     int *h_any = nullptr;        // pinned
     TermP tp{};
     int64_t launches = 0, md_steps = 0;
@@ -364,7 +369,6 @@ private:
         int beads = 0, reps = 0, nat = 0, cells = 0, chunks = 0, fp = 0, ct = 0, qab = 0, ss = 0, afm = 0;
     } cap;
     bool dynamic = false;
-    size_t bytes = 0;                          // device memory held
     RangeAlloc a_beads, a_nat, a_cells, a_chunks, a_fp, a_ct, a_ss, a_afm;
     int qa_bchunk_next = 0;   // next free chunk of the QA re-listing (static contexts)
     std::vector<int32_t> owner_h;              // bead slot -> replica (or -1)

@@ -6,8 +6,8 @@
 // (process_candidates.cpp:4-29) and where re-freed pairs land
 // (process_contacts.cpp:48-55).  Here each replica owns contiguous regions of
 // free-pair and contact slots; slot order is kept by ordered block-wide
-// compaction, and the order-dependent greedy acceptance runs sequentially on
-// one thread per replica over the (few) compacted candidates.  Geometry that
+// compaction, and the order-dependent greedy acceptance decides the compacted
+// candidates of a replica in dependency rounds (k_qa_step).  Geometry that
 // feeds a yes/no decision is evaluated with explicitly rounded FP64 operations
 // so the decisions match an uncontracted CPU build.
 #pragma once
@@ -108,10 +108,18 @@ __global__ void __launch_bounds__(QA_SIFT) k_qa_sift(Dev d, TermP p, int cur) {
     live = live && slot - rp.fp_off < rp.fp_n;
     int type = 0;
     int32_t d1p = 0, d2p = 0;
+    const double4_32a *pos = d.pos[cur];
+    D3 r12{0.0, 0.0, 0.0};
+    int i1 = 0, i2 = 0;
     if (live && !q.fp_vac[slot]) {
-        const int i1 = q.fp_i1[slot], i2 = q.fp_i2[slot];
-        const double4_32a *pos = d.pos[cur];
-        D3 r12 = d3ruv(rp.box, pos[i1], pos[i2]);
+        i1 = q.fp_i1[slot];
+        i2 = q.fp_i2[slot];
+        r12 = d3ruv(rp.box, pos[i1], pos[i2]);
+    }
+    // beyond every type's formation distance (with a 1e-9 margin, far above
+    // the rounding of the exact test below) no pair is a candidate: no FP64
+    // square root, division or n/h loads for it
+    if (live && !q.fp_vac[slot] && d3dot(r12, r12) <= q.req_out2) {
         double r12_rn = __ddiv_rn(1.0, __dsqrt_rn(d3dot(r12, r12)));
         D3 u = d3scl(r12_rn, r12);
         const size_t N = d.N;
@@ -158,19 +166,37 @@ __global__ void __launch_bounds__(QA_SIFT) k_qa_sift(Dev d, TermP p, int cur) {
 }
 
 // ---- acceptance: process_candidates::iter (process_candidates.cpp:10-29) in
-// candidate order, one block per replica (the greedy choice of shared
-// valences is sequential); the transitions follow in k_qa_trans.
+// candidate order, one block per replica; the transitions follow in
+// k_qa_trans.
+//
+// The greedy choice is sequential by definition: a candidate is accepted when
+// both beads still have the valence it needs after every EARLIER candidate
+// was decided.  Only earlier candidates that share a bead with it matter, so
+// the block decides in rounds: in each round a pending candidate decides when
+// it is the lowest-ordered pending candidate of both its beads (an atomicMin
+// per bead into a shared table).  At that moment every earlier candidate on
+// its beads has decided and no later one has, so it sees exactly the valences
+// the sequential loop would; candidates deciding in one round share no bead.
+// The table is hashed (bead mod QA_HASH): two beads in one entry only make
+// the later candidate wait a round, and the lowest pending candidate always
+// decides, so every round makes progress.  Accepted contacts then take their
+// slots in candidate order (an ordered compaction).  A chunk that could
+// overflow the replica's contact region runs the plain sequential loop, which
+// stops at the first candidate without a slot.
+constexpr int QA_HASH = 4096;
 __global__ void __launch_bounds__(1024) k_qa_step(Dev d, TermP p, int cur) {
     const int r = blockIdx.x, t = threadIdx.x;
     RepDev &rp = d.rep[r];
     const QaDev &q = d.qa;
     __shared__ int s_slots[1024];
     __shared__ int s_warp[33];
+    __shared__ int s_first[QA_HASH];
     __shared__ int s_ct_n, s_fp_n, s_err;
     if (t == 0) { s_ct_n = rp.ct_n; s_fp_n = rp.fp_n; s_err = 0; }
+    for (int k = t; k < QA_HASH; k += 1024) s_first[k] = INT_MAX;
     __syncthreads();
     const double tnow = rp.t;
-    const int fp_off = rp.fp_off, ct_off = rp.ct_off;
+    const int fp_off = rp.fp_off, ct_off = rp.ct_off, ct_cap = rp.ct_cap;
     const int fp_n0 = s_fp_n;
     // 1. greedy acceptance in free-pair slot order, over the sift blocks'
     //    ordered candidate lists (slots outside this replica's live range are
@@ -183,39 +209,80 @@ __global__ void __launch_bounds__(1024) k_qa_step(Dev d, TermP p, int cur) {
         int pos;
         const int total = block_exscan(cnt, &pos, s_warp);
         for (int g0 = 0; g0 < total; g0 += 1024) {
-        // gather candidates [g0, g0 + 1024) of this round with their data
-        for (int k = max(0, g0 - pos); k < cnt && pos + k < g0 + 1024; ++k) {
-            const int s = q.cand_list[(size_t)blk * QA_SIFT + k];
-            const int o = pos + k - g0;
-            const bool mine = s >= fp_off && s < fp_off + fp_n0;
-            s_slots[o] = mine ? s : -1;
-            if (mine) {
-                s_i1[o] = q.fp_i1[s]; s_i2[o] = q.fp_i2[s];
-                s_d1[o] = q.cand_d1[s]; s_d2[o] = q.cand_d2[s]; s_ty[o] = q.cand_type[s];
-            }
-        }
-        __syncthreads();
-        if (t == 0) {
-            const int m = min(1024, total - g0);
-            for (int k = 0; k < m; ++k) {
-                int s = s_slots[k];
-                if (s < 0) continue;
-                int i1 = s_i1[k], i2 = s_i2[k];
-                int32_t d1p = s_d1[k], d2p = s_d2[k];
-                int32_t y1 = q.sync[i1], y2 = q.sync[i2];
-                if (sync_ok_after(y1, d1p) && sync_ok_after(y2, d2p)) {
-                    if (s_ct_n >= rp.ct_cap) { s_err = 1; break; }
-                    int c = ct_off + s_ct_n++;
-                    q.ct_i1[c] = i1; q.ct_i2[c] = i2; q.ct_type[c] = s_ty[k];
-                    q.ct_status[c] = QA_FORMING; q.ct_ref[c] = tnow; q.ct_vac[c] = 0;
-                    q.ct_d1[c] = d1p; q.ct_d2[c] = d2p;
-                    q.sync[i1] = y1 - d1p;   // bytes never borrow: each stays >= 0
-                    q.sync[i2] = (i2 == i1 ? y1 - d1p : y2) - d2p;
-                    q.fp_vac[s] = 1;
+            // gather candidates [g0, g0 + 1024) of this round with their data
+            for (int k = max(0, g0 - pos); k < cnt && pos + k < g0 + 1024; ++k) {
+                const int s = q.cand_list[(size_t)blk * QA_SIFT + k];
+                const int o = pos + k - g0;
+                const bool mine = s >= fp_off && s < fp_off + fp_n0;
+                s_slots[o] = mine ? s : -1;
+                if (mine) {
+                    s_i1[o] = q.fp_i1[s]; s_i2[o] = q.fp_i2[s];
+                    s_d1[o] = q.cand_d1[s]; s_d2[o] = q.cand_d2[s]; s_ty[o] = q.cand_type[s];
                 }
             }
-        }
-        __syncthreads();
+            __syncthreads();
+            const int m = min(1024, total - g0);
+            if (s_ct_n + m > ct_cap) {
+                // the sequential loop (can run out of contact slots)
+                if (t == 0) {
+                    for (int k = 0; k < m; ++k) {
+                        const int s = s_slots[k];
+                        if (s < 0) continue;
+                        const int i1 = s_i1[k], i2 = s_i2[k];
+                        const int32_t d1p = s_d1[k], d2p = s_d2[k];
+                        const int32_t y1 = q.sync[i1], y2 = q.sync[i2];
+                        if (sync_ok_after(y1, d1p) && sync_ok_after(y2, d2p)) {
+                            if (s_ct_n >= ct_cap) { s_err = 1; break; }
+                            const int c = ct_off + s_ct_n++;
+                            q.ct_i1[c] = i1; q.ct_i2[c] = i2; q.ct_type[c] = s_ty[k];
+                            q.ct_status[c] = QA_FORMING; q.ct_ref[c] = tnow; q.ct_vac[c] = 0;
+                            q.ct_d1[c] = d1p; q.ct_d2[c] = d2p;
+                            q.sync[i1] = y1 - d1p;   // bytes never borrow: each stays >= 0
+                            q.sync[i2] = (i2 == i1 ? y1 - d1p : y2) - d2p;
+                            q.fp_vac[s] = 1;
+                        }
+                    }
+                }
+                __syncthreads();
+                continue;
+            }
+            // rounds: candidate t decides once it is the lowest pending one
+            // of both its beads
+            bool pend = t < m && s_slots[t] >= 0, acc = false;
+            int i1 = 0, i2 = 0;
+            int32_t d1p = 0, d2p = 0;
+            if (pend) { i1 = s_i1[t]; i2 = s_i2[t]; d1p = s_d1[t]; d2p = s_d2[t]; }
+            const int h1 = i1 & (QA_HASH - 1), h2 = i2 & (QA_HASH - 1);
+            while (__syncthreads_or(pend)) {
+                if (pend) { atomicMin(&s_first[h1], t); atomicMin(&s_first[h2], t); }
+                __syncthreads();
+                const bool go = pend && s_first[h1] == t && s_first[h2] == t;
+                __syncthreads();
+                if (pend) { s_first[h1] = INT_MAX; s_first[h2] = INT_MAX; }
+                if (go) {
+                    const int32_t y1 = q.sync[i1], y2 = q.sync[i2];
+                    if (sync_ok_after(y1, d1p) && sync_ok_after(y2, d2p)) {
+                        acc = true;
+                        q.sync[i1] = y1 - d1p;
+                        q.sync[i2] = (i2 == i1 ? y1 - d1p : y2) - d2p;
+                    }
+                    pend = false;
+                }
+            }
+            // contact slots in candidate order
+            int at;
+            const int nacc = block_exscan(acc ? 1 : 0, &at, s_warp);
+            if (acc) {
+                const int s = s_slots[t];
+                const int c = ct_off + s_ct_n + at;
+                q.ct_i1[c] = i1; q.ct_i2[c] = i2; q.ct_type[c] = s_ty[t];
+                q.ct_status[c] = QA_FORMING; q.ct_ref[c] = tnow; q.ct_vac[c] = 0;
+                q.ct_d1[c] = d1p; q.ct_d2[c] = d2p;
+                q.fp_vac[s] = 1;
+            }
+            __syncthreads();
+            if (t == 0) s_ct_n += nacc;
+            __syncthreads();
         }
     }
     __syncthreads();

@@ -13,25 +13,50 @@ double now_s() {
     return duration<double>(steady_clock::now().time_since_epoch()).count();
 }
 
-// device bytes a bead slot costs at the default row capacity (positions x2,
-// history, list origin, forces, topology, rows, cells, generator) plus its
-// share of native-contact entries; the reservation is sized from it
-constexpr int64_t BYTES_PER_BEAD = 1024;
+// native-contact entries reserved per bead slot
 constexpr int NATIVES_PER_BEAD = 8;
+
+// Device bytes of a reserved context, fixed part and per bead slot, measured
+// on two small probe contexts of these parameters (their allocations at the
+// initial Verlet row capacity): the admission budget is enforced against the
+// engine's real allocation, not an estimate.
+static void reservation_cost(const xmd_params &p, double *fixed, double *per_bead) {
+    auto probe = [&](int beads) {
+        Engine e(p);
+        e.reserve(beads, std::max(16, beads / 30), NATIVES_PER_BEAD * beads);
+        return (double)e.device_bytes();
+    };
+    const int b1 = 4096, b2 = 8192;
+    const double m1 = probe(b1), m2 = probe(b2);
+    *per_bead = (m2 - m1) / (b2 - b1);
+    *fixed = m1 - *per_bead * b1;
+}
 
 Server::Server(const xmd_params &p, int64_t hbm_budget, int max_beads, int chunk_steps) : params(p) {
     if (!params.langevin_on) throw std::invalid_argument("server: langevin must be enabled");
     if (params.on[XMD_TERM_QA]) throw std::invalid_argument("server: the quasi-adiabatic term needs a static context");
     if (hbm_budget <= 0 || max_beads <= 0) throw std::invalid_argument("server: bad budget");
     chunk = chunk_steps > 0 ? chunk_steps : 256;
-    cap_beads = (int)std::min<int64_t>(max_beads, hbm_budget / BYTES_PER_BEAD);
+    budget = hbm_budget;
+    double fixed = 0.0;
+    reservation_cost(params, &fixed, &bytes_per_bead);
+    const double fit = ((double)hbm_budget - fixed) / bytes_per_bead;
+    cap_beads = (int)std::min<double>(max_beads, std::floor(fit));
     if (cap_beads < 1) throw std::invalid_argument("server: the HBM budget holds no bead");
-    cap_reps = std::min(1024, std::max(16, cap_beads / 30));
-    cap_nat = NATIVES_PER_BEAD * cap_beads;
-    eng = std::make_unique<Engine>(params);
-    // one request whose trajectory diverges fails alone; the others go on
-    eng->set_isolate_faults(true);
-    eng->reserve(cap_beads, cap_reps, cap_nat);
+    // the replica table grows with the bead capacity; shrink until the whole
+    // reservation fits the budget
+    for (;;) {
+        cap_reps = std::min(1024, std::max(16, cap_beads / 30));
+        cap_nat = NATIVES_PER_BEAD * cap_beads;
+        eng = std::make_unique<Engine>(params);
+        // one request whose trajectory diverges fails alone; the others go on
+        eng->set_isolate_faults(true);
+        eng->reserve(cap_beads, cap_reps, cap_nat);
+        if ((int64_t)eng->device_bytes() <= hbm_budget || cap_beads <= 1) break;
+        cap_beads = std::max(1, (int)(cap_beads * 0.98));
+    }
+    if ((int64_t)eng->device_bytes() > hbm_budget) throw std::invalid_argument("server: the HBM budget holds no bead");
+    dev_bytes = (int64_t)eng->device_bytes();
     worker = std::thread([this] { loop(); });
 }
 
@@ -117,6 +142,11 @@ void Server::stats(double *out) {
     out[XMD_SRV_BEAD_STEPS] = bead_steps;
     out[XMD_SRV_SPAN_S] = span;
     out[XMD_SRV_FAILED] = (double)failed;
+    out[XMD_SRV_DEVICE_BYTES] = (double)dev_bytes;
+    out[XMD_SRV_BUDGET_BYTES] = (double)budget;
+    out[XMD_SRV_BYTES_PER_BEAD] = bytes_per_bead;
+    out[XMD_SRV_ADMIT_S] = admit_s;
+    out[XMD_SRV_STEP_S] = step_s;
 }
 
 // place a queued request into a free slot; false when the capacity has no
@@ -188,6 +218,7 @@ void Server::loop() {
                 if (stop) break;
             }
             // admission, first come first served
+            const double ta = now_s();
             for (;;) {
                 Request *q;
                 {
@@ -221,10 +252,12 @@ void Server::loop() {
             }
             bool pending_zero = false;
             for (Request *q : running) pending_zero |= q->nsteps == 0;
+            const double ts = now_s();
             if (!pending_zero) {
                 eng->step(chunk);
                 ++chunks;
             }
+            const double te = now_s();
             left.assign(eng->capacity_replicas(), -2);
             eng->steps_left(left.data());
             std::vector<Request *> keep;
@@ -236,6 +269,10 @@ void Server::loop() {
             {
                 std::lock_guard<std::mutex> lk(mu);
                 running.swap(keep);
+                // host time between chunks (admission, retirement) and in them
+                admit_s += (ts - ta) + (now_s() - te);
+                step_s += te - ts;
+                dev_bytes = (int64_t)eng->device_bytes();
             }
             cv_done.notify_all();
         }

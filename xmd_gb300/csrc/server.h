@@ -74,6 +74,9 @@ private:
     int64_t chunks = 0;
     int peak_running = 0;
     int64_t failed = 0;     // requests retired by a diverged trajectory
+    int64_t budget = 0, dev_bytes = 0;
+    double bytes_per_bead = 0;       // measured device cost of a bead slot
+    double admit_s = 0, step_s = 0;  // worker time between chunks and in them
 
     void loop();
     bool admit(Request *q);
