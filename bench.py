@@ -457,9 +457,9 @@ def accuracy_c3(nrep, steps, every, device):
     Q over the second half.  Reported as paired mixed - FP64 differences,
     their mean and standard error over the replicas, and the drift
     criterion: |mean paired drift difference| <= 1 % of |FP64 drift|."""
-    from xmd_gb300 import Engine, observe, synth
+    from xmd_gb300 import Engine, XmdError, observe, synth
     s = synth.config_c3()
-    runs, forces, wall = {}, {}, {}
+    runs, forces, wall, frozen = {}, {}, {}, {}
     for prec in ("fp64", "mixed"):
         with Engine(synth.yaml_for("c3", prec) + f"  device: {device}\n") as e:
             for k in range(nrep):
@@ -468,11 +468,21 @@ def accuracy_c3(nrep, steps, every, device):
             t0 = time.perf_counter()
             samples = [[(0.0, *[e.observables(k)[f] for f in observe.FIELDS])] for k in range(nrep)]
             for t in range(every, steps + 1, every):
-                e.step(every)
+                try:
+                    e.step(every)
+                except XmdError as ex:
+                    # a replica whose force went non-finite (the reference's
+                    # terms are singular at some geometries) is frozen; the
+                    # others go on, and it leaves the paired comparison
+                    if "non-finite" not in str(ex):
+                        raise
                 for k in range(nrep):
                     samples[k].append((float(t), *[e.observables(k)[f] for f in observe.FIELDS]))
+            frozen[prec] = [int(k) for k in np.nonzero(e.steps_left()[:nrep] == -3)[0]]
             wall[prec] = time.perf_counter() - t0
             runs[prec] = [np.asarray(x) for x in samples]
+    keep = [k for k in range(nrep) if k not in frozen["fp64"] and k not in frozen["mixed"]]
+    runs = {prec: [runs[prec][k] for k in keep] for prec in runs}
     half = len(runs["fp64"][0]) // 2
 
     def per_rep(a):
@@ -494,6 +504,7 @@ def accuracy_c3(nrep, steps, every, device):
     return {"system": f"{nrep} replicas x 512 x 60 beads ({s.n} each), periodic, Go + Debye-Hueckel + "
                       "quasi-adiabatic, own generator seed per replica",
             "steps": steps, "sample_every": every, "force_rel_err_t0": ferr, "paired": res,
+            "replicas_paired": len(keep), "frozen_non_finite": frozen,
             "drift_rel_diff": rel, "drift_rel_diff_95": rel_hi, "drift_within_1pct": bool(rel <= 0.01),
             "drift_within_1pct_95": bool(rel_hi <= 0.01),
             "drift_definition": "energy change over the whole run (least-squares slope x duration), "

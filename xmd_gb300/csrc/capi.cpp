@@ -326,7 +326,7 @@ int xmd_gpu_autotune(xmd_gpu_ctx *ctx, int32_t steps, int32_t *shape, double *ms
     return guard([&] {
         ctx->eng->use_device();
         const xmdg::Engine::Tune t = ctx->eng->autotune(steps, ms_per_step);
-        if (shape) { shape[0] = t.fb; shape[1] = t.tile_per_sm; shape[2] = t.graph_steps; }
+        if (shape) { shape[0] = t.fb; shape[1] = t.tile_per_sm; shape[2] = t.graph_steps; shape[3] = t.lpb; }
     });
 }
 
@@ -339,6 +339,7 @@ int xmd_gpu_set_tuning(xmd_gpu_ctx *ctx, const int32_t *shape) {
         t.fb = shape[0];
         t.tile_per_sm = shape[1];
         t.graph_steps = shape[2];
+        t.lpb = shape[3];
         ctx->eng->set_tuning(t);
     });
 }
@@ -348,7 +349,7 @@ int xmd_gpu_get_tuning(xmd_gpu_ctx *ctx, int32_t *shape) {
     if (!shape) return XMD_ERR_ARG;
     return guard([&] {
         const xmdg::Engine::Tune t = ctx->eng->tuning();
-        shape[0] = t.fb; shape[1] = t.tile_per_sm; shape[2] = t.graph_steps;
+        shape[0] = t.fb; shape[1] = t.tile_per_sm; shape[2] = t.graph_steps; shape[3] = t.lpb;
     });
 }
 

@@ -253,42 +253,82 @@ __global__ void __launch_bounds__(256) k_ext(Dev d, TermP p, int cur) {
     fo[0] = f.x; fo[1] = f.y; fo[2] = f.z;
 }
 
-// Threads per bead in the step kernel.  A bead's pair entries (native
-// contacts, disulfides, Verlet row, quasi-adiabatic contacts) are spread over
-// its LPB lanes and their partial forces combined by shuffles in a fixed
-// order; its bonded centres are split in two tasks; its integrator runs one
-// axis per lane, with the generator, the new position and the skin test on
-// the fourth.  The lanes of a bead are adjacent threads of one warp.
-constexpr int LPB = 4;
+// Lanes of a bead in the step kernel.  A bead's pair entries (native
+// contacts, disulfides, Verlet row, quasi-adiabatic contacts) are dealt to
+// VL = 4 virtual lanes, entry k of a list to virtual lane k mod 4, each with
+// its own partial force; the partials are combined as ((v0 + v1) + (v2 + v3)).
+// The virtual lanes run on LPB = 1, 2 or 4 adjacent threads of one warp
+// (thread ln of a bead holds virtual lanes ln, ln + LPB, ...), a launch shape
+// chosen by the autotuner: the sums, and so the trajectory, are the same bits
+// for every LPB.  A bead's bonded centres are split in two tasks; its
+// integrator runs axis a on thread a mod LPB, with the generator, the new
+// position and the skin test on the last thread of the bead.
+constexpr int VL = 4;
 
-// sum of the bead's four lane partials, the same bits on every lane
-// ((a0 + a1) + (a2 + a3): each step adds a lane's value to its partner's,
-// which is commutative bit for bit for FP64 and for the float-float sum)
-__device__ __forceinline__ double quad_sum(unsigned m, double v) {
-    v += __shfl_xor_sync(m, v, 1, LPB);
-    v += __shfl_xor_sync(m, v, 2, LPB);
+template <int LPB> __device__ __forceinline__ unsigned bead_mask(int t) {
+    return ((1u << LPB) - 1u) << ((t & 31) & ~(LPB - 1));
+}
+__device__ __forceinline__ double vadd(double a, double b) { return a + b; }
+__device__ __forceinline__ FF vadd(FF a, FF b) { return ff_add(a, b); }
+__device__ __forceinline__ double xlane(unsigned m, double v, int o, int w) { return __shfl_xor_sync(m, v, o, w); }
+__device__ __forceinline__ FF xlane(unsigned m, FF v, int o, int w) {
+    return FF{__shfl_xor_sync(m, v.h, o, w), __shfl_xor_sync(m, v.l, o, w)};
+}
+// ((v0 + v1) + (v2 + v3)) of a bead's virtual lanes, the same bits on every
+// thread of the bead and for every LPB (each addition is commutative bit for
+// bit, for FP64 and for the float-float sum, so a thread may add its
+// partner's value to its own)
+template <int LPB, class T> __device__ __forceinline__ T vl_sum(unsigned m, const T (&a)[VL / LPB]) {
+    if constexpr (LPB == 4) {
+        const T s = vadd(a[0], xlane(m, a[0], 1, 4));
+        return vadd(s, xlane(m, s, 2, 4));
+    } else if constexpr (LPB == 2) {
+        // thread 0 holds v0 and v2, thread 1 v1 and v3
+        return vadd(vadd(a[0], xlane(m, a[0], 1, 2)), vadd(a[1], xlane(m, a[1], 1, 2)));
+    } else {
+        return vadd(vadd(a[0], a[1]), vadd(a[2], a[3]));
+    }
+}
+template <int LPB, class FT> __device__ __forceinline__ Acc3<FT> vl_sum3(unsigned m, const Acc3<FT> (&a)[VL / LPB]) {
+    constexpr int U = VL / LPB;
+    decltype(a[0].x) cx[U], cy[U], cz[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) { cx[u] = a[u].x; cy[u] = a[u].y; cz[u] = a[u].z; }
+    Acc3<FT> r;
+    r.x = vl_sum<LPB>(m, cx);
+    r.y = vl_sum<LPB>(m, cy);
+    r.z = vl_sum<LPB>(m, cz);
+    return r;
+}
+// sum over the threads of a bead (energies of the evaluation pass)
+template <int LPB> __device__ __forceinline__ double lane_sum(unsigned m, double v) {
+#pragma unroll
+    for (int o = 1; o < LPB; o <<= 1) v += __shfl_xor_sync(m, v, o, LPB);
     return v;
 }
-__device__ __forceinline__ FF quad_sum(unsigned m, FF v) {
-    v = ff_add(v, FF{__shfl_xor_sync(m, v.h, 1, LPB), __shfl_xor_sync(m, v.l, 1, LPB)});
-    v = ff_add(v, FF{__shfl_xor_sync(m, v.h, 2, LPB), __shfl_xor_sync(m, v.l, 2, LPB)});
-    return v;
-}
-template <class FT> __device__ __forceinline__ void quad_sum(unsigned m, Acc3<FT> &a) {
-    a.x = quad_sum(m, a.x);
-    a.y = quad_sum(m, a.y);
-    a.z = quad_sum(m, a.z);
+// entries [k0, k1) of a list dealt to the bead's threads: f(k, u) on thread
+// ln for k = k0 + ln + LPB u (mod VL), u being its virtual lane slot
+template <int LPB, class F> __device__ __forceinline__ void deal(int k0, int k1, int ln, F &&f) {
+    for (int kb = k0 + ln; kb < k1; kb += VL) {
+#pragma unroll
+        for (int u = 0; u < VL / LPB; ++u) {
+            const int k = kb + u * LPB;
+            if (k < k1) f(k, u);
+        }
+    }
 }
 __device__ __forceinline__ double comp3(double4_32a v, int a) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); }
 
-template <class FT, int MODE, int FBT>
+template <class FT, int MODE, int FBT, int LPB>
 __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cur) {
     constexpr int NT = FBT * LPB;
+    constexpr int U = VL / LPB;                 // virtual lanes per thread
+    constexpr int AX = (3 + LPB - 1) / LPB;     // integrator axes per thread
     const double4_32a *__restrict__ pin = d.pos[cur];
     const int N = d.N, t = threadIdx.x, i0 = blockIdx.x * FBT;
-    const int bs = t / LPB, ln = t % LPB;   // bead slot in the block, lane of the bead
+    const int bs = t / LPB, ln = t % LPB;   // bead slot in the block, thread of the bead
     const int i = i0 + bs;
-    const unsigned qm = 0xFu << ((t & 31) & ~(LPB - 1));   // the bead's lanes in the warp
+    const unsigned qm = bead_mask<LPB>(t);  // the bead's threads in the warp
     __shared__ double4_32a P[FBT + 6];
     __shared__ V3<FT> Ct[FBT + 3], Ca[3][FBT + 3], Cd[4][FBT + 3];
     // mixed path: every position of the tile split into float-float parts
@@ -306,12 +346,12 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
 
     // mixed path: the integrator's per-bead state does not depend on the
     // forces, so its loads are issued first and their latency passes under
-    // the force work (lanes 0-2 their axis of the history, lane 3 the
-    // generator and the list origin); the FP64 path is bound by its FP64
+    // the force work (each thread the history of its axes, the last thread
+    // the generator and the list origin); the FP64 path is bound by its FP64
     // pipe instead and loads them where they are used
     constexpr bool EARLY = MODE == 1 && sizeof(FT) == 4;
     const bool live = i < N;
-    double yv[5];
+    double yv[5 * AX];
     uint64_t st0 = 0;
     double4_32a o_i = make_double4_32a(0, 0, 0, 0);
     int pf_n0 = 0, pf_n1 = 0, pf_cnt = 0;   // the pair loops' bounds, loaded first too
@@ -322,10 +362,15 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
     }
     const size_t Ns = (size_t)N;
     if (EARLY && live) {
-        if (ln < 3) {
 #pragma unroll
-            for (int q = 0; q < 5; ++q) yv[q] = d.yh[(size_t)(q * 3 + ln) * Ns + i];
-        } else {
+        for (int u = 0; u < AX; ++u) {
+            const int a = ln + LPB * u;
+            if (a < 3) {
+#pragma unroll
+                for (int q = 0; q < 5; ++q) yv[q * AX + u] = d.yh[(size_t)(q * 3 + a) * Ns + i];
+            }
+        }
+        if (ln == LPB - 1) {
             st0 = d.rng[i];
             o_i = d.orig[i];
         }
@@ -467,7 +512,7 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
     }
     __syncthreads();
 
-    // from here on, the four lanes of a bead take the same branches
+    // from here on, the threads of a bead take the same branches
     if (!live) return;
     const int r = d.rep_of[i];
     if (r < 0) return;     // free bead slot
@@ -477,24 +522,27 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
         return;
     }
     const int s = bs + 2;   // centre slot of bead i
-    Acc3<FT> acc;
+    // the partial forces of this thread's virtual lanes; virtual lane 0
+    // (thread 0, slot 0) starts from the bonded sum
+    Acc3<FT> acc[U];
     if (ln == 0) {
+        Acc3<FT> &a0 = acc[0];
         if constexpr (sizeof(FT) == 4) {
             // the bonded contributions, computed in FP32, are summed in FP32
             // and enter the float-float accumulator once
             V3<float> bsum = Ct[s] - Ct[s - 1] + Ca[2][s - 1] + Ca[1][s] + Ca[0][s + 1] + Cd[0][s + 1] +
                              Cd[1][s] + Cd[2][s - 1] + Cd[3][s - 2];
-            acc.add(bsum);
+            a0.add(bsum);
         } else {
-            acc.add(Ct[s]);
-            acc.sub(Ct[s - 1]);
-            acc.add(Ca[2][s - 1]);
-            acc.add(Ca[1][s]);
-            acc.add(Ca[0][s + 1]);
-            acc.add(Cd[0][s + 1]);
-            acc.add(Cd[1][s]);
-            acc.add(Cd[2][s - 1]);
-            acc.add(Cd[3][s - 2]);
+            a0.add(Ct[s]);
+            a0.sub(Ct[s - 1]);
+            a0.add(Ca[2][s - 1]);
+            a0.add(Ca[1][s]);
+            a0.add(Ca[0][s + 1]);
+            a0.add(Cd[0][s + 1]);
+            a0.add(Cd[1][s]);
+            a0.add(Cd[2][s - 1]);
+            a0.add(Cd[3][s - 2]);
         }
     }
 
@@ -504,78 +552,103 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
     const PairGeo<FT> geo(bx, per, pi);
     double vgo = 0, vpa = 0, ves = 0;
 
-    // Each lane takes every LPB-th entry of the bead's lists.  The loops are
-    // software-pipelined: the next entry (native index data, or row entry)
-    // is loaded while the current partner's position is fetched.
+    // The pair loops take the thread's U entries of each round of VL
+    // together (their partners' positions are fetched side by side) and are
+    // software-pipelined: the next round's index data is loaded while this
+    // round's positions are fetched.
     if (p.on[XMD_TERM_GO]) {
-        int k = pf_n0 + ln;
         const int k1 = pf_n1;
-        int j = 0;
-        bool on = false;
-        FT nd = FT(0);
-        if (k < k1) {
-            j = d.nat_j[k];
-            on = d.nat_on[k] != 0;
-            nd = nat_dist<FT>(d, k);
-        }
-        for (; k < k1; k += LPB) {
-            int jn = 0;
-            bool onn = false;
-            FT ndn = FT(0);
-            if (k + LPB < k1) {
-                jn = d.nat_j[k + LPB];
-                onn = d.nat_on[k + LPB] != 0;
-                ndn = nat_dist<FT>(d, k + LPB);
+        int jn[U];
+        bool onn[U];
+        FT ndn[U];
+        auto fetch = [&](int kb) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int k = kb + u * LPB;
+                const bool in = k < k1;
+                jn[u] = in ? d.nat_j[k] : 0;
+                onn[u] = in && d.nat_on[k] != 0;
+                ndn[u] = in ? nat_dist<FT>(d, k) : FT(0);
             }
-            if (on) {
-                FT V_;
-                V3<FT> f = go_pair<FT>(p, geo.to(pin[j]), nd, &V_);
-                acc.add(f);
-                if (MODE == 0 && i < j) vgo += (double)V_;
-            }
-            j = jn;
-            on = onn;
-            nd = ndn;
+        };
+        fetch(pf_n0 + ln);
+        for (int kb = pf_n0 + ln; kb < k1; kb += VL) {
+            int j[U];
+            bool on[U];
+            FT nd[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) { j[u] = jn[u]; on[u] = onn[u]; nd[u] = ndn[u]; }
+            if (kb + VL < k1) fetch(kb + VL);
+            double4_32a pj[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (on[u]) pj[u] = pin[j[u]];
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (on[u]) {
+                    FT V_;
+                    V3<FT> f = go_pair<FT>(p, geo.to(pj[u]), nd[u], &V_);
+                    acc[u].add(f);
+                    if (MODE == 0 && i < j[u]) vgo += (double)V_;
+                }
         }
     }
     double vss = 0;
     if (p.on[XMD_TERM_NAT_SS]) {
-        const int s1 = d.ss_end[i];
-        for (int k = d.ss_start[i] + ln; k < s1; k += LPB) {
-            if (!d.ss_on[k]) continue;
+        deal<LPB>(d.ss_start[i], d.ss_end[i], ln, [&](int k, int u) {
+            if (!d.ss_on[k]) return;
             const int j = d.ss_j[k];
             FT V_;
             V3<FT> f = ss_pair<FT>(p, geo.to(pin[j]), &V_);
-            acc.add(f);
+            acc[u].add(f);
             if (MODE == 0 && i < j) vss += (double)V_;
-        }
+        });
     }
-    const int cnt = pf_cnt;
-    int e_next = ln < cnt ? d.nl_row[(size_t)ln * N + i] : 0;
-    for (int k = ln; k < cnt; k += LPB) {
-        const int e = e_next;
-        if (k + LPB < cnt) e_next = d.nl_row[(size_t)(k + LPB) * N + i];
-        int j = e & NL_MASK;
-        double4_32a pj = pin[j];
-        V3<FT> r12 = geo.to(pj);
-        if (e & NL_PAULI) {
-            FT V_;
-            V3<FT> f = pauli_pair<FT>(p, r12, &V_);
-            acc.add(f);
-            if (MODE == 0 && i < j) vpa += (double)V_;
-        }
-        if (e & NL_ES) {
-            FT V_;
-            V3<FT> f = es_pair<FT>(p, r12, charge_prod<FT>(pi.w, pj.w), &V_);
-            acc.add(f);
-            if (MODE == 0 && i < j) ves += (double)V_;
+    {
+        const int cnt = pf_cnt;
+        int en[U];
+        auto fetch = [&](int kb) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int k = kb + u * LPB;
+                en[u] = k < cnt ? d.nl_row[(size_t)k * N + i] : 0;
+            }
+        };
+        fetch(ln);
+        for (int kb = ln; kb < cnt; kb += VL) {
+            int e[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) e[u] = en[u];
+            if (kb + VL < cnt) fetch(kb + VL);
+            double4_32a pj[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (kb + u * LPB < cnt) pj[u] = pin[e[u] & NL_MASK];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (kb + u * LPB >= cnt) continue;
+                const int j = e[u] & NL_MASK;
+                V3<FT> r12 = geo.to(pj[u]);
+                if (e[u] & NL_PAULI) {
+                    FT V_;
+                    V3<FT> f = pauli_pair<FT>(p, r12, &V_);
+                    acc[u].add(f);
+                    if (MODE == 0 && i < j) vpa += (double)V_;
+                }
+                if (e[u] & NL_ES) {
+                    FT V_;
+                    V3<FT> f = es_pair<FT>(p, r12, charge_prod<FT>(pi.w, pj[u].w), &V_);
+                    acc[u].add(f);
+                    if (MODE == 0 && i < j) ves += (double)V_;
+                }
+            }
         }
     }
 
     // quasi-adiabatic contacts: the force part of process_contacts::iter
     // (process_contacts.cpp:25-40).  The bead's contact slots (at most
-    // QA_REF_CAP, held four per lane) are put in ascending order by rank, and
-    // lane l takes the l-th, (l+4)-th, ... of them.
+    // QA_REF_CAP, held QA_REF_CAP / LPB per thread) are put in ascending order
+    // by rank and dealt to the virtual lanes like a list.
     double vqa = 0;
     if (d.qa_on && p.on[XMD_TERM_QA]) {
         const QaDev &q = d.qa;
@@ -603,7 +676,7 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
             if (u * LPB + ln < nref) Qs[bs][rk[u]] = v[u];
         __syncwarp(qm);
         const double tnow = d.rep[r].t;
-        for (int k = ln; k < nref; k += LPB) {
+        deal<LPB>(0, nref, ln, [&](int k, int ul) {
             const int slot = Qs[bs][k];
             int i1 = q.ct_i1[slot], i2 = q.ct_i2[slot];
             V3<FT> r12 = geo.between(pin[i1], pin[i2]);
@@ -616,10 +689,10 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
             FT V_, dV_;
             sink_lj_eval<FT>((FT)depth, (FT)rmin, (FT)rmax, r12_rn * nsq(r12), r12_rn, &V_, &dV_);
             V3<FT> f = ((FT)sat * dV_) * u;
-            if (i == i1) acc.add(f);
-            else acc.sub(f);
+            if (i == i1) acc[ul].add(f);
+            else acc[ul].sub(f);
             if (MODE == 0 && i == i1) vqa += sat * (double)V_;
-        }
+        });
         if (MODE == 1 && ln == LPB - 1) {
             // n and h at this step's positions (precompute_nh.cpp:12-20)
             D3 n{0, 0, 0}, h{0, 0, 0};
@@ -630,9 +703,9 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
         }
     }
 
-    // the bead's force: its lanes' partial sums combined (every lane holds it)
-    quad_sum(qm, acc);
-    V3<double> ftot = acc.total();
+    // the bead's force: its virtual lanes' partial sums combined (every
+    // thread of the bead holds it)
+    V3<double> ftot = vl_sum3<LPB>(qm, acc).total();
     if (p.ext_on) {
         // AFM pulls and walls, from k_ext (launched just before)
         ftot = ftot + V3<double>{d.fext[3 * (size_t)i], d.fext[3 * (size_t)i + 1], d.fext[3 * (size_t)i + 2]};
@@ -653,12 +726,16 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
     }
 
     if (MODE == 0) {
-        if (ln < 3) d.F[3 * (size_t)i + ln] = ln == 0 ? fx : (ln == 1 ? fy : fz);
-        vgo = quad_sum(qm, vgo);
-        vpa = quad_sum(qm, vpa);
-        ves = quad_sum(qm, ves);
-        vqa = quad_sum(qm, vqa);
-        vss = quad_sum(qm, vss);
+#pragma unroll
+        for (int u = 0; u < AX; ++u) {
+            const int a = ln + LPB * u;
+            if (a < 3) d.F[3 * (size_t)i + a] = a == 0 ? fx : (a == 1 ? fy : fz);
+        }
+        vgo = lane_sum<LPB>(qm, vgo);
+        vpa = lane_sum<LPB>(qm, vpa);
+        ves = lane_sum<LPB>(qm, ves);
+        vqa = lane_sum<LPB>(qm, vqa);
+        vss = lane_sum<LPB>(qm, vss);
         if (ln == 0) {
             double *Vr = d.Vrep + r * XMD_NUM_TERMS;
             if (vgo != 0.0) atomicAdd(&Vr[XMD_TERM_GO], vgo);
@@ -671,7 +748,7 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
     }
 
     // ---- lang_pc_step::operator(), lang_pc.cpp:11-37, mass = 1 (main.cpp:156) ----
-    // lane 3: the bead's four generator draws, three normals
+    // the last thread of the bead: its four generator draws, three normals
     double nz0 = 0.0, nz1 = 0.0, nz2 = 0.0;
     if (ln == LPB - 1) {
         if (!EARLY) {
@@ -690,26 +767,33 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
         }
         d.rng[i] = gf2_apply_nib(d.jump + JUMP_WORDS * r, st);
     }
-    nz0 = __shfl_sync(qm, nz0, LPB - 1, LPB);
-    nz1 = __shfl_sync(qm, nz1, LPB - 1, LPB);
-    nz2 = __shfl_sync(qm, nz2, LPB - 1, LPB);
-    // lanes 0-2: the Gear-5 corrector and predictor of their axis
-    double y0 = 0.0;
-    if (ln < 3) {
+    if constexpr (LPB > 1) {
+        nz0 = __shfl_sync(qm, nz0, LPB - 1, LPB);
+        nz1 = __shfl_sync(qm, nz1, LPB - 1, LPB);
+        nz2 = __shfl_sync(qm, nz2, LPB - 1, LPB);
+    }
+    // the Gear-5 corrector and predictor of the thread's axes
+    double y0a[AX];
+#pragma unroll
+    for (int u = 0; u < AX; ++u) {
+        const int a = ln + LPB * u;
+        y0a[u] = 0.0;
+        if (a >= 3) continue;
         const double dt_inv = p.dt_inv, h = p.dt2_half;
         const double gamma = p.gamma_factor * 1.0;
         const double nsd = d.rep[r].noise_sd;
-        const double Fa = ln == 0 ? fx : (ln == 1 ? fy : fz);
-        const double nza = ln == 0 ? nz0 : (ln == 1 ? nz1 : nz2);
+        const double Fa = a == 0 ? fx : (a == 1 ? fy : fz);
+        const double nza = a == 0 ? nz0 : (a == 1 ? nz1 : nz2);
         double *yh = d.yh;
-        y0 = comp3(pi, ln);
+        double y0 = comp3(pi, a);
         double y1, y2, y3, y4, y5;
         if constexpr (EARLY) {
-            y1 = yv[0]; y2 = yv[1]; y3 = yv[2]; y4 = yv[3]; y5 = yv[4];
+            y1 = yv[0 * AX + u]; y2 = yv[1 * AX + u]; y3 = yv[2 * AX + u]; y4 = yv[3 * AX + u];
+            y5 = yv[4 * AX + u];
         } else {
-            y1 = yh[(size_t)(0 * 3 + ln) * Ns + i]; y2 = yh[(size_t)(1 * 3 + ln) * Ns + i];
-            y3 = yh[(size_t)(2 * 3 + ln) * Ns + i]; y4 = yh[(size_t)(3 * 3 + ln) * Ns + i];
-            y5 = yh[(size_t)(4 * 3 + ln) * Ns + i];
+            y1 = yh[(size_t)(0 * 3 + a) * Ns + i]; y2 = yh[(size_t)(1 * 3 + a) * Ns + i];
+            y3 = yh[(size_t)(2 * 3 + a) * Ns + i]; y4 = yh[(size_t)(3 * 3 + a) * Ns + i];
+            y5 = yh[(size_t)(4 * 3 + a) * Ns + i];
         }
         double v = y1 * dt_inv;
         double a_ = Fa * 1.0 - gamma * v + nsd * nza;
@@ -725,15 +809,18 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
         y2 += 3.0 * y3 + 6.0 * y4 + 10.0 * y5;
         y3 += 4.0 * y4 + 10.0 * y5;
         y4 += 5.0 * y5;
-        yh[(size_t)(0 * 3 + ln) * Ns + i] = y1;
-        yh[(size_t)(1 * 3 + ln) * Ns + i] = y2;
-        yh[(size_t)(2 * 3 + ln) * Ns + i] = y3;
-        yh[(size_t)(3 * 3 + ln) * Ns + i] = y4;
-        yh[(size_t)(4 * 3 + ln) * Ns + i] = y5;
+        yh[(size_t)(0 * 3 + a) * Ns + i] = y1;
+        yh[(size_t)(1 * 3 + a) * Ns + i] = y2;
+        yh[(size_t)(2 * 3 + a) * Ns + i] = y3;
+        yh[(size_t)(3 * 3 + a) * Ns + i] = y4;
+        yh[(size_t)(4 * 3 + a) * Ns + i] = y5;
+        y0a[u] = y0;
     }
-    // lane 3: the new position and the skin-test displacement
-    const double px = __shfl_sync(qm, y0, 0, LPB), py = __shfl_sync(qm, y0, 1, LPB);
-    const double pz = __shfl_sync(qm, y0, 2, LPB);
+    // the last thread: the new position (axis a from thread a mod LPB) and
+    // the skin-test displacement
+    const double px = __shfl_sync(qm, y0a[0 / LPB], 0 % LPB, LPB);
+    const double py = __shfl_sync(qm, y0a[1 / LPB], 1 % LPB, LPB);
+    const double pz = __shfl_sync(qm, y0a[2 / LPB], 2 % LPB, LPB);
     double disp = 0.0;
     if (ln == LPB - 1) {
         const double4_32a pn = make_double4_32a(px, py, pz, pi.w);
@@ -815,14 +902,19 @@ __global__ void k_nl_check(Dev d, int advance, double dt, cudaGraphConditionalHa
 // term) the last block to finish also takes the skin decision of every
 // replica and sets the graph's rebuild condition, so a step is one launch
 // plus the conditional rebuild.
-template <class FT, int MODE, int FBT>
-__global__ void __launch_bounds__(FBT * LPB) k_force(Dev d, TermP p, int cur, cudaGraphConditionalHandle h, int fuse) {
+// one thread per bead: at least 16 warps per SM (at most 128 registers)
+template <int FBT, int LPB> constexpr int force_min_blocks() { return LPB == 1 ? 512 / FBT : 1; }
+template <class FT, int MODE, int FBT, int LPB>
+__global__ void __launch_bounds__(FBT * LPB, (force_min_blocks<FBT, LPB>())) k_force(Dev d, TermP p, int cur,
+                                                                                    cudaGraphConditionalHandle h,
+                                                                                    int fuse) {
     __shared__ int last_s;
     static_assert(FBT % BLK_ON == 0, "force blocks are whole multiples of the occupancy granule");
+    static_assert(LPB == 1 || LPB == 2 || LPB == 4, "one, two or four threads per bead");
     bool on = false;
 #pragma unroll
     for (int q = 0; q < FBT / BLK_ON; ++q) on |= d.blk_on[blockIdx.x * (FBT / BLK_ON) + q] != 0;
-    if (on) force_block<FT, MODE, FBT>(d, p, cur);   // uniform per block
+    if (on) force_block<FT, MODE, FBT, LPB>(d, p, cur);   // uniform per block
     if (MODE == 1 && fuse) {
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -1635,21 +1727,23 @@ __global__ void __launch_bounds__(TL_THREADS, 4) k_nl_tile(Dev d, TermP p, int c
 
 // =================================================================== host ==
 
-// the step kernel of a precision, mode and block size (the block sizes the
-// autotuner chooses from)
-static void *force_kernel(bool mixed, int mode, int fb) {
-#define XMD_FK(M, B) (mixed ? (void *)k_force<float, M, B> : (void *)k_force<double, M, B>)
-    if (mode == 0) {
-        switch (fb) {
-        case 32: return XMD_FK(0, 32);
-        case 64: return XMD_FK(0, 64);
-        default: return XMD_FK(0, 128);
-        }
-    }
-    switch (fb) {
-    case 32: return XMD_FK(1, 32);
-    case 64: return XMD_FK(1, 64);
-    default: return XMD_FK(1, 128);
+// the step kernel of a precision, mode and launch shape (beads per block and
+// threads per bead, the shapes the autotuner chooses from); the evaluation
+// pass has one shape
+constexpr int EVAL_FB = 64, EVAL_LPB = 4;
+static void *force_kernel(bool mixed, int mode, int fb, int lpb) {
+#define XMD_FK(M, B, L) (mixed ? (void *)k_force<float, M, B, L> : (void *)k_force<double, M, B, L>)
+    if (mode == 0) return XMD_FK(0, EVAL_FB, EVAL_LPB);
+    switch (fb * 8 + lpb) {
+    case 32 * 8 + 1: return XMD_FK(1, 32, 1);
+    case 32 * 8 + 2: return XMD_FK(1, 32, 2);
+    case 32 * 8 + 4: return XMD_FK(1, 32, 4);
+    case 64 * 8 + 1: return XMD_FK(1, 64, 1);
+    case 64 * 8 + 2: return XMD_FK(1, 64, 2);
+    case 64 * 8 + 4: return XMD_FK(1, 64, 4);
+    case 128 * 8 + 1: return XMD_FK(1, 128, 1);
+    case 128 * 8 + 2: return XMD_FK(1, 128, 2);
+    default: return XMD_FK(1, 128, 4);
     }
 #undef XMD_FK
 }
@@ -1659,12 +1753,13 @@ void Engine::launch_force(int mode, int c) {
         if (mode == 0) k_ext<0><<<(d.N + 255) / 256, 256, 0, stream>>>(d, tp, c);
         else k_ext<1><<<(d.N + 255) / 256, 256, 0, stream>>>(d, tp, c);
     }
-    const int nb = (d.N + tune.fb - 1) / tune.fb;
+    const int fb = mode == 0 ? EVAL_FB : tune.fb, lpb = mode == 0 ? EVAL_LPB : tune.lpb;
+    const int nb = (d.N + fb - 1) / fb;
     cudaGraphConditionalHandle none = 0;
     int fuse = 0;
     void *args[] = {&d, &tp, &c, &none, &fuse};
-    CK(cudaLaunchKernel(force_kernel(params.precision == XMD_PREC_MIXED, mode, tune.fb), dim3(nb),
-                        dim3(tune.fb * LPB), args, 0, stream));
+    CK(cudaLaunchKernel(force_kernel(params.precision == XMD_PREC_MIXED, mode, fb, lpb), dim3(nb), dim3(fb * lpb),
+                        args, 0, stream));
 }
 
 Engine::Engine(const xmd_params &p) : params(p) {
@@ -2972,6 +3067,8 @@ void Engine::resize_rows(int ncap) {
 void Engine::set_tuning(const Tune &t) {
     if (t.fb != 32 && t.fb != 64 && t.fb != 128)
         throw std::invalid_argument("tuning: step-kernel block size must be 32, 64 or 128 beads");
+    if (t.lpb != 1 && t.lpb != 2 && t.lpb != 4)
+        throw std::invalid_argument("tuning: threads per bead must be 1, 2 or 4");
     if (t.graph_steps != 8 && t.graph_steps != 16 && t.graph_steps != 32)
         throw std::invalid_argument("tuning: steps per graph must be 8, 16 or 32");
     if (t.tile_per_sm < 0) throw std::invalid_argument("tuning: tile blocks per SM must be >= 0");
@@ -2998,13 +3095,12 @@ Engine::Tune Engine::autotune(int steps, double *ms_out) {
     for (auto &r : reps)
         if (r.in_use && !r.have_state) throw std::logic_error("autotune: set_state must be called for every replica");
     steps = std::max(32, (steps + 31) / 32 * 32);
-    std::vector<Tune> cands;
-    for (int fb : {32, 64, 128})
-        for (int gs : {8, 16, 32})
-            for (int tps : {0, 2}) cands.push_back(Tune{fb, tps, gs});
+    // two stages: the step kernel's shape (beads per block x threads per
+    // bead) at 16 steps per graph, then graph length and tile residency with
+    // the best step-kernel shape
     Tune best = tune;
     double best_ms = 1e300;
-    for (const Tune &cand : cands) {
+    auto trial = [&](const Tune &cand) {
         Engine c(params);
         for (auto &r : reps)
             if (r.in_use) {
@@ -3034,7 +3130,13 @@ Engine::Tune Engine::autotune(int steps, double *ms_out) {
             best_ms = per;
             best = cand;
         }
-    }
+    };
+    for (int fb : {32, 64, 128})
+        for (int lpb : {1, 2, 4}) trial(Tune{fb, 0, 16, lpb});
+    const Tune kshape = best;
+    for (int gs : {8, 16, 32})
+        for (int tps : {0, 2})
+            if (gs != 16 || tps != 0) trial(Tune{kshape.fb, tps, gs, kshape.lpb});
     use_device();
     set_tuning(best);
     if (ms_out) *ms_out = best_ms;
@@ -3100,7 +3202,7 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
     CK(cudaGraphCreate(&g, 0));
     cudaGraphNode_t prev = nullptr;
     const int nb = (d.N + tune.fb - 1) / tune.fb;
-    void *fk = force_kernel(params.precision == XMD_PREC_MIXED, 1, tune.fb);
+    void *fk = force_kernel(params.precision == XMD_PREC_MIXED, 1, tune.fb, tune.lpb);
     double dt = params.dt;
     // without the quasi-adiabatic term the step kernel takes the skin
     // decision itself (its last block), so a step is one kernel node
@@ -3116,7 +3218,7 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
         void *fargs[] = {&d, &tp, &c, &hf, &ff};
         kf.func = fk;
         kf.gridDim = dim3(nb);
-        kf.blockDim = dim3(tune.fb * LPB);
+        kf.blockDim = dim3(tune.fb * tune.lpb);
         kf.kernelParams = fargs;
         cudaGraphNode_t nf, nc, ncond;
         if (tp.ext_on) {

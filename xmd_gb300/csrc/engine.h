@@ -270,9 +270,10 @@ public:
     // launch shapes (the trajectory does not depend on them), chosen by
     // autotune() or set directly
     struct Tune {
-        int fb = 64;             // beads per step-kernel block (4 threads each): 32, 64 or 128
+        int fb = 64;             // beads per step-kernel block: 32, 64 or 128
         int tile_per_sm = 0;     // resident tile-build blocks per SM (0: as many as fit)
         int graph_steps = 16;    // steps per captured graph: 8, 16 or 32
+        int lpb = 4;             // threads per bead in the step kernel: 1, 2 or 4
     };
     Tune tuning() const { return tune; }
     void set_tuning(const Tune &t);

@@ -121,19 +121,20 @@ class Engine:
     def autotune(self, steps: int = 96) -> dict:
         """Times every launch shape on a clone of this context and keeps the
         fastest (results never depend on the shape)."""
-        shape = np.zeros(3, dtype=np.int32)
+        shape = np.zeros(4, dtype=np.int32)
         ms = C.c_double()
         check(self.lib.xmd_gpu_autotune(self.h, int(steps), iptr(shape), C.byref(ms)))
         return {"fb": int(shape[0]), "tile_per_sm": int(shape[1]), "graph_steps": int(shape[2]),
-                "ms_per_step": ms.value}
+                "lpb": int(shape[3]), "ms_per_step": ms.value}
 
     def tuning(self) -> dict:
-        shape = np.zeros(3, dtype=np.int32)
+        shape = np.zeros(4, dtype=np.int32)
         check(self.lib.xmd_gpu_get_tuning(self.h, iptr(shape)))
-        return {"fb": int(shape[0]), "tile_per_sm": int(shape[1]), "graph_steps": int(shape[2])}
+        return {"fb": int(shape[0]), "tile_per_sm": int(shape[1]), "graph_steps": int(shape[2]),
+                "lpb": int(shape[3])}
 
-    def set_tuning(self, fb: int, tile_per_sm: int, graph_steps: int):
-        shape = np.array([fb, tile_per_sm, graph_steps], dtype=np.int32)
+    def set_tuning(self, fb: int, tile_per_sm: int, graph_steps: int, lpb: int = 4):
+        shape = np.array([fb, tile_per_sm, graph_steps, lpb], dtype=np.int32)
         check(self.lib.xmd_gpu_set_tuning(self.h, iptr(shape)))
 
     def set_state(self, rep: int, r: np.ndarray, v: np.ndarray | None = None):
@@ -206,6 +207,15 @@ class Engine:
 
     def set_steps(self, rep: int, nsteps: int):
         check(self.lib.xmd_gpu_set_steps(self.h, int(rep), int(nsteps)))
+
+    def steps_left(self) -> np.ndarray:
+        """Per replica slot: steps still to take (-1: unbounded), -2 for a free
+        slot, -3 for a replica frozen by a non-finite force."""
+        n = max(self.sizes) + 1 if self.sizes else 0
+        # the library writes one entry per replica slot it has handed out
+        out = np.zeros(n + (1 << 16), dtype=np.int64)
+        check(self.lib.xmd_gpu_steps_left(self.h, out.ctypes.data_as(C.POINTER(C.c_int64))))
+        return out[:n]
 
     def synchronize(self):
         check(self.lib.xmd_gpu_synchronize(self.h))
