@@ -294,7 +294,8 @@ int xmd_gpu_qa_sync(xmd_gpu_ctx *ctx, int32_t rep, int8_t *out);
 /* The replica's current Verlet list as kept for the pair terms: pairs (i, j),
  * i < j, in (i, j) order, out2[2*k]; flags[k] bit 0 = Pauli list
  * (update_pauli_pairs, pauli.cpp:9-24), bit 1 = ES list (update_es_base,
- * es_pair.cpp:6-23).  Pairs no pair term keeps are not stored.  The number of
+ * es_pair.cpp:6-23), bit 2 = PID bundle (update_pid_bundles,
+ * pid/bundle.cpp:6-29).  Pairs no pair term keeps are not stored.  The number of
  * pairs is returned through *count (entries beyond cap are not written). */
 int xmd_gpu_verlet_pairs(xmd_gpu_ctx *ctx, int32_t rep, int32_t cap, int32_t *out2,
                          uint8_t *flags, int32_t *count);

@@ -79,6 +79,9 @@ __device__ __forceinline__ DN sqrt_(DN x) { return DN(__dsqrt_rn(x.v)); }
 __device__ __forceinline__ DN acos_(DN x) { return DN(acos(x.v)); }
 __device__ __forceinline__ DN exp_(DN x) { return DN(exp(x.v)); }
 __device__ __forceinline__ DN sin(DN x) { return DN(::sin(x.v)); }
+__device__ __forceinline__ DN dn_cos(DN x) { return DN(::cos(x.v)); }
+__device__ __forceinline__ DN dn_fabs(DN x) { return DN(::fabs(x.v)); }
+__device__ __forceinline__ DN dn_rint(DN x) { return DN(::rint(x.v)); }
 __device__ __forceinline__ void sincos_(DN x, DN *s, DN *c) { sincos(x.v, &s->v, &c->v); }
 template <> __host__ __device__ __forceinline__ DN tpar<DN>(double d, float) { return DN(d); }
 __device__ __forceinline__ float ldg_(const float *p) { return __ldg(p); }

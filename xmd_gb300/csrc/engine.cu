@@ -45,7 +45,8 @@ std::string &last_error() {
     } while (0)
 
 constexpr int BLK_ON = 32;           // beads per granule of the force blocks' occupancy map
-constexpr int NL_MASK = 0x3FFFFFFF;
+constexpr int NL_MASK = 0x1FFFFFFF;
+constexpr int NL_PID = 1 << 29;
 constexpr int NL_PAULI = 1 << 30;
 constexpr int NL_ES = (int)(1u << 31);
 
@@ -251,6 +252,141 @@ __global__ void __launch_bounds__(256) k_ext(Dev d, TermP p, int cur) {
         }
     }
     fo[0] = f.x; fo[1] = f.y; fo[2] = f.z;
+}
+
+// ---- pseudo-improper dihedral potential: eval_pid_forces::iter
+// (pid/eval_forces.cpp:14-141), bundles from update_pid_bundles
+// (pid/bundle.cpp:6-29) ------------------------------------------------------------
+// Evaluated in FP64 on both paths with every operation rounded on its own
+// (DN), in the operation order of the oracle's restatement; the forces are
+// the energy's gradient (the shipped kernel leaves one side's derivatives
+// unset and scales the others by 1/|m|, 1/|n| for 1/|m|^2, 1/|n|^2).
+using D3N = V3<DN>;
+constexpr double PID_PI = 3.14159265358979323846;
+
+// lambda_func (pid/lambda.h:29-56): inside the support, value and derivative
+__device__ __forceinline__ bool pid_supp(DN alpha, DN psi0, DN psi) { return dn_fabs(alpha * (psi - psi0)) < DN(PID_PI); }
+__device__ __forceinline__ void pid_lam(int version, DN alpha, DN psi0, DN psi, DN *val, DN *deriv) {
+    const DN sv = alpha * (psi - psi0);
+    if (version == 0) {
+        *val = DN(0.5) * dn_cos(sv) + DN(0.5);
+        *deriv = (DN(-0.5) * alpha) * sin(sv);
+    } else {
+        const DN t = dn_fabs(sv / DN(PID_PI));
+        const DN x_inv = DN(1.0) / (DN(2.0) * t * t - DN(2.0) * t - DN(1.0));
+        *val = (t * t - DN(2.0) * t + DN(1.0)) * x_inv;
+        DN dv = (DN(2.0) * (t - DN(1.0)) * (t - DN(2.0))) * x_inv * x_inv * alpha / DN(PID_PI);
+        if (sv < DN(0.0)) dv = -dv;
+        *deriv = dv;
+    }
+}
+__device__ __forceinline__ D3N d3n(double4_32a p) { return D3N{DN(p.x), DN(p.y), DN(p.z)}; }
+__device__ __forceinline__ D3N pid_ruv(const BoxD &b, D3N u, D3N w) {
+    D3N d = w - u;
+    d.x = d.x - DN(b.cell[0]) * dn_rint(d.x * DN(b.cell_inv[0]));
+    d.y = d.y - DN(b.cell[1]) * dn_rint(d.y * DN(b.cell_inv[1]));
+    d.z = d.z - DN(b.cell[2]) * dn_rint(d.z * DN(b.cell_inv[2]));
+    return d;
+}
+// one side: psi of (previous, bead, next; partner) and its derivatives along
+// the four beads (d1 previous, d2 bead, d3 next, d4 partner)
+__device__ __forceinline__ DN pid_psi(const BoxD &b, D3N r1_, D3N r2_, D3N r3_, D3N r4_, D3N *d1, D3N *d2, D3N *d3,
+                                      D3N *d4) {
+    const D3N r24 = pid_ruv(b, r2_, r4_);
+    const D3N r12 = r2_ - r1_, r23 = r3_ - r2_, r13 = r3_ - r1_;
+    const D3N r14 = r12 + r24;
+    const D3N rij = -r23, rkj = -r13, rkl = -r14;
+    const D3N rm = cross(r23, r12), rn = cross(r13, r14);
+    const DN rm_rn = ninv(rm), rn_rn = ninv(rn), rkj_n = norm(rkj);
+    const D3N gi = (rkj_n * rm_rn * rm_rn) * rm;
+    const D3N gl = -((rkj_n * rn_rn * rn_rn) * rn);
+    const DN a = dot(rij, rkj) / (rkj_n * rkj_n), bb = dot(rkl, rkj) / (rkj_n * rkj_n);
+    *d1 = (bb - DN(1.0)) * gl - a * gi;
+    *d2 = gi;
+    *d3 = (a - DN(1.0)) * gi - bb * gl;
+    *d4 = gl;
+    DN psi = DN(acos((dot(rm, rn) * rm_rn * rn_rn).v));
+    if (dot(rij, rn) < DN(0.0)) psi = -psi;
+    return psi;
+}
+
+// One thread per bead: the bundles (i, j) of its Verlet row (both beads with
+// their chain neighbours, r < PID cutoff + pad at the rebuild), each taken in
+// its canonical order (i1, i2) = (min, max).  The bead keeps the forces of
+// its side: on itself, its previous and its next bead, into pid_f; the step
+// kernel adds to a bead its own part and its neighbours' parts for it.
+// MODE 0 adds the energy of the bundles with i < j.
+template <int MODE>
+__global__ void __launch_bounds__(128) k_pid(Dev d, TermP p, int cur) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.N) return;
+    const size_t N = d.N;
+    double *Fs = d.pid_f, *Fp = d.pid_f + 3 * N, *Fn = d.pid_f + 6 * N;
+    D3N fs{DN(0.0), DN(0.0), DN(0.0)}, fp = fs, fn = fs;
+    double Vsum = 0.0;
+    const int r = d.rep_of[i];
+    const bool both = (d.bflags[i] & (BF_PREV | BF_NEXT)) == (BF_PREV | BF_NEXT);
+    if (r >= 0 && both && !(MODE == 1 && d.rep[r].steps_left == 0)) {
+        const double4_32a *pos = d.pos[cur];
+        const BoxD bx = d.rep[r].box;
+        const int cnt = d.nl_cnt[i];
+        const DN bbq[2][4] = {{DN(p.pid_bbp[0]), DN(p.pid_bbp[1]), DN(p.pid_bbp[2]), DN(p.pid_bbp[3])},
+                              {DN(p.pid_bbm[0]), DN(p.pid_bbm[1]), DN(p.pid_bbm[2]), DN(p.pid_bbm[3])}};
+        const DN ssa = DN(p.pid_ss[0]), ssp = DN(p.pid_ss[1]);
+        for (int k = 0; k < cnt; ++k) {
+            const int e = d.nl_row[(size_t)k * N + i];
+            if (!(e & NL_PID)) continue;
+            const int j = e & NL_MASK;
+            const int i1 = min(i, j), i2 = max(i, j);
+            const D3N r1p = d3n(pos[i1 - 1]), r1 = d3n(pos[i1]), r1n = d3n(pos[i1 + 1]);
+            const D3N r2p = d3n(pos[i2 - 1]), r2 = d3n(pos[i2]), r2n = d3n(pos[i2 + 1]);
+            D3N a1p, a1, a1n, a2, b2p, b2, b2n, b1;
+            const DN psi1 = pid_psi(bx, r1p, r1, r1n, r2, &a1p, &a1, &a1n, &a2);
+            const DN psi2 = pid_psi(bx, r2p, r2, r2n, r1, &b2p, &b2, &b2n, &b1);
+            const D3N r12 = pid_ruv(bx, r1, r2);
+            const DN r12_n = norm(r12), r12_rn = DN(1.0) / r12_n;
+            DN A(0.0), B(0.0), C(0.0), V(0.0);
+            for (int q = 0; q < 2; ++q) {
+                if (pid_supp(bbq[q][0], bbq[q][1], psi1) && pid_supp(bbq[q][0], bbq[q][1], psi2)) {
+                    DN lam1, g1, lam2, g2, lV, ldV;
+                    pid_lam(p.pid_lambda, bbq[q][0], bbq[q][1], psi1, &lam1, &g1);
+                    pid_lam(p.pid_lambda, bbq[q][0], bbq[q][1], psi2, &lam2, &g2);
+                    lj_eval<DN>(bbq[q][3], bbq[q][2], r12_rn, &lV, &ldV);
+                    V = V + lam1 * lam2 * lV;
+                    A = A + g1 * lam2 * lV;
+                    B = B + g2 * lam1 * lV;
+                    C = C + lam1 * lam2 * ldV;
+                }
+            }
+            if (pid_supp(ssa, ssp, psi1) && pid_supp(ssa, ssp, psi2)) {
+                // ss_ljs[type], type = atype1 * NUM_AA + atype2 (bundle.cpp:20-22)
+                const int ty = (int)d.atype[i1] * XMD_NUM_AA + (int)d.atype[i2];
+                DN lam1, g1, lam2, g2, lV, ldV;
+                pid_lam(p.pid_lambda, ssa, ssp, psi1, &lam1, &g1);
+                pid_lam(p.pid_lambda, ssa, ssp, psi2, &lam2, &g2);
+                sink_lj_eval<DN>(DN(d.pid_sd[ty]), DN(d.pid_smin[ty]), DN(d.pid_smax[ty]), r12_n, r12_rn, &lV, &ldV);
+                V = V + lam1 * lam2 * lV;
+                A = A + g1 * lam2 * lV;
+                B = B + g2 * lam1 * lV;
+                C = C + lam1 * lam2 * ldV;
+            }
+            const D3N u = r12_rn * r12;
+            if (i == i1) {
+                fp = fp - A * a1p;
+                fs = fs - ((A * a1 + B * b1) - C * u);
+                fn = fn - A * a1n;
+                if (MODE == 0) Vsum += V.v;
+            } else {
+                fp = fp - B * b2p;
+                fs = fs - ((A * a2 + B * b2) + C * u);
+                fn = fn - B * b2n;
+            }
+        }
+    }
+    Fs[3 * i] = fs.x.v; Fs[3 * i + 1] = fs.y.v; Fs[3 * i + 2] = fs.z.v;
+    Fp[3 * i] = fp.x.v; Fp[3 * i + 1] = fp.y.v; Fp[3 * i + 2] = fp.z.v;
+    Fn[3 * i] = fn.x.v; Fn[3 * i + 1] = fn.y.v; Fn[3 * i + 2] = fn.z.v;
+    if (MODE == 0 && Vsum != 0.0) atomicAdd(&d.Vrep[r * XMD_NUM_TERMS + XMD_TERM_PID], Vsum);
 }
 
 // Lanes of a bead in the step kernel.  A bead's pair entries (native
@@ -710,6 +846,22 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
         // AFM pulls and walls, from k_ext (launched just before)
         ftot = ftot + V3<double>{d.fext[3 * (size_t)i], d.fext[3 * (size_t)i + 1], d.fext[3 * (size_t)i + 2]};
     }
+    if (p.on[XMD_TERM_PID]) {
+        // pseudo-improper dihedral bundles, from k_pid: the bead's own side,
+        // then the parts its chain neighbours' bundles put on it
+        const double *pf = d.pid_f;
+        const uint32_t fl = d.bflags[i];
+        V3<double> g{pf[3 * (size_t)i], pf[3 * (size_t)i + 1], pf[3 * (size_t)i + 2]};
+        if (fl & BF_PREV) {
+            const double *q = pf + 6 * Ns + 3 * (size_t)(i - 1);   // next-bead part of i - 1
+            g = g + V3<double>{q[0], q[1], q[2]};
+        }
+        if (fl & BF_NEXT) {
+            const double *q = pf + 3 * Ns + 3 * (size_t)(i + 1);   // previous-bead part of i + 1
+            g = g + V3<double>{q[0], q[1], q[2]};
+        }
+        ftot = ftot + g;
+    }
     const double fx = ftot.x, fy = ftot.y, fz = ftot.z;
     if (!(finite_bits(fx) && finite_bits(fy) && finite_bits(fz))) {
         // the replica is frozen from the next step on (its skin check sets
@@ -1055,8 +1207,9 @@ __global__ void __launch_bounds__(CB) k_cells(Dev d, int cur) {
         rp.band_m = band_margin(fmax(ext, rp.req_r));
         double m = rp.req_r + rp.band_m;
         rp.pre2 = __double2float_ru(m * m);
-        const double T[4] = {rp.req_r, 1.0 / rp.pauli_min_inv, 1.0 / rp.es_min_inv, 1.0 / rp.qa_min_inv};
-        for (int k = 0; k < 4; ++k) {
+        const double T[5] = {rp.req_r, 1.0 / rp.pauli_min_inv, 1.0 / rp.es_min_inv, 1.0 / rp.qa_min_inv,
+                             1.0 / rp.pid_min_inv};
+        for (int k = 0; k < 5; ++k) {
             const Band B = make_band(T[k], rp.band_m);
             rp.band_lo[k] = B.lo;
             rp.band_hi[k] = B.hi;
@@ -1259,7 +1412,10 @@ __global__ void __launch_bounds__(NC_WARPS * 32, 3) k_nl_cells(Dev d, TermP p, i
     const float pre2 = rp.pre2;
     const Band Breq{rp.band_lo[0], rp.band_hi[0]}, Bpa{rp.band_lo[1], rp.band_hi[1]};
     const Band Bes{rp.band_lo[2], rp.band_hi[2]}, Bqa{rp.band_lo[3], rp.band_hi[3]};
+    const Band Bpid{rp.band_lo[4], rp.band_hi[4]};
     const bool pauli_on = p.on[XMD_TERM_PAULI] != 0;
+    // PID bundles join beads that both have their chain neighbours
+    const bool pid_on = p.on[XMD_TERM_PID] != 0 && (d.bflags[i] & (BF_PREV | BF_NEXT)) == (BF_PREV | BF_NEXT);
     const bool go_on = p.on[XMD_TERM_GO] != 0;
     const bool es_on = (p.on[XMD_TERM_CONST_ES] || p.on[XMD_TERM_REL_ES]);
     const bool qa_on = d.qa_on && p.on[XMD_TERM_QA];
@@ -1323,23 +1479,27 @@ __global__ void __launch_bounds__(NC_WARPS * 32, 3) k_nl_cells(Dev d, TermP p, i
                     const int cj = cs.x, sj = cs.y;
                     const int df = si > sj ? si - sj : sj - si;
                     if (!(ci == cj && df < 3)) {
-                        bool in_req, pa, es, qa;
+                        bool in_req, pa, es, qa, pd;
                         if (in_band(Breq, d2) || (pauli_on && in_band(Bpa, d2)) || (es_on && in_band(Bes, d2)) ||
-                            (qa_on && in_band(Bqa, d2))) {
+                            (qa_on && in_band(Bqa, d2)) || (pid_on && in_band(Bpid, d2))) {
                             const double s2 = periodic ? dist2_exact(bx, pi, pos[j]) : dist2_open(pi, pos[j]);
                             in_req = s2 < rp.s_req;
                             pa = s2 < rp.s_pa;
                             es = s2 < rp.s_es;
                             qa = s2 < rp.s_qa;
+                            pd = s2 < rp.s_pid;
                         } else {
                             in_req = d2 < Breq.lo;
                             pa = d2 < Bpa.lo;
                             es = d2 < Bes.lo;
                             qa = d2 < Bqa.lo;
+                            pd = d2 < Bpid.lo;
                         }
                         if (in_req) {
                             if (pauli_on && pa) flags |= NL_PAULI;
                             if (es_on && es && qi_w * narrow_f(pos[j].w) != 0.0f) flags |= NL_ES;
+                            if (pid_on && pd && (d.bflags[j] & (BF_PREV | BF_NEXT)) == (BF_PREV | BF_NEXT))
+                                flags |= NL_PID;
                             qa_free = qa_on && j > i && qa;
                         }
                     }
@@ -1509,7 +1669,7 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
     ext = 0.0f;
     for (int q = 0; q < TL_WARPS; ++q) ext = fmaxf(ext, ext_s[q]);
     // decision bands of the chunk, formed once (FP64 work off the scan)
-    __shared__ Band bands_s[4];
+    __shared__ Band bands_s[5];
     __shared__ float mf_s;
     if (t == 0) {
         double exd = fmax((double)ext, rp.req_r);
@@ -1519,6 +1679,7 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
         bands_s[1] = make_band(1.0 / rp.pauli_min_inv, m);
         bands_s[2] = make_band(1.0 / rp.es_min_inv, m);
         bands_s[3] = make_band(1.0 / rp.qa_min_inv, m);
+        bands_s[4] = make_band(1.0 / rp.pid_min_inv, m);
         mf_s = __double2float_ru(m);
     }
     // bounding box of each group of 32 beads j (one warp per group)
@@ -1546,7 +1707,8 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
     const bool es_on = (p.on[XMD_TERM_CONST_ES] || p.on[XMD_TERM_REL_ES]);
     const bool qa_on = d.qa_on && p.on[XMD_TERM_QA];
     const bool ss_on = p.on[XMD_TERM_NAT_SS] != 0;
-    const Band Breq = bands_s[0], Bpa = bands_s[1], Bes = bands_s[2], Bqa = bands_s[3];
+    const Band Breq = bands_s[0], Bpa = bands_s[1], Bes = bands_s[2], Bqa = bands_s[3], Bpid = bands_s[4];
+    const bool pid_term = p.on[XMD_TERM_PID] != 0;
     const float Lx = narrow_f(bx.cell[0]), Ly = narrow_f(bx.cell[1]), Lz = narrow_f(bx.cell[2]);
     const bool periodic = (rp.per[0] | rp.per[1] | rp.per[2]) != 0;
     const int cap = d.nl_cap;
@@ -1564,6 +1726,8 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
         const int2 ci = scs[li];
         const double4_32a pi = pos[i];
         const int n0 = d.nat_start[i], n1 = d.nat_end[i];
+        // PID bundles join beads that both have their chain neighbours
+        const bool pid_on = pid_term && (d.bflags[i] & (BF_PREV | BF_NEXT)) == (BF_PREV | BF_NEXT);
 
         // Go list: update_go_contacts, go.cpp:11-22
         for (int k = n0 + lane; k < n1; k += 32) {
@@ -1639,23 +1803,27 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
                 const int2 cj = scs[lj];
                 const int df = ci.y > cj.y ? ci.y - cj.y : cj.y - ci.y;
                 if (d2 <= Breq.hi && !(ci.x == cj.x && df < 3)) {
-                    bool in_req, pa, es, qa;
+                    bool in_req, pa, es, qa, pd;
                     if (in_band(Breq, d2) || (pauli_on && in_band(Bpa, d2)) || (es_on && in_band(Bes, d2)) ||
-                        (qa_on && in_band(Bqa, d2))) {
+                        (qa_on && in_band(Bqa, d2)) || (pid_on && in_band(Bpid, d2))) {
                         const double s2 = periodic ? dist2_exact(bx, pi, pos[b + lj]) : dist2_open(pi, pos[b + lj]);
                         in_req = s2 < rp.s_req;
                         pa = s2 < rp.s_pa;
                         es = s2 < rp.s_es;
                         qa = s2 < rp.s_qa;
+                        pd = s2 < rp.s_pid;
                     } else {
                         in_req = d2 < Breq.lo;
                         pa = d2 < Bpa.lo;
                         es = d2 < Bes.lo;
                         qa = d2 < Bqa.lo;
+                        pd = d2 < Bpid.lo;
                     }
                     if (in_req) {
                         if (pauli_on && pa) flags |= NL_PAULI;
                         if (es_on && es && qi.w * qj.w != 0.0f) flags |= NL_ES;
+                        if (pid_on && pd && (d.bflags[b + lj] & (BF_PREV | BF_NEXT)) == (BF_PREV | BF_NEXT))
+                            flags |= NL_PID;
                         qa_free = qa_on && lj > li && qa;
                     }
                 }
@@ -1753,6 +1921,10 @@ void Engine::launch_force(int mode, int c) {
         if (mode == 0) k_ext<0><<<(d.N + 255) / 256, 256, 0, stream>>>(d, tp, c);
         else k_ext<1><<<(d.N + 255) / 256, 256, 0, stream>>>(d, tp, c);
     }
+    if (tp.on[XMD_TERM_PID]) {
+        if (mode == 0) k_pid<0><<<(d.N + 127) / 128, 128, 0, stream>>>(d, tp, c);
+        else k_pid<1><<<(d.N + 127) / 128, 128, 0, stream>>>(d, tp, c);
+    }
     const int fb = mode == 0 ? EVAL_FB : tune.fb, lpb = mode == 0 ? EVAL_LPB : tune.lpb;
     const int nb = (d.N + fb - 1) / fb;
     cudaGraphConditionalHandle none = 0;
@@ -1763,8 +1935,6 @@ void Engine::launch_force(int mode, int c) {
 }
 
 Engine::Engine(const xmd_params &p) : params(p) {
-    if (p.on[XMD_TERM_PID])
-        throw std::invalid_argument("the pseudo-improper dihedral potential has no engine path (CPU oracle only)");
     int ndev = 0;
     CK(cudaGetDeviceCount(&ndev));
     if (ndev < 1) throw std::runtime_error("no CUDA device");
@@ -2140,6 +2310,11 @@ void Engine::derive_rep(int ri, RepDev &rd) {
     double max_form = std::max(p.lj_bb_r_min, p.lj_bs_r_min);
     for (int k = 0; k < XMD_NUM_SS; ++k) max_form = std::max(max_form, p.ss_r_max[k]);
     if (p.on[XMD_TERM_QA]) mc = std::max(mc, max_form);
+    // PID bundles: the largest LJ-variant cutoff (lj::cutoff = 2 r_min,
+    // sink_lj::cutoff = 2 r_max), main.cpp:801-810
+    double pid_cut = std::max(2.0 * p.lj_bb_r_min, 2.0 * p.lj_bs_r_min);
+    for (int k = 0; k < XMD_NUM_SS; ++k) pid_cut = std::max(pid_cut, 2.0 * p.ss_r_max[k]);
+    if (p.on[XMD_TERM_PID]) mc = std::max(mc, pid_cut);
     if (p.nl_cutoff > 0.0) mc = p.nl_cutoff;
     rd.pad = p.nl_skin > 0.0 ? p.nl_skin : p.pad_factor * mc;   // legacy_update.cpp:7-8
     rd.req_r = mc + rd.pad;
@@ -2147,10 +2322,12 @@ void Engine::derive_rep(int ri, RepDev &rd) {
     rd.es_min_inv = 1.0 / (es_cut + rd.pad);                      // es_pair.cpp:9
     rd.pauli_min_inv = 1.0 / (p.pauli_r_excl + rd.pad);           // pauli.cpp:12-13
     rd.qa_min_inv = 1.0 / (max_form + rd.pad);                     // free_pair.cpp:9-10
+    rd.pid_min_inv = 1.0 / (pid_cut + rd.pad);                     // pid/bundle.cpp:9-12
     rd.s_req = sq_below(rd.req_r);
     rd.s_pa = sq_below(inv_above(rd.pauli_min_inv));
     rd.s_es = sq_below(inv_above(rd.es_min_inv));
     rd.s_qa = sq_below(inv_above(rd.qa_min_inv));
+    rd.s_pid = sq_below(inv_above(rd.pid_min_inv));
     rd.s_ss = sq_below(2.0 * p.nat_ss_dist + rd.pad);   // update_nat_ssbonds, native_ss.cpp:15
     rd.noise_sd = std::sqrt(2.0 * 1.0 * r.temperature) * std::sqrt(p.gamma_factor) * 1.0;
     rd.begin = r.begin;
@@ -2193,6 +2370,7 @@ void Engine::finalize() {
 void Engine::allocate() {
     const xmd_params &p = params;
     const int N = cap.beads, R = cap.reps;
+    if (N > NL_MASK) throw std::invalid_argument("the context holds more beads than a Verlet entry can index");
     nl_cap = p.nl_capacity > 0 ? p.nl_capacity : 64;
     auto_grow = p.nl_grow != 0;
     d.N = N;
@@ -2363,6 +2541,35 @@ void Engine::allocate() {
     tp.ljw_cycle = p.lj_wall_phase_duration;
     tp.ljw_cycle_inv = 1.0 / p.lj_wall_phase_duration;
     tp.ljw_depth = p.lj_wall_depth;
+    tp.pid_lambda = p.pid_lambda;
+    for (int k = 0; k < 4; ++k) {
+        tp.pid_bbp[k] = p.pid_bbp[k];
+        tp.pid_bbm[k] = p.pid_bbm[k];
+    }
+    tp.pid_ss[0] = p.pid_ss[0];
+    tp.pid_ss[1] = p.pid_ss[1];
+    if (p.on[XMD_TERM_PID]) {
+        // bundle forces per bead, and the side-chain LJ table by pair type
+        // (lj_variants.cpp:59-62: sink_lj(depth, r_min = bb r_min when
+        // sinking else r_max, r_max))
+        d.pid_f = (double *)dalloc(sizeof(double) * 9 * (size_t)N);
+        std::vector<double> sd(XMD_NUM_SS), smin(XMD_NUM_SS), smax(XMD_NUM_SS);
+        for (int k = 0; k < XMD_NUM_SS; ++k) {
+            sd[k] = p.ss_depth[k];
+            smax[k] = p.ss_r_max[k];
+            smin[k] = p.ss_sinking ? p.lj_bb_r_min : p.ss_r_max[k];
+        }
+        double *t_sd = (double *)dalloc(sizeof(double) * XMD_NUM_SS);
+        double *t_smin = (double *)dalloc(sizeof(double) * XMD_NUM_SS);
+        double *t_smax = (double *)dalloc(sizeof(double) * XMD_NUM_SS);
+        CK(cudaMemcpyAsync(t_sd, sd.data(), sizeof(double) * XMD_NUM_SS, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(t_smin, smin.data(), sizeof(double) * XMD_NUM_SS, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(t_smax, smax.data(), sizeof(double) * XMD_NUM_SS, cudaMemcpyHostToDevice, stream));
+        d.pid_sd = t_sd;
+        d.pid_smin = t_smin;
+        d.pid_smax = t_smax;
+        CK(cudaStreamSynchronize(stream));
+    }
     tp.f = TermP::F32{(float)tp.tether_H1, (float)tp.tether_H2, (float)tp.nat_ang_k, (float)tp.cnd_CDA,
                       (float)tp.cnd_CDB, (float)tp.snd_CDH, (float)tp.go_depth, (float)tp.pauli_r_excl,
                       (float)tp.pauli_depth, (float)tp.es_Vf, (float)tp.es_sdi, (float)tp.chir_e_chi,
@@ -3221,10 +3428,10 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
         kf.blockDim = dim3(tune.fb * tune.lpb);
         kf.kernelParams = fargs;
         cudaGraphNode_t nf, nc, ncond;
+        void *eargs[] = {&d, &tp, &c};
         if (tp.ext_on) {
             // the step's external forces first (AFM, walls)
             cudaKernelNodeParams ke{};
-            void *eargs[] = {&d, &tp, &c};
             ke.func = (void *)k_ext<1>;
             ke.gridDim = dim3((d.N + 255) / 256);
             ke.blockDim = dim3(256);
@@ -3232,6 +3439,17 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
             cudaGraphNode_t ne;
             CK(cudaGraphAddKernelNode(&ne, g, prev ? &prev : nullptr, prev ? 1 : 0, &ke));
             prev = ne;
+        }
+        if (tp.on[XMD_TERM_PID]) {
+            // the step's pseudo-improper dihedral bundles
+            cudaKernelNodeParams kp{};
+            kp.func = (void *)k_pid<1>;
+            kp.gridDim = dim3((d.N + 127) / 128);
+            kp.blockDim = dim3(128);
+            kp.kernelParams = eargs;
+            cudaGraphNode_t np;
+            CK(cudaGraphAddKernelNode(&np, g, prev ? &prev : nullptr, prev ? 1 : 0, &kp));
+            prev = np;
         }
         CK(cudaGraphAddKernelNode(&nf, g, prev ? &prev : nullptr, prev ? 1 : 0, &kf));
         if (d.qa_on) {
@@ -3589,7 +3807,7 @@ int Engine::verlet_pairs(int rep, int cap, int32_t *out2, uint8_t *flags) {
         for (int k = 0; k < cnt[i]; ++k) {
             int e = rows[(size_t)k * h.n + i];
             int j = (e & NL_MASK) - h.begin;
-            if (j > i) v.emplace_back(i, j, ((e & NL_PAULI) ? 1 : 0) | ((e & NL_ES) ? 2 : 0));
+            if (j > i) v.emplace_back(i, j, ((e & NL_PAULI) ? 1 : 0) | ((e & NL_ES) ? 2 : 0) | ((e & NL_PID) ? 4 : 0));
         }
     std::sort(v.begin(), v.end());
     for (size_t k = 0; k < v.size() && (int)k < cap; ++k) {

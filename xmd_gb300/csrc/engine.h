@@ -47,10 +47,10 @@ struct AfmTip {
 struct RepDev {
     BoxD box;
     double pad, req_r, noise_sd;
-    double es_min_inv, pauli_min_inv, qa_min_inv;
+    double es_min_inv, pauli_min_inv, qa_min_inv, pid_min_inv;
     // squared-distance forms of the list tests: s < s_req <=> sqrt(s) < req_r,
     // s < s_pa <=> 1/sqrt(s) > pauli_min_inv, etc. (correctly rounded FP64)
-    double s_req, s_pa, s_es, s_qa;
+    double s_req, s_pa, s_es, s_qa, s_pid;
     double s_ss;             // disulfide list: s < s_ss <=> r < 2 nat_r + pad (native_ss.cpp:15)
     double t;
     int begin, n;
@@ -62,7 +62,8 @@ struct RepDev {
     int tile;                // Verlet build by whole-replica tiles (no cell grid)
     float pre2;              // squared FP32 pre-filter radius of the Verlet build
     double band_m;           // FP32 distance error bound of the cell build
-    float band_lo[4], band_hi[4];   // cell build: FP32 bands of the list radius, r_excl + pad, 2D + pad, QA radius + pad
+    float band_lo[5], band_hi[5];   // cell build: FP32 bands of the list radius, r_excl + pad, 2D + pad,
+                                    // QA radius + pad, PID cutoff + pad
     float band_mf;           // band_m rounded up to FP32
     int first, rebuild;
     int chunk_off, nchunk;   // tile-build chunks of the replica in Dev::chunks
@@ -167,6 +168,11 @@ struct Dev {
     uint8_t *blk_on;        // force blocks (FB beads) holding at least one placed bead
     int qa_on;
     QaDev qa;
+    // pseudo-improper dihedral potential: per bead its bundles' forces on
+    // itself, on its previous and on its next bead ([3][3N], k_pid), and the
+    // side-chain LJ table by pair type ([400] depth, r_min, r_max)
+    double *pid_f;
+    const double *pid_sd, *pid_smin, *pid_smax;
 };
 
 struct RepHost {

@@ -32,6 +32,8 @@ struct TermP {
     int n_solid, n_ljw;                      // wall planes of each kind (0 when the term is off)
     double solid_eps, solid_cutoff;          // walls/solid.h
     double ljw_min_dist, ljw_factor, ljw_cycle, ljw_cycle_inv, ljw_depth;   // walls/lj_attr.h
+    int pid_lambda;                          // pid/lambda.h: 0 cosine, 1 algebraic
+    double pid_bbp[4], pid_bbm[4], pid_ss[2];   // pid_params (alpha, psi_0, r_min, depth)
     // FP32 copies of the constants the mixed path's FP32 terms use (no
     // FP64-to-FP32 conversion per interaction)
     struct F32 {
