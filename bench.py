@@ -467,6 +467,7 @@ def accuracy_c3(nrep, steps, every, device):
             forces[prec], _ = e.eval_forces(0)
             t0 = time.perf_counter()
             samples = [[(0.0, *[e.observables(k)[f] for f in observe.FIELDS])] for k in range(nrep)]
+            frz = set()
             for t in range(every, steps + 1, every):
                 try:
                     e.step(every)
@@ -476,9 +477,12 @@ def accuracy_c3(nrep, steps, every, device):
                     # others go on, and it leaves the paired comparison
                     if "non-finite" not in str(ex):
                         raise
+                    frz |= {int(k) for k in np.nonzero(e.steps_left()[:nrep] == -3)[0]}
                 for k in range(nrep):
-                    samples[k].append((float(t), *[e.observables(k)[f] for f in observe.FIELDS]))
-            frozen[prec] = [int(k) for k in np.nonzero(e.steps_left()[:nrep] == -3)[0]]
+                    obs = (float("nan"),) * len(observe.FIELDS) if k in frz else \
+                        tuple(e.observables(k)[f] for f in observe.FIELDS)
+                    samples[k].append((float(t), *obs))
+            frozen[prec] = sorted(frz)
             wall[prec] = time.perf_counter() - t0
             runs[prec] = [np.asarray(x) for x in samples]
     keep = [k for k in range(nrep) if k not in frozen["fp64"] and k not in frozen["mixed"]]

@@ -155,3 +155,22 @@ def test_budget_is_the_real_allocation():
     assert 0.9 * budget <= st["device_bytes"] <= budget
     assert st["cap_beads"] * st["bytes_per_bead"] <= budget
     assert 500 <= st["bytes_per_bead"] <= 4096
+
+
+def test_frozen_replica_does_not_fail_the_others_evaluation():
+    """After a replica is frozen by a non-finite force, evaluating (and
+    observing) another replica of the context still works; evaluating the
+    frozen one reports the non-finite force."""
+    bad = diverging()
+    good = synth.make_system([80], 611, box=None, types="charged10", temperature=0.4, rng_seed=611)
+    with Engine(YAML) as e:
+        g = e.add_system(good)
+        b = e.add_system(bad)
+        with pytest.raises(abi.XmdError):
+            e.step(8)
+        assert e.steps_left()[b] == -3
+        F, _ = e.eval_forces(g)
+        assert np.isfinite(F).all()
+        assert np.isfinite(e.observables(g)["E"])
+        with pytest.raises(abi.XmdError):
+            e.eval_forces(b)

@@ -3614,11 +3614,29 @@ void Engine::eval_forces(int rep, double *F, double *V) {
     CK(cudaMemsetAsync(d.Vrep, 0, sizeof(double) * XMD_NUM_TERMS * d.R, stream));
     launch_force(0, cur);
     const RepHost &h = reps[rep];
-    if (F) CK(cudaMemcpyAsync(F, d.F + 3 * (size_t)h.begin, sizeof(double) * 3 * h.n, cudaMemcpyDeviceToHost, stream));
+    std::vector<double> Ft;
+    double *Fh = F;
+    if (!Fh) {
+        Ft.resize(3 * (size_t)h.n);
+        Fh = Ft.data();
+    }
+    CK(cudaMemcpyAsync(Fh, d.F + 3 * (size_t)h.begin, sizeof(double) * 3 * h.n, cudaMemcpyDeviceToHost, stream));
     if (V) CK(cudaMemcpyAsync(V, d.Vrep + (size_t)rep * XMD_NUM_TERMS, sizeof(double) * XMD_NUM_TERMS,
                               cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
-    check_status("eval_forces");
+    // only this replica's forces decide: a replica frozen by a non-finite
+    // force does not fail the evaluation of the others
+    const bool iso = isolate_faults;
+    isolate_faults = true;
+    try {
+        check_status("eval_forces");
+    } catch (...) {
+        isolate_faults = iso;
+        throw;
+    }
+    isolate_faults = iso;
+    for (size_t k = 0; k < 3 * (size_t)h.n; ++k)
+        if (!std::isfinite(Fh[k])) throw std::domain_error("eval_forces: non-finite force");
 }
 
 void Engine::step(int nsteps) {
