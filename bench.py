@@ -442,6 +442,8 @@ def serve_run(requests, precision, nsteps, rate_hz, device, seed=0):
     pct = (lambda q: 1e3 * float(np.percentile(lat, q, method="inverted_cdf"))) if len(lat) else (lambda q: None)
     return {"p50_ms": pct(50), "p99_ms": pct(99), "max_ms": pct(100),
             "bead_steps_per_s": work / wall, "wall_s": wall, "peak_concurrent": int(st["peak_running"]),
+            "worker_admit_s": st["admit_s"], "worker_step_s": st["step_s"], "chunks": int(st["chunks"]),
+            "device_bytes": int(st["device_bytes"]), "bytes_per_bead_slot": st["bytes_per_bead"],
             "requests": len(requests), "completed": len(lat), "failed": failed,
             "steps_per_request": nsteps, "rate_hz": rate_hz,
             "beads_total": int(sum(rq.n for rq in requests))}

@@ -533,10 +533,14 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
         __syncthreads();
     }
 
-    // bonded contributions of centres c in [i0-2, i0+FBT], two tasks per
-    // centre: (tether, angle) and (dihedral, chirality)
-    for (int w = t; w < 2 * (FBT + 3); w += NT) {
-        const int sc = w >> 1, task = w & 1;
+    // bonded contributions of centres c in [i0-2, i0+FBT].  A centre is two
+    // tasks, (tether, angle) and (dihedral, chirality).  With one thread per
+    // bead a thread takes both tasks of its centres; with more, the tasks are
+    // dealt so that the 32 threads of a warp take one task of 32 consecutive
+    // centres (no divergence between the two).
+    constexpr int NC = FBT + 3, NC32 = (NC + 31) / 32 * 32;
+    constexpr int NW = LPB == 1 ? NC : 2 * NC32;
+    auto bonded = [&](const int sc, const int task) {
         const int c = i0 - 2 + sc;
         const uint32_t fl = (c >= 0 && c < N) ? d.bflags[c] : 0u;
         const V3<FT> z{FT(0), FT(0), FT(0)};
@@ -644,6 +648,15 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
                 if (MODE == 0 && own) atomicAdd(&d.Vrep[rc * XMD_NUM_TERMS + XMD_TERM_CHIR], Vch);
             }
             Cd[0][sc] = q[0]; Cd[1][sc] = q[1]; Cd[2][sc] = q[2]; Cd[3][sc] = q[3];
+        }
+    };
+    for (int w = t; w < NW; w += NT) {
+        if constexpr (LPB == 1) {
+            bonded(w, 0);
+            bonded(w, 1);
+        } else {
+            const int sc = ((w >> 6) << 5) | (w & 31);
+            if (sc < NC) bonded(sc, (w >> 5) & 1);
         }
     }
     __syncthreads();
