@@ -442,14 +442,20 @@ template <int LPB> __device__ __forceinline__ double lane_sum(unsigned m, double
     for (int o = 1; o < LPB; o <<= 1) v += __shfl_xor_sync(m, v, o, LPB);
     return v;
 }
-// entries [k0, k1) of a list dealt to the bead's threads: f(k, u) on thread
-// ln for k = k0 + ln + LPB u (mod VL), u being its virtual lane slot
-template <int LPB, class F> __device__ __forceinline__ void deal(int k0, int k1, int ln, F &&f) {
-    for (int kb = k0 + ln; kb < k1; kb += VL) {
-#pragma unroll
-        for (int u = 0; u < VL / LPB; ++u) {
-            const int k = kb + u * LPB;
-            if (k < k1) f(k, u);
+// add f to the accumulator of the thread's m-th entry: virtual lane slot
+// m mod (VL / LPB)
+template <int LPB, class FT> __device__ __forceinline__ void acc_slot(Acc3<FT> (&acc)[VL / LPB], int m, V3<FT> f) {
+    if constexpr (LPB == 4) {
+        acc[0].add(f);
+    } else if constexpr (LPB == 2) {
+        if (m & 1) acc[1].add(f);
+        else acc[0].add(f);
+    } else {
+        switch (m & 3) {
+        case 0: acc[0].add(f); break;
+        case 1: acc[1].add(f); break;
+        case 2: acc[2].add(f); break;
+        default: acc[3].add(f); break;
         }
     }
 }
@@ -701,96 +707,84 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
     const PairGeo<FT> geo(bx, per, pi);
     double vgo = 0, vpa = 0, ves = 0;
 
-    // The pair loops take the thread's U entries of each round of VL
-    // together (their partners' positions are fetched side by side) and are
-    // software-pipelined: the next round's index data is loaded while this
-    // round's positions are fetched.
+    // Thread ln takes entries k0 + ln, k0 + ln + LPB, ... of each list; its
+    // m-th entry goes to its virtual lane slot m mod U (the same slot on every
+    // active thread of the warp, so the slot switch does not diverge).  Each
+    // loop body appears once in the code; the loops are software-pipelined
+    // (the next entry's index data is loaded while this entry's partner is
+    // fetched).
     if (p.on[XMD_TERM_GO]) {
         const int k1 = pf_n1;
-        int jn[U];
-        bool onn[U];
-        FT ndn[U];
-        auto fetch = [&](int kb) {
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int k = kb + u * LPB;
-                const bool in = k < k1;
-                jn[u] = in ? d.nat_j[k] : 0;
-                onn[u] = in && d.nat_on[k] != 0;
-                ndn[u] = in ? nat_dist<FT>(d, k) : FT(0);
+        int k = pf_n0 + ln, m = 0;
+        int j = 0;
+        bool on = false;
+        FT nd = FT(0);
+        if (k < k1) {
+            j = d.nat_j[k];
+            on = d.nat_on[k] != 0;
+            nd = nat_dist<FT>(d, k);
+        }
+        for (; k < k1; k += LPB, ++m) {
+            int jn = 0;
+            bool onn = false;
+            FT ndn = FT(0);
+            if (k + LPB < k1) {
+                jn = d.nat_j[k + LPB];
+                onn = d.nat_on[k + LPB] != 0;
+                ndn = nat_dist<FT>(d, k + LPB);
             }
-        };
-        fetch(pf_n0 + ln);
-        for (int kb = pf_n0 + ln; kb < k1; kb += VL) {
-            int j[U];
-            bool on[U];
-            FT nd[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) { j[u] = jn[u]; on[u] = onn[u]; nd[u] = ndn[u]; }
-            if (kb + VL < k1) fetch(kb + VL);
-            double4_32a pj[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u)
-                if (on[u]) pj[u] = pin[j[u]];
-#pragma unroll
-            for (int u = 0; u < U; ++u)
-                if (on[u]) {
-                    FT V_;
-                    V3<FT> f = go_pair<FT>(p, geo.to(pj[u]), nd[u], &V_);
-                    acc[u].add(f);
-                    if (MODE == 0 && i < j[u]) vgo += (double)V_;
-                }
+            if (on) {
+                FT V_;
+                const V3<FT> f = go_pair<FT>(p, geo.to(pin[j]), nd, &V_);
+                acc_slot<LPB>(acc, m, f);
+                if (MODE == 0 && i < j) vgo += (double)V_;
+            }
+            j = jn;
+            on = onn;
+            nd = ndn;
         }
     }
     double vss = 0;
     if (p.on[XMD_TERM_NAT_SS]) {
-        deal<LPB>(d.ss_start[i], d.ss_end[i], ln, [&](int k, int u) {
-            if (!d.ss_on[k]) return;
+        const int s1 = d.ss_end[i];
+        int m = 0;
+        for (int k = d.ss_start[i] + ln; k < s1; k += LPB, ++m) {
+            if (!d.ss_on[k]) continue;
             const int j = d.ss_j[k];
             FT V_;
-            V3<FT> f = ss_pair<FT>(p, geo.to(pin[j]), &V_);
-            acc[u].add(f);
+            const V3<FT> f = ss_pair<FT>(p, geo.to(pin[j]), &V_);
+            acc_slot<LPB>(acc, m, f);
             if (MODE == 0 && i < j) vss += (double)V_;
-        });
+        }
     }
     {
         const int cnt = pf_cnt;
-        int en[U];
-        auto fetch = [&](int kb) {
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int k = kb + u * LPB;
-                en[u] = k < cnt ? d.nl_row[(size_t)k * N + i] : 0;
+        int e_next = ln < cnt ? d.nl_row[(size_t)ln * N + i] : 0;
+        int m = 0;
+        for (int k = ln; k < cnt; k += LPB, ++m) {
+            const int e = e_next;
+            if (k + LPB < cnt) e_next = d.nl_row[(size_t)(k + LPB) * N + i];
+            const int j = e & NL_MASK;
+            const double4_32a pj = pin[j];
+            const V3<FT> r12 = geo.to(pj);
+            V3<FT> f{FT(0), FT(0), FT(0)};
+            bool any = false;
+            if (e & NL_PAULI) {
+                FT V_;
+                f = pauli_pair<FT>(p, r12, &V_);
+                any = true;
+                if (MODE == 0 && i < j) vpa += (double)V_;
             }
-        };
-        fetch(ln);
-        for (int kb = ln; kb < cnt; kb += VL) {
-            int e[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) e[u] = en[u];
-            if (kb + VL < cnt) fetch(kb + VL);
-            double4_32a pj[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u)
-                if (kb + u * LPB < cnt) pj[u] = pin[e[u] & NL_MASK];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                if (kb + u * LPB >= cnt) continue;
-                const int j = e[u] & NL_MASK;
-                V3<FT> r12 = geo.to(pj[u]);
-                if (e[u] & NL_PAULI) {
-                    FT V_;
-                    V3<FT> f = pauli_pair<FT>(p, r12, &V_);
-                    acc[u].add(f);
-                    if (MODE == 0 && i < j) vpa += (double)V_;
-                }
-                if (e[u] & NL_ES) {
-                    FT V_;
-                    V3<FT> f = es_pair<FT>(p, r12, charge_prod<FT>(pi.w, pj[u].w), &V_);
-                    acc[u].add(f);
-                    if (MODE == 0 && i < j) ves += (double)V_;
-                }
+            if (e & NL_ES) {
+                FT V_;
+                const V3<FT> g = es_pair<FT>(p, r12, charge_prod<FT>(pi.w, pj.w), &V_);
+                // a pair on both lists adds its two forces one after the other
+                if (any) acc_slot<LPB>(acc, m, f);
+                f = g;
+                any = true;
+                if (MODE == 0 && i < j) ves += (double)V_;
             }
+            if (any) acc_slot<LPB>(acc, m, f);
         }
     }
 
@@ -825,7 +819,8 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
             if (u * LPB + ln < nref) Qs[bs][rk[u]] = v[u];
         __syncwarp(qm);
         const double tnow = d.rep[r].t;
-        deal<LPB>(0, nref, ln, [&](int k, int ul) {
+        int m = 0;
+        for (int k = ln; k < nref; k += LPB, ++m) {
             const int slot = Qs[bs][k];
             int i1 = q.ct_i1[slot], i2 = q.ct_i2[slot];
             V3<FT> r12 = geo.between(pin[i1], pin[i2]);
@@ -838,10 +833,9 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
             FT V_, dV_;
             sink_lj_eval<FT>((FT)depth, (FT)rmin, (FT)rmax, r12_rn * nsq(r12), r12_rn, &V_, &dV_);
             V3<FT> f = ((FT)sat * dV_) * u;
-            if (i == i1) acc[ul].add(f);
-            else acc[ul].sub(f);
+            acc_slot<LPB>(acc, m, i == i1 ? f : -f);
             if (MODE == 0 && i == i1) vqa += sat * (double)V_;
-        });
+        }
         if (MODE == 1 && ln == LPB - 1) {
             // n and h at this step's positions (precompute_nh.cpp:12-20)
             D3 n{0, 0, 0}, h{0, 0, 0};
@@ -2663,6 +2657,10 @@ void Engine::allocate() {
         for (double v : req) rmax = std::max(rmax, v);
         const double w = rmax * (1.0 + 1e-9);
         q.req_out2 = w * w;
+        q.req_out2_f = (float)(q.req_out2 * (1.0 + 1e-4));
+        q.min_cos_hr_f = (float)q.min_cos_hr;
+        q.min_cos_hh_f = (float)q.min_cos_hh;
+        q.max_cos_nr_f = (float)q.max_cos_nr;
     }
     CK(cudaStreamSynchronize(stream));
 }

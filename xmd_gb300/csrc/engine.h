@@ -77,6 +77,7 @@ struct RepDev {
     int fp_off, fp_cap, fp_n;
     int qa_bchunk_off, qa_nbchunk;   // chunks of QA_BCHUNK beads in QaDev::bchunk
     int ct_off, ct_cap, ct_n;
+    int qa_removed;          // contacts removed at this step (k_qa_trans; k_qa_refree clears it)
     int afm;                 // some bead of the replica is pulled by an AFM tip
 };
 
@@ -114,6 +115,8 @@ struct QaDev {
     // a squared distance above which no contact type passes the formation
     // distance test (the largest req_min_dist, widened by 1e-9)
     double req_out2;
+    // FP32 forms of the sift's thresholds (the gate widened by 1e-4)
+    float req_out2_f, min_cos_hr_f, min_cos_hh_f, max_cos_nr_f;
 };
 
 // everything a kernel needs, passed by value

@@ -99,46 +99,112 @@ __device__ __forceinline__ int block_exscan(int v, int *out, int *s_warp) {
 // ---- sift_candidates::iter (sift_candidates.cpp:15-77), one thread per slot ----
 // Each block also lists its candidates in slot order (cand_list, cand_blk),
 // so the acceptance visits candidates instead of every free-pair slot.
+//
+// The decisions are taken in FP32 where they are certain: the pair vector
+// from split positions (float-float differences, error <= 2^-24 of each
+// component), unit vectors and the FP64 n, h narrowed on the integer pipe;
+// every dot product of unit vectors is then within 2e-6 of its FP64 value and
+// the squared distance within 1e-6 of it (relative).  A pair whose value lies
+// within QA_BAND of any threshold it is tested against is decided again from
+// scratch in FP64 with explicit rounding (the reference's operations), so the
+// candidate set is exactly the FP64 one.
+constexpr float QA_BAND = 1.0e-5f;
+
+// the FP64 decision (the reference's arithmetic, no contraction): the type
+// and the five geometric tests (back1, back2, bb, side1, side2 in bits 0-4)
+__device__ __noinline__ int qa_sift_fp64(const Dev &d, const RepDev &rp, int i1, int i2, int cur, int *tests) {
+    const QaDev &q = d.qa;
+    const double4_32a *pos = d.pos[cur];
+    const D3 r12 = d3ruv(rp.box, pos[i1], pos[i2]);
+    *tests = 0;
+    if (!(d3dot(r12, r12) <= q.req_out2)) return 0;
+    const double r12_rn = __ddiv_rn(1.0, __dsqrt_rn(d3dot(r12, r12)));
+    const D3 u = d3scl(r12_rn, r12);
+    const size_t N = d.N;
+    const D3 n1{q.nh[i1], q.nh[N + i1], q.nh[2 * N + i1]}, n2{q.nh[i2], q.nh[N + i2], q.nh[2 * N + i2]};
+    const D3 h1{q.nh[3 * N + i1], q.nh[4 * N + i1], q.nh[5 * N + i1]};
+    const D3 h2{q.nh[3 * N + i2], q.nh[4 * N + i2], q.nh[5 * N + i2]};
+    const bool back1 = fabs(d3dot(h1, u)) > q.min_cos_hr;
+    const bool back2 = fabs(d3dot(h2, u)) > q.min_cos_hr;
+    const bool bb_extra = fabs(d3dot(h1, h2)) > q.min_cos_hh;
+    const bool side1 = d3dot(n1, u) < q.max_cos_nr;
+    const bool side2 = -d3dot(n2, u) < q.max_cos_nr;
+    const int a1 = d.atype[i1], a2 = d.atype[i2];
+    int type = 0;
+    if (back1 && back2 && bb_extra) type = 1;
+    else if (back1 && side2) type = 2;
+    else if (side1 && back2) type = 3;
+    else if (side1 && side2) type = 4 + a1 + XMD_NUM_AA * a2;
+    if (type != 0 && 1.0 > __dmul_rn(r12_rn, q.req_min_dist[type])) type = 0;
+    *tests = (back1 ? 1 : 0) | (back2 ? 2 : 0) | (bb_extra ? 4 : 0) | (side1 ? 8 : 0) | (side2 ? 16 : 0);
+    return type;
+}
+
+__device__ __forceinline__ V3<float> nh_f(const QaDev &q, size_t N, int i, int off) {
+    return V3<float>{narrow_f(q.nh[(off + 0) * N + i]), narrow_f(q.nh[(off + 1) * N + i]),
+                     narrow_f(q.nh[(off + 2) * N + i])};
+}
+// x > T (or, with less, x < T) decided in FP32; *unsure when x is within
+// the band of T
+__device__ __forceinline__ bool cmp_band(float x, float T, bool less, bool *unsure) {
+    *unsure |= fabsf(x - T) <= QA_BAND;
+    return less ? x < T : x > T;
+}
+
 __global__ void __launch_bounds__(QA_SIFT) k_qa_sift(Dev d, TermP p, int cur) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     const QaDev &q = d.qa;
+    // the per-bead contact references are listed again at this step's end
+    // (k_qa_refs); nothing reads them before that
+    for (int k = slot; k < d.N; k += gridDim.x * blockDim.x) q.ref_cnt[k] = 0;
     bool live = slot < q.fp_total;
     const int r = live ? q.fp_rep[slot] : 0;
     const RepDev &rp = d.rep[r];
     live = live && slot - rp.fp_off < rp.fp_n;
-    int type = 0;
+    int type = 0, tests = 0;
     int32_t d1p = 0, d2p = 0;
-    const double4_32a *pos = d.pos[cur];
-    D3 r12{0.0, 0.0, 0.0};
     int i1 = 0, i2 = 0;
     if (live && !q.fp_vac[slot]) {
         i1 = q.fp_i1[slot];
         i2 = q.fp_i2[slot];
-        r12 = d3ruv(rp.box, pos[i1], pos[i2]);
-    }
-    // beyond every type's formation distance (with a 1e-9 margin, far above
-    // the rounding of the exact test below) no pair is a candidate: no FP64
-    // square root, division or n/h loads for it
-    if (live && !q.fp_vac[slot] && d3dot(r12, r12) <= q.req_out2) {
-        double r12_rn = __ddiv_rn(1.0, __dsqrt_rn(d3dot(r12, r12)));
-        D3 u = d3scl(r12_rn, r12);
-        const size_t N = d.N;
-        D3 n1{q.nh[i1], q.nh[N + i1], q.nh[2 * N + i1]}, n2{q.nh[i2], q.nh[N + i2], q.nh[2 * N + i2]};
-        D3 h1{q.nh[3 * N + i1], q.nh[4 * N + i1], q.nh[5 * N + i1]};
-        D3 h2{q.nh[3 * N + i2], q.nh[4 * N + i2], q.nh[5 * N + i2]};
-        bool back1 = fabs(d3dot(h1, u)) > q.min_cos_hr;
-        bool back2 = fabs(d3dot(h2, u)) > q.min_cos_hr;
-        bool bb_extra = fabs(d3dot(h1, h2)) > q.min_cos_hh;
-        bool side1 = d3dot(n1, u) < q.max_cos_nr;
-        bool side2 = -d3dot(n2, u) < q.max_cos_nr;
-        int a1 = d.atype[i1], a2 = d.atype[i2];
-        if (back1 && back2 && bb_extra) type = 1;
-        else if (back1 && side2) type = 2;
-        else if (side1 && back2) type = 3;
-        else if (side1 && side2) type = 4 + a1 + XMD_NUM_AA * a2;
-        if (type != 0 && 1.0 > __dmul_rn(r12_rn, q.req_min_dist[type])) type = 0;
+        const double4_32a *pos = d.pos[cur];
+        const bool per = (rp.per[0] | rp.per[1] | rp.per[2]) != 0;
+        const PairGeo<float> geo(rp.box, per, pos[i1]);
+        const V3<float> r12 = geo.to(pos[i2]);
+        const float d2 = r12.x * r12.x + r12.y * r12.y + r12.z * r12.z;
+        // beyond every type's formation distance no pair is a candidate (the
+        // widened FP32 gate keeps every pair the FP64 gate keeps)
+        if (d2 <= q.req_out2_f) {
+            const float rn = 1.0f / sqrtf(d2);
+            const V3<float> u{r12.x * rn, r12.y * rn, r12.z * rn};
+            const size_t N = d.N;
+            const V3<float> n1 = nh_f(q, N, i1, 0), n2 = nh_f(q, N, i2, 0);
+            const V3<float> h1 = nh_f(q, N, i1, 3), h2 = nh_f(q, N, i2, 3);
+            bool unsure = false;
+            const bool back1 = cmp_band(fabsf(dot(h1, u)), q.min_cos_hr_f, false, &unsure);
+            const bool back2 = cmp_band(fabsf(dot(h2, u)), q.min_cos_hr_f, false, &unsure);
+            const bool bb_extra = cmp_band(fabsf(dot(h1, h2)), q.min_cos_hh_f, false, &unsure);
+            const bool side1 = cmp_band(dot(n1, u), q.max_cos_nr_f, true, &unsure);
+            const bool side2 = cmp_band(-dot(n2, u), q.max_cos_nr_f, true, &unsure);
+            const int a1 = d.atype[i1], a2 = d.atype[i2];
+            if (back1 && back2 && bb_extra) type = 1;
+            else if (back1 && side2) type = 2;
+            else if (side1 && back2) type = 3;
+            else if (side1 && side2) type = 4 + a1 + XMD_NUM_AA * a2;
+            if (type != 0) {
+                // r < req_min_dist[type], on squared distances
+                const float rq = narrow_f(q.req_min_dist[type]);
+                const float rq2 = rq * rq;
+                unsure |= fabsf(d2 - rq2) <= QA_BAND * rq2;
+                if (!(d2 < rq2)) type = 0;
+            }
+            tests = (back1 ? 1 : 0) | (back2 ? 2 : 0) | (bb_extra ? 4 : 0) | (side1 ? 8 : 0) | (side2 ? 16 : 0);
+            if (unsure) type = qa_sift_fp64(d, rp, i1, i2, cur, &tests);
+        }
         if (type != 0) {
-            int pt2 = q.ptype[a2], pt1 = q.ptype[a1];
+            const int a1 = d.atype[i1], a2 = d.atype[i2];
+            const int pt2 = q.ptype[a2], pt1 = q.ptype[a1];
+            const bool back1 = tests & 1, back2 = tests & 2, side1 = tests & 8, side2 = tests & 16;
             d1p = pack4(back1, side1, side1 && pt2 == 1, side1 && pt2 == 2);
             d2p = pack4(back2, side2, side2 && pt1 == 1, side2 && pt1 == 2);
             if (!sync_ok_after(q.sync[i1], d1p) || !sync_ok_after(q.sync[i2], d2p)) type = 0;
@@ -318,6 +384,7 @@ __global__ void __launch_bounds__(256) k_qa_trans(Dev d, TermP p, int cur) {
             q.ct_ref[slot] = tnow;
         }
     } else if (status == QA_BREAKING && sat == 0.0) {
+        atomicAdd(&d.rep[r].qa_removed, 1);
         q.ct_vac[slot] = 1;
         atomicAdd(&q.sync[i1], q.ct_d1[slot]);   // bytes stay <= 127: no carry
         atomicAdd(&q.sync[i2], q.ct_d2[slot]);
@@ -326,11 +393,14 @@ __global__ void __launch_bounds__(256) k_qa_trans(Dev d, TermP p, int cur) {
 }
 
 // Removed pairs re-freed at the end of the free-pair list in contact-slot
-// order (process_contacts.cpp:48-55), and the per-bead contact lists cleared.
+// order (process_contacts.cpp:48-55); replicas without a removal at this step
+// return at once.
 __global__ void __launch_bounds__(1024) k_qa_refree(Dev d) {
     const int r = blockIdx.x, t = threadIdx.x;
     RepDev &rp = d.rep[r];
     if (!rp.active || rp.ct_cap == 0) return;
+    // most steps remove no contact: nothing to re-free
+    if (rp.qa_removed == 0) return;
     const QaDev &q = d.qa;
     __shared__ int s_warp[33];
     __shared__ int s_fp_n, s_err;
@@ -356,9 +426,9 @@ __global__ void __launch_bounds__(1024) k_qa_refree(Dev d) {
         if (t == 0) s_fp_n = min(s_fp_n + total, rp.fp_cap);
         __syncthreads();
     }
-    for (int i = rp.begin + t; i < rp.begin + rp.n; i += 1024) q.ref_cnt[i] = 0;
     __syncthreads();
     if (t == 0) {
+        rp.qa_removed = 0;
         rp.fp_n = s_fp_n;
         if (s_err) atomicOr(d.status, 4);
     }
