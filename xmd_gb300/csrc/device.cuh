@@ -689,10 +689,13 @@ __device__ __forceinline__ uint64_t gf2_apply(const uint64_t *__restrict__ col, 
 // and widened once; pair vectors from split positions in FP32 (the minimum
 // image subtracted in float-float), with no FP64 instruction per pair.
 template <class FT> struct Acc3;
+// FP64: every addition rounded on its own (never fused with the product that
+// formed the term), so the sums are the same bits whatever code shape the
+// compiler gives the loops
 template <> struct Acc3<double> {
     double x = 0, y = 0, z = 0;
-    __device__ __forceinline__ void add(V3<double> f) { x += f.x; y += f.y; z += f.z; }
-    __device__ __forceinline__ void sub(V3<double> f) { x += -f.x; y += -f.y; z += -f.z; }
+    __device__ __forceinline__ void add(V3<double> f) { x = __dadd_rn(x, f.x); y = __dadd_rn(y, f.y); z = __dadd_rn(z, f.z); }
+    __device__ __forceinline__ void sub(V3<double> f) { x = __dadd_rn(x, -f.x); y = __dadd_rn(y, -f.y); z = __dadd_rn(z, -f.z); }
     __device__ __forceinline__ V3<double> total() const { return V3<double>{x, y, z}; }
 };
 template <> struct Acc3<float> {

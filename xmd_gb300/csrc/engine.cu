@@ -404,7 +404,7 @@ constexpr int VL = 4;
 template <int LPB> __device__ __forceinline__ unsigned bead_mask(int t) {
     return ((1u << LPB) - 1u) << ((t & 31) & ~(LPB - 1));
 }
-__device__ __forceinline__ double vadd(double a, double b) { return a + b; }
+__device__ __forceinline__ double vadd(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ FF vadd(FF a, FF b) { return ff_add(a, b); }
 __device__ __forceinline__ double xlane(unsigned m, double v, int o, int w) { return __shfl_xor_sync(m, v, o, w); }
 __device__ __forceinline__ FF xlane(unsigned m, FF v, int o, int w) {
