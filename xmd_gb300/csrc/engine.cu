@@ -461,9 +461,15 @@ template <int LPB, class FT> __device__ __forceinline__ void acc_slot(Acc3<FT> (
 }
 __device__ __forceinline__ double comp3(double4_32a v, int a) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); }
 
-template <class FT, int MODE, int FBT, int LPB>
+// beads of a step-kernel block of FB bead slots: with one or two threads per
+// bead the three halo centres of the bonded terms take three slots, so the
+// block's bonded tasks fill its threads exactly once
+template <int FB, int LPB> constexpr int force_beads() { return LPB == 4 ? FB : FB - 3; }
+
+template <class FT, int MODE, int FB, int LPB>
 __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cur) {
-    constexpr int NT = FBT * LPB;
+    constexpr int NT = FB * LPB;
+    constexpr int FBT = force_beads<FB, LPB>();
     constexpr int U = VL / LPB;                 // virtual lanes per thread
     constexpr int AX = (3 + LPB - 1) / LPB;     // integrator axes per thread
     const double4_32a *__restrict__ pin = d.pos[cur];
@@ -492,7 +498,7 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
     // the generator and the list origin); the FP64 path is bound by its FP64
     // pipe instead and loads them where they are used
     constexpr bool EARLY = MODE == 1 && sizeof(FT) == 4;
-    const bool live = i < N;
+    const bool live = bs < FBT && i < N;
     double yv[5 * AX];
     uint64_t st0 = 0;
     double4_32a o_i = make_double4_32a(0, 0, 0, 0);
@@ -1062,18 +1068,19 @@ __global__ void k_nl_check(Dev d, int advance, double dt, cudaGraphConditionalHa
 // replica and sets the graph's rebuild condition, so a step is one launch
 // plus the conditional rebuild.
 // one thread per bead: at least 16 warps per SM (at most 128 registers)
-template <int FBT, int LPB> constexpr int force_min_blocks() { return LPB == 1 ? 512 / FBT : 1; }
-template <class FT, int MODE, int FBT, int LPB>
-__global__ void __launch_bounds__(FBT * LPB, (force_min_blocks<FBT, LPB>())) k_force(Dev d, TermP p, int cur,
-                                                                                    cudaGraphConditionalHandle h,
-                                                                                    int fuse) {
+template <int FB, int LPB> constexpr int force_min_blocks() { return LPB == 1 ? 512 / FB : 1; }
+template <class FT, int MODE, int FB, int LPB>
+__global__ void __launch_bounds__(FB * LPB, (force_min_blocks<FB, LPB>())) k_force(Dev d, TermP p, int cur,
+                                                                                  cudaGraphConditionalHandle h,
+                                                                                  int fuse) {
     __shared__ int last_s;
-    static_assert(FBT % BLK_ON == 0, "force blocks are whole multiples of the occupancy granule");
     static_assert(LPB == 1 || LPB == 2 || LPB == 4, "one, two or four threads per bead");
+    constexpr int FBT = force_beads<FB, LPB>();
+    // the block runs when an occupancy granule of its beads is on (uniform)
+    const int i0 = blockIdx.x * FBT, i1 = min(i0 + FBT, d.N) - 1;
     bool on = false;
-#pragma unroll
-    for (int q = 0; q < FBT / BLK_ON; ++q) on |= d.blk_on[blockIdx.x * (FBT / BLK_ON) + q] != 0;
-    if (on) force_block<FT, MODE, FBT, LPB>(d, p, cur);   // uniform per block
+    for (int g = i0 / BLK_ON; g <= i1 / BLK_ON; ++g) on |= d.blk_on[g] != 0;
+    if (on) force_block<FT, MODE, FB, LPB>(d, p, cur);
     if (MODE == 1 && fuse) {
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -1906,6 +1913,7 @@ __global__ void __launch_bounds__(TL_THREADS, 4) k_nl_tile(Dev d, TermP p, int c
 // threads per bead, the shapes the autotuner chooses from); the evaluation
 // pass has one shape
 constexpr int EVAL_FB = 64, EVAL_LPB = 4;
+static int force_block_beads(int fb, int lpb) { return lpb == 4 ? fb : fb - 3; }
 static void *force_kernel(bool mixed, int mode, int fb, int lpb) {
 #define XMD_FK(M, B, L) (mixed ? (void *)k_force<float, M, B, L> : (void *)k_force<double, M, B, L>)
     if (mode == 0) return XMD_FK(0, EVAL_FB, EVAL_LPB);
@@ -1933,7 +1941,7 @@ void Engine::launch_force(int mode, int c) {
         else k_pid<1><<<(d.N + 127) / 128, 128, 0, stream>>>(d, tp, c);
     }
     const int fb = mode == 0 ? EVAL_FB : tune.fb, lpb = mode == 0 ? EVAL_LPB : tune.lpb;
-    const int nb = (d.N + fb - 1) / fb;
+    const int nb = (d.N + force_block_beads(fb, lpb) - 1) / force_block_beads(fb, lpb);
     cudaGraphConditionalHandle none = 0;
     int fuse = 0;
     void *args[] = {&d, &tp, &c, &none, &fuse};
@@ -3419,7 +3427,7 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
     cudaGraph_t g;
     CK(cudaGraphCreate(&g, 0));
     cudaGraphNode_t prev = nullptr;
-    const int nb = (d.N + tune.fb - 1) / tune.fb;
+    const int nb = (d.N + force_block_beads(tune.fb, tune.lpb) - 1) / force_block_beads(tune.fb, tune.lpb);
     void *fk = force_kernel(params.precision == XMD_PREC_MIXED, 1, tune.fb, tune.lpb);
     double dt = params.dt;
     // without the quasi-adiabatic term the step kernel takes the skin
