@@ -461,10 +461,10 @@ template <int LPB, class FT> __device__ __forceinline__ void acc_slot(Acc3<FT> (
 }
 __device__ __forceinline__ double comp3(double4_32a v, int a) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); }
 
-// beads of a step-kernel block of FB bead slots: with one or two threads per
-// bead the three halo centres of the bonded terms take three slots, so the
-// block's bonded tasks fill its threads exactly once
-template <int FB, int LPB> constexpr int force_beads() { return LPB == 4 ? FB : FB - 3; }
+// beads of a step-kernel block of FB bead slots (a block of FB - 3 beads,
+// whose bonded tasks would fill its threads exactly once, measured slower on
+// config 4: at one thread per bead its grid no longer fits one wave)
+template <int FB, int LPB> constexpr int force_beads() { return FB; }
 
 template <class FT, int MODE, int FB, int LPB>
 __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cur) {
@@ -1068,7 +1068,7 @@ __global__ void k_nl_check(Dev d, int advance, double dt, cudaGraphConditionalHa
 // replica and sets the graph's rebuild condition, so a step is one launch
 // plus the conditional rebuild.
 // one thread per bead: at least 16 warps per SM (at most 128 registers)
-template <int FB, int LPB> constexpr int force_min_blocks() { return LPB == 1 ? 512 / FB : 1; }
+template <int FB, int LPB> constexpr int force_min_blocks() { return LPB == 1 ? 512 / FB : (LPB == 4 ? (768 / (FB * 4) > 0 ? 768 / (FB * 4) : 1) : 1); }
 template <class FT, int MODE, int FB, int LPB>
 __global__ void __launch_bounds__(FB * LPB, (force_min_blocks<FB, LPB>())) k_force(Dev d, TermP p, int cur,
                                                                                   cudaGraphConditionalHandle h,
@@ -1913,7 +1913,7 @@ __global__ void __launch_bounds__(TL_THREADS, 4) k_nl_tile(Dev d, TermP p, int c
 // threads per bead, the shapes the autotuner chooses from); the evaluation
 // pass has one shape
 constexpr int EVAL_FB = 64, EVAL_LPB = 4;
-static int force_block_beads(int fb, int lpb) { return lpb == 4 ? fb : fb - 3; }
+static int force_block_beads(int fb, int) { return fb; }
 static void *force_kernel(bool mixed, int mode, int fb, int lpb) {
 #define XMD_FK(M, B, L) (mixed ? (void *)k_force<float, M, B, L> : (void *)k_force<double, M, B, L>)
     if (mode == 0) return XMD_FK(0, EVAL_FB, EVAL_LPB);
@@ -1957,6 +1957,9 @@ Engine::Engine(const xmd_params &p) : params(p) {
     if (device < 0 || device >= ndev) throw std::invalid_argument("engine: device out of range");
     use_device();
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&ustream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&ev_staged, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ev_removed, cudaEventDisableTiming));
     CK(cudaMallocHost(&h_any, sizeof(int) * 4));
 }
 
@@ -1971,6 +1974,9 @@ Engine::~Engine() {
     for (auto e : ev_rebuild) cudaEventDestroy(e);
     release();
     if (h_any) cudaFreeHost(h_any);
+    if (ev_staged) cudaEventDestroy(ev_staged);
+    if (ev_removed) cudaEventDestroy(ev_removed);
+    if (ustream) cudaStreamDestroy(ustream);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -2080,9 +2086,95 @@ void Engine::remove_replica(int rep) {
         CK(cudaMemsetAsync(d.ss_end + b, 0, sizeof(int32_t) * n, stream));
         a_cells.release(r.cell_off, r.cell_len);
         a_chunks.release(r.chunk_off, r.chunk_len);
+        a_afm.release(r.afm_off, r.afm_len);
+        // staged uploads into these ranges wait for the clears above
+        CK(cudaEventRecord(ev_removed, stream));
+    } else if (r.staged) {
+        // staged, never activated: its uploads are ordered before any later
+        // staging on the side stream, so its ranges can be reused at once
+        for (size_t q = 0; q < staged_reps.size(); ++q)
+            if (staged_reps[q].k == rep) {
+                staged_reps.erase(staged_reps.begin() + (long)q);
+                break;
+            }
+        a_beads.release(r.begin, r.n);
+        a_nat.release(r.nat_off, r.nat_len);
+        a_ss.release(r.ss_off, r.ss_len);
+        a_cells.release(r.cell_off, r.cell_len);
+        a_chunks.release(r.chunk_off, r.chunk_len);
+        a_afm.release(r.afm_off, r.afm_len);
     }
     r = RepHost{};
     r.in_use = false;
+}
+
+void Engine::stage(int rep) {
+    check_rep(reps, rep);
+    if (!dynamic) throw std::logic_error("stage needs a context with reserved capacity");
+    ready_alloc();
+    RepHost &r = reps[rep];
+    if (r.placed || r.staged) return;
+    if (!r.have_state) throw std::logic_error("set_state must precede placement");
+    use_device();
+    Staged st;
+    place(rep, &st);
+    staged_reps.push_back(std::move(st));
+}
+
+void Engine::activate_staged() {
+    if (staged_reps.empty()) return;
+    use_device();
+    CK(cudaEventRecord(ev_staged, ustream));
+    CK(cudaStreamWaitEvent(stream, ev_staged, 0));
+    for (Staged &st : staged_reps) {
+        RepHost &r = reps[st.k];
+        CK(cudaMemcpyAsync(d.rep_of + r.begin, st.rep_of.data(), sizeof(int32_t) * r.n, cudaMemcpyHostToDevice,
+                           stream));
+        if (!st.cell_rep.empty())
+            CK(cudaMemcpyAsync(d.cell_rep + r.cell_off, st.cell_rep.data(), sizeof(int32_t) * st.cell_rep.size(),
+                               cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(d.rep + st.k, &st.rd, sizeof(RepDev), cudaMemcpyHostToDevice, stream));
+        for (int i = 0; i < r.n; ++i) owner_h[r.begin + i] = st.k;
+        update_blocks(r.begin, r.begin + r.n, false);
+        r.staged = false;
+        r.placed = true;
+    }
+    staged_reps.clear();
+}
+
+void Engine::step_async(int nsteps) {
+    use_device();
+    ready();
+    if (!params.langevin_on) throw std::invalid_argument("langevin: enabled is false; nothing integrates");
+    ensure_nl();
+    int s = 0;
+    if (!timing && use_graphs) {
+        const int gsteps = tune.graph_steps;
+        for (; s + gsteps <= nsteps; s += gsteps) {
+            CK(cudaGraphLaunch(graph_for(cur), stream));
+            // per step: the step kernel (plus the separate check and the
+            // quasi-adiabatic kernels with that term); rebuild kernels are
+            // counted per pass in stats()
+            launches += (d.qa_on ? 7 : 1) * gsteps;
+            md_steps += gsteps;
+        }
+    }
+    for (; s < nsteps; ++s) {
+        launch_force_step();
+        cur ^= 1;
+        k_nl_check<<<1, 1024, 0, stream>>>(d, 1, params.dt, (cudaGraphConditionalHandle)0, 0);
+        ++launches;
+        ++md_steps;
+        CK(cudaMemcpyAsync(h_any, d.any_rebuild, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        if (*h_any) launch_rebuild();
+    }
+}
+
+void Engine::step_wait() {
+    use_device();
+    check_status("step");
+    if (auto_grow) grow_rows(0.6);
 }
 
 void Engine::set_steps(int rep, long long nsteps) {
@@ -2683,7 +2775,7 @@ void Engine::ready_alloc() {
 
 void Engine::place_pending() {
     for (int k = 0; k < (int)reps.size(); ++k)
-        if (reps[k].in_use && !reps[k].placed) {
+        if (reps[k].in_use && !reps[k].placed && !reps[k].staged) {
             if (!reps[k].have_state) throw std::logic_error("set_state must be called for every replica");
             place(k);
         }
@@ -2691,7 +2783,7 @@ void Engine::place_pending() {
 
 // occupancy granules [b0/BLK_ON, (b1-1)/BLK_ON] on when any bead slot in them
 // is placed (a force block runs when any of its granules is on)
-void Engine::update_blocks(int b0, int b1) {
+void Engine::update_blocks(int b0, int b1, bool wait) {
     if (b1 <= b0) return;
     const int k0 = b0 / BLK_ON, k1 = (b1 - 1) / BLK_ON;
     std::vector<uint8_t> on(k1 - k0 + 1, 0);
@@ -2699,12 +2791,17 @@ void Engine::update_blocks(int b0, int b1) {
         for (int i = k * BLK_ON; i < std::min(cap.beads, (k + 1) * BLK_ON); ++i)
             if (owner_h[i] >= 0) { on[k - k0] = 1; break; }
     CK(cudaMemcpyAsync(d.blk_on + k0, on.data(), on.size(), cudaMemcpyHostToDevice, stream));
-    CK(cudaStreamSynchronize(stream));
+    if (wait) CK(cudaStreamSynchronize(stream));
 }
 
-// static data, lists and state of replica slot k onto the device
-void Engine::place(int k) {
+// static data, lists and state of replica slot k onto the device.  With st
+// (staged placement) every upload goes on the side stream, after the last
+// removal's clears, and the activation data (bead and bucket owners, the
+// replica record) is kept in st for activate_staged().
+void Engine::place(int k, Staged *st) {
     const xmd_params &p = params;
+    cudaStream_t us = st ? ustream : stream;
+    if (st) CK(cudaStreamWaitEvent(ustream, ev_removed, 0));
     RepHost &r = reps[k];
     const int n = r.n;
     const bool tile = p.nl_build == XMD_NL_BUILD_TILE || (p.nl_build == XMD_NL_BUILD_AUTO && n <= TILE_MAX);
@@ -2778,10 +2875,13 @@ void Engine::place(int k) {
         for (auto &e : nat[i]) { nj.push_back(e.first); nd.push_back(e.second); }
         ne[i] = no + (int)nj.size();
     }
+    // (pageable sources: each copy returns once the driver has taken the
+    // data, so the host vectors may go out of scope)
     auto up = [&](void *dst, const void *src, size_t bytes_) {
-        if (bytes_) CK(cudaMemcpyAsync(dst, src, bytes_, cudaMemcpyHostToDevice, stream));
+        if (bytes_) CK(cudaMemcpyAsync(dst, src, bytes_, cudaMemcpyHostToDevice, us));
     };
-    up(d.rep_of + b, rep_of.data(), sizeof(int32_t) * n);
+    if (st) st->rep_of = rep_of;
+    else up(d.rep_of + b, rep_of.data(), sizeof(int32_t) * n);
     up(d.chain + b, chain.data(), sizeof(int32_t) * n);
     up(d.seq + b, seq.data(), sizeof(int32_t) * n);
     up(d.atype + b, r.atype.data(), n);
@@ -2815,7 +2915,7 @@ void Engine::place(int k) {
         up(d.ss_start + b, sst.data(), sizeof(int32_t) * n);
         up(d.ss_end + b, sse.data(), sizeof(int32_t) * n);
         up(d.ss_j + so, sj.data(), sizeof(int32_t) * sj.size());
-        if (nss) CK(cudaMemsetAsync(d.ss_on + so, 0, nss, stream));
+        if (nss) CK(cudaMemsetAsync(d.ss_on + so, 0, nss, us));
     }
     std::vector<float4> bf(n);
     for (int i = 0; i < n; ++i) bf[i] = make_float4((float)tr[i], (float)ar[i], (float)dr[i], 0.0f);
@@ -2826,11 +2926,12 @@ void Engine::place(int k) {
     up(d.nat_d + no, nd.data(), sizeof(double) * nd.size());
     std::vector<float> ndf(nd.begin(), nd.end());
     up(d.nat_df + no, ndf.data(), sizeof(float) * ndf.size());
-    CK(cudaMemsetAsync(d.nat_on + no, 0, nnat, stream));
-    CK(cudaMemsetAsync(d.nl_cnt + b, 0, sizeof(int32_t) * n, stream));
+    CK(cudaMemsetAsync(d.nat_on + no, 0, nnat, us));
+    CK(cudaMemsetAsync(d.nl_cnt + b, 0, sizeof(int32_t) * n, us));
     if (ncell) {
         std::vector<int32_t> cr(ncell, k);
-        up(d.cell_rep + co, cr.data(), sizeof(int32_t) * ncell);
+        if (st) st->cell_rep = cr;
+        else up(d.cell_rep + co, cr.data(), sizeof(int32_t) * ncell);
     }
     std::vector<int2> ch(nchunk);
     for (int c = 0; c < nchunk; ++c) ch[c] = make_int2(k, b + c * TL_CH);
@@ -2900,9 +3001,9 @@ void Engine::place(int k) {
             sy[i] = (lim[0] & 0xff) | ((lim[1] & 0xff) << 8) | ((lim[2] & 0xff) << 16) | ((lim[3] & 0xff) << 24);
         }
         up(d.qa.sync + b, sy.data(), sizeof(int32_t) * n);
-        CK(cudaMemsetAsync(d.qa.ref_cnt + b, 0, sizeof(int32_t) * n, stream));
+        CK(cudaMemsetAsync(d.qa.ref_cnt + b, 0, sizeof(int32_t) * n, us));
     }
-    up(d.rep + k, &rd, sizeof(RepDev));
+    if (!st) up(d.rep + k, &rd, sizeof(RepDev));
     GF2 j = gf2_jump(4ull * (uint64_t)n);
     std::vector<uint64_t> jt(JUMP_WORDS);
     // nibble tables: entry [q][v] = XOR of the columns 4q+b for the bits b of v
@@ -2914,6 +3015,19 @@ void Engine::place(int k) {
             jt[16 * q + v] = e;
         }
     up(d.jump + (size_t)JUMP_WORDS * k, jt.data(), sizeof(uint64_t) * JUMP_WORDS);
+    if (st) {
+        // the state (upload_state's data) on the side stream too; the record
+        // starts as upload_state leaves it: t = 0, first list build pending
+        upload_state_data(k, us);
+        rd.t = 0.0;
+        rd.first = 1;
+        rd.maxdisp = 0;
+        rd.fault = 0;
+        st->k = k;
+        st->rd = rd;
+        r.staged = true;
+        return;
+    }
     CK(cudaStreamSynchronize(stream));
     for (int i = 0; i < n; ++i) owner_h[b + i] = k;
     update_blocks(b, b + n);
@@ -2921,7 +3035,9 @@ void Engine::place(int k) {
     upload_state(k);
 }
 
-void Engine::upload_state(int k) {
+// positions, history (y1 = v dt, y2..y5 = 0) and generator states of a
+// replica, uploaded on stream us
+void Engine::upload_state_data(int k, cudaStream_t us) {
     RepHost &r = reps[k];
     int n = r.n, b = r.begin;
     std::vector<double4_32a> pos(n);
@@ -2929,13 +3045,12 @@ void Engine::upload_state(int k) {
         double q = params.charge[r.atype[i]];
         pos[i] = make_double4_32a(r.r[3 * i], r.r[3 * i + 1], r.r[3 * i + 2], q);
     }
-    CK(cudaMemcpyAsync(d.pos[cur] + b, pos.data(), sizeof(double4_32a) * n, cudaMemcpyHostToDevice, stream));
-    // y1 = v*dt, y2..y5 = 0
+    CK(cudaMemcpyAsync(d.pos[cur] + b, pos.data(), sizeof(double4_32a) * n, cudaMemcpyHostToDevice, us));
     std::vector<double> col(n);
     for (int k2 = 0; k2 < 15; ++k2) {
         for (int i = 0; i < n; ++i) col[i] = k2 < 3 ? r.v[3 * i + k2] * params.dt : 0.0;
         CK(cudaMemcpyAsync(d.yh + (size_t)k2 * d.N + b, col.data(), sizeof(double) * n,
-                           cudaMemcpyHostToDevice, stream));
+                           cudaMemcpyHostToDevice, us));
     }
     std::vector<uint64_t> st(n);
     uint64_t s = r.seed;
@@ -2943,7 +3058,11 @@ void Engine::upload_state(int k) {
         st[i] = s;
         for (int q = 0; q < 4; ++q) s = xs_step(s);
     }
-    CK(cudaMemcpyAsync(d.rng + b, st.data(), sizeof(uint64_t) * n, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d.rng + b, st.data(), sizeof(uint64_t) * n, cudaMemcpyHostToDevice, us));
+}
+
+void Engine::upload_state(int k) {
+    upload_state_data(k, stream);
     RepDev rd;
     CK(cudaMemcpyAsync(&rd, d.rep + k, sizeof(RepDev), cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
@@ -3659,36 +3778,10 @@ void Engine::eval_forces(int rep, double *F, double *V) {
 }
 
 void Engine::step(int nsteps) {
-    use_device();
-    ready();
-    if (!params.langevin_on) throw std::invalid_argument("langevin: enabled is false; nothing integrates");
-    ensure_nl();
-    int s = 0;
-    if (!timing && use_graphs) {
-        const int gsteps = tune.graph_steps;
-        for (; s + gsteps <= nsteps; s += gsteps) {
-            CK(cudaGraphLaunch(graph_for(cur), stream));
-            // per step: the step kernel (plus the separate check and the
-            // quasi-adiabatic kernels with that term); rebuild kernels are
-            // counted per pass in stats()
-            launches += (d.qa_on ? 7 : 1) * gsteps;
-            md_steps += gsteps;
-        }
-    }
-    for (; s < nsteps; ++s) {
-        launch_force_step();
-        cur ^= 1;
-        k_nl_check<<<1, 1024, 0, stream>>>(d, 1, params.dt, (cudaGraphConditionalHandle)0, 0);
-        ++launches;
-        ++md_steps;
-        CK(cudaMemcpyAsync(h_any, d.any_rebuild, sizeof(int), cudaMemcpyDeviceToHost, stream));
-        CK(cudaStreamSynchronize(stream));
-        if (*h_any) launch_rebuild();
-    }
-    check_status("step");
+    step_async(nsteps);
     // rows keep their contents when they grow: no list needs rebuilding, so
     // no replica's trajectory depends on another's row lengths
-    if (auto_grow) grow_rows(0.6);
+    step_wait();
 }
 
 // ---- packed host-buffer path ----------------------------------------------------

@@ -205,6 +205,7 @@ struct RepHost {
     int chunk_off = 0, chunk_len = 0;   // tile-build chunks
     int fp_off = 0, fp_len = 0, ct_off = 0, ct_len = 0;   // quasi-adiabatic slots
     long long steps_left = -1;
+    bool staged = false;     // device data uploading on the side stream, not yet active
 };
 
 // first-fit allocator of index ranges [0, n)
@@ -270,6 +271,16 @@ public:
     void set_steps(int rep, long long nsteps);
     void steps_left(long long *out);   // per replica slot, -2 for a free slot
     void place_now(int rep);           // place a replica now (XMD_ERR_CAPACITY: no room yet)
+    // Overlapped placement (dynamic contexts): stage() allocates the
+    // replica's device ranges and uploads its data on a side stream while
+    // earlier work runs; activate_staged() then makes every staged replica
+    // live on the step stream, ordered after those uploads.  A staged replica
+    // takes no step before it is activated.
+    void stage(int rep);               // XMD_ERR_CAPACITY (length_error): no room yet
+    void activate_staged();
+    // step() in two halves: launch the steps, then wait for them and report
+    void step_async(int nsteps);
+    void step_wait();
     int capacity_replicas() const { return cap.reps; }
     // device memory this context holds (its allocations, rows at their current capacity)
     size_t device_bytes() const { return alloc_bytes; }
@@ -383,11 +394,21 @@ private:
     int qa_bchunk_next = 0;   // next free chunk of the QA re-listing (static contexts)
     std::vector<int32_t> owner_h;              // bead slot -> replica (or -1)
     void allocate();
-    void place(int k);
+    // the staged replicas' activation data: bead -> replica, bucket ->
+    // replica and the replica record, written on the step stream
+    struct Staged {
+        int k = 0;
+        std::vector<int32_t> rep_of, cell_rep;
+        RepDev rd{};
+    };
+    std::vector<Staged> staged_reps;
+    cudaStream_t ustream = nullptr;            // side stream of staged uploads
+    cudaEvent_t ev_staged = nullptr, ev_removed = nullptr;
+    void place(int k, Staged *st = nullptr);
     void place_pending();
     void ready();                              // allocated, every replica placed
     void ready_alloc();
-    void update_blocks(int b0, int b1);
+    void update_blocks(int b0, int b1, bool wait = true);
     void *dalloc(size_t bytes);
     void finalize();
     void release();
@@ -396,6 +417,7 @@ private:
     void launch_rebuild();
     void check_status(const char *where);
     void upload_state(int rep);
+    void upload_state_data(int rep, cudaStream_t us);
 };
 
 std::string &last_error();

@@ -168,7 +168,8 @@ bool Server::admit(Request *q) {
         e.set_native(slot, (int)q->n1.size(), q->n1.data(), q->n2.data(), q->nd.data());
         e.set_state(slot, q->r.data(), q->v.empty() ? nullptr : q->v.data());
         e.set_steps(slot, q->nsteps);
-        e.place_now(slot);
+        // device ranges and uploads on the side stream; live at activation
+        e.stage(slot);
     } catch (std::length_error &) {
         e.remove_replica(slot);
         return false;   // no contiguous room in the reserved capacity yet
@@ -208,14 +209,21 @@ void Server::fail(Request *q, const char *why) {
 }
 
 void Server::loop() {
+    // One chunk of steps is in flight while the worker admits the queued
+    // requests that fit: their host-side preparation and uploads (side
+    // stream, into free device ranges) overlap the chunk.  After the chunk,
+    // finished requests are retired, the staged ones are activated on the
+    // step stream (ordered after their uploads) and the next chunk starts.
+    std::vector<Request *> staged;
     try {
         eng->use_device();
         std::vector<long long> left;
+        bool inflight = false;
         for (;;) {
             {
                 std::unique_lock<std::mutex> lk(mu);
-                cv.wait(lk, [&] { return stop || !queue.empty() || !running.empty(); });
-                if (stop) break;
+                if (!inflight) cv.wait(lk, [&] { return stop || !queue.empty() || !running.empty(); });
+                if (stop && !inflight) break;
             }
             // admission, first come first served
             const double ta = now_s();
@@ -223,7 +231,7 @@ void Server::loop() {
                 Request *q;
                 {
                     std::lock_guard<std::mutex> lk(mu);
-                    if (queue.empty()) break;
+                    if (queue.empty() || stop) break;
                     q = queue.front();
                 }
                 if (!admit(q)) break;
@@ -233,48 +241,57 @@ void Server::loop() {
                     cv_done.notify_all();
                     continue;
                 }
-                q->state = XMD_REQ_RUNNING;
-                q->t_start = now_s();
-                running.push_back(q);
-                peak_running = std::max(peak_running, (int)running.size());
+                staged.push_back(q);
             }
-            if (running.empty()) {
-                // the head of the queue does not fit an empty context: it never will
+            const double ts = now_s();
+            if (inflight) {
+                eng->step_wait();
+                inflight = false;
+            }
+            const double te = now_s();
+            // retirement (the staged requests have not stepped yet)
+            if (!running.empty()) {
+                left.assign(eng->capacity_replicas(), -2);
+                eng->steps_left(left.data());
+                std::vector<Request *> keep;
+                for (Request *q : running) {
+                    if (left[q->slot] == -3) fail(q, "non-finite force: the trajectory diverged");
+                    else if (left[q->slot] == 0) retire(q);
+                    else keep.push_back(q);
+                }
                 std::lock_guard<std::mutex> lk(mu);
-                if (!queue.empty()) {
+                running.swap(keep);
+            }
+            eng->activate_staged();
+            {
+                std::lock_guard<std::mutex> lk(mu);
+                const double tn = now_s();
+                for (Request *q : staged) {
+                    q->state = XMD_REQ_RUNNING;
+                    q->t_start = tn;
+                    running.push_back(q);
+                }
+                staged.clear();
+                peak_running = std::max(peak_running, (int)running.size());
+                if (running.empty() && !queue.empty() && !stop) {
+                    // the head of the queue does not fit an empty context: it never will
                     Request *q = queue.front();
                     queue.pop_front();
                     q->state = XMD_REQ_FAILED;
                     q->error = "the request does not fit the reserved capacity";
-                    cv_done.notify_all();
                 }
-                continue;
-            }
-            bool pending_zero = false;
-            for (Request *q : running) pending_zero |= q->nsteps == 0;
-            const double ts = now_s();
-            if (!pending_zero) {
-                eng->step(chunk);
-                ++chunks;
-            }
-            const double te = now_s();
-            left.assign(eng->capacity_replicas(), -2);
-            eng->steps_left(left.data());
-            std::vector<Request *> keep;
-            for (Request *q : running) {
-                if (left[q->slot] == -3) fail(q, "non-finite force: the trajectory diverged");
-                else if (left[q->slot] == 0) retire(q);
-                else keep.push_back(q);
-            }
-            {
-                std::lock_guard<std::mutex> lk(mu);
-                running.swap(keep);
-                // host time between chunks (admission, retirement) and in them
+                // host time outside the chunks' device work: admission and
+                // the part of retirement and activation after the wait
                 admit_s += (ts - ta) + (now_s() - te);
                 step_s += te - ts;
                 dev_bytes = (int64_t)eng->device_bytes();
             }
             cv_done.notify_all();
+            if (!running.empty() && !stop) {
+                eng->step_async(chunk);
+                inflight = true;
+                ++chunks;
+            }
         }
     } catch (std::exception &ex) {
         std::lock_guard<std::mutex> lk(mu);
@@ -287,6 +304,11 @@ void Server::loop() {
             q->state = XMD_REQ_FAILED;
             q->error = fatal;
         }
+        for (Request *q : staged) {
+            q->state = XMD_REQ_FAILED;
+            q->error = fatal;
+        }
+        staged.clear();
         running.clear();
         queue.clear();
         cv_done.notify_all();

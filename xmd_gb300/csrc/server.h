@@ -2,12 +2,15 @@
 //
 // Requests (independent systems of one or more chains, each with its own
 // temperature, seed and step count) are queued by any host thread.  A worker
-// thread owns the engine: between step chunks it admits queued requests into
-// free replica slots while the reserved device capacity (sized from the HBM
-// budget) has room, advances every admitted request together in one batched
-// launch sequence, and retires requests whose step budget is spent: their
-// final state is copied out and their slots and device ranges are reused.
-// A request's trajectory does not depend on what else is in the batch.
+// thread owns the engine.  While a chunk of steps runs on the device it
+// admits queued requests into free replica slots while the reserved device
+// capacity (sized from the HBM budget) has room: their host-side preparation
+// and uploads (a side stream, into free device ranges) overlap the chunk.
+// When the chunk ends it retires requests whose step budget is spent (their
+// final state is copied out and their slots and device ranges are reused),
+// activates the staged requests on the step stream and launches the next
+// chunk for every running request together.  A request's trajectory does not
+// depend on what else is in the batch.
 #pragma once
 #include <condition_variable>
 #include <cstdint>
