@@ -174,3 +174,21 @@ def test_frozen_replica_does_not_fail_the_others_evaluation():
         assert np.isfinite(e.observables(g)["E"])
         with pytest.raises(abi.XmdError):
             e.eval_forces(b)
+
+
+def test_server_queues_until_capacity_frees():
+    """Requests that do not fit beside the running ones wait in the queue and
+    are admitted when capacity frees (admission overlaps the running chunk);
+    each still finishes with the state it reaches alone."""
+    ss = [synth.make_system([300], 700 + k, box=None, types="charged10", temperature=0.35, rng_seed=710 + k)
+          for k in range(4)]
+    steps = [64, 96, 32, 128]
+    with Server(YAML, hbm_budget=64 << 20, max_beads=650, chunk_steps=32) as srv:
+        ids = [srv.submit(s, steps[k]) for k, s in enumerate(ss)]
+        res = [srv.result(i) for i in ids]
+        st = srv.stats()
+    assert st["completed"] == 4 and st["failed"] == 0
+    assert st["peak_running"] <= 2
+    for k, s in enumerate(ss):
+        r, v, t = alone(s, steps[k])
+        assert np.array_equal(res[k][0], r), k

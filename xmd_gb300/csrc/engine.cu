@@ -1067,8 +1067,12 @@ __global__ void k_nl_check(Dev d, int advance, double dt, cudaGraphConditionalHa
 // term) the last block to finish also takes the skin decision of every
 // replica and sets the graph's rebuild condition, so a step is one launch
 // plus the conditional rebuild.
-// one thread per bead: at least 16 warps per SM (at most 128 registers)
-template <int FB, int LPB> constexpr int force_min_blocks() { return LPB == 1 ? 512 / FB : (LPB == 4 ? (768 / (FB * 4) > 0 ? 768 / (FB * 4) : 1) : 1); }
+// resident blocks the register allocation leaves room for: 16 warps per SM
+// (at most 128 registers) with one or two threads per bead, 24 (at most 85)
+// with four
+template <int FB, int LPB> constexpr int force_min_blocks() {
+    return LPB == 4 ? (768 / (FB * 4) > 0 ? 768 / (FB * 4) : 1) : 512 / (FB * LPB);
+}
 template <class FT, int MODE, int FB, int LPB>
 __global__ void __launch_bounds__(FB * LPB, (force_min_blocks<FB, LPB>())) k_force(Dev d, TermP p, int cur,
                                                                                   cudaGraphConditionalHandle h,

@@ -225,7 +225,9 @@ void Server::loop() {
                 if (!inflight) cv.wait(lk, [&] { return stop || !queue.empty() || !running.empty(); });
                 if (stop && !inflight) break;
             }
-            // admission, first come first served
+            // admission, first come first served (tried against an idle
+            // context when nothing runs, is staged or is in flight)
+            const bool idle = !inflight && running.empty() && staged.empty();
             const double ta = now_s();
             for (;;) {
                 Request *q;
@@ -273,7 +275,7 @@ void Server::loop() {
                 }
                 staged.clear();
                 peak_running = std::max(peak_running, (int)running.size());
-                if (running.empty() && !queue.empty() && !stop) {
+                if (idle && running.empty() && !queue.empty() && !stop) {
                     // the head of the queue does not fit an empty context: it never will
                     Request *q = queue.front();
                     queue.pop_front();
