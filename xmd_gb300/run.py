@@ -44,6 +44,8 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=None)
     ap.add_argument("--timing", action="store_true", help="CUDA events around every force/rebuild launch")
     ap.add_argument("--device", type=int, default=0)
+    ap.add_argument("--shape", default=None,
+                    help="launch shape fb,tile_per_sm,graph_steps,threads_per_bead (default: the engine's)")
     args = ap.parse_args(argv)
 
     y = synth.yaml_for(args.workload, args.precision) + f"  device: {args.device}\n"
@@ -57,6 +59,8 @@ def main(argv=None):
     with Engine(y) as e:
         for s in systems:
             e.add_system(s)
+        if args.shape:
+            e.set_tuning(*(int(x) for x in args.shape.split(",")))
         e.step(args.warmup)
         e.synchronize()
         if args.timing:
