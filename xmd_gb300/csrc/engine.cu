@@ -843,10 +843,12 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
             if (MODE == 0 && i == i1) vqa += sat * (double)V_;
         }
         if (MODE == 1 && ln == LPB - 1) {
-            // n and h at this step's positions (precompute_nh.cpp:12-20)
-            D3 n{0, 0, 0}, h{0, 0, 0};
+            // n and h at this step's positions (precompute_nh.cpp:12-20) to
+            // FP32 accuracy, for the sift's FP32 decisions (which recompute
+            // them in FP64 near a threshold)
+            V3<float> n{0.0f, 0.0f, 0.0f}, h{0.0f, 0.0f, 0.0f};
             const uint32_t fl = d.bflags[i];
-            if ((fl & BF_PREV) && (fl & BF_NEXT)) qa_nh(P[bs + 2], P[bs + 3], P[bs + 4], &n, &h);
+            if ((fl & BF_PREV) && (fl & BF_NEXT)) qa_nh_f(P[bs + 2], P[bs + 3], P[bs + 4], &n, &h);
             q.nh[i] = n.x; q.nh[Ns + i] = n.y; q.nh[2 * Ns + i] = n.z;
             q.nh[3 * Ns + i] = h.x; q.nh[4 * Ns + i] = h.y; q.nh[5 * Ns + i] = h.z;
         }
@@ -2689,7 +2691,7 @@ void Engine::allocate() {
         // quasi-adiabatic state (tables of main.cpp:681-700, lj_variants.cpp:59-62)
         d.qa_on = 1;
         QaDev &q = d.qa;
-        q.nh = (double *)dalloc(sizeof(double) * 6 * (size_t)N);
+        q.nh = (float *)dalloc(sizeof(float) * 6 * (size_t)N);
         q.sync = (int32_t *)dalloc(sizeof(int32_t) * N);
         q.ref_cnt = (int32_t *)dalloc(sizeof(int32_t) * N);
         q.ref = (int32_t *)dalloc(sizeof(int32_t) * QA_REF_CAP * (size_t)N);

@@ -90,7 +90,7 @@ constexpr int QA_BCHUNK = 1024;      // beads per chunk of the free-pair re-list
 
 // device record of the quasi-adiabatic state
 struct QaDev {
-    double *nh;                  // [6][N]: n then h (precompute_nh.cpp:12-20)
+    float *nh;                   // [6][N]: n then h (precompute_nh.cpp:12-20) to FP32 accuracy
     int32_t *sync;               // [N] packed int8 x4: back | side_all | side_polar | side_hydrophobic
     int32_t *ref_cnt, *ref;      // [N], [QA_REF_CAP][N] contact slots per bead
     int32_t *tmp_cnt, *tmp;      // [N], [QA_TMP_CAP][N] partners collected at a rebuild

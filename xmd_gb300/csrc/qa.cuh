@@ -66,6 +66,23 @@ __device__ __forceinline__ void qa_nh(double4_32a rp, double4_32a rc, double4_32
     *n = d3unit(d3sub(v2, v1));
     *h = d3unit(d3cross(v2, v1));
 }
+// the same to FP32 accuracy: bond vectors, their difference and their cross
+// product in float-float from split positions (within ~2^-44 of the exact
+// values however straight the chain), normalised in FP32; each component
+// is within ~3e-7 of the FP64 unit vector's
+__device__ __forceinline__ V3<float> unit_f(V3<float> a) {
+    const float s = 1.0f / sqrtf(a.x * a.x + a.y * a.y + a.z * a.z);
+    return V3<float>{a.x * s, a.y * s, a.z * s};
+}
+__device__ __forceinline__ void qa_nh_f(double4_32a rp, double4_32a rc, double4_32a rn, V3<float> *n, V3<float> *h) {
+    const P2 sp = split_p(rp), sc = split_p(rc), sn = split_p(rn);
+    const V3<FF> v1{ff_diff(sp.x, sc.x), ff_diff(sp.y, sc.y), ff_diff(sp.z, sc.z)};
+    const V3<FF> v2{ff_diff(sc.x, sn.x), ff_diff(sc.y, sn.y), ff_diff(sc.z, sn.z)};
+    const V3<FF> dv{ff_sub(v2.x, v1.x), ff_sub(v2.y, v1.y), ff_sub(v2.z, v1.z)};
+    const V3<FF> x = ff_cross(v2, v1);
+    *n = unit_f(V3<float>{dv.x.h, dv.y.h, dv.z.h});
+    *h = unit_f(V3<float>{x.x.h, x.y.h, x.z.h});
+}
 
 // ---- block-wide helpers (blockDim.x == 1024) ------------------------------------
 // Exclusive prefix of an int over the block; returns the total.
@@ -102,9 +119,9 @@ __device__ __forceinline__ int block_exscan(int v, int *out, int *s_warp) {
 //
 // The decisions are taken in FP32 where they are certain: the pair vector
 // from split positions (float-float differences, error <= 2^-24 of each
-// component), unit vectors and the FP64 n, h narrowed on the integer pipe;
-// every dot product of unit vectors is then within 2e-6 of its FP64 value and
-// the squared distance within 1e-6 of it (relative).  A pair whose value lies
+// component), its unit vector, and n, h to FP32 accuracy (qa_nh_f, written by
+// the step kernel); every dot product of unit vectors is then within 2e-6 of
+// its FP64 value and the squared distance within 1e-6 of it (relative).  A pair whose value lies
 // within QA_BAND of any threshold it is tested against is decided again from
 // scratch in FP64 with explicit rounding (the reference's operations), so the
 // candidate set is exactly the FP64 one.
@@ -120,10 +137,11 @@ __device__ __noinline__ int qa_sift_fp64(const Dev &d, const RepDev &rp, int i1,
     if (!(d3dot(r12, r12) <= q.req_out2)) return 0;
     const double r12_rn = __ddiv_rn(1.0, __dsqrt_rn(d3dot(r12, r12)));
     const D3 u = d3scl(r12_rn, r12);
-    const size_t N = d.N;
-    const D3 n1{q.nh[i1], q.nh[N + i1], q.nh[2 * N + i1]}, n2{q.nh[i2], q.nh[N + i2], q.nh[2 * N + i2]};
-    const D3 h1{q.nh[3 * N + i1], q.nh[4 * N + i1], q.nh[5 * N + i1]};
-    const D3 h2{q.nh[3 * N + i2], q.nh[4 * N + i2], q.nh[5 * N + i2]};
+    // n and h of both beads in FP64, as precompute_nh computes them
+    D3 n1{0.0, 0.0, 0.0}, h1 = n1, n2 = n1, h2 = n1;
+    const uint32_t both = BF_PREV | BF_NEXT;
+    if ((d.bflags[i1] & both) == both) qa_nh(pos[i1 - 1], pos[i1], pos[i1 + 1], &n1, &h1);
+    if ((d.bflags[i2] & both) == both) qa_nh(pos[i2 - 1], pos[i2], pos[i2 + 1], &n2, &h2);
     const bool back1 = fabs(d3dot(h1, u)) > q.min_cos_hr;
     const bool back2 = fabs(d3dot(h2, u)) > q.min_cos_hr;
     const bool bb_extra = fabs(d3dot(h1, h2)) > q.min_cos_hh;
@@ -141,8 +159,7 @@ __device__ __noinline__ int qa_sift_fp64(const Dev &d, const RepDev &rp, int i1,
 }
 
 __device__ __forceinline__ V3<float> nh_f(const QaDev &q, size_t N, int i, int off) {
-    return V3<float>{narrow_f(q.nh[(off + 0) * N + i]), narrow_f(q.nh[(off + 1) * N + i]),
-                     narrow_f(q.nh[(off + 2) * N + i])};
+    return V3<float>{q.nh[(off + 0) * N + i], q.nh[(off + 1) * N + i], q.nh[(off + 2) * N + i]};
 }
 // x > T (or, with less, x < T) decided in FP32; *unsure when x is within
 // the band of T
