@@ -227,7 +227,8 @@ __global__ void __launch_bounds__(QA_SIFT) k_qa_sift(Dev d, TermP p, int cur) {
             if (!sync_ok_after(q.sync[i1], d1p) || !sync_ok_after(q.sync[i2], d2p)) type = 0;
         }
     }
-    if (live) {
+    // only listed candidates are read (k_qa_step)
+    if (type != 0) {
         q.cand_type[slot] = type;
         q.cand_d1[slot] = d1p;
         q.cand_d2[slot] = d2p;
@@ -285,22 +286,33 @@ __global__ void __launch_bounds__(1024) k_qa_step(Dev d, TermP p, int cur) {
     //    ordered candidate lists (slots outside this replica's live range are
     //    skipped: blocks at the edges are shared)
     __shared__ int s_i1[1024], s_i2[1024], s_d1[1024], s_d2[1024], s_ty[1024];
+    // each thread takes a contiguous run of the replica's sift blocks, so
+    // one block-wide scan orders every candidate
     const int sb0 = fp_off / QA_SIFT, sb1 = (fp_off + fp_n0 + QA_SIFT - 1) / QA_SIFT;
-    for (int bb = sb0; bb < sb1; bb += 1024) {
-        const int blk = bb + t;
-        const int cnt = blk < sb1 ? q.cand_blk[blk] : 0;
+    {
+        const int per = (sb1 - sb0 + 1023) / 1024;
+        const int b0 = min(sb0 + t * per, sb1), b1 = min(b0 + per, sb1);
+        int cnt = 0;
+        for (int blk = b0; blk < b1; ++blk) cnt += q.cand_blk[blk];
         int pos;
         const int total = block_exscan(cnt, &pos, s_warp);
         for (int g0 = 0; g0 < total; g0 += 1024) {
             // gather candidates [g0, g0 + 1024) of this round with their data
-            for (int k = max(0, g0 - pos); k < cnt && pos + k < g0 + 1024; ++k) {
-                const int s = q.cand_list[(size_t)blk * QA_SIFT + k];
-                const int o = pos + k - g0;
-                const bool mine = s >= fp_off && s < fp_off + fp_n0;
-                s_slots[o] = mine ? s : -1;
-                if (mine) {
-                    s_i1[o] = q.fp_i1[s]; s_i2[o] = q.fp_i2[s];
-                    s_d1[o] = q.cand_d1[s]; s_d2[o] = q.cand_d2[s]; s_ty[o] = q.cand_type[s];
+            if (cnt && pos < g0 + 1024 && pos + cnt > g0) {
+                int o = pos;
+                for (int blk = b0; blk < b1 && o < g0 + 1024; ++blk) {
+                    const int c = q.cand_blk[blk];
+                    for (int k = 0; k < c && o < g0 + 1024; ++k, ++o) {
+                        if (o < g0) continue;
+                        const int s = q.cand_list[(size_t)blk * QA_SIFT + k];
+                        const int so = o - g0;
+                        const bool mine = s >= fp_off && s < fp_off + fp_n0;
+                        s_slots[so] = mine ? s : -1;
+                        if (mine) {
+                            s_i1[so] = q.fp_i1[s]; s_i2[so] = q.fp_i2[s];
+                            s_d1[so] = q.cand_d1[s]; s_d2[so] = q.cand_d2[s]; s_ty[so] = q.cand_type[s];
+                        }
+                    }
                 }
             }
             __syncthreads();
@@ -420,33 +432,33 @@ __global__ void __launch_bounds__(1024) k_qa_refree(Dev d) {
     if (rp.qa_removed == 0) return;
     const QaDev &q = d.qa;
     __shared__ int s_warp[33];
-    __shared__ int s_fp_n, s_err;
-    if (t == 0) { s_fp_n = rp.fp_n; s_err = 0; }
-    __syncthreads();
-    const int fp_off = rp.fp_off, ct_off = rp.ct_off, ct_n = rp.ct_n;
-    for (int base = 0; base < ct_n; base += 1024) {
-        const int slot = ct_off + base + t;
-        const int removed = base + t < ct_n ? q.ct_rm[slot] : 0;
-        int pos;
-        const int total = block_exscan(removed, &pos, s_warp);
-        if (removed) {
-            const int fs = fp_off + s_fp_n + pos;
-            if (s_fp_n + pos < rp.fp_cap) {
-                q.fp_i1[fs] = q.ct_i1[slot];
-                q.fp_i2[fs] = q.ct_i2[slot];
-                q.fp_vac[fs] = 0;
-            } else {
-                s_err = 1;
-            }
+    __shared__ int s_err;
+    if (t == 0) s_err = 0;
+    const int fp_off = rp.fp_off, ct_off = rp.ct_off, ct_n = rp.ct_n, fp_n0 = rp.fp_n, fp_cap = rp.fp_cap;
+    // each thread takes a contiguous run of contact slots, so one block-wide
+    // scan places every removed pair in slot order
+    const int per = (ct_n + 1023) / 1024;
+    const int k0 = min(t * per, ct_n), k1 = min(k0 + per, ct_n);
+    int cnt = 0;
+    for (int k = k0; k < k1; ++k) cnt += q.ct_rm[ct_off + k];
+    int pos;
+    const int total = block_exscan(cnt, &pos, s_warp);
+    for (int k = k0; k < k1 && cnt; ++k) {
+        const int slot = ct_off + k;
+        if (!q.ct_rm[slot]) continue;
+        const int o = fp_n0 + pos++;
+        if (o < fp_cap) {
+            q.fp_i1[fp_off + o] = q.ct_i1[slot];
+            q.fp_i2[fp_off + o] = q.ct_i2[slot];
+            q.fp_vac[fp_off + o] = 0;
+        } else {
+            s_err = 1;
         }
-        __syncthreads();
-        if (t == 0) s_fp_n = min(s_fp_n + total, rp.fp_cap);
-        __syncthreads();
     }
     __syncthreads();
     if (t == 0) {
         rp.qa_removed = 0;
-        rp.fp_n = s_fp_n;
+        rp.fp_n = min(fp_n0 + total, fp_cap);
         if (s_err) atomicOr(d.status, 4);
     }
 }
