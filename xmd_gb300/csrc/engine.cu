@@ -2161,7 +2161,7 @@ void Engine::step_async(int nsteps) {
             // per step: the step kernel (plus the separate check and the
             // quasi-adiabatic kernels with that term); rebuild kernels are
             // counted per pass in stats()
-            launches += (d.qa_on ? 7 : 1) * gsteps;
+            launches += (d.qa_on ? 6 : 1) * gsteps;
             md_steps += gsteps;
         }
     }
@@ -3537,8 +3537,7 @@ void Engine::launch_force_step() {
         const int gc = (d.qa.ct_total + 255) / 256;
         k_qa_trans<<<gc, 256, 0, stream>>>(d, tp, cur);
         k_qa_refree<<<d.R, 1024, 0, stream>>>(d);
-        k_qa_refs<<<gc, 256, 0, stream>>>(d);
-        launches += 5;
+        launches += 4;
     }
 }
 
@@ -3607,7 +3606,7 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
             kq.gridDim = dim3(d.R);
             kq.blockDim = dim3(1024);
             kq.kernelParams = sargs;
-            cudaKernelNodeParams kt{}, kr{}, kf2{};
+            cudaKernelNodeParams kt{}, kr{};
             void *dargs[] = {&d};
             const unsigned gc = (unsigned)((d.qa.ct_total + 255) / 256);
             kt.func = (void *)k_qa_trans;
@@ -3618,17 +3617,12 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
             kr.gridDim = dim3(d.R);
             kr.blockDim = dim3(1024);
             kr.kernelParams = dargs;
-            kf2.func = (void *)k_qa_refs;
-            kf2.gridDim = dim3(gc);
-            kf2.blockDim = dim3(256);
-            kf2.kernelParams = dargs;
-            cudaGraphNode_t n1, n2, n3, n4, n5;
+            cudaGraphNode_t n1, n2, n3, n4;
             CK(cudaGraphAddKernelNode(&n1, g, &nf, 1, &ks));
             CK(cudaGraphAddKernelNode(&n2, g, &n1, 1, &kq));
             CK(cudaGraphAddKernelNode(&n3, g, &n2, 1, &kt));
             CK(cudaGraphAddKernelNode(&n4, g, &n3, 1, &kr));
-            CK(cudaGraphAddKernelNode(&n5, g, &n4, 1, &kf2));
-            nf = n5;
+            nf = n4;
         }
         if (fuse) {
             nc = nf;

@@ -168,11 +168,11 @@ __device__ __forceinline__ bool cmp_band(float x, float T, bool less, bool *unsu
     return less ? x < T : x > T;
 }
 
-__global__ void __launch_bounds__(QA_SIFT) k_qa_sift(Dev d, TermP p, int cur) {
+__global__ void __launch_bounds__(QA_SIFT, 4) k_qa_sift(Dev d, TermP p, int cur) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     const QaDev &q = d.qa;
     // the per-bead contact references are listed again at this step's end
-    // (k_qa_refs); nothing reads them before that
+    // (k_qa_trans); nothing reads them before that
     for (int k = slot; k < d.N; k += gridDim.x * blockDim.x) q.ref_cnt[k] = 0;
     bool live = slot < q.fp_total;
     const int r = live ? q.fp_rep[slot] : 0;
@@ -389,6 +389,8 @@ __global__ void __launch_bounds__(1024) k_qa_step(Dev d, TermP p, int cur) {
 // One thread per contact slot of the pool: saturation, forming -> breaking,
 // and removal (valence returned, slot vacated, flagged for re-freeing).
 // Contacts accepted at this step have saturation 0 and stay as they are.
+// The contacts that stay are then listed per bead (the references the next
+// step's forces and list builds read; cleared by the sift).
 __global__ void __launch_bounds__(256) k_qa_trans(Dev d, TermP p, int cur) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     const QaDev &q = d.qa;
@@ -400,14 +402,15 @@ __global__ void __launch_bounds__(256) k_qa_trans(Dev d, TermP p, int cur) {
     if (!rp.active || slot - rp.ct_off >= rp.ct_n || q.ct_vac[slot]) return;
     const double tnow = rp.t;
     const int i1 = q.ct_i1[slot], i2 = q.ct_i2[slot];
-    D3 r12 = d3ruv(rp.box, d.pos[cur][i1], d.pos[cur][i2]);
-    double r12_rn = __ddiv_rn(1.0, __dsqrt_rn(d3dot(r12, r12)));
     int status = q.ct_status[slot];
     double sat = __dmul_rn(fmin(__dsub_rn(tnow, q.ct_ref[slot]), p.qa_cycle), p.qa_cycle_inv);
     if (status == QA_BREAKING) sat = __dsub_rn(1.0, sat);
-    double depth, rmin, rmax;
-    qa_lj(p, q, q.ct_type[slot], &depth, &rmin, &rmax);
     if (status == QA_FORMING && sat == 1.0) {
+        // the breaking test needs the distance (only formed contacts)
+        double depth, rmin, rmax;
+        qa_lj(p, q, q.ct_type[slot], &depth, &rmin, &rmax);
+        const D3 r12 = d3ruv(rp.box, d.pos[cur][i1], d.pos[cur][i2]);
+        const double r12_rn = __ddiv_rn(1.0, __dsqrt_rn(d3dot(r12, r12)));
         if (__dmul_rn(__dmul_rn(p.qa_factor, rmin), r12_rn) < 1.0) {
             q.ct_status[slot] = QA_BREAKING;
             q.ct_ref[slot] = tnow;
@@ -418,7 +421,13 @@ __global__ void __launch_bounds__(256) k_qa_trans(Dev d, TermP p, int cur) {
         atomicAdd(&q.sync[i1], q.ct_d1[slot]);   // bytes stay <= 127: no carry
         atomicAdd(&q.sync[i2], q.ct_d2[slot]);
         q.ct_rm[slot] = 1;
+        return;
     }
+    // per-bead contact references of the contacts that stay
+    const int k1 = atomicAdd(&q.ref_cnt[i1], 1), k2 = atomicAdd(&q.ref_cnt[i2], 1);
+    if (k1 < QA_REF_CAP) q.ref[(size_t)k1 * d.N + i1] = slot;
+    if (k2 < QA_REF_CAP) q.ref[(size_t)k2 * d.N + i2] = slot;
+    if (k1 >= QA_REF_CAP || k2 >= QA_REF_CAP) atomicOr(d.status, 4);
 }
 
 // Removed pairs re-freed at the end of the free-pair list in contact-slot
@@ -461,22 +470,6 @@ __global__ void __launch_bounds__(1024) k_qa_refree(Dev d) {
         rp.fp_n = min(fp_n0 + total, fp_cap);
         if (s_err) atomicOr(d.status, 4);
     }
-}
-
-// per-bead contact references, one thread per contact slot of the pool
-__global__ void __launch_bounds__(256) k_qa_refs(Dev d) {
-    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
-    const QaDev &q = d.qa;
-    if (slot >= q.ct_total) return;
-    const int r = q.ct_rep[slot];
-    if (r < 0) return;
-    const RepDev &rp = d.rep[r];
-    if (!rp.active || slot - rp.ct_off >= rp.ct_n || q.ct_vac[slot]) return;
-    const int i1 = q.ct_i1[slot], i2 = q.ct_i2[slot];
-    const int k1 = atomicAdd(&q.ref_cnt[i1], 1), k2 = atomicAdd(&q.ref_cnt[i2], 1);
-    if (k1 < QA_REF_CAP) q.ref[(size_t)k1 * d.N + i1] = slot;
-    if (k2 < QA_REF_CAP) q.ref[(size_t)k2 * d.N + i2] = slot;
-    if (k1 >= QA_REF_CAP || k2 >= QA_REF_CAP) atomicOr(d.status, 4);
 }
 
 // ---- after a Verlet rebuild: the free-pair list re-listed ------------------------
