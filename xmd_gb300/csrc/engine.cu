@@ -1070,10 +1070,10 @@ __global__ void k_nl_check(Dev d, int advance, double dt, cudaGraphConditionalHa
 // replica and sets the graph's rebuild condition, so a step is one launch
 // plus the conditional rebuild.
 // resident blocks the register allocation leaves room for: 16 warps per SM
-// (at most 128 registers) with one or two threads per bead, 24 (at most 85)
+// (at most 128 registers) with one or two threads per bead, 28 (at most 73)
 // with four
 template <int FB, int LPB> constexpr int force_min_blocks() {
-    return LPB == 4 ? (768 / (FB * 4) > 0 ? 768 / (FB * 4) : 1) : 512 / (FB * LPB);
+    return LPB == 4 ? (896 / (FB * 4) > 0 ? 896 / (FB * 4) : 1) : 512 / (FB * LPB);
 }
 template <class FT, int MODE, int FB, int LPB>
 __global__ void __launch_bounds__(FB * LPB, (force_min_blocks<FB, LPB>())) k_force(Dev d, TermP p, int cur,
