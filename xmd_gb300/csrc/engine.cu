@@ -720,44 +720,34 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
     // (the next entry's index data is loaded while this entry's partner is
     // fetched).
     if (p.on[XMD_TERM_GO]) {
-        // two-deep pipeline: the partner position of the next entry and the
-        // index data of the one after are in flight while an entry is computed
         const int k1 = pf_n1;
         int k = pf_n0 + ln, m = 0;
-        int j = 0, jn = 0;
-        bool on = false, onn = false;
-        FT nd = FT(0), ndn = FT(0);
-        double4_32a pj = make_double4_32a(0, 0, 0, 0);
+        int j = 0;
+        bool on = false;
+        FT nd = FT(0);
         if (k < k1) {
             j = d.nat_j[k];
             on = d.nat_on[k] != 0;
             nd = nat_dist<FT>(d, k);
         }
-        if (k + LPB < k1) {
-            jn = d.nat_j[k + LPB];
-            onn = d.nat_on[k + LPB] != 0;
-            ndn = nat_dist<FT>(d, k + LPB);
-        }
-        if (on) pj = pin[j];
         for (; k < k1; k += LPB, ++m) {
-            double4_32a pjn = make_double4_32a(0, 0, 0, 0);
-            if (onn) pjn = pin[jn];
-            int jnn = 0;
-            bool onnn = false;
-            FT ndnn = FT(0);
-            if (k + 2 * LPB < k1) {
-                jnn = d.nat_j[k + 2 * LPB];
-                onnn = d.nat_on[k + 2 * LPB] != 0;
-                ndnn = nat_dist<FT>(d, k + 2 * LPB);
+            int jn = 0;
+            bool onn = false;
+            FT ndn = FT(0);
+            if (k + LPB < k1) {
+                jn = d.nat_j[k + LPB];
+                onn = d.nat_on[k + LPB] != 0;
+                ndn = nat_dist<FT>(d, k + LPB);
             }
             if (on) {
                 FT V_;
-                const V3<FT> f = go_pair<FT>(p, geo.to(pj), nd, &V_);
+                const V3<FT> f = go_pair<FT>(p, geo.to(pin[j]), nd, &V_);
                 acc_slot<LPB>(acc, m, f);
                 if (MODE == 0 && i < j) vgo += (double)V_;
             }
-            j = jn; on = onn; nd = ndn; pj = pjn;
-            jn = jnn; onn = onnn; ndn = ndnn;
+            j = jn;
+            on = onn;
+            nd = ndn;
         }
     }
     double vss = 0;
@@ -774,18 +764,14 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
         }
     }
     {
-        // two-deep pipeline, as for the natives
         const int cnt = pf_cnt;
-        int e = ln < cnt ? d.nl_row[(size_t)ln * N + i] : 0;
-        int en = ln + LPB < cnt ? d.nl_row[(size_t)(ln + LPB) * N + i] : 0;
-        double4_32a pj = make_double4_32a(0, 0, 0, 0);
-        if (ln < cnt) pj = pin[e & NL_MASK];
+        int e_next = ln < cnt ? d.nl_row[(size_t)ln * N + i] : 0;
         int m = 0;
         for (int k = ln; k < cnt; k += LPB, ++m) {
-            double4_32a pjn = make_double4_32a(0, 0, 0, 0);
-            if (k + LPB < cnt) pjn = pin[en & NL_MASK];
-            const int enn = k + 2 * LPB < cnt ? d.nl_row[(size_t)(k + 2 * LPB) * N + i] : 0;
+            const int e = e_next;
+            if (k + LPB < cnt) e_next = d.nl_row[(size_t)(k + LPB) * N + i];
             const int j = e & NL_MASK;
+            const double4_32a pj = pin[j];
             const V3<FT> r12 = geo.to(pj);
             V3<FT> f{FT(0), FT(0), FT(0)};
             bool any = false;
@@ -805,7 +791,6 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
                 if (MODE == 0 && i < j) ves += (double)V_;
             }
             if (any) acc_slot<LPB>(acc, m, f);
-            e = en; en = enn; pj = pjn;
         }
     }
 
