@@ -400,9 +400,18 @@ def serve_section(args, device, workers):
     rate = args.serve_load * cap["mixed"]["bead_steps_per_s"] / mean_work
     lat = serve_run(reqs, "mixed", args.serve_steps, rate, device)
     lat["offered_load"] = args.serve_load
+    # a small sweep of the offered load on the head of the same stream
+    sweep = []
+    for load in (float(x) for x in args.serve_sweep.split(",") if x):
+        rq = reqs[:args.serve_sweep_requests]
+        mw = float(np.mean([r.n for r in rq])) * args.serve_steps
+        one = serve_run(rq, "mixed", args.serve_steps, load * cap["mixed"]["bead_steps_per_s"] / mw, device, seed=1)
+        sweep.append({"offered_load": load, "requests": one["requests"], "p50_ms": one["p50_ms"],
+                      "p99_ms": one["p99_ms"], "bead_steps_per_s": one["bead_steps_per_s"],
+                      "completed": one["completed"]})
     return {"capacity": cap,
             "capacity_mixed_over_fp64": cap["mixed"]["bead_steps_per_s"] / cap["fp64"]["bead_steps_per_s"],
-            "latency": lat}
+            "latency": lat, "load_sweep": sweep}
 
 
 def serve_run(requests, precision, nsteps, rate_hz, device, seed=0):
@@ -614,6 +623,8 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-capacity-requests", type=int, default=32)
     ap.add_argument("--serve-load", type=float, default=0.7)
+    ap.add_argument("--serve-sweep", default="0.4,0.9", help="offered loads of the latency sweep")
+    ap.add_argument("--serve-sweep-requests", type=int, default=64)
     ap.add_argument("--serve-steps", type=int, default=20000)
     ap.add_argument("--accuracy-replicas", type=int, default=8)
     ap.add_argument("--accuracy-steps", type=int, default=20000)
