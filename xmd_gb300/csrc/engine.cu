@@ -1026,31 +1026,37 @@ __device__ __forceinline__ void nl_check_block(const Dev &d, int advance, double
     int any = 0;
     for (int r = threadIdx.x; r < d.R; r += blockDim.x) {
         RepDev &rp = d.rep[r];
-        if (!rp.active) continue;
-        if (rp.fault) {   // frozen: no further step, no list
+        // every field the decision reads, loaded at once (one round trip)
+        const int active = rp.active, fault = rp.fault, first = rp.first, tile = rp.tile;
+        const int nchunk = rp.nchunk, chunk_off = rp.chunk_off;
+        long long left = rp.steps_left;
+        const unsigned long long mdb = rp.maxdisp;
+        const double pad = rp.pad, tr = rp.t;
+        if (!active) continue;
+        if (fault) {   // frozen: no further step, no list
             rp.steps_left = 0;
             rp.rebuild = 0;
             continue;
         }
-        if (advance && rp.steps_left == 0) {           // took no step (k_force kept it)
+        if (advance && left == 0) {           // took no step (k_force kept it)
             rp.rebuild = 0;
             continue;
         }
         if (advance) {
-            rp.t += dt;                                // *t = (*true_t += dt)
-            if (rp.steps_left > 0) rp.steps_left -= 1;
+            rp.t = tr + dt;                   // *t = (*true_t += dt)
+            if (left > 0) rp.steps_left = --left;
         }
-        double md = __dsqrt_rn(__longlong_as_double((long long)rp.maxdisp));
+        const double md = __dsqrt_rn(__longlong_as_double((long long)mdb));
         rp.maxdisp = 0ull;
-        int rb = rp.first || (2.0 * md + 0.0 > rp.pad);
-        if (advance && rp.steps_left == 0 && !rp.first) rb = 0;   // no further step uses a list
+        int rb = first || (2.0 * md + 0.0 > pad);
+        if (advance && left == 0 && !first) rb = 0;   // no further step uses a list
         rp.rebuild = rb;
         any |= rb;
         // the tile build's work list: every chunk of the flagged replicas
         // (order is free: each chunk writes its own rows)
-        if (rb && rp.tile) {
-            const int at = atomicAdd(&nwork_s, rp.nchunk);
-            for (int c = 0; c < rp.nchunk; ++c) d.work[at + c] = rp.chunk_off + c;
+        if (rb && tile) {
+            const int at = atomicAdd(&nwork_s, nchunk);
+            for (int c = 0; c < nchunk; ++c) d.work[at + c] = chunk_off + c;
         }
     }
     if (any) atomicOr(&any_s, 1);
@@ -1623,7 +1629,7 @@ __global__ void __launch_bounds__(NC_WARPS * 32, 3) k_nl_cells(Dev d, TermP p, i
 // of a distance between coordinates of magnitude <= ext, so both paths keep
 // exactly the same pairs.
 // Rows come out ordered by j (ballot compaction in lane order).
-constexpr int TL_CH = 16;      // rows per chunk: two per warp
+constexpr int TL_CH = 8;       // rows per chunk: one per warp (a pass of a few replicas spreads over more blocks)
 constexpr int TL_THREADS = 256;
 constexpr int TL_WARPS = TL_THREADS / 32;
 constexpr int TILE_MAX = 4096;
