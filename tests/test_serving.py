@@ -153,7 +153,9 @@ def test_budget_is_the_real_allocation():
         st = srv.stats()
     assert st["budget_bytes"] == budget
     assert 0.9 * budget <= st["device_bytes"] <= budget
-    assert st["cap_beads"] * st["bytes_per_bead"] <= budget
+    # the per-slot figure is the slope of the measured cost (its fixed part
+    # can be slightly negative), so the product only approximates the budget
+    assert st["cap_beads"] * st["bytes_per_bead"] <= 1.01 * budget
     assert 500 <= st["bytes_per_bead"] <= 4096
 
 
