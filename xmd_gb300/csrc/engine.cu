@@ -3538,10 +3538,10 @@ void Engine::launch_force_step() {
     ++launches;
     if (d.qa_on) {
         // sift + acceptance + transitions at this step's positions (qa.cpp:20-31)
-        k_qa_sift<<<(d.qa.fp_total + QA_SIFT - 1) / QA_SIFT, QA_SIFT, 0, stream>>>(d, tp, cur);
+        k_qa_sift<<<sift_grid(), QA_SIFT, 0, stream>>>(d, tp, cur);
         k_qa_step<<<d.R, 1024, 0, stream>>>(d, tp, cur);
         const int gc = (d.qa.ct_total + 255) / 256;
-        k_qa_trans<<<gc, 256, 0, stream>>>(d, tp, cur);
+        k_qa_trans<<<trans_grid(), QA_TG, 0, stream>>>(d, tp, cur);
         k_qa_refree<<<d.R, 1024, 0, stream>>>(d);
         launches += 4;
     }
@@ -3605,7 +3605,7 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
             cudaKernelNodeParams ks{}, kq{};
             void *sargs[] = {&d, &tp, &c};
             ks.func = (void *)k_qa_sift;
-            ks.gridDim = dim3((d.qa.fp_total + QA_SIFT - 1) / QA_SIFT);
+            ks.gridDim = dim3(sift_grid());
             ks.blockDim = dim3(QA_SIFT);
             ks.kernelParams = sargs;
             kq.func = (void *)k_qa_step;
@@ -3616,8 +3616,8 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
             void *dargs[] = {&d};
             const unsigned gc = (unsigned)((d.qa.ct_total + 255) / 256);
             kt.func = (void *)k_qa_trans;
-            kt.gridDim = dim3(gc);
-            kt.blockDim = dim3(256);
+            kt.gridDim = dim3(trans_grid());
+            kt.blockDim = dim3(QA_TG);
             kt.kernelParams = sargs;
             kr.func = (void *)k_qa_refree;
             kr.gridDim = dim3(d.R);

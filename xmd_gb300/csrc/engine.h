@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <map>
 #include <string>
@@ -364,6 +365,17 @@ private:
     bool isolate_faults = false;
     void launch_force(int mode, int c);
     int tile_sms = 1, tile_max_per_sm = 1;     // for the tile build's resident grid
+    // the QA sift's fixed grid: four blocks per SM, each taking at most
+    // QA_SIFT groups of free-pair slots
+    int sift_grid() const {
+        const int ng = (d.qa.fp_total + QA_SIFT - 1) / QA_SIFT;
+        return std::max(4 * tile_sms, (ng + QA_SIFT - 1) / QA_SIFT);
+    }
+    // the QA transitions' fixed grid (groups of 256 contact slots)
+    int trans_grid() const {
+        const int ng = (d.qa.ct_total + 255) / 256;
+        return std::max(4 * tile_sms, (ng + 255) / 256);
+    }
     std::vector<cudaEvent_t> ev_force, ev_rebuild;   // start/stop pairs
     size_t n_ev_force = 0, n_ev_rebuild = 0;
 

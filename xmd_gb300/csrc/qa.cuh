@@ -168,12 +168,11 @@ __device__ __forceinline__ bool cmp_band(float x, float T, bool less, bool *unsu
     return less ? x < T : x > T;
 }
 
-__global__ void __launch_bounds__(QA_SIFT, 4) k_qa_sift(Dev d, TermP p, int cur) {
-    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+// one group of QA_SIFT free-pair slots: the decisions, then the ordered
+// compaction of the group's candidates into its cand_list segment
+__device__ __forceinline__ void qa_sift_group(const Dev &d, const TermP &p, int cur, int sg) {
+    const int slot = sg * QA_SIFT + threadIdx.x;
     const QaDev &q = d.qa;
-    // the per-bead contact references are listed again at this step's end
-    // (k_qa_trans); nothing reads them before that
-    for (int k = slot; k < d.N; k += gridDim.x * blockDim.x) q.ref_cnt[k] = 0;
     bool live = slot < q.fp_total;
     const int r = live ? q.fp_rep[slot] : 0;
     const RepDev &rp = d.rep[r];
@@ -233,7 +232,7 @@ __global__ void __launch_bounds__(QA_SIFT, 4) k_qa_sift(Dev d, TermP p, int cur)
         q.cand_d1[slot] = d1p;
         q.cand_d2[slot] = d2p;
     }
-    // ordered compaction of the block's candidates
+    // ordered compaction of the group's candidates
     __shared__ int s_wc[QA_SIFT / 32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned bal = __ballot_sync(0xffffffffu, type != 0);
@@ -245,8 +244,39 @@ __global__ void __launch_bounds__(QA_SIFT, 4) k_qa_sift(Dev d, TermP p, int cur)
         before += k < w ? s_wc[k] : 0;
         total += s_wc[k];
     }
-    if (type != 0) q.cand_list[(size_t)blockIdx.x * QA_SIFT + before + __popc(bal & ((1u << lane) - 1u))] = slot;
-    if (threadIdx.x == 0) q.cand_blk[blockIdx.x] = total;
+    if (type != 0) q.cand_list[(size_t)sg * QA_SIFT + before + __popc(bal & ((1u << lane) - 1u))] = slot;
+    if (threadIdx.x == 0) q.cand_blk[sg] = total;
+    __syncthreads();   // s_wc is reused by the next group
+}
+
+// A fixed grid: each block takes a contiguous run of groups, finds with one
+// round of parallel loads which of them hold live slots (a replica's live
+// slots are a prefix of its region, and the free-pair capacity is far above
+// the live count), then sifts only those.  Groups without a live slot are
+// never read (k_qa_step reads the groups of each replica's live range).
+__global__ void __launch_bounds__(QA_SIFT, 4) k_qa_sift(Dev d, TermP p, int cur) {
+    const QaDev &q = d.qa;
+    const int t = threadIdx.x;
+    // the per-bead contact references are listed again at this step's end
+    // (k_qa_trans); nothing reads them before that
+    for (int k = blockIdx.x * blockDim.x + t; k < d.N; k += gridDim.x * blockDim.x) q.ref_cnt[k] = 0;
+    const int ng = (q.fp_total + QA_SIFT - 1) / QA_SIFT;
+    const int per = (ng + gridDim.x - 1) / gridDim.x;   // <= QA_SIFT (the grid is sized for it)
+    const int g0 = min(blockIdx.x * per, ng), g1 = min(g0 + per, ng);
+    bool lv = false;
+    if (t < g1 - g0) {
+        const int first = (g0 + t) * QA_SIFT, last = min(first + QA_SIFT, q.fp_total) - 1;
+        const int r1 = q.fp_rep[first], r2 = q.fp_rep[last];
+        const RepDev &a = d.rep[r1];
+        lv = first - a.fp_off < a.fp_n;               // the group starts inside r1's live prefix
+        if (r2 != r1) lv = lv || d.rep[r2].fp_n > 0;  // r2's region starts inside the group
+    }
+    __shared__ unsigned s_live[QA_SIFT / 32];
+    const unsigned bl = __ballot_sync(0xffffffffu, lv);
+    if ((t & 31) == 0) s_live[t >> 5] = bl;
+    __syncthreads();
+    for (int k = 0; k < g1 - g0; ++k)
+        if ((s_live[k >> 5] >> (k & 31)) & 1u) qa_sift_group(d, p, cur, g0 + k);
 }
 
 // ---- acceptance: process_candidates::iter (process_candidates.cpp:10-29) in
@@ -391,8 +421,7 @@ __global__ void __launch_bounds__(1024) k_qa_step(Dev d, TermP p, int cur) {
 // Contacts accepted at this step have saturation 0 and stay as they are.
 // The contacts that stay are then listed per bead (the references the next
 // step's forces and list builds read; cleared by the sift).
-__global__ void __launch_bounds__(256) k_qa_trans(Dev d, TermP p, int cur) {
-    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void qa_trans_slot(const Dev &d, const TermP &p, int cur, int slot) {
     const QaDev &q = d.qa;
     if (slot >= q.ct_total) return;
     q.ct_rm[slot] = 0;
@@ -428,6 +457,34 @@ __global__ void __launch_bounds__(256) k_qa_trans(Dev d, TermP p, int cur) {
     if (k1 < QA_REF_CAP) q.ref[(size_t)k1 * d.N + i1] = slot;
     if (k2 < QA_REF_CAP) q.ref[(size_t)k2 * d.N + i2] = slot;
     if (k1 >= QA_REF_CAP || k2 >= QA_REF_CAP) atomicOr(d.status, 4);
+}
+// A fixed grid, as the sift: each block takes a contiguous run of groups of
+// 256 contact slots and processes the groups that hold live slots (a
+// replica's live contacts are a prefix of its region; re-freeing reads the
+// removal flags of live slots only).
+constexpr int QA_TG = 256;
+__global__ void __launch_bounds__(QA_TG) k_qa_trans(Dev d, TermP p, int cur) {
+    const QaDev &q = d.qa;
+    const int t = threadIdx.x;
+    const int ng = (q.ct_total + QA_TG - 1) / QA_TG;
+    const int per = (ng + gridDim.x - 1) / gridDim.x;
+    const int g0 = min(blockIdx.x * per, ng), g1 = min(g0 + per, ng);
+    bool lv = false;
+    if (t < g1 - g0) {
+        const int first = (g0 + t) * QA_TG, last = min(first + QA_TG, q.ct_total) - 1;
+        const int r1 = q.ct_rep[first], r2 = q.ct_rep[last];
+        if (r1 >= 0) {
+            const RepDev &a = d.rep[r1];
+            lv = first - a.ct_off < a.ct_n;
+        }
+        if (r2 >= 0 && r2 != r1) lv = lv || d.rep[r2].ct_n > 0;
+    }
+    __shared__ unsigned s_live[QA_TG / 32];
+    const unsigned bl = __ballot_sync(0xffffffffu, lv);
+    if ((t & 31) == 0) s_live[t >> 5] = bl;
+    __syncthreads();
+    for (int k = 0; k < g1 - g0; ++k)
+        if ((s_live[k >> 5] >> (k & 31)) & 1u) qa_trans_slot(d, p, cur, (g0 + k) * QA_TG + t);
 }
 
 // Removed pairs re-freed at the end of the free-pair list in contact-slot
