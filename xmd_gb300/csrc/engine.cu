@@ -3540,7 +3540,6 @@ void Engine::launch_force_step() {
         // sift + acceptance + transitions at this step's positions (qa.cpp:20-31)
         k_qa_sift<<<sift_grid(), QA_SIFT, 0, stream>>>(d, tp, cur);
         k_qa_step<<<d.R, 1024, 0, stream>>>(d, tp, cur);
-        const int gc = (d.qa.ct_total + 255) / 256;
         k_qa_trans<<<trans_grid(), QA_TG, 0, stream>>>(d, tp, cur);
         k_qa_refree<<<d.R, 1024, 0, stream>>>(d);
         launches += 4;
@@ -3614,7 +3613,6 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
             kq.kernelParams = sargs;
             cudaKernelNodeParams kt{}, kr{};
             void *dargs[] = {&d};
-            const unsigned gc = (unsigned)((d.qa.ct_total + 255) / 256);
             kt.func = (void *)k_qa_trans;
             kt.gridDim = dim3(trans_grid());
             kt.blockDim = dim3(QA_TG);
