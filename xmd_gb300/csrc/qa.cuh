@@ -249,10 +249,12 @@ __device__ __forceinline__ void qa_sift_group(const Dev &d, const TermP &p, int 
     __syncthreads();   // s_wc is reused by the next group
 }
 
-// A fixed grid: each block takes a contiguous run of groups, finds with one
-// round of parallel loads which of them hold live slots (a replica's live
-// slots are a prefix of its region, and the free-pair capacity is far above
-// the live count), then sifts only those.  Groups without a live slot are
+// A fixed grid: block b takes groups b, b + G, b + 2G, ... (G blocks), finds
+// with one round of parallel loads which of them hold live slots (a
+// replica's live slots are a prefix of its region, and the free-pair
+// capacity is far above the live count), then sifts only those.  Dealing the
+// groups round-robin spreads a replica's live prefix over all blocks, so one
+// large replica is sifted by the whole grid.  Groups without a live slot are
 // never read (k_qa_step reads the groups of each replica's live range).
 __global__ void __launch_bounds__(QA_SIFT, 4) k_qa_sift(Dev d, TermP p, int cur) {
     const QaDev &q = d.qa;
@@ -260,12 +262,11 @@ __global__ void __launch_bounds__(QA_SIFT, 4) k_qa_sift(Dev d, TermP p, int cur)
     // the per-bead contact references are listed again at this step's end
     // (k_qa_trans); nothing reads them before that
     for (int k = blockIdx.x * blockDim.x + t; k < d.N; k += gridDim.x * blockDim.x) q.ref_cnt[k] = 0;
-    const int ng = (q.fp_total + QA_SIFT - 1) / QA_SIFT;
-    const int per = (ng + gridDim.x - 1) / gridDim.x;   // <= QA_SIFT (the grid is sized for it)
-    const int g0 = min(blockIdx.x * per, ng), g1 = min(g0 + per, ng);
+    const int ng = (q.fp_total + QA_SIFT - 1) / QA_SIFT, G = gridDim.x;
+    const int per = (ng - (int)blockIdx.x + G - 1) / G;   // <= QA_SIFT (the grid is sized for it)
     bool lv = false;
-    if (t < g1 - g0) {
-        const int first = (g0 + t) * QA_SIFT, last = min(first + QA_SIFT, q.fp_total) - 1;
+    if (t < per) {
+        const int first = (blockIdx.x + t * G) * QA_SIFT, last = min(first + QA_SIFT, q.fp_total) - 1;
         const int r1 = q.fp_rep[first], r2 = q.fp_rep[last];
         const RepDev &a = d.rep[r1];
         lv = first - a.fp_off < a.fp_n;               // the group starts inside r1's live prefix
@@ -275,8 +276,8 @@ __global__ void __launch_bounds__(QA_SIFT, 4) k_qa_sift(Dev d, TermP p, int cur)
     const unsigned bl = __ballot_sync(0xffffffffu, lv);
     if ((t & 31) == 0) s_live[t >> 5] = bl;
     __syncthreads();
-    for (int k = 0; k < g1 - g0; ++k)
-        if ((s_live[k >> 5] >> (k & 31)) & 1u) qa_sift_group(d, p, cur, g0 + k);
+    for (int k = 0; k < per; ++k)
+        if ((s_live[k >> 5] >> (k & 31)) & 1u) qa_sift_group(d, p, cur, blockIdx.x + k * G);
 }
 
 // ---- acceptance: process_candidates::iter (process_candidates.cpp:10-29) in
@@ -458,20 +459,19 @@ __device__ __forceinline__ void qa_trans_slot(const Dev &d, const TermP &p, int 
     if (k2 < QA_REF_CAP) q.ref[(size_t)k2 * d.N + i2] = slot;
     if (k1 >= QA_REF_CAP || k2 >= QA_REF_CAP) atomicOr(d.status, 4);
 }
-// A fixed grid, as the sift: each block takes a contiguous run of groups of
-// 256 contact slots and processes the groups that hold live slots (a
-// replica's live contacts are a prefix of its region; re-freeing reads the
-// removal flags of live slots only).
+// A fixed grid, as the sift: block b takes groups b, b + G, ... of 256
+// contact slots and processes the groups that hold live slots (a replica's
+// live contacts are a prefix of its region; re-freeing reads the removal
+// flags of live slots only).
 constexpr int QA_TG = 256;
 __global__ void __launch_bounds__(QA_TG) k_qa_trans(Dev d, TermP p, int cur) {
     const QaDev &q = d.qa;
     const int t = threadIdx.x;
-    const int ng = (q.ct_total + QA_TG - 1) / QA_TG;
-    const int per = (ng + gridDim.x - 1) / gridDim.x;
-    const int g0 = min(blockIdx.x * per, ng), g1 = min(g0 + per, ng);
+    const int ng = (q.ct_total + QA_TG - 1) / QA_TG, G = gridDim.x;
+    const int per = (ng - (int)blockIdx.x + G - 1) / G;   // <= QA_TG (the grid is sized for it)
     bool lv = false;
-    if (t < g1 - g0) {
-        const int first = (g0 + t) * QA_TG, last = min(first + QA_TG, q.ct_total) - 1;
+    if (t < per) {
+        const int first = (blockIdx.x + t * G) * QA_TG, last = min(first + QA_TG, q.ct_total) - 1;
         const int r1 = q.ct_rep[first], r2 = q.ct_rep[last];
         if (r1 >= 0) {
             const RepDev &a = d.rep[r1];
@@ -483,8 +483,8 @@ __global__ void __launch_bounds__(QA_TG) k_qa_trans(Dev d, TermP p, int cur) {
     const unsigned bl = __ballot_sync(0xffffffffu, lv);
     if ((t & 31) == 0) s_live[t >> 5] = bl;
     __syncthreads();
-    for (int k = 0; k < g1 - g0; ++k)
-        if ((s_live[k >> 5] >> (k & 31)) & 1u) qa_trans_slot(d, p, cur, (g0 + k) * QA_TG + t);
+    for (int k = 0; k < per; ++k)
+        if ((s_live[k >> 5] >> (k & 31)) & 1u) qa_trans_slot(d, p, cur, (blockIdx.x + k * G) * QA_TG + t);
 }
 
 // Removed pairs re-freed at the end of the free-pair list in contact-slot
