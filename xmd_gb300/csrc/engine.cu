@@ -1073,8 +1073,8 @@ __global__ void k_nl_check(Dev d, int advance, double dt, cudaGraphConditionalHa
 
 // The step kernel.  With `fuse` (graph steps without the quasi-adiabatic
 // term) the last block to finish also takes the skin decision of every
-// replica and sets the graph's rebuild condition, so a step is one launch
-// plus the conditional rebuild.
+// replica (fuse 1: and sets the graph's rebuild condition; fuse 2: the next
+// node, the row build, runs on the work list it leaves, empty or not).
 // resident blocks the register allocation leaves room for: 16 warps per SM
 // (at most 128 registers) with one or two threads per bead, 28 (at most 73)
 // with four
@@ -1102,7 +1102,7 @@ __global__ void __launch_bounds__(FB * LPB, (force_min_blocks<FB, LPB>())) k_for
         __syncthreads();
         if (last_s) {
             __threadfence();
-            nl_check_block(d, 1, p.dt, h, 1);
+            nl_check_block(d, 1, p.dt, h, fuse == 1);
             if (threadIdx.x == 0) d.ctr[2] = 0ull;
         }
     }
@@ -1910,9 +1910,11 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
     }
 }
 
-__global__ void __launch_bounds__(TL_THREADS, 4) k_nl_tile(Dev d, TermP p, int cur) {
-    if (blockIdx.x == 0 && threadIdx.x == 0 && !d.any_cell) atomicAdd(d.ctr, 1ull);
+// `count`: a pass with work adds to the pass counter (launches that run
+// every step, with or without work, are counted where they are issued)
+__global__ void __launch_bounds__(TL_THREADS, 4) k_nl_tile(Dev d, TermP p, int cur, int count) {
     const int nw = *d.nwork;
+    if (count && blockIdx.x == 0 && threadIdx.x == 0 && !d.any_cell && nw > 0) atomicAdd(d.ctr, 1ull);
     for (int w = blockIdx.x; w < nw; w += gridDim.x) {
         tl_chunk(d, p, cur, d.chunks[d.work[w]]);
         __syncthreads();   // the next chunk overwrites the shared tile
@@ -2165,9 +2167,11 @@ void Engine::step_async(int nsteps) {
         for (; s + gsteps <= nsteps; s += gsteps) {
             CK(cudaGraphLaunch(graph_for(cur), stream));
             // per step: the step kernel (plus the separate check and the
-            // quasi-adiabatic kernels with that term); rebuild kernels are
-            // counted per pass in stats()
-            launches += (d.qa_on ? 6 : 1) * gsteps;
+            // quasi-adiabatic kernels with that term, the external-force and
+            // PID kernels, and a plain row-build node); rebuild kernels of IF
+            // nodes are counted per pass in stats()
+            launches += (int64_t)((d.qa_on ? 6 : 1) + (tp.ext_on ? 1 : 0) + (tp.on[XMD_TERM_PID] ? 1 : 0) +
+                                  (plain_rebuild() ? 1 : 0)) * gsteps;
             md_steps += gsteps;
         }
     }
@@ -3378,7 +3382,7 @@ void Engine::launch_rebuild() {
         k_cell_finish<<<(d.ncells + CF_WARPS - 1) / CF_WARPS, CF_WARPS * 32, 0, stream>>>(d, cur);
         k_nl_cells<<<(d.N + NC_WARPS - 1) / NC_WARPS, NC_WARPS * 32, 0, stream>>>(d, tp, cur);
     }
-    if (any_tile) k_nl_tile<<<tile_grid, TL_THREADS, tile_smem, stream>>>(d, tp, cur);
+    if (any_tile) k_nl_tile<<<tile_grid, TL_THREADS, tile_smem, stream>>>(d, tp, cur, 1);
     if (d.qa_on) {
         k_qa_fp_scan<<<d.qa.nbchunk, QA_BCHUNK, 0, stream>>>(d);
         k_qa_fp_base<<<d.R, 1024, 0, stream>>>(d);
@@ -3535,7 +3539,7 @@ void Engine::launch_force_step() {
     if (timing) record(ev_force, n_ev_force);
     launch_force(1, cur);
     if (timing) record(ev_force, n_ev_force);
-    ++launches;
+    launches += 1 + (tp.ext_on ? 1 : 0) + (tp.on[XMD_TERM_PID] ? 1 : 0);
     if (d.qa_on) {
         // sift + acceptance + transitions at this step's positions (qa.cpp:20-31)
         k_qa_sift<<<sift_grid(), QA_SIFT, 0, stream>>>(d, tp, cur);
@@ -3548,8 +3552,12 @@ void Engine::launch_force_step() {
 
 // One graph runs tune.graph_steps steps: per step a force+integrate node, a skin
 // check that sets a conditional handle on the device, and an IF node whose
-// body rebuilds the lists of the flagged replicas (cells, then rows).  An
-// even step count leaves the position double buffer where it started.
+// body rebuilds the lists of the flagged replicas (cells, then rows).  Where
+// the rebuild is the row build alone (no cell-path replica, no
+// quasi-adiabatic term) it is a plain node after the step kernel instead: it
+// returns at once when the work list is empty, and an IF node costs more per
+// step than that empty launch.  An even step count leaves the position double
+// buffer where it started.
 cudaGraphExec_t Engine::graph_for(int start_cur) {
     GraphSet &gs = graphs[params.precision == XMD_PREC_MIXED][start_cur];
     if (gs.exec) return gs.exec;
@@ -3561,12 +3569,14 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
     double dt = params.dt;
     // without the quasi-adiabatic term the step kernel takes the skin
     // decision itself (its last block), so a step is one kernel node
-    const int fuse = d.qa_on ? 0 : 1;
+    const bool plain = plain_rebuild();
+    const int fuse = d.qa_on ? 0 : plain ? 2 : 1;
+    int zero = 0;
     for (int s = 0; s < tune.graph_steps; ++s) {
         int c = start_cur ^ (s & 1), cn = c ^ 1;
         int adv = 1, setc = 1;
-        cudaGraphConditionalHandle h;
-        CK(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
+        cudaGraphConditionalHandle h = 0;
+        if (!plain) CK(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
         cudaKernelNodeParams kf{};
         cudaGraphConditionalHandle hf = fuse ? h : 0;
         int ff = fuse;
@@ -3639,6 +3649,18 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
             kc.kernelParams = cargs;
             CK(cudaGraphAddKernelNode(&nc, g, &nf, 1, &kc));
         }
+        if (plain) {
+            cudaKernelNodeParams kt{};
+            void *targs[] = {&d, &tp, &cn, &zero};
+            kt.func = (void *)k_nl_tile;
+            kt.gridDim = dim3(tile_grid);
+            kt.blockDim = dim3(TL_THREADS);
+            kt.sharedMemBytes = (unsigned)tile_smem;
+            kt.kernelParams = targs;
+            CK(cudaGraphAddKernelNode(&ncond, g, &nc, 1, &kt));
+            prev = ncond;
+            continue;
+        }
         cudaGraphNodeParams cp{};
         cp.type = cudaGraphNodeTypeConditional;
         cp.conditional.handle = h;
@@ -3664,6 +3686,8 @@ void Engine::add_rebuild_nodes(cudaGraph_t body, int cn) {
     void *a1[] = {&d, &cn};
     void *a2[] = {&d, &tp, &cn};
     void *a3[] = {&d};
+    int one = 1;
+    void *a4[] = {&d, &tp, &cn, &one};
     if (any_cell) {
         cudaKernelNodeParams k1{}, k2{}, kc{}, ks{}, kx{}, kf{};
         k1.func = (void *)k_cells;
@@ -3704,7 +3728,7 @@ void Engine::add_rebuild_nodes(cudaGraph_t body, int cn) {
         kt.gridDim = dim3(tile_grid);
         kt.blockDim = dim3(TL_THREADS);
         kt.sharedMemBytes = (unsigned)tile_smem;
-        kt.kernelParams = a2;
+        kt.kernelParams = a4;
         add(kt);
     }
     if (d.qa_on) {

@@ -371,6 +371,8 @@ private:
         const int ng = (d.qa.fp_total + QA_SIFT - 1) / QA_SIFT;
         return std::max(4 * tile_sms, (ng + QA_SIFT - 1) / QA_SIFT);
     }
+    // graphs rebuild with a plain row-build node instead of an IF node
+    bool plain_rebuild() const { return any_tile && !any_cell && !d.qa_on; }
     // the QA transitions' fixed grid (groups of 256 contact slots)
     int trans_grid() const {
         const int ng = (d.qa.ct_total + 255) / 256;
