@@ -208,7 +208,7 @@ __device__ __forceinline__ WallOut wall_forces(const double *wall, LjWallState *
 template <int MODE>
 __global__ void __launch_bounds__(256) k_ext(Dev d, TermP p, int cur) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= d.N) return;
+    if (i >= d.N || (MODE == 1 && d.gate[0])) return;
     double *fo = d.fext + 3 * (size_t)i;
     fo[0] = fo[1] = fo[2] = 0.0;
     const int r = d.rep_of[i];
@@ -319,7 +319,7 @@ __device__ __forceinline__ DN pid_psi(const BoxD &b, D3N r1_, D3N r2_, D3N r3_, 
 template <int MODE>
 __global__ void __launch_bounds__(128) k_pid(Dev d, TermP p, int cur) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= d.N) return;
+    if (i >= d.N || (MODE == 1 && d.gate[0])) return;
     const size_t N = d.N;
     double *Fs = d.pid_f, *Fp = d.pid_f + 3 * N, *Fn = d.pid_f + 6 * N;
     D3N fs{DN(0.0), DN(0.0), DN(0.0)}, fp = fs, fn = fs;
@@ -1017,7 +1017,10 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
 }
 
 // ---- skin decision (nl::verify, verify.cpp:4-23) --------------------------------
-// setc: also set the conditional handle of the graph's rebuild IF node
+// setc 1: also set the conditional handle of the graph's rebuild IF node;
+// setc 2: count the step in the gate and halt the graph when a replica is
+// flagged or the budget of steps is spent
+enum : int { CHECK_PLAIN = 0, CHECK_COND = 1, CHECK_GATE = 2 };
 __device__ __forceinline__ void nl_check_block(const Dev &d, int advance, double dt, cudaGraphConditionalHandle h,
                                                int setc) {
     __shared__ int any_s, nwork_s;
@@ -1064,17 +1067,26 @@ __device__ __forceinline__ void nl_check_block(const Dev &d, int advance, double
     if (threadIdx.x == 0) {
         *d.any_rebuild = any_s;
         *d.nwork = nwork_s;
-        if (setc) cudaGraphSetConditional(h, any_s ? 1u : 0u);
+        if (setc == CHECK_COND) cudaGraphSetConditional(h, any_s ? 1u : 0u);
+        if (setc == CHECK_GATE) {
+            const int done = d.gate[1] + 1;
+            d.gate[1] = done;
+            if (any_s || done >= d.gate[2]) d.gate[0] = 1;
+        }
     }
 }
 __global__ void k_nl_check(Dev d, int advance, double dt, cudaGraphConditionalHandle h, int setc) {
+    if (setc == CHECK_GATE && d.gate[0]) return;
     nl_check_block(d, advance, dt, h, setc);
 }
 
 // The step kernel.  With `fuse` (graph steps without the quasi-adiabatic
 // term) the last block to finish also takes the skin decision of every
 // replica (fuse 1: and sets the graph's rebuild condition; fuse 2: the next
-// node, the row build, runs on the work list it leaves, empty or not).
+// node, the row build, runs on the work list it leaves, empty or not;
+// fuse 3: it keeps the gate, and the kernel returns at once while the gate
+// is closed).  fuse 4: no fused decision; the kernel returns at once while
+// the gate is closed (the separate check keeps it).
 // resident blocks the register allocation leaves room for: 16 warps per SM
 // (at most 128 registers) with one or two threads per bead, 28 (at most 73)
 // with four
@@ -1087,13 +1099,14 @@ __global__ void __launch_bounds__(FB * LPB, (force_min_blocks<FB, LPB>())) k_for
                                                                                   int fuse) {
     __shared__ int last_s;
     static_assert(LPB == 1 || LPB == 2 || LPB == 4, "one, two or four threads per bead");
+    if (MODE == 1 && fuse >= 3 && d.gate[0]) return;   // uniform: the gate changes between launches
     constexpr int FBT = force_beads<FB, LPB>();
     // the block runs when an occupancy granule of its beads is on (uniform)
     const int i0 = blockIdx.x * FBT, i1 = min(i0 + FBT, d.N) - 1;
     bool on = false;
     for (int g = i0 / BLK_ON; g <= i1 / BLK_ON; ++g) on |= d.blk_on[g] != 0;
     if (on) force_block<FT, MODE, FB, LPB>(d, p, cur);
-    if (MODE == 1 && fuse) {
+    if (MODE == 1 && fuse >= 1 && fuse <= 3) {
         __syncthreads();
         if (threadIdx.x == 0) {
             __threadfence();
@@ -1102,7 +1115,7 @@ __global__ void __launch_bounds__(FB * LPB, (force_min_blocks<FB, LPB>())) k_for
         __syncthreads();
         if (last_s) {
             __threadfence();
-            nl_check_block(d, 1, p.dt, h, fuse == 1);
+            nl_check_block(d, 1, p.dt, h, fuse == 1 ? CHECK_COND : fuse == 3 ? CHECK_GATE : CHECK_PLAIN);
             if (threadIdx.x == 0) d.ctr[2] = 0ull;
         }
     }
@@ -2164,15 +2177,40 @@ void Engine::step_async(int nsteps) {
     int s = 0;
     if (!timing && use_graphs) {
         const int gsteps = tune.graph_steps;
-        for (; s + gsteps <= nsteps; s += gsteps) {
-            CK(cudaGraphLaunch(graph_for(cur), stream));
-            // per step: the step kernel (plus the separate check and the
-            // quasi-adiabatic kernels with that term, the external-force and
-            // PID kernels, and a plain row-build node); rebuild kernels of IF
-            // nodes are counted per pass in stats()
-            launches += (int64_t)((d.qa_on ? 6 : 1) + (tp.ext_on ? 1 : 0) + (tp.on[XMD_TERM_PID] ? 1 : 0) +
-                                  (plain_rebuild() ? 1 : 0)) * gsteps;
-            md_steps += gsteps;
+        // per step: the step kernel (plus the separate check and the
+        // quasi-adiabatic kernels with that term, the external-force and PID
+        // kernels, and a plain row-build node); rebuild kernels of IF nodes
+        // are counted per pass in stats()
+        const int64_t per_step = (d.qa_on ? 6 : 1) + (tp.ext_on ? 1 : 0) + (tp.on[XMD_TERM_PID] ? 1 : 0) +
+                                 (plain_rebuild() ? 1 : 0);
+        if (gated_graphs()) {
+            // each graph runs until a check flags a replica (or its steps are
+            // done); the host then rebuilds and goes on from the steps taken.
+            // The gate is open outside these graphs (per-launch steps read it).
+            struct Open {
+                Engine *e;
+                ~Open() { cudaMemsetAsync(e->d.gate, 0, sizeof(int) * 3, e->stream); }
+            } open_gate{this};
+            while (nsteps - s >= gsteps) {
+                h_any[0] = 0; h_any[1] = 0; h_any[2] = 0; h_any[3] = gsteps;
+                CK(cudaMemcpyAsync(d.any_rebuild, h_any, sizeof(int) * 4, cudaMemcpyHostToDevice, stream));
+                CK(cudaGraphLaunch(graph_for(cur), stream));
+                CK(cudaMemcpyAsync(h_any, d.any_rebuild, sizeof(int) * 4, cudaMemcpyDeviceToHost, stream));
+                CK(cudaStreamSynchronize(stream));
+                const int done = h_any[2];
+                if (done < 1 || done > gsteps) throw std::logic_error("engine: graph step count out of range");
+                launches += per_step * gsteps;
+                md_steps += done;
+                s += done;
+                cur ^= done & 1;
+                if (h_any[0]) launch_rebuild();
+            }
+        } else {
+            for (; s + gsteps <= nsteps; s += gsteps) {
+                CK(cudaGraphLaunch(graph_for(cur), stream));
+                launches += per_step * gsteps;
+                md_steps += gsteps;
+            }
         }
     }
     for (; s < nsteps; ++s) {
@@ -2579,6 +2617,7 @@ void Engine::allocate() {
     d.jump = (uint64_t *)dalloc(sizeof(uint64_t) * JUMP_WORDS * R);
     d.rep = (RepDev *)dalloc(sizeof(RepDev) * R);
     d.any_rebuild = (int *)dalloc(sizeof(int) * 4);
+    d.gate = d.any_rebuild + 1;
     d.status = (int *)dalloc(sizeof(int) * 4);
     d.ctr = (unsigned long long *)dalloc(sizeof(unsigned long long) * 4);
     d.nchunks = std::max(1, cap.chunks);
@@ -3569,14 +3608,14 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
     double dt = params.dt;
     // without the quasi-adiabatic term the step kernel takes the skin
     // decision itself (its last block), so a step is one kernel node
-    const bool plain = plain_rebuild();
-    const int fuse = d.qa_on ? 0 : plain ? 2 : 1;
+    const bool plain = plain_rebuild(), gated = gated_graphs();
+    const int fuse = d.qa_on ? (gated ? 4 : 0) : plain ? 2 : gated ? 3 : 1;
     int zero = 0;
     for (int s = 0; s < tune.graph_steps; ++s) {
         int c = start_cur ^ (s & 1), cn = c ^ 1;
-        int adv = 1, setc = 1;
+        int adv = 1, setc = gated ? CHECK_GATE : CHECK_COND;
         cudaGraphConditionalHandle h = 0;
-        if (!plain) CK(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
+        if (!plain && !gated) CK(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
         cudaKernelNodeParams kf{};
         cudaGraphConditionalHandle hf = fuse ? h : 0;
         int ff = fuse;
@@ -3638,7 +3677,7 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
             CK(cudaGraphAddKernelNode(&n4, g, &n3, 1, &kr));
             nf = n4;
         }
-        if (fuse) {
+        if (fuse >= 1 && fuse <= 3) {
             nc = nf;
         } else {
             cudaKernelNodeParams kc{};
@@ -3648,6 +3687,10 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
             kc.blockDim = dim3(1024);
             kc.kernelParams = cargs;
             CK(cudaGraphAddKernelNode(&nc, g, &nf, 1, &kc));
+        }
+        if (gated) {   // the host rebuilds after a halt
+            prev = nc;
+            continue;
         }
         if (plain) {
             cudaKernelNodeParams kt{};

@@ -161,7 +161,10 @@ struct Dev {
     uint64_t *rng;          // per-bead generator state
     uint64_t *jump;         // [R][16][16] nibble tables of the GF(2) jump (4 N_r draws)
     RepDev *rep;
-    int *any_rebuild;
+    int *any_rebuild;       // [0]: some replica flagged at the last check; [1..3]: gate
+    // gate of the graphs that rebuild on the host (halted, steps done,
+    // budget): while gate[0] is set every step kernel returns at once
+    int *gate;
     int *status;            // device error word
     unsigned long long *ctr;  // [0]: list-rebuild passes launched
     int2 *chunks;           // (replica, first bead) of each tile-build block
@@ -373,6 +376,11 @@ private:
     }
     // graphs rebuild with a plain row-build node instead of an IF node
     bool plain_rebuild() const { return any_tile && !any_cell && !d.qa_on; }
+    // graphs without rebuild nodes: a flagged check halts the graph's
+    // remaining steps and the host rebuilds (static contexts with cell-path
+    // replicas or the quasi-adiabatic term, where the rebuild is a chain of
+    // kernels and rebuilds are rare)
+    bool gated_graphs() const { return !plain_rebuild() && !dynamic; }
     // the QA transitions' fixed grid (groups of 256 contact slots)
     int trans_grid() const {
         const int ng = (d.qa.ct_total + 255) / 256;

@@ -257,6 +257,7 @@ __device__ __forceinline__ void qa_sift_group(const Dev &d, const TermP &p, int 
 // large replica is sifted by the whole grid.  Groups without a live slot are
 // never read (k_qa_step reads the groups of each replica's live range).
 __global__ void __launch_bounds__(QA_SIFT, 4) k_qa_sift(Dev d, TermP p, int cur) {
+    if (d.gate[0]) return;   // a halted graph step
     const QaDev &q = d.qa;
     const int t = threadIdx.x;
     // the per-bead contact references are listed again at this step's end
@@ -300,6 +301,7 @@ __global__ void __launch_bounds__(QA_SIFT, 4) k_qa_sift(Dev d, TermP p, int cur)
 // stops at the first candidate without a slot.
 constexpr int QA_HASH = 4096;
 __global__ void __launch_bounds__(1024) k_qa_step(Dev d, TermP p, int cur) {
+    if (d.gate[0]) return;
     const int r = blockIdx.x, t = threadIdx.x;
     RepDev &rp = d.rep[r];
     const QaDev &q = d.qa;
@@ -465,6 +467,7 @@ __device__ __forceinline__ void qa_trans_slot(const Dev &d, const TermP &p, int 
 // flags of live slots only).
 constexpr int QA_TG = 256;
 __global__ void __launch_bounds__(QA_TG) k_qa_trans(Dev d, TermP p, int cur) {
+    if (d.gate[0]) return;
     const QaDev &q = d.qa;
     const int t = threadIdx.x;
     const int ng = (q.ct_total + QA_TG - 1) / QA_TG, G = gridDim.x;
@@ -491,6 +494,7 @@ __global__ void __launch_bounds__(QA_TG) k_qa_trans(Dev d, TermP p, int cur) {
 // order (process_contacts.cpp:48-55); replicas without a removal at this step
 // return at once.
 __global__ void __launch_bounds__(1024) k_qa_refree(Dev d) {
+    if (d.gate[0]) return;
     const int r = blockIdx.x, t = threadIdx.x;
     RepDev &rp = d.rep[r];
     if (!rp.active || rp.ct_cap == 0) return;
