@@ -326,7 +326,7 @@ int xmd_gpu_set_kernel_timing(xmd_gpu_ctx *ctx, int on);
 /* ---- launch shapes and the autotuner ------------------------------------------
  * No counterpart in the reference (its OpenMP loop has no launch shape).
  * shape[4] = {beads per step-kernel block (32, 64, 128), resident tile-build
- * blocks per SM (0 = as many as fit), steps per captured graph (8, 16, 32),
+ * blocks per SM (0 = as many as fit), steps per captured graph (8, 16, 32, 64),
  * threads per bead in the step kernel (1, 2, 4)}.
  * Results never depend on the shape.  xmd_gpu_autotune times every candidate
  * on a clone of the context (same replicas, same starting state; the

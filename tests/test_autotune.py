@@ -33,7 +33,7 @@ def run(prec, shape, nsteps=200, workload="c4"):
         return [e.get_state(r)[0] for r in range(len(systems))]
 
 
-SHAPES = [(32, 0, 8, 1), (64, 2, 32, 2), (128, 1, 16, 4), (128, 0, 16, 1), (32, 0, 16, 2)]
+SHAPES = [(32, 0, 8, 1), (64, 2, 32, 2), (128, 1, 16, 4), (128, 0, 16, 1), (32, 0, 64, 2)]
 
 
 @pytest.mark.parametrize("workload", ["c4", "c3"])
@@ -57,7 +57,7 @@ def test_autotune_keeps_state_and_picks_a_valid_shape():
         e.step(32)
         f.step(32)
         best = e.autotune(64)
-        assert best["fb"] in (32, 64, 128) and best["graph_steps"] in (8, 16, 32) and best["lpb"] in (1, 2, 4)
+        assert best["fb"] in (32, 64, 128) and best["graph_steps"] in (8, 16, 32, 64) and best["lpb"] in (1, 2, 4)
         assert best["ms_per_step"] > 0
         assert e.tuning() == {k: best[k] for k in ("fb", "tile_per_sm", "graph_steps", "lpb")}
         e.step(96)

@@ -1080,6 +1080,27 @@ __global__ void k_nl_check(Dev d, int advance, double dt, cudaGraphConditionalHa
     nl_check_block(d, advance, dt, h, setc);
 }
 
+// The quasi-adiabatic re-freeing (one block per replica).  With `check` (the
+// gated graph steps) the last block to finish also takes the step's skin
+// decision, which otherwise is a launch of its own.
+__global__ void __launch_bounds__(1024) k_qa_refree(Dev d, double dt, int check) {
+    if (d.gate[0]) return;
+    qa_refree_block(d);
+    if (!check) return;
+    __shared__ int last_s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last_s = atomicAdd(&d.ctr[2], 1ull) == (unsigned long long)(gridDim.x - 1);
+    }
+    __syncthreads();
+    if (last_s) {
+        __threadfence();
+        nl_check_block(d, 1, dt, (cudaGraphConditionalHandle)0, CHECK_GATE);
+        if (threadIdx.x == 0) d.ctr[2] = 0ull;
+    }
+}
+
 // The step kernel.  With `fuse` (graph steps without the quasi-adiabatic
 // term) the last block to finish also takes the skin decision of every
 // replica (fuse 1: and sets the graph's rebuild condition; fuse 2: the next
@@ -2177,12 +2198,12 @@ void Engine::step_async(int nsteps) {
     int s = 0;
     if (!timing && use_graphs) {
         const int gsteps = tune.graph_steps;
-        // per step: the step kernel (plus the separate check and the
-        // quasi-adiabatic kernels with that term, the external-force and PID
-        // kernels, and a plain row-build node); rebuild kernels of IF nodes
-        // are counted per pass in stats()
-        const int64_t per_step = (d.qa_on ? 6 : 1) + (tp.ext_on ? 1 : 0) + (tp.on[XMD_TERM_PID] ? 1 : 0) +
-                                 (plain_rebuild() ? 1 : 0);
+        // per step: the step kernel (plus the quasi-adiabatic kernels with
+        // that term and a separate check where the re-freeing does not take
+        // it, the external-force and PID kernels, and a plain row-build
+        // node); rebuild kernels of IF nodes are counted per pass in stats()
+        const int64_t per_step = (d.qa_on ? (gated_graphs() ? 5 : 6) : 1) + (tp.ext_on ? 1 : 0) +
+                                 (tp.on[XMD_TERM_PID] ? 1 : 0) + (plain_rebuild() ? 1 : 0);
         if (gated_graphs()) {
             // each graph runs until a check flags a replica (or its steps are
             // done); the host then rebuilds and goes on from the steps taken.
@@ -3469,8 +3490,8 @@ void Engine::set_tuning(const Tune &t) {
         throw std::invalid_argument("tuning: step-kernel block size must be 32, 64 or 128 beads");
     if (t.lpb != 1 && t.lpb != 2 && t.lpb != 4)
         throw std::invalid_argument("tuning: threads per bead must be 1, 2 or 4");
-    if (t.graph_steps != 8 && t.graph_steps != 16 && t.graph_steps != 32)
-        throw std::invalid_argument("tuning: steps per graph must be 8, 16 or 32");
+    if (t.graph_steps != 8 && t.graph_steps != 16 && t.graph_steps != 32 && t.graph_steps != 64)
+        throw std::invalid_argument("tuning: steps per graph must be 8, 16, 32 or 64");
     if (t.tile_per_sm < 0) throw std::invalid_argument("tuning: tile blocks per SM must be >= 0");
     tune = t;
     if (finalized) {
@@ -3534,7 +3555,7 @@ Engine::Tune Engine::autotune(int steps, double *ms_out) {
     for (int fb : {32, 64, 128})
         for (int lpb : {1, 2, 4}) trial(Tune{fb, 0, 16, lpb});
     const Tune kshape = best;
-    for (int gs : {8, 16, 32})
+    for (int gs : {8, 16, 32, 64})
         for (int tps : {0, 2})
             if (gs != 16 || tps != 0) trial(Tune{kshape.fb, tps, gs, kshape.lpb});
     use_device();
@@ -3584,7 +3605,7 @@ void Engine::launch_force_step() {
         k_qa_sift<<<sift_grid(), QA_SIFT, 0, stream>>>(d, tp, cur);
         k_qa_step<<<d.R, 1024, 0, stream>>>(d, tp, cur);
         k_qa_trans<<<trans_grid(), QA_TG, 0, stream>>>(d, tp, cur);
-        k_qa_refree<<<d.R, 1024, 0, stream>>>(d);
+        k_qa_refree<<<d.R, 1024, 0, stream>>>(d, 0.0, 0);
         launches += 4;
     }
 }
@@ -3661,7 +3682,8 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
             kq.blockDim = dim3(1024);
             kq.kernelParams = sargs;
             cudaKernelNodeParams kt{}, kr{};
-            void *dargs[] = {&d};
+            int rcheck = gated ? 1 : 0;   // the re-freeing's last block takes the skin decision
+            void *dargs[] = {&d, &dt, &rcheck};
             kt.func = (void *)k_qa_trans;
             kt.gridDim = dim3(trans_grid());
             kt.blockDim = dim3(QA_TG);
@@ -3677,7 +3699,7 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
             CK(cudaGraphAddKernelNode(&n4, g, &n3, 1, &kr));
             nf = n4;
         }
-        if (fuse >= 1 && fuse <= 3) {
+        if ((fuse >= 1 && fuse <= 3) || (d.qa_on && gated)) {
             nc = nf;
         } else {
             cudaKernelNodeParams kc{};

@@ -493,8 +493,8 @@ __global__ void __launch_bounds__(QA_TG) k_qa_trans(Dev d, TermP p, int cur) {
 // Removed pairs re-freed at the end of the free-pair list in contact-slot
 // order (process_contacts.cpp:48-55); replicas without a removal at this step
 // return at once.
-__global__ void __launch_bounds__(1024) k_qa_refree(Dev d) {
-    if (d.gate[0]) return;
+// (the body of k_qa_refree: one 1024-thread block per replica)
+__device__ __forceinline__ void qa_refree_block(const Dev &d) {
     const int r = blockIdx.x, t = threadIdx.x;
     RepDev &rp = d.rep[r];
     if (!rp.active || rp.ct_cap == 0) return;
