@@ -1220,14 +1220,20 @@ __global__ void __launch_bounds__(CB) k_cells(Dev d, int cur) {
     __shared__ double red_lo[3][32], red_hi[3][32];
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
 
-    // bounding box along open axes
+    // bounding box along open axes (none in a fully periodic box); four
+    // loads in flight per thread
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (int i = b + t; i < b + n; i += CB) {
-        double4_32a q = pos[i];
-        for (int a = 0; a < 3; ++a) {
-            lo[a] = fmin(lo[a], comp(q, a));
-            hi[a] = fmax(hi[a], comp(q, a));
-        }
+    const bool any_open = !(rp.per[0] && rp.per[1] && rp.per[2]);
+    for (int i0 = b + t; any_open && i0 < b + n; i0 += 4 * CB) {
+        double4_32a q[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) q[u] = pos[min(i0 + u * CB, b + n - 1)];   // repeats are harmless
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = fmin(lo[a], comp(q[u], a));
+                hi[a] = fmax(hi[a], comp(q[u], a));
+            }
     }
     for (int a = 0; a < 3; ++a) {
         for (int o = 16; o; o >>= 1) {
@@ -1408,7 +1414,7 @@ __global__ void __launch_bounds__(CF_WARPS * 32) k_cell_finish(Dev d, int cur) {
 // by j within the warp at the end, so the free-pair source list is ordered as
 // update_free_pairs (free_pair.cpp:9-19) walks it.
 constexpr int NC_WARPS = 8;
-__global__ void __launch_bounds__(NC_WARPS * 32, 3) k_nl_cells(Dev d, TermP p, int cur) {
+__global__ void __launch_bounds__(NC_WARPS * 32, 4) k_nl_cells(Dev d, TermP p, int cur) {
     const int lane = threadIdx.x & 31;
     const int i = blockIdx.x * NC_WARPS + (threadIdx.x >> 5);
     if (i >= d.N) return;   // warp-uniform exits
