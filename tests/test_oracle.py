@@ -111,3 +111,19 @@ def test_oracle_edge_single_bead_and_open_box():
     o.step(10)
     r, _, t = o.get_state()
     assert np.isfinite(r).all() and abs(t - 0.05) < 1e-12
+
+
+def test_serving_request_diverges_in_the_reference_kernels():
+    """Serving request 15 of the seeded set (3,712 beads in 10 chains, open
+    boundaries, seed 5015) goes non-finite in FP64 within 8,000 steps
+    under the reference's own operations, as it does on the device: the
+    server's failed requests are the reference's behaviour, not the engine's."""
+    from oracle.pyoracle import parse_params
+    from xmd_gb300 import synth
+    s = synth._c5_one((5 * 1000 + 15, 64))
+    o = Oracle(parse_params(synth.yaml_for("c5", "fp64")), s, "port")
+    for _ in range(16):
+        o.step_omp(500, 8)
+        if not np.isfinite(o.get_state()[0]).all():
+            break
+    assert not np.isfinite(o.get_state()[0]).all()

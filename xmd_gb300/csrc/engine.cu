@@ -1021,8 +1021,8 @@ __device__ __forceinline__ void force_block(const Dev &d, const TermP &p, int cu
 // setc 2: count the step in the gate and halt the graph when a replica is
 // flagged or the budget of steps is spent
 enum : int { CHECK_PLAIN = 0, CHECK_COND = 1, CHECK_GATE = 2 };
-__device__ __forceinline__ void nl_check_block(const Dev &d, int advance, double dt, cudaGraphConditionalHandle h,
-                                               int setc) {
+template <int SETC>
+__device__ __forceinline__ void nl_check_block(const Dev &d, int advance, double dt, cudaGraphConditionalHandle h) {
     __shared__ int any_s, nwork_s;
     if (threadIdx.x == 0) any_s = nwork_s = 0;
     __syncthreads();
@@ -1067,8 +1067,8 @@ __device__ __forceinline__ void nl_check_block(const Dev &d, int advance, double
     if (threadIdx.x == 0) {
         *d.any_rebuild = any_s;
         *d.nwork = nwork_s;
-        if (setc == CHECK_COND) cudaGraphSetConditional(h, any_s ? 1u : 0u);
-        if (setc == CHECK_GATE) {
+        if constexpr (SETC == CHECK_COND) cudaGraphSetConditional(h, any_s ? 1u : 0u);
+        if constexpr (SETC == CHECK_GATE) {
             const int done = d.gate[1] + 1;
             d.gate[1] = done;
             if (any_s || done >= d.gate[2]) d.gate[0] = 1;
@@ -1077,7 +1077,9 @@ __device__ __forceinline__ void nl_check_block(const Dev &d, int advance, double
 }
 __global__ void k_nl_check(Dev d, int advance, double dt, cudaGraphConditionalHandle h, int setc) {
     if (setc == CHECK_GATE && d.gate[0]) return;
-    nl_check_block(d, advance, dt, h, setc);
+    if (setc == CHECK_COND) nl_check_block<CHECK_COND>(d, advance, dt, h);
+    else if (setc == CHECK_GATE) nl_check_block<CHECK_GATE>(d, advance, dt, h);
+    else nl_check_block<CHECK_PLAIN>(d, advance, dt, h);
 }
 
 // The quasi-adiabatic re-freeing (one block per replica).  With `check` (the
@@ -1096,38 +1098,39 @@ __global__ void __launch_bounds__(1024) k_qa_refree(Dev d, double dt, int check)
     __syncthreads();
     if (last_s) {
         __threadfence();
-        nl_check_block(d, 1, dt, (cudaGraphConditionalHandle)0, CHECK_GATE);
+        nl_check_block<CHECK_GATE>(d, 1, dt, (cudaGraphConditionalHandle)0);
         if (threadIdx.x == 0) d.ctr[2] = 0ull;
     }
 }
 
-// The step kernel.  With `fuse` (graph steps without the quasi-adiabatic
-// term) the last block to finish also takes the skin decision of every
-// replica (fuse 1: and sets the graph's rebuild condition; fuse 2: the next
-// node, the row build, runs on the work list it leaves, empty or not;
-// fuse 3: it keeps the gate, and the kernel returns at once while the gate
-// is closed).  fuse 4: no fused decision; the kernel returns at once while
-// the gate is closed (the separate check keeps it).
+// The step kernel.  `fuse` (graph steps): FUSE_CHECK, the last block to
+// finish also takes the skin decision of every replica (the next node, the
+// row build, runs on the work list it leaves, empty or not); FUSE_CHECK_GATE,
+// the same, and the decision keeps the gate: the kernel returns at once
+// while the gate is closed; FUSE_GATE, no decision (a later kernel of the step
+// takes it), and the kernel returns at once while the gate is closed.  The
+// kernel holds no device-side graph call, so profilers see it in graphs.
 // resident blocks the register allocation leaves room for: 16 warps per SM
 // (at most 128 registers) with one or two threads per bead, 28 (at most 73)
 // with four
 template <int FB, int LPB> constexpr int force_min_blocks() {
     return LPB == 4 ? (896 / (FB * 4) > 0 ? 896 / (FB * 4) : 1) : 512 / (FB * LPB);
 }
+enum : int { FUSE_NONE = 0, FUSE_CHECK = 1, FUSE_CHECK_GATE = 2, FUSE_GATE = 3 };
 template <class FT, int MODE, int FB, int LPB>
 __global__ void __launch_bounds__(FB * LPB, (force_min_blocks<FB, LPB>())) k_force(Dev d, TermP p, int cur,
-                                                                                  cudaGraphConditionalHandle h,
                                                                                   int fuse) {
     __shared__ int last_s;
     static_assert(LPB == 1 || LPB == 2 || LPB == 4, "one, two or four threads per bead");
-    if (MODE == 1 && fuse >= 3 && d.gate[0]) return;   // uniform: the gate changes between launches
+    // uniform: the gate changes between launches
+    if (MODE == 1 && (fuse == FUSE_CHECK_GATE || fuse == FUSE_GATE) && d.gate[0]) return;
     constexpr int FBT = force_beads<FB, LPB>();
     // the block runs when an occupancy granule of its beads is on (uniform)
     const int i0 = blockIdx.x * FBT, i1 = min(i0 + FBT, d.N) - 1;
     bool on = false;
     for (int g = i0 / BLK_ON; g <= i1 / BLK_ON; ++g) on |= d.blk_on[g] != 0;
     if (on) force_block<FT, MODE, FB, LPB>(d, p, cur);
-    if (MODE == 1 && fuse >= 1 && fuse <= 3) {
+    if (MODE == 1 && (fuse == FUSE_CHECK || fuse == FUSE_CHECK_GATE)) {
         __syncthreads();
         if (threadIdx.x == 0) {
             __threadfence();
@@ -1136,7 +1139,8 @@ __global__ void __launch_bounds__(FB * LPB, (force_min_blocks<FB, LPB>())) k_for
         __syncthreads();
         if (last_s) {
             __threadfence();
-            nl_check_block(d, 1, p.dt, h, fuse == 1 ? CHECK_COND : fuse == 3 ? CHECK_GATE : CHECK_PLAIN);
+            if (fuse == FUSE_CHECK_GATE) nl_check_block<CHECK_GATE>(d, 1, p.dt, (cudaGraphConditionalHandle)0);
+            else nl_check_block<CHECK_PLAIN>(d, 1, p.dt, (cudaGraphConditionalHandle)0);
             if (threadIdx.x == 0) d.ctr[2] = 0ull;
         }
     }
@@ -1996,9 +2000,8 @@ void Engine::launch_force(int mode, int c) {
     }
     const int fb = mode == 0 ? EVAL_FB : tune.fb, lpb = mode == 0 ? EVAL_LPB : tune.lpb;
     const int nb = (d.N + force_block_beads(fb, lpb) - 1) / force_block_beads(fb, lpb);
-    cudaGraphConditionalHandle none = 0;
-    int fuse = 0;
-    void *args[] = {&d, &tp, &c, &none, &fuse};
+    int fuse = FUSE_NONE;
+    void *args[] = {&d, &tp, &c, &fuse};
     CK(cudaLaunchKernel(force_kernel(params.precision == XMD_PREC_MIXED, mode, fb, lpb), dim3(nb), dim3(fb * lpb),
                         args, 0, stream));
 }
@@ -3634,9 +3637,11 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
     void *fk = force_kernel(params.precision == XMD_PREC_MIXED, 1, tune.fb, tune.lpb);
     double dt = params.dt;
     // without the quasi-adiabatic term the step kernel takes the skin
-    // decision itself (its last block), so a step is one kernel node
+    // decision itself (its last block) where no IF node needs it; with it,
+    // the re-freeing kernel does in gated graphs
     const bool plain = plain_rebuild(), gated = gated_graphs();
-    const int fuse = d.qa_on ? (gated ? 4 : 0) : plain ? 2 : gated ? 3 : 1;
+    const int fuse = d.qa_on ? (gated ? FUSE_GATE : FUSE_NONE) : plain ? FUSE_CHECK
+                     : gated ? FUSE_CHECK_GATE : FUSE_NONE;
     int zero = 0;
     for (int s = 0; s < tune.graph_steps; ++s) {
         int c = start_cur ^ (s & 1), cn = c ^ 1;
@@ -3644,9 +3649,8 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
         cudaGraphConditionalHandle h = 0;
         if (!plain && !gated) CK(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
         cudaKernelNodeParams kf{};
-        cudaGraphConditionalHandle hf = fuse ? h : 0;
         int ff = fuse;
-        void *fargs[] = {&d, &tp, &c, &hf, &ff};
+        void *fargs[] = {&d, &tp, &c, &ff};
         kf.func = fk;
         kf.gridDim = dim3(nb);
         kf.blockDim = dim3(tune.fb * tune.lpb);
@@ -3705,7 +3709,7 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
             CK(cudaGraphAddKernelNode(&n4, g, &n3, 1, &kr));
             nf = n4;
         }
-        if ((fuse >= 1 && fuse <= 3) || (d.qa_on && gated)) {
+        if (fuse == FUSE_CHECK || fuse == FUSE_CHECK_GATE || (d.qa_on && gated)) {
             nc = nf;
         } else {
             cudaKernelNodeParams kc{};
