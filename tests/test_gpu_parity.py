@@ -159,6 +159,30 @@ def test_graph_and_stream_paths_agree():
     assert np.array_equal(ya, yb) and ta == tb and sa == sb
 
 
+@pytest.mark.parametrize("case,build", [("c2_periodic480", "cell"), ("c3_qa600", "tile"), ("c3_qa600", "cell")])
+def test_gated_graphs_agree_with_stream_path(case, build):
+    """Cell-path and quasi-adiabatic contexts run graphs without rebuild
+    nodes that halt at a flagged skin check (the host rebuilds), and graphs
+    with IF rebuild nodes while rebuilds come every few steps; both give the
+    per-step path's trajectory bit for bit (200 steps from the fixture's
+    start, where the lists are rebuilt often and then rarely)."""
+    s, y, _ = load_golden(case)
+    y = with_engine_key(y, f"nl build: {build}")
+    with Engine(y) as a, Engine(y) as b:
+        a.add_system(s)
+        b.add_system(s)
+        a.step(200)
+        abi.check(b.lib.xmd_gpu_set_kernel_timing(b.h, 1))   # timing forces the per-step path
+        b.step(200)
+        ya, ta, sa = a.get_history(0)
+        yb, tb, sb = b.get_history(0)
+        assert a.stats()["rebuilds"] == b.stats()["rebuilds"]
+        if "qa" in case:
+            ca, cb = a.qa_contacts(0), b.qa_contacts(0)
+            assert np.array_equal(ca[0], cb[0]) and np.array_equal(ca[1], cb[1])
+    assert np.array_equal(ya, yb) and ta == tb and sa == sb
+
+
 def test_packed_upload_download_roundtrip():
     systems = [synth.make_system([L], 500 + k, temperature=0.4) for k, L in enumerate([40, 75])]
     with Engine(synth.yaml_for("c2")) as e:

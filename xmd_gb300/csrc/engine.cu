@@ -2022,11 +2022,12 @@ Engine::Engine(const xmd_params &p) : params(p) {
 
 Engine::~Engine() {
     cudaSetDevice(device);
-    for (auto &row : graphs)
-        for (auto &g : row) {
-            if (g.exec) cudaGraphExecDestroy(g.exec);
-            if (g.graph) cudaGraphDestroy(g.graph);
-        }
+    for (auto &kind : graphs)
+        for (auto &row : kind)
+            for (auto &g : row) {
+                if (g.exec) cudaGraphExecDestroy(g.exec);
+                if (g.graph) cudaGraphDestroy(g.graph);
+            }
     for (auto e : ev_force) cudaEventDestroy(e);
     for (auto e : ev_rebuild) cudaEventDestroy(e);
     release();
@@ -2211,33 +2212,49 @@ void Engine::step_async(int nsteps) {
         // that term and a separate check where the re-freeing does not take
         // it, the external-force and PID kernels, and a plain row-build
         // node); rebuild kernels of IF nodes are counted per pass in stats()
-        const int64_t per_step = (d.qa_on ? (gated_graphs() ? 5 : 6) : 1) + (tp.ext_on ? 1 : 0) +
-                                 (tp.on[XMD_TERM_PID] ? 1 : 0) + (plain_rebuild() ? 1 : 0);
+        const int64_t extra = (tp.ext_on ? 1 : 0) + (tp.on[XMD_TERM_PID] ? 1 : 0);
+        const int64_t per_step = (d.qa_on ? (gated_graphs() ? 5 : 6) : 1) + extra + (plain_rebuild() ? 1 : 0);
+        const int64_t per_step_cond = (d.qa_on ? 6 : 2) + extra;   // IF-node graphs: a separate check
         if (gated_graphs()) {
             // each graph runs until a check flags a replica (or its steps are
             // done); the host then rebuilds and goes on from the steps taken.
-            // The gate is open outside these graphs (per-launch steps read it).
+            // While rebuilds come every few steps (a relaxing start) the
+            // halted steps would be launches for nothing: graphs with IF
+            // rebuild nodes run instead for a while.  The gate is open
+            // outside the gated graphs (per-launch steps read it).
             struct Open {
                 Engine *e;
                 ~Open() { cudaMemsetAsync(e->d.gate, 0, sizeof(int) * 3, e->stream); }
             } open_gate{this};
             while (nsteps - s >= gsteps) {
+                if (cond_graphs_left > 0) {
+                    CK(cudaGraphLaunch(graph_for(cur, false), stream));
+                    launches += per_step_cond * gsteps;
+                    md_steps += gsteps;
+                    s += gsteps;
+                    --cond_graphs_left;
+                    continue;
+                }
                 h_any[0] = 0; h_any[1] = 0; h_any[2] = 0; h_any[3] = gsteps;
                 CK(cudaMemcpyAsync(d.any_rebuild, h_any, sizeof(int) * 4, cudaMemcpyHostToDevice, stream));
-                CK(cudaGraphLaunch(graph_for(cur), stream));
+                CK(cudaGraphLaunch(graph_for(cur, true), stream));
                 CK(cudaMemcpyAsync(h_any, d.any_rebuild, sizeof(int) * 4, cudaMemcpyDeviceToHost, stream));
                 CK(cudaStreamSynchronize(stream));
                 const int done = h_any[2];
                 if (done < 1 || done > gsteps) throw std::logic_error("engine: graph step count out of range");
+                CK(cudaMemsetAsync(d.gate, 0, sizeof(int) * 3, stream));   // open for what follows
                 launches += per_step * gsteps;
                 md_steps += done;
                 s += done;
                 cur ^= done & 1;
-                if (h_any[0]) launch_rebuild();
+                if (h_any[0]) {
+                    launch_rebuild();
+                    if (done < gsteps / 4) cond_graphs_left = 8;
+                }
             }
         } else {
             for (; s + gsteps <= nsteps; s += gsteps) {
-                CK(cudaGraphLaunch(graph_for(cur), stream));
+                CK(cudaGraphLaunch(graph_for(cur, false), stream));
                 launches += per_step * gsteps;
                 md_steps += gsteps;
             }
@@ -3574,13 +3591,14 @@ Engine::Tune Engine::autotune(int steps, double *ms_out) {
 }
 
 void Engine::drop_graphs() {
-    for (auto &row : graphs)
-        for (auto &g : row) {
-            if (g.exec) cudaGraphExecDestroy(g.exec);
-            if (g.graph) cudaGraphDestroy(g.graph);
-            g.exec = nullptr;
-            g.graph = nullptr;
-        }
+    for (auto &kind : graphs)
+        for (auto &row : kind)
+            for (auto &g : row) {
+                if (g.exec) cudaGraphExecDestroy(g.exec);
+                if (g.graph) cudaGraphDestroy(g.graph);
+                g.exec = nullptr;
+                g.graph = nullptr;
+            }
 }
 
 void Engine::ensure_nl() {
@@ -3627,8 +3645,8 @@ void Engine::launch_force_step() {
 // returns at once when the work list is empty, and an IF node costs more per
 // step than that empty launch.  An even step count leaves the position double
 // buffer where it started.
-cudaGraphExec_t Engine::graph_for(int start_cur) {
-    GraphSet &gs = graphs[params.precision == XMD_PREC_MIXED][start_cur];
+cudaGraphExec_t Engine::graph_for(int start_cur, bool gated) {
+    GraphSet &gs = graphs[params.precision == XMD_PREC_MIXED][gated ? 1 : 0][start_cur];
     if (gs.exec) return gs.exec;
     cudaGraph_t g;
     CK(cudaGraphCreate(&g, 0));
@@ -3639,7 +3657,7 @@ cudaGraphExec_t Engine::graph_for(int start_cur) {
     // without the quasi-adiabatic term the step kernel takes the skin
     // decision itself (its last block) where no IF node needs it; with it,
     // the re-freeing kernel does in gated graphs
-    const bool plain = plain_rebuild(), gated = gated_graphs();
+    const bool plain = plain_rebuild();
     const int fuse = d.qa_on ? (gated ? FUSE_GATE : FUSE_NONE) : plain ? FUSE_CHECK
                      : gated ? FUSE_CHECK_GATE : FUSE_NONE;
     int zero = 0;
