@@ -41,7 +41,7 @@ L2_FLUSH_BYTES = 256 << 20
 # ncu DRAM read + write of one k_force<float,1> launch on this workload (the
 # capture and its command are in profiles/k_force_mixed_c4.md); a committed
 # figure, not measured by this run
-FORCE_TRAFFIC_NCU = 25729024
+FORCE_TRAFFIC_NCU = 25555712
 
 
 # ---------------------------------------------------------------- helpers --
