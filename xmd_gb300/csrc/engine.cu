@@ -2022,12 +2022,10 @@ Engine::Engine(const xmd_params &p) : params(p) {
 
 Engine::~Engine() {
     cudaSetDevice(device);
-    for (auto &kind : graphs)
-        for (auto &row : kind)
-            for (auto &g : row) {
-                if (g.exec) cudaGraphExecDestroy(g.exec);
-                if (g.graph) cudaGraphDestroy(g.graph);
-            }
+    for (auto &kv : graphs) {
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+        if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
+    }
     for (auto e : ev_force) cudaEventDestroy(e);
     for (auto e : ev_rebuild) cudaEventDestroy(e);
     release();
@@ -2208,13 +2206,23 @@ void Engine::step_async(int nsteps) {
     int s = 0;
     if (!timing && use_graphs) {
         const int gsteps = tune.graph_steps;
-        // per step: the step kernel (plus the quasi-adiabatic kernels with
-        // that term and a separate check where the re-freeing does not take
-        // it, the external-force and PID kernels, and a plain row-build
-        // node); rebuild kernels of IF nodes are counted per pass in stats()
+        // launches per step of each graph form: the step kernel, plus the
+        // quasi-adiabatic kernels with that term, the external-force and PID
+        // kernels, and the plain form's row-build node or the IF form's
+        // separate check (gated QA graphs take the decision in the
+        // re-freeing kernel); rebuild kernels of IF nodes and of the host's
+        // rebuilds are counted per pass in stats()
         const int64_t extra = (tp.ext_on ? 1 : 0) + (tp.on[XMD_TERM_PID] ? 1 : 0);
-        const int64_t per_step = (d.qa_on ? (gated_graphs() ? 5 : 6) : 1) + extra + (plain_rebuild() ? 1 : 0);
-        const int64_t per_step_cond = (d.qa_on ? 6 : 2) + extra;   // IF-node graphs: a separate check
+        const int64_t per_plain = 2 + extra, per_gated = (d.qa_on ? 5 : 1) + extra,
+                      per_cond = (d.qa_on ? 6 : 2) + extra;
+        // graphs of graph_steps steps, and the rest in graphs of the largest
+        // powers of two that fit
+        auto chunk = [&](int left) {
+            if (left >= gsteps) return gsteps;
+            int l = 1;
+            while (2 * l <= left) l *= 2;
+            return l;
+        };
         if (gated_graphs()) {
             // each graph runs until a check flags a replica (or its steps are
             // done); the host then rebuilds and goes on from the steps taken.
@@ -2226,37 +2234,43 @@ void Engine::step_async(int nsteps) {
                 Engine *e;
                 ~Open() { cudaMemsetAsync(e->d.gate, 0, sizeof(int) * 3, e->stream); }
             } open_gate{this};
-            while (nsteps - s >= gsteps) {
+            while (s < nsteps) {
+                const int len = chunk(nsteps - s);
                 if (cond_graphs_left > 0) {
-                    CK(cudaGraphLaunch(graph_for(cur, false), stream));
-                    launches += per_step_cond * gsteps;
-                    md_steps += gsteps;
-                    s += gsteps;
+                    CK(cudaGraphLaunch(graph_for(cur, false, len), stream));
+                    launches += per_cond * len;
+                    md_steps += len;
+                    s += len;
+                    cur ^= len & 1;
                     --cond_graphs_left;
                     continue;
                 }
-                h_any[0] = 0; h_any[1] = 0; h_any[2] = 0; h_any[3] = gsteps;
+                h_any[0] = 0; h_any[1] = 0; h_any[2] = 0; h_any[3] = len;
                 CK(cudaMemcpyAsync(d.any_rebuild, h_any, sizeof(int) * 4, cudaMemcpyHostToDevice, stream));
-                CK(cudaGraphLaunch(graph_for(cur, true), stream));
+                CK(cudaGraphLaunch(graph_for(cur, true, len), stream));
                 CK(cudaMemcpyAsync(h_any, d.any_rebuild, sizeof(int) * 4, cudaMemcpyDeviceToHost, stream));
                 CK(cudaStreamSynchronize(stream));
                 const int done = h_any[2];
-                if (done < 1 || done > gsteps) throw std::logic_error("engine: graph step count out of range");
+                if (done < 1 || done > len) throw std::logic_error("engine: graph step count out of range");
                 CK(cudaMemsetAsync(d.gate, 0, sizeof(int) * 3, stream));   // open for what follows
-                launches += per_step * gsteps;
+                launches += per_gated * len;
                 md_steps += done;
                 s += done;
                 cur ^= done & 1;
                 if (h_any[0]) {
                     launch_rebuild();
-                    if (done < gsteps / 4) cond_graphs_left = 8;
+                    if (done < len / 4) cond_graphs_left = 8;
                 }
             }
         } else {
-            for (; s + gsteps <= nsteps; s += gsteps) {
-                CK(cudaGraphLaunch(graph_for(cur, false), stream));
-                launches += per_step * gsteps;
-                md_steps += gsteps;
+            const int64_t per = plain_rebuild() ? per_plain : per_cond;
+            while (s < nsteps) {
+                const int len = chunk(nsteps - s);
+                CK(cudaGraphLaunch(graph_for(cur, false, len), stream));
+                launches += per * len;
+                md_steps += len;
+                s += len;
+                cur ^= len & 1;
             }
         }
     }
@@ -3591,14 +3605,11 @@ Engine::Tune Engine::autotune(int steps, double *ms_out) {
 }
 
 void Engine::drop_graphs() {
-    for (auto &kind : graphs)
-        for (auto &row : kind)
-            for (auto &g : row) {
-                if (g.exec) cudaGraphExecDestroy(g.exec);
-                if (g.graph) cudaGraphDestroy(g.graph);
-                g.exec = nullptr;
-                g.graph = nullptr;
-            }
+    for (auto &kv : graphs) {
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+        if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
+    }
+    graphs.clear();
 }
 
 void Engine::ensure_nl() {
@@ -3637,16 +3648,20 @@ void Engine::launch_force_step() {
     }
 }
 
-// One graph runs tune.graph_steps steps: per step a force+integrate node, a skin
-// check that sets a conditional handle on the device, and an IF node whose
-// body rebuilds the lists of the flagged replicas (cells, then rows).  Where
-// the rebuild is the row build alone (no cell-path replica, no
-// quasi-adiabatic term) it is a plain node after the step kernel instead: it
-// returns at once when the work list is empty, and an IF node costs more per
-// step than that empty launch.  An even step count leaves the position double
-// buffer where it started.
-cudaGraphExec_t Engine::graph_for(int start_cur, bool gated) {
-    GraphSet &gs = graphs[params.precision == XMD_PREC_MIXED][gated ? 1 : 0][start_cur];
+// One graph runs `len` steps (tune.graph_steps, or a power of two for the
+// rest of a call).  IF form: per step a force+integrate node, a skin check
+// that sets a conditional handle on the device, and an IF node whose body
+// rebuilds the lists of the flagged replicas (cells, then rows).  Plain form
+// (the rebuild is the row build alone: no cell-path replica, no
+// quasi-adiabatic term): the step kernel takes the decision and a row-build
+// node follows, which returns at once when the work list is empty (an IF
+// node costs more per step than that empty launch).  Gated form (`gated`):
+// no rebuild node; the check halts the graph's remaining steps and the host
+// rebuilds.  A graph of odd length leaves the position double buffer
+// swapped.
+cudaGraphExec_t Engine::graph_for(int start_cur, bool gated, int len) {
+    const int key = ((len * 2 + (params.precision == XMD_PREC_MIXED ? 1 : 0)) * 2 + (gated ? 1 : 0)) * 2 + start_cur;
+    GraphSet &gs = graphs[key];
     if (gs.exec) return gs.exec;
     cudaGraph_t g;
     CK(cudaGraphCreate(&g, 0));
@@ -3661,7 +3676,7 @@ cudaGraphExec_t Engine::graph_for(int start_cur, bool gated) {
     const int fuse = d.qa_on ? (gated ? FUSE_GATE : FUSE_NONE) : plain ? FUSE_CHECK
                      : gated ? FUSE_CHECK_GATE : FUSE_NONE;
     int zero = 0;
-    for (int s = 0; s < tune.graph_steps; ++s) {
+    for (int s = 0; s < len; ++s) {
         int c = start_cur ^ (s & 1), cn = c ^ 1;
         int adv = 1, setc = gated ? CHECK_GATE : CHECK_COND;
         cudaGraphConditionalHandle h = 0;

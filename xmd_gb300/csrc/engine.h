@@ -392,17 +392,17 @@ private:
     void record(std::vector<cudaEvent_t> &pool, size_t &n);
     void launch_force_step();
 
-    // graph-captured step chunks, per precision, kind (gated or with IF
-    // rebuild nodes) and starting buffer
+    // graph-captured step chunks, per (precision, kind: gated or with IF
+    // rebuild nodes, starting buffer, steps)
     struct GraphSet {
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
     };
-    GraphSet graphs[2][2][2];
+    std::map<int, GraphSet> graphs;
     bool use_graphs = true;
     bool auto_grow = true;       // grow Verlet rows instead of failing
     int cond_graphs_left = 0;    // gated contexts: IF-node graphs to run before the next gated one
-    cudaGraphExec_t graph_for(int start_cur, bool gated);
+    cudaGraphExec_t graph_for(int start_cur, bool gated, int len);
     bool any_cell = false, any_tile = false;   // which Verlet builds the replicas use
     size_t tile_smem = 0;                      // dynamic shared memory of k_nl_tile
     int tile_grid = 1;                         // resident blocks of k_nl_tile over all SMs
