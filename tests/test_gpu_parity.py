@@ -146,14 +146,17 @@ def test_batched_replicas_equal_alone():
 
 def test_graph_and_stream_paths_agree():
     """Graph-captured chunks (device-side rebuild decisions) and the plain
-    per-step path give identical trajectories."""
+    per-step path give identical trajectories; a step count that is not a
+    multiple of the graph length runs its rest in graphs of 4, 2 and 1 steps
+    (the last one leaves the position buffers swapped)."""
     s, y, _ = load_golden("c2_periodic480")
     with Engine(y) as a, Engine(y) as b:
         a.add_system(s)
         b.add_system(s)
-        a.step(64)                       # 4 graph chunks
+        a.set_tuning(64, 0, 16, 1)
+        a.step(71)                       # graphs of 16, 16, 16, 16, 4, 2, 1 steps
         abi.check(b.lib.xmd_gpu_set_kernel_timing(b.h, 1))   # timing forces the per-step path
-        b.step(64)
+        b.step(71)
         ya, ta, sa = a.get_history(0)
         yb, tb, sb = b.get_history(0)
     assert np.array_equal(ya, yb) and ta == tb and sa == sb

@@ -1739,18 +1739,17 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
     ext = 0.0f;
     for (int q = 0; q < TL_WARPS; ++q) ext = fmaxf(ext, ext_s[q]);
     // decision bands of the chunk, formed once (FP64 work off the scan)
+    // (one thread per band: the reciprocals are FP64 divisions)
     __shared__ Band bands_s[5];
     __shared__ float mf_s;
-    if (t == 0) {
+    if (t < 5) {
         double exd = fmax((double)ext, rp.req_r);
         for (int a = 0; a < 3; ++a) exd = fmax(exd, bx.cell[a]);
         const double m = band_margin(exd);
-        bands_s[0] = make_band(rp.req_r, m);
-        bands_s[1] = make_band(1.0 / rp.pauli_min_inv, m);
-        bands_s[2] = make_band(1.0 / rp.es_min_inv, m);
-        bands_s[3] = make_band(1.0 / rp.qa_min_inv, m);
-        bands_s[4] = make_band(1.0 / rp.pid_min_inv, m);
-        mf_s = __double2float_ru(m);
+        const double inv = t == 1 ? rp.pauli_min_inv : t == 2 ? rp.es_min_inv : t == 3 ? rp.qa_min_inv
+                                                                                       : rp.pid_min_inv;
+        bands_s[t] = make_band(t == 0 ? rp.req_r : 1.0 / inv, m);
+        if (t == 0) mf_s = __double2float_ru(m);
     }
     // bounding box of each group of 32 beads j (one warp per group)
     for (int g = w; g < ng; g += TL_WARPS) {
