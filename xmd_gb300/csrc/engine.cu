@@ -1714,41 +1714,23 @@ __device__ __forceinline__ void tl_chunk(const Dev &d, const TermP &p, int cur, 
 
     float ext = 0.0f;
     // two loops on a block-uniform flag, so the open-box loop carries no
-    // FP64 work (a select between the two forms would execute both); each
-    // thread issues the loads of up to four beads before using them
-    constexpr int TL_U = 4;
-    const bool open_box = (rp.per[0] | rp.per[1] | rp.per[2]) == 0;
-    for (int k0 = t; k0 < n; k0 += TL_U * TL_THREADS) {
-        double4_32a q[TL_U];
-        int2 cs[TL_U];
-#pragma unroll
-        for (int u = 0; u < TL_U; ++u) {
-            const int k = min(k0 + u * TL_THREADS, n - 1);   // repeats of bead n - 1 are harmless
-            q[u] = pos[b + k];
-            cs[u] = make_int2(d.chain[b + k], d.seq[b + k]);
+    // FP64 work (a select between the two forms would execute both)
+    if ((rp.per[0] | rp.per[1] | rp.per[2]) == 0) {
+        for (int k = t; k < n; k += TL_THREADS) {
+            const double4_32a q = pos[b + k];
+            const float x = ff_diff(p0.x, split_d(q.x)).h, y = ff_diff(p0.y, split_d(q.y)).h,
+                        z = ff_diff(p0.z, split_d(q.z)).h;
+            sq[k] = make_float4(x, y, z, narrow_f(q.w));
+            scs[k] = make_int2(d.chain[b + k], d.seq[b + k]);
+            ext = fmaxf(ext, fmaxf(fabsf(x), fmaxf(fabsf(y), fabsf(z))));
         }
-        if (open_box) {
-#pragma unroll
-            for (int u = 0; u < TL_U; ++u) {
-                const int k = k0 + u * TL_THREADS;
-                if (k >= n) break;
-                const float x = ff_diff(p0.x, split_d(q[u].x)).h, y = ff_diff(p0.y, split_d(q[u].y)).h,
-                            z = ff_diff(p0.z, split_d(q[u].z)).h;
-                sq[k] = make_float4(x, y, z, narrow_f(q[u].w));
-                scs[k] = cs[u];
-                ext = fmaxf(ext, fmaxf(fabsf(x), fmaxf(fabsf(y), fabsf(z))));
-            }
-        } else {
-#pragma unroll
-            for (int u = 0; u < TL_U; ++u) {
-                const int k = k0 + u * TL_THREADS;
-                if (k >= n) break;
-                const float x = tl_rel(rp, 0, q[u].x, p0.x), y = tl_rel(rp, 1, q[u].y, p0.y),
-                            z = tl_rel(rp, 2, q[u].z, p0.z);
-                sq[k] = make_float4(x, y, z, narrow_f(q[u].w));
-                scs[k] = cs[u];
-                ext = fmaxf(ext, fmaxf(fabsf(x), fmaxf(fabsf(y), fabsf(z))));
-            }
+    } else {
+        for (int k = t; k < n; k += TL_THREADS) {
+            const double4_32a q = pos[b + k];
+            const float x = tl_rel(rp, 0, q.x, p0.x), y = tl_rel(rp, 1, q.y, p0.y), z = tl_rel(rp, 2, q.z, p0.z);
+            sq[k] = make_float4(x, y, z, narrow_f(q.w));
+            scs[k] = make_int2(d.chain[b + k], d.seq[b + k]);
+            ext = fmaxf(ext, fmaxf(fabsf(x), fmaxf(fabsf(y), fabsf(z))));
         }
     }
     for (int o = 16; o; o >>= 1) ext = fmaxf(ext, __shfl_xor_sync(0xffffffffu, ext, o));
