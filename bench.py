@@ -524,7 +524,11 @@ def accuracy_c3(nrep, steps, every, device):
             "drift_within_1pct_95": bool(rel_hi <= 0.01),
             "drift_definition": "energy change over the whole run (least-squares slope x duration), "
                                 "per replica, paired mixed - FP64; 95 = mean + 2 SE",
-            "wall_s": wall, "reference": "plain FP64 engine (pinned to the oracle by the parity tests)"}
+            "wall_s": wall,
+            "bead_steps_per_s": {prec: nrep * s.n * steps / wall[prec] for prec in wall},
+            "bead_steps_note": "replicas x beads x steps / host wall time of the run, observables sampled "
+                               "every sample_every steps; a frozen replica stops stepping when it freezes",
+            "reference": "plain FP64 engine (pinned to the oracle by the parity tests)"}
 
 
 # ------------------------------------------------------------- CPU arms --
